@@ -1,0 +1,263 @@
+"""CPU oracle for the PIC-step hot path -- TEST INFRASTRUCTURE ONLY.
+
+This package is the checker.  Only ``tests/``, ``__graft_entry__.smoke()`` and
+``bench.py``'s CPU-baseline leg import it; the product package
+``smilei_gb300`` never does, and fails loudly when its CUDA library is missing
+instead of falling back here.
+
+Two back ends with the same Python signatures:
+
+* ``Oracle`` wraps ``oracle/pic_oracle.c`` (``liboracle.so``), a plain-C FP64
+  restatement of the reference operators (each C function cites the reference
+  file:line it follows);
+* ``RefOps`` wraps ``oracle/_ref/libsmilei_ref_ops.so``, the reference's own
+  operator sources compiled by ``oracle/build_ref.sh`` (only where the
+  reference tree is present; used to make and check the golden fixtures).
+
+Array conventions (the reference's): fields are C-contiguous float64 arrays in
+x-major order with ghost cells; particles are SoA ``pos[ndim, n]``,
+``mom[3, n]``; interpolator scratch ``E[3, n]``, ``B[3, n]``,
+``iold[ndim, n]`` (int32) and ``delta[ndim, n]``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libsmilei_ref_ops.so")
+
+# Yee staggering (dual flag per dimension) of each named component.
+STAGGER = {
+    "Ex": (1, 0, 0), "Ey": (0, 1, 0), "Ez": (0, 0, 1),
+    "Bx": (0, 1, 1), "By": (1, 0, 1), "Bz": (1, 1, 0),
+    "Jx": (1, 0, 0), "Jy": (0, 1, 0), "Jz": (0, 0, 1),
+    "rho": (0, 0, 0),
+}
+PUSHERS = {"boris": 0, "vay": 1, "higueracary": 2}
+
+
+def field_shape(ndim: int, n_prim, comp: str):
+    """Extents of component ``comp`` on a grid whose primal extents (with ghosts) are ``n_prim``."""
+    st = STAGGER[comp.replace("_m", "")]
+    return tuple(int(n_prim[d]) + st[d] for d in range(ndim))
+
+
+def build(force: bool = False) -> str:
+    """Compile ``pic_oracle.c`` into ``liboracle.so`` (gcc, OpenMP, no FP contraction)."""
+    src = os.path.join(HERE, "pic_oracle.c")
+    srcs = [src, os.path.join(HERE, "rad_oracle.c")]
+    srcs = [s for s in srcs if os.path.exists(s)]
+    if (not force and os.path.exists(LIB_PATH)
+            and all(os.path.getmtime(LIB_PATH) >= os.path.getmtime(s) for s in srcs)):
+        return LIB_PATH
+    tmp = LIB_PATH + ".tmp%d" % os.getpid()
+    cmd = ["gcc", "-O3", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-std=c11",
+           "-o", tmp] + srcs + ["-lm"]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+def build_ref() -> str | None:
+    """Compile the reference's operator sources (only where the reference tree exists)."""
+    script = os.path.join(HERE, "build_ref.sh")
+    if not os.path.isdir("/root/reference/src"):
+        return None
+    subprocess.run(["bash", script], check=True, stdout=subprocess.DEVNULL)
+    return REF_PATH if os.path.exists(REF_PATH) else None
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def _ptrs(arrs):
+    return (ctypes.c_void_p * len(arrs))(*[_ptr(a) for a in arrs])
+
+
+def _i32(v):
+    return (ctypes.c_int * len(v))(*[int(x) for x in v])
+
+
+def _d(v):
+    return (ctypes.c_double * len(v))(*[float(x) for x in v])
+
+
+class _Backend:
+    """Shared numpy marshalling for the oracle and the compiled reference."""
+
+    lib: ctypes.CDLL
+    prefix: str
+
+    def _fn(self, name):
+        return getattr(self.lib, self.prefix + name)
+
+    # -- Interpolator -------------------------------------------------------
+    def interpolate(self, ndim, n_prim, domain_begin, cell_length, fields, pos):
+        """fields = [Ex, Ey, Ez, Bx_m, By_m, Bz_m]; returns (E[3,n], B[3,n], iold[ndim,n], delta[ndim,n])."""
+        pos = _f64(pos)
+        n = pos.shape[1]
+        fields = [_f64(f) for f in fields]
+        E = np.zeros((3, n)); B = np.zeros((3, n))
+        iold = np.zeros((ndim, n), dtype=np.int32); delta = np.zeros((ndim, n))
+        self._interpolate(ndim, n_prim, domain_begin, cell_length, fields, n, pos, E, B, iold, delta)
+        return E, B, iold, delta
+
+    # -- Pusher -------------------------------------------------------------
+    def push(self, kind, ndim, dt, mass, pos, mom, charge, E, B):
+        """Returns (pos, mom, invgf) after one push; inputs are not modified."""
+        pos = _f64(pos).copy(); mom = _f64(mom).copy()
+        charge = np.ascontiguousarray(charge, dtype=np.int16)
+        n = mom.shape[1]
+        invgf = np.zeros(n)
+        k = PUSHERS[kind] if isinstance(kind, str) else int(kind)
+        self._fn("push")(k, ndim, ctypes.c_double(dt), ctypes.c_double(mass), self._n(n), _ptr(pos), _ptr(mom),
+                         _ptr(charge), _ptr(_f64(E)), _ptr(_f64(B)), _ptr(invgf))
+        return pos, mom, invgf
+
+
+class Oracle(_Backend):
+    """The C restatement in ``pic_oracle.c``."""
+
+    prefix = "or_"
+
+    def __init__(self):
+        build()
+        self.lib = ctypes.CDLL(LIB_PATH)
+
+    @staticmethod
+    def _n(n):
+        return ctypes.c_int64(n)
+
+    def _interpolate(self, ndim, n_prim, domain_begin, cell_length, fields, n, pos, E, B, iold, delta):
+        dx_inv = [1.0 / c for c in cell_length]
+        self.lib.or_interpolate(ndim, _i32(n_prim), _i32(domain_begin), _d(dx_inv), _ptrs(fields),
+                                ctypes.c_int64(n), _ptr(pos), _ptr(E), _ptr(B), _ptr(iold), _ptr(delta))
+
+    def project(self, mode, ndim, n_prim, domain_begin, cell_length, dt, pos, mom, weight, charge, invgf,
+                iold, delta, J):
+        """J = [Jx, Jy, Jz, rho] accumulated in place (arrays may be None when unused)."""
+        pos = _f64(pos); n = pos.shape[1]
+        J = [_f64(a) if a is not None else None for a in J]
+        self.lib.or_project(mode, ndim, _i32(n_prim), _i32(domain_begin), _d(cell_length), ctypes.c_double(dt),
+                            ctypes.c_int64(n), _ptr(pos), _ptr(_f64(mom)), _ptr(_f64(weight)),
+                            _ptr(np.ascontiguousarray(charge, dtype=np.int16)),
+                            _ptr(_f64(invgf) if invgf is not None else None),
+                            _ptr(np.ascontiguousarray(iold, dtype=np.int32) if iold is not None else None),
+                            _ptr(_f64(delta) if delta is not None else None), _ptrs(J))
+        return J
+
+    def maxwell(self, which, ndim, n_prim, cell_length, dt, F, periodic=False, n_cells=None):
+        """which 0: Ampere, 1: Faraday.  F = [Ex,Ey,Ez,Bx,By,Bz,Jx,Jy,Jz] updated in place."""
+        if which == 0:
+            self.lib.or_maxwell_ampere(ndim, _i32(n_prim), _d(cell_length), ctypes.c_double(dt), _ptrs(F))
+        else:
+            self.lib.or_maxwell_faraday(ndim, _i32(n_prim), _d(cell_length), ctypes.c_double(dt), _ptrs(F),
+                                        int(periodic), _i32(n_cells if n_cells is not None else [0, 0, 0]))
+        return F
+
+    def fold_periodic(self, ndim, arr, dual, n_cells, oversize=2):
+        self.lib.or_fold_periodic(ndim, _i32(arr.shape), _i32(dual), _i32(n_cells), oversize, _ptr(arr))
+        return arr
+
+    def pic_step(self, ndim, n_cells, oversize, cell_length, dt, fields, species):
+        """fields: dict Ex..Bz, Bx_m..Bz_m, Jx..Jz (float64, updated in place).
+        species: list of dicts pos, mom, weight, charge, mass, pusher (pos/mom updated in place)."""
+        order = ["Ex", "Ey", "Ez", "Bx", "By", "Bz", "Bx_m", "By_m", "Bz_m", "Jx", "Jy", "Jz"]
+        farr = [fields[k] for k in order]
+        for a in farr:
+            assert a.dtype == np.float64 and a.flags.c_contiguous
+        ns = len(species)
+        npart = (ctypes.c_int64 * ns)(*[s["mom"].shape[1] for s in species])
+        mass = _d([s["mass"] for s in species])
+        pusher = _i32([PUSHERS[s["pusher"]] for s in species])
+        for s in species:
+            assert s["pos"].dtype == np.float64 and s["pos"].flags.c_contiguous
+            assert s["mom"].dtype == np.float64 and s["mom"].flags.c_contiguous
+        self.lib.or_pic_step(ndim, _i32(n_cells), oversize, _d(cell_length), ctypes.c_double(dt), _ptrs(farr),
+                             ns, npart, mass, pusher, _ptrs([s["pos"] for s in species]),
+                             _ptrs([s["mom"] for s in species]),
+                             _ptrs([_f64(s["weight"]) for s in species]),
+                             _ptrs([np.ascontiguousarray(s["charge"], dtype=np.int16) for s in species]))
+
+    def sort(self, ndim, patch_size, xmin, cell_length, pos):
+        """Per-cell sort: returns (keys, first_index, last_index, perm)."""
+        pos = _f64(pos); n = pos.shape[1]
+        keys = np.zeros(n, dtype=np.int32)
+        self.lib.or_sort_keys(ndim, _i32(patch_size), _d(xmin), _d([1.0 / c for c in cell_length]),
+                              ctypes.c_int64(n), _ptr(pos), _ptr(keys))
+        ncell = int(np.prod([p + 1 for p in patch_size]))
+        first = np.zeros(ncell, dtype=np.int32); last = np.zeros(ncell, dtype=np.int32)
+        perm = np.zeros(n, dtype=np.int64)
+        self.lib.or_sort_bins(ctypes.c_int64(n), _ptr(keys), ncell, _ptr(first), _ptr(last), _ptr(perm))
+        return keys, first, last, perm
+
+
+class RefOps(_Backend):
+    """The reference's own operators, compiled by ``build_ref.sh``."""
+
+    prefix = "ref_"
+
+    def __init__(self, path: str = REF_PATH):
+        self.lib = ctypes.CDLL(path, mode=os.RTLD_LAZY)
+
+    @staticmethod
+    def _n(n):
+        return ctypes.c_int(n)
+
+    @staticmethod
+    def _patch(ndim, n_prim, oversize=2):
+        return _i32([n_prim[d] - 1 - 2 * oversize for d in range(ndim)]), _i32([oversize] * ndim)
+
+    def _interpolate(self, ndim, n_prim, domain_begin, cell_length, fields, n, pos, E, B, iold, delta):
+        cells, os_ = self._patch(ndim, n_prim)
+        self.lib.ref_interpolate(ndim, cells, os_, _i32(domain_begin), _d(cell_length), _ptrs(fields), n,
+                                 _ptr(pos), _ptr(E), _ptr(B), _ptr(iold), _ptr(delta))
+
+    def project(self, mode, ndim, n_prim, domain_begin, cell_length, dt, pos, mom, weight, charge, invgf,
+                iold, delta, J):
+        pos = _f64(pos); n = pos.shape[1]
+        cells, os_ = self._patch(ndim, n_prim)
+        J = [_f64(a) for a in J]
+        self.lib.ref_project(mode, ndim, cells, os_, _i32(domain_begin), _d(cell_length), ctypes.c_double(dt), n,
+                             _ptr(pos), _ptr(_f64(mom)), _ptr(_f64(weight)),
+                             _ptr(np.ascontiguousarray(charge, dtype=np.int16)),
+                             _ptr(_f64(invgf) if invgf is not None else None),
+                             _ptr(np.ascontiguousarray(iold, dtype=np.int32) if iold is not None else None),
+                             _ptr(_f64(delta) if delta is not None else None), _ptrs(J))
+        return J
+
+    def maxwell(self, which, ndim, n_prim, cell_length, dt, F):
+        cells, os_ = self._patch(ndim, n_prim)
+        self.lib.ref_maxwell(which, ndim, cells, os_, _d(cell_length), ctypes.c_double(dt), _ptrs(F))
+        return F
+
+    # -- radiation tables --------------------------------------------------
+    def rad_tables(self):
+        isz = ctypes.c_int(); imin = ctypes.c_double(); imax = ctypes.c_double()
+        xd = (ctypes.c_int * 2)(); xmin = ctypes.c_double(); xmax = ctypes.c_double()
+        self.lib.ref_rad_table_info(ctypes.byref(isz), ctypes.byref(imin), ctypes.byref(imax), xd,
+                                    ctypes.byref(xmin), ctypes.byref(xmax))
+        integ = np.zeros(isz.value); xi = np.zeros((xd[0], xd[1])); amin = np.zeros(xd[0])
+        self.lib.ref_rad_table_data(_ptr(integ), _ptr(xi), _ptr(amin))
+        return dict(integfochi=integ, integfochi_min=imin.value, integfochi_max=imax.value,
+                    xi=xi, xi_min=xmin.value, xi_max=xmax.value, xi_axis1_min=amin)
+
+    def rad_yield(self, chi, gamma, factor):
+        chi = _f64(chi); gamma = _f64(gamma); out = np.zeros_like(chi)
+        self.lib.ref_rad_yield(len(chi), _ptr(chi), _ptr(gamma), ctypes.c_double(factor), _ptr(out))
+        return out
+
+    def rad_photon_chi(self, chi, xi):
+        chi = _f64(chi); xi = _f64(xi); out = np.zeros_like(chi)
+        self.lib.ref_rad_photon_chi(len(chi), _ptr(chi), _ptr(xi), _ptr(out))
+        return out

@@ -1,0 +1,164 @@
+"""Generate the golden fixtures in tests/golden from the reference's own operators.
+
+Run here, where the reference tree is present:
+
+    python tests/golden/make_golden.py
+
+It compiles the reference's operator sources (oracle/build_ref.sh), feeds them
+seeded inputs, and stores inputs and outputs as .npz files next to this script.
+The tests compare the C oracle (oracle/pic_oracle.c) against these files on any
+machine, and the GPU kernels against the oracle; nothing at test time reads the
+reference tree.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+import oracle  # noqa: E402
+
+FIELDS_EB = ["Ex", "Ey", "Ez", "Bx", "By", "Bz"]
+
+
+def geometry(ndim, cells, patch_start, oversize=2):
+    n_prim = [cells[d] + 1 + 2 * oversize for d in range(ndim)]
+    domain_begin = [patch_start[d] - oversize for d in range(ndim)]
+    return n_prim, domain_begin
+
+
+def random_fields(rng, ndim, n_prim, names, scale=1.0):
+    return {k: rng.normal(0.0, scale, oracle.field_shape(ndim, n_prim, k)) for k in names}
+
+
+def random_positions(rng, ndim, cells, patch_start, cell_length, n):
+    """Uniform positions inside the patch, plus a few exactly on half-cell points (rounding edge)."""
+    pos = np.zeros((ndim, n))
+    for d in range(ndim):
+        lo = patch_start[d] * cell_length[d]
+        pos[d] = lo + rng.uniform(0.0, cells[d], n) * cell_length[d]
+    # Put some particles exactly on half-integer node coordinates, where round()'s
+    # half-away-from-zero rule matters.
+    k = max(1, n // 16)
+    for d in range(ndim):
+        idx = rng.integers(0, cells[d], k)
+        pos[d, :k] = (patch_start[d] + idx + 0.5) * cell_length[d]
+    return pos
+
+
+def case_interpolate(ref, rng, ndim):
+    cells = [6, 5, 4][:ndim]
+    start = [3, -1, 2][:ndim] if ndim == 3 else [4, 2]
+    cell_length = [0.1, 0.15, 0.2][:ndim]
+    n_prim, db = geometry(ndim, cells, start)
+    F = random_fields(rng, ndim, n_prim, FIELDS_EB)
+    pos = random_positions(rng, ndim, cells, start, cell_length, 600)
+    E, B, iold, delta = ref.interpolate(ndim, n_prim, db, cell_length, [F[k] for k in FIELDS_EB], pos)
+    return dict(ndim=ndim, n_prim=n_prim, domain_begin=db, cell_length=cell_length, pos=pos,
+                **{k: F[k] for k in FIELDS_EB}, E=E, B=B, iold=iold, delta=delta)
+
+
+def case_push(ref, rng, ndim, kind, mass, field_scale):
+    n = 500
+    pos = rng.uniform(0.0, 2.0, (ndim, n))
+    mom = rng.normal(0.0, 1.0, (3, n)) * np.where(rng.uniform(size=n) < 0.3, 30.0, 0.2)
+    charge = rng.choice(np.array([-2, -1, 1, 2], dtype=np.int16), n)
+    E = rng.normal(0.0, field_scale, (3, n))
+    B = rng.normal(0.0, field_scale, (3, n))
+    dt = 0.05
+    pos1, mom1, invgf = ref.push(kind, ndim, dt, mass, pos, mom, charge, E, B)
+    return dict(kind=kind, ndim=ndim, dt=dt, mass=mass, pos=pos, mom=mom, charge=charge, E=E, B=B,
+                pos_out=pos1, mom_out=mom1, invgf=invgf)
+
+
+def case_project(ref, rng, ndim, mode):
+    cells = [7, 6, 5][:ndim]
+    start = [2, 4, -3][:ndim]
+    cell_length = [0.1, 0.12, 0.09][:ndim]
+    dt = 0.05
+    n_prim, db = geometry(ndim, cells, start)
+    n = 400
+    # Keep old positions one cell away from the patch edges so the 5-point stencil stays inside.
+    pos_old = np.zeros((ndim, n))
+    for d in range(ndim):
+        pos_old[d] = (start[d] + 1 + rng.uniform(0.0, cells[d] - 2, n)) * cell_length[d]
+    zeros = random_fields(rng, ndim, n_prim, FIELDS_EB, 0.0)
+    _, _, iold, delta = ref.interpolate(ndim, n_prim, db, cell_length, [zeros[k] for k in FIELDS_EB], pos_old)
+    disp = rng.uniform(-0.95, 0.95, (ndim, n)) * np.array(cell_length)[:, None]
+    pos = pos_old + disp
+    mom = rng.normal(0.0, 0.5, (3, n))
+    invgf = 1.0 / np.sqrt(1.0 + (mom ** 2).sum(0))
+    weight = rng.uniform(0.5, 1.5, n)
+    charge = rng.choice(np.array([-1, 1, 2], dtype=np.int16), n)
+    J0 = random_fields(rng, ndim, n_prim, ["Jx", "Jy", "Jz", "rho"], 0.1)
+    Jin = [J0[k].copy() for k in ["Jx", "Jy", "Jz", "rho"]]
+    Jout = ref.project(mode, ndim, n_prim, db, cell_length, dt, pos, mom, weight, charge, invgf, iold, delta,
+                       [a.copy() for a in Jin])
+    return dict(mode=mode, ndim=ndim, n_prim=n_prim, domain_begin=db, cell_length=cell_length, dt=dt, pos=pos,
+                mom=mom, weight=weight, charge=charge, invgf=invgf, iold=iold, delta=delta,
+                Jx_in=Jin[0], Jy_in=Jin[1], Jz_in=Jin[2], rho_in=Jin[3],
+                Jx=Jout[0], Jy=Jout[1], Jz=Jout[2], rho=Jout[3])
+
+
+def case_maxwell(ref, rng, ndim, which):
+    cells = [6, 7, 5][:ndim]
+    cell_length = [0.1, 0.12, 0.08][:ndim]
+    dt = 0.04
+    n_prim, _ = geometry(ndim, cells, [0, 0, 0][:ndim])
+    names = FIELDS_EB + ["Jx", "Jy", "Jz"]
+    F = random_fields(rng, ndim, n_prim, names)
+    Fin = [F[k].copy() for k in names]
+    Fout = ref.maxwell(which, ndim, n_prim, cell_length, dt, [a.copy() for a in Fin])
+    out = dict(which=which, ndim=ndim, n_prim=n_prim, cell_length=cell_length, dt=dt)
+    for k, a, b in zip(names, Fin, Fout):
+        out[k + "_in"] = a
+        out[k] = b
+    return out
+
+
+def case_radiation(ref, rng):
+    t = ref.rad_tables()
+    n = 4000
+    # particle chi across and beyond the table range, xi in [0, 1)
+    chi = 10.0 ** rng.uniform(-4.5, 3.5, n)
+    xi = rng.uniform(0.0, 1.0, n)
+    xi[:50] = 0.0
+    gamma = 1.0 + 10.0 ** rng.uniform(0.0, 4.0, n)
+    factor = 3.7e3
+    y = ref.rad_yield(chi, gamma, factor)
+    pc = ref.rad_photon_chi(chi, xi)
+    return dict(chi=chi, xi=xi, gamma=gamma, factor=factor, yield_=y, photon_chi=pc,
+                integfochi=t["integfochi"], integfochi_min=t["integfochi_min"],
+                integfochi_max=t["integfochi_max"], xi_table=t["xi"], xi_min=t["xi_min"], xi_max=t["xi_max"],
+                xi_axis1_min=t["xi_axis1_min"])
+
+
+def main():
+    path = oracle.build_ref()
+    if path is None:
+        raise SystemExit("reference tree not found; the fixtures cannot be regenerated here")
+    ref = oracle.RefOps(path)
+    rng = np.random.default_rng(20261204)
+    cases = {}
+    for ndim in (2, 3):
+        cases[f"interp{ndim}d"] = case_interpolate(ref, rng, ndim)
+        for kind in ("boris", "vay", "higueracary"):
+            for mass, scale in ((1.0, 0.5), (1836.0, 30.0)):
+                cases[f"push_{kind}_{ndim}d_m{int(mass)}"] = case_push(ref, rng, ndim, kind, mass, scale)
+        for mode in (0, 1, 2):
+            cases[f"project{ndim}d_mode{mode}"] = case_project(ref, rng, ndim, mode)
+        for which in (0, 1):
+            cases[f"maxwell{ndim}d_{'ampere' if which == 0 else 'faraday'}"] = case_maxwell(ref, rng, ndim, which)
+    np.savez_compressed(os.path.join(HERE, "operators.npz"),
+                        **{f"{c}/{k}": np.asarray(v) for c, d in cases.items() for k, v in d.items()})
+    rad = case_radiation(ref, rng)
+    np.savez_compressed(os.path.join(HERE, "radiation.npz"), **{k: np.asarray(v) for k, v in rad.items()})
+    print("wrote", len(cases), "operator cases and the radiation case")
+
+
+if __name__ == "__main__":
+    main()
