@@ -1,0 +1,338 @@
+"""Benchmark: particle-steps/s of the resident PIC timestep on one GB300 (and replicas on N GPUs).
+
+Workload (default): the 3D thermal plasma -- 256^3 cells, dx = 0.1 c/omega_p,
+dt = 0.95 CFL, periodic, electrons only over an immobile neutralising
+background, 8 particles per cell (134,217,728 particles), Maxwellian
+T = 10 keV (sigma_p = sqrt(10/511)), Higuera-Cary pusher, order-2 gather and
+Esirkepov deposit, Yee solver -- in the split-precision form (int cell index +
+FP32 offset, FP32 arithmetic); ``--form fp64`` runs the plain FP64 form.
+Synthetic seeded inputs are generated on the device.
+
+One step = gather + push + deposit + per-tile sort of every particle, J ghost
+fold, Ampere, Faraday and B centring (sg_sim_step).  ``value`` is the
+device-timed throughput with the state resident in HBM (134M particles, far
+larger than L2); ``e2e`` drives the same step through the C ABI from host
+buffers: each step copies the particle state host->device, steps, copies it
+back and reads the energy scalars.
+
+``--impl reference`` times the CPU restatement of the reference operators
+(oracle/pic_oracle.c, OpenMP on every host core) on a bounded sample of the
+same workload; it is the reference arm because the reference's OpenACC GPU
+build needs a compiler that is not installed and the reference tree is not
+present on the GPU host.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s on 1 GB300 (mixed vs FP64 form), % of HBM roofline"
+UNIT = "particle-steps/s"
+SIGMA_10KEV = float(np.sqrt(10.0 / 511.0))
+
+
+def workload_cfg(args):
+    n = args.cells
+    dx = 0.1
+    dt = 0.95 * dx / np.sqrt(3.0)
+    return dict(n_cells=[n, n, n], cell_length=[dx, dx, dx], dt=float(dt), ppc=args.ppc, pusher="higueracary",
+                sigma=SIGMA_10KEV)
+
+
+def bytes_alg_per_particle_step(form, ppc):
+    """B_alg = S_state + 24 * s / ppc (state read+write once; 24 grid values per cell per step)."""
+    if form == "mixed":
+        return 60.0 + 24 * 4 / ppc, 60.0, 4
+    return 104.0 + 24 * 8 / ppc, 104.0, 8
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join("/tmp", f"sg_clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.gpu)], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None:
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    mx.append(float(f[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, f[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        except OSError:
+            return None
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_plasma(cfg, seed, device):
+    """Seeded thermal plasma generated on the device (FP64 positions, momenta, weights)."""
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    n_cells, cl, ppc = cfg["n_cells"], cfg["cell_length"], cfg["ppc"]
+    ncell = int(np.prod(n_cells))
+    n = ncell * ppc
+    pos = torch.empty((3, n), dtype=torch.float64, device=device)
+    cell = torch.arange(n, device=device, dtype=torch.int64) // ppc
+    strides = [n_cells[1] * n_cells[2], n_cells[2], 1]
+    for d in range(3):
+        c = (cell // strides[d]) % n_cells[d]
+        pos[d] = (c.to(torch.float64) + torch.rand(n, generator=g, device=device, dtype=torch.float64)) * cl[d]
+        del c
+    del cell
+    mom = torch.randn((3, n), generator=g, device=device, dtype=torch.float64) * cfg["sigma"]
+    w = torch.full((n,), float(np.prod(cl)) / ppc, dtype=torch.float64, device=device)
+    return pos, mom, w
+
+
+def run_gpu(args, rank, world, local_rank):
+    import torch
+    from smilei_gb300 import simulation
+    device = f"cuda:{local_rank}"
+    torch.cuda.set_device(local_rank)
+    cfg = workload_cfg(args)
+    pos, mom, w = make_plasma(cfg, args.seed + rank, device)
+    n = int(w.shape[0])
+    sim = simulation.Simulation(cfg["n_cells"], cfg["cell_length"], cfg["dt"], form=args.form,
+                                tile=[args.tile] * 3 if args.tile else None, use_graph=True)
+    stream = torch.cuda.current_stream()
+    from smilei_gb300 import _lib
+    _lib.check(_lib.lib().sg_sim_set_stream(sim._h, stream.cuda_stream), "set_stream")
+    sim.add_species(1.0, -1.0, cfg["pusher"], pos, mom, w)
+    del pos, mom, w
+    torch.cuda.empty_cache()
+    uk0, ue0 = sim.energy()
+    for _ in range(args.warmup):
+        sim.step(1)
+    dist = world > 1
+    if dist:
+        import torch.distributed as td
+        td.barrier()
+    torch.cuda.synchronize()
+    t_part = []
+    launches = 0
+    with ClockSampler(local_rank) as clk:
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        wall0 = time.perf_counter()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            sim.step(1)
+            tp, tf, tt, launches = sim.last_timing()
+            t_part.append(tp)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        wall1 = time.perf_counter()
+    if dist:
+        td.barrier()
+    ms = ev0.elapsed_time(ev1)
+    if dist:
+        t = torch.tensor([ms], device=device)
+        td.all_reduce(t, op=td.ReduceOp.MAX)
+        ms = float(t.item())
+    uk1, ue1 = sim.energy()
+
+    # e2e: the same step driven from host buffers through the C ABI
+    e2e = None
+    if not args.no_e2e:
+        nbytes = sim.state_bytes(0)
+        host = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+        sim.copy_state(0, host.data_ptr(), False)
+        torch.cuda.synchronize()
+        ke = max(1, min(args.steps, args.e2e_steps))
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        if dist:
+            td.barrier()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(ke):
+            sim.copy_state(0, host.data_ptr(), True)
+            sim.step(1)
+            sim.copy_state(0, host.data_ptr(), False)
+            sim.energy()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ems = e0.elapsed_time(e1)
+        if dist:
+            t = torch.tensor([ems], device=device)
+            td.all_reduce(t, op=td.ReduceOp.MAX)
+            ems = float(t.item())
+        e2e = {"value": n * world * ke / (ems / 1e3), "unit": UNIT, "h2d_bytes_per_step": int(nbytes),
+               "d2h_bytes_per_step": int(nbytes + 16), "steps": ke}
+        del host
+    sim.close()
+    B_alg, s_state, s = bytes_alg_per_particle_step(args.form, args.ppc)
+    ncell = int(np.prod(cfg["n_cells"]))
+    kernel_bytes = n * s_state + ncell * 9 * s  # state read+write; gather E,B_m and J write per cell
+    t_kernel = float(np.mean(t_part)) / 1e3
+    peak, peak_kind = measured_peak()
+    value = n * world * args.steps / (ms / 1e3)
+    return dict(n=n, ms=ms, value=value, wall_ms_per_step=(wall1 - wall0) * 1e3 / args.steps, e2e=e2e,
+                kernel_bytes=kernel_bytes, t_kernel=t_kernel, peak=peak, peak_kind=peak_kind, B_alg=B_alg,
+                launches=launches, clocks=clk.summary(), energy=(uk0, ue0, uk1, ue1), cfg=cfg)
+
+
+def run_cpu_sample(args, steps=None):
+    """The oracle's FP64 timestep on a bounded sample of the workload (all host cores)."""
+    import oracle
+    n = args.cpu_cells
+    dx = 0.1
+    dt = 0.95 * dx / np.sqrt(3.0)
+    from smilei_gb300 import synthetic
+    pos, mom, w = synthetic.thermal_plasma([n, n, n], [dx] * 3, args.ppc, SIGMA_10KEV, args.seed)
+    fields = synthetic.periodic_em(args.seed, [n, n, n], 0.0, 0.0)
+    sp = [dict(pos=pos, mom=mom, weight=w, charge=np.full(w.shape, -1, np.int16), mass=1.0, pusher="higueracary")]
+    O = oracle.Oracle()
+    steps = steps or args.cpu_steps
+    O.pic_step(3, [n] * 3, 2, [dx] * 3, dt, fields, sp)  # warm-up
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        O.pic_step(3, [n] * 3, 2, [dx] * 3, dt, fields, sp)
+    t1 = time.perf_counter()
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    value = pos.shape[1] * steps / (t1 - t0)
+    return dict(value=value, unit=UNIT, cores=cores, kind="port",
+                sample=f"3D thermal {n}^3 cells x {args.ppc} ppc ({pos.shape[1]} electrons), Higuera-Cary, "
+                       f"{steps} FP64 steps of oracle/pic_oracle.c (OpenMP)")
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--form", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--cells", type=int, default=256)
+    ap.add_argument("--ppc", type=int, default=8)
+    ap.add_argument("--tile", type=int, default=0)
+    ap.add_argument("--seed", type=int, default=1234)
+    ap.add_argument("--cpu-cells", type=int, default=64)
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    workload = (f"3D thermal plasma {args.cells}^3 cells, {args.ppc} ppc electrons "
+                f"({args.cells ** 3 * args.ppc} particles per GPU), Higuera-Cary, dt=0.95 CFL, periodic")
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        r = run_cpu_sample(args)
+        line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+                "steps": args.cpu_steps, "warmup": 1, "ms_per_step": None, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, host)",
+                "config": {"workload": workload, "sample": r["sample"], "form": "fp64"},
+                "cpu_baseline": r,
+                "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    if world > 1:
+        import torch.distributed as td
+        td.init_process_group("nccl")
+    res = run_gpu(args, rank, world, local_rank)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            cpu = run_cpu_sample(args)
+        except Exception as e:  # the baseline is reported, not required
+            cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {e}"}
+    if rank != 0:
+        if world > 1:
+            import torch.distributed as td
+            td.destroy_process_group()
+        return
+    achieved = res["kernel_bytes"] / res["t_kernel"] / 1e9
+    step_gbs = res["B_alg"] * res["value"] / 1e9
+    line = {
+        "metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": res["ms"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+i32" if args.form == "mixed" else "f64",
+        "data": "synthetic (seeded Maxwellian, generated on device)",
+        "config": {"workload": workload, "form": args.form, "global_particles": res["n"] * world,
+                   "cells": args.cells ** 3, "parallelism": f"replicas x{world}", "l2": "inputs larger than L2",
+                   "B_alg_bytes_per_particle_step": res["B_alg"],
+                   "hbm_fraction_of_step": step_gbs / res["peak"], "wall_ms_per_step": res["wall_ms_per_step"],
+                   "energy_ukin_uelm_before_after": res["energy"]},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": res["peak"], "unit": "GB/s",
+                     "frac": achieved / res["peak"], "traffic": None, "kernel": "k_step_particles",
+                     "peak_source": res["peak_kind"]},
+        "cpu_baseline": cpu,
+        "e2e": res["e2e"],
+        "gpu_launches": res["launches"] * args.steps,
+        "clocks": res["clocks"],
+    }
+    print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as td
+        td.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

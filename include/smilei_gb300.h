@@ -1,0 +1,187 @@
+/* smilei_gb300.h -- C ABI of libsmileigb300.so, the GB300 (sm_103a) PIC-step hot path.
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, runs on the
+ * caller's CUDA stream (NULL = legacy default stream), returns an int status
+ * (SG_OK = 0, negative on error) and never exits the process.  The text of
+ * the last error of the calling thread is returned by sg_last_error().
+ *
+ * Data layout is the reference's (Smilei):
+ *   - fields: one array per component, x-major with the last dimension
+ *     fastest, ghost cells included; a primal dimension has
+ *     n_cells + 1 + 2*oversize points and a dual one has one more
+ *     (src/ElectroMagn/ElectroMagn3D.cpp:115-123, src/Params/Params.cpp:1202-1207).
+ *     Staggering Ex(d,p,p) Ey(p,d,p) Ez(p,p,d) Bx(p,d,d) By(d,p,d) Bz(d,d,p),
+ *     J like E, rho primal; in 2D the third index is dropped.
+ *   - particles: structure of arrays, absolute positions pos[d*n + i],
+ *     momenta mom[d*n + i], weight[i], charge[i] (short)
+ *     (src/Particles/Particles.h:48, property order Particles.cpp:71-98).
+ *   - interpolator -> pusher -> projector scratch Epart[3n], Bpart[3n],
+ *     invgf[n], iold[ndim*n] (int), deltaold[ndim*n]
+ *     (src/SmileiMPI/SmileiMPI.h:213-221).
+ * Pointers given to the operator entry points are device pointers.
+ */
+#ifndef SMILEI_GB300_H
+#define SMILEI_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SG_OK 0
+#define SG_ERR_ARG (-1)        /* invalid argument */
+#define SG_ERR_CUDA (-2)       /* a CUDA runtime call failed */
+#define SG_ERR_BOUNDS (-3)     /* a particle left the region its kernel can reach (device check) */
+#define SG_ERR_OVERFLOW (-4)   /* a capacity was exceeded and could not be grown */
+#define SG_ERR_STATE (-5)      /* call not valid in the object's current state */
+#define SG_ERR_NOMEM (-6)      /* device allocation failed */
+
+typedef void *sg_stream_t; /* a cudaStream_t */
+
+/* Geometry of one patch's field arrays.
+ * n_prim[d]       primal extent with ghosts (patch_size[d] + 1 + 2*oversize[d])
+ * domain_begin[d] global index of local point 0 (patch start - oversize),
+ *                 as src/Interpolator/Interpolator3D.cpp:14-16 and
+ *                 src/Projector/Projector3D2Order.cpp:29-31 compute it. */
+typedef struct sg_grid_geom {
+    int ndim;
+    int n_prim[3];
+    int domain_begin[3];
+    double cell_length[3];
+} sg_grid_geom;
+
+const char *sg_last_error( void );
+int sg_version( void );
+
+/* ---- operator entry points (FP64, the reference's arrays on the device) ---- */
+
+/* Order-2 gather of E and B_m at the particles.
+ * Replaces Interpolator3D2Order::fieldsWrapper / Interpolator2D2Order::fieldsWrapper
+ * (src/Interpolator/Interpolator.h:23, Interpolator3D2Order.cpp:163,
+ * Interpolator2D2Order.cpp:158).  fields = {Ex, Ey, Ez, Bx_m, By_m, Bz_m}. */
+int sg_interpolate_fields( const sg_grid_geom *geom, const double *const *fields, int64_t npart,
+                           const double *pos, double *Epart, double *Bpart, int *iold, double *deltaold,
+                           sg_stream_t stream );
+
+/* Particle push; kind 0 = Boris, 1 = Vay, 2 = Higuera-Cary.
+ * Replaces Pusher::operator() (src/Pusher/Pusher.h:22; PusherBoris.cpp:23,
+ * PusherVay.cpp:32, PusherHigueraCary.cpp:32).  pos/mom updated in place. */
+int sg_push_particles( int kind, int ndim, double dt, double mass, int64_t npart, double *pos, double *mom,
+                       const short *charge, const double *Epart, const double *Bpart, double *invgf,
+                       sg_stream_t stream );
+
+/* Charge-conserving (Esirkepov) deposit, accumulated into J.
+ * mode 0: currents; 1: currents and rho (diagnostic step); 2: rho only from the
+ * current positions (Projector3D2Order::basic, used at initialisation).
+ * Replaces Projector::currentsAndDensityWrapper (src/Projector/Projector.h:44;
+ * Projector3D2Order.cpp:733, Projector2D2Order.cpp:498) and the reference's own
+ * device entry point currentDeposition3DOnDevice
+ * (src/Projector/Projector3D2OrderGPUKernel.cpp:40).
+ * J = {Jx, Jy, Jz, rho}; unused entries may be NULL. */
+int sg_project_currents( int mode, const sg_grid_geom *geom, double dt, int64_t npart, const double *pos,
+                         const double *mom, const double *weight, const short *charge, const double *invgf,
+                         const int *iold, const double *deltaold, double *const *J, sg_stream_t stream );
+
+/* Yee solver on one patch.  F = {Ex, Ey, Ez, Bx, By, Bz, Jx, Jy, Jz}.
+ * Ampere replaces MA_Solver3D_norm/MA_Solver2D_norm::operator()
+ * (src/ElectroMagnSolver/MA_Solver3D_norm.cpp:18), all points.
+ * Faraday replaces MF_Solver3D_Yee/MF_Solver2D_Yee::operator()
+ * (src/ElectroMagnSolver/MF_Solver3D_Yee.cpp:18), interior points. */
+int sg_maxwell_ampere( const sg_grid_geom *geom, double dt, double *const *F, sg_stream_t stream );
+int sg_maxwell_faraday( const sg_grid_geom *geom, double dt, double *const *F, sg_stream_t stream );
+
+/* B_m <- B and B_m <- (B + B_m)/2 on all points.  B = {Bx, By, Bz}, Bm likewise.
+ * Replace ElectroMagn3D::saveMagneticFields / centerMagneticFields
+ * (src/ElectroMagn/ElectroMagn3D.cpp:1048, :1191). */
+int sg_save_magnetic_fields( const sg_grid_geom *geom, double *const *B, double *const *Bm, sg_stream_t stream );
+int sg_center_magnetic_fields( const sg_grid_geom *geom, double *const *B, double *const *Bm, sg_stream_t stream );
+
+/* Per-cell particle sort.  key = sum_d (round(x_d/dx_d) - round(xmin_d/dx_d)) * stride_d
+ * over the (patch_size+1)^ndim node lattice (src/Species/SpeciesV.cpp:766-857);
+ * counts -> prefix sum -> first_index/last_index (SpeciesV.cpp:645-652); then every
+ * double property (pos[ndim], mom[3], weight, and any extra arrays) and the charge are
+ * permuted so each cell's particles are contiguous (stable: original order kept inside
+ * a cell).  Replaces Species::sortParticles (src/Species/Species.cpp:1046) for
+ * particles that stay in the patch.  A particle whose key falls outside the lattice
+ * is an error (SG_ERR_BOUNDS).
+ * dprops: n_dprops device arrays of npart doubles; scratch is allocated internally. */
+int sg_sort_particles( int ndim, const int *patch_size, const double *xmin, const double *cell_length,
+                       int64_t npart, double *const *dprops, int n_dprops, short *charge, int *first_index,
+                       int *last_index, int *cell_keys, sg_stream_t stream );
+
+/* ---- simulation object: the whole timestep resident on one GPU ---- */
+
+/* Form of the particle/field arithmetic. */
+#define SG_FORM_FP64 0  /* absolute FP64 positions, FP64 fields and currents (the reference's) */
+#define SG_FORM_MIXED 1 /* int cell index + FP32 in-cell offset, FP32 momenta/fields/currents */
+
+typedef struct sg_sim_config {
+    int ndim;              /* 2 or 3 */
+    int form;              /* SG_FORM_FP64 or SG_FORM_MIXED */
+    int n_cells[3];        /* global cells per dimension (periodic) */
+    double cell_length[3];
+    double dt;
+    int tile[3];           /* cells per tile (bin) per dimension; 0 = choose automatically */
+    double capacity_slack; /* extra room per tile, as a fraction of its count (e.g. 0.25) */
+    int use_graph;         /* capture each timestep as a CUDA graph */
+} sg_sim_config;
+
+typedef struct sg_sim sg_sim;
+
+int sg_sim_create( const sg_sim_config *cfg, sg_sim **out );
+int sg_sim_destroy( sg_sim *sim );
+
+/* Adds a species from host arrays (absolute FP64 positions pos[ndim*n],
+ * momenta mom[3*n], weights[n]); pusher: 0 Boris, 1 Vay, 2 Higuera-Cary.
+ * Returns the species index in *index. */
+int sg_sim_add_species( sg_sim *sim, double mass, double charge, int pusher, int64_t npart, const double *pos,
+                        const double *mom, const double *weight, int *index );
+
+/* Same, from device arrays (same layout), without host copies. */
+int sg_sim_add_species_device( sg_sim *sim, double mass, double charge, int pusher, int64_t npart,
+                               const double *pos, const double *mom, const double *weight, int *index );
+
+/* Field access, reference layout with ghosts, FP64, host (set/get) or device (_device) buffers.
+ * comp: 0..2 Ex Ey Ez, 3..5 Bx By Bz, 6..8 Bx_m By_m Bz_m, 9..11 Jx Jy Jz. */
+int sg_sim_set_field( sg_sim *sim, int comp, const double *host );
+int sg_sim_get_field( sg_sim *sim, int comp, double *host );
+int sg_sim_field_shape( sg_sim *sim, int comp, int *shape3 );
+
+/* Runs nsteps full timesteps (gather, push, deposit, bin sort, J ghost fold,
+ * Ampere, Faraday, B centring) on the simulation's stream. */
+int sg_sim_step( sg_sim *sim, int nsteps );
+
+/* Synchronises and copies a species back as absolute FP64 positions, momenta and
+ * weights (sorted by tile; the order is not the input order).  *npart receives the
+ * count; the arrays must hold at least that many particles. */
+int sg_sim_species_count( sg_sim *sim, int species, int64_t *npart );
+int sg_sim_get_species( sg_sim *sim, int species, double *pos, double *mom, double *weight );
+
+/* Energy diagnostics (FP64 device reductions): kinetic energy per species summed,
+ * sum_p w m (gamma - 1), and field energy 0.5 * sum (E^2 + B_m^2) * V_cell over the
+ * interior points (src/Diagnostic/DiagnosticScalar.cpp:174-277). */
+int sg_sim_energy( sg_sim *sim, double *ukin, double *uelm );
+
+/* Raw particle state of a species (the library's own SoA layout, tile segments
+ * included): its size, and a copy of the current buffer to (to_device = 0) or
+ * from (to_device = 1) a host buffer of that size, on the simulation's stream
+ * (asynchronous with pinned host memory).  A copy taken and restored unchanged
+ * leaves the simulation as it was; this is how a caller that keeps particles in
+ * host memory drives the resident step. */
+int sg_sim_state_bytes( sg_sim *sim, int species, size_t *bytes );
+int sg_sim_copy_state( sg_sim *sim, int species, void *host, int to_device );
+
+/* Device time of the last sg_sim_step call split by stage (ms): particles, fold,
+ * maxwell, total; and the number of kernel launches per step. */
+int sg_sim_last_timing( sg_sim *sim, double *ms_particles, double *ms_fields, double *ms_total, int *launches_per_step );
+
+/* Sets the stream the simulation runs on (default: a stream it creates). */
+int sg_sim_set_stream( sg_sim *sim, sg_stream_t stream );
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SMILEI_GB300_H */

@@ -226,9 +226,10 @@ static void old_new_shapes( double d_old, double xn, int ipo_global, int *shift_
     *shift_out = shift;
 }
 
-int or_project( int mode, int ndim, const int *n_prim, const int *domain_begin, const double *cell_length, double dt,
-                int64_t npart, const double *pos, const double *mom, const double *weight, const short *charge,
-                const double *invgf, const int *iold, const double *delta, double *const *J )
+static void project_range( int mode, int ndim, const int *n_prim, const int *domain_begin, const double *cell_length,
+                           double dt, int64_t npart, const double *pos, const double *mom, const double *weight,
+                           const short *charge, const double *invgf, const int *iold, const double *delta,
+                           double *const *J, int64_t p_begin, int64_t p_end )
 {
     double inv_vol = 1.0, dx_inv[3], dx_ov_dt[3];
     for( int d = 0; d < ndim; d++ ) {
@@ -240,7 +241,7 @@ int or_project( int mode, int ndim, const int *n_prim, const int *domain_begin, 
     double *Jx = J[0], *Jy = J[1], *Jz = J[2], *rho = J[3];
     const int nxp = n_prim[0], nyp = n_prim[1], nzp = ndim == 3 ? n_prim[2] : 1;
     ( void )nxp;
-    for( int64_t p = 0; p < npart; p++ ) {
+    for( int64_t p = p_begin; p < p_end; p++ ) {
         const double cw = inv_vol * ( double )charge[p] * weight[p];
         if( mode == 2 ) {
             /* basic(): rho from the current position only. */
@@ -338,6 +339,62 @@ int or_project( int mode, int ndim, const int *n_prim, const int *domain_begin, 
                 }
         }
     }
+}
+
+/* Large particle counts are split over OpenMP threads, each depositing into a
+ * private copy of the current arrays that is summed afterwards (the reference
+ * gets the same effect from per-thread patches).  Small counts keep the
+ * sequential order of the reference's loop. */
+int or_project( int mode, int ndim, const int *n_prim, const int *domain_begin, const double *cell_length, double dt,
+                int64_t npart, const double *pos, const double *mom, const double *weight, const short *charge,
+                const double *invgf, const int *iold, const double *delta, double *const *J )
+{
+#ifdef _OPENMP
+    const int nthr = omp_get_max_threads();
+    if( npart >= 100000 && nthr > 1 ) {
+        int64_t size[4];
+        const int st[4][3] = { { 1, 0, 0 }, { 0, 1, 0 }, { 0, 0, 1 }, { 0, 0, 0 } };
+        int64_t total = 0;
+        for( int c = 0; c < 4; c++ ) {
+            size[c] = 1;
+            for( int d = 0; d < ndim; d++ ) size[c] *= n_prim[d] + st[c][d];
+            if( J[c] ) total += size[c];
+        }
+        double *priv = calloc( ( size_t )total * nthr, sizeof( double ) );
+        if( priv ) {
+#pragma omp parallel num_threads( nthr )
+            {
+                const int t = omp_get_thread_num();
+                double *Jt[4] = { NULL, NULL, NULL, NULL };
+                double *base = priv + ( int64_t )t * total;
+                for( int c = 0; c < 4; c++ )
+                    if( J[c] ) { Jt[c] = base; base += size[c]; }
+                const int64_t chunk = ( npart + nthr - 1 ) / nthr;
+                const int64_t a = t * chunk, b = a + chunk < npart ? a + chunk : npart;
+                if( a < b )
+                    project_range( mode, ndim, n_prim, domain_begin, cell_length, dt, npart, pos, mom, weight, charge,
+                                   invgf, iold, delta, Jt, a, b );
+            }
+            int64_t off = 0;
+            for( int c = 0; c < 4; c++ ) {
+                if( !J[c] ) continue;
+                double *dst = J[c];
+                const int64_t sc = size[c];
+#pragma omp parallel for schedule( static )
+                for( int64_t i = 0; i < sc; i++ ) {
+                    double acc = dst[i];
+                    for( int t = 0; t < nthr; t++ ) acc += priv[( int64_t )t * total + off + i];
+                    dst[i] = acc;
+                }
+                off += sc;
+            }
+            free( priv );
+            return 0;
+        }
+    }
+#endif
+    project_range( mode, ndim, n_prim, domain_begin, cell_length, dt, npart, pos, mom, weight, charge, invgf, iold,
+                   delta, J, 0, npart );
     return 0;
 }
 

@@ -1,0 +1,124 @@
+"""ctypes binding of libsmileigb300.so (the C ABI declared in include/smilei_gb300.h).
+
+The library is the only compute path: there is no CPU fallback.  If it is
+missing it is built with nvcc on first use; if that fails the import error is
+raised to the caller.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+from . import build as _build
+
+_lock = threading.Lock()
+_lib = None
+
+SG_OK = 0
+ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "particle out of reach", -4: "capacity overflow",
+          -5: "invalid state", -6: "out of device memory"}
+
+FORM_FP64 = 0
+FORM_MIXED = 1
+PUSHERS = {"boris": 0, "vay": 1, "higueracary": 2}
+
+
+class SmileiGPUError(RuntimeError):
+    def __init__(self, code: int, where: str, message: str):
+        super().__init__(f"{where}: {ERRORS.get(code, code)} ({code}): {message}")
+        self.code = code
+
+
+class GridGeom(ctypes.Structure):
+    _fields_ = [("ndim", ctypes.c_int), ("n_prim", ctypes.c_int * 3), ("domain_begin", ctypes.c_int * 3),
+                ("cell_length", ctypes.c_double * 3)]
+
+
+class SimConfig(ctypes.Structure):
+    _fields_ = [("ndim", ctypes.c_int), ("form", ctypes.c_int), ("n_cells", ctypes.c_int * 3),
+                ("cell_length", ctypes.c_double * 3), ("dt", ctypes.c_double), ("tile", ctypes.c_int * 3),
+                ("capacity_slack", ctypes.c_double), ("use_graph", ctypes.c_int)]
+
+
+_VP = ctypes.c_void_p
+_I = ctypes.c_int
+_I64 = ctypes.c_int64
+_D = ctypes.c_double
+_PP = ctypes.POINTER(ctypes.c_void_p)
+
+_SIGNATURES = {
+    "sg_last_error": (ctypes.c_char_p, []),
+    "sg_version": (_I, []),
+    "sg_interpolate_fields": (_I, [ctypes.POINTER(GridGeom), _PP, _I64, _VP, _VP, _VP, _VP, _VP, _VP]),
+    "sg_push_particles": (_I, [_I, _I, _D, _D, _I64, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
+    "sg_project_currents": (_I, [_I, ctypes.POINTER(GridGeom), _D, _I64, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _PP,
+                                 _VP]),
+    "sg_maxwell_ampere": (_I, [ctypes.POINTER(GridGeom), _D, _PP, _VP]),
+    "sg_maxwell_faraday": (_I, [ctypes.POINTER(GridGeom), _D, _PP, _VP]),
+    "sg_save_magnetic_fields": (_I, [ctypes.POINTER(GridGeom), _PP, _PP, _VP]),
+    "sg_center_magnetic_fields": (_I, [ctypes.POINTER(GridGeom), _PP, _PP, _VP]),
+    "sg_sort_particles": (_I, [_I, ctypes.POINTER(_I), ctypes.POINTER(_D), ctypes.POINTER(_D), _I64, _PP, _I, _VP,
+                               _VP, _VP, _VP, _VP]),
+    "sg_sim_create": (_I, [ctypes.POINTER(SimConfig), ctypes.POINTER(_VP)]),
+    "sg_sim_destroy": (_I, [_VP]),
+    "sg_sim_add_species": (_I, [_VP, _D, _D, _I, _I64, _VP, _VP, _VP, ctypes.POINTER(_I)]),
+    "sg_sim_add_species_device": (_I, [_VP, _D, _D, _I, _I64, _VP, _VP, _VP, ctypes.POINTER(_I)]),
+    "sg_sim_set_field": (_I, [_VP, _I, _VP]),
+    "sg_sim_get_field": (_I, [_VP, _I, _VP]),
+    "sg_sim_field_shape": (_I, [_VP, _I, ctypes.POINTER(_I)]),
+    "sg_sim_step": (_I, [_VP, _I]),
+    "sg_sim_species_count": (_I, [_VP, _I, ctypes.POINTER(_I64)]),
+    "sg_sim_get_species": (_I, [_VP, _I, _VP, _VP, _VP]),
+    "sg_sim_energy": (_I, [_VP, ctypes.POINTER(_D), ctypes.POINTER(_D)]),
+    "sg_sim_last_timing": (_I, [_VP, ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.POINTER(_D),
+                                ctypes.POINTER(_I)]),
+    "sg_sim_set_stream": (_I, [_VP, _VP]),
+    "sg_sim_state_bytes": (_I, [_VP, _I, ctypes.POINTER(ctypes.c_size_t)]),
+    "sg_sim_copy_state": (_I, [_VP, _I, _VP, _I]),
+}
+
+
+def declared_symbols() -> list[str]:
+    """Entry points declared in include/smilei_gb300.h (parsed from the header)."""
+    import re
+    hdr = os.path.join(_build.ROOT, "include", "smilei_gb300.h")
+    text = open(hdr).read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(sg_\w+)\s*\(", text, re.M)))
+
+
+def lib() -> ctypes.CDLL:
+    """The loaded library (built on first use when missing or stale)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            path = _build.build()
+            L = ctypes.CDLL(path)
+            for name, (res, args) in _SIGNATURES.items():
+                fn = getattr(L, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = L
+    return _lib
+
+
+def last_error() -> str:
+    return lib().sg_last_error().decode(errors="replace")
+
+
+def check(code: int, where: str):
+    if code != SG_OK:
+        raise SmileiGPUError(code, where, last_error())
+
+
+def ptr(t) -> int | None:
+    """Device (or host) address of a torch tensor / numpy array, or None."""
+    if t is None:
+        return None
+    if hasattr(t, "data_ptr"):
+        return t.data_ptr()
+    return t.ctypes.data
+
+
+def ptr_array(ts) -> ctypes.Array:
+    return (ctypes.c_void_p * len(ts))(*[ptr(t) for t in ts])

@@ -1,0 +1,1664 @@
+// The simulation object: a whole periodic PIC timestep resident on one GPU.
+//
+// Layout in HBM
+//   fields   one array per component in the reference's layout (ghost width
+//            2, primal N+5 / dual N+6 points per dimension, x-major), in the
+//            form's precision (FP64 or FP32): E, B, B_m, J.
+//   tiles    the grid is cut into tiles (bins) of T cells per dimension; a
+//            particle belongs to the tile of its nearest primal node.
+//   particles per species, two structure-of-arrays buffers (ping-pong).  Each
+//            tile owns a segment [seg_start[t], seg_start[t] + cap[t]) in both
+//            buffers; count[t] particles of the segment are live.
+//            FP64 form:  x, y, z, px, py, pz, w          (double)
+//            mixed form: key (packed node index), dx, dy, dz (in-cell offset
+//                        in [-0.5, 0.5), cell units), px, py, pz, w (float)
+//
+// One step (all on the simulation's stream, optionally one CUDA graph):
+//   J <- 0; per species: k_step_particles (one CTA per tile: stage the tile's
+//   E and B_m in shared memory, gather, push, Esirkepov deposit into a
+//   shared J tile, write each particle to its destination tile's segment in the
+//   other buffer, flush the J tile with global atomics); fold the periodic J
+//   ghosts; Ampere on all points; Faraday on all points (periodic images for the
+//   boundary layer) fused with B_m <- (B_new + B_old)/2.
+// A tile whose segment fills up spills particles to an overflow list; the host
+// sees the spill after the step and re-lays the segments out (rare).
+
+#include "common.cuh"
+#include "scan.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace sg {
+namespace {
+
+constexpr int OS = 2; // ghost width (oversize) of order-2 interpolation
+
+struct GridInfo {
+    int ndim;
+    int N[3];   // cells per dimension
+    int np[3];  // primal extents with ghosts (N + 1 + 2*OS); 1 for an absent dimension
+    int T[3];   // tile size in cells
+    int nt[3];  // tiles per dimension
+    int ntiles;
+    double dx[3], dxi[3], L[3], dt;
+};
+
+// Extent of a component with staggering flags s[] (dual adds one point).
+__host__ __device__ inline int ext( const GridInfo &g, int d, int dual ) { return d < g.ndim ? g.np[d] + dual : 1; }
+
+// Staggering of E, B, J components: comp 0..2 E/J, 3..5 B.
+__host__ __device__ inline int stag( int comp, int d )
+{
+    // Ex(d,p,p) Ey(p,d,p) Ez(p,p,d) Bx(p,d,d) By(d,p,d) Bz(d,d,p)
+    if( comp < 3 ) return d == comp ? 1 : 0;
+    return d == comp - 3 ? 0 : 1;
+}
+
+template <class T>
+struct Fields {
+    T *E[3], *B[3], *Bm[3], *J[3];
+};
+
+template <bool MIXED>
+struct PBuf;
+template <>
+struct PBuf<false> {
+    double *x[3];
+    double *p[3];
+    double *w;
+};
+template <>
+struct PBuf<true> {
+    unsigned *key;
+    float *d[3];
+    float *p[3];
+    float *w;
+};
+
+struct SpecParams {
+    double qm_dts2;  // charge / mass * dt / 2
+    double charge;
+    double mass;
+    double cw;       // charge * inverse cell volume (per unit weight)
+};
+
+// Packed node index of the mixed form: 3D x:11 y:10 z:10 bits, 2D x:16 y:16 bits.
+__host__ __device__ inline unsigned pack_key( int ndim, int ix, int iy, int iz )
+{
+    return ndim == 3 ? ( ( unsigned )ix << 20 ) | ( ( unsigned )iy << 10 ) | ( unsigned )iz
+                     : ( ( unsigned )ix << 16 ) | ( unsigned )iy;
+}
+__host__ __device__ inline void unpack_key( int ndim, unsigned k, int &ix, int &iy, int &iz )
+{
+    if( ndim == 3 ) {
+        ix = ( int )( k >> 20 );
+        iy = ( int )( ( k >> 10 ) & 1023u );
+        iz = ( int )( k & 1023u );
+    } else {
+        ix = ( int )( k >> 16 );
+        iy = ( int )( k & 65535u );
+        iz = 0;
+    }
+}
+
+__host__ __device__ inline int tile_of( const GridInfo &g, int ix, int iy, int iz )
+{
+    int t = ix / g.T[0];
+    t = t * g.nt[1] + iy / g.T[1];
+    if( g.ndim == 3 ) t = t * g.nt[2] + iz / g.T[2];
+    return t;
+}
+
+// ------------------------------------------------------------------------------
+// The fused particle kernel.
+// ------------------------------------------------------------------------------
+template <class T>
+__device__ __forceinline__ T rsqrt_t( T x );
+template <>
+__device__ __forceinline__ double rsqrt_t<double>( double x ) { return 1.0 / sqrt( x ); }
+template <>
+__device__ __forceinline__ float rsqrt_t<float>( float x ) { return 1.0f / sqrtf( x ); }
+
+template <int KIND, class T>
+__device__ __forceinline__ T push_t( T qm, T Ex, T Ey, T Ez, T Bx, T By, T Bz, T &px, T &py, T &pz )
+{
+    if( KIND == 0 ) {
+        T pxsm = qm * Ex, pysm = qm * Ey, pzsm = qm * Ez;
+        const T umx = px + pxsm, umy = py + pysm, umz = pz + pzsm;
+        const T lg = qm * rsqrt_t<T>( T( 1 ) + umx * umx + umy * umy + umz * umz );
+        const T Tx = lg * Bx, Ty = lg * By, Tz = lg * Bz;
+        const T inv_det = T( 1 ) / ( T( 1 ) + Tx * Tx + Ty * Ty + Tz * Tz );
+        pxsm += ( ( T( 1 ) + Tx * Tx - Ty * Ty - Tz * Tz ) * umx + T( 2 ) * ( Tx * Ty + Tz ) * umy + T( 2 ) * ( Tz * Tx - Ty ) * umz ) * inv_det;
+        pysm += ( T( 2 ) * ( Tx * Ty - Tz ) * umx + ( T( 1 ) - Tx * Tx + Ty * Ty - Tz * Tz ) * umy + T( 2 ) * ( Ty * Tz + Tx ) * umz ) * inv_det;
+        pzsm += ( T( 2 ) * ( Tz * Tx + Ty ) * umx + T( 2 ) * ( Ty * Tz - Tx ) * umy + ( T( 1 ) - Tx * Tx - Ty * Ty + Tz * Tz ) * umz ) * inv_det;
+        px = pxsm; py = pysm; pz = pzsm;
+    } else if( KIND == 1 ) {
+        const T g0 = rsqrt_t<T>( T( 1 ) + px * px + py * py + pz * pz );
+        T upx = px + T( 2 ) * qm * Ex, upy = py + T( 2 ) * qm * Ey, upz = pz + T( 2 ) * qm * Ez;
+        T Tx = qm * Bx, Ty = qm * By, Tz = qm * Bz;
+        upx += g0 * ( py * Tz - pz * Ty );
+        upy += g0 * ( pz * Tx - px * Tz );
+        upz += g0 * ( px * Ty - py * Tx );
+        T alpha = T( 1 ) + upx * upx + upy * upy + upz * upz;
+        const T T2 = Tx * Tx + Ty * Ty + Tz * Tz;
+        T s = alpha - T2;
+        T us2 = upx * Tx + upy * Ty + upz * Tz;
+        us2 = us2 * us2;
+        alpha = rsqrt_t<T>( T( 0.5 ) * ( s + sqrt( s * s + T( 4 ) * ( T2 + us2 ) ) ) );
+        Tx *= alpha; Ty *= alpha; Tz *= alpha;
+        s = T( 1 ) / ( T( 1 ) + Tx * Tx + Ty * Ty + Tz * Tz );
+        alpha = upx * Tx + upy * Ty + upz * Tz;
+        px = s * ( upx + alpha * Tx + Tz * upy - Ty * upz );
+        py = s * ( upy + alpha * Ty + Tx * upz - Tz * upx );
+        pz = s * ( upz + alpha * Tz + Ty * upx - Tx * upy );
+    } else {
+        T pxsm = qm * Ex, pysm = qm * Ey, pzsm = qm * Ez;
+        const T umx = px + pxsm, umy = py + pysm, umz = pz + pzsm;
+        const T gfm2 = T( 1 ) + umx * umx + umy * umy + umz * umz;
+        T Tx = qm * Bx, Ty = qm * By, Tz = qm * Bz;
+        const T beta2 = Tx * Tx + Ty * Ty + Tz * Tz;
+        const T Tum = Tx * umx + Ty * umy + Tz * umz;
+        const T lg = rsqrt_t<T>( T( 0.5 ) * ( gfm2 - beta2 + sqrt( ( gfm2 - beta2 ) * ( gfm2 - beta2 ) + T( 4 ) * ( beta2 + Tum * Tum ) ) ) );
+        Tx *= lg; Ty *= lg; Tz *= lg;
+        const T Tx2 = Tx * Tx, Ty2 = Ty * Ty, Tz2 = Tz * Tz;
+        const T TxTy = Tx * Ty, TyTz = Ty * Tz, TzTx = Tz * Tx;
+        const T inv_det = T( 1 ) / ( T( 1 ) + Tx2 + Ty2 + Tz2 );
+        const T upx = ( ( T( 1 ) + Tx2 - Ty2 - Tz2 ) * umx + T( 2 ) * ( TxTy + Tz ) * umy + T( 2 ) * ( TzTx - Ty ) * umz ) * inv_det;
+        const T upy = ( T( 2 ) * ( TxTy - Tz ) * umx + ( T( 1 ) - Tx2 + Ty2 - Tz2 ) * umy + T( 2 ) * ( TyTz + Tx ) * umz ) * inv_det;
+        const T upz = ( T( 2 ) * ( TzTx + Ty ) * umx + T( 2 ) * ( TyTz - Tx ) * umy + ( T( 1 ) - Tx2 - Ty2 + Tz2 ) * umz ) * inv_det;
+        px = pxsm + upx; py = pysm + upy; pz = pzsm + upz;
+    }
+    return rsqrt_t<T>( T( 1 ) + px * px + py * py + pz * pz );
+}
+
+struct TileDims {
+    int FX, FY, FZ; // field tile extents (T + 3)
+    int JX, JY, JZ; // current tile extents (T + 4)
+};
+
+__host__ __device__ inline TileDims tile_dims( const GridInfo &g )
+{
+    TileDims t;
+    t.FX = g.T[0] + 3;
+    t.FY = g.T[1] + 3;
+    t.FZ = g.ndim == 3 ? g.T[2] + 3 : 1;
+    t.JX = g.T[0] + 4;
+    t.JY = g.T[1] + 4;
+    t.JZ = g.ndim == 3 ? g.T[2] + 4 : 1;
+    return t;
+}
+
+// Gather one component from the shared tile: sum_a cx[a] sum_b cy[b] sum_c cz[c] F.
+template <int DIM, class T>
+__device__ __forceinline__ T gather_tile( const T *__restrict__ F, const TileDims &td, const T *cx, const T *cy,
+                                          const T *cz, int bx, int by, int bz )
+{
+    T r = T( 0 );
+#pragma unroll
+    for( int a = 0; a < 3; a++ ) {
+        T ra = T( 0 );
+#pragma unroll
+        for( int b = 0; b < 3; b++ ) {
+            const T *row = F + ( ( bx + a ) * td.FY + ( by + b ) ) * td.FZ + bz;
+            if( DIM == 3 ) {
+                const T rb = cz[0] * row[0] + cz[1] * row[1] + cz[2] * row[2];
+                ra += cy[b] * rb;
+            } else {
+                ra += cy[b] * row[0];
+            }
+        }
+        r += cx[a] * ra;
+    }
+    return r;
+}
+
+template <class T>
+__device__ __forceinline__ void sh_add( T *a, T v )
+{
+    if( v != T( 0 ) ) atomicAdd( a, v );
+}
+
+// Per-dimension Esirkepov window: 4 nodes starting at lo (0 or 1) of the
+// 5-point stencil; A = (S0+S1)/2, D = S1-S0, P = running sums of D.
+template <class T>
+struct EsirWin {
+    int lo;
+    T A[4], D[4], P[3];
+};
+
+template <class T>
+__device__ __forceinline__ void esir_win( T c0o, T c1o, T c2o, T dnew, int shift, EsirWin<T> &w )
+{
+    T S0[5] = { T( 0 ), c0o, c1o, c2o, T( 0 ) };
+    T S1[5] = { T( 0 ), T( 0 ), T( 0 ), T( 0 ), T( 0 ) };
+    T c0, c1, c2;
+    bspline2( dnew, c0, c1, c2 );
+    S1[shift + 1] = c0;
+    S1[shift + 2] = c1;
+    S1[shift + 3] = c2;
+    w.lo = shift < 0 ? 0 : 1;
+    T run = T( 0 );
+#pragma unroll
+    for( int i = 0; i < 4; i++ ) {
+        const T s0 = S0[w.lo + i], s1 = S1[w.lo + i];
+        w.A[i] = T( 0.5 ) * ( s0 + s1 );
+        w.D[i] = s1 - s0;
+        if( i < 3 ) {
+            run += w.D[i];
+            w.P[i] = run;
+        }
+    }
+}
+
+template <int DIM, bool MIXED, int KIND>
+__global__ void __launch_bounds__( 128 ) k_step_particles(
+    GridInfo g, Fields<typename std::conditional<MIXED, float, double>::type> f, SpecParams sp, PBuf<MIXED> in,
+    PBuf<MIXED> out, const int64_t *__restrict__ seg_start, const int *__restrict__ cap,
+    const int *__restrict__ count_in, int *__restrict__ count_out, PBuf<MIXED> ovf, int *__restrict__ ovf_tile,
+    int *__restrict__ ovf_count, int ovf_cap, int *__restrict__ status )
+{
+    using T = typename std::conditional<MIXED, float, double>::type;
+    extern __shared__ __align__( 16 ) unsigned char smem_raw[];
+    T *sF = reinterpret_cast<T *>( smem_raw );
+    const TileDims td = tile_dims( g );
+    const int fsz = td.FX * td.FY * td.FZ;
+    const int jsz = td.JX * td.JY * td.JZ;
+    T *sJ = sF + 6 * fsz;
+
+    const int tile = blockIdx.x;
+    int tz = 0, ty, tx;
+    if( DIM == 3 ) {
+        tz = tile % g.nt[2];
+        ty = ( tile / g.nt[2] ) % g.nt[1];
+        tx = tile / ( g.nt[2] * g.nt[1] );
+    } else {
+        ty = tile % g.nt[1];
+        tx = tile / g.nt[1];
+    }
+    const int ix0 = tx * g.T[0], iy0 = ty * g.T[1], iz0 = DIM == 3 ? tz * g.T[2] : 0;
+
+    // 1. stage E and B_m (field tile origin = array index (i0 + OS - 1)) and clear J
+    for( int c = 0; c < 6; c++ ) {
+        const T *src = c < 3 ? f.E[c] : f.Bm[c - 3];
+        const int ny = ext( g, 1, stag( c, 1 ) ), nz = ext( g, 2, stag( c, 2 ) );
+        const int nx = ext( g, 0, stag( c, 0 ) );
+        for( int e = threadIdx.x; e < fsz; e += blockDim.x ) {
+            const int cz = e % td.FZ, cy = ( e / td.FZ ) % td.FY, cx = e / ( td.FZ * td.FY );
+            const int gx = ix0 + OS - 1 + cx, gy = iy0 + OS - 1 + cy, gz = DIM == 3 ? iz0 + OS - 1 + cz : 0;
+            T v = T( 0 );
+            if( gx < nx && gy < ny && gz < nz ) v = src[( ( int64_t )gx * ny + gy ) * nz + gz];
+            sF[c * fsz + e] = v;
+        }
+    }
+    for( int e = threadIdx.x; e < 3 * jsz; e += blockDim.x ) sJ[e] = T( 0 );
+    __syncthreads();
+
+    const int n = count_in[tile];
+    const int64_t s0 = seg_start[tile];
+    const T dt = T( g.dt );
+    const T qm = T( sp.qm_dts2 );
+    const unsigned lane = threadIdx.x & 31u;
+
+    for( int base = 0; base < n; base += blockDim.x ) {
+        const int q = base + threadIdx.x;
+        const bool valid = q < n;
+        const int64_t src = s0 + ( valid ? q : 0 );
+        // ---- load the particle ------------------------------------------------
+        int lx[3] = { 0, 0, 0 };   // old nearest node, tile-local
+        T dlt[3] = { T( 0 ), T( 0 ), T( 0 ) };
+        int gnode[3] = { 0, 0, 0 };
+        int img[3] = { 0, 0, 0 }; // FP64 form: N when the old node was wrapped to its image 0
+        double xabs[3] = { 0.0, 0.0, 0.0 };
+        double xpn[3] = { 0.0, 0.0, 0.0 };
+        T px = T( 0 ), py = T( 0 ), pz = T( 0 ), w = T( 0 );
+        if( valid ) {
+            if constexpr( MIXED ) {
+                const unsigned key = in.key[src];
+                unpack_key( DIM, key, gnode[0], gnode[1], gnode[2] );
+#pragma unroll
+                for( int d = 0; d < DIM; d++ ) dlt[d] = ( T )in.d[d][src];
+            } else {
+#pragma unroll
+                for( int d = 0; d < DIM; d++ ) {
+                    xabs[d] = ( double )in.x[d][src];
+                    xpn[d] = xabs[d] * g.dxi[d];
+                    int ip = round_half_away( xpn[d] );
+                    if( ip >= g.N[d] ) { // x in [L - dx/2, L): use the image node 0
+                        ip -= g.N[d];
+                        img[d] = g.N[d];
+                        xpn[d] -= ( double )g.N[d];
+                    }
+                    gnode[d] = ip;
+                    dlt[d] = ( T )( xpn[d] - ( double )ip );
+                }
+            }
+            px = ( T )in.p[0][src];
+            py = ( T )in.p[1][src];
+            pz = ( T )in.p[2][src];
+            w = ( T )in.w[src];
+        }
+        lx[0] = gnode[0] - ix0;
+        lx[1] = gnode[1] - iy0;
+        lx[2] = DIM == 3 ? gnode[2] - iz0 : 0;
+        bool ok = !valid || ( lx[0] >= 0 && lx[0] < g.T[0] && lx[1] >= 0 && lx[1] < g.T[1] &&
+                              ( DIM == 2 || ( lx[2] >= 0 && lx[2] < g.T[2] ) ) );
+        if( !ok ) {
+            atomicCAS( status, 0, SG_ERR_BOUNDS );
+            lx[0] = lx[1] = lx[2] = 0;
+        }
+
+        // ---- gather ---------------------------------------------------------------
+        T cp[3][3], cd[3][3];
+        int sd[3] = { 0, 0, 0 };
+#pragma unroll
+        for( int d = 0; d < 3; d++ ) {
+            if( d < DIM ) {
+                bspline2( dlt[d], cp[d][0], cp[d][1], cp[d][2] );
+                T dd;
+                if constexpr( MIXED ) {
+                    sd[d] = dlt[d] >= T( 0 ) ? 1 : 0;
+                    dd = dlt[d] + T( 0.5 ) - T( sd[d] );
+                } else {
+                    const int id = round_half_away( xpn[d] + 0.5 );
+                    sd[d] = id - gnode[d];
+                    dd = ( T )( xpn[d] - ( double )id + 0.5 );
+                }
+                bspline2( dd, cd[d][0], cd[d][1], cd[d][2] );
+            } else {
+                cp[d][0] = cp[d][2] = T( 0 ); cp[d][1] = T( 1 );
+                cd[d][0] = cd[d][2] = T( 0 ); cd[d][1] = T( 1 );
+            }
+        }
+        // clamp the dual shift for safety (0 or 1 by construction)
+#pragma unroll
+        for( int d = 0; d < 3; d++ ) sd[d] = sd[d] < 0 ? 0 : ( sd[d] > 1 ? 1 : sd[d] );
+        const int bz_p = DIM == 3 ? lx[2] : 0, bz_d = DIM == 3 ? lx[2] + sd[2] : 0;
+        const int bx_p = lx[0], bx_d = lx[0] + sd[0], by_p = lx[1], by_d = lx[1] + sd[1];
+        // Ex(d,p,p) Ey(p,d,p) Ez(p,p,d) Bx(p,d,d) By(d,p,d) Bz(d,d,p)
+        const T Ex = gather_tile<DIM, T>( sF + 0 * fsz, td, cd[0], cp[1], cp[2], bx_d, by_p, bz_p );
+        const T Ey = gather_tile<DIM, T>( sF + 1 * fsz, td, cp[0], cd[1], cp[2], bx_p, by_d, bz_p );
+        const T Ez = gather_tile<DIM, T>( sF + 2 * fsz, td, cp[0], cp[1], cd[2], bx_p, by_p, bz_d );
+        const T Bx = gather_tile<DIM, T>( sF + 3 * fsz, td, cp[0], cd[1], cd[2], bx_p, by_d, bz_d );
+        const T By = gather_tile<DIM, T>( sF + 4 * fsz, td, cd[0], cp[1], cd[2], bx_d, by_p, bz_d );
+        const T Bz = gather_tile<DIM, T>( sF + 5 * fsz, td, cd[0], cd[1], cp[2], bx_d, by_d, bz_p );
+
+        // ---- push -----------------------------------------------------------------
+        const T ginv = push_t<KIND, T>( qm, Ex, Ey, Ez, Bx, By, Bz, px, py, pz );
+
+        // ---- move: new position, node shift per dimension ---------------------
+        int shift[3] = { 0, 0, 0 };
+        T dnew[3] = { T( 0 ), T( 0 ), T( 0 ) };
+        const T pm[3] = { px, py, pz };
+        if constexpr( MIXED ) {
+#pragma unroll
+            for( int d = 0; d < DIM; d++ ) {
+                const T dn = dlt[d] + pm[d] * ( ginv * dt * T( g.dxi[d] ) );
+                const int sh = ( int )floorf( ( float )dn + 0.5f );
+                shift[d] = sh;
+                dnew[d] = dn - T( sh );
+            }
+        } else {
+#pragma unroll
+            for( int d = 0; d < DIM; d++ ) {
+                double xn;
+                if( KIND == 0 ) xn = xabs[d] + ( double )pm[d] * ( ( double )ginv * g.dt );
+                else xn = xabs[d] + g.dt * ( double )pm[d] * ( double )ginv;
+                xabs[d] = xn;
+                // same image shift as the old position (exact: both terms are near N)
+                const double xnn = xn * g.dxi[d] - ( double )img[d];
+                const int ipn = round_half_away( xnn );
+                shift[d] = ipn - gnode[d];
+                dnew[d] = ( T )( xnn - ( double )ipn );
+            }
+        }
+        bool moved_ok = true;
+#pragma unroll
+        for( int d = 0; d < DIM; d++ ) {
+            if( shift[d] < -1 || shift[d] > 1 ) moved_ok = false;
+        }
+        if( valid && !moved_ok ) {
+            atomicCAS( status, 0, SG_ERR_BOUNDS );
+#pragma unroll
+            for( int d = 0; d < DIM; d++ ) shift[d] = shift[d] < -1 ? -1 : ( shift[d] > 1 ? 1 : shift[d] );
+        }
+
+        // ---- Esirkepov deposit into the shared J tile ------------------------
+        if( valid ) {
+            EsirWin<T> W[3];
+#pragma unroll
+            for( int d = 0; d < DIM; d++ ) esir_win<T>( cp[d][0], cp[d][1], cp[d][2], dnew[d], shift[d], W[d] );
+            const T cw = T( sp.cw ) * w;
+            const T twelfth = T( 1.0 / 12.0 );
+            if( DIM == 3 ) {
+                const T cr[3] = { cw * T( g.dx[0] / g.dt ), cw * T( g.dx[1] / g.dt ), cw * T( g.dx[2] / g.dt ) };
+                // Jx(d,p,p): node i' = lo+1+m, j = lo+jw, k = lo+kw (tile index = old node + stencil index)
+#pragma unroll
+                for( int c = 0; c < 3; c++ ) {
+                    const int a = c, b = ( c + 1 ) % 3, e = ( c + 2 ) % 3;
+                    T *J = sJ + c * jsz;
+#pragma unroll
+                    for( int u = 0; u < 4; u++ )
+#pragma unroll
+                        for( int v = 0; v < 4; v++ ) {
+                            const T wgt = W[b].A[u] * W[e].A[v] + twelfth * W[b].D[u] * W[e].D[v];
+                            if( wgt == T( 0 ) ) continue;
+                            int idx[3];
+                            idx[b] = lx[b] + W[b].lo + u;
+                            idx[e] = lx[e] + W[e].lo + v;
+#pragma unroll
+                            for( int m = 0; m < 3; m++ ) {
+                                idx[a] = lx[a] + W[a].lo + 1 + m;
+                                const T val = -cr[a] * W[a].P[m] * wgt;
+                                sh_add( &J[( idx[0] * td.JY + idx[1] ) * td.JZ + idx[2]], val );
+                            }
+                        }
+                }
+            } else {
+                const T crx = cw * T( g.dx[0] / g.dt ), cry = cw * T( g.dx[1] / g.dt );
+                const T crz = cw * pz * ginv;
+                T *J0 = sJ, *J1 = sJ + jsz, *J2 = sJ + 2 * jsz;
+#pragma unroll
+                for( int u = 0; u < 4; u++ ) {
+                    const T ay = W[1].A[u];
+                    if( ay != T( 0 ) ) {
+#pragma unroll
+                        for( int m = 0; m < 3; m++ )
+                            sh_add( &J0[( lx[0] + W[0].lo + 1 + m ) * td.JY + lx[1] + W[1].lo + u], -crx * W[0].P[m] * ay );
+                    }
+                    const T ax = W[0].A[u];
+                    if( ax != T( 0 ) ) {
+#pragma unroll
+                        for( int m = 0; m < 3; m++ )
+                            sh_add( &J1[( lx[0] + W[0].lo + u ) * td.JY + lx[1] + W[1].lo + 1 + m], -cry * W[1].P[m] * ax );
+                    }
+#pragma unroll
+                    for( int v = 0; v < 4; v++ ) {
+                        const T wz = W[0].A[u] * W[1].A[v] + twelfth * W[0].D[u] * W[1].D[v];
+                        sh_add( &J2[( lx[0] + W[0].lo + u ) * td.JY + lx[1] + W[1].lo + v], crz * wz );
+                    }
+                }
+            }
+        }
+
+        // ---- destination tile and write-out --------------------------------------
+        int nn[3] = { 0, 0, 0 };
+        if constexpr( MIXED ) {
+#pragma unroll
+            for( int d = 0; d < DIM; d++ ) {
+                int v = gnode[d] + shift[d];
+                if( v < 0 ) v += g.N[d];
+                if( v >= g.N[d] ) v -= g.N[d];
+                nn[d] = v;
+            }
+        } else {
+#pragma unroll
+            for( int d = 0; d < DIM; d++ ) {
+                double x = xabs[d];
+                if( x < 0.0 ) x += g.L[d];
+                if( x >= g.L[d] ) x -= g.L[d];
+                xabs[d] = x;
+                int ip = round_half_away( x * g.dxi[d] );
+                if( ip >= g.N[d] ) ip -= g.N[d];
+                nn[d] = ip;
+            }
+        }
+        // a non-finite or runaway particle must not index outside the tile tables
+#pragma unroll
+        for( int d = 0; d < DIM; d++ ) {
+            if( valid && ( nn[d] < 0 || nn[d] >= g.N[d] ) ) {
+                atomicCAS( status, 0, SG_ERR_BOUNDS );
+                nn[d] = 0;
+            }
+        }
+        const int dest = valid ? tile_of( g, nn[0], nn[1], DIM == 3 ? nn[2] : 0 ) : -1;
+        // warp-aggregated slot allocation per destination tile
+        const unsigned peers = __match_any_sync( 0xffffffffu, dest );
+        const int leader = __ffs( peers ) - 1;
+        int slot_base = 0;
+        if( valid && ( int )lane == leader ) slot_base = atomicAdd( &count_out[dest], __popc( peers ) );
+        slot_base = __shfl_sync( 0xffffffffu, slot_base, leader );
+        if( valid ) {
+            const int slot = slot_base + __popc( peers & ( ( 1u << lane ) - 1u ) );
+            PBuf<MIXED> dst = out;
+            int64_t o;
+            if( slot < cap[dest] ) {
+                o = seg_start[dest] + slot;
+            } else {
+                const int k = atomicAdd( ovf_count, 1 );
+                if( k >= ovf_cap ) {
+                    atomicCAS( status, 0, SG_ERR_OVERFLOW );
+                    o = -1;
+                } else {
+                    dst = ovf;
+                    o = k;
+                    ovf_tile[k] = dest;
+                }
+            }
+            if( o >= 0 ) {
+                if constexpr( MIXED ) {
+                    dst.key[o] = pack_key( DIM, nn[0], nn[1], nn[2] );
+#pragma unroll
+                    for( int d = 0; d < DIM; d++ ) dst.d[d][o] = ( float )dnew[d];
+                } else {
+#pragma unroll
+                    for( int d = 0; d < DIM; d++ ) dst.x[d][o] = xabs[d];
+                }
+                dst.p[0][o] = px;
+                dst.p[1][o] = py;
+                dst.p[2][o] = pz;
+                dst.w[o] = w;
+            }
+        }
+    }
+    __syncthreads();
+
+    // 4. flush the J tile (origin = array index i0 + OS - 2) with global atomics
+    for( int c = 0; c < 3; c++ ) {
+        T *dstJ = f.J[c];
+        const int ny = ext( g, 1, stag( c, 1 ) ), nz = ext( g, 2, stag( c, 2 ) );
+        const int nx = ext( g, 0, stag( c, 0 ) );
+        for( int e = threadIdx.x; e < jsz; e += blockDim.x ) {
+            const T v = sJ[c * jsz + e];
+            if( v == T( 0 ) ) continue;
+            const int cz = e % td.JZ, cy = ( e / td.JZ ) % td.JY, cx = e / ( td.JZ * td.JY );
+            const int gx = ix0 + OS - 2 + cx, gy = iy0 + OS - 2 + cy, gz = DIM == 3 ? iz0 + OS - 2 + cz : 0;
+            if( gx < nx && gy < ny && gz < nz ) atomicAdd( &dstJ[( ( int64_t )gx * ny + gy ) * nz + gz], v );
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------
+// Field kernels of the periodic single-grid step.
+// ------------------------------------------------------------------------------
+
+// Periodic J ghost fold along dimension d (the same-process branch of
+// SyncVectorPatch::sumAllComponents, SyncVectorPatch.cpp:203-330): the first
+// 1 + 2*OS (+1 if dual) planes and their images N planes further are summed and
+// both set to the sum.  blockIdx.y = component.
+template <class T>
+__global__ void k_fold( GridInfo g, int d, Fields<T> f )
+{
+    const int c = blockIdx.y;
+    T *a = f.J[c];
+    const int e0 = ext( g, 0, stag( c, 0 ) ), e1 = ext( g, 1, stag( c, 1 ) ), e2 = ext( g, 2, stag( c, 2 ) );
+    int se[3] = { e0, e1, e2 };
+    se[d] = 1 + 2 * OS + stag( c, d );
+    const int64_t n = ( int64_t )se[0] * se[1] * se[2];
+    for( int64_t t = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x; t < n; t += ( int64_t )gridDim.x * blockDim.x ) {
+        const int k = ( int )( t % se[2] );
+        const int j = ( int )( ( t / se[2] ) % se[1] );
+        const int i = ( int )( t / ( ( int64_t )se[2] * se[1] ) );
+        int i2 = i, j2 = j, k2 = k;
+        if( d == 0 ) i2 += g.N[0];
+        else if( d == 1 ) j2 += g.N[1];
+        else k2 += g.N[2];
+        const int64_t a1 = ( ( int64_t )i * e1 + j ) * e2 + k;
+        const int64_t a2 = ( ( int64_t )i2 * e1 + j2 ) * e2 + k2;
+        const T v = a[a2] + a[a1];
+        a[a2] = v;
+        a[a1] = v;
+    }
+}
+
+// Ampere on every point (MA_Solver3D_norm.cpp:18-115 / MA_Solver2D_norm.cpp:18-107).
+// One block per row of the last dimension; E stays consistent between a node and
+// its periodic image because J (folded) and B (synchronised) are.
+template <int DIM, class T>
+__global__ void k_ampere_all( GridInfo g, Fields<T> f, T dt, T dtdx, T dtdy, T dtdz )
+{
+    const int nxp = g.np[0], nyp = g.np[1], nxd = nxp + 1, nyd = nyp + 1;
+    if( DIM == 3 ) {
+        const int nzp = g.np[2], nzd = nzp + 1;
+        const int row = blockIdx.x; // over nxd * nyd
+        const int i = row / nyd, j = row % nyd;
+        for( int k = threadIdx.x; k < nzd; k += blockDim.x ) {
+            if( j < nyp && k < nzp ) {
+                const int64_t t = ( ( int64_t )i * nyp + j ) * nzp + k;
+                f.E[0][t] += -dt * f.J[0][t] + dtdy * ( f.B[2][( ( int64_t )i * nyd + j + 1 ) * nzp + k] - f.B[2][( ( int64_t )i * nyd + j ) * nzp + k] )
+                             - dtdz * ( f.B[1][( ( int64_t )i * nyp + j ) * nzd + k + 1] - f.B[1][( ( int64_t )i * nyp + j ) * nzd + k] );
+            }
+            if( i < nxp && k < nzp ) {
+                const int64_t t = ( ( int64_t )i * nyd + j ) * nzp + k;
+                f.E[1][t] += -dt * f.J[1][t] - dtdx * ( f.B[2][( ( int64_t )( i + 1 ) * nyd + j ) * nzp + k] - f.B[2][t] )
+                             + dtdz * ( f.B[0][( ( int64_t )i * nyd + j ) * nzd + k + 1] - f.B[0][( ( int64_t )i * nyd + j ) * nzd + k] );
+            }
+            if( i < nxp && j < nyp ) {
+                const int64_t t = ( ( int64_t )i * nyp + j ) * nzd + k;
+                f.E[2][t] += -dt * f.J[2][t] + dtdx * ( f.B[1][( ( int64_t )( i + 1 ) * nyp + j ) * nzd + k] - f.B[1][t] )
+                             - dtdy * ( f.B[0][( ( int64_t )i * nyd + j + 1 ) * nzd + k] - f.B[0][( ( int64_t )i * nyd + j ) * nzd + k] );
+            }
+        }
+    } else {
+        const int i = blockIdx.x; // over nxd
+        for( int j = threadIdx.x; j < nyd; j += blockDim.x ) {
+            if( j < nyp ) {
+                const int64_t t = ( int64_t )i * nyp + j;
+                f.E[0][t] += -dt * f.J[0][t] + dtdy * ( f.B[2][( int64_t )i * nyd + j + 1] - f.B[2][( int64_t )i * nyd + j] );
+            }
+            if( i < nxp ) {
+                const int64_t t = ( int64_t )i * nyd + j;
+                f.E[1][t] += -dt * f.J[1][t] - dtdx * ( f.B[2][( int64_t )( i + 1 ) * nyd + j] - f.B[2][t] );
+            }
+            if( i < nxp && j < nyp ) {
+                const int64_t t = ( int64_t )i * nyp + j;
+                f.E[2][t] += -dt * f.J[2][t] + dtdx * ( f.B[1][( int64_t )( i + 1 ) * nyp + j] - f.B[1][t] )
+                             - dtdy * ( f.B[0][( int64_t )i * nyd + j + 1] - f.B[0][( int64_t )i * nyd + j] );
+            }
+        }
+    }
+}
+
+// Periodic image of a dual index in the outermost layers (0 -> N, nd-1 -> nd-1-N).
+__device__ __forceinline__ int canon( int i, int nd, int N ) { return i == 0 ? N : ( i == nd - 1 ? i - N : i ); }
+
+// Faraday on every point (MF_Solver3D_Yee.cpp:18-111 on the interior; the
+// outermost dual layers take their periodic image's update, which is what the
+// reference's B exchange copies there), fused with the B_m centring
+// (ElectroMagn3D::centerMagneticFields, ElectroMagn3D.cpp:1191): B_m = (B_new + B_old)/2.
+template <int DIM, class T>
+__global__ void k_faraday_center( GridInfo g, Fields<T> f, T dtdx, T dtdy, T dtdz )
+{
+    const int nxp = g.np[0], nyp = g.np[1], nxd = nxp + 1, nyd = nyp + 1;
+    const int Nx = g.N[0], Ny = g.N[1];
+    if( DIM == 3 ) {
+        const int nzp = g.np[2], nzd = nzp + 1, Nz = g.N[2];
+        const int row = blockIdx.x;
+        const int i = row / nyd, j = row % nyd;
+        const T *Ex = f.E[0], *Ey = f.E[1], *Ez = f.E[2];
+        for( int k = threadIdx.x; k < nzd; k += blockDim.x ) {
+            if( i < nxp ) { // Bx(p,d,d)
+                const int jc = canon( j, nyd, Ny ), kc = canon( k, nzd, Nz );
+                const int64_t t = ( ( int64_t )i * nyd + j ) * nzd + k;
+                const T old = f.B[0][t];
+                const T nw = old + ( -dtdy * ( Ez[( ( int64_t )i * nyp + jc ) * nzd + k] - Ez[( ( int64_t )i * nyp + jc - 1 ) * nzd + k] )
+                                     + dtdz * ( Ey[( ( int64_t )i * nyd + j ) * nzp + kc] - Ey[( ( int64_t )i * nyd + j ) * nzp + kc - 1] ) );
+                f.B[0][t] = nw;
+                f.Bm[0][t] = ( nw + old ) * T( 0.5 );
+            }
+            if( j < nyp ) { // By(d,p,d)
+                const int ic = canon( i, nxd, Nx ), kc = canon( k, nzd, Nz );
+                const int64_t t = ( ( int64_t )i * nyp + j ) * nzd + k;
+                const T old = f.B[1][t];
+                const T nw = old + ( -dtdz * ( Ex[( ( int64_t )i * nyp + j ) * nzp + kc] - Ex[( ( int64_t )i * nyp + j ) * nzp + kc - 1] )
+                                     + dtdx * ( Ez[( ( int64_t )ic * nyp + j ) * nzd + k] - Ez[( ( int64_t )( ic - 1 ) * nyp + j ) * nzd + k] ) );
+                f.B[1][t] = nw;
+                f.Bm[1][t] = ( nw + old ) * T( 0.5 );
+            }
+            if( k < nzp ) { // Bz(d,d,p)
+                const int ic = canon( i, nxd, Nx ), jc = canon( j, nyd, Ny );
+                const int64_t t = ( ( int64_t )i * nyd + j ) * nzp + k;
+                const T old = f.B[2][t];
+                const T nw = old + ( -dtdx * ( Ey[( ( int64_t )ic * nyd + j ) * nzp + k] - Ey[( ( int64_t )( ic - 1 ) * nyd + j ) * nzp + k] )
+                                     + dtdy * ( Ex[( ( int64_t )i * nyp + jc ) * nzp + k] - Ex[( ( int64_t )i * nyp + jc - 1 ) * nzp + k] ) );
+                f.B[2][t] = nw;
+                f.Bm[2][t] = ( nw + old ) * T( 0.5 );
+            }
+        }
+    } else {
+        const int i = blockIdx.x;
+        const T *Ex = f.E[0], *Ey = f.E[1], *Ez = f.E[2];
+        for( int j = threadIdx.x; j < nyd; j += blockDim.x ) {
+            if( i < nxp ) { // Bx(p,d)
+                const int jc = canon( j, nyd, Ny );
+                const int64_t t = ( int64_t )i * nyd + j;
+                const T old = f.B[0][t];
+                const T nw = old - dtdy * ( Ez[( int64_t )i * nyp + jc] - Ez[( int64_t )i * nyp + jc - 1] );
+                f.B[0][t] = nw;
+                f.Bm[0][t] = ( nw + old ) * T( 0.5 );
+            }
+            if( j < nyp ) { // By(d,p)
+                const int ic = canon( i, nxd, Nx );
+                const int64_t t = ( int64_t )i * nyp + j;
+                const T old = f.B[1][t];
+                const T nw = old + dtdx * ( Ez[( int64_t )ic * nyp + j] - Ez[( int64_t )( ic - 1 ) * nyp + j] );
+                f.B[1][t] = nw;
+                f.Bm[1][t] = ( nw + old ) * T( 0.5 );
+            }
+            { // Bz(d,d)
+                const int ic = canon( i, nxd, Nx ), jc = canon( j, nyd, Ny );
+                const int64_t t = ( int64_t )i * nyd + j;
+                const T old = f.B[2][t];
+                const T nw = old + ( dtdy * ( Ex[( int64_t )i * nyp + jc] - Ex[( int64_t )i * nyp + jc - 1] )
+                                     - dtdx * ( Ey[( int64_t )ic * nyd + j] - Ey[( int64_t )( ic - 1 ) * nyd + j] ) );
+                f.B[2][t] = nw;
+                f.Bm[2][t] = ( nw + old ) * T( 0.5 );
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------
+// Layout kernels (initial placement and re-layout after a spill; not per step).
+// ------------------------------------------------------------------------------
+
+// From FP64 positions/momenta/weights to the form's state; records the tile and counts it.
+template <int DIM, bool MIXED>
+__global__ void k_stage( GridInfo g, int64_t n, const double *__restrict__ pos, const double *__restrict__ mom,
+                         const double *__restrict__ wgt, PBuf<MIXED> st, int *__restrict__ st_tile,
+                         int *__restrict__ count )
+{
+    const int64_t p = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x;
+    if( p >= n ) return;
+    int node[3] = { 0, 0, 0 };
+#pragma unroll
+    for( int d = 0; d < DIM; d++ ) {
+        double x = pos[d * n + p];
+        if( x < 0.0 ) x += g.L[d];
+        if( x >= g.L[d] ) x -= g.L[d];
+        const double xn = x * g.dxi[d];
+        int ip = round_half_away( xn );
+        double dl = xn - ( double )ip;
+        if( ip >= g.N[d] ) ip -= g.N[d];
+        if( ip < 0 ) ip += g.N[d];
+        if( ip < 0 || ip >= g.N[d] ) ip = 0; // non-finite input: keep the index inside the tables
+        node[d] = ip;
+        if constexpr( MIXED ) st.d[d][p] = ( float )dl;
+        else st.x[d][p] = x;
+    }
+    if constexpr( MIXED ) st.key[p] = pack_key( DIM, node[0], node[1], node[2] );
+    st.p[0][p] = ( decltype( st.p[0][0] ) )mom[p];
+    st.p[1][p] = ( decltype( st.p[0][0] ) )mom[n + p];
+    st.p[2][p] = ( decltype( st.p[0][0] ) )mom[2 * n + p];
+    st.w[p] = ( decltype( st.w[0] ) )wgt[p];
+    const int t = tile_of( g, node[0], node[1], node[2] );
+    st_tile[p] = t;
+    atomicAdd( &count[t], 1 );
+}
+
+// cap[t] = count[t] * (1 + slack) + min_extra, rounded up to a multiple of 4.
+__global__ void k_caps( int nt, const int *__restrict__ count, int *__restrict__ cap, float slack, int min_extra )
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if( t >= nt ) return;
+    const int c = count[t];
+    int v = c + max( ( int )ceilf( c * slack ), min_extra );
+    cap[t] = ( v + 3 ) & ~3;
+}
+
+template <bool MIXED>
+__device__ __forceinline__ void copy_particle( const PBuf<MIXED> &s, int64_t i, const PBuf<MIXED> &d, int64_t o,
+                                               int ndim )
+{
+    if constexpr( MIXED ) {
+        d.key[o] = s.key[i];
+        for( int k = 0; k < ndim; k++ ) d.d[k][o] = s.d[k][i];
+    } else {
+        for( int k = 0; k < ndim; k++ ) d.x[k][o] = s.x[k][i];
+    }
+    d.p[0][o] = s.p[0][i];
+    d.p[1][o] = s.p[1][i];
+    d.p[2][o] = s.p[2][i];
+    d.w[o] = s.w[i];
+}
+
+// Staged (or spilled) particle p -> next free slot of its tile in the destination buffer.
+template <bool MIXED>
+__global__ void k_place( int ndim, int64_t n, PBuf<MIXED> st, const int *__restrict__ st_tile,
+                         const int64_t *__restrict__ seg_start, int *__restrict__ fill, PBuf<MIXED> dst )
+{
+    const int64_t p = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x;
+    if( p >= n ) return;
+    const int t = st_tile[p];
+    const int slot = atomicAdd( &fill[t], 1 );
+    copy_particle<MIXED>( st, p, dst, seg_start[t] + slot, ndim );
+}
+
+// Re-layout: the live part of every old segment is copied to the new segment; fill = copied count.
+template <bool MIXED>
+__global__ void k_relayout_tiles( int ndim, int nt, const int64_t *__restrict__ old_start,
+                                  const int *__restrict__ old_cap, const int *__restrict__ count, PBuf<MIXED> src,
+                                  const int64_t *__restrict__ new_start, PBuf<MIXED> dst, int *__restrict__ fill )
+{
+    const int t = blockIdx.x;
+    if( t >= nt ) return;
+    const int n = min( count[t], old_cap[t] );
+    for( int i = threadIdx.x; i < n; i += blockDim.x )
+        copy_particle<MIXED>( src, old_start[t] + i, dst, new_start[t] + i, ndim );
+    if( threadIdx.x == 0 ) fill[t] = n;
+}
+
+// ------------------------------------------------------------------------------
+// FP64 reductions for the energy diagnostics.
+// ------------------------------------------------------------------------------
+__device__ __forceinline__ double block_sum( double v )
+{
+    __shared__ double red[32];
+#pragma unroll
+    for( int o = 16; o > 0; o >>= 1 ) v += __shfl_down_sync( 0xffffffffu, v, o );
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if( lane == 0 ) red[warp] = v;
+    __syncthreads();
+    v = threadIdx.x < ( blockDim.x >> 5 ) ? red[threadIdx.x] : 0.0;
+    if( warp == 0 ) {
+#pragma unroll
+        for( int o = 16; o > 0; o >>= 1 ) v += __shfl_down_sync( 0xffffffffu, v, o );
+    }
+    return v;
+}
+
+// sum over live particles of w * (gamma - 1) (DiagnosticScalar.cpp:505-522), one block per tile.
+template <bool MIXED>
+__global__ void k_kinetic( int nt, const int64_t *__restrict__ seg_start, const int *__restrict__ count,
+                           PBuf<MIXED> b, double *__restrict__ out )
+{
+    double acc = 0.0;
+    for( int t = blockIdx.x; t < nt; t += gridDim.x ) {
+        const int n = count[t];
+        const int64_t s0 = seg_start[t];
+        for( int i = threadIdx.x; i < n; i += blockDim.x ) {
+            const double px = b.p[0][s0 + i], py = b.p[1][s0 + i], pz = b.p[2][s0 + i];
+            acc += ( double )b.w[s0 + i] * ( sqrt( 1.0 + px * px + py * py + pz * pz ) - 1.0 );
+        }
+    }
+    acc = block_sum( acc );
+    if( threadIdx.x == 0 ) atomicAdd( out, acc );
+}
+
+// sum of F^2 over the N physical points per dimension (array index OS .. OS+N-1).
+template <class T>
+__global__ void k_norm2( GridInfo g, const T *__restrict__ a, int sx, int sy, int sz, double *__restrict__ out )
+{
+    const int e1 = ext( g, 1, sy ), e2 = ext( g, 2, sz );
+    const int n0 = g.N[0], n1 = g.N[1], n2 = g.ndim == 3 ? g.N[2] : 1;
+    const int o2 = g.ndim == 3 ? OS : 0;
+    const int64_t n = ( int64_t )n0 * n1 * n2;
+    double acc = 0.0;
+    for( int64_t t = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x; t < n; t += ( int64_t )gridDim.x * blockDim.x ) {
+        const int k = ( int )( t % n2 ), j = ( int )( ( t / n2 ) % n1 ), i = ( int )( t / ( ( int64_t )n2 * n1 ) );
+        const double v = a[( ( int64_t )( i + OS ) * e1 + ( j + OS ) ) * e2 + ( k + o2 )];
+        acc += v * v;
+    }
+    ( void )sx;
+    acc = block_sum( acc );
+    if( threadIdx.x == 0 ) atomicAdd( out, acc );
+}
+
+template <class Src, class Dst>
+__global__ void k_convert( int64_t n, const Src *__restrict__ s, Dst *__restrict__ d )
+{
+    const int64_t i = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x;
+    if( i < n ) d[i] = ( Dst )s[i];
+}
+
+// Back to absolute FP64 positions (tile-sorted order) for output.
+template <int DIM, bool MIXED>
+__global__ void k_export( GridInfo g, int nt, const int64_t *__restrict__ seg_start, const int *__restrict__ count,
+                          const int64_t *__restrict__ out_off, PBuf<MIXED> b, int64_t ntot, double *__restrict__ pos,
+                          double *__restrict__ mom, double *__restrict__ wgt )
+{
+    const int t = blockIdx.x;
+    if( t >= nt ) return;
+    const int n = count[t];
+    for( int i = threadIdx.x; i < n; i += blockDim.x ) {
+        const int64_t src = seg_start[t] + i, o = out_off[t] + i;
+        if constexpr( MIXED ) {
+            int node[3];
+            unpack_key( DIM, b.key[src], node[0], node[1], node[2] );
+            for( int d = 0; d < DIM; d++ ) {
+                double x = ( ( double )node[d] + ( double )b.d[d][src] ) * g.dx[d];
+                if( x < 0.0 ) x += g.L[d];
+                if( x >= g.L[d] ) x -= g.L[d];
+                pos[d * ntot + o] = x;
+            }
+        } else {
+            for( int d = 0; d < DIM; d++ ) pos[d * ntot + o] = b.x[d][src];
+        }
+        mom[o] = b.p[0][src];
+        mom[ntot + o] = b.p[1][src];
+        mom[2 * ntot + o] = b.p[2][src];
+        wgt[o] = b.w[src];
+    }
+}
+
+} // namespace
+} // namespace sg
+
+// ==============================================================================
+// Host side: the sg_sim object.
+// ==============================================================================
+namespace sg {
+namespace {
+
+struct SpeciesState {
+    double mass = 1.0, charge = -1.0;
+    int pusher = 0;
+    int64_t npart = 0;
+    int64_t capacity = 0;
+    void *mem[2] = { nullptr, nullptr };
+    PBuf<false> bd[2]{};
+    PBuf<true> bm[2]{};
+    int cur = 0;
+    int64_t *seg_start = nullptr;
+    int *cap = nullptr;
+    int *count[2] = { nullptr, nullptr };
+    int64_t ovf_capacity = 0;
+    void *ovf_mem = nullptr;
+    PBuf<false> od{};
+    PBuf<true> om{};
+    int *ovf_tile = nullptr;
+};
+
+// Carves a particle SoA of `n` elements out of one allocation.
+template <bool MIXED>
+size_t pbuf_bytes( int ndim, int64_t n )
+{
+    return MIXED ? ( size_t )( 1 + ndim + 4 ) * 4 * ( size_t )n + 256 * 9 : ( size_t )( ndim + 4 ) * 8 * ( size_t )n + 256 * 9;
+}
+
+inline char *align256( char *p ) { return reinterpret_cast<char *>( ( reinterpret_cast<uintptr_t>( p ) + 255 ) & ~uintptr_t( 255 ) ); }
+
+void carve( void *mem, int ndim, int64_t n, PBuf<false> &b )
+{
+    char *p = align256( static_cast<char *>( mem ) );
+    for( int d = 0; d < 3; d++ ) {
+        b.x[d] = d < ndim ? reinterpret_cast<double *>( p ) : nullptr;
+        if( d < ndim ) p = align256( p + 8 * n );
+    }
+    for( int d = 0; d < 3; d++ ) { b.p[d] = reinterpret_cast<double *>( p ); p = align256( p + 8 * n ); }
+    b.w = reinterpret_cast<double *>( p );
+}
+
+void carve( void *mem, int ndim, int64_t n, PBuf<true> &b )
+{
+    char *p = align256( static_cast<char *>( mem ) );
+    b.key = reinterpret_cast<unsigned *>( p );
+    p = align256( p + 4 * n );
+    for( int d = 0; d < 3; d++ ) {
+        b.d[d] = d < ndim ? reinterpret_cast<float *>( p ) : nullptr;
+        if( d < ndim ) p = align256( p + 4 * n );
+    }
+    for( int d = 0; d < 3; d++ ) { b.p[d] = reinterpret_cast<float *>( p ); p = align256( p + 4 * n ); }
+    b.w = reinterpret_cast<float *>( p );
+}
+
+} // namespace
+} // namespace sg
+
+using namespace sg;
+
+struct sg_sim {
+    sg_sim_config cfg{};
+    GridInfo g{};
+    bool mixed = false;
+    size_t esz = 8;
+    void *fmem = nullptr;
+    void *fptr[12] = {};
+    int64_t fsize[12] = {};
+    int fshape[12][3] = {};
+    std::vector<SpeciesState> sp;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int *d_flags = nullptr; // [0] status, [1 + s] spill count of species s
+    int *h_flags = nullptr; // pinned copy
+    int max_species = 16;
+    int64_t *scan_scratch = nullptr;
+    int64_t *tmp_start = nullptr;
+    int *tmp_cap = nullptr;
+    int *fill = nullptr;
+    double *d_red = nullptr;
+    cudaGraphExec_t graph[2] = { nullptr, nullptr };
+    int graph_parity = -1; // parity of species 0 that graph[0] starts from
+    cudaEvent_t ev[4] = { nullptr, nullptr, nullptr, nullptr }; // step start, particles start/end, step end
+    float last_ms[3] = { 0, 0, 0 };
+    int launches_per_step = 0;
+    size_t smem_bytes = 0;
+};
+
+namespace sg {
+namespace {
+
+template <class T>
+Fields<T> field_view( sg_sim *S )
+{
+    Fields<T> f;
+    for( int c = 0; c < 3; c++ ) {
+        f.E[c] = static_cast<T *>( S->fptr[c] );
+        f.B[c] = static_cast<T *>( S->fptr[3 + c] );
+        f.Bm[c] = static_cast<T *>( S->fptr[6 + c] );
+        f.J[c] = static_cast<T *>( S->fptr[9 + c] );
+    }
+    return f;
+}
+
+// comp 0..2 E, 3..5 B, 6..8 B_m, 9..11 J -> staggering flags
+inline int comp_stag( int comp, int d ) { return comp < 3 ? stag( comp, d ) : ( comp < 9 ? stag( 3 + ( comp % 3 ), d ) : stag( comp - 9, d ) ); }
+
+template <int DIM, bool MIXED, int KIND>
+int launch_particles( sg_sim *S, SpeciesState &s, cudaStream_t st )
+{
+    using T = typename std::conditional<MIXED, float, double>::type;
+    const int in = s.cur, out = 1 - s.cur;
+    PBuf<MIXED> bin, bout, bov;
+    if constexpr( MIXED ) { bin = s.bm[in]; bout = s.bm[out]; bov = s.om; }
+    else { bin = s.bd[in]; bout = s.bd[out]; bov = s.od; }
+    SpecParams sp;
+    sp.charge = s.charge;
+    sp.mass = s.mass;
+    sp.qm_dts2 = s.charge / s.mass * S->g.dt * 0.5;
+    double vol = 1.0;
+    for( int d = 0; d < S->g.ndim; d++ ) vol *= S->g.dx[d];
+    sp.cw = s.charge / vol;
+    auto kern = k_step_particles<DIM, MIXED, KIND>;
+    if( S->smem_bytes > 48 * 1024 ) SG_CUDA_TRY( cudaFuncSetAttribute( kern, cudaFuncAttributeMaxDynamicSharedMemorySize, ( int )S->smem_bytes ) );
+    const int sidx = ( int )( &s - &S->sp[0] );
+    kern<<<S->g.ntiles, 128, S->smem_bytes, st>>>( S->g, field_view<T>( S ), sp, bin, bout, s.seg_start, s.cap, s.count[in],
+                                                   s.count[out], bov, s.ovf_tile, S->d_flags + 1 + sidx,
+                                                   ( int )s.ovf_capacity, S->d_flags );
+    SG_LAUNCH_CHECK( "k_step_particles" );
+    return SG_OK;
+}
+
+template <int DIM, bool MIXED>
+int launch_particles_kind( sg_sim *S, SpeciesState &s, cudaStream_t st )
+{
+    if( s.pusher == 0 ) return launch_particles<DIM, MIXED, 0>( S, s, st );
+    if( s.pusher == 1 ) return launch_particles<DIM, MIXED, 1>( S, s, st );
+    return launch_particles<DIM, MIXED, 2>( S, s, st );
+}
+
+int launch_particles_any( sg_sim *S, SpeciesState &s, cudaStream_t st )
+{
+    if( S->g.ndim == 3 ) return S->mixed ? launch_particles_kind<3, true>( S, s, st ) : launch_particles_kind<3, false>( S, s, st );
+    return S->mixed ? launch_particles_kind<2, true>( S, s, st ) : launch_particles_kind<2, false>( S, s, st );
+}
+
+template <int DIM, class T>
+int launch_fields( sg_sim *S, cudaStream_t st, int &launches )
+{
+    Fields<T> f = field_view<T>( S );
+    const GridInfo &g = S->g;
+    for( int d = 0; d < DIM; d++ ) {
+        int64_t slab = 6;
+        for( int k = 0; k < DIM; k++ )
+            if( k != d ) slab *= g.np[k] + 1;
+        dim3 grid( ( unsigned )std::min<int64_t>( ( slab + 255 ) / 256, 4096 ), 3 );
+        k_fold<T><<<grid, 256, 0, st>>>( g, d, f );
+        SG_LAUNCH_CHECK( "k_fold" );
+        launches++;
+    }
+    const T dt = T( g.dt ), dtdx = T( g.dt / g.dx[0] ), dtdy = T( g.dt / g.dx[1] ), dtdz = T( DIM == 3 ? g.dt / g.dx[2] : 0.0 );
+    const unsigned rows = DIM == 3 ? ( unsigned )( ( g.np[0] + 1 ) * ( g.np[1] + 1 ) ) : ( unsigned )( g.np[0] + 1 );
+    const int tpb = DIM == 3 ? ( g.np[2] + 1 <= 128 ? 128 : 256 ) : 256;
+    k_ampere_all<DIM, T><<<rows, tpb, 0, st>>>( g, f, dt, dtdx, dtdy, dtdz );
+    SG_LAUNCH_CHECK( "k_ampere_all" );
+    k_faraday_center<DIM, T><<<rows, tpb, 0, st>>>( g, f, dtdx, dtdy, dtdz );
+    SG_LAUNCH_CHECK( "k_faraday_center" );
+    launches += 2;
+    return SG_OK;
+}
+
+// Enqueues one full timestep on `st` (no host synchronisation).
+int enqueue_step( sg_sim *S, cudaStream_t st )
+{
+    int launches = 0;
+    SG_CUDA_TRY( cudaEventRecord( S->ev[3], st ) );
+    for( int c = 9; c < 12; c++ ) SG_CUDA_TRY( cudaMemsetAsync( S->fptr[c], 0, S->fsize[c] * S->esz, st ) );
+    SG_CUDA_TRY( cudaMemsetAsync( S->d_flags, 0, ( 1 + S->sp.size() ) * sizeof( int ), st ) );
+    for( auto &s : S->sp ) SG_CUDA_TRY( cudaMemsetAsync( s.count[1 - s.cur], 0, S->g.ntiles * sizeof( int ), st ) );
+    SG_CUDA_TRY( cudaEventRecord( S->ev[0], st ) );
+    for( auto &s : S->sp ) {
+        int r = launch_particles_any( S, s, st );
+        if( r ) return r;
+        launches++;
+    }
+    SG_CUDA_TRY( cudaEventRecord( S->ev[1], st ) );
+    int r;
+    if( S->g.ndim == 3 ) r = S->mixed ? launch_fields<3, float>( S, st, launches ) : launch_fields<3, double>( S, st, launches );
+    else r = S->mixed ? launch_fields<2, float>( S, st, launches ) : launch_fields<2, double>( S, st, launches );
+    if( r ) return r;
+    SG_CUDA_TRY( cudaEventRecord( S->ev[2], st ) );
+    SG_CUDA_TRY( cudaMemcpyAsync( S->h_flags, S->d_flags, ( 1 + S->sp.size() ) * sizeof( int ), cudaMemcpyDeviceToHost, st ) );
+    S->launches_per_step = launches;
+    return SG_OK;
+}
+
+void drop_graphs( sg_sim *S )
+{
+    for( int i = 0; i < 2; i++ ) {
+        if( S->graph[i] ) cudaGraphExecDestroy( S->graph[i] );
+        S->graph[i] = nullptr;
+    }
+    S->graph_parity = -1;
+}
+
+int capture( sg_sim *S, cudaGraphExec_t *out )
+{
+    cudaGraph_t graph = nullptr;
+    SG_CUDA_TRY( cudaStreamBeginCapture( S->stream, cudaStreamCaptureModeThreadLocal ) );
+    int r = enqueue_step( S, S->stream );
+    cudaError_t e = cudaStreamEndCapture( S->stream, &graph );
+    if( r ) {
+        if( graph ) cudaGraphDestroy( graph );
+        return r;
+    }
+    if( e != cudaSuccess ) return cuda_fail( e, "cudaStreamEndCapture", __FILE__, __LINE__ );
+    e = cudaGraphInstantiate( out, graph, 0 );
+    cudaGraphDestroy( graph );
+    if( e != cudaSuccess ) return cuda_fail( e, "cudaGraphInstantiate", __FILE__, __LINE__ );
+    return SG_OK;
+}
+
+int alloc_species_buffers( sg_sim *S, SpeciesState &s, int64_t capacity )
+{
+    const int nd = S->g.ndim;
+    const size_t bytes = S->mixed ? pbuf_bytes<true>( nd, capacity ) : pbuf_bytes<false>( nd, capacity );
+    for( int b = 0; b < 2; b++ ) {
+        void *m = nullptr;
+        cudaError_t e = cudaMalloc( &m, bytes );
+        if( e != cudaSuccess ) return set_error( SG_ERR_NOMEM, "cannot allocate %zu bytes of particle buffer", bytes );
+        s.mem[b] = m;
+        if( S->mixed ) carve( m, nd, capacity, s.bm[b] );
+        else carve( m, nd, capacity, s.bd[b] );
+    }
+    s.capacity = capacity;
+    return SG_OK;
+}
+
+// New segment layout from counts: cap, seg_start into (new_cap, new_start); returns the total.
+int layout_from_counts( sg_sim *S, const int *count, int *new_cap, int64_t *new_start, int64_t *total )
+{
+    const int nt = S->g.ntiles;
+    const float slack = ( float )( S->cfg.capacity_slack > 0.0 ? S->cfg.capacity_slack : 0.25 );
+    // room beyond the slack fraction: 16 particles at the default slack of 0.25, less when the slack is smaller
+    const int min_extra = ( int )std::ceil( 16.0 * std::min( 1.0, slack / 0.25 ) );
+    k_caps<<<grid_for( nt, 256 ), 256, 0, S->stream>>>( nt, count, new_cap, slack, min_extra );
+    SG_LAUNCH_CHECK( "k_caps" );
+    int r = exclusive_scan<int>( new_cap, nt, new_start, S->scan_scratch, S->stream );
+    if( r ) return r;
+    int64_t last_start = 0;
+    int last_cap = 0;
+    SG_CUDA_TRY( cudaMemcpyAsync( &last_start, new_start + nt - 1, sizeof( int64_t ), cudaMemcpyDeviceToHost, S->stream ) );
+    SG_CUDA_TRY( cudaMemcpyAsync( &last_cap, new_cap + nt - 1, sizeof( int ), cudaMemcpyDeviceToHost, S->stream ) );
+    SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
+    *total = last_start + last_cap;
+    return SG_OK;
+}
+
+template <bool MIXED>
+int place_staged( sg_sim *S, SpeciesState &s, int64_t n, PBuf<MIXED> st, const int *st_tile, int dst_buf )
+{
+    if( n == 0 ) return SG_OK;
+    PBuf<MIXED> dst;
+    if constexpr( MIXED ) dst = s.bm[dst_buf];
+    else dst = s.bd[dst_buf];
+    k_place<MIXED><<<grid_for( n, 256 ), 256, 0, S->stream>>>( S->g.ndim, n, st, st_tile, s.seg_start, S->fill, dst );
+    SG_LAUNCH_CHECK( "k_place" );
+    return SG_OK;
+}
+
+// Re-lays species s out after a spill: counts come from the step just done.
+int relayout( sg_sim *S, SpeciesState &s, int nspill )
+{
+    const int nt = S->g.ntiles;
+    int64_t total = 0;
+    int r = layout_from_counts( S, s.count[s.cur], S->tmp_cap, S->tmp_start, &total );
+    if( r ) return r;
+    // destination: the idle buffer, or fresh buffers when the layout no longer fits
+    void *old_mem[2] = { s.mem[0], s.mem[1] };
+    PBuf<false> old_bd = s.bd[s.cur];
+    PBuf<true> old_bm = s.bm[s.cur];
+    int dst_buf = 1 - s.cur;
+    bool realloc = total > s.capacity;
+    if( realloc ) {
+        r = alloc_species_buffers( S, s, total + total / 8 );
+        if( r ) return r;
+        dst_buf = s.cur;
+    }
+    if( S->mixed )
+        k_relayout_tiles<true><<<nt, 128, 0, S->stream>>>( S->g.ndim, nt, s.seg_start, s.cap, s.count[s.cur], old_bm, S->tmp_start, s.bm[dst_buf], S->fill );
+    else
+        k_relayout_tiles<false><<<nt, 128, 0, S->stream>>>( S->g.ndim, nt, s.seg_start, s.cap, s.count[s.cur], old_bd, S->tmp_start, s.bd[dst_buf], S->fill );
+    SG_LAUNCH_CHECK( "k_relayout_tiles" );
+    // new layout becomes current
+    std::swap( s.seg_start, S->tmp_start );
+    std::swap( s.cap, S->tmp_cap );
+    if( S->mixed ) r = place_staged<true>( S, s, nspill, s.om, s.ovf_tile, dst_buf );
+    else r = place_staged<false>( S, s, nspill, s.od, s.ovf_tile, dst_buf );
+    if( r ) return r;
+    SG_CUDA_TRY( cudaMemcpyAsync( s.count[dst_buf], s.count[s.cur], nt * sizeof( int ), cudaMemcpyDeviceToDevice, S->stream ) );
+    SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
+    if( realloc ) {
+        cudaFree( old_mem[0] );
+        cudaFree( old_mem[1] );
+    }
+    s.cur = dst_buf;
+    drop_graphs( S );
+    return SG_OK;
+}
+
+int choose_tiles( sg_sim *S )
+{
+    GridInfo &g = S->g;
+    for( int d = 0; d < 3; d++ ) {
+        if( d >= g.ndim ) { g.T[d] = 1; g.nt[d] = 1; continue; }
+        int t = S->cfg.tile[d];
+        if( t <= 0 ) {
+            const int pref = g.ndim == 3 ? 4 : 8;
+            t = pref;
+            while( t > 1 && g.N[d] % t ) t--;
+        }
+        if( g.N[d] % t ) return set_error( SG_ERR_ARG, "tile size %d does not divide %d cells in dimension %d", t, g.N[d], d );
+        g.T[d] = t;
+        g.nt[d] = g.N[d] / t;
+    }
+    g.ntiles = g.nt[0] * g.nt[1] * ( g.ndim == 3 ? g.nt[2] : 1 );
+    const TileDims td = tile_dims( g );
+    S->smem_bytes = ( size_t )( 6 * td.FX * td.FY * td.FZ + 3 * td.JX * td.JY * td.JZ ) * S->esz;
+    if( S->smem_bytes > 200 * 1024 ) return set_error( SG_ERR_ARG, "tile too large for shared memory (%zu bytes)", S->smem_bytes );
+    return SG_OK;
+}
+
+} // namespace
+} // namespace sg
+
+extern "C" {
+
+int sg_sim_create( const sg_sim_config *cfg, sg_sim **out )
+{
+    SG_REQUIRE( cfg && out, "NULL argument" );
+    SG_REQUIRE( cfg->ndim == 2 || cfg->ndim == 3, "ndim must be 2 or 3" );
+    SG_REQUIRE( cfg->form == SG_FORM_FP64 || cfg->form == SG_FORM_MIXED, "unknown form %d", cfg->form );
+    SG_REQUIRE( cfg->dt > 0.0, "dt must be positive" );
+    for( int d = 0; d < cfg->ndim; d++ ) {
+        SG_REQUIRE( cfg->n_cells[d] >= 8, "at least 8 cells per dimension are needed (dimension %d has %d)", d, cfg->n_cells[d] );
+        SG_REQUIRE( cfg->cell_length[d] > 0.0, "cell_length[%d] must be positive", d );
+        if( cfg->form == SG_FORM_MIXED )
+            SG_REQUIRE( cfg->n_cells[d] <= ( cfg->ndim == 3 ? ( d == 0 ? 2048 : 1024 ) : 65536 ), "mixed form: too many cells in dimension %d", d );
+        SG_REQUIRE( cfg->dt < cfg->cell_length[d], "dt must be below every cell length (a particle may cross at most one cell per step)" );
+    }
+    sg_sim *S = new sg_sim();
+    S->cfg = *cfg;
+    S->mixed = cfg->form == SG_FORM_MIXED;
+    S->esz = S->mixed ? 4 : 8;
+    GridInfo &g = S->g;
+    g.ndim = cfg->ndim;
+    g.dt = cfg->dt;
+    for( int d = 0; d < 3; d++ ) {
+        g.N[d] = d < g.ndim ? cfg->n_cells[d] : 1;
+        g.np[d] = d < g.ndim ? g.N[d] + 1 + 2 * OS : 1;
+        g.dx[d] = d < g.ndim ? cfg->cell_length[d] : 1.0;
+        g.dxi[d] = 1.0 / g.dx[d];
+        g.L[d] = g.N[d] * g.dx[d];
+    }
+    int r = choose_tiles( S );
+    if( r ) { delete S; return r; }
+    // fields
+    size_t total = 0;
+    for( int c = 0; c < 12; c++ ) {
+        int64_t n = 1;
+        for( int d = 0; d < 3; d++ ) {
+            S->fshape[c][d] = ext( g, d, comp_stag( c, d ) );
+            n *= S->fshape[c][d];
+        }
+        S->fsize[c] = n;
+        total += ( ( n * S->esz + 255 ) / 256 ) * 256;
+    }
+    cudaError_t e = cudaMalloc( &S->fmem, total );
+    if( e != cudaSuccess ) { delete S; return set_error( SG_ERR_NOMEM, "cannot allocate %zu bytes of fields", total ); }
+    cudaMemset( S->fmem, 0, total );
+    char *p = static_cast<char *>( S->fmem );
+    for( int c = 0; c < 12; c++ ) {
+        S->fptr[c] = p;
+        p += ( ( S->fsize[c] * S->esz + 255 ) / 256 ) * 256;
+    }
+    const int nt = g.ntiles;
+    e = cudaMalloc( &S->d_flags, ( 1 + S->max_species ) * sizeof( int ) );
+    if( e == cudaSuccess ) e = cudaMallocHost( &S->h_flags, ( 1 + S->max_species ) * sizeof( int ) );
+    if( e == cudaSuccess ) e = cudaMalloc( &S->scan_scratch, scan_scratch_elems( nt ) * sizeof( int64_t ) );
+    if( e == cudaSuccess ) e = cudaMalloc( &S->tmp_start, nt * sizeof( int64_t ) );
+    if( e == cudaSuccess ) e = cudaMalloc( &S->tmp_cap, nt * sizeof( int ) );
+    if( e == cudaSuccess ) e = cudaMalloc( &S->fill, nt * sizeof( int ) );
+    if( e == cudaSuccess ) e = cudaMalloc( &S->d_red, 16 * sizeof( double ) );
+    if( e == cudaSuccess ) e = cudaStreamCreateWithFlags( &S->stream, cudaStreamNonBlocking );
+    for( int i = 0; i < 4 && e == cudaSuccess; i++ ) e = cudaEventCreate( &S->ev[i] );
+    if( e != cudaSuccess ) {
+        sg_sim_destroy( S );
+        return cuda_fail( e, "sg_sim_create allocations", __FILE__, __LINE__ );
+    }
+    S->own_stream = true;
+    *out = S;
+    return SG_OK;
+}
+
+int sg_sim_destroy( sg_sim *S )
+{
+    if( !S ) return SG_OK;
+    if( S->stream ) cudaStreamSynchronize( S->stream );
+    drop_graphs( S );
+    for( auto &s : S->sp ) {
+        cudaFree( s.mem[0] );
+        cudaFree( s.mem[1] );
+        cudaFree( s.seg_start );
+        cudaFree( s.cap );
+        cudaFree( s.count[0] );
+        cudaFree( s.count[1] );
+        cudaFree( s.ovf_mem );
+        cudaFree( s.ovf_tile );
+    }
+    cudaFree( S->fmem );
+    cudaFree( S->d_flags );
+    if( S->h_flags ) cudaFreeHost( S->h_flags );
+    cudaFree( S->scan_scratch );
+    cudaFree( S->tmp_start );
+    cudaFree( S->tmp_cap );
+    cudaFree( S->fill );
+    cudaFree( S->d_red );
+    for( int i = 0; i < 4; i++ )
+        if( S->ev[i] ) cudaEventDestroy( S->ev[i] );
+    if( S->own_stream && S->stream ) cudaStreamDestroy( S->stream );
+    delete S;
+    return SG_OK;
+}
+
+int sg_sim_set_stream( sg_sim *S, sg_stream_t stream )
+{
+    SG_REQUIRE( S, "NULL simulation" );
+    SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
+    if( S->own_stream ) cudaStreamDestroy( S->stream );
+    S->stream = as_stream( stream );
+    S->own_stream = false;
+    drop_graphs( S );
+    return SG_OK;
+}
+
+int sg_sim_add_species_device( sg_sim *S, double mass, double charge, int pusher, int64_t npart, const double *pos,
+                               const double *mom, const double *weight, int *index )
+{
+    SG_REQUIRE( S, "NULL simulation" );
+    SG_REQUIRE( mass > 0.0, "mass must be positive" );
+    SG_REQUIRE( pusher >= 0 && pusher <= 2, "pusher must be 0 (boris), 1 (vay) or 2 (higueracary)" );
+    SG_REQUIRE( npart >= 0 && npart < ( int64_t )1 << 31, "npart out of range" );
+    SG_REQUIRE( ( int )S->sp.size() < S->max_species, "too many species" );
+    if( npart > 0 ) SG_REQUIRE( pos && mom && weight, "NULL particle array" );
+    const int nt = S->g.ntiles, nd = S->g.ndim;
+    S->sp.emplace_back();
+    SpeciesState &s = S->sp.back();
+    s.mass = mass;
+    s.charge = charge;
+    s.pusher = pusher;
+    s.npart = npart;
+    cudaStream_t st = S->stream;
+    SG_CUDA_TRY( cudaMalloc( &s.seg_start, nt * sizeof( int64_t ) ) );
+    SG_CUDA_TRY( cudaMalloc( &s.cap, nt * sizeof( int ) ) );
+    SG_CUDA_TRY( cudaMalloc( &s.count[0], nt * sizeof( int ) ) );
+    SG_CUDA_TRY( cudaMalloc( &s.count[1], nt * sizeof( int ) ) );
+    SG_CUDA_TRY( cudaMemsetAsync( s.count[0], 0, nt * sizeof( int ), st ) );
+    SG_CUDA_TRY( cudaMemsetAsync( s.count[1], 0, nt * sizeof( int ), st ) );
+    // spill list (also used as the staging area here)
+    s.ovf_capacity = std::max<int64_t>( npart, std::max<int64_t>( 4096, npart / 16 ) );
+    const size_t obytes = S->mixed ? pbuf_bytes<true>( nd, s.ovf_capacity ) : pbuf_bytes<false>( nd, s.ovf_capacity );
+    SG_CUDA_TRY( cudaMalloc( &s.ovf_mem, obytes ) );
+    SG_CUDA_TRY( cudaMalloc( &s.ovf_tile, s.ovf_capacity * sizeof( int ) ) );
+    if( S->mixed ) carve( s.ovf_mem, nd, s.ovf_capacity, s.om );
+    else carve( s.ovf_mem, nd, s.ovf_capacity, s.od );
+    if( npart > 0 ) {
+        if( nd == 3 ) {
+            if( S->mixed ) k_stage<3, true><<<grid_for( npart, 256 ), 256, 0, st>>>( S->g, npart, pos, mom, weight, s.om, s.ovf_tile, s.count[1] );
+            else k_stage<3, false><<<grid_for( npart, 256 ), 256, 0, st>>>( S->g, npart, pos, mom, weight, s.od, s.ovf_tile, s.count[1] );
+        } else {
+            if( S->mixed ) k_stage<2, true><<<grid_for( npart, 256 ), 256, 0, st>>>( S->g, npart, pos, mom, weight, s.om, s.ovf_tile, s.count[1] );
+            else k_stage<2, false><<<grid_for( npart, 256 ), 256, 0, st>>>( S->g, npart, pos, mom, weight, s.od, s.ovf_tile, s.count[1] );
+        }
+        SG_LAUNCH_CHECK( "k_stage" );
+    }
+    int64_t total = 0;
+    int r = layout_from_counts( S, s.count[1], s.cap, s.seg_start, &total );
+    if( r ) return r;
+    r = alloc_species_buffers( S, s, std::max<int64_t>( total, 1 ) );
+    if( r ) return r;
+    SG_CUDA_TRY( cudaMemsetAsync( S->fill, 0, nt * sizeof( int ), st ) );
+    if( S->mixed ) r = place_staged<true>( S, s, npart, s.om, s.ovf_tile, 0 );
+    else r = place_staged<false>( S, s, npart, s.od, s.ovf_tile, 0 );
+    if( r ) return r;
+    SG_CUDA_TRY( cudaMemcpyAsync( s.count[0], S->fill, nt * sizeof( int ), cudaMemcpyDeviceToDevice, st ) );
+    SG_CUDA_TRY( cudaStreamSynchronize( st ) );
+    // the spill list only needs a fraction of the species once placed
+    const int64_t spill_cap = std::max<int64_t>( 4096, npart / 16 );
+    if( spill_cap < s.ovf_capacity ) {
+        cudaFree( s.ovf_mem );
+        cudaFree( s.ovf_tile );
+        s.ovf_mem = nullptr;
+        s.ovf_tile = nullptr;
+        s.ovf_capacity = spill_cap;
+        const size_t sbytes = S->mixed ? pbuf_bytes<true>( nd, spill_cap ) : pbuf_bytes<false>( nd, spill_cap );
+        SG_CUDA_TRY( cudaMalloc( &s.ovf_mem, sbytes ) );
+        SG_CUDA_TRY( cudaMalloc( &s.ovf_tile, spill_cap * sizeof( int ) ) );
+        if( S->mixed ) carve( s.ovf_mem, nd, spill_cap, s.om );
+        else carve( s.ovf_mem, nd, spill_cap, s.od );
+    }
+    s.cur = S->sp.size() > 1 ? S->sp[0].cur : 0;
+    if( s.cur != 0 ) {
+        // keep every species on the same buffer parity: move the data to buffer 1
+        const size_t bytes = S->mixed ? pbuf_bytes<true>( nd, s.capacity ) : pbuf_bytes<false>( nd, s.capacity );
+        SG_CUDA_TRY( cudaMemcpyAsync( s.mem[1], s.mem[0], bytes, cudaMemcpyDeviceToDevice, st ) );
+        SG_CUDA_TRY( cudaMemcpyAsync( s.count[1], s.count[0], nt * sizeof( int ), cudaMemcpyDeviceToDevice, st ) );
+        SG_CUDA_TRY( cudaStreamSynchronize( st ) );
+    }
+    drop_graphs( S );
+    if( index ) *index = ( int )S->sp.size() - 1;
+    return SG_OK;
+}
+
+int sg_sim_add_species( sg_sim *S, double mass, double charge, int pusher, int64_t npart, const double *pos,
+                        const double *mom, const double *weight, int *index )
+{
+    SG_REQUIRE( S, "NULL simulation" );
+    SG_REQUIRE( npart >= 0, "npart < 0" );
+    const int nd = S->g.ndim;
+    double *d = nullptr;
+    const size_t bytes = ( size_t )( nd + 4 ) * ( size_t )std::max<int64_t>( npart, 1 ) * 8;
+    SG_CUDA_TRY( cudaMalloc( &d, bytes ) );
+    if( npart > 0 ) {
+        SG_CUDA_TRY( cudaMemcpy( d, pos, nd * npart * 8, cudaMemcpyHostToDevice ) );
+        SG_CUDA_TRY( cudaMemcpy( d + nd * npart, mom, 3 * npart * 8, cudaMemcpyHostToDevice ) );
+        SG_CUDA_TRY( cudaMemcpy( d + ( nd + 3 ) * npart, weight, npart * 8, cudaMemcpyHostToDevice ) );
+    }
+    int r = sg_sim_add_species_device( S, mass, charge, pusher, npart, d, d + nd * npart, d + ( nd + 3 ) * npart, index );
+    cudaFree( d );
+    return r;
+}
+
+int sg_sim_field_shape( sg_sim *S, int comp, int *shape3 )
+{
+    SG_REQUIRE( S && shape3, "NULL argument" );
+    SG_REQUIRE( comp >= 0 && comp < 12, "component out of range" );
+    for( int d = 0; d < 3; d++ ) shape3[d] = S->fshape[comp][d];
+    return SG_OK;
+}
+
+int sg_sim_set_field( sg_sim *S, int comp, const double *host )
+{
+    SG_REQUIRE( S && host, "NULL argument" );
+    SG_REQUIRE( comp >= 0 && comp < 12, "component out of range" );
+    const int64_t n = S->fsize[comp];
+    SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
+    if( !S->mixed ) {
+        SG_CUDA_TRY( cudaMemcpy( S->fptr[comp], host, n * 8, cudaMemcpyHostToDevice ) );
+    } else {
+        double *d = nullptr;
+        SG_CUDA_TRY( cudaMalloc( &d, n * 8 ) );
+        SG_CUDA_TRY( cudaMemcpy( d, host, n * 8, cudaMemcpyHostToDevice ) );
+        k_convert<double, float><<<grid_for( n, 256 ), 256, 0, S->stream>>>( n, d, static_cast<float *>( S->fptr[comp] ) );
+        SG_LAUNCH_CHECK( "k_convert" );
+        SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
+        cudaFree( d );
+    }
+    return SG_OK;
+}
+
+int sg_sim_get_field( sg_sim *S, int comp, double *host )
+{
+    SG_REQUIRE( S && host, "NULL argument" );
+    SG_REQUIRE( comp >= 0 && comp < 12, "component out of range" );
+    const int64_t n = S->fsize[comp];
+    SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
+    if( !S->mixed ) {
+        SG_CUDA_TRY( cudaMemcpy( host, S->fptr[comp], n * 8, cudaMemcpyDeviceToHost ) );
+    } else {
+        double *d = nullptr;
+        SG_CUDA_TRY( cudaMalloc( &d, n * 8 ) );
+        k_convert<float, double><<<grid_for( n, 256 ), 256, 0, S->stream>>>( n, static_cast<float *>( S->fptr[comp] ), d );
+        SG_LAUNCH_CHECK( "k_convert" );
+        SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
+        SG_CUDA_TRY( cudaMemcpy( host, d, n * 8, cudaMemcpyDeviceToHost ) );
+        cudaFree( d );
+    }
+    return SG_OK;
+}
+
+int sg_sim_step( sg_sim *S, int nsteps )
+{
+    SG_REQUIRE( S, "NULL simulation" );
+    SG_REQUIRE( nsteps >= 0, "nsteps < 0" );
+    for( int it = 0; it < nsteps; it++ ) {
+        const int parity = S->sp.empty() ? 0 : S->sp[0].cur;
+        if( S->cfg.use_graph ) {
+            if( S->graph_parity < 0 ) {
+                // capture both parities: the step from the current state and the one after it
+                int r = capture( S, &S->graph[0] );
+                if( r ) return r;
+                for( auto &s : S->sp ) s.cur = 1 - s.cur;
+                r = capture( S, &S->graph[1] );
+                for( auto &s : S->sp ) s.cur = 1 - s.cur;
+                if( r ) return r;
+                S->graph_parity = parity;
+            }
+            SG_CUDA_TRY( cudaGraphLaunch( S->graph[parity == S->graph_parity ? 0 : 1], S->stream ) );
+        } else {
+            int r = enqueue_step( S, S->stream );
+            if( r ) return r;
+        }
+        SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
+        for( auto &s : S->sp ) s.cur = 1 - s.cur;
+        const int status = S->h_flags[0];
+        cudaEventElapsedTime( &S->last_ms[0], S->ev[0], S->ev[1] );
+        cudaEventElapsedTime( &S->last_ms[1], S->ev[1], S->ev[2] );
+        cudaEventElapsedTime( &S->last_ms[2], S->ev[3], S->ev[2] );
+        if( status ) {
+            return set_error( status, status == SG_ERR_BOUNDS ? "a particle moved more than one cell in a step or left its tile"
+                                                              : "the spill list overflowed (capacity too small)" );
+        }
+        for( size_t k = 0; k < S->sp.size(); k++ ) {
+            const int nspill = S->h_flags[1 + k];
+            if( nspill > 0 ) {
+                int r = relayout( S, S->sp[k], nspill );
+                if( r ) return r;
+            }
+        }
+    }
+    return SG_OK;
+}
+
+int sg_sim_last_timing( sg_sim *S, double *ms_particles, double *ms_fields, double *ms_total, int *launches_per_step )
+{
+    SG_REQUIRE( S, "NULL simulation" );
+    if( ms_particles ) *ms_particles = S->last_ms[0];
+    if( ms_fields ) *ms_fields = S->last_ms[1];
+    if( ms_total ) *ms_total = S->last_ms[2];
+    if( launches_per_step ) *launches_per_step = S->launches_per_step;
+    return SG_OK;
+}
+
+int sg_sim_species_count( sg_sim *S, int species, int64_t *npart )
+{
+    SG_REQUIRE( S && npart, "NULL argument" );
+    SG_REQUIRE( species >= 0 && species < ( int )S->sp.size(), "no species %d", species );
+    SpeciesState &s = S->sp[species];
+    const int nt = S->g.ntiles;
+    std::vector<int> c( nt );
+    SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
+    SG_CUDA_TRY( cudaMemcpy( c.data(), s.count[s.cur], nt * sizeof( int ), cudaMemcpyDeviceToHost ) );
+    int64_t n = 0;
+    for( int v : c ) n += v;
+    *npart = n;
+    return SG_OK;
+}
+
+int sg_sim_get_species( sg_sim *S, int species, double *pos, double *mom, double *weight )
+{
+    SG_REQUIRE( S && pos && mom && weight, "NULL argument" );
+    SG_REQUIRE( species >= 0 && species < ( int )S->sp.size(), "no species %d", species );
+    SpeciesState &s = S->sp[species];
+    const int nt = S->g.ntiles, nd = S->g.ndim;
+    int64_t n = 0;
+    int r = sg_sim_species_count( S, species, &n );
+    if( r ) return r;
+    int64_t *off = nullptr;
+    double *d = nullptr;
+    SG_CUDA_TRY( cudaMalloc( &off, nt * sizeof( int64_t ) ) );
+    SG_CUDA_TRY( cudaMalloc( &d, ( size_t )( nd + 4 ) * std::max<int64_t>( n, 1 ) * 8 ) );
+    r = exclusive_scan<int>( s.count[s.cur], nt, off, S->scan_scratch, S->stream );
+    if( r ) return r;
+    if( nd == 3 ) {
+        if( S->mixed ) k_export<3, true><<<nt, 128, 0, S->stream>>>( S->g, nt, s.seg_start, s.count[s.cur], off, s.bm[s.cur], n, d, d + nd * n, d + ( nd + 3 ) * n );
+        else k_export<3, false><<<nt, 128, 0, S->stream>>>( S->g, nt, s.seg_start, s.count[s.cur], off, s.bd[s.cur], n, d, d + nd * n, d + ( nd + 3 ) * n );
+    } else {
+        if( S->mixed ) k_export<2, true><<<nt, 128, 0, S->stream>>>( S->g, nt, s.seg_start, s.count[s.cur], off, s.bm[s.cur], n, d, d + nd * n, d + ( nd + 3 ) * n );
+        else k_export<2, false><<<nt, 128, 0, S->stream>>>( S->g, nt, s.seg_start, s.count[s.cur], off, s.bd[s.cur], n, d, d + nd * n, d + ( nd + 3 ) * n );
+    }
+    SG_LAUNCH_CHECK( "k_export" );
+    SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
+    SG_CUDA_TRY( cudaMemcpy( pos, d, nd * n * 8, cudaMemcpyDeviceToHost ) );
+    SG_CUDA_TRY( cudaMemcpy( mom, d + nd * n, 3 * n * 8, cudaMemcpyDeviceToHost ) );
+    SG_CUDA_TRY( cudaMemcpy( weight, d + ( nd + 3 ) * n, n * 8, cudaMemcpyDeviceToHost ) );
+    cudaFree( off );
+    cudaFree( d );
+    return SG_OK;
+}
+
+int sg_sim_state_bytes( sg_sim *S, int species, size_t *bytes )
+{
+    SG_REQUIRE( S && bytes, "NULL argument" );
+    SG_REQUIRE( species >= 0 && species < ( int )S->sp.size(), "no species %d", species );
+    const SpeciesState &s = S->sp[species];
+    *bytes = S->mixed ? pbuf_bytes<true>( S->g.ndim, s.capacity ) : pbuf_bytes<false>( S->g.ndim, s.capacity );
+    return SG_OK;
+}
+
+int sg_sim_copy_state( sg_sim *S, int species, void *host, int to_device )
+{
+    SG_REQUIRE( S && host, "NULL argument" );
+    SG_REQUIRE( species >= 0 && species < ( int )S->sp.size(), "no species %d", species );
+    SpeciesState &s = S->sp[species];
+    size_t bytes = 0;
+    sg_sim_state_bytes( S, species, &bytes );
+    if( to_device ) SG_CUDA_TRY( cudaMemcpyAsync( s.mem[s.cur], host, bytes, cudaMemcpyHostToDevice, S->stream ) );
+    else SG_CUDA_TRY( cudaMemcpyAsync( host, s.mem[s.cur], bytes, cudaMemcpyDeviceToHost, S->stream ) );
+    return SG_OK;
+}
+
+int sg_sim_energy( sg_sim *S, double *ukin, double *uelm )
+{
+    SG_REQUIRE( S, "NULL simulation" );
+    cudaStream_t st = S->stream;
+    SG_CUDA_TRY( cudaMemsetAsync( S->d_red, 0, 16 * sizeof( double ), st ) );
+    const int nt = S->g.ntiles;
+    for( size_t k = 0; k < S->sp.size(); k++ ) {
+        SpeciesState &s = S->sp[k];
+        if( S->mixed ) k_kinetic<true><<<std::min( nt, 1216 ), 256, 0, st>>>( nt, s.seg_start, s.count[s.cur], s.bm[s.cur], S->d_red + 2 + k % 14 );
+        else k_kinetic<false><<<std::min( nt, 1216 ), 256, 0, st>>>( nt, s.seg_start, s.count[s.cur], s.bd[s.cur], S->d_red + 2 + k % 14 );
+        SG_LAUNCH_CHECK( "k_kinetic" );
+    }
+    const int comps[6] = { 0, 1, 2, 6, 7, 8 }; // E and the time-centred B_m (DiagnosticScalar.cpp:640-646)
+    for( int c : comps ) {
+        const int sx = comp_stag( c, 0 ), sy = comp_stag( c, 1 ), sz = comp_stag( c, 2 );
+        if( S->mixed ) k_norm2<float><<<1216, 256, 0, st>>>( S->g, static_cast<float *>( S->fptr[c] ), sx, sy, sz, S->d_red + 1 );
+        else k_norm2<double><<<1216, 256, 0, st>>>( S->g, static_cast<double *>( S->fptr[c] ), sx, sy, sz, S->d_red + 1 );
+        SG_LAUNCH_CHECK( "k_norm2" );
+    }
+    double h[16];
+    SG_CUDA_TRY( cudaMemcpyAsync( h, S->d_red, sizeof( h ), cudaMemcpyDeviceToHost, st ) );
+    SG_CUDA_TRY( cudaStreamSynchronize( st ) );
+    double vol = 1.0;
+    for( int d = 0; d < S->g.ndim; d++ ) vol *= S->g.dx[d];
+    double uk = 0.0;
+    for( size_t k = 0; k < S->sp.size(); k++ ) uk += S->sp[k].mass * h[2 + k % 14];
+    if( ukin ) *ukin = uk;
+    if( uelm ) *uelm = 0.5 * vol * h[1];
+    return SG_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,136 @@
+"""Python handle of the resident simulation object (sg_sim in include/smilei_gb300.h).
+
+A ``Simulation`` owns one periodic grid and its species on the GPU and runs
+whole timesteps (gather, push, Esirkepov deposit, per-tile sort, J fold, Yee,
+B centring) with the fused kernels of smilei_gb300/csrc/sim.cu.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import check
+
+FIELD_INDEX = {"Ex": 0, "Ey": 1, "Ez": 2, "Bx": 3, "By": 4, "Bz": 5, "Bx_m": 6, "By_m": 7, "Bz_m": 8,
+               "Jx": 9, "Jy": 10, "Jz": 11}
+
+
+class Simulation:
+    def __init__(self, n_cells, cell_length, dt, form="mixed", tile=None, capacity_slack=0.25, use_graph=True):
+        self.ndim = len(n_cells)
+        self.n_cells = [int(n) for n in n_cells]
+        self.cell_length = [float(c) for c in cell_length]
+        self.dt = float(dt)
+        self.form = form
+        cfg = _lib.SimConfig()
+        cfg.ndim = self.ndim
+        cfg.form = _lib.FORM_MIXED if form == "mixed" else _lib.FORM_FP64
+        for d in range(self.ndim):
+            cfg.n_cells[d] = self.n_cells[d]
+            cfg.cell_length[d] = self.cell_length[d]
+            cfg.tile[d] = int(tile[d]) if tile else 0
+        cfg.dt = self.dt
+        cfg.capacity_slack = float(capacity_slack)
+        cfg.use_graph = int(bool(use_graph))
+        h = ctypes.c_void_p()
+        check(_lib.lib().sg_sim_create(ctypes.byref(cfg), ctypes.byref(h)), "sg_sim_create")
+        self._h = h
+        self.species = []
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.lib().sg_sim_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- species -----------------------------------------------------------
+    def add_species(self, mass, charge, pusher, position, momentum, weight):
+        """position[ndim, n], momentum[3, n], weight[n] as float64 numpy arrays (host) or CUDA tensors."""
+        idx = ctypes.c_int()
+        kind = _lib.PUSHERS[pusher] if isinstance(pusher, str) else int(pusher)
+        if hasattr(position, "is_cuda") and position.is_cuda:
+            n = int(position.shape[1])
+            pos, mom, w = position.contiguous(), momentum.contiguous(), weight.contiguous()
+            check(_lib.lib().sg_sim_add_species_device(self._h, float(mass), float(charge), kind, n, pos.data_ptr(),
+                                                       mom.data_ptr(), w.data_ptr(), ctypes.byref(idx)),
+                  "add_species")
+        else:
+            pos = np.ascontiguousarray(position, dtype=np.float64)
+            mom = np.ascontiguousarray(momentum, dtype=np.float64)
+            w = np.ascontiguousarray(weight, dtype=np.float64)
+            n = int(pos.shape[1])
+            check(_lib.lib().sg_sim_add_species(self._h, float(mass), float(charge), kind, n, pos.ctypes.data,
+                                                mom.ctypes.data, w.ctypes.data, ctypes.byref(idx)), "add_species")
+        self.species.append(dict(mass=mass, charge=charge, pusher=pusher))
+        return idx.value
+
+    def species_count(self, s: int) -> int:
+        n = ctypes.c_int64()
+        check(_lib.lib().sg_sim_species_count(self._h, s, ctypes.byref(n)), "species_count")
+        return n.value
+
+    def get_species(self, s: int):
+        n = self.species_count(s)
+        pos = np.zeros((self.ndim, n))
+        mom = np.zeros((3, n))
+        w = np.zeros(n)
+        check(_lib.lib().sg_sim_get_species(self._h, s, pos.ctypes.data, mom.ctypes.data, w.ctypes.data),
+              "get_species")
+        return pos, mom, w
+
+    def state_bytes(self, s: int) -> int:
+        b = ctypes.c_size_t()
+        check(_lib.lib().sg_sim_state_bytes(self._h, s, ctypes.byref(b)), "state_bytes")
+        return b.value
+
+    def copy_state(self, s: int, host_ptr: int, to_device: bool):
+        """Raw state of species s to/from a host buffer of state_bytes(s) bytes (pinned for async)."""
+        check(_lib.lib().sg_sim_copy_state(self._h, s, host_ptr, int(bool(to_device))), "copy_state")
+
+    # -- fields ------------------------------------------------------------
+    def field_shape(self, name: str):
+        sh = (ctypes.c_int * 3)()
+        check(_lib.lib().sg_sim_field_shape(self._h, FIELD_INDEX[name], sh), "field_shape")
+        return tuple(sh[d] for d in range(self.ndim))
+
+    def get_field(self, name: str) -> np.ndarray:
+        a = np.zeros(self.field_shape(name))
+        check(_lib.lib().sg_sim_get_field(self._h, FIELD_INDEX[name], a.ctypes.data), "get_field")
+        return a
+
+    def set_field(self, name: str, value: np.ndarray):
+        a = np.ascontiguousarray(value, dtype=np.float64)
+        if a.shape != self.field_shape(name):
+            raise ValueError(f"{name}: expected shape {self.field_shape(name)}, got {a.shape}")
+        check(_lib.lib().sg_sim_set_field(self._h, FIELD_INDEX[name], a.ctypes.data), "set_field")
+
+    # -- stepping ----------------------------------------------------------
+    def step(self, n: int = 1):
+        check(_lib.lib().sg_sim_step(self._h, int(n)), "step")
+
+    def energy(self):
+        """(Ukin, Uelm) as the reference's scalar diagnostics define them."""
+        uk, ue = ctypes.c_double(), ctypes.c_double()
+        check(_lib.lib().sg_sim_energy(self._h, ctypes.byref(uk), ctypes.byref(ue)), "energy")
+        return uk.value, ue.value
+
+    def last_timing(self):
+        """Device ms of the last step: (particles, fields, total) and kernel launches per step."""
+        a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        n = ctypes.c_int()
+        check(_lib.lib().sg_sim_last_timing(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
+                                            ctypes.byref(n)), "last_timing")
+        return a.value, b.value, c.value, n.value

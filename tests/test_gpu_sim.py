@@ -1,0 +1,142 @@
+"""GPU parity of the resident timestep (sg_sim) with the oracle's full PIC step.
+
+The oracle step (or_pic_step: gather, push, Esirkepov deposit, periodic wrap,
+J ghost fold, Ampere, Faraday, B centring) runs on the same seeded plasma and
+fields; particles are matched by their (unique) weights.  FP64 form: 1e-12
+relative on every field and on momenta/positions.  Mixed form (int cell +
+FP32 offset, FP32 arithmetic): 1e-5 relative after one step.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+FIELDS = ["Ex", "Ey", "Ez", "Bx", "By", "Bz", "Bx_m", "By_m", "Bz_m", "Jx", "Jy", "Jz"]
+
+
+@pytest.fixture(scope="module")
+def sim_mod():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from smilei_gb300 import simulation, synthetic
+    return simulation, synthetic
+
+
+def make_case(synthetic, ndim, seed, species_spec):
+    n_cells = [16, 12, 8][:ndim] if ndim == 3 else [32, 24]
+    cl = [0.1, 0.12, 0.09][:ndim]
+    dt = 0.95 / np.sqrt(sum(1.0 / c ** 2 for c in cl))
+    fields = synthetic.periodic_em(seed, n_cells)
+    species = []
+    for k, (mass, charge, pusher, ppc, sigma) in enumerate(species_spec):
+        pos, mom, w = synthetic.thermal_plasma(n_cells, cl, ppc, sigma, seed + 10 + k, unique_weights=True)
+        species.append(dict(pos=pos, mom=mom, weight=w, charge=np.full(w.shape, int(charge), np.int16),
+                            mass=mass, pusher=pusher, q=charge))
+    return n_cells, cl, dt, fields, species
+
+
+def run_pair(sim_mod, cpu_oracle, ndim, form, nsteps, species_spec, seed=5, tile=None):
+    simulation, synthetic = sim_mod
+    n_cells, cl, dt, fields, species = make_case(synthetic, ndim, seed, species_spec)
+    sim = simulation.Simulation(n_cells, cl, dt, form=form, tile=tile, use_graph=True)
+    for k in FIELDS:
+        sim.set_field(k, fields[k])
+    for s in species:
+        sim.add_species(s["mass"], s["q"], s["pusher"], s["pos"], s["mom"], s["weight"])
+    sim.step(nsteps)
+    ref = {k: v.copy() for k, v in fields.items()}
+    ref_sp = [dict(s, pos=s["pos"].copy(), mom=s["mom"].copy()) for s in species]
+    for _ in range(nsteps):
+        cpu_oracle.pic_step(ndim, n_cells, 2, cl, dt, ref, ref_sp)
+    got = {k: sim.get_field(k) for k in FIELDS}
+    parts = []
+    for i, s in enumerate(ref_sp):
+        pos, mom, w = sim.get_species(i)
+        assert pos.shape[1] == s["pos"].shape[1]
+        order_got = np.argsort(w, kind="stable")
+        order_ref = np.argsort(s["weight"].astype(np.float32) if form == "mixed" else s["weight"], kind="stable")
+        parts.append((pos[:, order_got], mom[:, order_got], s["pos"][:, order_ref], s["mom"][:, order_ref], cl,
+                      n_cells))
+    sim.close()
+    return got, ref, parts
+
+
+def position_error(p_got, p_ref, cl, n_cells):
+    """Largest periodic distance between matched particles, in cells."""
+    err = 0.0
+    for d in range(p_got.shape[0]):
+        L = n_cells[d] * cl[d]
+        dd = np.abs(p_got[d] - p_ref[d])
+        dd = np.minimum(dd, L - dd) / cl[d]
+        err = max(err, float(dd.max()))
+    return err
+
+
+@pytest.mark.parametrize("ndim,pusher", [(3, "higueracary"), (3, "boris"), (2, "boris"), (2, "vay")])
+def test_fp64_step_matches_oracle(sim_mod, cpu_oracle, ndim, pusher):
+    spec = [(1.0, -1, pusher, 4, 0.3), (1836.0, 1, pusher, 2, 0.01)]
+    got, ref, parts = run_pair(sim_mod, cpu_oracle, ndim, "fp64", 3, spec)
+    for k in FIELDS:
+        assert rel_err(got[k], ref[k]) <= 1e-12, k
+    for pg, mg, pr, mr, cl, nc in parts:
+        assert rel_err(mg, mr) <= 1e-12
+        assert position_error(pg, pr, cl, nc) <= 1e-10
+
+
+@pytest.mark.parametrize("ndim,pusher", [(3, "higueracary"), (2, "boris")])
+def test_mixed_step_matches_fp64_oracle(sim_mod, cpu_oracle, ndim, pusher):
+    spec = [(1.0, -1, pusher, 4, 0.3)]
+    got, ref, parts = run_pair(sim_mod, cpu_oracle, ndim, "mixed", 1, spec)
+    for k in FIELDS:
+        assert rel_err(got[k], ref[k]) <= 1e-5, k
+    for pg, mg, pr, mr, cl, nc in parts:
+        assert rel_err(mg, mr) <= 1e-5
+        assert position_error(pg, pr, cl, nc) <= 1e-5
+
+
+def test_fp64_step_with_tile_spill_and_relayout(sim_mod, cpu_oracle):
+    """Hot particles and zero slack force spills and re-layouts; results must not change."""
+    simulation, synthetic = sim_mod
+    spec = [(1.0, -1, "boris", 3, 2.0)]
+    n_cells, cl, dt, fields, species = make_case(synthetic, 3, 11, spec)
+    sim = simulation.Simulation(n_cells, cl, dt, form="fp64", tile=[2, 2, 2], capacity_slack=1e-6, use_graph=True)
+    for k in FIELDS:
+        sim.set_field(k, fields[k])
+    s = species[0]
+    sim.add_species(s["mass"], s["q"], s["pusher"], s["pos"], s["mom"], s["weight"])
+    sim.step(4)
+    ref = {k: v.copy() for k, v in fields.items()}
+    ref_sp = [dict(s, pos=s["pos"].copy(), mom=s["mom"].copy())]
+    for _ in range(4):
+        cpu_oracle.pic_step(3, n_cells, 2, cl, dt, ref, ref_sp)
+    for k in FIELDS:
+        assert rel_err(sim.get_field(k), ref[k]) <= 1e-12, k
+    pos, mom, w = sim.get_species(0)
+    assert pos.shape[1] == s["pos"].shape[1]
+    o = np.argsort(w)
+    r = np.argsort(ref_sp[0]["weight"])
+    assert rel_err(mom[:, o], ref_sp[0]["mom"][:, r]) <= 1e-12
+    sim.close()
+
+
+def test_energy_diagnostic_matches_numpy(sim_mod):
+    simulation, synthetic = sim_mod
+    n_cells, cl = [16, 16, 8], [0.1, 0.1, 0.1]
+    fields = synthetic.periodic_em(3, n_cells, 0.2, 0.3)
+    pos, mom, w = synthetic.thermal_plasma(n_cells, cl, 2, 0.2, 4)
+    sim = simulation.Simulation(n_cells, cl, 0.05, form="fp64")
+    for k in FIELDS:
+        sim.set_field(k, fields[k])
+    sim.add_species(1.0, -1.0, "boris", pos, mom, w)
+    uk, ue = sim.energy()
+    uk_ref = np.sum(w * (np.sqrt(1 + (mom ** 2).sum(0)) - 1.0))
+    ue_ref = 0.0
+    for k in ("Ex", "Ey", "Ez", "Bx_m", "By_m", "Bz_m"):
+        a = fields[k][2:2 + n_cells[0], 2:2 + n_cells[1], 2:2 + n_cells[2]]
+        ue_ref += 0.5 * np.prod(cl) * np.sum(a * a)
+    assert abs(uk - uk_ref) <= 1e-12 * abs(uk_ref)
+    assert abs(ue - ue_ref) <= 1e-12 * abs(ue_ref)
+    sim.close()
