@@ -164,6 +164,26 @@ int sg_sim_get_species( sg_sim *sim, int species, double *pos, double *mom, doub
  * interior points (src/Diagnostic/DiagnosticScalar.cpp:174-277). */
 int sg_sim_energy( sg_sim *sim, double *ukin, double *uelm );
 
+/* Charge density of all species at the current positions, FP64, reference layout
+ * (primal, ghosts, periodic copies folded): the basic() projection of
+ * src/Projector/Projector3D2Order.cpp:526-618 summed over species. */
+int sg_sim_get_rho( sg_sim *sim, double *host );
+
+/* Initial electrostatic field: FP64 conjugate gradient for Laplacian(phi) = -rho on
+ * the periodic lattice, rho of all species with its mean removed (a uniform
+ * neutralising background), then E_d = (phi(i-1) - phi(i)) / dx_d with each
+ * component's mean removed.  Follows VectorPatch::solvePoisson
+ * (src/Patch/VectorPatch.cpp:1523-1620) and ElectroMagn3D::initPoisson, compute_Ap,
+ * update_pand_r, update_p, initE (src/ElectroMagn/ElectroMagn3D.cpp:255-560);
+ * stops when r.r / n_nodes <= max_error (the reference's poisson_max_error, 1e-14)
+ * or after max_iter iterations (poisson_max_iteration, 50000).  Overwrites E. */
+int sg_sim_solve_poisson( sg_sim *sim, double max_error, int max_iter, int *iterations, double *ctrl );
+
+/* Charge-conservation residual max|div E - (rho - <rho>)| / max|rho - <rho>| over the
+ * physical nodes, with rho deposited in FP64 from the current particles.
+ * rho_max (optional) receives max|rho - <rho>|. */
+int sg_sim_charge_residual( sg_sim *sim, double *residual, double *rho_max );
+
 /* Raw particle state of a species (the library's own SoA layout, tile segments
  * included): its size, and a copy of the current buffer to (to_device = 0) or
  * from (to_device = 1) a host buffer of that size, on the simulation's stream

@@ -75,6 +75,9 @@ _SIGNATURES = {
                                 ctypes.POINTER(_I)]),
     "sg_sim_set_stream": (_I, [_VP, _VP]),
     "sg_sim_state_bytes": (_I, [_VP, _I, ctypes.POINTER(ctypes.c_size_t)]),
+    "sg_sim_get_rho": (_I, [_VP, _VP]),
+    "sg_sim_solve_poisson": (_I, [_VP, _D, _I, ctypes.POINTER(_I), ctypes.POINTER(_D)]),
+    "sg_sim_charge_residual": (_I, [_VP, ctypes.POINTER(_D), ctypes.POINTER(_D)]),
     "sg_sim_copy_state": (_I, [_VP, _I, _VP, _I]),
 }
 

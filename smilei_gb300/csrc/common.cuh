@@ -27,7 +27,18 @@ inline int cuda_fail( cudaError_t e, const char *what, const char *file, int lin
         if( sg_e_ != cudaSuccess ) return ::sg::cuda_fail( sg_e_, #call, __FILE__, __LINE__ ); \
     } while( 0 )
 
-#define SG_LAUNCH_CHECK( what ) SG_CUDA_TRY( cudaPeekAtLastError() )
+#define SG_LAUNCH_CHECK( what ) SG_CUDA_TRY( cudaGetLastError() )
+
+// Releases device memory in cleanup paths; a failure there is not reported and
+// must not stay pending as the thread's last error.
+inline void release( void *p )
+{
+    if( p && cudaFree( p ) != cudaSuccess ) cudaGetLastError();
+}
+inline void release_async( void *p, cudaStream_t s )
+{
+    if( p && cudaFreeAsync( p, s ) != cudaSuccess ) cudaGetLastError();
+}
 
 #define SG_REQUIRE( cond, ... )                                        \
     do {                                                               \

@@ -343,12 +343,12 @@ __global__ void __launch_bounds__( 128 ) k_step_particles(
         lx[0] = gnode[0] - ix0;
         lx[1] = gnode[1] - iy0;
         lx[2] = DIM == 3 ? gnode[2] - iz0 : 0;
-        bool ok = !valid || ( lx[0] >= 0 && lx[0] < g.T[0] && lx[1] >= 0 && lx[1] < g.T[1] &&
-                              ( DIM == 2 || ( lx[2] >= 0 && lx[2] < g.T[2] ) ) );
-        if( !ok ) {
-            atomicCAS( status, 0, SG_ERR_BOUNDS );
-            lx[0] = lx[1] = lx[2] = 0;
-        }
+        const bool inside = lx[0] >= 0 && lx[0] < g.T[0] && lx[1] >= 0 && lx[1] < g.T[1] &&
+                            ( DIM == 2 || ( lx[2] >= 0 && lx[2] < g.T[2] ) );
+        if( valid && !inside ) atomicCAS( status, 0, SG_ERR_BOUNDS );
+        // lanes past the tile's last particle, and particles found outside the
+        // tile, read the tile at its origin: every shared-memory index stays in range
+        if( !valid || !inside ) lx[0] = lx[1] = lx[2] = 0;
 
         // ---- gather ---------------------------------------------------------------
         T cp[3][3], cd[3][3];
@@ -1094,22 +1094,22 @@ int launch_fields( sg_sim *S, cudaStream_t st, int &launches )
 int enqueue_step( sg_sim *S, cudaStream_t st )
 {
     int launches = 0;
-    SG_CUDA_TRY( cudaEventRecord( S->ev[3], st ) );
+    SG_CUDA_TRY( cudaEventRecordWithFlags( S->ev[3], st, cudaEventRecordExternal ) );
     for( int c = 9; c < 12; c++ ) SG_CUDA_TRY( cudaMemsetAsync( S->fptr[c], 0, S->fsize[c] * S->esz, st ) );
     SG_CUDA_TRY( cudaMemsetAsync( S->d_flags, 0, ( 1 + S->sp.size() ) * sizeof( int ), st ) );
     for( auto &s : S->sp ) SG_CUDA_TRY( cudaMemsetAsync( s.count[1 - s.cur], 0, S->g.ntiles * sizeof( int ), st ) );
-    SG_CUDA_TRY( cudaEventRecord( S->ev[0], st ) );
+    SG_CUDA_TRY( cudaEventRecordWithFlags( S->ev[0], st, cudaEventRecordExternal ) );
     for( auto &s : S->sp ) {
         int r = launch_particles_any( S, s, st );
         if( r ) return r;
         launches++;
     }
-    SG_CUDA_TRY( cudaEventRecord( S->ev[1], st ) );
+    SG_CUDA_TRY( cudaEventRecordWithFlags( S->ev[1], st, cudaEventRecordExternal ) );
     int r;
     if( S->g.ndim == 3 ) r = S->mixed ? launch_fields<3, float>( S, st, launches ) : launch_fields<3, double>( S, st, launches );
     else r = S->mixed ? launch_fields<2, float>( S, st, launches ) : launch_fields<2, double>( S, st, launches );
     if( r ) return r;
-    SG_CUDA_TRY( cudaEventRecord( S->ev[2], st ) );
+    SG_CUDA_TRY( cudaEventRecordWithFlags( S->ev[2], st, cudaEventRecordExternal ) );
     SG_CUDA_TRY( cudaMemcpyAsync( S->h_flags, S->d_flags, ( 1 + S->sp.size() ) * sizeof( int ), cudaMemcpyDeviceToHost, st ) );
     S->launches_per_step = launches;
     return SG_OK;
@@ -1221,8 +1221,8 @@ int relayout( sg_sim *S, SpeciesState &s, int nspill )
     SG_CUDA_TRY( cudaMemcpyAsync( s.count[dst_buf], s.count[s.cur], nt * sizeof( int ), cudaMemcpyDeviceToDevice, S->stream ) );
     SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
     if( realloc ) {
-        cudaFree( old_mem[0] );
-        cudaFree( old_mem[1] );
+        release( old_mem[0] );
+        release( old_mem[1] );
     }
     s.cur = dst_buf;
     drop_graphs( S );
@@ -1329,23 +1329,23 @@ int sg_sim_destroy( sg_sim *S )
     if( S->stream ) cudaStreamSynchronize( S->stream );
     drop_graphs( S );
     for( auto &s : S->sp ) {
-        cudaFree( s.mem[0] );
-        cudaFree( s.mem[1] );
-        cudaFree( s.seg_start );
-        cudaFree( s.cap );
-        cudaFree( s.count[0] );
-        cudaFree( s.count[1] );
-        cudaFree( s.ovf_mem );
-        cudaFree( s.ovf_tile );
+        release( s.mem[0] );
+        release( s.mem[1] );
+        release( s.seg_start );
+        release( s.cap );
+        release( s.count[0] );
+        release( s.count[1] );
+        release( s.ovf_mem );
+        release( s.ovf_tile );
     }
-    cudaFree( S->fmem );
-    cudaFree( S->d_flags );
+    release( S->fmem );
+    release( S->d_flags );
     if( S->h_flags ) cudaFreeHost( S->h_flags );
-    cudaFree( S->scan_scratch );
-    cudaFree( S->tmp_start );
-    cudaFree( S->tmp_cap );
-    cudaFree( S->fill );
-    cudaFree( S->d_red );
+    release( S->scan_scratch );
+    release( S->tmp_start );
+    release( S->tmp_cap );
+    release( S->fill );
+    release( S->d_red );
     for( int i = 0; i < 4; i++ )
         if( S->ev[i] ) cudaEventDestroy( S->ev[i] );
     if( S->own_stream && S->stream ) cudaStreamDestroy( S->stream );
@@ -1418,8 +1418,8 @@ int sg_sim_add_species_device( sg_sim *S, double mass, double charge, int pusher
     // the spill list only needs a fraction of the species once placed
     const int64_t spill_cap = std::max<int64_t>( 4096, npart / 16 );
     if( spill_cap < s.ovf_capacity ) {
-        cudaFree( s.ovf_mem );
-        cudaFree( s.ovf_tile );
+        release( s.ovf_mem );
+        release( s.ovf_tile );
         s.ovf_mem = nullptr;
         s.ovf_tile = nullptr;
         s.ovf_capacity = spill_cap;
@@ -1457,7 +1457,7 @@ int sg_sim_add_species( sg_sim *S, double mass, double charge, int pusher, int64
         SG_CUDA_TRY( cudaMemcpy( d + ( nd + 3 ) * npart, weight, npart * 8, cudaMemcpyHostToDevice ) );
     }
     int r = sg_sim_add_species_device( S, mass, charge, pusher, npart, d, d + nd * npart, d + ( nd + 3 ) * npart, index );
-    cudaFree( d );
+    release( d );
     return r;
 }
 
@@ -1484,7 +1484,7 @@ int sg_sim_set_field( sg_sim *S, int comp, const double *host )
         k_convert<double, float><<<grid_for( n, 256 ), 256, 0, S->stream>>>( n, d, static_cast<float *>( S->fptr[comp] ) );
         SG_LAUNCH_CHECK( "k_convert" );
         SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
-        cudaFree( d );
+        release( d );
     }
     return SG_OK;
 }
@@ -1504,7 +1504,7 @@ int sg_sim_get_field( sg_sim *S, int comp, double *host )
         SG_LAUNCH_CHECK( "k_convert" );
         SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
         SG_CUDA_TRY( cudaMemcpy( host, d, n * 8, cudaMemcpyDeviceToHost ) );
-        cudaFree( d );
+        release( d );
     }
     return SG_OK;
 }
@@ -1534,9 +1534,13 @@ int sg_sim_step( sg_sim *S, int nsteps )
         SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
         for( auto &s : S->sp ) s.cur = 1 - s.cur;
         const int status = S->h_flags[0];
-        cudaEventElapsedTime( &S->last_ms[0], S->ev[0], S->ev[1] );
-        cudaEventElapsedTime( &S->last_ms[1], S->ev[1], S->ev[2] );
-        cudaEventElapsedTime( &S->last_ms[2], S->ev[3], S->ev[2] );
+        // stage times from the events recorded inside the step (external event nodes in a graph)
+        if( cudaEventElapsedTime( &S->last_ms[0], S->ev[0], S->ev[1] ) != cudaSuccess ||
+            cudaEventElapsedTime( &S->last_ms[1], S->ev[1], S->ev[2] ) != cudaSuccess ||
+            cudaEventElapsedTime( &S->last_ms[2], S->ev[3], S->ev[2] ) != cudaSuccess ) {
+            cudaGetLastError(); // timing is informative only; do not leave the error pending
+            S->last_ms[0] = S->last_ms[1] = S->last_ms[2] = -1.0f;
+        }
         if( status ) {
             return set_error( status, status == SG_ERR_BOUNDS ? "a particle moved more than one cell in a step or left its tile"
                                                               : "the spill list overflowed (capacity too small)" );
@@ -1604,8 +1608,8 @@ int sg_sim_get_species( sg_sim *S, int species, double *pos, double *mom, double
     SG_CUDA_TRY( cudaMemcpy( pos, d, nd * n * 8, cudaMemcpyDeviceToHost ) );
     SG_CUDA_TRY( cudaMemcpy( mom, d + nd * n, 3 * n * 8, cudaMemcpyDeviceToHost ) );
     SG_CUDA_TRY( cudaMemcpy( weight, d + ( nd + 3 ) * n, n * 8, cudaMemcpyDeviceToHost ) );
-    cudaFree( off );
-    cudaFree( d );
+    release( off );
+    release( d );
     return SG_OK;
 }
 
@@ -1658,6 +1662,450 @@ int sg_sim_energy( sg_sim *S, double *ukin, double *uelm )
     for( size_t k = 0; k < S->sp.size(); k++ ) uk += S->sp[k].mass * h[2 + k % 14];
     if( ukin ) *ukin = uk;
     if( uelm ) *uelm = 0.5 * vol * h[1];
+    return SG_OK;
+}
+
+} // extern "C"
+
+// ==============================================================================
+// Charge density, initial-field Poisson solve (FP64 conjugate gradient) and
+// the charge-conservation residual.
+// ==============================================================================
+namespace sg {
+namespace {
+
+// rho of the current particle positions (Projector3D2Order::basic, type 0,
+// src/Projector/Projector3D2Order.cpp:526-618), FP64 accumulation in a
+// per-tile shared array, flushed into the FP64 rho array (reference layout,
+// primal, ghosts).  One block per tile.
+template <int DIM, bool MIXED>
+__global__ void k_rho_tiles( GridInfo g, const int64_t *__restrict__ seg_start, const int *__restrict__ count,
+                             PBuf<MIXED> b, double cw, double *__restrict__ rho )
+{
+    extern __shared__ __align__( 16 ) unsigned char smem_raw[];
+    double *sR = reinterpret_cast<double *>( smem_raw );
+    const TileDims td = tile_dims( g );
+    const int jsz = td.JX * td.JY * td.JZ;
+    const int tile = blockIdx.x;
+    int tz = 0, ty, tx;
+    if( DIM == 3 ) {
+        tz = tile % g.nt[2];
+        ty = ( tile / g.nt[2] ) % g.nt[1];
+        tx = tile / ( g.nt[2] * g.nt[1] );
+    } else {
+        ty = tile % g.nt[1];
+        tx = tile / g.nt[1];
+    }
+    const int i0[3] = { tx * g.T[0], ty * g.T[1], DIM == 3 ? tz * g.T[2] : 0 };
+    for( int e = threadIdx.x; e < jsz; e += blockDim.x ) sR[e] = 0.0;
+    __syncthreads();
+    const int n = count[tile];
+    const int64_t s0 = seg_start[tile];
+    for( int q = threadIdx.x; q < n; q += blockDim.x ) {
+        const int64_t src = s0 + q;
+        int node[3] = { 0, 0, 0 };
+        double dl[3] = { 0.0, 0.0, 0.0 };
+        if constexpr( MIXED ) {
+            unpack_key( DIM, b.key[src], node[0], node[1], node[2] );
+            for( int d = 0; d < DIM; d++ ) dl[d] = ( double )b.d[d][src];
+        } else {
+            for( int d = 0; d < DIM; d++ ) {
+                double xn = b.x[d][src] * g.dxi[d];
+                int ip = round_half_away( xn );
+                if( ip >= g.N[d] ) { ip -= g.N[d]; xn -= ( double )g.N[d]; }
+                node[d] = ip;
+                dl[d] = xn - ( double )ip;
+            }
+        }
+        double S[3][3];
+        int l[3] = { 0, 0, 0 };
+        bool inside = true;
+        for( int d = 0; d < 3; d++ ) {
+            if( d < DIM ) {
+                bspline2( dl[d], S[d][0], S[d][1], S[d][2] );
+                l[d] = node[d] - i0[d];
+                if( l[d] < 0 || l[d] >= g.T[d] ) inside = false;
+            } else {
+                S[d][0] = S[d][2] = 0.0;
+                S[d][1] = 1.0;
+            }
+        }
+        if( !inside ) continue; // cannot happen for a sorted buffer
+        const double c = cw * ( double )b.w[src];
+        // nodes node-1 .. node+1 -> tile index l+1 .. l+3 (tile origin at node i0-2)
+        for( int a = 0; a < 3; a++ )
+            for( int bb = 0; bb < 3; bb++ )
+                for( int cc = 0; cc < ( DIM == 3 ? 3 : 1 ); cc++ ) {
+                    const double v = c * S[0][a] * S[1][bb] * ( DIM == 3 ? S[2][cc] : 1.0 );
+                    const int iz = DIM == 3 ? l[2] + 1 + cc : 0;
+                    atomicAdd( &sR[( ( l[0] + 1 + a ) * td.JY + ( l[1] + 1 + bb ) ) * td.JZ + iz], v );
+                }
+    }
+    __syncthreads();
+    const int nx = ext( g, 0, 0 ), ny = ext( g, 1, 0 ), nz = ext( g, 2, 0 );
+    for( int e = threadIdx.x; e < jsz; e += blockDim.x ) {
+        const double v = sR[e];
+        if( v == 0.0 ) continue;
+        const int cz = e % td.JZ, cy = ( e / td.JZ ) % td.JY, cx = e / ( td.JZ * td.JY );
+        const int gx = i0[0] + OS - 2 + cx, gy = i0[1] + OS - 2 + cy, gz = DIM == 3 ? i0[2] + OS - 2 + cz : 0;
+        if( gx < nx && gy < ny && gz < nz ) atomicAdd( &rho[( ( int64_t )gx * ny + gy ) * nz + gz], v );
+    }
+}
+
+// Periodic fold of one primal array (as k_fold, for rho).
+__global__ void k_fold_one( GridInfo g, int d, double *a )
+{
+    const int e0 = ext( g, 0, 0 ), e1 = ext( g, 1, 0 ), e2 = ext( g, 2, 0 );
+    int se[3] = { e0, e1, e2 };
+    se[d] = 1 + 2 * OS;
+    const int64_t n = ( int64_t )se[0] * se[1] * se[2];
+    for( int64_t t = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x; t < n; t += ( int64_t )gridDim.x * blockDim.x ) {
+        const int k = ( int )( t % se[2] ), j = ( int )( ( t / se[2] ) % se[1] ), i = ( int )( t / ( ( int64_t )se[2] * se[1] ) );
+        int i2 = i, j2 = j, k2 = k;
+        if( d == 0 ) i2 += g.N[0]; else if( d == 1 ) j2 += g.N[1]; else k2 += g.N[2];
+        const int64_t a1 = ( ( int64_t )i * e1 + j ) * e2 + k, a2 = ( ( int64_t )i2 * e1 + j2 ) * e2 + k2;
+        const double v = a[a2] + a[a1];
+        a[a2] = v;
+        a[a1] = v;
+    }
+}
+
+// Physical node t (x-major over N^ndim) <-> array index of the ghosted array.
+__device__ __forceinline__ void phys_ijk( const GridInfo &g, int64_t t, int &i, int &j, int &k )
+{
+    const int n1 = g.N[1], n2 = g.ndim == 3 ? g.N[2] : 1;
+    k = ( int )( t % n2 );
+    j = ( int )( ( t / n2 ) % n1 );
+    i = ( int )( t / ( ( int64_t )n2 * n1 ) );
+}
+
+__device__ __forceinline__ int64_t phys_lin( const GridInfo &g, int i, int j, int k )
+{
+    const int n1 = g.N[1], n2 = g.ndim == 3 ? g.N[2] : 1;
+    return ( ( int64_t )i * n1 + j ) * n2 + k;
+}
+
+__device__ __forceinline__ int wrapi( int i, int n ) { return i < 0 ? i + n : ( i >= n ? i - n : i ); }
+
+// b = rho (physical nodes) minus the mean given in mean[0]; r = -b... the CG
+// starts from phi = 0, r = -rho, p = r (ElectroMagn3D::initPoisson).
+__global__ void k_cg_init( GridInfo g, const double *__restrict__ rho_g, const double *__restrict__ sums,
+                           double *__restrict__ phi, double *__restrict__ r, double *__restrict__ p, int64_t n )
+{
+    const double mean = sums[0] / ( double )n;
+    for( int64_t t = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x; t < n; t += ( int64_t )gridDim.x * blockDim.x ) {
+        int i, j, k;
+        phys_ijk( g, t, i, j, k );
+        const int ny = ext( g, 1, 0 ), nz = ext( g, 2, 0 );
+        const double v = rho_g[( ( int64_t )( i + OS ) * ny + ( j + OS ) ) * nz + ( g.ndim == 3 ? k + OS : 0 )] - mean;
+        phi[t] = 0.0;
+        r[t] = -v;
+        p[t] = -v;
+    }
+}
+
+// sum of rho over the physical nodes (for the mean) -> sums[0]
+__global__ void k_rho_sum( GridInfo g, const double *__restrict__ rho_g, int64_t n, double *__restrict__ sums )
+{
+    double acc = 0.0;
+    for( int64_t t = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x; t < n; t += ( int64_t )gridDim.x * blockDim.x ) {
+        int i, j, k;
+        phys_ijk( g, t, i, j, k );
+        const int ny = ext( g, 1, 0 ), nz = ext( g, 2, 0 );
+        acc += rho_g[( ( int64_t )( i + OS ) * ny + ( j + OS ) ) * nz + ( g.ndim == 3 ? k + OS : 0 )];
+    }
+    acc = block_sum( acc );
+    if( threadIdx.x == 0 ) atomicAdd( sums, acc );
+}
+
+__global__ void k_dot( const double *__restrict__ a, const double *__restrict__ b, int64_t n, double *__restrict__ out )
+{
+    double acc = 0.0;
+    for( int64_t t = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x; t < n; t += ( int64_t )gridDim.x * blockDim.x )
+        acc += a[t] * b[t];
+    acc = block_sum( acc );
+    if( threadIdx.x == 0 ) atomicAdd( out, acc );
+}
+
+// Ap = periodic 7-point (5-point in 2D) Laplacian of p (ElectroMagn3D::compute_Ap), and p.Ap -> s[1]
+__global__ void k_cg_ap( GridInfo g, const double *__restrict__ p, double *__restrict__ Ap, int64_t n,
+                         double *__restrict__ s )
+{
+    const double ix2 = g.dxi[0] * g.dxi[0], iy2 = g.dxi[1] * g.dxi[1];
+    const double iz2 = g.ndim == 3 ? g.dxi[2] * g.dxi[2] : 0.0;
+    const double two = 2.0 * ( ix2 + iy2 + iz2 );
+    double acc = 0.0;
+    for( int64_t t = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x; t < n; t += ( int64_t )gridDim.x * blockDim.x ) {
+        int i, j, k;
+        phys_ijk( g, t, i, j, k );
+        double v = ix2 * ( p[phys_lin( g, wrapi( i - 1, g.N[0] ), j, k )] + p[phys_lin( g, wrapi( i + 1, g.N[0] ), j, k )] )
+                   + iy2 * ( p[phys_lin( g, i, wrapi( j - 1, g.N[1] ), k )] + p[phys_lin( g, i, wrapi( j + 1, g.N[1] ), k )] );
+        if( g.ndim == 3 ) v += iz2 * ( p[phys_lin( g, i, j, wrapi( k - 1, g.N[2] ) )] + p[phys_lin( g, i, j, wrapi( k + 1, g.N[2] ) )] );
+        v -= two * p[t];
+        Ap[t] = v;
+        acc += p[t] * v;
+    }
+    acc = block_sum( acc );
+    if( threadIdx.x == 0 ) atomicAdd( &s[1], acc );
+}
+
+// alpha = r.r / p.Ap; phi += alpha p; r -= alpha Ap; r_new.r_new -> s[2] (update_pand_r)
+__global__ void k_cg_update_r( const double *__restrict__ p, const double *__restrict__ Ap, double *__restrict__ phi,
+                               double *__restrict__ r, int64_t n, double *__restrict__ s )
+{
+    const double alpha = s[0] / s[1];
+    double acc = 0.0;
+    for( int64_t t = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x; t < n; t += ( int64_t )gridDim.x * blockDim.x ) {
+        phi[t] += alpha * p[t];
+        const double rv = r[t] - alpha * Ap[t];
+        r[t] = rv;
+        acc += rv * rv;
+    }
+    acc = block_sum( acc );
+    if( threadIdx.x == 0 ) atomicAdd( &s[2], acc );
+}
+
+// p = r + beta p with beta = r_new.r_new / r.r (update_p)
+__global__ void k_cg_update_p( const double *__restrict__ r, double *__restrict__ p, int64_t n,
+                               const double *__restrict__ s )
+{
+    const double beta = s[2] / s[0];
+    for( int64_t t = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x; t < n; t += ( int64_t )gridDim.x * blockDim.x )
+        p[t] = r[t] + beta * p[t];
+}
+
+// s[0] <- s[2], s[1] = s[2] = 0, s[3] = ctrl = r.r / n
+__global__ void k_cg_scalars( double *s, int64_t n )
+{
+    s[0] = s[2];
+    s[1] = 0.0;
+    s[2] = 0.0;
+    s[3] = s[0] / ( double )n;
+}
+
+// E_d on the dual nodes from phi (ElectroMagn3D::initE): E_d(i) = (phi(i-1) - phi(i)) / dx_d,
+// physical layout; also accumulates each component's sum (for the mean) into sums[d].
+__global__ void k_efield( GridInfo g, const double *__restrict__ phi, double *__restrict__ E, int64_t n,
+                          double *__restrict__ sums )
+{
+    const int d = blockIdx.y;
+    double acc = 0.0;
+    for( int64_t t = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x; t < n; t += ( int64_t )gridDim.x * blockDim.x ) {
+        int i, j, k;
+        phys_ijk( g, t, i, j, k );
+        int a = i, b = j, c = k;
+        if( d == 0 ) a = wrapi( i - 1, g.N[0] );
+        else if( d == 1 ) b = wrapi( j - 1, g.N[1] );
+        else c = wrapi( k - 1, g.N[2] );
+        const double v = ( phi[phys_lin( g, a, b, c )] - phi[t] ) * g.dxi[d];
+        E[( int64_t )d * n + t] = v;
+        acc += v;
+    }
+    acc = block_sum( acc );
+    if( threadIdx.x == 0 ) atomicAdd( &sums[d], acc );
+}
+
+// Writes E_d minus its mean into every point (ghosts included) of the simulation's E_d array.
+template <class T>
+__global__ void k_efield_store( GridInfo g, const double *__restrict__ E, int64_t n, const double *__restrict__ sums,
+                                T *__restrict__ dst, int d )
+{
+    const int sx = stag( d, 0 ), sy = stag( d, 1 ), sz = stag( d, 2 );
+    const int e0 = ext( g, 0, sx ), e1 = ext( g, 1, sy ), e2 = ext( g, 2, sz );
+    const int64_t tot = ( int64_t )e0 * e1 * e2;
+    const double mean = sums[d] / ( double )n;
+    for( int64_t t = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += ( int64_t )gridDim.x * blockDim.x ) {
+        const int k = ( int )( t % e2 ), j = ( int )( ( t / e2 ) % e1 ), i = ( int )( t / ( ( int64_t )e2 * e1 ) );
+        const int pi = ( ( i - OS ) % g.N[0] + g.N[0] ) % g.N[0];
+        const int pj = ( ( j - OS ) % g.N[1] + g.N[1] ) % g.N[1];
+        const int pk = g.ndim == 3 ? ( ( k - OS ) % g.N[2] + g.N[2] ) % g.N[2] : 0;
+        dst[t] = ( T )( E[( int64_t )d * n + phys_lin( g, pi, pj, pk )] - mean );
+    }
+}
+
+// max |div E - (rho - mean rho)| and max |rho - mean rho| over the physical nodes -> out[0], out[1]
+// (as unsigned-long-long bit patterns of non-negative doubles, so atomicMax orders them).
+template <class T>
+__global__ void k_residual( GridInfo g, const T *__restrict__ Ex, const T *__restrict__ Ey, const T *__restrict__ Ez,
+                            const double *__restrict__ rho_g, const double *__restrict__ sums, int64_t n,
+                            unsigned long long *__restrict__ out )
+{
+    const double mean = sums[0] / ( double )n;
+    const int nyp = ext( g, 1, 0 ), nzp = ext( g, 2, 0 );
+    double m0 = 0.0, m1 = 0.0;
+    for( int64_t t = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x; t < n; t += ( int64_t )gridDim.x * blockDim.x ) {
+        int i, j, k;
+        phys_ijk( g, t, i, j, k );
+        const int a = i + OS, b = j + OS, c = g.ndim == 3 ? k + OS : 0;
+        // primal node (a,b,c): Ex dual in x at a and a+1, etc.
+        double div = ( ( double )Ex[( ( int64_t )( a + 1 ) * nyp + b ) * nzp + c] - ( double )Ex[( ( int64_t )a * nyp + b ) * nzp + c] ) * g.dxi[0]
+                     + ( ( double )Ey[( ( int64_t )a * ( nyp + 1 ) + b + 1 ) * nzp + c] - ( double )Ey[( ( int64_t )a * ( nyp + 1 ) + b ) * nzp + c] ) * g.dxi[1];
+        if( g.ndim == 3 )
+            div += ( ( double )Ez[( ( int64_t )a * nyp + b ) * ( nzp + 1 ) + c + 1] - ( double )Ez[( ( int64_t )a * nyp + b ) * ( nzp + 1 ) + c] ) * g.dxi[2];
+        const double rv = rho_g[( ( int64_t )a * nyp + b ) * nzp + c] - mean;
+        m0 = fmax( m0, fabs( div - rv ) );
+        m1 = fmax( m1, fabs( rv ) );
+    }
+    for( int o = 16; o > 0; o >>= 1 ) {
+        m0 = fmax( m0, __shfl_down_sync( 0xffffffffu, m0, o ) );
+        m1 = fmax( m1, __shfl_down_sync( 0xffffffffu, m1, o ) );
+    }
+    if( ( threadIdx.x & 31 ) == 0 ) {
+        atomicMax( &out[0], ( unsigned long long )__double_as_longlong( m0 ) );
+        atomicMax( &out[1], ( unsigned long long )__double_as_longlong( m1 ) );
+    }
+}
+
+// Deposits rho of all species (FP64) into S->rho (reference layout, primal), folded.
+int deposit_rho( sg_sim *S, double *rho )
+{
+    cudaStream_t st = S->stream;
+    const GridInfo &g = S->g;
+    SG_CUDA_TRY( cudaMemsetAsync( rho, 0, ( size_t )ext( g, 0, 0 ) * ext( g, 1, 0 ) * ext( g, 2, 0 ) * sizeof( double ), st ) );
+    const TileDims td = tile_dims( g );
+    const size_t smem = ( size_t )td.JX * td.JY * td.JZ * sizeof( double );
+    double vol = 1.0;
+    for( int d = 0; d < g.ndim; d++ ) vol *= g.dx[d];
+    for( auto &s : S->sp ) {
+        const double cw = s.charge / vol;
+        if( g.ndim == 3 ) {
+            if( S->mixed ) k_rho_tiles<3, true><<<g.ntiles, 128, smem, st>>>( g, s.seg_start, s.count[s.cur], s.bm[s.cur], cw, rho );
+            else k_rho_tiles<3, false><<<g.ntiles, 128, smem, st>>>( g, s.seg_start, s.count[s.cur], s.bd[s.cur], cw, rho );
+        } else {
+            if( S->mixed ) k_rho_tiles<2, true><<<g.ntiles, 128, smem, st>>>( g, s.seg_start, s.count[s.cur], s.bm[s.cur], cw, rho );
+            else k_rho_tiles<2, false><<<g.ntiles, 128, smem, st>>>( g, s.seg_start, s.count[s.cur], s.bd[s.cur], cw, rho );
+        }
+        SG_LAUNCH_CHECK( "k_rho_tiles" );
+    }
+    for( int d = 0; d < g.ndim; d++ ) {
+        k_fold_one<<<1024, 256, 0, st>>>( g, d, rho );
+        SG_LAUNCH_CHECK( "k_fold_one" );
+    }
+    return SG_OK;
+}
+
+int64_t phys_nodes( const GridInfo &g )
+{
+    int64_t n = 1;
+    for( int d = 0; d < g.ndim; d++ ) n *= g.N[d];
+    return n;
+}
+
+} // namespace
+} // namespace sg
+
+extern "C" {
+
+int sg_sim_get_rho( sg_sim *S, double *host )
+{
+    SG_REQUIRE( S && host, "NULL argument" );
+    const GridInfo &g = S->g;
+    const size_t n = ( size_t )ext( g, 0, 0 ) * ext( g, 1, 0 ) * ext( g, 2, 0 );
+    double *rho = nullptr;
+    SG_CUDA_TRY( cudaMallocAsync( &rho, n * sizeof( double ), S->stream ) );
+    int r = deposit_rho( S, rho );
+    if( r == SG_OK ) {
+        SG_CUDA_TRY( cudaMemcpyAsync( host, rho, n * sizeof( double ), cudaMemcpyDeviceToHost, S->stream ) );
+    }
+    release_async( rho, S->stream );
+    SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
+    return r;
+}
+
+int sg_sim_solve_poisson( sg_sim *S, double max_error, int max_iter, int *iterations, double *ctrl_out )
+{
+    SG_REQUIRE( S, "NULL simulation" );
+    SG_REQUIRE( max_iter >= 0, "max_iter < 0" );
+    const GridInfo &g = S->g;
+    cudaStream_t st = S->stream;
+    const int64_t n = phys_nodes( g );
+    const size_t nrho = ( size_t )ext( g, 0, 0 ) * ext( g, 1, 0 ) * ext( g, 2, 0 );
+    // scratch: rho (ghosted) + phi, r, p, Ap (physical) + E (ndim x physical) + scalars
+    double *mem = nullptr;
+    const size_t elems = nrho + ( 4 + ( size_t )g.ndim ) * ( size_t )n + 16;
+    SG_CUDA_TRY( cudaMallocAsync( &mem, elems * sizeof( double ), st ) );
+    double *rho = mem, *phi = rho + nrho, *r = phi + n, *p = r + n, *Ap = p + n, *E = Ap + n;
+    double *s = E + ( size_t )g.ndim * n; // [0] r.r [1] p.Ap [2] rnew [3] ctrl [4] rho sum [8..10] E sums
+    int rc = SG_OK;
+    int it = 0;
+    double ctrl = 0.0;
+    do {
+        if( cudaMemsetAsync( s, 0, 16 * sizeof( double ), st ) != cudaSuccess ) { rc = set_error( SG_ERR_CUDA, "memset" ); break; }
+        if( ( rc = deposit_rho( S, rho ) ) ) break;
+        k_rho_sum<<<1024, 256, 0, st>>>( g, rho, n, s + 4 );
+        k_cg_init<<<1024, 256, 0, st>>>( g, rho, s + 4, phi, r, p, n );
+        k_dot<<<1024, 256, 0, st>>>( r, r, n, s + 2 );
+        k_cg_scalars<<<1, 1, 0, st>>>( s, n );
+        if( cudaGetLastError() != cudaSuccess ) { rc = set_error( SG_ERR_CUDA, "CG init launch failed" ); break; }
+        double h[4];
+        if( cudaMemcpyAsync( h, s, 4 * sizeof( double ), cudaMemcpyDeviceToHost, st ) != cudaSuccess ||
+            cudaStreamSynchronize( st ) != cudaSuccess ) { rc = set_error( SG_ERR_CUDA, "CG init failed" ); break; }
+        ctrl = h[3];
+        const int check_every = 16;
+        while( ctrl > max_error && it < max_iter ) {
+            const int todo = std::min( check_every, max_iter - it );
+            for( int k = 0; k < todo; k++ ) {
+                k_cg_ap<<<1216, 256, 0, st>>>( g, p, Ap, n, s );
+                k_cg_update_r<<<1216, 256, 0, st>>>( p, Ap, phi, r, n, s );
+                k_cg_update_p<<<1216, 256, 0, st>>>( r, p, n, s );
+                k_cg_scalars<<<1, 1, 0, st>>>( s, n );
+            }
+            if( cudaGetLastError() != cudaSuccess ) { rc = set_error( SG_ERR_CUDA, "CG launch failed" ); break; }
+            if( cudaMemcpyAsync( h, s, 4 * sizeof( double ), cudaMemcpyDeviceToHost, st ) != cudaSuccess ||
+                cudaStreamSynchronize( st ) != cudaSuccess ) { rc = set_error( SG_ERR_CUDA, "CG iteration failed" ); break; }
+            // iterations past convergence inside a batch only shrink r further; count them all
+            it += todo;
+            ctrl = h[3];
+        }
+        if( rc ) break;
+        dim3 ge( 1024, g.ndim );
+        k_efield<<<ge, 256, 0, st>>>( g, phi, E, n, s + 8 );
+        for( int d = 0; d < g.ndim; d++ ) {
+            if( S->mixed ) k_efield_store<float><<<1024, 256, 0, st>>>( g, E, n, s + 8, static_cast<float *>( S->fptr[d] ), d );
+            else k_efield_store<double><<<1024, 256, 0, st>>>( g, E, n, s + 8, static_cast<double *>( S->fptr[d] ), d );
+        }
+        if( cudaGetLastError() != cudaSuccess ) { rc = set_error( SG_ERR_CUDA, "E from phi failed" ); break; }
+    } while( 0 );
+    release_async( mem, st );
+    if( cudaStreamSynchronize( st ) != cudaSuccess && rc == SG_OK ) rc = set_error( SG_ERR_CUDA, "Poisson solve failed" );
+    if( iterations ) *iterations = it;
+    if( ctrl_out ) *ctrl_out = ctrl;
+    drop_graphs( S );
+    return rc;
+}
+
+int sg_sim_charge_residual( sg_sim *S, double *residual, double *rho_max )
+{
+    SG_REQUIRE( S && residual, "NULL argument" );
+    const GridInfo &g = S->g;
+    cudaStream_t st = S->stream;
+    const int64_t n = phys_nodes( g );
+    const size_t nrho = ( size_t )ext( g, 0, 0 ) * ext( g, 1, 0 ) * ext( g, 2, 0 );
+    double *mem = nullptr;
+    SG_CUDA_TRY( cudaMallocAsync( &mem, ( nrho + 8 ) * sizeof( double ), st ) );
+    double *rho = mem, *s = mem + nrho;
+    unsigned long long *mx = reinterpret_cast<unsigned long long *>( s + 4 );
+    int rc = SG_OK;
+    do {
+        if( cudaMemsetAsync( s, 0, 8 * sizeof( double ), st ) != cudaSuccess ) { rc = set_error( SG_ERR_CUDA, "memset" ); break; }
+        if( ( rc = deposit_rho( S, rho ) ) ) break;
+        k_rho_sum<<<1024, 256, 0, st>>>( g, rho, n, s );
+        if( S->mixed )
+            k_residual<float><<<1024, 256, 0, st>>>( g, static_cast<float *>( S->fptr[0] ), static_cast<float *>( S->fptr[1] ), static_cast<float *>( S->fptr[2] ), rho, s, n, mx );
+        else
+            k_residual<double><<<1024, 256, 0, st>>>( g, static_cast<double *>( S->fptr[0] ), static_cast<double *>( S->fptr[1] ), static_cast<double *>( S->fptr[2] ), rho, s, n, mx );
+        if( cudaGetLastError() != cudaSuccess ) { rc = set_error( SG_ERR_CUDA, "residual launch failed" ); break; }
+    } while( 0 );
+    unsigned long long h[2] = { 0, 0 };
+    if( rc == SG_OK ) cudaMemcpyAsync( h, mx, sizeof( h ), cudaMemcpyDeviceToHost, st );
+    release_async( mem, st );
+    if( cudaStreamSynchronize( st ) != cudaSuccess && rc == SG_OK ) rc = set_error( SG_ERR_CUDA, "residual failed" );
+    if( rc ) return rc;
+    double m0, m1;
+    std::memcpy( &m0, &h[0], 8 );
+    std::memcpy( &m1, &h[1], 8 );
+    *residual = m1 > 0.0 ? m0 / m1 : m0;
+    if( rho_max ) *rho_max = m1;
     return SG_OK;
 }
 

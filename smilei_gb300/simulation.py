@@ -127,6 +127,25 @@ class Simulation:
         check(_lib.lib().sg_sim_energy(self._h, ctypes.byref(uk), ctypes.byref(ue)), "energy")
         return uk.value, ue.value
 
+    def rho(self) -> np.ndarray:
+        """FP64 charge density of all species (reference layout, primal, ghosts folded)."""
+        a = np.zeros(tuple(n + 5 for n in self.n_cells))
+        check(_lib.lib().sg_sim_get_rho(self._h, a.ctypes.data), "rho")
+        return a
+
+    def solve_poisson(self, max_error=1e-14, max_iter=50000):
+        """Initial E from the particles' charge (FP64 CG); returns (iterations, final r.r/n)."""
+        it, ctrl = ctypes.c_int(), ctypes.c_double()
+        check(_lib.lib().sg_sim_solve_poisson(self._h, float(max_error), int(max_iter), ctypes.byref(it),
+                                              ctypes.byref(ctrl)), "solve_poisson")
+        return it.value, ctrl.value
+
+    def charge_residual(self):
+        """max|div E - rho| / max|rho| (rho minus its mean) from the current particles, FP64."""
+        r, m = ctypes.c_double(), ctypes.c_double()
+        check(_lib.lib().sg_sim_charge_residual(self._h, ctypes.byref(r), ctypes.byref(m)), "charge_residual")
+        return r.value
+
     def last_timing(self):
         """Device ms of the last step: (particles, fields, total) and kernel launches per step."""
         a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()

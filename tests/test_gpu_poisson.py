@@ -1,0 +1,81 @@
+"""GPU charge density, FP64 Poisson solve and charge-conservation residual.
+
+rho: the simulation's FP64 deposit of all species against the oracle's basic()
+projection plus the periodic fold (1e-12).  Poisson: the GPU conjugate gradient
+against oracle/poisson.py on the same rho (E to 1e-8 relative: both CGs
+converge to r.r/n <= 1e-14 but along different rounding paths).  Residual:
+div E - rho stays at round-off through Esirkepov steps (FP64) and within
+the split-precision bound (mixed).
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+FIELDS = ["Ex", "Ey", "Ez", "Bx", "By", "Bz", "Bx_m", "By_m", "Bz_m", "Jx", "Jy", "Jz"]
+
+
+@pytest.fixture(scope="module")
+def mods():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from smilei_gb300 import simulation, synthetic
+    import oracle.poisson as P
+    return simulation, synthetic, P
+
+
+def plasma_sim(simulation, synthetic, form, ndim=3, seed=3, ppc=8, sigma=0.14):
+    n_cells = [16, 16, 12][:ndim] if ndim == 3 else [32, 24]
+    cl = [0.1] * ndim
+    dt = 0.95 / np.sqrt(sum(1.0 / c ** 2 for c in cl))
+    pos, mom, w = synthetic.thermal_plasma(n_cells, cl, ppc, sigma, seed)
+    sim = simulation.Simulation(n_cells, cl, dt, form=form)
+    sim.add_species(1.0, -1.0, "higueracary", pos, mom, w)
+    return sim, n_cells, cl, dt, pos, mom, w
+
+
+@pytest.mark.parametrize("ndim", [2, 3])
+def test_rho_matches_oracle(mods, cpu_oracle, ndim):
+    simulation, synthetic, P = mods
+    sim, n_cells, cl, dt, pos, mom, w = plasma_sim(simulation, synthetic, "fp64", ndim)
+    rho = sim.rho()
+    ref = np.zeros(tuple(n + 5 for n in n_cells))
+    n_prim = [n + 5 for n in n_cells]
+    cpu_oracle.project(2, ndim, n_prim, [-2] * ndim, cl, dt, pos, mom, w, np.full(w.shape, -1, np.int16),
+                       None, None, None, [None, None, None, ref])
+    cpu_oracle.fold_periodic(ndim, ref, [0, 0, 0], n_cells)
+    assert rel_err(rho, ref) <= 1e-12
+    sim.close()
+
+
+@pytest.mark.parametrize("form", ["fp64", "mixed"])
+def test_poisson_matches_oracle_and_zeroes_the_residual(mods, form):
+    simulation, synthetic, P = mods
+    sim, n_cells, cl, dt, pos, mom, w = plasma_sim(simulation, synthetic, form, 3)
+    it, ctrl = sim.solve_poisson()
+    assert ctrl <= 1e-14 and it > 0
+    rho = sim.rho()
+    phys = rho[2:2 + n_cells[0], 2:2 + n_cells[1], 2:2 + n_cells[2]]
+    _, E, it_ref, _ = P.solve_poisson(phys, cl)
+    tol = 1e-8 if form == "fp64" else 2e-6
+    for d, k in enumerate(("Ex", "Ey", "Ez")):
+        got = sim.get_field(k)[2:2 + n_cells[0], 2:2 + n_cells[1], 2:2 + n_cells[2]]
+        assert rel_err(got, E[d]) <= tol, k
+    res = sim.charge_residual()
+    assert res <= (1e-10 if form == "fp64" else 1e-5), res
+    sim.close()
+
+
+@pytest.mark.parametrize("form,limit", [("fp64", 1e-9), ("mixed", 1e-5)])
+def test_charge_residual_is_conserved_by_the_step(mods, form, limit):
+    simulation, synthetic, P = mods
+    sim, *_ = plasma_sim(simulation, synthetic, form, 3, sigma=0.3)
+    sim.solve_poisson()
+    r0 = sim.charge_residual()
+    sim.step(50)
+    r1 = sim.charge_residual()
+    assert r1 <= limit, (r0, r1)
+    sim.close()
