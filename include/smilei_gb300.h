@@ -200,6 +200,69 @@ int sg_sim_last_timing( sg_sim *sim, double *ms_particles, double *ms_fields, do
 /* Sets the stream the simulation runs on (default: a stream it creates). */
 int sg_sim_set_stream( sg_sim *sim, sg_stream_t stream );
 
+/* ---- Monte-Carlo radiation reaction ---- */
+
+typedef struct sg_rad_tables sg_rad_tables;
+typedef struct sg_mlp sg_mlp;
+
+/* Uploads the radiation tables (host arrays, FP64) in the reference's conventions
+ * (src/Radiation/Table.cpp:77-110; RadiationTables::initialization,
+ * src/Radiation/RadiationTables.cpp:41-200): integfochi[n_integ] on log10-spaced
+ * particle chi in [integ_min, integ_max]; xi[n_chi * n_ph] the cumulative photon-chi
+ * distribution per particle chi in [xi_min, xi_max]; axis1_min[n_chi] the log10 of
+ * each row's smallest photon chi.  factors = {factor_dNph_dt, factor_classical_radiated_power,
+ * inv_norm_E_Schwinger, minimum_chi_continuous, minimum_chi_discontinuous}. */
+int sg_rad_tables_create( const double *integ, int n_integ, double integ_min, double integ_max, const double *xi,
+                          int n_chi, int n_ph, double xi_min, double xi_max, const double *axis1_min,
+                          const double *factors, sg_rad_tables **out );
+int sg_rad_tables_destroy( sg_rad_tables *tables );
+
+/* Inverse CDF (particle chi, xi) -> photon chi: replaces
+ * RadiationTables::computeRandomPhotonChiWithInterpolation (RadiationTables.cpp:375). */
+int sg_rad_photon_chi( const sg_rad_tables *tables, int64_t n, const double *chi, const double *xi, double *out,
+                       sg_stream_t stream );
+
+/* dN_photon/dt: replaces RadiationTables::computePhotonProductionYield (RadiationTables.cpp:225). */
+int sg_rad_production_yield( const sg_rad_tables *tables, int64_t n, const double *chi, const double *gamma,
+                             double *out, sg_stream_t stream );
+
+/* One Monte-Carlo radiation pass over n particles (device arrays: mom[3n] updated,
+ * weight[n], tau[n] optical depth updated, chi_out[n] optional, Epart/Bpart[3n] the
+ * interpolated fields): replaces RadiationMonteCarlo::operator()
+ * (src/Radiation/RadiationMonteCarlo.cpp:62, called from Species.cpp:615) with the
+ * emitted energy tallied instead of macro-photons created.  Particle p draws from its
+ * own counter-based stream (seed, first_id + p, step).  radiated (device double) and
+ * n_emissions (device) are accumulated.  mlp: NULL for the table inverse CDF, or a
+ * validated network (sg_mlp_validate) used wherever its checked error is within
+ * tolerance. */
+int sg_rad_monte_carlo( const sg_rad_tables *tables, const sg_mlp *mlp, int64_t n, double dt, double mass,
+                        double charge, double *mom, const double *weight, double *tau, double *chi_out,
+                        const double *Epart, const double *Bpart, uint32_t seed, uint32_t first_id, uint32_t step,
+                        double *radiated, unsigned long long *n_emissions, sg_stream_t stream );
+
+/* The learned inverse CDF: an FP32 MLP 2 -> hidden -> hidden -> 1 (tanh) from
+ * (log10 chi normalised to [log10_chi_min, log10_chi_max], xi) to
+ * log10(photon chi / chi) / 8.  Trained on the GPU (forward, backward, batch
+ * gradient reduction, Adam) on samples whose targets are the table inverse CDF. */
+int sg_mlp_create( int hidden, uint32_t seed, double log10_chi_min, double log10_chi_max, sg_mlp **out );
+int sg_mlp_destroy( sg_mlp *mlp );
+int sg_mlp_nparams( const sg_mlp *mlp, int *n );
+int sg_mlp_get_params( const sg_mlp *mlp, float *host );
+int sg_mlp_set_params( sg_mlp *mlp, const float *host );
+/* Gradient of the mean-squared loss over a host batch (inputs[2B] normalised, targets[B]). */
+int sg_mlp_gradients( sg_mlp *mlp, int batch, const float *inputs, const float *targets, float *grad, float *loss );
+/* steps of Adam on fresh table samples of the given batch size; final_loss optional. */
+int sg_mlp_train( sg_mlp *mlp, const sg_rad_tables *tables, int steps, int batch, float lr, uint32_t seed,
+                  float *final_loss, sg_stream_t stream );
+/* Measures max |log10 mlp - log10 table| on per_bin^2 points of each of the
+ * n_chi_bins x n_xi_bins bins and masks (falls back to the table on) every bin
+ * above tol.  err_out[n_chi_bins * n_xi_bins] optional. */
+int sg_mlp_validate( sg_mlp *mlp, const sg_rad_tables *tables, int n_chi_bins, int n_xi_bins, int per_bin,
+                     float tol, float *err_out, int *n_masked );
+/* Network inverse CDF alone (no fallback), device arrays. */
+int sg_mlp_photon_chi( const sg_mlp *mlp, int64_t n, const double *chi, const double *xi, double *out,
+                       sg_stream_t stream );
+
 #ifdef __cplusplus
 }
 #endif

@@ -261,3 +261,102 @@ class RefOps(_Backend):
         chi = _f64(chi); xi = _f64(xi); out = np.zeros_like(chi)
         self.lib.ref_rad_photon_chi(len(chi), _ptr(chi), _ptr(xi), _ptr(out))
         return out
+
+
+class RadTablesC(ctypes.Structure):
+    """Mirror of or_rad_tables in rad_oracle.c."""
+    _fields_ = [("integ", ctypes.c_void_p), ("n_integ", ctypes.c_int), ("integ_log10_min", ctypes.c_double),
+                ("integ_delta", ctypes.c_double), ("integ_inv_delta", ctypes.c_double),
+                ("xi", ctypes.c_void_p), ("n_chi", ctypes.c_int), ("n_ph", ctypes.c_int),
+                ("xi_log10_min", ctypes.c_double), ("xi_delta", ctypes.c_double), ("xi_inv_delta", ctypes.c_double),
+                ("inv_nph_m1", ctypes.c_double), ("axis1_min", ctypes.c_void_p),
+                ("factor_dNph_dt", ctypes.c_double), ("factor_classical", ctypes.c_double),
+                ("min_chi_continuous", ctypes.c_double), ("min_chi_discontinuous", ctypes.c_double),
+                ("inv_norm_E_schwinger", ctypes.c_double)]
+
+
+class RadTables:
+    """Monte-Carlo radiation tables in the reference's conventions (src/Radiation/Table.cpp:77-110).
+
+    integfochi[n] on log10-spaced chi in [integ_min, integ_max]; xi[n_chi, n_ph] with the
+    per-row log10 of the minimum photon chi (axis1_min); physical factors as
+    RadiationTables::initialization computes them (RadiationTables.cpp:92-103)."""
+
+    def __init__(self, integfochi, integ_min, integ_max, xi, xi_min, xi_max, axis1_min,
+                 factor_dNph_dt=1.0, factor_classical=1.0, inv_norm_E_schwinger=1.0,
+                 min_chi_continuous=1e-3, min_chi_discontinuous=1e-2):
+        self.integfochi = _f64(integfochi)
+        self.xi = _f64(xi)
+        self.axis1_min = _f64(axis1_min)
+        self.integ_min, self.integ_max = float(integ_min), float(integ_max)
+        self.xi_min, self.xi_max = float(xi_min), float(xi_max)
+        self.factor_dNph_dt = float(factor_dNph_dt)
+        self.factor_classical = float(factor_classical)
+        self.inv_norm_E_schwinger = float(inv_norm_E_schwinger)
+        self.min_chi_continuous = float(min_chi_continuous)
+        self.min_chi_discontinuous = float(min_chi_discontinuous)
+
+    @staticmethod
+    def axis(vmin, vmax, n):
+        lmin = np.log10(vmin) if vmin != 0 else 0.0
+        delta = (np.log10(vmax) - lmin) / (n - 1)
+        return lmin, delta, 1.0 / delta
+
+    def c_struct(self) -> RadTablesC:
+        t = RadTablesC()
+        t.integ = self.integfochi.ctypes.data
+        t.n_integ = len(self.integfochi)
+        t.integ_log10_min, t.integ_delta, t.integ_inv_delta = self.axis(self.integ_min, self.integ_max,
+                                                                         len(self.integfochi))
+        t.xi = self.xi.ctypes.data
+        t.n_chi, t.n_ph = self.xi.shape
+        t.xi_log10_min, t.xi_delta, t.xi_inv_delta = self.axis(self.xi_min, self.xi_max, self.xi.shape[0])
+        t.inv_nph_m1 = 1.0 / (self.xi.shape[1] - 1)
+        t.axis1_min = self.axis1_min.ctypes.data
+        t.factor_dNph_dt = self.factor_dNph_dt
+        t.factor_classical = self.factor_classical
+        t.min_chi_continuous = self.min_chi_continuous
+        t.min_chi_discontinuous = self.min_chi_discontinuous
+        t.inv_norm_E_schwinger = self.inv_norm_E_schwinger
+        return t
+
+    @classmethod
+    def from_golden(cls, g, **kw):
+        return cls(g["integfochi"], g["integfochi_min"], g["integfochi_max"], g["xi_table"], g["xi_min"],
+                   g["xi_max"], g["xi_axis1_min"], **kw)
+
+
+def _rad_lib():
+    L = Oracle().lib
+    L.or_rad_monte_carlo.restype = ctypes.c_double
+    L.or_rng_init.restype = ctypes.c_uint32
+    return L
+
+
+def rad_yield(tables: RadTables, chi, gamma):
+    chi = _f64(chi); gamma = _f64(gamma); out = np.zeros_like(chi)
+    ts = tables.c_struct()
+    _rad_lib().or_rad_yield_n(ctypes.byref(ts), ctypes.c_int64(len(chi)), _ptr(chi), _ptr(gamma), _ptr(out))
+    return out
+
+
+def rad_photon_chi(tables: RadTables, chi, xi):
+    chi = _f64(chi); xi = _f64(xi); out = np.zeros_like(chi)
+    ts = tables.c_struct()
+    _rad_lib().or_rad_photon_chi_n(ctypes.byref(ts), ctypes.c_int64(len(chi)), _ptr(chi), _ptr(xi), _ptr(out))
+    return out
+
+
+def rad_monte_carlo(tables: RadTables, dt, mass, charge, mom, weight, tau, E, B, seed, first_id=0, step=0):
+    """One Monte-Carlo radiation pass; mom and tau updated in place.  Returns (radiated, n_emissions, chi)."""
+    n = mom.shape[1]
+    assert mom.dtype == np.float64 and mom.flags.c_contiguous and tau.dtype == np.float64
+    chi = np.zeros(n)
+    nem = ctypes.c_int64()
+    ts = tables.c_struct()
+    rad = _rad_lib().or_rad_monte_carlo(ctypes.byref(ts), ctypes.c_int64(n), ctypes.c_double(dt),
+                                        ctypes.c_double(mass), ctypes.c_double(charge), _ptr(mom),
+                                        _ptr(_f64(weight)), _ptr(tau), _ptr(chi), _ptr(_f64(E)), _ptr(_f64(B)),
+                                        ctypes.c_uint32(seed), ctypes.c_uint32(first_id), ctypes.c_uint32(step),
+                                        ctypes.byref(nem))
+    return rad, nem.value, chi

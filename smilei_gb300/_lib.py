@@ -76,6 +76,21 @@ _SIGNATURES = {
     "sg_sim_set_stream": (_I, [_VP, _VP]),
     "sg_sim_state_bytes": (_I, [_VP, _I, ctypes.POINTER(ctypes.c_size_t)]),
     "sg_sim_get_rho": (_I, [_VP, _VP]),
+    "sg_rad_tables_create": (_I, [_VP, _I, _D, _D, _VP, _I, _I, _D, _D, _VP, _VP, ctypes.POINTER(_VP)]),
+    "sg_rad_tables_destroy": (_I, [_VP]),
+    "sg_rad_photon_chi": (_I, [_VP, _I64, _VP, _VP, _VP, _VP]),
+    "sg_rad_production_yield": (_I, [_VP, _I64, _VP, _VP, _VP, _VP]),
+    "sg_rad_monte_carlo": (_I, [_VP, _VP, _I64, _D, _D, _D, _VP, _VP, _VP, _VP, _VP, _VP, ctypes.c_uint32,
+                                ctypes.c_uint32, ctypes.c_uint32, _VP, _VP, _VP]),
+    "sg_mlp_create": (_I, [_I, ctypes.c_uint32, _D, _D, ctypes.POINTER(_VP)]),
+    "sg_mlp_destroy": (_I, [_VP]),
+    "sg_mlp_nparams": (_I, [_VP, ctypes.POINTER(_I)]),
+    "sg_mlp_get_params": (_I, [_VP, _VP]),
+    "sg_mlp_set_params": (_I, [_VP, _VP]),
+    "sg_mlp_gradients": (_I, [_VP, _I, _VP, _VP, _VP, _VP]),
+    "sg_mlp_train": (_I, [_VP, _VP, _I, _I, ctypes.c_float, ctypes.c_uint32, _VP, _VP]),
+    "sg_mlp_validate": (_I, [_VP, _VP, _I, _I, _I, ctypes.c_float, _VP, ctypes.POINTER(_I)]),
+    "sg_mlp_photon_chi": (_I, [_VP, _I64, _VP, _VP, _VP, _VP]),
     "sg_sim_solve_poisson": (_I, [_VP, _D, _I, ctypes.POINTER(_I), ctypes.POINTER(_D)]),
     "sg_sim_charge_residual": (_I, [_VP, ctypes.POINTER(_D), ctypes.POINTER(_D)]),
     "sg_sim_copy_state": (_I, [_VP, _I, _VP, _I]),

@@ -1,0 +1,716 @@
+// Monte-Carlo radiation reaction and its learned inverse-CDF surrogate.
+//
+// Tables (FP64, the reference's conventions, src/Radiation/Table.cpp:77-110):
+//   integfochi[n]            on log10-spaced chi in [min, max]
+//   xi[n_chi, n_ph]          cumulative photon-chi distribution per particle chi
+//   axis1_min[n_chi]         log10 of the smallest photon chi of each row
+// Kernels:
+//   photon-chi inverse CDF   RadiationTables::computeRandomPhotonChiWithInterpolation
+//                            (src/Radiation/RadiationTables.cpp:375-512)
+//   production yield         computePhotonProductionYield (:225-262)
+//   Monte-Carlo pass         RadiationMonteCarlo::operator() (src/Radiation/RadiationMonteCarlo.cpp:62-611),
+//                            emitted energy tallied (no macro-photons)
+// Learned part: an FP32 MLP 2 -> H -> H -> 1 (tanh) maps (log10 chi, xi) to
+// log10(photon chi / chi).  It is trained on the GPU by the kernels below
+// (forward, backward, batch-reduced weight gradients, Adam) on samples whose
+// targets come from the table kernel, validated per (chi, xi) bin against the
+// table, and used in the Monte-Carlo pass only where its measured error is
+// within tolerance; elsewhere the table answers.
+//
+// Random numbers: each particle draws from its own counter-based stream,
+// fmix32(seed ^ fmix32(id) ^ fmix32(step + 0x9e3779b9)) (MurmurHash3's 32-bit
+// finaliser) advanced by xorshift32 (Marsaglia 2003, as the reference's
+// src/Tools/Random.h:9-20) and mapped to [0, 1) by x * (1 - 1e-11) / 2^32.
+
+#include "common.cuh"
+
+#include <cmath>
+#include <vector>
+
+namespace sg {
+namespace {
+
+struct RadTab {
+    const double *integ;
+    int n_integ;
+    double integ_l0, integ_d, integ_id;
+    const double *xi;
+    int n_chi, n_ph;
+    double xi_l0, xi_d, xi_id, inv_nph_m1;
+    const double *axis1_min;
+    double factor_dNph_dt, factor_classical, min_cont, min_disc, inv_es;
+};
+
+__host__ __device__ inline uint32_t fmix32( uint32_t h )
+{
+    h ^= h >> 16;
+    h *= 0x85ebca6bu;
+    h ^= h >> 13;
+    h *= 0xc2b2ae35u;
+    h ^= h >> 16;
+    return h;
+}
+
+__device__ __forceinline__ uint32_t rng_init( uint32_t seed, uint32_t id, uint32_t step )
+{
+    const uint32_t s = fmix32( seed ^ fmix32( id ) ^ fmix32( step + 0x9e3779b9u ) );
+    return s ? s : 0xffffffffu;
+}
+
+__device__ __forceinline__ double rng_uniform( uint32_t &s )
+{
+    s ^= s << 13;
+    s ^= s >> 17;
+    s ^= s << 5;
+    return ( double )s * ( ( 1.0 - 1e-11 ) / 4294967296.0 );
+}
+
+// userFunctions::searchValuesInMonotonicArray (src/Tools/userFunctions.h:248-272)
+__device__ __forceinline__ int search_monotonic( const double *__restrict__ a, double v, int n )
+{
+    int imin = 0, imax = n - 1;
+    if( v == a[0] ) return 0;
+    if( v == a[n - 1] ) return n - 2;
+    while( imax - imin > 1 ) {
+        const int imid = ( imin + imax ) / 2;
+        if( v >= a[imid] ) imin = imid;
+        else imax = imid;
+    }
+    return imin;
+}
+
+__device__ double tab_yield( const RadTab &t, double chi, double gamma )
+{
+    const double lc = log10( chi );
+    const int i = ( int )floor( ( lc - t.integ_l0 ) * t.integ_id );
+    double v;
+    if( i < 0 ) v = t.integ[0];
+    else if( i >= t.n_integ - 1 ) v = t.integ[t.n_integ - 2];
+    else {
+        const double lm = i * t.integ_d + t.integ_l0, lp = lm + t.integ_d;
+        v = ( t.integ[i + 1] * fabs( lc - lm ) + t.integ[i] * fabs( lp - lc ) ) * t.integ_id;
+    }
+    return t.factor_dNph_dt * v * chi / gamma;
+}
+
+__device__ double tab_photon_chi( const RadTab &t, double chi, double xi )
+{
+    const int n1 = t.n_ph;
+    const double lc = log10( chi );
+    int ic = ( int )floor( ( lc - t.xi_l0 ) * t.xi_id );
+    if( ic < 0 ) ic = 0;
+    else if( ic > t.n_chi - 2 ) ic = t.n_chi - 2;
+    int i1, i2;
+    if( xi <= t.xi[ic * n1] ) {
+        i1 = 0;
+        i2 = 0;
+        xi = t.xi[ic * n1];
+    } else {
+        i1 = search_monotonic( &t.xi[ic * n1], xi, n1 );
+        i2 = search_monotonic( &t.xi[( ic + 1 ) * n1], xi, n1 );
+    }
+    const double dchi = ( lc - ( ic * t.xi_d + t.xi_l0 ) ) * t.xi_id;
+    const double d1 = ( ic * t.xi_d + t.xi_l0 - t.axis1_min[ic] ) * t.inv_nph_m1;
+    const double d2 = ( ( ic + 1 ) * t.xi_d + t.xi_l0 - t.axis1_min[ic + 1] ) * t.inv_nph_m1;
+    const int x1 = ic * n1 + i1, x2 = ( ic + 1 ) * n1 + i2;
+    double p1, p2;
+    if( t.xi[x1] < 1.0 && t.xi[x1 + 1] - t.xi[x1] > 1e-15 ) {
+        const double lm = i1 * d1 + t.axis1_min[ic], lp = lm + d1;
+        const double d = ( xi - t.xi[x1] ) / ( t.xi[x1 + 1] - t.xi[x1] );
+        p1 = lm * ( 1.0 - d ) + lp * d;
+    } else {
+        p1 = i1 * d1 + t.axis1_min[ic];
+    }
+    if( t.xi[x2] < 1.0 && t.xi[x2 + 1] - t.xi[x2] > 1e-15 ) {
+        const double lm = i2 * d2 + t.axis1_min[ic + 1], lp = lm + d2;
+        const double d = ( xi - t.xi[x2] ) / ( t.xi[x2 + 1] - t.xi[x2] );
+        p2 = lm * ( 1.0 - d ) + lp * d;
+    } else {
+        p2 = i2 * d2 + t.axis1_min[ic + 1];
+    }
+    return pow( 10.0, p1 * ( 1 - dchi ) + p2 * dchi );
+}
+
+// ---- the MLP ----------------------------------------------------------------
+constexpr int MLP_MAX_H = 128;
+
+struct MlpView {
+    int H;
+    const float *W1, *b1, *W2, *b2, *W3, *b3; // W1[H][2] W2[H][H] W3[H]
+    float lmin, lspan;                         // input normalisation of log10 chi
+    float out_scale;                           // network output * out_scale = log10(photon chi / chi)
+    const int *mask;                           // fallback mask [nbc][nbx] (1 = use the table)
+    int nbc, nbx;
+};
+
+__host__ __device__ inline int mlp_nparams( int H ) { return H * H + 5 * H + 1; }
+
+// Forward pass of one sample; optional activations out.
+__device__ __forceinline__ float mlp_forward( const MlpView &m, float u0, float u1, float *h1, float *h2 )
+{
+    const int H = m.H;
+    for( int i = 0; i < H; i++ ) h1[i] = tanhf( m.W1[2 * i] * u0 + m.W1[2 * i + 1] * u1 + m.b1[i] );
+    float y = m.b3[0];
+    for( int i = 0; i < H; i++ ) {
+        float a = m.b2[i];
+        const float *w = m.W2 + i * H;
+        for( int j = 0; j < H; j++ ) a = fmaf( w[j], h1[j], a );
+        h2[i] = tanhf( a );
+        y = fmaf( m.W3[i], h2[i], y );
+    }
+    return y;
+}
+
+__device__ __forceinline__ void mlp_inputs( const MlpView &m, double chi, double xi, float &u0, float &u1 )
+{
+    u0 = 2.0f * ( ( float )log10( chi ) - m.lmin ) / m.lspan - 1.0f;
+    u1 = 2.0f * ( float )xi - 1.0f;
+}
+
+__device__ double mlp_photon_chi( const MlpView &m, double chi, double xi )
+{
+    float h1[MLP_MAX_H], h2[MLP_MAX_H];
+    float u0, u1;
+    mlp_inputs( m, chi, xi, u0, u1 );
+    const float y = mlp_forward( m, u0, u1, h1, h2 );
+    return chi * pow( 10.0, ( double )( y * m.out_scale ) );
+}
+
+__device__ __forceinline__ bool mlp_masked( const MlpView &m, double chi, double xi )
+{
+    float u0 = ( ( float )log10( chi ) - m.lmin ) / m.lspan;
+    int bc = ( int )floorf( u0 * m.nbc ), bx = ( int )floor( xi * m.nbx );
+    if( bc < 0 || bc >= m.nbc ) return true; // outside the trained range
+    bx = bx < 0 ? 0 : ( bx >= m.nbx ? m.nbx - 1 : bx );
+    return m.mask[bc * m.nbx + bx] != 0;
+}
+
+// ---- kernels ------------------------------------------------------------------
+__global__ void k_photon_chi( RadTab t, int64_t n, const double *__restrict__ chi, const double *__restrict__ xi,
+                              double *__restrict__ out )
+{
+    const int64_t i = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x;
+    if( i < n ) out[i] = tab_photon_chi( t, chi[i], xi[i] );
+}
+
+__global__ void k_yield( RadTab t, int64_t n, const double *__restrict__ chi, const double *__restrict__ g,
+                         double *__restrict__ out )
+{
+    const int64_t i = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x;
+    if( i < n ) out[i] = tab_yield( t, chi[i], g[i] );
+}
+
+__global__ void k_mlp_photon_chi( MlpView m, int64_t n, const double *__restrict__ chi, const double *__restrict__ xi,
+                                  double *__restrict__ out )
+{
+    const int64_t i = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x;
+    if( i < n ) out[i] = mlp_photon_chi( m, chi[i], xi[i] );
+}
+
+// RadiationMonteCarlo::operator() per particle (see the file header).
+__global__ void k_monte_carlo( RadTab t, MlpView m, int use_mlp, int64_t n, double dt, double qm2,
+                               double *__restrict__ mom, const double *__restrict__ w, double *__restrict__ tau,
+                               double *__restrict__ chi_out, const double *__restrict__ Ep,
+                               const double *__restrict__ Bp, uint32_t seed, uint32_t first_id, uint32_t step,
+                               double *__restrict__ radiated, unsigned long long *__restrict__ n_emit )
+{
+    const int64_t p = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x;
+    double rad = 0.0;
+    unsigned long long nem = 0;
+    if( p < n ) {
+        double px = mom[p], py = mom[n + p], pz = mom[2 * n + p];
+        const double Ex = Ep[p], Ey = Ep[n + p], Ez = Ep[2 * n + p];
+        const double Bx = Bp[p], By = Bp[n + p], Bz = Bp[2 * n + p];
+        double tp = tau[p];
+        uint32_t rs = rng_init( seed, first_id + ( uint32_t )p, step );
+        double local_time = 0.0, emission_time = 0.0, last_chi = 0.0;
+        int it = 0;
+        const double eps_tau = 1e-100;
+        while( local_time < dt && it < 100 ) {
+            const double g = sqrt( 1.0 + px * px + py * py + pz * pz );
+            if( g < 1.1 ) break;
+            const double a = Ex * px + Ey * py + Ez * pz;
+            const double b = g * Ex - By * pz + Bz * py;
+            const double c = g * Ey - Bz * px + Bx * pz;
+            const double d = g * Ez - Bx * py + By * px;
+            const double chi = fabs( qm2 ) * t.inv_es * sqrt( fabs( a * a - b * b - c * c - d * d ) );
+            last_chi = chi;
+            if( chi > t.min_disc && tp <= eps_tau ) {
+                while( tp <= eps_tau ) tp = -log( 1.0 - rng_uniform( rs ) );
+            }
+            if( tp > eps_tau ) {
+                const double rate = tab_yield( t, chi, g );
+                emission_time = fmin( tp / rate, dt - local_time );
+                tp -= rate * emission_time;
+                if( tp <= eps_tau ) {
+                    const double u = rng_uniform( rs );
+                    const double pchi = ( use_mlp && !mlp_masked( m, chi, u ) ) ? mlp_photon_chi( m, chi, u )
+                                                                               : tab_photon_chi( t, chi, u );
+                    const double pg = pchi / chi * ( g - 1.0 );
+                    const double f = pg / sqrt( g * g - 1.0 );
+                    px -= px * f;
+                    py -= py * f;
+                    pz -= pz * f;
+                    rad += w[p] * ( g - sqrt( 1.0 + px * px + py * py + pz * pz ) );
+                    nem++;
+                    tp = -1.0;
+                }
+                it++;
+                local_time += emission_time;
+            } else if( chi <= t.min_disc && tp <= eps_tau && chi > t.min_cont ) {
+                emission_time = dt - local_time;
+                const double aa = 1.0 + 4.8 * ( 1.0 + chi ) * log( 1.0 + 1.7 * chi ) + 2.44 * chi * chi;
+                const double e = ( 1.0 / cbrt( aa * aa ) ) * emission_time * chi * chi * t.factor_classical;
+                const double tmp = e * g / ( g * g - 1.0 );
+                px -= tmp * px;
+                py -= tmp * py;
+                pz -= tmp * pz;
+                rad += w[p] * ( g - sqrt( 1.0 + px * px + py * py + pz * pz ) );
+                local_time = dt;
+            } else {
+                local_time = dt;
+            }
+        }
+        mom[p] = px;
+        mom[n + p] = py;
+        mom[2 * n + p] = pz;
+        tau[p] = tp;
+        if( chi_out ) chi_out[p] = last_chi;
+    }
+    // block reduction of the tallies
+    __shared__ double srad[32];
+    __shared__ unsigned long long snem[32];
+    for( int o = 16; o > 0; o >>= 1 ) {
+        rad += __shfl_down_sync( 0xffffffffu, rad, o );
+        nem += __shfl_down_sync( 0xffffffffu, nem, o );
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if( lane == 0 ) { srad[warp] = rad; snem[warp] = nem; }
+    __syncthreads();
+    if( threadIdx.x == 0 ) {
+        double r = 0.0;
+        unsigned long long e = 0;
+        for( int k = 0; k < ( int )( blockDim.x >> 5 ); k++ ) { r += srad[k]; e += snem[k]; }
+        if( r != 0.0 ) atomicAdd( radiated, r );
+        if( e ) atomicAdd( n_emit, e );
+    }
+}
+
+// ---- MLP training ------------------------------------------------------------
+// Samples: log10 chi uniform in [lmin, lmin + lspan], xi uniform in [0, 1);
+// target = log10(table photon chi / chi) / out_scale.
+__global__ void k_mlp_samples( RadTab t, int B, float lmin, float lspan, float out_scale, uint32_t seed,
+                               uint32_t step, float *__restrict__ X, float *__restrict__ Y )
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if( b >= B ) return;
+    uint32_t rs = rng_init( seed, ( uint32_t )b, step );
+    const double l = lmin + lspan * rng_uniform( rs );
+    const double xi = rng_uniform( rs );
+    const double chi = pow( 10.0, l );
+    const double pc = tab_photon_chi( t, chi, xi );
+    X[2 * b] = 2.0f * ( float )( ( l - lmin ) / lspan ) - 1.0f;
+    X[2 * b + 1] = 2.0f * ( float )xi - 1.0f;
+    Y[b] = ( float )( log10( pc / chi ) / out_scale );
+}
+
+// Forward + backward per sample for the mean-squared loss; stores h1, h2 and the
+// deltas of both hidden layers for the weight-gradient reduction.
+__global__ void k_mlp_fwd_bwd( MlpView m, int B, const float *__restrict__ X, const float *__restrict__ Y,
+                               float *__restrict__ H1, float *__restrict__ H2, float *__restrict__ D1,
+                               float *__restrict__ D2, float *__restrict__ D3, float *__restrict__ loss )
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const int H = m.H;
+    float l = 0.0f;
+    if( b < B ) {
+        float h1[MLP_MAX_H], h2[MLP_MAX_H], d2[MLP_MAX_H];
+        const float u0 = X[2 * b], u1 = X[2 * b + 1];
+        const float y = mlp_forward( m, u0, u1, h1, h2 );
+        const float e = y - Y[b];
+        l = e * e;
+        const float d3 = 2.0f * e / ( float )B;
+        D3[b] = d3;
+        for( int i = 0; i < H; i++ ) {
+            d2[i] = m.W3[i] * d3 * ( 1.0f - h2[i] * h2[i] );
+            H1[( int64_t )b * H + i] = h1[i];
+            H2[( int64_t )b * H + i] = h2[i];
+            D2[( int64_t )b * H + i] = d2[i];
+        }
+        for( int j = 0; j < H; j++ ) {
+            float a = 0.0f;
+            for( int i = 0; i < H; i++ ) a = fmaf( m.W2[i * H + j], d2[i], a );
+            D1[( int64_t )b * H + j] = a * ( 1.0f - h1[j] * h1[j] );
+        }
+    }
+    for( int o = 16; o > 0; o >>= 1 ) l += __shfl_down_sync( 0xffffffffu, l, o );
+    if( ( threadIdx.x & 31 ) == 0 && loss ) atomicAdd( loss, l / ( float )B );
+}
+
+// One thread per parameter: the gradient as a sum over the batch (deterministic order).
+__global__ void k_mlp_grads( int H, int B, const float *__restrict__ X, const float *__restrict__ H1,
+                             const float *__restrict__ H2, const float *__restrict__ D1, const float *__restrict__ D2,
+                             const float *__restrict__ D3, float *__restrict__ G )
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int P = mlp_nparams( H );
+    if( k >= P ) return;
+    // layout: W1[H*2] b1[H] W2[H*H] b2[H] W3[H] b3[1]
+    float acc = 0.0f;
+    if( k < 2 * H ) {
+        const int i = k / 2, c = k % 2;
+        for( int b = 0; b < B; b++ ) acc = fmaf( D1[( int64_t )b * H + i], X[2 * b + c], acc );
+    } else if( k < 3 * H ) {
+        const int i = k - 2 * H;
+        for( int b = 0; b < B; b++ ) acc += D1[( int64_t )b * H + i];
+    } else if( k < 3 * H + H * H ) {
+        const int q = k - 3 * H, i = q / H, j = q % H;
+        for( int b = 0; b < B; b++ ) acc = fmaf( D2[( int64_t )b * H + i], H1[( int64_t )b * H + j], acc );
+    } else if( k < 4 * H + H * H ) {
+        const int i = k - 3 * H - H * H;
+        for( int b = 0; b < B; b++ ) acc += D2[( int64_t )b * H + i];
+    } else if( k < 5 * H + H * H ) {
+        const int j = k - 4 * H - H * H;
+        for( int b = 0; b < B; b++ ) acc = fmaf( D3[b], H2[( int64_t )b * H + j], acc );
+    } else {
+        for( int b = 0; b < B; b++ ) acc += D3[b];
+    }
+    G[k] = acc;
+}
+
+// Adam (Kingma & Ba 2015) with bias correction.
+__global__ void k_adam( int P, float *__restrict__ w, const float *__restrict__ g, float *__restrict__ m1,
+                        float *__restrict__ m2, float lr, float b1, float b2, float eps, int t )
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if( k >= P ) return;
+    const float gk = g[k];
+    const float a = b1 * m1[k] + ( 1.0f - b1 ) * gk;
+    const float c = b2 * m2[k] + ( 1.0f - b2 ) * gk * gk;
+    m1[k] = a;
+    m2[k] = c;
+    const float ah = a / ( 1.0f - powf( b1, ( float )t ) ), ch = c / ( 1.0f - powf( b2, ( float )t ) );
+    w[k] -= lr * ah / ( sqrtf( ch ) + eps );
+}
+
+// Validation: per (chi bin, xi bin), the largest |log10 mlp - log10 table| over a
+// regular sub-grid of the bin.
+__global__ void k_mlp_validate( RadTab t, MlpView m, int per_bin, float *__restrict__ err )
+{
+    const int bin = blockIdx.x;
+    const int bc = bin / m.nbx, bx = bin % m.nbx;
+    float e = 0.0f;
+    for( int s = threadIdx.x; s < per_bin * per_bin; s += blockDim.x ) {
+        const int sc = s / per_bin, sx = s % per_bin;
+        const double l = m.lmin + m.lspan * ( bc + ( sc + 0.5 ) / per_bin ) / m.nbc;
+        const double xi = ( bx + ( sx + 0.5 ) / per_bin ) / m.nbx;
+        const double chi = pow( 10.0, l );
+        const double a = log10( mlp_photon_chi( m, chi, xi ) ), b = log10( tab_photon_chi( t, chi, xi ) );
+        e = fmaxf( e, ( float )fabs( a - b ) );
+    }
+    for( int o = 16; o > 0; o >>= 1 ) e = fmaxf( e, __shfl_down_sync( 0xffffffffu, e, o ) );
+    __shared__ float se[32];
+    if( ( threadIdx.x & 31 ) == 0 ) se[threadIdx.x >> 5] = e;
+    __syncthreads();
+    if( threadIdx.x == 0 ) {
+        float r = 0.0f;
+        for( int k = 0; k < ( int )( blockDim.x >> 5 ); k++ ) r = fmaxf( r, se[k] );
+        err[bin] = r;
+    }
+}
+
+} // namespace
+} // namespace sg
+
+using namespace sg;
+
+struct sg_rad_tables {
+    RadTab t;
+    double *mem = nullptr;
+};
+
+struct sg_mlp {
+    int H = 64;
+    float *params = nullptr; // device, nparams
+    float *m1 = nullptr, *m2 = nullptr, *grad = nullptr;
+    int adam_t = 0;
+    float lmin = -4.0f, lspan = 7.0f, out_scale = 8.0f;
+    int *mask = nullptr; // device
+    int nbc = 0, nbx = 0;
+    float *scratch = nullptr;
+    int scratch_B = 0;
+};
+
+namespace {
+
+MlpView view( const sg_mlp *m )
+{
+    MlpView v;
+    v.H = m->H;
+    const int H = m->H;
+    v.W1 = m->params;
+    v.b1 = v.W1 + 2 * H;
+    v.W2 = v.b1 + H;
+    v.b2 = v.W2 + H * H;
+    v.W3 = v.b2 + H;
+    v.b3 = v.W3 + H;
+    v.lmin = m->lmin;
+    v.lspan = m->lspan;
+    v.out_scale = m->out_scale;
+    v.mask = m->mask;
+    v.nbc = m->nbc;
+    v.nbx = m->nbx;
+    return v;
+}
+
+int ensure_scratch( sg_mlp *m, int B )
+{
+    if( m->scratch_B >= B ) return SG_OK;
+    release( m->scratch );
+    m->scratch = nullptr;
+    const size_t floats = ( size_t )B * ( 4 * m->H + 4 ) + 64;
+    SG_CUDA_TRY( cudaMalloc( &m->scratch, floats * sizeof( float ) ) );
+    m->scratch_B = B;
+    return SG_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int sg_rad_tables_create( const double *integ, int n_integ, double integ_min, double integ_max, const double *xi,
+                          int n_chi, int n_ph, double xi_min, double xi_max, const double *axis1_min,
+                          const double *factors, sg_rad_tables **out )
+{
+    SG_REQUIRE( integ && xi && axis1_min && factors && out, "NULL argument" );
+    SG_REQUIRE( n_integ >= 2 && n_chi >= 2 && n_ph >= 2, "tables need at least two points per axis" );
+    SG_REQUIRE( integ_min > 0 && integ_max > integ_min && xi_min > 0 && xi_max > xi_min, "bad table range" );
+    sg_rad_tables *T = new sg_rad_tables();
+    const size_t n = ( size_t )n_integ + ( size_t )n_chi * n_ph + n_chi;
+    cudaError_t e = cudaMalloc( &T->mem, n * sizeof( double ) );
+    if( e != cudaSuccess ) { delete T; return set_error( SG_ERR_NOMEM, "cannot allocate the radiation tables" ); }
+    double *d_integ = T->mem, *d_xi = d_integ + n_integ, *d_ax = d_xi + ( size_t )n_chi * n_ph;
+    if( cudaMemcpy( d_integ, integ, n_integ * sizeof( double ), cudaMemcpyHostToDevice ) != cudaSuccess ||
+        cudaMemcpy( d_xi, xi, ( size_t )n_chi * n_ph * sizeof( double ), cudaMemcpyHostToDevice ) != cudaSuccess ||
+        cudaMemcpy( d_ax, axis1_min, n_chi * sizeof( double ), cudaMemcpyHostToDevice ) != cudaSuccess ) {
+        release( T->mem );
+        delete T;
+        return set_error( SG_ERR_CUDA, "cannot copy the radiation tables" );
+    }
+    RadTab &t = T->t;
+    t.integ = d_integ;
+    t.n_integ = n_integ;
+    t.integ_l0 = std::log10( integ_min );
+    t.integ_d = ( std::log10( integ_max ) - t.integ_l0 ) / ( n_integ - 1 );
+    t.integ_id = 1.0 / t.integ_d;
+    t.xi = d_xi;
+    t.n_chi = n_chi;
+    t.n_ph = n_ph;
+    t.xi_l0 = std::log10( xi_min );
+    t.xi_d = ( std::log10( xi_max ) - t.xi_l0 ) / ( n_chi - 1 );
+    t.xi_id = 1.0 / t.xi_d;
+    t.inv_nph_m1 = 1.0 / ( n_ph - 1 );
+    t.axis1_min = d_ax;
+    t.factor_dNph_dt = factors[0];
+    t.factor_classical = factors[1];
+    t.inv_es = factors[2];
+    t.min_cont = factors[3];
+    t.min_disc = factors[4];
+    *out = T;
+    return SG_OK;
+}
+
+int sg_rad_tables_destroy( sg_rad_tables *T )
+{
+    if( !T ) return SG_OK;
+    release( T->mem );
+    delete T;
+    return SG_OK;
+}
+
+int sg_rad_photon_chi( const sg_rad_tables *T, int64_t n, const double *chi, const double *xi, double *out,
+                       sg_stream_t stream )
+{
+    SG_REQUIRE( T && chi && xi && out, "NULL argument" );
+    if( n <= 0 ) return SG_OK;
+    k_photon_chi<<<grid_for( n, 256 ), 256, 0, as_stream( stream )>>>( T->t, n, chi, xi, out );
+    SG_LAUNCH_CHECK( "k_photon_chi" );
+    return SG_OK;
+}
+
+int sg_rad_production_yield( const sg_rad_tables *T, int64_t n, const double *chi, const double *gamma, double *out,
+                             sg_stream_t stream )
+{
+    SG_REQUIRE( T && chi && gamma && out, "NULL argument" );
+    if( n <= 0 ) return SG_OK;
+    k_yield<<<grid_for( n, 256 ), 256, 0, as_stream( stream )>>>( T->t, n, chi, gamma, out );
+    SG_LAUNCH_CHECK( "k_yield" );
+    return SG_OK;
+}
+
+int sg_rad_monte_carlo( const sg_rad_tables *T, const sg_mlp *mlp, int64_t n, double dt, double mass,
+                        double charge, double *mom, const double *weight, double *tau, double *chi_out,
+                        const double *Epart, const double *Bpart, uint32_t seed, uint32_t first_id, uint32_t step,
+                        double *radiated, unsigned long long *n_emissions, sg_stream_t stream )
+{
+    SG_REQUIRE( T && mom && weight && tau && Epart && Bpart && radiated && n_emissions, "NULL argument" );
+    SG_REQUIRE( mass > 0.0, "mass must be positive" );
+    if( mlp ) SG_REQUIRE( mlp->mask != nullptr, "the network has not been validated (sg_mlp_validate)" );
+    if( n <= 0 ) return SG_OK;
+    const double oom = 1.0 / mass;
+    MlpView v{};
+    if( mlp ) v = view( mlp );
+    k_monte_carlo<<<grid_for( n, 256 ), 256, 0, as_stream( stream )>>>( T->t, v, mlp ? 1 : 0, n, dt, charge * oom * oom, mom,
+                                                                          weight, tau, chi_out, Epart, Bpart, seed,
+                                                                          first_id, step, radiated, n_emissions );
+    SG_LAUNCH_CHECK( "k_monte_carlo" );
+    return SG_OK;
+}
+
+int sg_mlp_create( int hidden, uint32_t seed, double log10_chi_min, double log10_chi_max, sg_mlp **out )
+{
+    SG_REQUIRE( out, "NULL argument" );
+    SG_REQUIRE( hidden >= 4 && hidden <= MLP_MAX_H, "hidden width must be in [4, %d]", MLP_MAX_H );
+    SG_REQUIRE( log10_chi_max > log10_chi_min, "empty chi range" );
+    sg_mlp *m = new sg_mlp();
+    m->H = hidden;
+    m->lmin = ( float )log10_chi_min;
+    m->lspan = ( float )( log10_chi_max - log10_chi_min );
+    const int P = mlp_nparams( hidden );
+    std::vector<float> h( P, 0.0f );
+    // Xavier-uniform weights from a hashed counter, zero biases
+    auto u = [&]( uint32_t k ) { return ( fmix32( seed * 0x9e3779b9u + k ) >> 8 ) * ( 1.0f / 16777216.0f ) * 2.0f - 1.0f; };
+    const int H = hidden;
+    for( int k = 0; k < 2 * H; k++ ) h[k] = u( k ) * std::sqrt( 6.0f / ( 2 + H ) );
+    for( int k = 0; k < H * H; k++ ) h[3 * H + k] = u( 100000 + k ) * std::sqrt( 6.0f / ( 2 * H ) );
+    for( int k = 0; k < H; k++ ) h[4 * H + H * H + k] = u( 200000 + k ) * std::sqrt( 6.0f / ( H + 1 ) );
+    cudaError_t e = cudaMalloc( &m->params, 4 * ( size_t )P * sizeof( float ) );
+    if( e != cudaSuccess ) { delete m; return set_error( SG_ERR_NOMEM, "cannot allocate the network" ); }
+    m->m1 = m->params + P;
+    m->m2 = m->m1 + P;
+    m->grad = m->m2 + P;
+    cudaMemcpy( m->params, h.data(), P * sizeof( float ), cudaMemcpyHostToDevice );
+    cudaMemset( m->m1, 0, 3 * ( size_t )P * sizeof( float ) );
+    if( cudaGetLastError() != cudaSuccess ) { release( m->params ); delete m; return set_error( SG_ERR_CUDA, "network init failed" ); }
+    *out = m;
+    return SG_OK;
+}
+
+int sg_mlp_destroy( sg_mlp *m )
+{
+    if( !m ) return SG_OK;
+    release( m->params );
+    release( m->mask );
+    release( m->scratch );
+    delete m;
+    return SG_OK;
+}
+
+int sg_mlp_nparams( const sg_mlp *m, int *n )
+{
+    SG_REQUIRE( m && n, "NULL argument" );
+    *n = mlp_nparams( m->H );
+    return SG_OK;
+}
+
+int sg_mlp_get_params( const sg_mlp *m, float *host )
+{
+    SG_REQUIRE( m && host, "NULL argument" );
+    SG_CUDA_TRY( cudaMemcpy( host, m->params, mlp_nparams( m->H ) * sizeof( float ), cudaMemcpyDeviceToHost ) );
+    return SG_OK;
+}
+
+int sg_mlp_set_params( sg_mlp *m, const float *host )
+{
+    SG_REQUIRE( m && host, "NULL argument" );
+    SG_CUDA_TRY( cudaMemcpy( m->params, host, mlp_nparams( m->H ) * sizeof( float ), cudaMemcpyHostToDevice ) );
+    return SG_OK;
+}
+
+int sg_mlp_gradients( sg_mlp *m, int B, const float *inputs, const float *targets, float *grad, float *loss )
+{
+    SG_REQUIRE( m && inputs && targets && grad && loss, "NULL argument" );
+    SG_REQUIRE( B > 0, "empty batch" );
+    int r = ensure_scratch( m, B );
+    if( r ) return r;
+    const int H = m->H, P = mlp_nparams( H );
+    float *X = m->scratch, *Y = X + 2 * ( size_t )B, *H1 = Y + B, *H2 = H1 + ( size_t )B * H, *D1 = H2 + ( size_t )B * H;
+    float *D2 = D1 + ( size_t )B * H, *D3 = D2 + ( size_t )B * H, *L = D3 + B;
+    SG_CUDA_TRY( cudaMemcpy( X, inputs, 2 * ( size_t )B * sizeof( float ), cudaMemcpyHostToDevice ) );
+    SG_CUDA_TRY( cudaMemcpy( Y, targets, ( size_t )B * sizeof( float ), cudaMemcpyHostToDevice ) );
+    SG_CUDA_TRY( cudaMemset( L, 0, sizeof( float ) ) );
+    k_mlp_fwd_bwd<<<grid_for( B, 128 ), 128>>>( view( m ), B, X, Y, H1, H2, D1, D2, D3, L );
+    k_mlp_grads<<<grid_for( P, 128 ), 128>>>( H, B, X, H1, H2, D1, D2, D3, m->grad );
+    SG_LAUNCH_CHECK( "k_mlp_grads" );
+    SG_CUDA_TRY( cudaMemcpy( grad, m->grad, P * sizeof( float ), cudaMemcpyDeviceToHost ) );
+    SG_CUDA_TRY( cudaMemcpy( loss, L, sizeof( float ), cudaMemcpyDeviceToHost ) );
+    return SG_OK;
+}
+
+int sg_mlp_train( sg_mlp *m, const sg_rad_tables *T, int steps, int B, float lr, uint32_t seed, float *final_loss,
+                  sg_stream_t stream )
+{
+    SG_REQUIRE( m && T, "NULL argument" );
+    SG_REQUIRE( steps >= 0 && B > 0, "bad training sizes" );
+    int r = ensure_scratch( m, B );
+    if( r ) return r;
+    cudaStream_t st = as_stream( stream );
+    const int H = m->H, P = mlp_nparams( H );
+    float *X = m->scratch, *Y = X + 2 * ( size_t )B, *H1 = Y + B, *H2 = H1 + ( size_t )B * H, *D1 = H2 + ( size_t )B * H;
+    float *D2 = D1 + ( size_t )B * H, *D3 = D2 + ( size_t )B * H, *L = D3 + B;
+    for( int s = 0; s < steps; s++ ) {
+        k_mlp_samples<<<grid_for( B, 256 ), 256, 0, st>>>( T->t, B, m->lmin, m->lspan, m->out_scale, seed, ( uint32_t )s, X, Y );
+        if( s == steps - 1 ) SG_CUDA_TRY( cudaMemsetAsync( L, 0, sizeof( float ), st ) );
+        k_mlp_fwd_bwd<<<grid_for( B, 128 ), 128, 0, st>>>( view( m ), B, X, Y, H1, H2, D1, D2, D3, s == steps - 1 ? L : nullptr );
+        k_mlp_grads<<<grid_for( P, 128 ), 128, 0, st>>>( H, B, X, H1, H2, D1, D2, D3, m->grad );
+        m->adam_t++;
+        k_adam<<<grid_for( P, 256 ), 256, 0, st>>>( P, m->params, m->grad, m->m1, m->m2, lr, 0.9f, 0.999f, 1e-8f, m->adam_t );
+        SG_LAUNCH_CHECK( "k_adam" );
+    }
+    if( final_loss ) {
+        SG_CUDA_TRY( cudaMemcpyAsync( final_loss, L, sizeof( float ), cudaMemcpyDeviceToHost, st ) );
+        SG_CUDA_TRY( cudaStreamSynchronize( st ) );
+    }
+    return SG_OK;
+}
+
+int sg_mlp_validate( sg_mlp *m, const sg_rad_tables *T, int n_chi_bins, int n_xi_bins, int per_bin, float tol,
+                     float *err_out, int *n_masked )
+{
+    SG_REQUIRE( m && T, "NULL argument" );
+    SG_REQUIRE( n_chi_bins > 0 && n_xi_bins > 0 && per_bin > 0, "bad validation grid" );
+    const int nb = n_chi_bins * n_xi_bins;
+    release( m->mask );
+    m->mask = nullptr;
+    SG_CUDA_TRY( cudaMalloc( &m->mask, nb * sizeof( int ) ) );
+    m->nbc = n_chi_bins;
+    m->nbx = n_xi_bins;
+    float *d_err = nullptr;
+    SG_CUDA_TRY( cudaMalloc( &d_err, nb * sizeof( float ) ) );
+    k_mlp_validate<<<nb, 256>>>( T->t, view( m ), per_bin, d_err );
+    SG_LAUNCH_CHECK( "k_mlp_validate" );
+    std::vector<float> h( nb );
+    SG_CUDA_TRY( cudaMemcpy( h.data(), d_err, nb * sizeof( float ), cudaMemcpyDeviceToHost ) );
+    release( d_err );
+    std::vector<int> mask( nb );
+    int cnt = 0;
+    for( int i = 0; i < nb; i++ ) {
+        mask[i] = !( h[i] <= tol ); // NaN -> masked
+        cnt += mask[i];
+    }
+    SG_CUDA_TRY( cudaMemcpy( m->mask, mask.data(), nb * sizeof( int ), cudaMemcpyHostToDevice ) );
+    if( err_out ) std::copy( h.begin(), h.end(), err_out );
+    if( n_masked ) *n_masked = cnt;
+    return SG_OK;
+}
+
+int sg_mlp_photon_chi( const sg_mlp *m, int64_t n, const double *chi, const double *xi, double *out, sg_stream_t stream )
+{
+    SG_REQUIRE( m && chi && xi && out, "NULL argument" );
+    if( n <= 0 ) return SG_OK;
+    k_mlp_photon_chi<<<grid_for( n, 128 ), 128, 0, as_stream( stream )>>>( view( m ), n, chi, xi, out );
+    SG_LAUNCH_CHECK( "k_mlp_photon_chi" );
+    return SG_OK;
+}
+
+} // extern "C"

@@ -758,11 +758,12 @@ __global__ void k_stage( GridInfo g, int64_t n, const double *__restrict__ pos, 
         if constexpr( MIXED ) st.d[d][p] = ( float )dl;
         else st.x[d][p] = x;
     }
+    using PT = typename std::conditional<MIXED, float, double>::type;
     if constexpr( MIXED ) st.key[p] = pack_key( DIM, node[0], node[1], node[2] );
-    st.p[0][p] = ( decltype( st.p[0][0] ) )mom[p];
-    st.p[1][p] = ( decltype( st.p[0][0] ) )mom[n + p];
-    st.p[2][p] = ( decltype( st.p[0][0] ) )mom[2 * n + p];
-    st.w[p] = ( decltype( st.w[0] ) )wgt[p];
+    st.p[0][p] = ( PT )mom[p];
+    st.p[1][p] = ( PT )mom[n + p];
+    st.p[2][p] = ( PT )mom[2 * n + p];
+    st.w[p] = ( PT )wgt[p];
     const int t = tile_of( g, node[0], node[1], node[2] );
     st_tile[p] = t;
     atomicAdd( &count[t], 1 );

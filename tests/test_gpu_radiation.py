@@ -1,0 +1,124 @@
+"""GPU Monte-Carlo radiation: table kernels, the Monte-Carlo pass and the MLP surrogate.
+
+Tables are the reference's default tables (tests/golden/radiation.npz, dumped
+from the reference's RadiationTablesDefault).  Table kernels must reproduce the
+reference's outputs; the Monte-Carlo pass must reproduce the oracle's pass
+drawing the same per-particle random streams; the network's gradients must
+match the FP64 oracle's; the trained network is judged by the table: its
+per-bin error decides where it is used, and the emitted spectrum and mean
+energy loss of a Monte-Carlo pass using it are compared with the table-only pass.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import rel_err
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def rad(golden_rad):
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from smilei_gb300 import radiation
+    g = golden_rad
+    f_dn, f_cl, inv_es = radiation.normalised_factors(2.0 * np.pi * 299792458.0 / 1e-6)  # lambda_r = 1 um
+    T = radiation.RadiationTables(g["integfochi"], g["integfochi_min"], g["integfochi_max"], g["xi_table"],
+                                  g["xi_min"], g["xi_max"], g["xi_axis1_min"], f_dn, f_cl, inv_es)
+    Tc = oracle.RadTables.from_golden(g, factor_dNph_dt=f_dn, factor_classical=f_cl, inv_norm_E_schwinger=inv_es)
+    return radiation, T, Tc
+
+
+def cu(a):
+    return torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64), device="cuda")
+
+
+def test_table_kernels_match_reference(rad, golden_rad):
+    radiation, T, _ = rad
+    g = golden_rad
+    pc = T.photon_chi(cu(g["chi"]), cu(g["xi"])).cpu().numpy()
+    assert np.max(np.abs(pc / g["photon_chi"] - 1.0)) <= 1e-13
+    Ty = radiation.RadiationTables(g["integfochi"], g["integfochi_min"], g["integfochi_max"], g["xi_table"],
+                                   g["xi_min"], g["xi_max"], g["xi_axis1_min"], float(g["factor"]), 1.0, 1.0)
+    y = Ty.production_yield(cu(g["chi"]), cu(g["gamma"])).cpu().numpy()
+    assert rel_err(y, g["yield_"]) <= 1e-13
+
+
+def beam(n, seed):
+    """An electron beam (gamma ~ 2000) in a strong field: chi spans about 0.1 - 10."""
+    rng = np.random.default_rng(seed)
+    mom = np.ascontiguousarray(np.stack([rng.normal(-2000, 40, n), rng.normal(0, 4, n), rng.normal(0, 4, n)]))
+    E = rng.normal(0, 60, (3, n))
+    B = rng.normal(0, 60, (3, n))
+    return mom, E, B, np.ones(n)
+
+
+def test_monte_carlo_pass_matches_oracle(rad):
+    radiation, T, Tc = rad
+    n = 20000
+    mom, E, B, w = beam(n, 1)
+    tau = np.full(n, -1.0)
+    m_gpu, tau_gpu = cu(mom), cu(tau)
+    chi_gpu = torch.zeros(n, dtype=torch.float64, device="cuda")
+    total_g = total_o = 0.0
+    nem_g = nem_o = 0
+    for step in range(3):
+        r_g, e_g = radiation.monte_carlo(T, 0.1, 1.0, -1.0, m_gpu, cu(w), tau_gpu, cu(E), cu(B), seed=99,
+                                         step=step, chi_out=chi_gpu)
+        r_o, e_o, chi_o = oracle.rad_monte_carlo(Tc, 0.1, 1.0, -1.0, mom, w, tau, E, B, seed=99, step=step)
+        total_g += r_g; total_o += r_o; nem_g += e_g; nem_o += e_o
+    assert nem_g == nem_o and nem_g > 1000
+    assert abs(total_g - total_o) <= 1e-10 * total_o
+    assert rel_err(m_gpu.cpu().numpy(), mom) <= 1e-12
+    assert rel_err(chi_gpu.cpu().numpy(), chi_o) <= 1e-12
+    assert 0.05 < chi_o.mean() < 20.0
+
+
+def test_mlp_gradients_match_cpu_oracle(rad):
+    radiation, _, _ = rad
+    from oracle import mlp as M
+    net = radiation.PhotonChiMLP(hidden=64, seed=3)
+    p = net.params().astype(np.float64)
+    rng = np.random.default_rng(5)
+    X = rng.uniform(-1, 1, (512, 2))
+    Y = rng.normal(0, 1, 512)
+    g_gpu, l_gpu = net.gradients(X, Y)
+    g_ref, l_ref = M.gradients(p, 64, X.astype(np.float32).astype(np.float64), Y.astype(np.float32).astype(np.float64))
+    assert abs(l_gpu - l_ref) <= 1e-5 * l_ref
+    assert rel_err(g_gpu, g_ref) <= 2e-5
+    fd = M.fd_gradients(p, 64, X, Y, idx=[0, 200, 1000, 3000, net.nparams - 1])
+    for k, v in fd.items():
+        assert abs(g_ref[k] - v) <= 1e-6 * max(1.0, abs(v))
+    net.close()
+
+
+def test_trained_mlp_with_table_fallback(rad):
+    radiation, T, _ = rad
+    net = radiation.PhotonChiMLP(hidden=64, seed=1)
+    l0 = net.train(T, steps=1, batch=4096)
+    l1 = net.train(T, steps=3000, batch=8192, lr=2e-3)
+    assert l1 < 0.05 * l0
+    err, n_masked = net.validate(T, tol=0.05)
+    assert n_masked < err.size  # the network is used somewhere
+    # Monte-Carlo with the network (table where masked) vs table only: same draws
+    n = 100000
+    mom, E, B, w = beam(n, 2)
+    res = {}
+    for name, m in (("table", None), ("mlp", net)):
+        mm = cu(mom)
+        tau = torch.full((n,), -1.0, dtype=torch.float64, device="cuda")
+        tot, nem = 0.0, 0
+        for step in range(4):
+            r, e = radiation.monte_carlo(T, 0.1, 1.0, -1.0, mm, cu(w), tau, cu(E), cu(B), seed=5, step=step, mlp=m)
+            tot += r; nem += e
+        g = torch.sqrt(1 + (mm ** 2).sum(0)).cpu().numpy()
+        res[name] = (tot, nem, g)
+    (t_tab, n_tab, g_tab), (t_mlp, n_mlp, g_mlp) = res["table"], res["mlp"]
+    assert abs(n_mlp - n_tab) <= 0.05 * n_tab
+    assert abs(t_mlp - t_tab) / t_tab < 0.05  # mean energy loss within 5 %
+    h_tab, edges = np.histogram(np.log10(g_tab), bins=40)
+    h_mlp, _ = np.histogram(np.log10(g_mlp), bins=edges)
+    assert np.abs(h_mlp - h_tab).sum() / h_tab.sum() < 0.1  # final energy spectrum
+    net.close()
