@@ -73,13 +73,14 @@ def test_poisson_matches_oracle_and_zeroes_the_residual(mods, form):
     sim.close()
 
 
-@pytest.mark.parametrize("form,limit", [("fp64", 1e-9), ("mixed", 1e-5)])
-def test_charge_residual_is_conserved_by_the_step(mods, form, limit):
+@pytest.mark.parametrize("form,start,limit", [("fp64", 1e-12, 1e-9), ("mixed", 1e-7, 1e-6)])
+def test_charge_residual_is_conserved_by_the_step(mods, form, start, limit):
     simulation, synthetic, P = mods
     sim, *_ = plasma_sim(simulation, synthetic, form, 3, sigma=0.3)
     sim.solve_poisson(max_error=1e-26)  # start from round-off so the step's own error shows
     r0 = sim.charge_residual()
     sim.step(50)
     r1 = sim.charge_residual()
-    assert r0 <= 1e-12 and r1 <= limit, (r0, r1)
+    # FP32 storage of E alone leaves ~2e-8 after the solve in the mixed form
+    assert r0 <= start and r1 <= limit, (r0, r1)
     sim.close()
