@@ -154,7 +154,9 @@ def run_gpu(args, rank, world, local_rank):
     n = int(w.shape[0])
     sim = simulation.Simulation(cfg["n_cells"], cfg["cell_length"], cfg["dt"], form=args.form,
                                 tile=[args.tile] * 3 if args.tile else None, use_graph=True)
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: the step is captured as a CUDA graph, which the legacy default stream does not allow
+    stream = torch.cuda.Stream(device=device)
+    torch.cuda.set_stream(stream)
     from smilei_gb300 import _lib
     _lib.check(_lib.lib().sg_sim_set_stream(sim._h, stream.cuda_stream), "set_stream")
     sim.add_species(1.0, -1.0, cfg["pusher"], pos, mom, w)
