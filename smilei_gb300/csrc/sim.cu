@@ -83,6 +83,8 @@ struct SpecParams {
     double charge;
     double mass;
     double cw;       // charge * inverse cell volume (per unit weight)
+    double cr[3];    // cw * dx_d / dt: Esirkepov current factor per unit weight
+    double vs[3];    // dt / dx_d: displacement in cells per unit velocity
 };
 
 // Packed node index of the mixed form: 3D x:11 y:10 z:10 bits, 2D x:16 y:16 bits.
@@ -222,7 +224,9 @@ __device__ __forceinline__ void sh_add( T *a, T v )
 }
 
 // Per-dimension Esirkepov window: 4 nodes starting at lo (0 or 1) of the
-// 5-point stencil; A = (S0+S1)/2, D = S1-S0, P = running sums of D.
+// 5-point stencil; A = (S0+S1)/2, D = S1-S0, P = running sums of D.  S0 sits
+// at stencil points 1..3, S1 at shift+1..shift+3; everything stays in registers
+// (selects instead of indexed stores).
 template <class T>
 struct EsirWin {
     int lo;
@@ -230,20 +234,23 @@ struct EsirWin {
 };
 
 template <class T>
+__device__ __forceinline__ T pick3( int j, T c0, T c1, T c2 )
+{
+    return j == 0 ? c0 : ( j == 1 ? c1 : ( j == 2 ? c2 : T( 0 ) ) );
+}
+
+template <class T>
 __device__ __forceinline__ void esir_win( T c0o, T c1o, T c2o, T dnew, int shift, EsirWin<T> &w )
 {
-    T S0[5] = { T( 0 ), c0o, c1o, c2o, T( 0 ) };
-    T S1[5] = { T( 0 ), T( 0 ), T( 0 ), T( 0 ), T( 0 ) };
     T c0, c1, c2;
     bspline2( dnew, c0, c1, c2 );
-    S1[shift + 1] = c0;
-    S1[shift + 2] = c1;
-    S1[shift + 3] = c2;
     w.lo = shift < 0 ? 0 : 1;
     T run = T( 0 );
 #pragma unroll
     for( int i = 0; i < 4; i++ ) {
-        const T s0 = S0[w.lo + i], s1 = S1[w.lo + i];
+        const int k = w.lo + i;
+        const T s0 = pick3( k - 1, c0o, c1o, c2o );
+        const T s1 = pick3( k - 1 - shift, c0, c1, c2 );
         w.A[i] = T( 0.5 ) * ( s0 + s1 );
         w.D[i] = s1 - s0;
         if( i < 3 ) {
@@ -254,7 +261,7 @@ __device__ __forceinline__ void esir_win( T c0o, T c1o, T c2o, T dnew, int shift
 }
 
 template <int DIM, bool MIXED, int KIND>
-__global__ void __launch_bounds__( 128 ) k_step_particles(
+__global__ void __launch_bounds__( 128, MIXED ? 8 : 4 ) k_step_particles(
     GridInfo g, Fields<typename std::conditional<MIXED, float, double>::type> f, SpecParams sp, PBuf<MIXED> in,
     PBuf<MIXED> out, const int64_t *__restrict__ seg_start, const int *__restrict__ cap,
     const int *__restrict__ count_in, int *__restrict__ count_out, PBuf<MIXED> ovf, int *__restrict__ ovf_tile,
@@ -298,8 +305,10 @@ __global__ void __launch_bounds__( 128 ) k_step_particles(
 
     const int n = count_in[tile];
     const int64_t s0 = seg_start[tile];
-    const T dt = T( g.dt );
     const T qm = T( sp.qm_dts2 );
+    const T vs[3] = { T( sp.vs[0] ), T( sp.vs[1] ), T( sp.vs[2] ) };
+    const T cr3[3] = { T( sp.cr[0] ), T( sp.cr[1] ), T( sp.cr[2] ) };
+    const T cw0 = T( sp.cw );
     const unsigned lane = threadIdx.x & 31u;
 
     for( int base = 0; base < n; base += blockDim.x ) {
@@ -395,7 +404,7 @@ __global__ void __launch_bounds__( 128 ) k_step_particles(
         if constexpr( MIXED ) {
 #pragma unroll
             for( int d = 0; d < DIM; d++ ) {
-                const T dn = dlt[d] + pm[d] * ( ginv * dt * T( g.dxi[d] ) );
+                const T dn = dlt[d] + pm[d] * ( ginv * vs[d] );
                 const int sh = ( int )floorf( ( float )dn + 0.5f );
                 shift[d] = sh;
                 dnew[d] = dn - T( sh );
@@ -430,10 +439,10 @@ __global__ void __launch_bounds__( 128 ) k_step_particles(
             EsirWin<T> W[3];
 #pragma unroll
             for( int d = 0; d < DIM; d++ ) esir_win<T>( cp[d][0], cp[d][1], cp[d][2], dnew[d], shift[d], W[d] );
-            const T cw = T( sp.cw ) * w;
+            const T cw = cw0 * w;
             const T twelfth = T( 1.0 / 12.0 );
             if( DIM == 3 ) {
-                const T cr[3] = { cw * T( g.dx[0] / g.dt ), cw * T( g.dx[1] / g.dt ), cw * T( g.dx[2] / g.dt ) };
+                const T cr[3] = { cr3[0] * w, cr3[1] * w, cr3[2] * w };
                 // Jx(d,p,p): node i' = lo+1+m, j = lo+jw, k = lo+kw (tile index = old node + stencil index)
 #pragma unroll
                 for( int c = 0; c < 3; c++ ) {
@@ -444,7 +453,6 @@ __global__ void __launch_bounds__( 128 ) k_step_particles(
 #pragma unroll
                         for( int v = 0; v < 4; v++ ) {
                             const T wgt = W[b].A[u] * W[e].A[v] + twelfth * W[b].D[u] * W[e].D[v];
-                            if( wgt == T( 0 ) ) continue;
                             int idx[3];
                             idx[b] = lx[b] + W[b].lo + u;
                             idx[e] = lx[e] + W[e].lo + v;
@@ -457,7 +465,7 @@ __global__ void __launch_bounds__( 128 ) k_step_particles(
                         }
                 }
             } else {
-                const T crx = cw * T( g.dx[0] / g.dt ), cry = cw * T( g.dx[1] / g.dt );
+                const T crx = cr3[0] * w, cry = cr3[1] * w;
                 const T crz = cw * pz * ginv;
                 T *J0 = sJ, *J1 = sJ + jsz, *J2 = sJ + 2 * jsz;
 #pragma unroll
@@ -795,13 +803,19 @@ __device__ __forceinline__ void copy_particle( const PBuf<MIXED> &s, int64_t i, 
     d.w[o] = s.w[i];
 }
 
-// Staged (or spilled) particle p -> next free slot of its tile in the destination buffer.
+// Staged (or spilled) particle -> next free slot of its tile in the destination buffer.
+// Thread t places particle (t * 2654435761) mod n, a permutation of [0, n) (the
+// multiplier is a prime above 2^31 > n): inputs usually arrive cell by cell, and
+// scrambling them inside each tile keeps the lanes of a warp on different cells,
+// which is what keeps the deposit's shared-memory atomics free of conflicts.
 template <bool MIXED>
 __global__ void k_place( int ndim, int64_t n, PBuf<MIXED> st, const int *__restrict__ st_tile,
                          const int64_t *__restrict__ seg_start, int *__restrict__ fill, PBuf<MIXED> dst )
 {
-    const int64_t p = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x;
-    if( p >= n ) return;
+    const int64_t th = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x;
+    if( th >= n ) return;
+    // th < 2^31 and the multiplier < 2^32: the product fits in 64 bits
+    const int64_t p = ( int64_t )( ( ( unsigned long long )th * 2654435761ull ) % ( unsigned long long )n );
     const int t = st_tile[p];
     const int slot = atomicAdd( &fill[t], 1 );
     copy_particle<MIXED>( st, p, dst, seg_start[t] + slot, ndim );
@@ -1042,6 +1056,10 @@ int launch_particles( sg_sim *S, SpeciesState &s, cudaStream_t st )
     double vol = 1.0;
     for( int d = 0; d < S->g.ndim; d++ ) vol *= S->g.dx[d];
     sp.cw = s.charge / vol;
+    for( int d = 0; d < 3; d++ ) {
+        sp.cr[d] = sp.cw * S->g.dx[d] / S->g.dt;
+        sp.vs[d] = S->g.dt * S->g.dxi[d];
+    }
     auto kern = k_step_particles<DIM, MIXED, KIND>;
     if( S->smem_bytes > 48 * 1024 ) SG_CUDA_TRY( cudaFuncSetAttribute( kern, cudaFuncAttributeMaxDynamicSharedMemorySize, ( int )S->smem_bytes ) );
     const int sidx = ( int )( &s - &S->sp[0] );
