@@ -41,6 +41,7 @@ struct GridInfo {
     int N[3];   // cells per dimension
     int np[3];  // primal extents with ghosts (N + 1 + 2*OS); 1 for an absent dimension
     int T[3];   // tile size in cells
+    int tshift[3]; // log2(T) when T is a power of two, else -1
     int nt[3];  // tiles per dimension
     int ntiles;
     double dx[3], dxi[3], L[3], dt;
@@ -106,12 +107,52 @@ __host__ __device__ inline void unpack_key( int ndim, unsigned k, int &ix, int &
     }
 }
 
+__host__ __device__ inline int tile_div( const GridInfo &g, int i, int d )
+{
+    return g.tshift[d] >= 0 ? i >> g.tshift[d] : i / g.T[d];
+}
+
 __host__ __device__ inline int tile_of( const GridInfo &g, int ix, int iy, int iz )
 {
-    int t = ix / g.T[0];
-    t = t * g.nt[1] + iy / g.T[1];
-    if( g.ndim == 3 ) t = t * g.nt[2] + iz / g.T[2];
+    int t = tile_div( g, ix, 0 );
+    t = t * g.nt[1] + tile_div( g, iy, 1 );
+    if( g.ndim == 3 ) t = t * g.nt[2] + tile_div( g, iz, 2 );
     return t;
+}
+
+// Thread map for tile copies: lanes along the last dimension.  3D tiles with a
+// cross section of at most 8 x 8 use 8 lanes per row and 8 rows per x plane
+// (no divisions); 2D tiles with at most 16 points per row use 16 lanes per row.
+// Other shapes fall back to a division per point.
+struct TileMap {
+    int cx0, cy, cz, step; // first x, this thread's (y, z), x stride
+    bool fast, active;
+};
+
+template <int DIM>
+__device__ __forceinline__ TileMap tile_map( int NY, int NZ )
+{
+    TileMap m;
+    if( DIM == 3 && NY <= 8 && NZ <= 8 ) {
+        m.cz = threadIdx.x & 7;
+        m.cy = ( threadIdx.x >> 3 ) & 7;
+        m.cx0 = threadIdx.x >> 6;
+        m.step = blockDim.x >> 6;
+        m.fast = true;
+        m.active = m.cz < NZ && m.cy < NY;
+    } else if( DIM == 2 && NY <= 16 ) {
+        m.cz = 0;
+        m.cy = threadIdx.x & 15;
+        m.cx0 = threadIdx.x >> 4;
+        m.step = blockDim.x >> 4;
+        m.fast = true;
+        m.active = m.cy < NY;
+    } else {
+        m.cz = m.cy = m.cx0 = m.step = 0;
+        m.fast = false;
+        m.active = true;
+    }
+    return m;
 }
 
 // ------------------------------------------------------------------------------
@@ -288,16 +329,31 @@ __global__ void __launch_bounds__( 128, MIXED ? 8 : 4 ) k_step_particles(
     const int ix0 = tx * g.T[0], iy0 = ty * g.T[1], iz0 = DIM == 3 ? tz * g.T[2] : 0;
 
     // 1. stage E and B_m (field tile origin = array index (i0 + OS - 1)) and clear J
+    const TileMap fm = tile_map<DIM>( td.FY, td.FZ );
+#pragma unroll
     for( int c = 0; c < 6; c++ ) {
         const T *src = c < 3 ? f.E[c] : f.Bm[c - 3];
         const int ny = ext( g, 1, stag( c, 1 ) ), nz = ext( g, 2, stag( c, 2 ) );
         const int nx = ext( g, 0, stag( c, 0 ) );
-        for( int e = threadIdx.x; e < fsz; e += blockDim.x ) {
-            const int cz = e % td.FZ, cy = ( e / td.FZ ) % td.FY, cx = e / ( td.FZ * td.FY );
-            const int gx = ix0 + OS - 1 + cx, gy = iy0 + OS - 1 + cy, gz = DIM == 3 ? iz0 + OS - 1 + cz : 0;
-            T v = T( 0 );
-            if( gx < nx && gy < ny && gz < nz ) v = src[( ( int64_t )gx * ny + gy ) * nz + gz];
-            sF[c * fsz + e] = v;
+        T *dst = sF + c * fsz;
+        if( fm.fast ) {
+            if( fm.active ) {
+                const int gy = iy0 + OS - 1 + fm.cy, gz = DIM == 3 ? iz0 + OS - 1 + fm.cz : 0;
+                for( int cx = fm.cx0; cx < td.FX; cx += fm.step ) {
+                    const int gx = ix0 + OS - 1 + cx;
+                    T v = T( 0 );
+                    if( gx < nx && gy < ny && gz < nz ) v = src[( ( int64_t )gx * ny + gy ) * nz + gz];
+                    dst[( cx * td.FY + fm.cy ) * td.FZ + fm.cz] = v;
+                }
+            }
+        } else {
+            for( int e = threadIdx.x; e < fsz; e += blockDim.x ) {
+                const int cz = e % td.FZ, cy = ( e / td.FZ ) % td.FY, cx = e / ( td.FZ * td.FY );
+                const int gx = ix0 + OS - 1 + cx, gy = iy0 + OS - 1 + cy, gz = DIM == 3 ? iz0 + OS - 1 + cz : 0;
+                T v = T( 0 );
+                if( gx < nx && gy < ny && gz < nz ) v = src[( ( int64_t )gx * ny + gy ) * nz + gz];
+                dst[e] = v;
+            }
         }
     }
     for( int e = threadIdx.x; e < 3 * jsz; e += blockDim.x ) sJ[e] = T( 0 );
@@ -564,16 +620,30 @@ __global__ void __launch_bounds__( 128, MIXED ? 8 : 4 ) k_step_particles(
     __syncthreads();
 
     // 4. flush the J tile (origin = array index i0 + OS - 2) with global atomics
+    const TileMap jm = tile_map<DIM>( td.JY, td.JZ );
+#pragma unroll
     for( int c = 0; c < 3; c++ ) {
         T *dstJ = f.J[c];
         const int ny = ext( g, 1, stag( c, 1 ) ), nz = ext( g, 2, stag( c, 2 ) );
         const int nx = ext( g, 0, stag( c, 0 ) );
-        for( int e = threadIdx.x; e < jsz; e += blockDim.x ) {
-            const T v = sJ[c * jsz + e];
-            if( v == T( 0 ) ) continue;
-            const int cz = e % td.JZ, cy = ( e / td.JZ ) % td.JY, cx = e / ( td.JZ * td.JY );
-            const int gx = ix0 + OS - 2 + cx, gy = iy0 + OS - 2 + cy, gz = DIM == 3 ? iz0 + OS - 2 + cz : 0;
-            if( gx < nx && gy < ny && gz < nz ) atomicAdd( &dstJ[( ( int64_t )gx * ny + gy ) * nz + gz], v );
+        const T *srcJ = sJ + c * jsz;
+        if( jm.fast ) {
+            if( jm.active ) {
+                const int gy = iy0 + OS - 2 + jm.cy, gz = DIM == 3 ? iz0 + OS - 2 + jm.cz : 0;
+                for( int cx = jm.cx0; cx < td.JX; cx += jm.step ) {
+                    const T v = srcJ[( cx * td.JY + jm.cy ) * td.JZ + jm.cz];
+                    const int gx = ix0 + OS - 2 + cx;
+                    if( v != T( 0 ) && gx < nx && gy < ny && gz < nz ) atomicAdd( &dstJ[( ( int64_t )gx * ny + gy ) * nz + gz], v );
+                }
+            }
+        } else {
+            for( int e = threadIdx.x; e < jsz; e += blockDim.x ) {
+                const T v = srcJ[e];
+                if( v == T( 0 ) ) continue;
+                const int cz = e % td.JZ, cy = ( e / td.JZ ) % td.JY, cx = e / ( td.JZ * td.JY );
+                const int gx = ix0 + OS - 2 + cx, gy = iy0 + OS - 2 + cy, gz = DIM == 3 ? iz0 + OS - 2 + cz : 0;
+                if( gx < nx && gy < ny && gz < nz ) atomicAdd( &dstJ[( ( int64_t )gx * ny + gy ) * nz + gz], v );
+            }
         }
     }
 }
@@ -1252,7 +1322,7 @@ int choose_tiles( sg_sim *S )
 {
     GridInfo &g = S->g;
     for( int d = 0; d < 3; d++ ) {
-        if( d >= g.ndim ) { g.T[d] = 1; g.nt[d] = 1; continue; }
+        if( d >= g.ndim ) { g.T[d] = 1; g.nt[d] = 1; g.tshift[d] = 0; continue; }
         int t = S->cfg.tile[d];
         if( t <= 0 ) {
             const int pref = g.ndim == 3 ? 4 : 8;
@@ -1262,6 +1332,7 @@ int choose_tiles( sg_sim *S )
         if( g.N[d] % t ) return set_error( SG_ERR_ARG, "tile size %d does not divide %d cells in dimension %d", t, g.N[d], d );
         g.T[d] = t;
         g.nt[d] = g.N[d] / t;
+        g.tshift[d] = ( t & ( t - 1 ) ) == 0 ? __builtin_ctz( ( unsigned )t ) : -1;
     }
     g.ntiles = g.nt[0] * g.nt[1] * ( g.ndim == 3 ? g.nt[2] : 1 );
     const TileDims td = tile_dims( g );
