@@ -18,6 +18,10 @@
 //   E and B_m in shared memory, gather, push, Esirkepov deposit into a
 //   shared J tile, write each particle to its destination tile's segment in the
 //   other buffer, flush the J tile with global atomics); fold the periodic J
+//   (mixed form, per-cell mode: the tile's particles are first ranked by cell and
+//   loaded into shared memory in cell order, so the lanes of a warp gather from
+//   the same few cells; after the push, particles that keep their node are
+//   deposited per cell from register sums, the others one per thread)
 //   ghosts; Ampere on all points; Faraday on all points (periodic images for the
 //   boundary layer) fused with B_m <- (B_new + B_old)/2.
 // A tile whose segment fills up spills particles to an overflow list; the host
@@ -301,12 +305,78 @@ __device__ __forceinline__ void esir_win( T c0o, T c1o, T c2o, T dnew, int shift
     }
 }
 
-template <int DIM, bool MIXED, int KIND>
-__global__ void __launch_bounds__( 128, MIXED ? 8 : 4 ) k_step_particles(
+// Esirkepov deposit of one particle straight into the shared J tile (atomics):
+// Jx(d,p,p) at node (lo+1+m, lo+u, lo+v) of the 5-point stencil gets
+// -cr_x P_x[m] (A_y[u] A_z[v] + D_y[u] D_z[v] / 12), and cyclically for Jy, Jz;
+// in 2D, Jz = crz (A_x A_y + D_x D_y / 12) with crz = q w v_z / V.  lx = the old
+// node, tile-local; the J tile origin is two nodes below the tile.
+template <int DIM, class T>
+__device__ __forceinline__ void deposit_direct( T *sJ, const TileDims &td, int jsz, const int *lx,
+                                                const EsirWin<T> *W, const T *cr, T crz, unsigned cmask = 7u )
+{
+    const T twelfth = T( 1.0 / 12.0 );
+    if( DIM == 3 ) {
+#pragma unroll
+        for( int c = 0; c < 3; c++ ) {
+            if( !( ( cmask >> c ) & 1u ) ) continue;
+            const int a = c, b = ( c + 1 ) % 3, e = ( c + 2 ) % 3;
+            T *J = sJ + c * jsz;
+#pragma unroll
+            for( int u = 0; u < 4; u++ )
+#pragma unroll
+                for( int v = 0; v < 4; v++ ) {
+                    const T wgt = W[b].A[u] * W[e].A[v] + twelfth * W[b].D[u] * W[e].D[v];
+                    int idx[3];
+                    idx[b] = lx[b] + W[b].lo + u;
+                    idx[e] = lx[e] + W[e].lo + v;
+#pragma unroll
+                    for( int m = 0; m < 3; m++ ) {
+                        idx[a] = lx[a] + W[a].lo + 1 + m;
+                        sh_add( &J[( idx[0] * td.JY + idx[1] ) * td.JZ + idx[2]], -cr[a] * W[a].P[m] * wgt );
+                    }
+                }
+        }
+    } else {
+        T *J0 = sJ, *J1 = sJ + jsz, *J2 = sJ + 2 * jsz;
+#pragma unroll
+        for( int u = 0; u < 4; u++ ) {
+            const T ay = W[1].A[u];
+            if( ( cmask & 1u ) && ay != T( 0 ) ) {
+#pragma unroll
+                for( int m = 0; m < 3; m++ )
+                    sh_add( &J0[( lx[0] + W[0].lo + 1 + m ) * td.JY + lx[1] + W[1].lo + u], -cr[0] * W[0].P[m] * ay );
+            }
+            const T ax = W[0].A[u];
+            if( ( cmask & 2u ) && ax != T( 0 ) ) {
+#pragma unroll
+                for( int m = 0; m < 3; m++ )
+                    sh_add( &J1[( lx[0] + W[0].lo + u ) * td.JY + lx[1] + W[1].lo + 1 + m], -cr[1] * W[1].P[m] * ax );
+            }
+            if( cmask & 4u ) {
+#pragma unroll
+                for( int v = 0; v < 4; v++ ) {
+                    const T wz = W[0].A[u] * W[1].A[v] + twelfth * W[0].D[u] * W[1].D[v];
+                    sh_add( &J2[( lx[0] + W[0].lo + u ) * td.JY + lx[1] + W[1].lo + v], crz * wz );
+                }
+            }
+        }
+    }
+}
+
+// Per-cell mode keeps the tile's particles in shared memory in cell order, as
+// REC planes of nmax words (plane k of slot s at k * nmax + s).  Loaded state:
+// planes 0-2 in-cell offsets, 3-5 momenta, 7 weight.  After the push the slot
+// becomes the deposit record: planes 3-5 new offsets (2D: 3-4 new offsets, 5
+// v_z), plane 6 the packed node shifts; planes 0-2 and 7 are kept.
+constexpr int REC = 8;
+constexpr int NO_SHIFT = 1 | ( 1 << 2 ) | ( 1 << 4 ); // packed shifts (s + 1 per 2 bits) of a particle that keeps its node
+
+template <int DIM, bool MIXED, int KIND, bool CELLS>
+__global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_particles(
     GridInfo g, Fields<typename std::conditional<MIXED, float, double>::type> f, SpecParams sp, PBuf<MIXED> in,
     PBuf<MIXED> out, const int64_t *__restrict__ seg_start, const int *__restrict__ cap,
     const int *__restrict__ count_in, int *__restrict__ count_out, PBuf<MIXED> ovf, int *__restrict__ ovf_tile,
-    int *__restrict__ ovf_count, int ovf_cap, int *__restrict__ status )
+    int *__restrict__ ovf_count, int ovf_cap, int *__restrict__ status, int nmax )
 {
     using T = typename std::conditional<MIXED, float, double>::type;
     extern __shared__ __align__( 16 ) unsigned char smem_raw[];
@@ -315,6 +385,15 @@ __global__ void __launch_bounds__( 128, MIXED ? 8 : 4 ) k_step_particles(
     const int fsz = td.FX * td.FY * td.FZ;
     const int jsz = td.JX * td.JY * td.JZ;
     T *sJ = sF + 6 * fsz;
+    // per-cell mode (CELLS): particle planes, per-cell counts and starts, each
+    // particle's (cell << 16 | rank in cell), each slot's cell
+    const int TC = g.T[0] * g.T[1] * ( DIM == 3 ? g.T[2] : 1 );
+    float *sRec = reinterpret_cast<float *>( sJ + 3 * jsz );
+    int *sCnt = reinterpret_cast<int *>( sRec + ( CELLS ? REC * nmax : 0 ) );
+    int *sStart = sCnt + TC;
+    int *sRank = sStart + TC;   // reused after loading as the list of node-changing slots
+    unsigned char *sSlotCell = reinterpret_cast<unsigned char *>( sRank + ( CELLS ? nmax : 0 ) );
+    __shared__ int sNX;         // length of that list
 
     const int tile = blockIdx.x;
     int tz = 0, ty, tx;
@@ -359,8 +438,62 @@ __global__ void __launch_bounds__( 128, MIXED ? 8 : 4 ) k_step_particles(
     for( int e = threadIdx.x; e < 3 * jsz; e += blockDim.x ) sJ[e] = T( 0 );
     __syncthreads();
 
-    const int n = count_in[tile];
+    int n = count_in[tile];
     const int64_t s0 = seg_start[tile];
+    if constexpr( CELLS ) {
+        // a tile never holds more than its segment (the largest is nmax): anything
+        // else is a corrupt layout, reported instead of overrunning the records
+        if( n > nmax ) {
+            if( threadIdx.x == 0 ) atomicCAS( status, 0, SG_ERR_STATE );
+            n = nmax;
+        }
+        // rank of every particle inside its cell, then the cells' start offsets
+        for( int c = threadIdx.x; c < TC; c += blockDim.x ) sCnt[c] = 0;
+        __syncthreads();
+        for( int q = threadIdx.x; q < n; q += blockDim.x ) {
+            int gx, gy, gz;
+            unpack_key( DIM, in.key[s0 + q], gx, gy, gz );
+            int l0 = gx - ix0, l1 = gy - iy0, l2 = DIM == 3 ? gz - iz0 : 0;
+            if( l0 < 0 || l0 >= g.T[0] || l1 < 0 || l1 >= g.T[1] || ( DIM == 3 && ( l2 < 0 || l2 >= g.T[2] ) ) ) {
+                atomicCAS( status, 0, SG_ERR_BOUNDS );
+                l0 = l1 = l2 = 0;
+            }
+            const int lc = DIM == 3 ? ( l0 * g.T[1] + l1 ) * g.T[2] + l2 : l0 * g.T[1] + l1;
+            sRank[q] = ( lc << 16 ) | atomicAdd( &sCnt[lc], 1 );
+        }
+        __syncthreads();
+        if( threadIdx.x < 32 ) {
+            int run = 0;
+            for( int base = 0; base < TC; base += 32 ) {
+                const int c = base + ( int )threadIdx.x;
+                const int v = c < TC ? sCnt[c] : 0;
+                int x = v;
+#pragma unroll
+                for( int o = 1; o < 32; o <<= 1 ) {
+                    const int y = __shfl_up_sync( 0xffffffffu, x, o );
+                    if( ( int )threadIdx.x >= o ) x += y;
+                }
+                if( c < TC ) sStart[c] = run + x - v;
+                run += __shfl_sync( 0xffffffffu, x, 31 );
+            }
+        }
+        __syncthreads();
+        // load the tile's particles into their cell-ordered slots (coalesced reads)
+        for( int q = threadIdx.x; q < n; q += blockDim.x ) {
+            const int v = sRank[q];
+            const int lc = v >> 16;
+            const int slot = sStart[lc] + ( v & 0xffff );
+            const int64_t src = s0 + q;
+#pragma unroll
+            for( int d = 0; d < DIM; d++ ) sRec[d * nmax + slot] = in.d[d][src];
+#pragma unroll
+            for( int k = 0; k < 3; k++ ) sRec[( 3 + k ) * nmax + slot] = ( float )in.p[k][src];
+            sRec[7 * nmax + slot] = ( float )in.w[src];
+            sSlotCell[slot] = ( unsigned char )lc;
+        }
+        if( threadIdx.x == 0 ) sNX = 0;
+        __syncthreads();
+    }
     const T qm = T( sp.qm_dts2 );
     const T vs[3] = { T( sp.vs[0] ), T( sp.vs[1] ), T( sp.vs[2] ) };
     const T cr3[3] = { T( sp.cr[0] ), T( sp.cr[1] ), T( sp.cr[2] ) };
@@ -380,7 +513,20 @@ __global__ void __launch_bounds__( 128, MIXED ? 8 : 4 ) k_step_particles(
         double xpn[3] = { 0.0, 0.0, 0.0 };
         T px = T( 0 ), py = T( 0 ), pz = T( 0 ), w = T( 0 );
         if( valid ) {
-            if constexpr( MIXED ) {
+            if constexpr( CELLS ) {
+                // slot q of the cell-ordered planes
+                const int lc = sSlotCell[q];
+                if( DIM == 3 ) {
+                    gnode[0] = ix0 + lc / ( g.T[1] * g.T[2] );
+                    gnode[1] = iy0 + ( lc / g.T[2] ) % g.T[1];
+                    gnode[2] = iz0 + lc % g.T[2];
+                } else {
+                    gnode[0] = ix0 + lc / g.T[1];
+                    gnode[1] = iy0 + lc % g.T[1];
+                }
+#pragma unroll
+                for( int d = 0; d < DIM; d++ ) dlt[d] = ( T )sRec[d * nmax + q];
+            } else if constexpr( MIXED ) {
                 const unsigned key = in.key[src];
                 unpack_key( DIM, key, gnode[0], gnode[1], gnode[2] );
 #pragma unroll
@@ -400,10 +546,17 @@ __global__ void __launch_bounds__( 128, MIXED ? 8 : 4 ) k_step_particles(
                     dlt[d] = ( T )( xpn[d] - ( double )ip );
                 }
             }
-            px = ( T )in.p[0][src];
-            py = ( T )in.p[1][src];
-            pz = ( T )in.p[2][src];
-            w = ( T )in.w[src];
+            if constexpr( CELLS ) {
+                px = ( T )sRec[3 * nmax + q];
+                py = ( T )sRec[4 * nmax + q];
+                pz = ( T )sRec[5 * nmax + q];
+                w = ( T )sRec[7 * nmax + q];
+            } else {
+                px = ( T )in.p[0][src];
+                py = ( T )in.p[1][src];
+                pz = ( T )in.p[2][src];
+                w = ( T )in.w[src];
+            }
         }
         lx[0] = gnode[0] - ix0;
         lx[1] = gnode[1] - iy0;
@@ -490,60 +643,32 @@ __global__ void __launch_bounds__( 128, MIXED ? 8 : 4 ) k_step_particles(
             for( int d = 0; d < DIM; d++ ) shift[d] = shift[d] < -1 ? -1 : ( shift[d] > 1 ? 1 : shift[d] );
         }
 
-        // ---- Esirkepov deposit into the shared J tile ------------------------
+        // ---- Esirkepov deposit: direct, or a record for the per-cell pass ----
         if( valid ) {
-            EsirWin<T> W[3];
-#pragma unroll
-            for( int d = 0; d < DIM; d++ ) esir_win<T>( cp[d][0], cp[d][1], cp[d][2], dnew[d], shift[d], W[d] );
-            const T cw = cw0 * w;
-            const T twelfth = T( 1.0 / 12.0 );
-            if( DIM == 3 ) {
-                const T cr[3] = { cr3[0] * w, cr3[1] * w, cr3[2] * w };
-                // Jx(d,p,p): node i' = lo+1+m, j = lo+jw, k = lo+kw (tile index = old node + stencil index)
-#pragma unroll
-                for( int c = 0; c < 3; c++ ) {
-                    const int a = c, b = ( c + 1 ) % 3, e = ( c + 2 ) % 3;
-                    T *J = sJ + c * jsz;
-#pragma unroll
-                    for( int u = 0; u < 4; u++ )
-#pragma unroll
-                        for( int v = 0; v < 4; v++ ) {
-                            const T wgt = W[b].A[u] * W[e].A[v] + twelfth * W[b].D[u] * W[e].D[v];
-                            int idx[3];
-                            idx[b] = lx[b] + W[b].lo + u;
-                            idx[e] = lx[e] + W[e].lo + v;
-#pragma unroll
-                            for( int m = 0; m < 3; m++ ) {
-                                idx[a] = lx[a] + W[a].lo + 1 + m;
-                                const T val = -cr[a] * W[a].P[m] * wgt;
-                                sh_add( &J[( idx[0] * td.JY + idx[1] ) * td.JZ + idx[2]], val );
-                            }
-                        }
-                }
+            if constexpr( CELLS ) {
+                const int sbits = ( shift[0] + 1 ) | ( ( shift[1] + 1 ) << 2 ) | ( ( shift[2] + 1 ) << 4 );
+                sRec[3 * nmax + q] = ( float )dnew[0];
+                sRec[4 * nmax + q] = ( float )dnew[1];
+                sRec[5 * nmax + q] = DIM == 3 ? ( float )dnew[2] : ( float )( pz * ginv );
+                sRec[6 * nmax + q] = __int_as_float( sbits );
             } else {
-                const T crx = cr3[0] * w, cry = cr3[1] * w;
-                const T crz = cw * pz * ginv;
-                T *J0 = sJ, *J1 = sJ + jsz, *J2 = sJ + 2 * jsz;
+                EsirWin<T> W[3];
 #pragma unroll
-                for( int u = 0; u < 4; u++ ) {
-                    const T ay = W[1].A[u];
-                    if( ay != T( 0 ) ) {
-#pragma unroll
-                        for( int m = 0; m < 3; m++ )
-                            sh_add( &J0[( lx[0] + W[0].lo + 1 + m ) * td.JY + lx[1] + W[1].lo + u], -crx * W[0].P[m] * ay );
-                    }
-                    const T ax = W[0].A[u];
-                    if( ax != T( 0 ) ) {
-#pragma unroll
-                        for( int m = 0; m < 3; m++ )
-                            sh_add( &J1[( lx[0] + W[0].lo + u ) * td.JY + lx[1] + W[1].lo + 1 + m], -cry * W[1].P[m] * ax );
-                    }
-#pragma unroll
-                    for( int v = 0; v < 4; v++ ) {
-                        const T wz = W[0].A[u] * W[1].A[v] + twelfth * W[0].D[u] * W[1].D[v];
-                        sh_add( &J2[( lx[0] + W[0].lo + u ) * td.JY + lx[1] + W[1].lo + v], crz * wz );
-                    }
-                }
+                for( int d = 0; d < DIM; d++ ) esir_win<T>( cp[d][0], cp[d][1], cp[d][2], dnew[d], shift[d], W[d] );
+                const T cr[3] = { cr3[0] * w, cr3[1] * w, cr3[2] * w };
+                deposit_direct<DIM, T>( sJ, td, jsz, lx, W, cr, cw0 * w * pz * ginv );
+            }
+        }
+
+        if constexpr( CELLS ) {
+            // node-changing particles go to a list deposited with full warps later
+            const bool cross = valid && ( shift[0] | shift[1] | shift[2] ) != 0;
+            const unsigned xm = __ballot_sync( 0xffffffffu, cross );
+            if( xm ) {
+                int xb = 0;
+                if( lane == 0 ) xb = atomicAdd( &sNX, __popc( xm ) );
+                xb = __shfl_sync( 0xffffffffu, xb, 0 );
+                if( cross ) sRank[xb + __popc( xm & ( ( 1u << lane ) - 1u ) )] = q;
             }
         }
 
@@ -618,6 +743,154 @@ __global__ void __launch_bounds__( 128, MIXED ? 8 : 4 ) k_step_particles(
         }
     }
     __syncthreads();
+
+    // 3. per-cell deposit (CELLS).  Particles that stay on their node in every
+    // dimension share their cell's fixed footprint: stencil points 1..3 across the
+    // current, 2..3 along it (point 4 carries only the rounding residue of a sum
+    // that is zero).  Their contributions are summed in registers and added once
+    // per cell; particles that change node are deposited directly.  3D: thread
+    // t works on cell t % TC, group j = t / TC; even groups own Jx and the lower
+    // Jz plane, odd groups Jy and the upper one; groups j>>1 split the records.
+    // 2D: the groups split the records and own all three components.
+    if constexpr( CELLS ) {
+        // groups per cell (even in 3D: the two halves of the footprint pair up)
+        const int tpc = DIM == 3 ? ( ( int )( blockDim.x / TC ) & ~1 ) : ( int )( blockDim.x / TC );
+        const int c = threadIdx.x % TC, grp = threadIdx.x / TC;
+        if( grp < tpc ) {
+            int cl[3];
+            if( DIM == 3 ) {
+                cl[2] = c % g.T[2];
+                cl[1] = ( c / g.T[2] ) % g.T[1];
+                cl[0] = c / ( g.T[2] * g.T[1] );
+            } else {
+                cl[2] = 0;
+                cl[1] = c % g.T[1];
+                cl[0] = c / g.T[1];
+            }
+            const T twelfth = T( 1.0 / 12.0 );
+            const int hf = DIM == 3 ? ( grp & 1 ) : 0;
+            const int q0 = DIM == 3 ? ( grp >> 1 ) : grp, qstep = DIM == 3 ? ( tpc >> 1 ) : tpc;
+            // 3D: acc = along-axis current (m, u, v), accz = Jz plane hf (u, v)
+            // 2D: acc = Jx (m, u) then Jy (u, m), accz = Jz (u, v)
+            T acc[18], accz[9];
+#pragma unroll
+            for( int k = 0; k < 18; k++ ) acc[k] = T( 0 );
+#pragma unroll
+            for( int k = 0; k < 9; k++ ) accz[k] = T( 0 );
+            const int end = sStart[c] + sCnt[c];
+            for( int q = sStart[c] + q0; q < end; q += qstep ) {
+                if( __float_as_int( sRec[6 * nmax + q] ) != NO_SHIFT ) continue; // in the node-changing list
+                T dold[3], dn[3];
+                dold[0] = sRec[q];
+                dold[1] = sRec[nmax + q];
+                dold[2] = DIM == 3 ? sRec[2 * nmax + q] : T( 0 );
+                dn[0] = sRec[3 * nmax + q];
+                dn[1] = sRec[4 * nmax + q];
+                dn[2] = DIM == 3 ? sRec[5 * nmax + q] : T( 0 );
+                const T vz = DIM == 3 ? T( 0 ) : sRec[5 * nmax + q];
+                const T wq = sRec[7 * nmax + q];
+                const T cr[3] = { cr3[0] * wq, cr3[1] * wq, cr3[2] * wq };
+                {
+                    T A[3][3], D[3][3], P[3][2];
+#pragma unroll
+                    for( int d = 0; d < DIM; d++ ) {
+                        T o0, o1, o2, n0, n1, n2;
+                        bspline2( dold[d], o0, o1, o2 );
+                        bspline2( dn[d], n0, n1, n2 );
+                        A[d][0] = T( 0.5 ) * ( o0 + n0 ); A[d][1] = T( 0.5 ) * ( o1 + n1 ); A[d][2] = T( 0.5 ) * ( o2 + n2 );
+                        D[d][0] = n0 - o0; D[d][1] = n1 - o1; D[d][2] = n2 - o2;
+                        P[d][0] = D[d][0];
+                        P[d][1] = D[d][0] + D[d][1];
+                    }
+                    if( DIM == 3 ) {
+                        // along-axis a = hf, transverse b = 1 - hf and 2
+                        const T cra = hf ? cr[1] : cr[0];
+                        const T pa0 = hf ? P[1][0] : P[0][0], pa1 = hf ? P[1][1] : P[0][1];
+                        const T pz = hf ? P[2][1] : P[2][0];
+#pragma unroll
+                        for( int u = 0; u < 3; u++ ) {
+                            const T ab = hf ? A[0][u] : A[1][u], db = hf ? D[0][u] : D[1][u];
+#pragma unroll
+                            for( int v = 0; v < 3; v++ ) {
+                                const T wt = ab * A[2][v] + twelfth * db * D[2][v];
+                                acc[( 0 * 3 + u ) * 3 + v] -= cra * pa0 * wt;
+                                acc[( 1 * 3 + u ) * 3 + v] -= cra * pa1 * wt;
+                                const T wz = A[0][u] * A[1][v] + twelfth * D[0][u] * D[1][v];
+                                accz[u * 3 + v] -= cr[2] * pz * wz;
+                            }
+                        }
+                    } else {
+                        const T crz = cw0 * wq * vz;
+#pragma unroll
+                        for( int u = 0; u < 3; u++ ) {
+#pragma unroll
+                            for( int m = 0; m < 2; m++ ) {
+                                acc[m * 3 + u] -= cr[0] * P[0][m] * A[1][u];
+                                acc[6 + u * 2 + m] -= cr[1] * P[1][m] * A[0][u];
+                            }
+#pragma unroll
+                            for( int v = 0; v < 3; v++ ) accz[u * 3 + v] += crz * ( A[0][u] * A[1][v] + twelfth * D[0][u] * D[1][v] );
+                        }
+                    }
+                }
+            }
+            if( DIM == 3 ) {
+                T *Ja = sJ + hf * jsz, *Jz = sJ + 2 * jsz;
+#pragma unroll
+                for( int u = 0; u < 3; u++ )
+#pragma unroll
+                    for( int v = 0; v < 3; v++ ) {
+#pragma unroll
+                        for( int m = 0; m < 2; m++ ) {
+                            const int ia = ( hf ? cl[0] + 1 + u : cl[0] + 2 + m ), ib = ( hf ? cl[1] + 2 + m : cl[1] + 1 + u );
+                            sh_add( &Ja[( ia * td.JY + ib ) * td.JZ + cl[2] + 1 + v], acc[( m * 3 + u ) * 3 + v] );
+                        }
+                        sh_add( &Jz[( ( cl[0] + 1 + u ) * td.JY + cl[1] + 1 + v ) * td.JZ + cl[2] + 2 + hf], accz[u * 3 + v] );
+                    }
+            } else {
+                T *J0 = sJ, *J1 = sJ + jsz, *J2 = sJ + 2 * jsz;
+#pragma unroll
+                for( int u = 0; u < 3; u++ ) {
+#pragma unroll
+                    for( int m = 0; m < 2; m++ ) {
+                        sh_add( &J0[( cl[0] + 2 + m ) * td.JY + cl[1] + 1 + u], acc[m * 3 + u] );
+                        sh_add( &J1[( cl[0] + 1 + u ) * td.JY + cl[1] + 2 + m], acc[6 + u * 2 + m] );
+                    }
+#pragma unroll
+                    for( int v = 0; v < 3; v++ ) sh_add( &J2[( cl[0] + 1 + u ) * td.JY + cl[1] + 1 + v], accz[u * 3 + v] );
+                }
+            }
+        }
+        // node-changing particles, one per thread
+        for( int k = threadIdx.x; k < sNX; k += blockDim.x ) {
+            const int q = sRank[k];
+            const int lc = sSlotCell[q];
+            int cl[3];
+            if( DIM == 3 ) {
+                cl[2] = lc % g.T[2];
+                cl[1] = ( lc / g.T[2] ) % g.T[1];
+                cl[0] = lc / ( g.T[2] * g.T[1] );
+            } else {
+                cl[2] = 0;
+                cl[1] = lc % g.T[1];
+                cl[0] = lc / g.T[1];
+            }
+            const int sbits = __float_as_int( sRec[6 * nmax + q] );
+            const int sh[3] = { ( sbits & 3 ) - 1, ( ( sbits >> 2 ) & 3 ) - 1, ( ( sbits >> 4 ) & 3 ) - 1 };
+            const T wq = sRec[7 * nmax + q];
+            const T cr[3] = { cr3[0] * wq, cr3[1] * wq, cr3[2] * wq };
+            const T vz = DIM == 3 ? T( 0 ) : sRec[5 * nmax + q];
+            EsirWin<T> W[3];
+#pragma unroll
+            for( int d = 0; d < DIM; d++ ) {
+                T o0, o1, o2;
+                bspline2( ( T )sRec[d * nmax + q], o0, o1, o2 );
+                esir_win<T>( o0, o1, o2, ( T )sRec[( 3 + d ) * nmax + q], sh[d], W[d] );
+            }
+            deposit_direct<DIM, T>( sJ, td, jsz, cl, W, cr, cw0 * wq * vz );
+        }
+        __syncthreads();
+    }
 
     // 4. flush the J tile (origin = array index i0 + OS - 2) with global atomics
     const TileMap jm = tile_map<DIM>( td.JY, td.JZ );
@@ -1024,6 +1297,7 @@ struct SpeciesState {
     PBuf<false> od{};
     PBuf<true> om{};
     int *ovf_tile = nullptr;
+    int max_cap = 0; // largest tile segment of the current layout
 };
 
 // Carves a particle SoA of `n` elements out of one allocation.
@@ -1111,6 +1385,14 @@ Fields<T> field_view( sg_sim *S )
 // comp 0..2 E, 3..5 B, 6..8 B_m, 9..11 J -> staggering flags
 inline int comp_stag( int comp, int d ) { return comp < 3 ? stag( comp, d ) : ( comp < 9 ? stag( 3 + ( comp % 3 ), d ) : stag( comp - 9, d ) ); }
 
+// Shared memory of the per-cell mode: REC planes of nmax floats, a count and a
+// start per cell, a packed (cell, rank) word per particle, a cell byte per slot.
+constexpr size_t CELLS_SMEM_LIMIT = 200 * 1024;
+inline size_t cells_smem_bytes( int tc, int nmax )
+{
+    return ( size_t )REC * 4 * nmax + ( size_t )8 * tc + ( size_t )4 * nmax + ( ( ( size_t )nmax + 15 ) & ~( size_t )15 );
+}
+
 template <int DIM, bool MIXED, int KIND>
 int launch_particles( sg_sim *S, SpeciesState &s, cudaStream_t st )
 {
@@ -1130,12 +1412,24 @@ int launch_particles( sg_sim *S, SpeciesState &s, cudaStream_t st )
         sp.cr[d] = sp.cw * S->g.dx[d] / S->g.dt;
         sp.vs[d] = S->g.dt * S->g.dxi[d];
     }
-    auto kern = k_step_particles<DIM, MIXED, KIND>;
-    if( S->smem_bytes > 48 * 1024 ) SG_CUDA_TRY( cudaFuncSetAttribute( kern, cudaFuncAttributeMaxDynamicSharedMemorySize, ( int )S->smem_bytes ) );
+    // The mixed form deposits per cell when the tile's records fit in shared memory
+    // next to the field and current tiles (one tile = at most 128 cells).
+    auto kern = k_step_particles<DIM, MIXED, KIND, false>;
+    size_t smem = S->smem_bytes;
+    if constexpr( MIXED ) {
+        const int tc = S->g.T[0] * S->g.T[1] * ( DIM == 3 ? S->g.T[2] : 1 );
+        const size_t extra = cells_smem_bytes( tc, s.max_cap );
+        // 3D needs two thread groups per cell (the footprint is split between them)
+        if( tc <= ( DIM == 3 ? 64 : 128 ) && s.max_cap < 32768 && smem + extra <= CELLS_SMEM_LIMIT ) {
+            kern = k_step_particles<DIM, MIXED, KIND, true>;
+            smem += extra;
+        }
+    }
+    if( smem > 48 * 1024 ) SG_CUDA_TRY( cudaFuncSetAttribute( kern, cudaFuncAttributeMaxDynamicSharedMemorySize, ( int )smem ) );
     const int sidx = ( int )( &s - &S->sp[0] );
-    kern<<<S->g.ntiles, 128, S->smem_bytes, st>>>( S->g, field_view<T>( S ), sp, bin, bout, s.seg_start, s.cap, s.count[in],
-                                                   s.count[out], bov, s.ovf_tile, S->d_flags + 1 + sidx,
-                                                   ( int )s.ovf_capacity, S->d_flags );
+    kern<<<S->g.ntiles, 128, smem, st>>>( S->g, field_view<T>( S ), sp, bin, bout, s.seg_start, s.cap, s.count[in],
+                                          s.count[out], bov, s.ovf_tile, S->d_flags + 1 + sidx, ( int )s.ovf_capacity,
+                                          S->d_flags, s.max_cap );
     SG_LAUNCH_CHECK( "k_step_particles" );
     return SG_OK;
 }
@@ -1247,7 +1541,7 @@ int alloc_species_buffers( sg_sim *S, SpeciesState &s, int64_t capacity )
 }
 
 // New segment layout from counts: cap, seg_start into (new_cap, new_start); returns the total.
-int layout_from_counts( sg_sim *S, const int *count, int *new_cap, int64_t *new_start, int64_t *total )
+int layout_from_counts( sg_sim *S, const int *count, int *new_cap, int64_t *new_start, int64_t *total, int *max_cap )
 {
     const int nt = S->g.ntiles;
     const float slack = ( float )( S->cfg.capacity_slack > 0.0 ? S->cfg.capacity_slack : 0.25 );
@@ -1261,8 +1555,12 @@ int layout_from_counts( sg_sim *S, const int *count, int *new_cap, int64_t *new_
     int last_cap = 0;
     SG_CUDA_TRY( cudaMemcpyAsync( &last_start, new_start + nt - 1, sizeof( int64_t ), cudaMemcpyDeviceToHost, S->stream ) );
     SG_CUDA_TRY( cudaMemcpyAsync( &last_cap, new_cap + nt - 1, sizeof( int ), cudaMemcpyDeviceToHost, S->stream ) );
+    std::vector<int> caps( nt );
+    SG_CUDA_TRY( cudaMemcpyAsync( caps.data(), new_cap, nt * sizeof( int ), cudaMemcpyDeviceToHost, S->stream ) );
     SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
     *total = last_start + last_cap;
+    *max_cap = 0;
+    for( int t = 0; t < nt; t++ ) *max_cap = std::max( *max_cap, caps[t] );
     return SG_OK;
 }
 
@@ -1283,7 +1581,8 @@ int relayout( sg_sim *S, SpeciesState &s, int nspill )
 {
     const int nt = S->g.ntiles;
     int64_t total = 0;
-    int r = layout_from_counts( S, s.count[s.cur], S->tmp_cap, S->tmp_start, &total );
+    int new_max_cap = 0;
+    int r = layout_from_counts( S, s.count[s.cur], S->tmp_cap, S->tmp_start, &total, &new_max_cap );
     if( r ) return r;
     // destination: the idle buffer, or fresh buffers when the layout no longer fits
     void *old_mem[2] = { s.mem[0], s.mem[1] };
@@ -1304,6 +1603,7 @@ int relayout( sg_sim *S, SpeciesState &s, int nspill )
     // new layout becomes current
     std::swap( s.seg_start, S->tmp_start );
     std::swap( s.cap, S->tmp_cap );
+    s.max_cap = new_max_cap;
     if( S->mixed ) r = place_staged<true>( S, s, nspill, s.om, s.ovf_tile, dst_buf );
     else r = place_staged<false>( S, s, nspill, s.od, s.ovf_tile, dst_buf );
     if( r ) return r;
@@ -1495,7 +1795,7 @@ int sg_sim_add_species_device( sg_sim *S, double mass, double charge, int pusher
         SG_LAUNCH_CHECK( "k_stage" );
     }
     int64_t total = 0;
-    int r = layout_from_counts( S, s.count[1], s.cap, s.seg_start, &total );
+    int r = layout_from_counts( S, s.count[1], s.cap, s.seg_start, &total, &s.max_cap );
     if( r ) return r;
     r = alloc_species_buffers( S, s, std::max<int64_t>( total, 1 ) );
     if( r ) return r;
