@@ -60,6 +60,8 @@ _SIGNATURES = {
     "sg_center_magnetic_fields": (_I, [ctypes.POINTER(GridGeom), _PP, _PP, _VP]),
     "sg_sort_particles": (_I, [_I, ctypes.POINTER(_I), ctypes.POINTER(_D), ctypes.POINTER(_D), _I64, _PP, _I, _VP,
                                _VP, _VP, _VP, _VP]),
+    "sg_sort_particles_noalloc": (_I, [_I, ctypes.POINTER(_I), ctypes.POINTER(_D), ctypes.POINTER(_D), _I64, _PP,
+                                       _I, _VP, _VP, _VP, _VP, _VP]),
     "sg_sim_create": (_I, [ctypes.POINTER(SimConfig), ctypes.POINTER(_VP)]),
     "sg_sim_destroy": (_I, [_VP]),
     "sg_sim_add_species": (_I, [_VP, _D, _D, _I, _I64, _VP, _VP, _VP, ctypes.POINTER(_I)]),

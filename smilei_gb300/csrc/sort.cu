@@ -11,6 +11,9 @@
 #include "common.cuh"
 #include "scan.cuh"
 
+#include <cmath>
+#include <mutex>
+
 namespace sg {
 namespace {
 
@@ -186,6 +189,115 @@ extern "C" int sg_sort_particles( int ndim, const int *patch_size, const double 
     cudaError_t fe = cudaFreeAsync( scratch, s );
     if( rc ) return rc;
     if( fe != cudaSuccess ) return cuda_fail( fe, "cudaFreeAsync", __FILE__, __LINE__ );
+    SG_CUDA_TRY( cudaStreamSynchronize( s ) );
+    if( h_status ) return set_error( h_status, "a particle lies outside the patch's node lattice" );
+    return SG_OK;
+}
+
+// ---- per-cell sort without allocation --------------------------------------
+//
+// Some callers cannot call cudaMalloc: code running while a CUDA graph is being
+// captured in global mode, where allocation calls are refused; hosts that hand
+// the library a fixed device-memory budget and forbid it to grow; and real-time
+// loops in which an allocation's implicit synchronisation or latency is not
+// acceptable.  sg_sort_particles_noalloc serves them with the same sort on a
+// scratch area that is part of the library's own device image: a file-scope
+// __device__ array of SG_SORT_NOALLOC_SCRATCH_BYTES, present on every GPU that
+// loads the library until the process exits.  The host learns its device
+// address once per device through cudaGetSymbolAddress (the array's name in
+// host code is only a host-side stand-in and must never be passed to a kernel).
+
+namespace sg {
+namespace {
+
+static __device__ __align__( 256 ) unsigned char g_sort_scratch[SG_SORT_NOALLOC_SCRATCH_BYTES];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_scratch_mu;
+void *g_scratch_dev[NOALLOC_MAX_DEVICES] = {};
+
+// Device address of g_sort_scratch on the current device, looked up on the first
+// call made with that device current.
+int noalloc_scratch( char **out )
+{
+    int dev = -1;
+    SG_CUDA_TRY( cudaGetDevice( &dev ) );
+    if( dev < 0 || dev >= NOALLOC_MAX_DEVICES ) return set_error( SG_ERR_ARG, "device ordinal %d not supported", dev );
+    std::lock_guard<std::mutex> lock( g_scratch_mu );
+    if( !g_scratch_dev[dev] ) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress( &p, g_sort_scratch );
+        if( e != cudaSuccess ) return cuda_fail( e, "cudaGetSymbolAddress(g_sort_scratch)", __FILE__, __LINE__ );
+        g_scratch_dev[dev] = p;
+    }
+    *out = static_cast<char *>( g_scratch_dev[dev] );
+    return SG_OK;
+}
+
+} // namespace
+} // namespace sg
+
+extern "C" int sg_sort_particles_noalloc( int ndim, const int *patch_size, const double *xmin,
+                                          const double *cell_length, int64_t npart, double *const *dprops,
+                                          int n_dprops, short *charge, int *first_index, int *last_index,
+                                          int *cell_keys, sg_stream_t stream )
+{
+    SG_REQUIRE( ndim >= 1 && ndim <= 3, "ndim must be 1..3" );
+    SG_REQUIRE( patch_size && xmin && cell_length, "NULL geometry" );
+    SG_REQUIRE( npart >= 0, "npart out of range" );
+    SG_REQUIRE( npart <= SG_SORT_NOALLOC_MAX_PARTICLES,
+                "sg_sort_particles_noalloc: %lld particles exceed its fixed scratch limit of %d; use sg_sort_particles",
+                ( long long )npart, SG_SORT_NOALLOC_MAX_PARTICLES );
+    SG_REQUIRE( n_dprops >= ndim, "dprops must start with the ndim position arrays" );
+    SG_REQUIRE( dprops && first_index && last_index, "NULL array" );
+    KeyGeom g{};
+    g.ndim = ndim;
+    int64_t ncell64 = 1;
+    for( int d = 0; d < ndim; d++ ) {
+        SG_REQUIRE( patch_size[d] > 0 && cell_length[d] > 0.0, "bad patch size / cell length in dim %d", d );
+        g.len[d] = patch_size[d] + 1;
+        g.dxi[d] = 1.0 / cell_length[d];
+        g.mn[d] = std::round( xmin[d] * g.dxi[d] );
+        ncell64 *= g.len[d];
+    }
+    SG_REQUIRE( ncell64 <= SG_SORT_NOALLOC_MAX_CELLS,
+                "sg_sort_particles_noalloc: %lld cells exceed its fixed scratch limit of %d; use sg_sort_particles",
+                ( long long )ncell64, SG_SORT_NOALLOC_MAX_CELLS );
+    const int ncell = ( int )ncell64;
+    // same scratch layout as sg_sort_particles, carved from the static array
+    const int64_t scan_elems = scan_scratch_elems( ncell );
+    const size_t n_i64 = ( size_t )ncell + ( size_t )scan_elems + 8;
+    const size_t n_int = ( size_t )npart * 2 + ( size_t )ncell * 2 + 64;
+    const size_t off_int = n_i64 * 8;
+    const size_t off_tmp = ( ( off_int + n_int * 4 + 255 ) / 256 ) * 256;
+    const size_t bytes = off_tmp + ( size_t )npart * 8;
+    SG_REQUIRE( bytes <= ( size_t )SG_SORT_NOALLOC_SCRATCH_BYTES,
+                "sg_sort_particles_noalloc: needs %zu scratch bytes, more than its %d", bytes,
+                SG_SORT_NOALLOC_SCRATCH_BYTES );
+    char *scratch = nullptr;
+    int rc = noalloc_scratch( &scratch );
+    if( rc ) return rc;
+    cudaStream_t s = as_stream( stream );
+    if( npart == 0 ) {
+        SG_CUDA_TRY( cudaMemsetAsync( first_index, 0, ncell * sizeof( int ), s ) );
+        SG_CUDA_TRY( cudaMemsetAsync( last_index, 0, ncell * sizeof( int ), s ) );
+        return SG_OK;
+    }
+    int64_t *off = reinterpret_cast<int64_t *>( scratch );
+    int64_t *scan_tmp = off + ncell;
+    int *keys = reinterpret_cast<int *>( scratch + off_int );
+    int *perm = keys + npart;
+    int *count = perm + npart;
+    int *fill = count + ncell;
+    int *status = fill + ncell;
+    double *tmp = reinterpret_cast<double *>( scratch + off_tmp );
+    // The array keeps the previous call's contents: the per-cell counts and the
+    // status word are cleared inside sort_with_scratch; every other region is
+    // fully written before it is read.
+    int h_status = 0;
+    rc = sort_with_scratch( g, ncell, npart, dprops, n_dprops, charge, first_index, last_index, cell_keys, off,
+                            scan_tmp, keys, perm, count, fill, status, tmp, s, &h_status );
+    if( rc ) return rc;
     SG_CUDA_TRY( cudaStreamSynchronize( s ) );
     if( h_status ) return set_error( h_status, "a particle lies outside the patch's node lattice" );
     return SG_OK;
