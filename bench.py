@@ -49,6 +49,13 @@ def workload_cfg(args):
                 sigma=SIGMA_10KEV)
 
 
+# DRAM bytes read + written per particle by one k_step_particles launch: one ncu
+# capture (dram__bytes_read.sum + dram__bytes_write.sum) of the 3D thermal case at
+# 128^3 cells x 8 ppc, divided by its 16,777,216 particles; a launch over N particles
+# at the same ppc moves N times this.  None where no capture has been taken.
+NCU_TRAFFIC_BYTES_PER_PARTICLE = {"mixed": (664.260096e6 + 530.957312e6) / 16777216, "fp64": None}
+
+
 def bytes_alg_per_particle_step(form, ppc):
     """B_alg = S_state + 24 * s / ppc (state read+write once; 24 grid values per cell per step)."""
     if form == "mixed":
@@ -311,6 +318,8 @@ def main():
             td.destroy_process_group()
         return
     achieved = res["kernel_bytes"] / res["t_kernel"] / 1e9
+    tpp = NCU_TRAFFIC_BYTES_PER_PARTICLE.get(args.form)
+    traffic = tpp * res["n"] if (tpp is not None and args.ppc == 8) else None
     step_gbs = res["B_alg"] * res["value"] / 1e9
     line = {
         "metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -323,8 +332,8 @@ def main():
                    "hbm_fraction_of_step": step_gbs / res["peak"], "wall_ms_per_step": res["wall_ms_per_step"],
                    "energy_ukin_uelm_before_after": res["energy"]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": res["peak"], "unit": "GB/s",
-                     "frac": achieved / res["peak"], "traffic": None, "kernel": "k_step_particles",
-                     "peak_source": res["peak_kind"]},
+                     "frac": achieved / res["peak"], "traffic": traffic, "kernel": "k_step_particles",
+                     "algorithmic_bytes_per_launch": res["kernel_bytes"], "peak_source": res["peak_kind"]},
         "cpu_baseline": cpu,
         "e2e": res["e2e"],
         "gpu_launches": res["launches"] * args.steps,

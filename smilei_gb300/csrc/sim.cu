@@ -128,6 +128,26 @@ __host__ __device__ inline int tile_of( const GridInfo &g, int ix, int iy, int i
 // cross section of at most 8 x 8 use 8 lanes per row and 8 rows per x plane
 // (no divisions); 2D tiles with at most 16 points per row use 16 lanes per row.
 // Other shapes fall back to a division per point.
+// Asynchronous global -> shared copy of one 4- or 8-byte word (cp.async, sm_80+).
+// When `valid` is false nothing is read (src-size 0) and the word is zero-filled;
+// `src` must still be a valid address then.
+template <class T>
+__device__ __forceinline__ void cp_async_word( T *dst, const T *src, bool valid )
+{
+    static_assert( sizeof( T ) == 4 || sizeof( T ) == 8, "4- or 8-byte words" );
+    const unsigned d = ( unsigned )__cvta_generic_to_shared( dst );
+    const int n = valid ? ( int )sizeof( T ) : 0;
+    if( sizeof( T ) == 4 )
+        asm volatile( "cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"( d ), "l"( src ), "r"( n ) : "memory" );
+    else
+        asm volatile( "cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"( d ), "l"( src ), "r"( n ) : "memory" );
+}
+
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile( "cp.async.wait_all;\n" ::: "memory" );
+}
+
 struct TileMap {
     int cx0, cy, cz, step; // first x, this thread's (y, z), x stride
     bool fast, active;
@@ -303,6 +323,9 @@ __device__ __forceinline__ void esir_win( T c0o, T c1o, T c2o, T dnew, int shift
             w.P[i] = run;
         }
     }
+    // with no node change the sum over the whole window is S1 - S0 summed, zero up to
+    // rounding: the last current node gets nothing
+    if( shift == 0 ) w.P[2] = T( 0 );
 }
 
 // Esirkepov deposit of one particle straight into the shared J tile (atomics):
@@ -415,27 +438,30 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
         const int ny = ext( g, 1, stag( c, 1 ) ), nz = ext( g, 2, stag( c, 2 ) );
         const int nx = ext( g, 0, stag( c, 0 ) );
         T *dst = sF + c * fsz;
+        // asynchronous copies: every word of the tile is in flight at once
         if( fm.fast ) {
             if( fm.active ) {
                 const int gy = iy0 + OS - 1 + fm.cy, gz = DIM == 3 ? iz0 + OS - 1 + fm.cz : 0;
                 for( int cx = fm.cx0; cx < td.FX; cx += fm.step ) {
                     const int gx = ix0 + OS - 1 + cx;
-                    T v = T( 0 );
-                    if( gx < nx && gy < ny && gz < nz ) v = src[( ( int64_t )gx * ny + gy ) * nz + gz];
-                    dst[( cx * td.FY + fm.cy ) * td.FZ + fm.cz] = v;
+                    const bool in = gx < nx && gy < ny && gz < nz;
+                    cp_async_word( &dst[( cx * td.FY + fm.cy ) * td.FZ + fm.cz],
+                                   in ? &src[( ( int64_t )gx * ny + gy ) * nz + gz] : src, in );
                 }
             }
         } else {
             for( int e = threadIdx.x; e < fsz; e += blockDim.x ) {
                 const int cz = e % td.FZ, cy = ( e / td.FZ ) % td.FY, cx = e / ( td.FZ * td.FY );
                 const int gx = ix0 + OS - 1 + cx, gy = iy0 + OS - 1 + cy, gz = DIM == 3 ? iz0 + OS - 1 + cz : 0;
-                T v = T( 0 );
-                if( gx < nx && gy < ny && gz < nz ) v = src[( ( int64_t )gx * ny + gy ) * nz + gz];
-                dst[e] = v;
+                const bool in = gx < nx && gy < ny && gz < nz;
+                cp_async_word( &dst[e], in ? &src[( ( int64_t )gx * ny + gy ) * nz + gz] : src, in );
             }
         }
     }
     for( int e = threadIdx.x; e < 3 * jsz; e += blockDim.x ) sJ[e] = T( 0 );
+    // per-cell mode keeps the field copies in flight through the ranking and waits
+    // for them together with the particle copies
+    if constexpr( !CELLS ) cp_async_wait_all();
     __syncthreads();
 
     int n = count_in[tile];
@@ -450,16 +476,28 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
         // rank of every particle inside its cell, then the cells' start offsets
         for( int c = threadIdx.x; c < TC; c += blockDim.x ) sCnt[c] = 0;
         __syncthreads();
-        for( int q = threadIdx.x; q < n; q += blockDim.x ) {
-            int gx, gy, gz;
-            unpack_key( DIM, in.key[s0 + q], gx, gy, gz );
-            int l0 = gx - ix0, l1 = gy - iy0, l2 = DIM == 3 ? gz - iz0 : 0;
-            if( l0 < 0 || l0 >= g.T[0] || l1 < 0 || l1 >= g.T[1] || ( DIM == 3 && ( l2 < 0 || l2 >= g.T[2] ) ) ) {
-                atomicCAS( status, 0, SG_ERR_BOUNDS );
-                l0 = l1 = l2 = 0;
+        constexpr int KB = 4; // keys loaded per thread before ranking (independent loads in flight)
+        for( int qb = threadIdx.x; qb < n; qb += KB * blockDim.x ) {
+            unsigned key[KB];
+#pragma unroll
+            for( int j = 0; j < KB; j++ ) {
+                const int q = qb + j * blockDim.x;
+                key[j] = q < n ? in.key[s0 + q] : 0u;
             }
-            const int lc = DIM == 3 ? ( l0 * g.T[1] + l1 ) * g.T[2] + l2 : l0 * g.T[1] + l1;
-            sRank[q] = ( lc << 16 ) | atomicAdd( &sCnt[lc], 1 );
+#pragma unroll
+            for( int j = 0; j < KB; j++ ) {
+                const int q = qb + j * blockDim.x;
+                if( q >= n ) break;
+                int gx, gy, gz;
+                unpack_key( DIM, key[j], gx, gy, gz );
+                int l0 = gx - ix0, l1 = gy - iy0, l2 = DIM == 3 ? gz - iz0 : 0;
+                if( l0 < 0 || l0 >= g.T[0] || l1 < 0 || l1 >= g.T[1] || ( DIM == 3 && ( l2 < 0 || l2 >= g.T[2] ) ) ) {
+                    atomicCAS( status, 0, SG_ERR_BOUNDS );
+                    l0 = l1 = l2 = 0;
+                }
+                const int lc = DIM == 3 ? ( l0 * g.T[1] + l1 ) * g.T[2] + l2 : l0 * g.T[1] + l1;
+                sRank[q] = ( lc << 16 ) | atomicAdd( &sCnt[lc], 1 );
+            }
         }
         __syncthreads();
         if( threadIdx.x < 32 ) {
@@ -485,13 +523,14 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
             const int slot = sStart[lc] + ( v & 0xffff );
             const int64_t src = s0 + q;
 #pragma unroll
-            for( int d = 0; d < DIM; d++ ) sRec[d * nmax + slot] = in.d[d][src];
+            for( int d = 0; d < DIM; d++ ) cp_async_word( &sRec[d * nmax + slot], &in.d[d][src], true );
 #pragma unroll
-            for( int k = 0; k < 3; k++ ) sRec[( 3 + k ) * nmax + slot] = ( float )in.p[k][src];
-            sRec[7 * nmax + slot] = ( float )in.w[src];
+            for( int k = 0; k < 3; k++ ) cp_async_word( &sRec[( 3 + k ) * nmax + slot], &in.p[k][src], true );
+            cp_async_word( &sRec[7 * nmax + slot], &in.w[src], true );
             sSlotCell[slot] = ( unsigned char )lc;
         }
         if( threadIdx.x == 0 ) sNX = 0;
+        cp_async_wait_all(); // the field tile and the particle planes
         __syncthreads();
     }
     const T qm = T( sp.qm_dts2 );
