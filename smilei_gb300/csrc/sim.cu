@@ -333,9 +333,23 @@ __device__ __forceinline__ void esir_win( T c0o, T c1o, T c2o, T dnew, int shift
 // -cr_x P_x[m] (A_y[u] A_z[v] + D_y[u] D_z[v] / 12), and cyclically for Jy, Jz;
 // in 2D, Jz = crz (A_x A_y + D_x D_y / 12) with crz = q w v_z / V.  lx = the old
 // node, tile-local; the J tile origin is two nodes below the tile.
-template <int DIM, class T>
+// FIXED: the adds go instead to an int32 fixed-point tile Ji (same layout),
+// value * sc[component] rounded to nearest, with native integer atomics.
+template <bool FIXED, class T>
+__device__ __forceinline__ void j_add( T *J, int *Ji, int i, T v, float sc )
+{
+    if constexpr( FIXED ) {
+        const int q = __float2int_rn( ( float )v * sc );
+        if( q != 0 ) atomicAdd( &Ji[i], q );
+    } else {
+        sh_add( &J[i], v );
+    }
+}
+
+template <int DIM, class T, bool FIXED = false>
 __device__ __forceinline__ void deposit_direct( T *sJ, const TileDims &td, int jsz, const int *lx,
-                                                const EsirWin<T> *W, const T *cr, T crz, unsigned cmask = 7u )
+                                                const EsirWin<T> *W, const T *cr, T crz, unsigned cmask = 7u,
+                                                int *sJi = nullptr, const float *sc = nullptr )
 {
     const T twelfth = T( 1.0 / 12.0 );
     if( DIM == 3 ) {
@@ -344,6 +358,8 @@ __device__ __forceinline__ void deposit_direct( T *sJ, const TileDims &td, int j
             if( !( ( cmask >> c ) & 1u ) ) continue;
             const int a = c, b = ( c + 1 ) % 3, e = ( c + 2 ) % 3;
             T *J = sJ + c * jsz;
+            int *Ji = sJi + c * jsz;
+            const float scc = FIXED ? sc[c] : 0.0f;
 #pragma unroll
             for( int u = 0; u < 4; u++ )
 #pragma unroll
@@ -355,31 +371,33 @@ __device__ __forceinline__ void deposit_direct( T *sJ, const TileDims &td, int j
 #pragma unroll
                     for( int m = 0; m < 3; m++ ) {
                         idx[a] = lx[a] + W[a].lo + 1 + m;
-                        sh_add( &J[( idx[0] * td.JY + idx[1] ) * td.JZ + idx[2]], -cr[a] * W[a].P[m] * wgt );
+                        j_add<FIXED>( J, Ji, ( idx[0] * td.JY + idx[1] ) * td.JZ + idx[2], -cr[a] * W[a].P[m] * wgt, scc );
                     }
                 }
         }
     } else {
         T *J0 = sJ, *J1 = sJ + jsz, *J2 = sJ + 2 * jsz;
+        int *I0 = sJi, *I1 = sJi + jsz, *I2 = sJi + 2 * jsz;
+        const float s0 = FIXED ? sc[0] : 0.0f, s1 = FIXED ? sc[1] : 0.0f, s2 = FIXED ? sc[2] : 0.0f;
 #pragma unroll
         for( int u = 0; u < 4; u++ ) {
             const T ay = W[1].A[u];
             if( ( cmask & 1u ) && ay != T( 0 ) ) {
 #pragma unroll
                 for( int m = 0; m < 3; m++ )
-                    sh_add( &J0[( lx[0] + W[0].lo + 1 + m ) * td.JY + lx[1] + W[1].lo + u], -cr[0] * W[0].P[m] * ay );
+                    j_add<FIXED>( J0, I0, ( lx[0] + W[0].lo + 1 + m ) * td.JY + lx[1] + W[1].lo + u, -cr[0] * W[0].P[m] * ay, s0 );
             }
             const T ax = W[0].A[u];
             if( ( cmask & 2u ) && ax != T( 0 ) ) {
 #pragma unroll
                 for( int m = 0; m < 3; m++ )
-                    sh_add( &J1[( lx[0] + W[0].lo + u ) * td.JY + lx[1] + W[1].lo + 1 + m], -cr[1] * W[1].P[m] * ax );
+                    j_add<FIXED>( J1, I1, ( lx[0] + W[0].lo + u ) * td.JY + lx[1] + W[1].lo + 1 + m, -cr[1] * W[1].P[m] * ax, s1 );
             }
             if( cmask & 4u ) {
 #pragma unroll
                 for( int v = 0; v < 4; v++ ) {
                     const T wz = W[0].A[u] * W[1].A[v] + twelfth * W[0].D[u] * W[1].D[v];
-                    sh_add( &J2[( lx[0] + W[0].lo + u ) * td.JY + lx[1] + W[1].lo + v], crz * wz );
+                    j_add<FIXED>( J2, I2, ( lx[0] + W[0].lo + u ) * td.JY + lx[1] + W[1].lo + v, crz * wz, s2 );
                 }
             }
         }
@@ -417,6 +435,7 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
     int *sRank = sStart + TC;   // reused after loading as the list of node-changing slots
     unsigned char *sSlotCell = reinterpret_cast<unsigned char *>( sRank + ( CELLS ? nmax : 0 ) );
     __shared__ int sNX;         // length of that list
+    __shared__ unsigned sWX;    // largest |w| on it (float bits)
 
     const int tile = blockIdx.x;
     int tz = 0, ty, tx;
@@ -529,7 +548,10 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
             cp_async_word( &sRec[7 * nmax + slot], &in.w[src], true );
             sSlotCell[slot] = ( unsigned char )lc;
         }
-        if( threadIdx.x == 0 ) sNX = 0;
+        if( threadIdx.x == 0 ) {
+            sNX = 0;
+            sWX = 0u;
+        }
         cp_async_wait_all(); // the field tile and the particle planes
         __syncthreads();
     }
@@ -708,6 +730,8 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
                 if( lane == 0 ) xb = atomicAdd( &sNX, __popc( xm ) );
                 xb = __shfl_sync( 0xffffffffu, xb, 0 );
                 if( cross ) sRank[xb + __popc( xm & ( ( 1u << lane ) - 1u ) )] = q;
+                const unsigned wb = __reduce_max_sync( 0xffffffffu, cross ? __float_as_uint( fabsf( ( float )w ) ) : 0u );
+                if( lane == 0 ) atomicMax( &sWX, wb );
             }
         }
 
@@ -782,6 +806,35 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
         }
     }
     __syncthreads();
+
+    // Node-changing particles of the per-cell mode are added to an int32
+    // fixed-point J tile (native integer shared atomics) laid over the field tile,
+    // which is dead after the gather.  With nX particles on the list and weights up
+    // to wmax, one particle adds at most 1.1 cr w to a node (|P| <= 1, weight
+    // product <= 1 + 1/12), so a scale of 2^30 / (1.1 nX cr wmax) cannot overflow
+    // and rounds each add to 0.55 nX cr wmax / 2^30 (FP32 rounding of the same
+    // sums is of that order).  Lists longer than JFIX_MAX_LIST use FP32 atomics.
+    constexpr int JFIX_MAX_LIST = 4096;
+    int *sJi = reinterpret_cast<int *>( sF );
+    bool jfix = false;
+    float jsc[3] = { 0.0f, 0.0f, 0.0f }, jisc[3] = { 0.0f, 0.0f, 0.0f };
+    if constexpr( CELLS ) {
+        const int nx = sNX;
+        const float wmax = __uint_as_float( sWX );
+        jfix = nx > 0 && nx <= JFIX_MAX_LIST;
+#pragma unroll
+        for( int c = 0; c < 3; c++ ) {
+            const float crc = DIM == 2 && c == 2 ? ( float )cw0 : ( float )cr3[c];
+            const float bnd = 1.1f * ( float )nx * wmax * fabsf( crc );
+            if( !( bnd > 0.0f && bnd < 1e30f ) ) jfix = false;
+            jsc[c] = 1073741824.0f / bnd;
+            jisc[c] = bnd * ( 1.0f / 1073741824.0f );
+        }
+        if( jfix ) { // block-uniform
+            for( int e = threadIdx.x; e < 3 * jsz; e += blockDim.x ) sJi[e] = 0;
+            __syncthreads();
+        }
+    }
 
     // 3. per-cell deposit (CELLS).  Particles that stay on their node in every
     // dimension share their cell's fixed footprint: stencil points 1..3 across the
@@ -926,7 +979,8 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
                 bspline2( ( T )sRec[d * nmax + q], o0, o1, o2 );
                 esir_win<T>( o0, o1, o2, ( T )sRec[( 3 + d ) * nmax + q], sh[d], W[d] );
             }
-            deposit_direct<DIM, T>( sJ, td, jsz, cl, W, cr, cw0 * wq * vz );
+            if( jfix ) deposit_direct<DIM, T, true>( sJ, td, jsz, cl, W, cr, cw0 * wq * vz, 7u, sJi, jsc );
+            else deposit_direct<DIM, T>( sJ, td, jsz, cl, W, cr, cw0 * wq * vz );
         }
         __syncthreads();
     }
@@ -939,18 +993,21 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
         const int ny = ext( g, 1, stag( c, 1 ) ), nz = ext( g, 2, stag( c, 2 ) );
         const int nx = ext( g, 0, stag( c, 0 ) );
         const T *srcJ = sJ + c * jsz;
+        const int *srcJi = sJi + c * jsz;
+        const float isc = jisc[c];
         if( jm.fast ) {
             if( jm.active ) {
                 const int gy = iy0 + OS - 2 + jm.cy, gz = DIM == 3 ? iz0 + OS - 2 + jm.cz : 0;
                 for( int cx = jm.cx0; cx < td.JX; cx += jm.step ) {
-                    const T v = srcJ[( cx * td.JY + jm.cy ) * td.JZ + jm.cz];
+                    const int e = ( cx * td.JY + jm.cy ) * td.JZ + jm.cz;
+                    const T v = jfix ? srcJ[e] + ( T )( ( float )srcJi[e] * isc ) : srcJ[e];
                     const int gx = ix0 + OS - 2 + cx;
                     if( v != T( 0 ) && gx < nx && gy < ny && gz < nz ) atomicAdd( &dstJ[( ( int64_t )gx * ny + gy ) * nz + gz], v );
                 }
             }
         } else {
             for( int e = threadIdx.x; e < jsz; e += blockDim.x ) {
-                const T v = srcJ[e];
+                const T v = jfix ? srcJ[e] + ( T )( ( float )srcJi[e] * isc ) : srcJ[e];
                 if( v == T( 0 ) ) continue;
                 const int cz = e % td.JZ, cy = ( e / td.JZ ) % td.JY, cx = e / ( td.JZ * td.JY );
                 const int gx = ix0 + OS - 2 + cx, gy = iy0 + OS - 2 + cy, gz = DIM == 3 ? iz0 + OS - 2 + cz : 0;
