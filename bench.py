@@ -151,6 +151,22 @@ def make_plasma(cfg, seed, device):
     return pos, mom, w
 
 
+def max_over_ranks(x: float, device) -> float:
+    """The largest of every rank's x (the job's time is its slowest replica's)."""
+    import torch
+    import torch.distributed as td
+    if not (td.is_available() and td.is_initialized()) or td.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(particles_per_rank: int, world: int, steps: int, ms: float) -> float:
+    """Particle-steps/s of the whole job: every replica's particles over the slowest replica's time."""
+    return particles_per_rank * world * steps / (ms / 1e3)
+
+
 def run_gpu(args, rank, world, local_rank):
     import torch
     from smilei_gb300 import simulation
@@ -193,11 +209,7 @@ def run_gpu(args, rank, world, local_rank):
         wall1 = time.perf_counter()
     if dist:
         td.barrier()
-    ms = ev0.elapsed_time(ev1)
-    if dist:
-        t = torch.tensor([ms], device=device)
-        td.all_reduce(t, op=td.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ev0.elapsed_time(ev1), device)
     uk1, ue1 = sim.energy()
 
     # e2e: the same step driven from host buffers through the C ABI
@@ -221,12 +233,8 @@ def run_gpu(args, rank, world, local_rank):
             sim.energy()
         e1.record(stream)
         torch.cuda.synchronize()
-        ems = e0.elapsed_time(e1)
-        if dist:
-            t = torch.tensor([ems], device=device)
-            td.all_reduce(t, op=td.ReduceOp.MAX)
-            ems = float(t.item())
-        e2e = {"value": n * world * ke / (ems / 1e3), "unit": UNIT, "h2d_bytes_per_step": int(nbytes),
+        ems = max_over_ranks(e0.elapsed_time(e1), device)
+        e2e = {"value": whole_job_rate(n, world, ke, ems), "unit": UNIT, "h2d_bytes_per_step": int(nbytes),
                "d2h_bytes_per_step": int(nbytes + 16), "steps": ke}
         del host
     sim.close()
@@ -235,7 +243,7 @@ def run_gpu(args, rank, world, local_rank):
     kernel_bytes = n * s_state + ncell * 9 * s  # state read+write; gather E,B_m and J write per cell
     t_kernel = float(np.mean(t_part)) / 1e3
     peak, peak_kind = measured_peak()
-    value = n * world * args.steps / (ms / 1e3)
+    value = whole_job_rate(n, world, args.steps, ms)
     return dict(n=n, ms=ms, value=value, wall_ms_per_step=(wall1 - wall0) * 1e3 / args.steps, e2e=e2e,
                 kernel_bytes=kernel_bytes, t_kernel=t_kernel, peak=peak, peak_kind=peak_kind, B_alg=B_alg,
                 launches=launches, clocks=clk.summary(), energy=(uk0, ue0, uk1, ue1), cfg=cfg)
