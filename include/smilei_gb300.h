@@ -183,6 +183,14 @@ int sg_sim_get_species( sg_sim *sim, int species, double *pos, double *mom, doub
  * interior points (src/Diagnostic/DiagnosticScalar.cpp:174-277). */
 int sg_sim_energy( sg_sim *sim, double *ukin, double *uelm );
 
+/* Per-species and per-field scalars of DiagnosticScalar::compute
+ * (src/Diagnostic/DiagnosticScalar.cpp:470-700), FP64 device reductions.
+ * sg_sim_species_scalars: out[4] = {Dens = sum w, Ntot, Zavg numerator q sum w,
+ * Ukin = m sum w (gamma - 1)}.  sg_sim_field_energies: out[6] = 0.5 V_cell sum F^2
+ * for Ex, Ey, Ez, Bx_m, By_m, Bz_m over the N physical points per dimension. */
+int sg_sim_species_scalars( sg_sim *sim, int species, double *out );
+int sg_sim_field_energies( sg_sim *sim, double *out );
+
 /* Charge density of all species at the current positions, FP64, reference layout
  * (primal, ghosts, periodic copies folded): the basic() projection of
  * src/Projector/Projector3D2Order.cpp:526-618 summed over species. */

@@ -72,6 +72,8 @@ _SIGNATURES = {
     "sg_sim_step": (_I, [_VP, _I]),
     "sg_sim_species_count": (_I, [_VP, _I, ctypes.POINTER(_I64)]),
     "sg_sim_get_species": (_I, [_VP, _I, _VP, _VP, _VP]),
+    "sg_sim_species_scalars": (_I, [_VP, _I, _VP]),
+    "sg_sim_field_energies": (_I, [_VP, _VP]),
     "sg_sim_energy": (_I, [_VP, ctypes.POINTER(_D), ctypes.POINTER(_D)]),
     "sg_sim_last_timing": (_I, [_VP, ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.POINTER(_D),
                                 ctypes.POINTER(_I)]),

@@ -65,6 +65,7 @@ __host__ __device__ inline int stag( int comp, int d )
 template <class T>
 struct Fields {
     T *E[3], *B[3], *Bm[3], *J[3];
+    T *Ec[3]; // compensation of E's FP32 sums (mixed form), else null
 };
 
 template <bool MIXED>
@@ -333,23 +334,9 @@ __device__ __forceinline__ void esir_win( T c0o, T c1o, T c2o, T dnew, int shift
 // -cr_x P_x[m] (A_y[u] A_z[v] + D_y[u] D_z[v] / 12), and cyclically for Jy, Jz;
 // in 2D, Jz = crz (A_x A_y + D_x D_y / 12) with crz = q w v_z / V.  lx = the old
 // node, tile-local; the J tile origin is two nodes below the tile.
-// FIXED: the adds go instead to an int32 fixed-point tile Ji (same layout),
-// value * sc[component] rounded to nearest, with native integer atomics.
-template <bool FIXED, class T>
-__device__ __forceinline__ void j_add( T *J, int *Ji, int i, T v, float sc )
-{
-    if constexpr( FIXED ) {
-        const int q = __float2int_rn( ( float )v * sc );
-        if( q != 0 ) atomicAdd( &Ji[i], q );
-    } else {
-        sh_add( &J[i], v );
-    }
-}
-
-template <int DIM, class T, bool FIXED = false>
+template <int DIM, class T>
 __device__ __forceinline__ void deposit_direct( T *sJ, const TileDims &td, int jsz, const int *lx,
-                                                const EsirWin<T> *W, const T *cr, T crz, unsigned cmask = 7u,
-                                                int *sJi = nullptr, const float *sc = nullptr )
+                                                const EsirWin<T> *W, const T *cr, T crz, unsigned cmask = 7u )
 {
     const T twelfth = T( 1.0 / 12.0 );
     if( DIM == 3 ) {
@@ -358,8 +345,6 @@ __device__ __forceinline__ void deposit_direct( T *sJ, const TileDims &td, int j
             if( !( ( cmask >> c ) & 1u ) ) continue;
             const int a = c, b = ( c + 1 ) % 3, e = ( c + 2 ) % 3;
             T *J = sJ + c * jsz;
-            int *Ji = sJi + c * jsz;
-            const float scc = FIXED ? sc[c] : 0.0f;
 #pragma unroll
             for( int u = 0; u < 4; u++ )
 #pragma unroll
@@ -371,35 +356,38 @@ __device__ __forceinline__ void deposit_direct( T *sJ, const TileDims &td, int j
 #pragma unroll
                     for( int m = 0; m < 3; m++ ) {
                         idx[a] = lx[a] + W[a].lo + 1 + m;
-                        j_add<FIXED>( J, Ji, ( idx[0] * td.JY + idx[1] ) * td.JZ + idx[2], -cr[a] * W[a].P[m] * wgt, scc );
+                        sh_add( &J[( idx[0] * td.JY + idx[1] ) * td.JZ + idx[2]], -cr[a] * W[a].P[m] * wgt );
                     }
                 }
         }
     } else {
         T *J0 = sJ, *J1 = sJ + jsz, *J2 = sJ + 2 * jsz;
-        int *I0 = sJi, *I1 = sJi + jsz, *I2 = sJi + 2 * jsz;
-        const float s0 = FIXED ? sc[0] : 0.0f, s1 = FIXED ? sc[1] : 0.0f, s2 = FIXED ? sc[2] : 0.0f;
+        if( cmask & 1u ) {
 #pragma unroll
-        for( int u = 0; u < 4; u++ ) {
-            const T ay = W[1].A[u];
-            if( ( cmask & 1u ) && ay != T( 0 ) ) {
+            for( int u = 0; u < 4; u++ ) {
+                const T ay = W[1].A[u];
 #pragma unroll
                 for( int m = 0; m < 3; m++ )
-                    j_add<FIXED>( J0, I0, ( lx[0] + W[0].lo + 1 + m ) * td.JY + lx[1] + W[1].lo + u, -cr[0] * W[0].P[m] * ay, s0 );
+                    sh_add( &J0[( lx[0] + W[0].lo + 1 + m ) * td.JY + lx[1] + W[1].lo + u], -cr[0] * W[0].P[m] * ay );
             }
-            const T ax = W[0].A[u];
-            if( ( cmask & 2u ) && ax != T( 0 ) ) {
+        }
+        if( cmask & 2u ) {
+#pragma unroll
+            for( int u = 0; u < 4; u++ ) {
+                const T ax = W[0].A[u];
 #pragma unroll
                 for( int m = 0; m < 3; m++ )
-                    j_add<FIXED>( J1, I1, ( lx[0] + W[0].lo + u ) * td.JY + lx[1] + W[1].lo + 1 + m, -cr[1] * W[1].P[m] * ax, s1 );
+                    sh_add( &J1[( lx[0] + W[0].lo + u ) * td.JY + lx[1] + W[1].lo + 1 + m], -cr[1] * W[1].P[m] * ax );
             }
-            if( cmask & 4u ) {
+        }
+        if( cmask & 4u ) {
+#pragma unroll
+            for( int u = 0; u < 4; u++ )
 #pragma unroll
                 for( int v = 0; v < 4; v++ ) {
                     const T wz = W[0].A[u] * W[1].A[v] + twelfth * W[0].D[u] * W[1].D[v];
-                    j_add<FIXED>( J2, I2, ( lx[0] + W[0].lo + u ) * td.JY + lx[1] + W[1].lo + v, crz * wz, s2 );
+                    sh_add( &J2[( lx[0] + W[0].lo + u ) * td.JY + lx[1] + W[1].lo + v], crz * wz );
                 }
-            }
         }
     }
 }
@@ -433,9 +421,10 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
     int *sCnt = reinterpret_cast<int *>( sRec + ( CELLS ? REC * nmax : 0 ) );
     int *sStart = sCnt + TC;
     int *sRank = sStart + TC;   // reused after loading as the list of node-changing slots
-    unsigned char *sSlotCell = reinterpret_cast<unsigned char *>( sRank + ( CELLS ? nmax : 0 ) );
+    int *sXs = sRank + ( CELLS ? nmax : 0 ); // that list grouped by crossing class
+    unsigned char *sSlotCell = reinterpret_cast<unsigned char *>( sXs + ( CELLS ? nmax : 0 ) );
     __shared__ int sNX;         // length of that list
-    __shared__ unsigned sWX;    // largest |w| on it (float bits)
+    __shared__ int sXc[4];      // node-changing particles per class (x, y, z only; several)
 
     const int tile = blockIdx.x;
     int tz = 0, ty, tx;
@@ -550,8 +539,8 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
         }
         if( threadIdx.x == 0 ) {
             sNX = 0;
-            sWX = 0u;
         }
+        if( threadIdx.x < 4 ) sXc[threadIdx.x] = 0;
         cp_async_wait_all(); // the field tile and the particle planes
         __syncthreads();
     }
@@ -724,14 +713,16 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
         if constexpr( CELLS ) {
             // node-changing particles go to a list deposited with full warps later
             const bool cross = valid && ( shift[0] | shift[1] | shift[2] ) != 0;
+            if( cross ) {
+                const int nsh = ( shift[0] != 0 ) + ( shift[1] != 0 ) + ( shift[2] != 0 );
+                atomicAdd( &sXc[nsh == 1 ? ( shift[0] != 0 ? 0 : ( shift[1] != 0 ? 1 : 2 ) ) : 3], 1 );
+            }
             const unsigned xm = __ballot_sync( 0xffffffffu, cross );
             if( xm ) {
                 int xb = 0;
                 if( lane == 0 ) xb = atomicAdd( &sNX, __popc( xm ) );
                 xb = __shfl_sync( 0xffffffffu, xb, 0 );
                 if( cross ) sRank[xb + __popc( xm & ( ( 1u << lane ) - 1u ) )] = q;
-                const unsigned wb = __reduce_max_sync( 0xffffffffu, cross ? __float_as_uint( fabsf( ( float )w ) ) : 0u );
-                if( lane == 0 ) atomicMax( &sWX, wb );
             }
         }
 
@@ -807,33 +798,26 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
     }
     __syncthreads();
 
-    // Node-changing particles of the per-cell mode are added to an int32
-    // fixed-point J tile (native integer shared atomics) laid over the field tile,
-    // which is dead after the gather.  With nX particles on the list and weights up
-    // to wmax, one particle adds at most 1.1 cr w to a node (|P| <= 1, weight
-    // product <= 1 + 1/12), so a scale of 2^30 / (1.1 nX cr wmax) cannot overflow
-    // and rounds each add to 0.55 nX cr wmax / 2^30 (FP32 rounding of the same
-    // sums is of that order).  Lists longer than JFIX_MAX_LIST use FP32 atomics.
-    constexpr int JFIX_MAX_LIST = 4096;
-    int *sJi = reinterpret_cast<int *>( sF );
-    bool jfix = false;
-    float jsc[3] = { 0.0f, 0.0f, 0.0f }, jisc[3] = { 0.0f, 0.0f, 0.0f };
     if constexpr( CELLS ) {
-        const int nx = sNX;
-        const float wmax = __uint_as_float( sWX );
-        jfix = nx > 0 && nx <= JFIX_MAX_LIST;
-#pragma unroll
-        for( int c = 0; c < 3; c++ ) {
-            const float crc = DIM == 2 && c == 2 ? ( float )cw0 : ( float )cr3[c];
-            const float bnd = 1.1f * ( float )nx * wmax * fabsf( crc );
-            if( !( bnd > 0.0f && bnd < 1e30f ) ) jfix = false;
-            jsc[c] = 1073741824.0f / bnd;
-            jisc[c] = bnd * ( 1.0f / 1073741824.0f );
+        // group the node-changing list by class (counting sort); class starts in sXc
+        if( threadIdx.x == 0 ) {
+            int run = 0;
+            for( int k = 0; k < 4; k++ ) {
+                const int c = sXc[k];
+                sXc[k] = run;
+                run += c;
+            }
         }
-        if( jfix ) { // block-uniform
-            for( int e = threadIdx.x; e < 3 * jsz; e += blockDim.x ) sJi[e] = 0;
-            __syncthreads();
+        __syncthreads();
+        for( int k = threadIdx.x; k < sNX; k += blockDim.x ) {
+            const int q = sRank[k];
+            const int sb = __float_as_int( sRec[6 * nmax + q] );
+            const int h0 = ( sb & 3 ) - 1, h1 = ( ( sb >> 2 ) & 3 ) - 1, h2 = ( ( sb >> 4 ) & 3 ) - 1;
+            const int nsh = ( h0 != 0 ) + ( h1 != 0 ) + ( h2 != 0 );
+            const int cls = nsh == 1 ? ( h0 != 0 ? 0 : ( h1 != 0 ? 1 : 2 ) ) : 3;
+            sXs[atomicAdd( &sXc[cls], 1 )] = q;
         }
+        __syncthreads();
     }
 
     // 3. per-cell deposit (CELLS).  Particles that stay on their node in every
@@ -935,9 +919,11 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
 #pragma unroll
                         for( int m = 0; m < 2; m++ ) {
                             const int ia = ( hf ? cl[0] + 1 + u : cl[0] + 2 + m ), ib = ( hf ? cl[1] + 2 + m : cl[1] + 1 + u );
-                            sh_add( &Ja[( ia * td.JY + ib ) * td.JZ + cl[2] + 1 + v], acc[( m * 3 + u ) * 3 + v] );
+                            const int ea = ( ia * td.JY + ib ) * td.JZ + cl[2] + 1 + v;
+                            sh_add( &Ja[ea], acc[( m * 3 + u ) * 3 + v] );
                         }
-                        sh_add( &Jz[( ( cl[0] + 1 + u ) * td.JY + cl[1] + 1 + v ) * td.JZ + cl[2] + 2 + hf], accz[u * 3 + v] );
+                        const int ez = ( ( cl[0] + 1 + u ) * td.JY + cl[1] + 1 + v ) * td.JZ + cl[2] + 2 + hf;
+                        sh_add( &Jz[ez], accz[u * 3 + v] );
                     }
             } else {
                 T *J0 = sJ, *J1 = sJ + jsz, *J2 = sJ + 2 * jsz;
@@ -945,17 +931,21 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
                 for( int u = 0; u < 3; u++ ) {
 #pragma unroll
                     for( int m = 0; m < 2; m++ ) {
-                        sh_add( &J0[( cl[0] + 2 + m ) * td.JY + cl[1] + 1 + u], acc[m * 3 + u] );
-                        sh_add( &J1[( cl[0] + 1 + u ) * td.JY + cl[1] + 2 + m], acc[6 + u * 2 + m] );
+                        const int e0 = ( cl[0] + 2 + m ) * td.JY + cl[1] + 1 + u, e1 = ( cl[0] + 1 + u ) * td.JY + cl[1] + 2 + m;
+                        sh_add( &J0[e0], acc[m * 3 + u] );
+                        sh_add( &J1[e1], acc[6 + u * 2 + m] );
                     }
 #pragma unroll
-                    for( int v = 0; v < 3; v++ ) sh_add( &J2[( cl[0] + 1 + u ) * td.JY + cl[1] + 1 + v], accz[u * 3 + v] );
+                    for( int v = 0; v < 3; v++ ) {
+                        const int e2 = ( cl[0] + 1 + u ) * td.JY + cl[1] + 1 + v;
+                        sh_add( &J2[e2], accz[u * 3 + v] );
+                    }
                 }
             }
         }
         // node-changing particles, one per thread
         for( int k = threadIdx.x; k < sNX; k += blockDim.x ) {
-            const int q = sRank[k];
+            const int q = sXs[k];
             const int lc = sSlotCell[q];
             int cl[3];
             if( DIM == 3 ) {
@@ -979,8 +969,9 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
                 bspline2( ( T )sRec[d * nmax + q], o0, o1, o2 );
                 esir_win<T>( o0, o1, o2, ( T )sRec[( 3 + d ) * nmax + q], sh[d], W[d] );
             }
-            if( jfix ) deposit_direct<DIM, T, true>( sJ, td, jsz, cl, W, cr, cw0 * wq * vz, 7u, sJi, jsc );
-            else deposit_direct<DIM, T>( sJ, td, jsz, cl, W, cr, cw0 * wq * vz );
+            // the list is grouped by crossing dimension, so a warp's zero nodes mostly coincide
+            const T crz = cw0 * wq * vz;
+            deposit_direct<DIM, T>( sJ, td, jsz, cl, W, cr, crz );
         }
         __syncthreads();
     }
@@ -993,21 +984,19 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
         const int ny = ext( g, 1, stag( c, 1 ) ), nz = ext( g, 2, stag( c, 2 ) );
         const int nx = ext( g, 0, stag( c, 0 ) );
         const T *srcJ = sJ + c * jsz;
-        const int *srcJi = sJi + c * jsz;
-        const float isc = jisc[c];
         if( jm.fast ) {
             if( jm.active ) {
                 const int gy = iy0 + OS - 2 + jm.cy, gz = DIM == 3 ? iz0 + OS - 2 + jm.cz : 0;
                 for( int cx = jm.cx0; cx < td.JX; cx += jm.step ) {
                     const int e = ( cx * td.JY + jm.cy ) * td.JZ + jm.cz;
-                    const T v = jfix ? srcJ[e] + ( T )( ( float )srcJi[e] * isc ) : srcJ[e];
+                    const T v = srcJ[e];
                     const int gx = ix0 + OS - 2 + cx;
                     if( v != T( 0 ) && gx < nx && gy < ny && gz < nz ) atomicAdd( &dstJ[( ( int64_t )gx * ny + gy ) * nz + gz], v );
                 }
             }
         } else {
             for( int e = threadIdx.x; e < jsz; e += blockDim.x ) {
-                const T v = jfix ? srcJ[e] + ( T )( ( float )srcJi[e] * isc ) : srcJ[e];
+                const T v = srcJ[e];
                 if( v == T( 0 ) ) continue;
                 const int cz = e % td.JZ, cy = ( e / td.JZ ) % td.JY, cx = e / ( td.JZ * td.JY );
                 const int gx = ix0 + OS - 2 + cx, gy = iy0 + OS - 2 + cy, gz = DIM == 3 ? iz0 + OS - 2 + cz : 0;
@@ -1053,29 +1042,46 @@ __global__ void k_fold( GridInfo g, int d, Fields<T> f )
 // Ampere on every point (MA_Solver3D_norm.cpp:18-115 / MA_Solver2D_norm.cpp:18-107).
 // One block per row of the last dimension; E stays consistent between a node and
 // its periodic image because J (folded) and B (synchronised) are.
+// E[t] += d.  With a compensation array C (FP32 fields) the add is Kahan's: the
+// part of d that the FP32 sum drops is kept in C[t] and added back on the next
+// step, so the stored E carries one rounding instead of one per step.
+template <class T>
+__device__ __forceinline__ void add_comp( T *E, T *C, int64_t t, T d )
+{
+    if( C ) {
+        const T y = d - C[t];
+        const T e = E[t];
+        const T s = e + y;
+        C[t] = ( s - e ) - y;
+        E[t] = s;
+    } else {
+        E[t] += d;
+    }
+}
+
 template <int DIM, class T>
 __global__ void k_ampere_all( GridInfo g, Fields<T> f, T dt, T dtdx, T dtdy, T dtdz )
 {
-    const int nxp = g.np[0], nyp = g.np[1], nxd = nxp + 1, nyd = nyp + 1;
+    const int nxp = g.np[0], nyp = g.np[1], nyd = nyp + 1;
     if( DIM == 3 ) {
         const int nzp = g.np[2], nzd = nzp + 1;
-        const int row = blockIdx.x; // over nxd * nyd
+        const int row = blockIdx.x; // over (nxp + 1) * nyd
         const int i = row / nyd, j = row % nyd;
         for( int k = threadIdx.x; k < nzd; k += blockDim.x ) {
             if( j < nyp && k < nzp ) {
                 const int64_t t = ( ( int64_t )i * nyp + j ) * nzp + k;
-                f.E[0][t] += -dt * f.J[0][t] + dtdy * ( f.B[2][( ( int64_t )i * nyd + j + 1 ) * nzp + k] - f.B[2][( ( int64_t )i * nyd + j ) * nzp + k] )
-                             - dtdz * ( f.B[1][( ( int64_t )i * nyp + j ) * nzd + k + 1] - f.B[1][( ( int64_t )i * nyp + j ) * nzd + k] );
+                add_comp( f.E[0], f.Ec[0], t, -dt * f.J[0][t] + dtdy * ( f.B[2][( ( int64_t )i * nyd + j + 1 ) * nzp + k] - f.B[2][( ( int64_t )i * nyd + j ) * nzp + k] )
+                             - dtdz * ( f.B[1][( ( int64_t )i * nyp + j ) * nzd + k + 1] - f.B[1][( ( int64_t )i * nyp + j ) * nzd + k] ) );
             }
             if( i < nxp && k < nzp ) {
                 const int64_t t = ( ( int64_t )i * nyd + j ) * nzp + k;
-                f.E[1][t] += -dt * f.J[1][t] - dtdx * ( f.B[2][( ( int64_t )( i + 1 ) * nyd + j ) * nzp + k] - f.B[2][t] )
-                             + dtdz * ( f.B[0][( ( int64_t )i * nyd + j ) * nzd + k + 1] - f.B[0][( ( int64_t )i * nyd + j ) * nzd + k] );
+                add_comp( f.E[1], f.Ec[1], t, -dt * f.J[1][t] - dtdx * ( f.B[2][( ( int64_t )( i + 1 ) * nyd + j ) * nzp + k] - f.B[2][t] )
+                             + dtdz * ( f.B[0][( ( int64_t )i * nyd + j ) * nzd + k + 1] - f.B[0][( ( int64_t )i * nyd + j ) * nzd + k] ) );
             }
             if( i < nxp && j < nyp ) {
                 const int64_t t = ( ( int64_t )i * nyp + j ) * nzd + k;
-                f.E[2][t] += -dt * f.J[2][t] + dtdx * ( f.B[1][( ( int64_t )( i + 1 ) * nyp + j ) * nzd + k] - f.B[1][t] )
-                             - dtdy * ( f.B[0][( ( int64_t )i * nyd + j + 1 ) * nzd + k] - f.B[0][( ( int64_t )i * nyd + j ) * nzd + k] );
+                add_comp( f.E[2], f.Ec[2], t, -dt * f.J[2][t] + dtdx * ( f.B[1][( ( int64_t )( i + 1 ) * nyp + j ) * nzd + k] - f.B[1][t] )
+                             - dtdy * ( f.B[0][( ( int64_t )i * nyd + j + 1 ) * nzd + k] - f.B[0][( ( int64_t )i * nyd + j ) * nzd + k] ) );
             }
         }
     } else {
@@ -1083,16 +1089,16 @@ __global__ void k_ampere_all( GridInfo g, Fields<T> f, T dt, T dtdx, T dtdy, T d
         for( int j = threadIdx.x; j < nyd; j += blockDim.x ) {
             if( j < nyp ) {
                 const int64_t t = ( int64_t )i * nyp + j;
-                f.E[0][t] += -dt * f.J[0][t] + dtdy * ( f.B[2][( int64_t )i * nyd + j + 1] - f.B[2][( int64_t )i * nyd + j] );
+                add_comp( f.E[0], f.Ec[0], t, -dt * f.J[0][t] + dtdy * ( f.B[2][( int64_t )i * nyd + j + 1] - f.B[2][( int64_t )i * nyd + j] ) );
             }
             if( i < nxp ) {
                 const int64_t t = ( int64_t )i * nyd + j;
-                f.E[1][t] += -dt * f.J[1][t] - dtdx * ( f.B[2][( int64_t )( i + 1 ) * nyd + j] - f.B[2][t] );
+                add_comp( f.E[1], f.Ec[1], t, -dt * f.J[1][t] - dtdx * ( f.B[2][( int64_t )( i + 1 ) * nyd + j] - f.B[2][t] ) );
             }
             if( i < nxp && j < nyp ) {
                 const int64_t t = ( int64_t )i * nyp + j;
-                f.E[2][t] += -dt * f.J[2][t] + dtdx * ( f.B[1][( int64_t )( i + 1 ) * nyp + j] - f.B[1][t] )
-                             - dtdy * ( f.B[0][( int64_t )i * nyd + j + 1] - f.B[0][( int64_t )i * nyd + j] );
+                add_comp( f.E[2], f.Ec[2], t, -dt * f.J[2][t] + dtdx * ( f.B[1][( int64_t )( i + 1 ) * nyp + j] - f.B[1][t] )
+                             - dtdy * ( f.B[0][( int64_t )i * nyd + j + 1] - f.B[0][( int64_t )i * nyd + j] ) );
             }
         }
     }
@@ -1311,6 +1317,30 @@ __global__ void k_kinetic( int nt, const int64_t *__restrict__ seg_start, const 
     if( threadIdx.x == 0 ) atomicAdd( out, acc );
 }
 
+// sum of w and of w (gamma - 1) over one species (the scalar diagnostics' Dens and Ukin).
+template <bool MIXED>
+__global__ void k_species_sums( int nt, const int64_t *__restrict__ seg_start, const int *__restrict__ count,
+                                PBuf<MIXED> b, double *__restrict__ out )
+{
+    double sw = 0.0, se = 0.0;
+    for( int t = blockIdx.x; t < nt; t += gridDim.x ) {
+        const int n = count[t];
+        const int64_t s0 = seg_start[t];
+        for( int i = threadIdx.x; i < n; i += blockDim.x ) {
+            const double px = b.p[0][s0 + i], py = b.p[1][s0 + i], pz = b.p[2][s0 + i];
+            const double w = b.w[s0 + i];
+            sw += w;
+            se += w * ( sqrt( 1.0 + px * px + py * py + pz * pz ) - 1.0 );
+        }
+    }
+    sw = block_sum( sw );
+    se = block_sum( se );
+    if( threadIdx.x == 0 ) {
+        atomicAdd( out, sw );
+        atomicAdd( out + 1, se );
+    }
+}
+
 // sum of F^2 over the N physical points per dimension (array index OS .. OS+N-1).
 template <class T>
 __global__ void k_norm2( GridInfo g, const T *__restrict__ a, int sx, int sy, int sz, double *__restrict__ out )
@@ -1441,6 +1471,7 @@ struct sg_sim {
     size_t esz = 8;
     void *fmem = nullptr;
     void *fptr[12] = {};
+    void *ecomp[3] = {}; // mixed form: compensation words of Ex, Ey, Ez
     int64_t fsize[12] = {};
     int fshape[12][3] = {};
     std::vector<SpeciesState> sp;
@@ -1474,6 +1505,7 @@ Fields<T> field_view( sg_sim *S )
         f.B[c] = static_cast<T *>( S->fptr[3 + c] );
         f.Bm[c] = static_cast<T *>( S->fptr[6 + c] );
         f.J[c] = static_cast<T *>( S->fptr[9 + c] );
+        f.Ec[c] = static_cast<T *>( S->ecomp[c] );
     }
     return f;
 }
@@ -1482,11 +1514,12 @@ Fields<T> field_view( sg_sim *S )
 inline int comp_stag( int comp, int d ) { return comp < 3 ? stag( comp, d ) : ( comp < 9 ? stag( 3 + ( comp % 3 ), d ) : stag( comp - 9, d ) ); }
 
 // Shared memory of the per-cell mode: REC planes of nmax floats, a count and a
-// start per cell, a packed (cell, rank) word per particle, a cell byte per slot.
+// start per cell, a packed (cell, rank) word and a list word per particle, a
+// cell byte per slot.
 constexpr size_t CELLS_SMEM_LIMIT = 200 * 1024;
 inline size_t cells_smem_bytes( int tc, int nmax )
 {
-    return ( size_t )REC * 4 * nmax + ( size_t )8 * tc + ( size_t )4 * nmax + ( ( ( size_t )nmax + 15 ) & ~( size_t )15 );
+    return ( size_t )REC * 4 * nmax + ( size_t )8 * tc + ( size_t )8 * nmax + ( ( ( size_t )nmax + 15 ) & ~( size_t )15 );
 }
 
 template <int DIM, bool MIXED, int KIND>
@@ -1782,6 +1815,8 @@ int sg_sim_create( const sg_sim_config *cfg, sg_sim **out )
         S->fsize[c] = n;
         total += ( ( n * S->esz + 255 ) / 256 ) * 256;
     }
+    if( S->mixed )
+        for( int c = 0; c < 3; c++ ) total += ( ( S->fsize[c] * S->esz + 255 ) / 256 ) * 256;
     cudaError_t e = cudaMalloc( &S->fmem, total );
     if( e != cudaSuccess ) { delete S; return set_error( SG_ERR_NOMEM, "cannot allocate %zu bytes of fields", total ); }
     cudaMemset( S->fmem, 0, total );
@@ -1790,6 +1825,11 @@ int sg_sim_create( const sg_sim_config *cfg, sg_sim **out )
         S->fptr[c] = p;
         p += ( ( S->fsize[c] * S->esz + 255 ) / 256 ) * 256;
     }
+    if( S->mixed )
+        for( int c = 0; c < 3; c++ ) {
+            S->ecomp[c] = p;
+            p += ( ( S->fsize[c] * S->esz + 255 ) / 256 ) * 256;
+        }
     const int nt = g.ntiles;
     e = cudaMalloc( &S->d_flags, ( 1 + S->max_species ) * sizeof( int ) );
     if( e == cudaSuccess ) e = cudaMallocHost( &S->h_flags, ( 1 + S->max_species ) * sizeof( int ) );
@@ -1969,6 +2009,7 @@ int sg_sim_set_field( sg_sim *S, int comp, const double *host )
         SG_CUDA_TRY( cudaMemcpy( d, host, n * 8, cudaMemcpyHostToDevice ) );
         k_convert<double, float><<<grid_for( n, 256 ), 256, 0, S->stream>>>( n, d, static_cast<float *>( S->fptr[comp] ) );
         SG_LAUNCH_CHECK( "k_convert" );
+        if( comp < 3 && S->ecomp[comp] ) SG_CUDA_TRY( cudaMemsetAsync( S->ecomp[comp], 0, n * S->esz, S->stream ) );
         SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
         release( d );
     }
@@ -2148,6 +2189,49 @@ int sg_sim_energy( sg_sim *S, double *ukin, double *uelm )
     for( size_t k = 0; k < S->sp.size(); k++ ) uk += S->sp[k].mass * h[2 + k % 14];
     if( ukin ) *ukin = uk;
     if( uelm ) *uelm = 0.5 * vol * h[1];
+    return SG_OK;
+}
+
+int sg_sim_species_scalars( sg_sim *S, int species, double *out )
+{
+    SG_REQUIRE( S && out, "NULL argument" );
+    SG_REQUIRE( species >= 0 && species < ( int )S->sp.size(), "no species %d", species );
+    SpeciesState &s = S->sp[species];
+    cudaStream_t st = S->stream;
+    const int nt = S->g.ntiles;
+    SG_CUDA_TRY( cudaMemsetAsync( S->d_red, 0, 2 * sizeof( double ), st ) );
+    if( S->mixed ) k_species_sums<true><<<std::min( nt, 1216 ), 256, 0, st>>>( nt, s.seg_start, s.count[s.cur], s.bm[s.cur], S->d_red );
+    else k_species_sums<false><<<std::min( nt, 1216 ), 256, 0, st>>>( nt, s.seg_start, s.count[s.cur], s.bd[s.cur], S->d_red );
+    SG_LAUNCH_CHECK( "k_species_sums" );
+    double h[2];
+    SG_CUDA_TRY( cudaMemcpyAsync( h, S->d_red, sizeof( h ), cudaMemcpyDeviceToHost, st ) );
+    SG_CUDA_TRY( cudaStreamSynchronize( st ) );
+    out[0] = h[0];
+    out[1] = ( double )s.npart;
+    out[2] = s.charge * h[0];
+    out[3] = s.mass * h[1];
+    return SG_OK;
+}
+
+int sg_sim_field_energies( sg_sim *S, double *out )
+{
+    SG_REQUIRE( S && out, "NULL argument" );
+    cudaStream_t st = S->stream;
+    SG_CUDA_TRY( cudaMemsetAsync( S->d_red, 0, 6 * sizeof( double ), st ) );
+    const int comps[6] = { 0, 1, 2, 6, 7, 8 };
+    for( int k = 0; k < 6; k++ ) {
+        const int c = comps[k];
+        const int sx = comp_stag( c, 0 ), sy = comp_stag( c, 1 ), sz = comp_stag( c, 2 );
+        if( S->mixed ) k_norm2<float><<<1216, 256, 0, st>>>( S->g, static_cast<float *>( S->fptr[c] ), sx, sy, sz, S->d_red + k );
+        else k_norm2<double><<<1216, 256, 0, st>>>( S->g, static_cast<double *>( S->fptr[c] ), sx, sy, sz, S->d_red + k );
+        SG_LAUNCH_CHECK( "k_norm2" );
+    }
+    double h[6];
+    SG_CUDA_TRY( cudaMemcpyAsync( h, S->d_red, sizeof( h ), cudaMemcpyDeviceToHost, st ) );
+    SG_CUDA_TRY( cudaStreamSynchronize( st ) );
+    double vol = 1.0;
+    for( int d = 0; d < S->g.ndim; d++ ) vol *= S->g.dx[d];
+    for( int k = 0; k < 6; k++ ) out[k] = 0.5 * vol * h[k];
     return SG_OK;
 }
 
@@ -2548,6 +2632,7 @@ int sg_sim_solve_poisson( sg_sim *S, double max_error, int max_iter, int *iterat
         k_efield<<<ge, 256, 0, st>>>( g, phi, E, n, s + 8 );
         for( int d = 0; d < g.ndim; d++ ) {
             if( S->mixed ) k_efield_store<float><<<1024, 256, 0, st>>>( g, E, n, s + 8, static_cast<float *>( S->fptr[d] ), d );
+            if( S->ecomp[d] ) cudaMemsetAsync( S->ecomp[d], 0, S->fsize[d] * S->esz, st );
             else k_efield_store<double><<<1024, 256, 0, st>>>( g, E, n, s + 8, static_cast<double *>( S->fptr[d] ), d );
         }
         if( cudaGetLastError() != cudaSuccess ) { rc = set_error( SG_ERR_CUDA, "E from phi failed" ); break; }

@@ -57,7 +57,7 @@ class Simulation:
         self.close()
 
     # -- species -----------------------------------------------------------
-    def add_species(self, mass, charge, pusher, position, momentum, weight):
+    def add_species(self, mass, charge, pusher, position, momentum, weight, name=None):
         """position[ndim, n], momentum[3, n], weight[n] as float64 numpy arrays (host) or CUDA tensors."""
         idx = ctypes.c_int()
         kind = _lib.PUSHERS[pusher] if isinstance(pusher, str) else int(pusher)
@@ -74,7 +74,8 @@ class Simulation:
             n = int(pos.shape[1])
             check(_lib.lib().sg_sim_add_species(self._h, float(mass), float(charge), kind, n, pos.ctypes.data,
                                                 mom.ctypes.data, w.ctypes.data, ctypes.byref(idx)), "add_species")
-        self.species.append(dict(mass=mass, charge=charge, pusher=pusher))
+        self.species.append(dict(mass=mass, charge=charge, pusher=pusher,
+                                 name=name if name is not None else f"species{idx.value}"))
         return idx.value
 
     def species_count(self, s: int) -> int:
@@ -126,6 +127,18 @@ class Simulation:
         uk, ue = ctypes.c_double(), ctypes.c_double()
         check(_lib.lib().sg_sim_energy(self._h, ctypes.byref(uk), ctypes.byref(ue)), "energy")
         return uk.value, ue.value
+
+    def species_scalars(self, s: int):
+        """(Dens, Ntot, q * Dens, Ukin) of species s, as DiagnosticScalar sums them (FP64 on the device)."""
+        a = np.zeros(4)
+        check(_lib.lib().sg_sim_species_scalars(self._h, int(s), a.ctypes.data), "species_scalars")
+        return tuple(float(v) for v in a)
+
+    def field_energies(self):
+        """0.5 V_cell sum F^2 for Ex, Ey, Ez, Bx_m, By_m, Bz_m (FP64 on the device)."""
+        a = np.zeros(6)
+        check(_lib.lib().sg_sim_field_energies(self._h, a.ctypes.data), "field_energies")
+        return a
 
     def rho(self) -> np.ndarray:
         """FP64 charge density of all species (reference layout, primal, ghosts folded)."""
