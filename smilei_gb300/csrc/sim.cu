@@ -472,15 +472,22 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
     if constexpr( !CELLS ) cp_async_wait_all();
     __syncthreads();
 
-    int n = count_in[tile];
-    const int64_t s0 = seg_start[tile];
+    const T qm = T( sp.qm_dts2 );
+    const T vs[3] = { T( sp.vs[0] ), T( sp.vs[1] ), T( sp.vs[2] ) };
+    const T cr3[3] = { T( sp.cr[0] ), T( sp.cr[1] ), T( sp.cr[2] ) };
+    const T cw0 = T( sp.cw );
+    const unsigned lane = threadIdx.x & 31u;
+
+    // Per-cell mode takes the tile's particles in chunks of at most nmax (the
+    // shared planes' capacity), so a dense tile costs more passes, not more
+    // shared memory; the J tile accumulates over the chunks.  The FP64 form
+    // makes one pass over the whole tile.
+    const int ntot = count_in[tile];
+    const int64_t seg0 = seg_start[tile];
+    for( int c0 = 0; c0 < ( CELLS ? ntot : 1 ); c0 += ( CELLS ? nmax : 1 ) ) {
+    const int n = CELLS ? min( nmax, ntot - c0 ) : ntot;
+    const int64_t s0 = seg0 + c0;
     if constexpr( CELLS ) {
-        // a tile never holds more than its segment (the largest is nmax): anything
-        // else is a corrupt layout, reported instead of overrunning the records
-        if( n > nmax ) {
-            if( threadIdx.x == 0 ) atomicCAS( status, 0, SG_ERR_STATE );
-            n = nmax;
-        }
         // rank of every particle inside its cell, then the cells' start offsets
         for( int c = threadIdx.x; c < TC; c += blockDim.x ) sCnt[c] = 0;
         __syncthreads();
@@ -541,14 +548,9 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
             sNX = 0;
         }
         if( threadIdx.x < 4 ) sXc[threadIdx.x] = 0;
-        cp_async_wait_all(); // the field tile and the particle planes
+        cp_async_wait_all(); // the particle planes (and, on the first chunk, the field tile)
         __syncthreads();
     }
-    const T qm = T( sp.qm_dts2 );
-    const T vs[3] = { T( sp.vs[0] ), T( sp.vs[1] ), T( sp.vs[2] ) };
-    const T cr3[3] = { T( sp.cr[0] ), T( sp.cr[1] ), T( sp.cr[2] ) };
-    const T cw0 = T( sp.cw );
-    const unsigned lane = threadIdx.x & 31u;
 
     for( int base = 0; base < n; base += blockDim.x ) {
         const int q = base + threadIdx.x;
@@ -975,6 +977,9 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
         }
         __syncthreads();
     }
+    } // chunk
+    // a tile without particles still waits for its field copies before the CTA ends
+    if constexpr( CELLS ) cp_async_wait_all();
 
     // 4. flush the J tile (origin = array index i0 + OS - 2) with global atomics
     const TileMap jm = tile_map<DIM>( td.JY, td.JZ );
@@ -1517,7 +1522,7 @@ inline int comp_stag( int comp, int d ) { return comp < 3 ? stag( comp, d ) : ( 
 // Shared memory of the per-cell mode: REC planes of nmax floats, a count and a
 // start per cell, a packed (cell, rank) word and a list word per particle, a
 // cell byte per slot.
-constexpr size_t CELLS_SMEM_LIMIT = 200 * 1024;
+constexpr size_t CELLS_SMEM_TARGET = 44 * 1024; // five 128-thread blocks per SM
 inline size_t cells_smem_bytes( int tc, int nmax )
 {
     return ( size_t )REC * 4 * nmax + ( size_t )8 * tc + ( size_t )8 * nmax + ( ( ( size_t )nmax + 15 ) & ~( size_t )15 );
@@ -1542,24 +1547,29 @@ int launch_particles( sg_sim *S, SpeciesState &s, cudaStream_t st )
         sp.cr[d] = sp.cw * S->g.dx[d] / S->g.dt;
         sp.vs[d] = S->g.dt * S->g.dxi[d];
     }
-    // The mixed form deposits per cell when the tile's records fit in shared memory
-    // next to the field and current tiles (one tile = at most 128 cells).
+    // The mixed form deposits per cell (one tile = at most 64 cells in 3D, where two
+    // thread groups split a cell's footprint, 128 in 2D).  Its particles go through
+    // shared memory in chunks: the chunk is the largest segment when that fits the
+    // budget of five blocks per SM, else the most that does.
     auto kern = k_step_particles<DIM, MIXED, KIND, false>;
     size_t smem = S->smem_bytes;
+    int chunk = s.max_cap;
     if constexpr( MIXED ) {
         const int tc = S->g.T[0] * S->g.T[1] * ( DIM == 3 ? S->g.T[2] : 1 );
-        const size_t extra = cells_smem_bytes( tc, s.max_cap );
-        // 3D needs two thread groups per cell (the footprint is split between them)
-        if( tc <= ( DIM == 3 ? 64 : 128 ) && s.max_cap < 32768 && smem + extra <= CELLS_SMEM_LIMIT ) {
+        const size_t per = ( size_t )REC * 4 + 8 + 1; // planes, rank and list words, cell byte
+        const size_t fixed = smem + cells_smem_bytes( tc, 0 ) + 16;
+        const int fit = fixed < CELLS_SMEM_TARGET ? ( int )( ( CELLS_SMEM_TARGET - fixed ) / per ) : 0;
+        chunk = std::max( 1, std::min( s.max_cap, fit & ~31 ) );
+        if( tc <= ( DIM == 3 ? 64 : 128 ) && fit >= 128 ) {
             kern = k_step_particles<DIM, MIXED, KIND, true>;
-            smem += extra;
+            smem += cells_smem_bytes( tc, chunk );
         }
     }
     if( smem > 48 * 1024 ) SG_CUDA_TRY( cudaFuncSetAttribute( kern, cudaFuncAttributeMaxDynamicSharedMemorySize, ( int )smem ) );
     const int sidx = ( int )( &s - &S->sp[0] );
     kern<<<S->g.ntiles, 128, smem, st>>>( S->g, field_view<T>( S ), sp, bin, bout, s.seg_start, s.cap, s.count[in],
                                           s.count[out], bov, s.ovf_tile, S->d_flags + 1 + sidx, ( int )s.ovf_capacity,
-                                          S->d_flags, s.max_cap );
+                                          S->d_flags, chunk );
     SG_LAUNCH_CHECK( "k_step_particles" );
     return SG_OK;
 }

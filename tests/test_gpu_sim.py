@@ -86,9 +86,12 @@ def test_fp64_step_matches_oracle(sim_mod, cpu_oracle, ndim, pusher):
         assert position_error(pg, pr, cl, nc) <= 1e-10
 
 
-@pytest.mark.parametrize("ndim,pusher", [(3, "higueracary"), (2, "boris")])
-def test_mixed_step_matches_fp64_oracle(sim_mod, cpu_oracle, ndim, pusher):
-    spec = [(1.0, -1, pusher, 4, 0.3)]
+# ppc 64 (3D) and 96 (2D) put 4096 / 6144 particles in a tile: several chunks of the
+# per-cell mode's shared planes per tile
+@pytest.mark.parametrize("ndim,pusher,ppc", [(3, "higueracary", 4), (2, "boris", 4), (3, "boris", 64),
+                                             (2, "vay", 96)])
+def test_mixed_step_matches_fp64_oracle(sim_mod, cpu_oracle, ndim, pusher, ppc):
+    spec = [(1.0, -1, pusher, ppc, 0.3)]
     got, ref, parts = run_pair(sim_mod, cpu_oracle, ndim, "mixed", 1, spec)
     for k in FIELDS:
         assert rel_err(got[k], ref[k]) <= 1e-5, k
