@@ -1047,21 +1047,22 @@ __global__ void k_fold( GridInfo g, int d, Fields<T> f )
 // Ampere on every point (MA_Solver3D_norm.cpp:18-115 / MA_Solver2D_norm.cpp:18-107).
 // One block per row of the last dimension; E stays consistent between a node and
 // its periodic image because J (folded) and B (synchronised) are.
-// E[t] += d, with the increment d evaluated in FP64.  With a compensation array
-// C (FP32 fields) the add is Kahan's: the part of d that the FP32 sum drops is
-// kept in C[t] and added back on the next step, so the stored E carries one
-// rounding instead of one per step.
+// E[t] += d.  With a compensation array C (FP32 fields) the add is Kahan's: the
+// part of d that the FP32 sum drops is kept in C[t] and added back on the next
+// step, so the stored E carries one rounding instead of one per step.  (An FP64
+// increment lowers the residual a little more but costs 2 ms per 256^3 step: FP64
+// arithmetic is slow on this GPU.)
 template <class T>
-__device__ __forceinline__ void add_comp( T *E, T *C, int64_t t, double d )
+__device__ __forceinline__ void add_comp( T *E, T *C, int64_t t, T d )
 {
     if( C ) {
-        const double y = d - ( double )C[t];
+        const T y = d - C[t];
         const T e = E[t];
-        const T s = ( T )( ( double )e + y );
-        C[t] = ( T )( ( ( double )s - ( double )e ) - y );
+        const T s = e + y;
+        C[t] = ( s - e ) - y;
         E[t] = s;
     } else {
-        E[t] += ( T )d;
+        E[t] += d;
     }
 }
 
@@ -1076,18 +1077,18 @@ __global__ void k_ampere_all( GridInfo g, Fields<T> f, T dt, T dtdx, T dtdy, T d
         for( int k = threadIdx.x; k < nzd; k += blockDim.x ) {
             if( j < nyp && k < nzp ) {
                 const int64_t t = ( ( int64_t )i * nyp + j ) * nzp + k;
-                add_comp( f.E[0], f.Ec[0], t, -( double )dt * ( double )f.J[0][t] + ( double )dtdy * ( ( double )f.B[2][( ( int64_t )i * nyd + j + 1 ) * nzp + k] - ( double )f.B[2][( ( int64_t )i * nyd + j ) * nzp + k] )
-                             - ( double )dtdz * ( ( double )f.B[1][( ( int64_t )i * nyp + j ) * nzd + k + 1] - ( double )f.B[1][( ( int64_t )i * nyp + j ) * nzd + k] ) );
+                add_comp( f.E[0], f.Ec[0], t, -dt * f.J[0][t] + dtdy * ( f.B[2][( ( int64_t )i * nyd + j + 1 ) * nzp + k] - f.B[2][( ( int64_t )i * nyd + j ) * nzp + k] )
+                             - dtdz * ( f.B[1][( ( int64_t )i * nyp + j ) * nzd + k + 1] - f.B[1][( ( int64_t )i * nyp + j ) * nzd + k] ) );
             }
             if( i < nxp && k < nzp ) {
                 const int64_t t = ( ( int64_t )i * nyd + j ) * nzp + k;
-                add_comp( f.E[1], f.Ec[1], t, -( double )dt * ( double )f.J[1][t] - ( double )dtdx * ( ( double )f.B[2][( ( int64_t )( i + 1 ) * nyd + j ) * nzp + k] - ( double )f.B[2][t] )
-                             + ( double )dtdz * ( ( double )f.B[0][( ( int64_t )i * nyd + j ) * nzd + k + 1] - ( double )f.B[0][( ( int64_t )i * nyd + j ) * nzd + k] ) );
+                add_comp( f.E[1], f.Ec[1], t, -dt * f.J[1][t] - dtdx * ( f.B[2][( ( int64_t )( i + 1 ) * nyd + j ) * nzp + k] - f.B[2][t] )
+                             + dtdz * ( f.B[0][( ( int64_t )i * nyd + j ) * nzd + k + 1] - f.B[0][( ( int64_t )i * nyd + j ) * nzd + k] ) );
             }
             if( i < nxp && j < nyp ) {
                 const int64_t t = ( ( int64_t )i * nyp + j ) * nzd + k;
-                add_comp( f.E[2], f.Ec[2], t, -( double )dt * ( double )f.J[2][t] + ( double )dtdx * ( ( double )f.B[1][( ( int64_t )( i + 1 ) * nyp + j ) * nzd + k] - ( double )f.B[1][t] )
-                             - ( double )dtdy * ( ( double )f.B[0][( ( int64_t )i * nyd + j + 1 ) * nzd + k] - ( double )f.B[0][( ( int64_t )i * nyd + j ) * nzd + k] ) );
+                add_comp( f.E[2], f.Ec[2], t, -dt * f.J[2][t] + dtdx * ( f.B[1][( ( int64_t )( i + 1 ) * nyp + j ) * nzd + k] - f.B[1][t] )
+                             - dtdy * ( f.B[0][( ( int64_t )i * nyd + j + 1 ) * nzd + k] - f.B[0][( ( int64_t )i * nyd + j ) * nzd + k] ) );
             }
         }
     } else {
@@ -1095,16 +1096,16 @@ __global__ void k_ampere_all( GridInfo g, Fields<T> f, T dt, T dtdx, T dtdy, T d
         for( int j = threadIdx.x; j < nyd; j += blockDim.x ) {
             if( j < nyp ) {
                 const int64_t t = ( int64_t )i * nyp + j;
-                add_comp( f.E[0], f.Ec[0], t, -( double )dt * ( double )f.J[0][t] + ( double )dtdy * ( ( double )f.B[2][( int64_t )i * nyd + j + 1] - ( double )f.B[2][( int64_t )i * nyd + j] ) );
+                add_comp( f.E[0], f.Ec[0], t, -dt * f.J[0][t] + dtdy * ( f.B[2][( int64_t )i * nyd + j + 1] - f.B[2][( int64_t )i * nyd + j] ) );
             }
             if( i < nxp ) {
                 const int64_t t = ( int64_t )i * nyd + j;
-                add_comp( f.E[1], f.Ec[1], t, -( double )dt * ( double )f.J[1][t] - ( double )dtdx * ( ( double )f.B[2][( int64_t )( i + 1 ) * nyd + j] - ( double )f.B[2][t] ) );
+                add_comp( f.E[1], f.Ec[1], t, -dt * f.J[1][t] - dtdx * ( f.B[2][( int64_t )( i + 1 ) * nyd + j] - f.B[2][t] ) );
             }
             if( i < nxp && j < nyp ) {
                 const int64_t t = ( int64_t )i * nyp + j;
-                add_comp( f.E[2], f.Ec[2], t, -( double )dt * ( double )f.J[2][t] + ( double )dtdx * ( ( double )f.B[1][( int64_t )( i + 1 ) * nyp + j] - ( double )f.B[1][t] )
-                             - ( double )dtdy * ( ( double )f.B[0][( int64_t )i * nyd + j + 1] - ( double )f.B[0][( int64_t )i * nyd + j] ) );
+                add_comp( f.E[2], f.Ec[2], t, -dt * f.J[2][t] + dtdx * ( f.B[1][( int64_t )( i + 1 ) * nyp + j] - f.B[1][t] )
+                             - dtdy * ( f.B[0][( int64_t )i * nyd + j + 1] - f.B[0][( int64_t )i * nyd + j] ) );
             }
         }
     }
