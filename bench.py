@@ -42,9 +42,14 @@ SIGMA_10KEV = float(np.sqrt(10.0 / 511.0))
 
 
 def workload_cfg(args):
-    n = args.cells
     dx = 0.1
     dt = 0.95 * dx / np.sqrt(3.0)
+    if getattr(args, "workload", "thermal") == "uneven":
+        # batched uneven patches: 512 x 256 x 256 cells in 1024 patches of 32^3, particles per
+        # cell per patch 8 * exp(N(0, 1.5)) floored and clipped to [0, 64], T = 5 keV, Boris
+        return dict(n_cells=[512, 256, 256], cell_length=[dx, dx, dx], dt=float(dt), ppc=8, pusher="boris",
+                    sigma=float(np.sqrt(5.0 / 511.0)), patch=[32, 32, 32], sigma_ln=1.5, ppc_max=64)
+    n = args.cells
     return dict(n_cells=[n, n, n], cell_length=[dx, dx, dx], dt=float(dt), ppc=args.ppc, pusher="higueracary",
                 sigma=SIGMA_10KEV)
 
@@ -131,15 +136,30 @@ class ClockSampler:
 
 
 def make_plasma(cfg, seed, device):
-    """Seeded thermal plasma generated on the device (FP64 positions, momenta, weights)."""
+    """Seeded plasma generated on the device (FP64 positions, momenta, weights).
+
+    Uniform ppc, or for the uneven workload a particles-per-cell count per patch
+    (smilei_gb300.synthetic.patch_ppc); every particle has the median density's weight."""
     import torch
     g = torch.Generator(device=device)
     g.manual_seed(seed)
     n_cells, cl, ppc = cfg["n_cells"], cfg["cell_length"], cfg["ppc"]
     ncell = int(np.prod(n_cells))
-    n = ncell * ppc
+    if "patch" in cfg:
+        from smilei_gb300 import synthetic
+        patch = cfg["patch"]
+        npat = [n_cells[d] // patch[d] for d in range(3)]
+        ppc_p = torch.as_tensor(synthetic.patch_ppc(npat, ppc, cfg["sigma_ln"], cfg["ppc_max"], seed), device=device)
+        ids = torch.arange(ncell, device=device, dtype=torch.int64)
+        pidx = ((ids // (n_cells[1] * n_cells[2])) // patch[0]) * npat[1] * npat[2] + \
+            (((ids // n_cells[2]) % n_cells[1]) // patch[1]) * npat[2] + ((ids % n_cells[2]) // patch[2])
+        cell = torch.repeat_interleave(ids, ppc_p.reshape(-1)[pidx])
+        del ids, pidx
+        n = int(cell.numel())
+    else:
+        n = ncell * ppc
+        cell = torch.arange(n, device=device, dtype=torch.int64) // ppc
     pos = torch.empty((3, n), dtype=torch.float64, device=device)
-    cell = torch.arange(n, device=device, dtype=torch.int64) // ppc
     strides = [n_cells[1] * n_cells[2], n_cells[2], 1]
     for d in range(3):
         c = (cell // strides[d]) % n_cells[d]
@@ -175,14 +195,24 @@ def run_gpu(args, rank, world, local_rank):
     cfg = workload_cfg(args)
     pos, mom, w = make_plasma(cfg, args.seed + rank, device)
     n = int(w.shape[0])
-    sim = simulation.Simulation(cfg["n_cells"], cfg["cell_length"], cfg["dt"], form=args.form,
-                                tile=[args.tile] * 3 if args.tile else None, use_graph=True)
     # a dedicated stream: the step is captured as a CUDA graph, which the legacy default stream does not allow
     stream = torch.cuda.Stream(device=device)
     torch.cuda.set_stream(stream)
     from smilei_gb300 import _lib
-    _lib.check(_lib.lib().sg_sim_set_stream(sim._h, stream.cuda_stream), "set_stream")
-    sim.add_species(1.0, -1.0, cfg["pusher"], pos, mom, w)
+
+    def build(tile):
+        sm = simulation.Simulation(cfg["n_cells"], cfg["cell_length"], cfg["dt"], form=args.form,
+                                   tile=list(tile) if tile else None, use_graph=True)
+        _lib.check(_lib.lib().sg_sim_set_stream(sm._h, stream.cuda_stream), "set_stream")
+        sm.add_species(1.0, -1.0, cfg["pusher"], pos, mom, w)
+        return sm
+
+    tile, tuning = ([args.tile] * 3 if args.tile else None), None
+    if args.autotune:
+        from smilei_gb300 import autotune
+        best, times = autotune.tune_tiles(build, ndim=3)
+        tile, tuning = list(best), {"x".join(map(str, k)): round(v, 3) for k, v in times.items()}
+    sim = build(tile)
     del pos, mom, w
     torch.cuda.empty_cache()
     uk0, ue0 = sim.energy()
@@ -211,6 +241,7 @@ def run_gpu(args, rank, world, local_rank):
         td.barrier()
     ms = max_over_ranks(ev0.elapsed_time(ev1), device)
     uk1, ue1 = sim.energy()
+    relayouts = sim.layout_stats()
 
     # e2e: the same step driven from host buffers through the C ABI
     e2e = None
@@ -238,7 +269,8 @@ def run_gpu(args, rank, world, local_rank):
                "d2h_bytes_per_step": int(nbytes + 16), "steps": ke}
         del host
     sim.close()
-    B_alg, s_state, s = bytes_alg_per_particle_step(args.form, args.ppc)
+    ncell_all = int(np.prod(cfg["n_cells"]))
+    B_alg, s_state, s = bytes_alg_per_particle_step(args.form, n / ncell_all)
     ncell = int(np.prod(cfg["n_cells"]))
     kernel_bytes = n * s_state + ncell * 9 * s  # state read+write; gather E,B_m and J write per cell
     t_kernel = float(np.mean(t_part)) / 1e3
@@ -246,7 +278,8 @@ def run_gpu(args, rank, world, local_rank):
     value = whole_job_rate(n, world, args.steps, ms)
     return dict(n=n, ms=ms, value=value, wall_ms_per_step=(wall1 - wall0) * 1e3 / args.steps, e2e=e2e,
                 kernel_bytes=kernel_bytes, t_kernel=t_kernel, peak=peak, peak_kind=peak_kind, B_alg=B_alg,
-                launches=launches, clocks=clk.summary(), energy=(uk0, ue0, uk1, ue1), cfg=cfg)
+                launches=launches, clocks=clk.summary(), energy=(uk0, ue0, uk1, ue1), cfg=cfg, tile=tile,
+                tuning=tuning, relayouts=relayouts)
 
 
 def run_cpu_sample(args, steps=None):
@@ -256,9 +289,16 @@ def run_cpu_sample(args, steps=None):
     dx = 0.1
     dt = 0.95 * dx / np.sqrt(3.0)
     from smilei_gb300 import synthetic
-    pos, mom, w = synthetic.thermal_plasma([n, n, n], [dx] * 3, args.ppc, SIGMA_10KEV, args.seed)
+    if getattr(args, "workload", "thermal") == "uneven":
+        # the same patch statistics on an n^3 grid cut into 8^3-cell patches
+        pos, mom, w, _ = synthetic.uneven_plasma([n, n, n], [dx] * 3, [8, 8, 8], 8, 1.5, 64, np.sqrt(5.0 / 511.0),
+                                                 args.seed)
+        pusher, what = "boris", f"3D uneven patches {n}^3 cells in 8^3 patches"
+    else:
+        pos, mom, w = synthetic.thermal_plasma([n, n, n], [dx] * 3, args.ppc, SIGMA_10KEV, args.seed)
+        pusher, what = "higueracary", f"3D thermal {n}^3 cells x {args.ppc} ppc"
     fields = synthetic.periodic_em(args.seed, [n, n, n], 0.0, 0.0)
-    sp = [dict(pos=pos, mom=mom, weight=w, charge=np.full(w.shape, -1, np.int16), mass=1.0, pusher="higueracary")]
+    sp = [dict(pos=pos, mom=mom, weight=w, charge=np.full(w.shape, -1, np.int16), mass=1.0, pusher=pusher)]
     O = oracle.Oracle()
     steps = steps or args.cpu_steps
     O.pic_step(3, [n] * 3, 2, [dx] * 3, dt, fields, sp)  # warm-up
@@ -269,7 +309,7 @@ def run_cpu_sample(args, steps=None):
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     value = pos.shape[1] * steps / (t1 - t0)
     return dict(value=value, unit=UNIT, cores=cores, kind="port",
-                sample=f"3D thermal {n}^3 cells x {args.ppc} ppc ({pos.shape[1]} electrons), Higuera-Cary, "
+                sample=f"{what} ({pos.shape[1]} electrons), {pusher}, "
                        f"{steps} FP64 steps of oracle/pic_oracle.c (OpenMP)")
 
 
@@ -289,13 +329,19 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="thermal", choices=["thermal", "uneven"])
+    ap.add_argument("--autotune", action="store_true", help="pick the tile shape by timing candidates first")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-    workload = (f"3D thermal plasma {args.cells}^3 cells, {args.ppc} ppc electrons "
-                f"({args.cells ** 3 * args.ppc} particles per GPU), Higuera-Cary, dt=0.95 CFL, periodic")
+    if args.workload == "uneven":
+        workload = ("3D uneven patches: 512x256x256 cells in 1024 patches of 32^3, particles per cell per patch "
+                    "8*exp(N(0,1.5)) floored and clipped to [0,64], T=5 keV electrons, Boris, dt=0.95 CFL, periodic")
+    else:
+        workload = (f"3D thermal plasma {args.cells}^3 cells, {args.ppc} ppc electrons "
+                    f"({args.cells ** 3 * args.ppc} particles per GPU), Higuera-Cary, dt=0.95 CFL, periodic")
 
     if args.impl == "reference":
         if rank != 0:
@@ -327,7 +373,7 @@ def main():
         return
     achieved = res["kernel_bytes"] / res["t_kernel"] / 1e9
     tpp = NCU_TRAFFIC_BYTES_PER_PARTICLE.get(args.form)
-    traffic = tpp * res["n"] if (tpp is not None and args.ppc == 8) else None
+    traffic = tpp * res["n"] if (tpp is not None and args.ppc == 8 and args.workload == "thermal") else None
     step_gbs = res["B_alg"] * res["value"] / 1e9
     line = {
         "metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -335,10 +381,12 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+i32" if args.form == "mixed" else "f64",
         "data": "synthetic (seeded Maxwellian, generated on device)",
         "config": {"workload": workload, "form": args.form, "global_particles": res["n"] * world,
-                   "cells": args.cells ** 3, "parallelism": f"replicas x{world}", "l2": "inputs larger than L2",
+                   "cells": int(np.prod(res["cfg"]["n_cells"])), "parallelism": f"replicas x{world}", "l2": "inputs larger than L2",
                    "B_alg_bytes_per_particle_step": res["B_alg"],
                    "hbm_fraction_of_step": step_gbs / res["peak"], "wall_ms_per_step": res["wall_ms_per_step"],
-                   "energy_ukin_uelm_before_after": res["energy"]},
+                   "energy_ukin_uelm_before_after": res["energy"], "tile": res["tile"] or "default 4x4x4",
+                   "autotune_ms_per_step": res["tuning"],
+                   "relayouts_spilled_over_run": res["relayouts"]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": res["peak"], "unit": "GB/s",
                      "frac": achieved / res["peak"], "traffic": traffic, "kernel": "k_step_particles",
                      "algorithmic_bytes_per_launch": res["kernel_bytes"], "peak_source": res["peak_kind"]},

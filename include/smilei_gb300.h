@@ -222,6 +222,10 @@ int sg_sim_copy_state( sg_sim *sim, int species, void *host, int to_device );
 
 /* Device time of the last sg_sim_step call split by stage (ms): particles, fold,
  * maxwell, total; and the number of kernel launches per step. */
+/* Segment re-layouts so far (each follows a step in which some tile's segment filled
+ * up) and the particles that went through the spill list.  No reference counterpart:
+ * the reference re-sorts every step. */
+int sg_sim_layout_stats( sg_sim *sim, int64_t *relayouts, int64_t *spilled );
 int sg_sim_last_timing( sg_sim *sim, double *ms_particles, double *ms_fields, double *ms_total, int *launches_per_step );
 
 /* Sets the stream the simulation runs on (default: a stream it creates). */

@@ -74,6 +74,7 @@ _SIGNATURES = {
     "sg_sim_get_species": (_I, [_VP, _I, _VP, _VP, _VP]),
     "sg_sim_species_scalars": (_I, [_VP, _I, _VP]),
     "sg_sim_field_energies": (_I, [_VP, _VP]),
+    "sg_sim_layout_stats": (_I, [_VP, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
     "sg_sim_energy": (_I, [_VP, ctypes.POINTER(_D), ctypes.POINTER(_D)]),
     "sg_sim_last_timing": (_I, [_VP, ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.POINTER(_D),
                                 ctypes.POINTER(_I)]),

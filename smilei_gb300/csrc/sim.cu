@@ -1229,13 +1229,28 @@ __global__ void k_stage( GridInfo g, int64_t n, const double *__restrict__ pos, 
     atomicAdd( &count[t], 1 );
 }
 
-// cap[t] = count[t] * (1 + slack) + min_extra, rounded up to a multiple of 4.
-__global__ void k_caps( int nt, const int *__restrict__ count, int *__restrict__ cap, float slack, int min_extra )
+// cap[t] = count[t] + max(count[t] * slack, slack * (largest count of the face
+// neighbours), min_extra), rounded up to a multiple of 4.  The neighbour term
+// gives a sparse tile next to a dense one room for the particles that flow in,
+// so density edges do not spill every step.
+__global__ void k_caps( GridInfo g, const int *__restrict__ count, int *__restrict__ cap, float slack, int min_extra )
 {
+    const int nt = g.ntiles;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if( t >= nt ) return;
+    const int n2 = g.ndim == 3 ? g.nt[2] : 1, n1 = g.nt[1], n0 = g.nt[0];
+    const int tz = t % n2, ty = ( t / n2 ) % n1, tx = t / ( n2 * n1 );
+    int nb = 0;
+    for( int d = 0; d < g.ndim; d++ )
+        for( int sgn = -1; sgn <= 1; sgn += 2 ) {
+            int x = tx, y = ty, z = tz;
+            if( d == 0 ) x = ( tx + sgn + n0 ) % n0;
+            if( d == 1 ) y = ( ty + sgn + n1 ) % n1;
+            if( d == 2 ) z = ( tz + sgn + n2 ) % n2;
+            nb = max( nb, count[( x * n1 + y ) * n2 + z] );
+        }
     const int c = count[t];
-    int v = c + max( ( int )ceilf( c * slack ), min_extra );
+    const int v = c + max( max( ( int )ceilf( c * slack ), ( int )ceilf( nb * slack ) ), min_extra );
     cap[t] = ( v + 3 ) & ~3;
 }
 
@@ -1497,6 +1512,8 @@ struct sg_sim {
     cudaEvent_t ev[4] = { nullptr, nullptr, nullptr, nullptr }; // step start, particles start/end, step end
     float last_ms[3] = { 0, 0, 0 };
     int launches_per_step = 0;
+    int64_t relayouts = 0;       // segment re-layouts after a spill
+    int64_t spilled = 0;         // particles that went through the spill list
     size_t smem_bytes = 0;
 };
 
@@ -1688,7 +1705,7 @@ int layout_from_counts( sg_sim *S, const int *count, int *new_cap, int64_t *new_
     const float slack = ( float )( S->cfg.capacity_slack > 0.0 ? S->cfg.capacity_slack : 0.25 );
     // room beyond the slack fraction: 16 particles at the default slack of 0.25, less when the slack is smaller
     const int min_extra = ( int )std::ceil( 16.0 * std::min( 1.0, slack / 0.25 ) );
-    k_caps<<<grid_for( nt, 256 ), 256, 0, S->stream>>>( nt, count, new_cap, slack, min_extra );
+    k_caps<<<grid_for( nt, 256 ), 256, 0, S->stream>>>( S->g, count, new_cap, slack, min_extra );
     SG_LAUNCH_CHECK( "k_caps" );
     int r = exclusive_scan<int>( new_cap, nt, new_start, S->scan_scratch, S->stream );
     if( r ) return r;
@@ -2087,11 +2104,21 @@ int sg_sim_step( sg_sim *S, int nsteps )
         for( size_t k = 0; k < S->sp.size(); k++ ) {
             const int nspill = S->h_flags[1 + k];
             if( nspill > 0 ) {
+                S->relayouts++;
+                S->spilled += nspill;
                 int r = relayout( S, S->sp[k], nspill );
                 if( r ) return r;
             }
         }
     }
+    return SG_OK;
+}
+
+int sg_sim_layout_stats( sg_sim *S, int64_t *relayouts, int64_t *spilled )
+{
+    SG_REQUIRE( S, "NULL simulation" );
+    if( relayouts ) *relayouts = S->relayouts;
+    if( spilled ) *spilled = S->spilled;
     return SG_OK;
 }
 

@@ -159,6 +159,12 @@ class Simulation:
         check(_lib.lib().sg_sim_charge_residual(self._h, ctypes.byref(r), ctypes.byref(m)), "charge_residual")
         return r.value
 
+    def layout_stats(self):
+        """(segment re-layouts so far, particles that went through the spill list)."""
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        check(_lib.lib().sg_sim_layout_stats(self._h, ctypes.byref(a), ctypes.byref(b)), "layout_stats")
+        return a.value, b.value
+
     def last_timing(self):
         """Device ms of the last step: (particles, fields, total) and kernel launches per step."""
         a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()

@@ -64,3 +64,35 @@ def periodic_em(seed, n_cells, e_scale=0.05, b_scale=0.05):
         st = STAGGER[k][:ndim]
         out[k] = np.zeros(tuple(n_cells[d] + 5 + st[d] for d in range(ndim)))
     return out
+
+
+def patch_ppc(n_patches, median_ppc, sigma_ln, ppc_max, seed):
+    """Particles per cell of each patch: median_ppc * exp(N(0, sigma_ln)), floored, clipped to [0, ppc_max]."""
+    rng = np.random.default_rng(seed)
+    z = rng.normal(0.0, sigma_ln, int(np.prod(n_patches)))
+    return np.clip(np.floor(median_ppc * np.exp(z)), 0, ppc_max).astype(np.int64).reshape(tuple(n_patches))
+
+
+def uneven_plasma(n_cells, cell_length, patch, median_ppc, sigma_ln, ppc_max, sigma_p, seed, density=1.0):
+    """Plasma whose particles per cell vary by patch (log-normal, clipped): pos, mom, weight, ppc per patch.
+
+    Every macro-particle carries the weight of the median density, so a patch's
+    density is proportional to its particles per cell."""
+    ndim = len(n_cells)
+    n_patches = [n_cells[d] // patch[d] for d in range(ndim)]
+    ppc_p = patch_ppc(n_patches, median_ppc, sigma_ln, ppc_max, seed)
+    rng = np.random.default_rng(seed + 1)
+    grids = np.meshgrid(*[np.arange(n) for n in n_cells], indexing="ij")
+    cell_ppc = ppc_p[tuple(g // patch[d] for d, g in enumerate(grids))].ravel()
+    cells = np.repeat(np.arange(int(np.prod(n_cells)), dtype=np.int64), cell_ppc)
+    n = cells.size
+    pos = np.empty((ndim, n))
+    rem = cells
+    strides = [int(np.prod(n_cells[d + 1:])) for d in range(ndim)]
+    for d in range(ndim):
+        c = rem // strides[d]
+        rem = rem % strides[d]
+        pos[d] = (c + rng.random(n)) * cell_length[d]
+    mom = rng.normal(0.0, sigma_p, (3, n))
+    w = np.full(n, density * float(np.prod(cell_length)) / median_ppc)
+    return pos, mom, w, ppc_p

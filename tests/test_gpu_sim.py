@@ -143,3 +143,21 @@ def test_energy_diagnostic_matches_numpy(sim_mod):
     assert abs(uk - uk_ref) <= 1e-12 * abs(uk_ref)
     assert abs(ue - ue_ref) <= 1e-12 * abs(ue_ref)
     sim.close()
+
+
+def test_autotune_times_every_candidate_and_keeps_the_fastest(sim_mod):
+    simulation, synthetic = sim_mod
+    from smilei_gb300 import autotune
+    n_cells, cl = [16, 16, 16], [0.1, 0.1, 0.1]
+    dt = 0.95 / np.sqrt(sum(1.0 / c ** 2 for c in cl))
+    pos, mom, w, ppc_p = synthetic.uneven_plasma(n_cells, cl, [8, 8, 8], 8, 1.5, 64, 0.14, 4)
+    assert ppc_p.max() > ppc_p.min()
+
+    def build(tile):
+        sim = simulation.Simulation(n_cells, cl, dt, form="mixed", tile=list(tile))
+        sim.add_species(1.0, -1.0, "boris", pos, mom, w)
+        return sim
+
+    best, times = autotune.tune_tiles(build, ndim=3, warmup=1, steps=2)
+    assert set(times) == set(autotune.CANDIDATES_3D)
+    assert best == min(times, key=times.get) and all(t > 0 for t in times.values())
