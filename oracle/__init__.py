@@ -50,7 +50,7 @@ def field_shape(ndim: int, n_prim, comp: str):
 def build(force: bool = False) -> str:
     """Compile ``pic_oracle.c`` into ``liboracle.so`` (gcc, OpenMP, no FP contraction)."""
     src = os.path.join(HERE, "pic_oracle.c")
-    srcs = [src, os.path.join(HERE, "rad_oracle.c")]
+    srcs = [src, os.path.join(HERE, "rad_oracle.c"), os.path.join(HERE, "bc_oracle.c")]
     srcs = [s for s in srcs if os.path.exists(s)]
     if (not force and os.path.exists(LIB_PATH)
             and all(os.path.getmtime(LIB_PATH) >= os.path.getmtime(s) for s in srcs)):
@@ -70,6 +70,15 @@ def build_ref() -> str | None:
         return None
     subprocess.run(["bash", script], check=True, stdout=subprocess.DEVNULL)
     return REF_PATH if os.path.exists(REF_PATH) else None
+
+
+LASER_KEYS = ["a0", "omega", "waist", "focus_x", "focus_y", "polarization_phi", "ellipticity", "phase_offset",
+              "t_start", "t_duration", "t_center", "t_fwhm", "t_order"]
+
+
+def laser_params(laser: dict) -> list:
+    """The 13 numbers of bc_oracle.c's Gaussian 2D laser, in order."""
+    return [float(laser[k]) for k in LASER_KEYS]
 
 
 def _f64(a):
@@ -189,6 +198,51 @@ class Oracle(_Backend):
                              _ptrs([_f64(s["weight"]) for s in species]),
                              _ptrs([np.ascontiguousarray(s["charge"], dtype=np.int16) for s in species]))
 
+    def pic_step_bc(self, n_cells, oversize, cell_length, dt, fields, species, periodic, laser=None, time_dual=0.0):
+        """2D step with open boundaries (bc_oracle.c or_pic_step_bc).  periodic: (px, py) flags;
+        laser: LASER_KEYS dict for a Gaussian laser on xmin, or None.  Species arrays are
+        replaced by their compacted survivors (pos, mom, weight, charge)."""
+        order = ["Ex", "Ey", "Ez", "Bx", "By", "Bz", "Bx_m", "By_m", "Bz_m", "Jx", "Jy", "Jz"]
+        farr = [fields[k] for k in order]
+        for a in farr:
+            assert a.dtype == np.float64 and a.flags.c_contiguous
+        ns = len(species)
+        npart = (ctypes.c_int64 * ns)(*[s["mom"].shape[1] for s in species])
+        mass = _d([s["mass"] for s in species])
+        pusher = _i32([PUSHERS[s["pusher"]] for s in species])
+        arrs = []
+        for s in species:
+            s["pos"] = np.ascontiguousarray(s["pos"], dtype=np.float64)
+            s["mom"] = np.ascontiguousarray(s["mom"], dtype=np.float64)
+            s["weight"] = np.ascontiguousarray(s["weight"], dtype=np.float64)
+            s["charge"] = np.ascontiguousarray(s["charge"], dtype=np.int16)
+            arrs.append(s)
+        lz = _d(laser_params(laser)) if laser is not None else None
+        self.lib.or_pic_step_bc(_i32(n_cells), oversize, _d(cell_length), ctypes.c_double(dt), _ptrs(farr), ns, npart,
+                                mass, pusher, _ptrs([s["pos"] for s in arrs]), _ptrs([s["mom"] for s in arrs]),
+                                _ptrs([s["weight"] for s in arrs]), _ptrs([s["charge"] for s in arrs]),
+                                _i32(list(periodic)), lz, ctypes.c_double(time_dual))
+        for k, s in enumerate(arrs):
+            m = int(npart[k])
+            nd = s["pos"].shape[0]
+            s["pos"] = s["pos"].ravel()[: nd * m].reshape(nd, m).copy()
+            s["mom"] = s["mom"].ravel()[: 3 * m].reshape(3, m).copy()
+            s["weight"] = s["weight"][:m].copy()
+            s["charge"] = s["charge"][:m].copy()
+
+    def sm_apply_2d(self, side, n_prim, cell_length, dt, F, b1=None, b2=None, tmin=1, tmax=1, k=None):
+        """One Silver-Mueller side on F = [Ex, Ey, Ez, Bx, By, Bz] (updated in place)."""
+        kdef = [(1.0, 0.0), (-1.0, 0.0), (0.0, 1.0), (0.0, -1.0)][side]
+        self.lib.or_sm_apply_2d(side, _i32(n_prim), _d(cell_length), ctypes.c_double(dt), _d(k or kdef), _ptrs(F),
+                                _ptr(b1) if b1 is not None else None, _ptr(b2) if b2 is not None else None, tmin, tmax)
+
+    def laser_gaussian2d(self, laser, y, profile, t):
+        """Separable amplitude of a Gaussian 2D laser (profile 0: primal points, 1: dual) at y, time t."""
+        y = _f64(y)
+        out = np.zeros_like(y)
+        self.lib.or_laser_gaussian2d(_d(laser_params(laser)), y.size, _ptr(y), profile, ctypes.c_double(t), _ptr(out))
+        return out
+
     def sort(self, ndim, patch_size, xmin, cell_length, pos):
         """Per-cell sort: returns (keys, first_index, last_index, perm)."""
         pos = _f64(pos); n = pos.shape[1]
@@ -239,6 +293,23 @@ class RefOps(_Backend):
     def maxwell(self, which, ndim, n_prim, cell_length, dt, F):
         cells, os_ = self._patch(ndim, n_prim)
         self.lib.ref_maxwell(which, ndim, cells, os_, _d(cell_length), ctypes.c_double(dt), _ptrs(F))
+        return F
+
+    def sm_apply_2d(self, side, n_prim, cell_length, dt, F, tmin=1, tmax=1, laser=None, time_dual=0.0):
+        """The reference's ElectroMagnBC2D_SM::apply on F = [Ex..Bz] (in place).  laser: dict with
+        lt = [start, end, invsigma, center, order], omega, sp1/ph1 (primal points), d1, sp2/ph2 (dual), d2."""
+        cells, os_ = self._patch(2, n_prim)
+        F = [_f64(a) for a in F]
+        if laser is None:
+            self.lib.ref_sm_apply_2d(side, cells, os_, _d(cell_length), ctypes.c_double(dt), _ptrs(F), tmin, tmax,
+                                     None, ctypes.c_double(1.0), None, None, ctypes.c_double(0.0), None, None,
+                                     ctypes.c_double(0.0), ctypes.c_double(time_dual))
+        else:
+            L = {k: (_f64(v) if isinstance(v, np.ndarray) else v) for k, v in laser.items()}
+            self.lib.ref_sm_apply_2d(side, cells, os_, _d(cell_length), ctypes.c_double(dt), _ptrs(F), tmin, tmax,
+                                     _d(L["lt"]), ctypes.c_double(L["omega"]), _ptr(L["sp1"]), _ptr(L["ph1"]),
+                                     ctypes.c_double(L["d1"]), _ptr(L["sp2"]), _ptr(L["ph2"]), ctypes.c_double(L["d2"]),
+                                     ctypes.c_double(time_dual))
         return F
 
     # -- radiation tables --------------------------------------------------

@@ -37,6 +37,8 @@ ElectroMagnSolver/MF_Solver2D_Yee.cpp ElectroMagnSolver/MF_Solver3D_Yee.cpp
 Field/Field.cpp Field/Field2D.cpp Field/Field3D.cpp Particles/Particles.cpp
 Radiation/RadiationTables.cpp Radiation/RadiationTablesDefault.cpp Radiation/Table.cpp Radiation/Table2D.cpp
 SmileiMPI/AsyncMPIbuffers.cpp Tools/H5.cpp Particles/Particle.cpp
+ElectroMagnBC/ElectroMagnBC.cpp ElectroMagnBC/ElectroMagnBC2D.cpp ElectroMagnBC/ElectroMagnBC2D_SM.cpp
+ElectroMagn/Laser.cpp Profiles/Function.cpp Profiles/Profile.cpp Tools/gpu.cpp
 "
 
 pids=()

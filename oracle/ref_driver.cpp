@@ -62,6 +62,10 @@
 #include "MF_Solver3D_Yee.h"
 #include "RadiationTables.h"
 #include "RadiationTablesDefault.h"
+#include "ElectroMagnBC2D_SM.h"
+#include "Laser.h"
+#include "Profile.h"
+#include "Function.h"
 #undef private
 #undef protected
 
@@ -379,6 +383,77 @@ int ref_rad_photon_chi( int n, const double *chi, const double *xi, double *out 
 {
     RadiationTables *r = rad();
     for( int i = 0; i < n; i++ ) out[i] = r->computeRandomPhotonChiWithInterpolation( chi[i], xi[i] );
+    return 0;
+}
+
+// One side of the reference's 2D Silver-Mueller condition
+// (ElectroMagnBC2D_SM::apply, ElectroMagnBC2D_SM.cpp:118-265) on a single patch.
+// Tangent ends are boundaries when tmin/tmax are set.  With lt != NULL a separable
+// laser (LaserProfileSeparable, Laser.cpp:287-302,453-460) is attached: its time
+// profile is the compiled tgaussian (Function_TimeGaussian, Function.cpp:528-535;
+// lt = {start, end, invsigma, center, order}), its chirp the constant 1, and its
+// space envelope and phase are given per point (sp1/ph1 on the primal points along
+// the side, sp2/ph2 on the dual points), with delays d1, d2 and frequency omega.
+int ref_sm_apply_2d( int side, const int *patch_cells, const int *oversize, const double *cell_length, double dt,
+                     double *const *F, int tmin, int tmax, const double *lt, double omega, const double *sp1,
+                     const double *ph1, double d1, const double *sp2, const double *ph2, double d2, double time_dual )
+{
+    Geometry g = make_geom( 2, patch_cells, oversize );
+    Params *params = make_params( g, cell_length, dt );
+    static const double kdef[4][2] = { { 1.0, 0.0 }, { -1.0, 0.0 }, { 0.0, 1.0 }, { 0.0, -1.0 } };
+    new( &params->EM_BCs_k ) std::vector<std::vector<double>>();
+    for( int k = 0; k < 4; k++ ) params->EM_BCs_k.push_back( std::vector<double>( kdef[k], kdef[k] + 2 ) );
+    const int begin[2] = { -oversize[0], -oversize[1] };
+    Patch *patch = make_patch( 2, begin );
+    new( &patch->size_ ) std::vector<unsigned int>( g.patch, g.patch + 2 );
+    new( &patch->oversize ) std::vector<unsigned int>( g.oversize, g.oversize + 2 );
+    new( &patch->min_local_ ) std::vector<double>( 2, 0.0 );
+    new( &patch->neighbor_ ) std::vector<std::vector<int>>( 2, std::vector<int>( 2, 0 ) );
+    const int ax = side / 2, tan = ax == 0 ? 1 : 0;
+    patch->neighbor_[ax][0] = patch->neighbor_[ax][1] = MPI_PROC_NULL;
+    if( tmin ) patch->neighbor_[tan][0] = MPI_PROC_NULL;
+    if( tmax ) patch->neighbor_[tan][1] = MPI_PROC_NULL;
+    double *arr[13] = { F[0], F[1], F[2], F[3], F[4], F[5], nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr };
+    ElectroMagn *em = make_em( g, arr );
+    new( &em->oversize ) std::vector<unsigned int>( g.oversize, g.oversize + 2 );
+    ElectroMagnBC2D_SM *bc = new ElectroMagnBC2D_SM( *params, patch, ( unsigned int )side );
+    if( lt ) {
+        Function_TimeGaussian *tmpl = zeroed<Function_TimeGaussian>();
+        tmpl->start = lt[0];
+        tmpl->end = lt[1];
+        tmpl->invsigma = lt[2];
+        tmpl->center = lt[3];
+        tmpl->order = lt[4];
+        Function_TimeConstant *ctmpl = zeroed<Function_TimeConstant>();
+        ctmpl->start = -1e300;
+        Profile *tprof[2], *cprof[2];
+        for( int k = 0; k < 2; k++ ) {
+            tprof[k] = zeroed<Profile>();
+            tprof[k]->function_ = new Function_TimeGaussian( tmpl );
+            cprof[k] = zeroed<Profile>();
+            cprof[k]->function_ = new Function_TimeConstant( ctmpl );
+        }
+        Laser *laser = zeroed<Laser>();
+        new( &laser->profiles ) std::vector<LaserProfile *>();
+        const unsigned n1p = g.n_prim[tan], n1d = g.n_dual[tan];
+        for( int k = 0; k < 2; k++ ) {
+            LaserProfileSeparable *lp = new LaserProfileSeparable( omega, cprof[k], tprof[k], nullptr, nullptr,
+                                                                   k == 0 ? d1 : d2, k == 0, ( unsigned int )ax );
+            const unsigned n = k == 0 ? n1p : n1d;
+            std::vector<unsigned int> dims = { n, 1 };
+            lp->space_envelope = new Field2D( dims );
+            lp->phase = new Field2D( dims );
+            for( unsigned j = 0; j < n; j++ ) {
+                ( *lp->space_envelope )( j, 0 ) = ( k == 0 ? sp1 : sp2 )[j];
+                ( *lp->phase )( j, 0 ) = ( k == 0 ? ph1 : ph2 )[j];
+            }
+            laser->profiles.push_back( lp );
+        }
+        bc->vecLaser.push_back( laser );
+    }
+    bc->apply( em, time_dual, patch );
+    double *out[13] = { F[0], F[1], F[2], F[3], F[4], F[5], nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr };
+    copy_back( em, out );
     return 0;
 }
 

@@ -137,6 +137,66 @@ def case_radiation(ref, rng):
                 xi_axis1_min=t["xi_axis1_min"])
 
 
+def reference_laser_gaussian2d(cfg):
+    """Runs the reference's own pyinit.py and pyprofiles.py (pure Python, from the reference
+    tree) to build LaserGaussian2D and returns its Laser component."""
+    ns = {}
+    for f in ("pyinit.py", "pyprofiles.py"):
+        path = os.path.join("/root/reference/src/Python", f)
+        exec(compile(open(path).read(), path, "exec"), ns)
+    ns["Main"](geometry="2Dcartesian", interpolation_order=2, timestep=cfg["dt"], simulation_time=cfg["t_sim"],
+               cell_length=list(cfg["cell_length"]), grid_length=list(cfg["grid_length"]), number_of_patches=[1, 1])
+    ns["LaserGaussian2D"](box_side="xmin", a0=cfg["a0"], omega=cfg["omega"], focus=list(cfg["focus"]),
+                          waist=cfg["waist"], polarization_phi=cfg["polarization_phi"], ellipticity=cfg["ellipticity"],
+                          time_envelope=ns["tgaussian"](center=cfg["t_center"], fwhm=cfg["t_fwhm"]))
+    return ns["Laser"][0]
+
+
+def case_silver_mueller(ref, rng, side, tmin, tmax, laser_cfg=None, time_dual=0.0):
+    """One side of the reference's 2D Silver-Mueller condition on random fields, with or
+    without a Gaussian laser on xmin (space and phase from the reference's Python profiles)."""
+    cells, cl, dt, os_ = [9, 7], [0.1, 0.3], 0.08, 2
+    n_prim = [c + 1 + 2 * os_ for c in cells]
+    F = random_fields(rng, 2, n_prim, FIELDS_EB)
+    out = dict(side=side, tmin=tmin, tmax=tmax, n_prim=n_prim, cell_length=cl, dt=dt, time_dual=time_dual,
+               **{k + "_in": F[k].copy() for k in FIELDS_EB})
+    laser = None
+    if laser_cfg is not None:
+        L = reference_laser_gaussian2d(dict(laser_cfg, dt=dt, cell_length=cl,
+                                            grid_length=[cells[0] * cl[0], cells[1] * cl[1]]))
+        te = L.time_envelope
+        yp = (np.arange(n_prim[1]) - os_) * cl[1]
+        yd = (np.arange(n_prim[1] + 1) - 0.5 - os_) * cl[1]
+        laser = dict(lt=[te.start, te.start + te.duration, 1.0 / te.sigma, te.center, te.order], omega=L.omega,
+                     sp1=np.array([L.space_envelope[0](y) for y in yp]), ph1=np.array([L.phase[0](y) for y in yp]),
+                     d1=L.delay_phase[0], sp2=np.array([L.space_envelope[1](y) for y in yd]),
+                     ph2=np.array([L.phase[1](y) for y in yd]), d2=L.delay_phase[1])
+        out.update({"laser_" + k: np.asarray(v) for k, v in laser.items()})
+        out.update({"cfg_" + k: np.asarray(v) for k, v in laser_cfg.items()})
+        out["t_duration"] = te.duration
+    res = ref.sm_apply_2d(side, n_prim, cl, dt, [F[k] for k in FIELDS_EB], tmin, tmax, laser, time_dual)
+    out.update({k: res[i] for i, k in enumerate(FIELDS_EB)})
+    return out
+
+
+def boundary_cases(ref):
+    rng = np.random.default_rng(20261205)
+    cases = {}
+    for side in range(4):
+        for tmin, tmax in ((1, 1), (0, 0)):
+            cases[f"sm_side{side}_t{tmin}{tmax}"] = case_silver_mueller(ref, rng, side, tmin, tmax)
+    lasers = {
+        "linear_focus0": dict(a0=2.0, omega=1.0, focus=[0.0, 1.05], waist=0.8, polarization_phi=0.0,
+                              ellipticity=0.0, t_center=0.5, t_fwhm=0.6, t_sim=3.0),
+        "elliptic_focus_inside": dict(a0=1.3, omega=2.0, focus=[0.4, 0.9], waist=0.6, polarization_phi=0.7,
+                                      ellipticity=0.3, t_center=0.8, t_fwhm=0.9, t_sim=3.0),
+    }
+    for name, cfg in lasers.items():
+        for k, t in enumerate((0.3, 0.55, 1.7)):
+            cases[f"laser_{name}_{k}"] = case_silver_mueller(ref, rng, 0, 1, 1, cfg, t)
+    return cases
+
+
 def main():
     path = oracle.build_ref()
     if path is None:
@@ -157,7 +217,10 @@ def main():
                         **{f"{c}/{k}": np.asarray(v) for c, d in cases.items() for k, v in d.items()})
     rad = case_radiation(ref, rng)
     np.savez_compressed(os.path.join(HERE, "radiation.npz"), **{k: np.asarray(v) for k, v in rad.items()})
-    print("wrote", len(cases), "operator cases and the radiation case")
+    bcases = boundary_cases(ref)
+    np.savez_compressed(os.path.join(HERE, "boundaries.npz"),
+                        **{f"{c}/{k}": np.asarray(v) for c, d in bcases.items() for k, v in d.items()})
+    print("wrote", len(cases), "operator cases, the radiation case and", len(bcases), "boundary cases")
 
 
 if __name__ == "__main__":
