@@ -139,13 +139,19 @@ int sg_sort_particles_noalloc( int ndim, const int *patch_size, const double *xm
 typedef struct sg_sim_config {
     int ndim;              /* 2 or 3 */
     int form;              /* SG_FORM_FP64 or SG_FORM_MIXED */
-    int n_cells[3];        /* global cells per dimension (periodic) */
+    int n_cells[3];        /* global cells per dimension */
     double cell_length[3];
     double dt;
     int tile[3];           /* cells per tile (bin) per dimension; 0 = choose automatically */
     double capacity_slack; /* extra room per tile, as a fraction of its count (e.g. 0.25) */
     int use_graph;         /* capture each timestep as a CUDA graph */
+    int bc[3];             /* per dimension: SG_BC_PERIODIC, or SG_BC_OPEN (2D only): Silver-Mueller
+                              field boundaries (ElectroMagnBC2D_SM) on both sides and particles removed
+                              when they leave (remove_particle_inf/_sup) */
 } sg_sim_config;
+
+#define SG_BC_PERIODIC 0
+#define SG_BC_OPEN 1
 
 typedef struct sg_sim sg_sim;
 
@@ -222,6 +228,15 @@ int sg_sim_copy_state( sg_sim *sim, int species, void *host, int to_device );
 
 /* Device time of the last sg_sim_step call split by stage (ms): particles, fold,
  * maxwell, total; and the number of kernel launches per step. */
+/* Adds a Gaussian 2D laser injected through the Silver-Mueller condition on xmin
+ * (LaserGaussian2D, src/Python/pyprofiles.py:507; ElectroMagnBC2D_SM::apply,
+ * src/ElectroMagnBC/ElectroMagnBC2D_SM.cpp:118).  p = {a0, omega, waist, focus_x,
+ * focus_y, polarization_phi, ellipticity, phase_offset, t_start, t_duration, t_center,
+ * t_fwhm, t_order} (time envelope tgaussian).  The step k (0-based, counted from
+ * creation) applies it at time (k + 1.5) dt, the reference's time_dual of iteration k+1.
+ * Needs a 2D grid with an open x axis; at most 4 lasers. */
+int sg_sim_add_laser_gaussian2d( sg_sim *sim, const double *params );
+
 /* Segment re-layouts so far (each follows a step in which some tile's segment filled
  * up) and the particles that went through the spill list.  No reference counterpart:
  * the reference re-sorts every step. */

@@ -21,6 +21,8 @@ ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "particle out of reach",
 
 FORM_FP64 = 0
 FORM_MIXED = 1
+BC_PERIODIC = 0
+BC_OPEN = 1
 PUSHERS = {"boris": 0, "vay": 1, "higueracary": 2}
 
 
@@ -38,7 +40,7 @@ class GridGeom(ctypes.Structure):
 class SimConfig(ctypes.Structure):
     _fields_ = [("ndim", ctypes.c_int), ("form", ctypes.c_int), ("n_cells", ctypes.c_int * 3),
                 ("cell_length", ctypes.c_double * 3), ("dt", ctypes.c_double), ("tile", ctypes.c_int * 3),
-                ("capacity_slack", ctypes.c_double), ("use_graph", ctypes.c_int)]
+                ("capacity_slack", ctypes.c_double), ("use_graph", ctypes.c_int), ("bc", ctypes.c_int * 3)]
 
 
 _VP = ctypes.c_void_p
@@ -74,6 +76,7 @@ _SIGNATURES = {
     "sg_sim_get_species": (_I, [_VP, _I, _VP, _VP, _VP]),
     "sg_sim_species_scalars": (_I, [_VP, _I, _VP]),
     "sg_sim_field_energies": (_I, [_VP, _VP]),
+    "sg_sim_add_laser_gaussian2d": (_I, [_VP, _VP]),
     "sg_sim_layout_stats": (_I, [_VP, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
     "sg_sim_energy": (_I, [_VP, ctypes.POINTER(_D), ctypes.POINTER(_D)]),
     "sg_sim_last_timing": (_I, [_VP, ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.POINTER(_D),

@@ -48,6 +48,7 @@ struct GridInfo {
     int tshift[3]; // log2(T) when T is a power of two, else -1
     int nt[3];  // tiles per dimension
     int ntiles;
+    int open[3]; // 1: open axis (Silver-Mueller fields, particles removed at x < 0 or x >= L)
     double dx[3], dxi[3], L[3], dt;
 };
 
@@ -399,13 +400,14 @@ __device__ __forceinline__ void deposit_direct( T *sJ, const TileDims &td, int j
 // v_z), plane 6 the packed node shifts; planes 0-2 and 7 are kept.
 constexpr int REC = 8;
 constexpr int NO_SHIFT = 1 | ( 1 << 2 ) | ( 1 << 4 ); // packed shifts (s + 1 per 2 bits) of a particle that keeps its node
+constexpr int GONE_RECORD = 1 << 8;                  // record of a particle removed at an open boundary: deposits nothing
 
 template <int DIM, bool MIXED, int KIND, bool CELLS>
 __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_particles(
     GridInfo g, Fields<typename std::conditional<MIXED, float, double>::type> f, SpecParams sp, PBuf<MIXED> in,
     PBuf<MIXED> out, const int64_t *__restrict__ seg_start, const int *__restrict__ cap,
     const int *__restrict__ count_in, int *__restrict__ count_out, PBuf<MIXED> ovf, int *__restrict__ ovf_tile,
-    int *__restrict__ ovf_count, int ovf_cap, int *__restrict__ status, int nmax )
+    int *__restrict__ ovf_count, int ovf_cap, int *__restrict__ status, int nmax, int *__restrict__ removed )
 {
     using T = typename std::conditional<MIXED, float, double>::type;
     extern __shared__ __align__( 16 ) unsigned char smem_raw[];
@@ -589,7 +591,7 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
                     xabs[d] = ( double )in.x[d][src];
                     xpn[d] = xabs[d] * g.dxi[d];
                     int ip = round_half_away( xpn[d] );
-                    if( ip >= g.N[d] ) { // x in [L - dx/2, L): use the image node 0
+                    if( !g.open[d] && ip >= g.N[d] ) { // periodic, x in [L - dx/2, L): use the image node 0
                         ip -= g.N[d];
                         img[d] = g.N[d];
                         xpn[d] -= ( double )g.N[d];
@@ -694,16 +696,30 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
 #pragma unroll
             for( int d = 0; d < DIM; d++ ) shift[d] = shift[d] < -1 ? -1 : ( shift[d] > 1 ? 1 : shift[d] );
         }
+        // leaving through an open boundary (x < 0 or x >= L): the particle loses its charge
+        // and deposits nothing (remove_particle_inf/_sup, BoundaryConditionType.cpp:204-294)
+        bool gone = false;
+#pragma unroll
+        for( int d = 0; d < DIM; d++ ) {
+            if( !g.open[d] ) continue;
+            if constexpr( MIXED ) {
+                const int v = gnode[d] + shift[d];
+                gone |= v < 0 || ( v == 0 && dnew[d] < T( 0 ) ) || v > g.N[d] || ( v == g.N[d] && dnew[d] >= T( 0 ) );
+            } else {
+                gone |= xabs[d] < 0.0 || xabs[d] >= g.L[d];
+            }
+        }
+        gone = gone && valid;
 
         // ---- Esirkepov deposit: direct, or a record for the per-cell pass ----
         if( valid ) {
             if constexpr( CELLS ) {
-                const int sbits = ( shift[0] + 1 ) | ( ( shift[1] + 1 ) << 2 ) | ( ( shift[2] + 1 ) << 4 );
+                const int sbits = gone ? GONE_RECORD : ( shift[0] + 1 ) | ( ( shift[1] + 1 ) << 2 ) | ( ( shift[2] + 1 ) << 4 );
                 sRec[3 * nmax + q] = ( float )dnew[0];
                 sRec[4 * nmax + q] = ( float )dnew[1];
                 sRec[5 * nmax + q] = DIM == 3 ? ( float )dnew[2] : ( float )( pz * ginv );
                 sRec[6 * nmax + q] = __int_as_float( sbits );
-            } else {
+            } else if( !gone ) {
                 EsirWin<T> W[3];
 #pragma unroll
                 for( int d = 0; d < DIM; d++ ) esir_win<T>( cp[d][0], cp[d][1], cp[d][2], dnew[d], shift[d], W[d] );
@@ -714,7 +730,7 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
 
         if constexpr( CELLS ) {
             // node-changing particles go to a list deposited with full warps later
-            const bool cross = valid && ( shift[0] | shift[1] | shift[2] ) != 0;
+            const bool cross = valid && !gone && ( shift[0] | shift[1] | shift[2] ) != 0;
             if( cross ) {
                 const int nsh = ( shift[0] != 0 ) + ( shift[1] != 0 ) + ( shift[2] != 0 );
                 atomicAdd( &sXc[nsh == 1 ? ( shift[0] != 0 ? 0 : ( shift[1] != 0 ? 1 : 2 ) ) : 3], 1 );
@@ -729,43 +745,53 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
         }
 
         // ---- destination tile and write-out --------------------------------------
+        // periodic axes wrap; an open axis keeps nodes 0..N (particles beyond are gone)
         int nn[3] = { 0, 0, 0 };
         if constexpr( MIXED ) {
 #pragma unroll
             for( int d = 0; d < DIM; d++ ) {
                 int v = gnode[d] + shift[d];
-                if( v < 0 ) v += g.N[d];
-                if( v >= g.N[d] ) v -= g.N[d];
+                if( !g.open[d] ) {
+                    if( v < 0 ) v += g.N[d];
+                    if( v >= g.N[d] ) v -= g.N[d];
+                }
                 nn[d] = v;
             }
         } else {
 #pragma unroll
             for( int d = 0; d < DIM; d++ ) {
                 double x = xabs[d];
-                if( x < 0.0 ) x += g.L[d];
-                if( x >= g.L[d] ) x -= g.L[d];
+                if( !g.open[d] ) {
+                    if( x < 0.0 ) x += g.L[d];
+                    if( x >= g.L[d] ) x -= g.L[d];
+                }
                 xabs[d] = x;
                 int ip = round_half_away( x * g.dxi[d] );
-                if( ip >= g.N[d] ) ip -= g.N[d];
+                if( !g.open[d] && ip >= g.N[d] ) ip -= g.N[d];
                 nn[d] = ip;
             }
         }
+        const bool keep = valid && !gone;
         // a non-finite or runaway particle must not index outside the tile tables
 #pragma unroll
         for( int d = 0; d < DIM; d++ ) {
-            if( valid && ( nn[d] < 0 || nn[d] >= g.N[d] ) ) {
+            if( keep && ( nn[d] < 0 || nn[d] >= g.N[d] + g.open[d] ) ) {
                 atomicCAS( status, 0, SG_ERR_BOUNDS );
                 nn[d] = 0;
             }
         }
-        const int dest = valid ? tile_of( g, nn[0], nn[1], DIM == 3 ? nn[2] : 0 ) : -1;
+        {
+            const unsigned gm = __ballot_sync( 0xffffffffu, gone );
+            if( gm && lane == 0 ) atomicAdd( removed, __popc( gm ) );
+        }
+        const int dest = keep ? tile_of( g, nn[0], nn[1], DIM == 3 ? nn[2] : 0 ) : -1;
         // warp-aggregated slot allocation per destination tile
         const unsigned peers = __match_any_sync( 0xffffffffu, dest );
         const int leader = __ffs( peers ) - 1;
         int slot_base = 0;
-        if( valid && ( int )lane == leader ) slot_base = atomicAdd( &count_out[dest], __popc( peers ) );
+        if( keep && ( int )lane == leader ) slot_base = atomicAdd( &count_out[dest], __popc( peers ) );
         slot_base = __shfl_sync( 0xffffffffu, slot_base, leader );
-        if( valid ) {
+        if( keep ) {
             const int slot = slot_base + __popc( peers & ( ( 1u << lane ) - 1u ) );
             PBuf<MIXED> dst = out;
             int64_t o;
@@ -1118,6 +1144,143 @@ __device__ __forceinline__ int canon( int i, int nd, int N ) { return i == 0 ? N
 // outermost dual layers take their periodic image's update, which is what the
 // reference's B exchange copies there), fused with the B_m centring
 // (ElectroMagn3D::centerMagneticFields, ElectroMagn3D.cpp:1191): B_m = (B_new + B_old)/2.
+// ---- open boundaries (2D) ---------------------------------------------------
+
+// Faraday on a 2D grid with open axes (MF_Solver2D_Yee::operator(),
+// MF_Solver2D_Yee.cpp:18-140): along an open axis only interior points are
+// updated (the boundary layer is left to the Silver-Mueller condition); along a
+// periodic one every point is, the outermost dual layer from its periodic image.
+// B_m receives the old B everywhere (saveMagneticFields).  One thread per point
+// of the (nxd x nyd) box.
+template <class T>
+__global__ void k_faraday_open2d( GridInfo g, Fields<T> f, T dtdx, T dtdy )
+{
+    const int nxp = g.np[0], nyp = g.np[1], nxd = nxp + 1, nyd = nyp + 1;
+    const int64_t t = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x;
+    if( t >= ( int64_t )nxd * nyd ) return;
+    const int x = ( int )( t / nyd ), y = ( int )( t % nyd );
+    const int lox = g.open[0] ? 1 : 0, hix = g.open[0] ? nxd - 1 : nxd;
+    const int loy = g.open[1] ? 1 : 0, hiy = g.open[1] ? nyd - 1 : nyd;
+    const int xc = g.open[0] ? x : canon( x, nxd, g.N[0] ), yc = g.open[1] ? y : canon( y, nyd, g.N[1] );
+    const T *Ex = f.E[0], *Ey = f.E[1], *Ez = f.E[2];
+    if( x < nxp ) { // Bx (p,d)
+        const int64_t i = ( int64_t )x * nyd + y;
+        const T old = f.B[0][i];
+        f.Bm[0][i] = old;
+        if( y >= loy && y < hiy ) f.B[0][i] = old - dtdy * ( Ez[x * nyp + yc] - Ez[x * nyp + yc - 1] );
+    }
+    if( y < nyp ) { // By (d,p)
+        const int64_t i = ( int64_t )x * nyp + y;
+        const T old = f.B[1][i];
+        f.Bm[1][i] = old;
+        if( x >= lox && x < hix ) f.B[1][i] = old + dtdx * ( Ez[( int64_t )xc * nyp + y] - Ez[( int64_t )( xc - 1 ) * nyp + y] );
+    }
+    { // Bz (d,d)
+        const int64_t i = ( int64_t )x * nyd + y;
+        const T old = f.B[2][i];
+        f.Bm[2][i] = old;
+        if( x >= lox && x < hix && y >= loy && y < hiy )
+            f.B[2][i] = old + dtdy * ( Ex[( int64_t )x * nyp + yc] - Ex[( int64_t )x * nyp + yc - 1] )
+                        - dtdx * ( Ey[( int64_t )xc * nyd + y] - Ey[( int64_t )( xc - 1 ) * nyd + y] );
+    }
+}
+
+// Gaussian 2D laser on xmin, in the terms of the reference's LaserGaussian2D
+// (pyprofiles.py:507-569, transformPolarization :458-468), time envelope tgaussian
+// (Function.cpp:528-535); amplitude of LaserProfileSeparable::getAmplitude
+// (Laser.cpp:453-460).  FP64.
+struct LaserG2 {
+    double omega, fy, invWaist2, coeff, sqrtw, amp[2], delay[2], phase_offset;
+    double t_start, t_end, t_center, t_invsigma, t_order;
+};
+
+__device__ inline double laser_amp( const LaserG2 &L, int profile, double y, double t )
+{
+    const double dy = y - L.fy;
+    const double S = L.amp[profile] * L.sqrtw * exp( -L.invWaist2 * dy * dy );
+    const double phi = L.coeff * dy * dy - L.phase_offset + L.delay[profile == 0 ? 1 : 0];
+    const double tt = t - ( phi + L.delay[profile] ) / L.omega;
+    const double env = ( tt < L.t_start || tt > L.t_end ) ? 0.0 : exp( -pow( tt - L.t_center, L.t_order ) * L.t_invsigma );
+    return env * S * sin( L.omega * t - phi );
+}
+
+constexpr int MAX_LASERS = 4;
+struct OpenBC {
+    double coef[4][5];      // Silver-Mueller Alpha..Epsilon per side (xmin, xmax, ymin, ymax)
+    int nlaser;             // lasers on xmin
+    LaserG2 laser[MAX_LASERS];
+};
+
+// Silver-Mueller on every open side of a 2D grid (ElectroMagnBC2D_SM::apply,
+// ElectroMagnBC2D_SM.cpp:118-265, no external fields), the lasers on xmin at
+// time_dual = (step + 1.5) dt.  The four sides write disjoint points and read
+// no point another side writes, so one launch covers them: blockIdx.y = side.
+template <class T>
+__global__ void k_silver_mueller2d( GridInfo g, Fields<T> f, OpenBC bc, const int64_t *__restrict__ step )
+{
+    const int side = blockIdx.y, ax = side / 2, tan = ax == 0 ? 1 : 0;
+    if( !g.open[ax] ) return;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nxp = g.np[0], nyp = g.np[1], nyd = nyp + 1;
+    const int mx = side % 2, sgn = mx ? 1 : -1;
+    const int np0 = g.np[ax], nd0 = np0 + 1;
+    int iB[3];
+    if( !mx ) {
+        iB[0] = iB[1] = iB[2] = 0;
+    } else {
+        iB[ax] = np0 - 1;
+        iB[tan] = nd0 - 1;
+        iB[2] = nd0 - 1;
+    }
+    const int p0 = iB[0] - sgn, p1 = iB[1] - sgn, p2 = iB[2] - sgn;
+    const int tmin = g.open[tan], tmax = g.open[tan];
+    const int n1p = g.np[tan], n1d = n1p + 1;
+    const double Al = bc.coef[side][0], Be = bc.coef[side][1], Ga = bc.coef[side][2], De = bc.coef[side][3],
+                 Ep = bc.coef[side][4];
+    const double t = ( ( double )*step + 1.5 ) * g.dt;
+    const T *Ex = f.E[0], *Ey = f.E[1], *Ez = f.E[2];
+    T *Bx = f.B[0], *By = f.B[1], *Bz = f.B[2];
+    if( j >= tmin && j < n1p - tmax ) {
+        double b1 = 0.0;
+        if( side == 0 )
+            for( int k = 0; k < bc.nlaser; k++ ) b1 += laser_amp( bc.laser[k], 0, ( j - OS ) * g.dx[1], t );
+        if( ax == 0 )
+            By[( int64_t )iB[1] * nyp + j] = ( T )( Al * Ez[( int64_t )iB[0] * nyp + j] + Be * By[( int64_t )p1 * nyp + j] + Ga * b1
+                                                    + De * Bx[( int64_t )iB[0] * nyd + j + 1] + Ep * Bx[( int64_t )iB[0] * nyd + j] );
+        else
+            Bx[iB[0] + ( int64_t )nyd * j] = ( T )( -Al * Ez[iB[1] + ( int64_t )nyp * j] + Be * Bx[p0 + ( int64_t )nyd * j] + Ga * b1
+                                                     + De * By[iB[1] + ( int64_t )nyp * ( j + 1 )] + Ep * By[iB[1] + ( int64_t )nyp * j] );
+    }
+    if( j >= tmin && j < n1d - tmax ) {
+        double b2 = 0.0;
+        if( side == 0 )
+            for( int k = 0; k < bc.nlaser; k++ ) b2 += laser_amp( bc.laser[k], 1, ( j - 0.5 - OS ) * g.dx[1], t );
+        if( ax == 0 )
+            Bz[( int64_t )iB[2] * nyd + j] = ( T )( -Al * Ey[( int64_t )iB[0] * nyd + j] + Be * Bz[( int64_t )p2 * nyd + j] + Ga * b2 );
+        else
+            Bz[( int64_t )j * nyd + iB[2]] = ( T )( Al * Ex[( int64_t )j * nyp + iB[1]] + Be * Bz[( int64_t )j * nyd + p2] + Ga * b2 );
+    }
+    ( void )nxp;
+}
+
+// B_m <- (B + B_m)/2 on every point (centerMagneticFields); block 0 advances the
+// step counter the boundary lasers read.
+template <class T>
+__global__ void k_center_b2d( GridInfo g, Fields<T> f, int64_t *__restrict__ step )
+{
+    const int nxp = g.np[0], nyp = g.np[1], nxd = nxp + 1, nyd = nyp + 1;
+    const int64_t t = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x;
+    if( t == 0 ) *step += 1;
+    if( t >= ( int64_t )nxd * nyd ) return;
+    const int x = ( int )( t / nyd ), y = ( int )( t % nyd );
+    if( x < nxp ) f.Bm[0][t] = ( f.B[0][t] + f.Bm[0][t] ) * T( 0.5 );
+    if( y < nyp ) {
+        const int64_t i = ( int64_t )x * nyp + y;
+        f.Bm[1][i] = ( f.B[1][i] + f.Bm[1][i] ) * T( 0.5 );
+    }
+    f.Bm[2][t] = ( f.B[2][t] + f.Bm[2][t] ) * T( 0.5 );
+}
+
 template <int DIM, class T>
 __global__ void k_faraday_center( GridInfo g, Fields<T> f, T dtdx, T dtdy, T dtdz )
 {
@@ -1206,14 +1369,21 @@ __global__ void k_stage( GridInfo g, int64_t n, const double *__restrict__ pos, 
 #pragma unroll
     for( int d = 0; d < DIM; d++ ) {
         double x = pos[d * n + p];
-        if( x < 0.0 ) x += g.L[d];
-        if( x >= g.L[d] ) x -= g.L[d];
+        if( !g.open[d] ) {
+            if( x < 0.0 ) x += g.L[d];
+            if( x >= g.L[d] ) x -= g.L[d];
+        }
         const double xn = x * g.dxi[d];
         int ip = round_half_away( xn );
         double dl = xn - ( double )ip;
-        if( ip >= g.N[d] ) ip -= g.N[d];
-        if( ip < 0 ) ip += g.N[d];
-        if( ip < 0 || ip >= g.N[d] ) ip = 0; // non-finite input: keep the index inside the tables
+        if( g.open[d] ) {
+            // positions on an open axis must lie in [0, L): nodes 0..N
+            if( ip < 0 || ip > g.N[d] ) ip = 0;
+        } else {
+            if( ip >= g.N[d] ) ip -= g.N[d];
+            if( ip < 0 ) ip += g.N[d];
+            if( ip < 0 || ip >= g.N[d] ) ip = 0; // non-finite input: keep the index inside the tables
+        }
         node[d] = ip;
         if constexpr( MIXED ) st.d[d][p] = ( float )dl;
         else st.x[d][p] = x;
@@ -1499,7 +1669,7 @@ struct sg_sim {
     std::vector<SpeciesState> sp;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
-    int *d_flags = nullptr; // [0] status, [1 + s] spill count of species s
+    int *d_flags = nullptr; // [0] status, [1 + s] spill count of species s, [1 + max_species + s] removed
     int *h_flags = nullptr; // pinned copy
     int max_species = 16;
     int64_t *scan_scratch = nullptr;
@@ -1512,6 +1682,8 @@ struct sg_sim {
     cudaEvent_t ev[4] = { nullptr, nullptr, nullptr, nullptr }; // step start, particles start/end, step end
     float last_ms[3] = { 0, 0, 0 };
     int launches_per_step = 0;
+    OpenBC obc{};                // Silver-Mueller coefficients and lasers (open axes)
+    int64_t *d_step = nullptr;   // steps done (device), read by the boundary lasers
     int64_t relayouts = 0;       // segment re-layouts after a spill
     int64_t spilled = 0;         // particles that went through the spill list
     size_t smem_bytes = 0;
@@ -1587,7 +1759,7 @@ int launch_particles( sg_sim *S, SpeciesState &s, cudaStream_t st )
     const int sidx = ( int )( &s - &S->sp[0] );
     kern<<<S->g.ntiles, 128, smem, st>>>( S->g, field_view<T>( S ), sp, bin, bout, s.seg_start, s.cap, s.count[in],
                                           s.count[out], bov, s.ovf_tile, S->d_flags + 1 + sidx, ( int )s.ovf_capacity,
-                                          S->d_flags, chunk );
+                                          S->d_flags, chunk, S->d_flags + 1 + S->max_species + sidx );
     SG_LAUNCH_CHECK( "k_step_particles" );
     return SG_OK;
 }
@@ -1612,6 +1784,7 @@ int launch_fields( sg_sim *S, cudaStream_t st, int &launches )
     Fields<T> f = field_view<T>( S );
     const GridInfo &g = S->g;
     for( int d = 0; d < DIM; d++ ) {
+        if( g.open[d] ) continue; // ghost currents at an open boundary are not folded
         int64_t slab = 6;
         for( int k = 0; k < DIM; k++ )
             if( k != d ) slab *= g.np[k] + 1;
@@ -1625,6 +1798,19 @@ int launch_fields( sg_sim *S, cudaStream_t st, int &launches )
     const int tpb = DIM == 3 ? ( g.np[2] + 1 <= 128 ? 128 : 256 ) : 256;
     k_ampere_all<DIM, T><<<rows, tpb, 0, st>>>( g, f, dt, dtdx, dtdy, dtdz );
     SG_LAUNCH_CHECK( "k_ampere_all" );
+    if( DIM == 2 && ( g.open[0] || g.open[1] ) ) {
+        const int64_t pts = ( int64_t )( g.np[0] + 1 ) * ( g.np[1] + 1 );
+        const unsigned blocks = ( unsigned )( ( pts + 255 ) / 256 );
+        k_faraday_open2d<T><<<blocks, 256, 0, st>>>( g, f, dtdx, dtdy );
+        SG_LAUNCH_CHECK( "k_faraday_open2d" );
+        const int nside = std::max( g.np[0], g.np[1] ) + 1;
+        k_silver_mueller2d<T><<<dim3( ( nside + 127 ) / 128, 4 ), 128, 0, st>>>( g, f, S->obc, S->d_step );
+        SG_LAUNCH_CHECK( "k_silver_mueller2d" );
+        k_center_b2d<T><<<blocks, 256, 0, st>>>( g, f, S->d_step );
+        SG_LAUNCH_CHECK( "k_center_b2d" );
+        launches += 4;
+        return SG_OK;
+    }
     k_faraday_center<DIM, T><<<rows, tpb, 0, st>>>( g, f, dtdx, dtdy, dtdz );
     SG_LAUNCH_CHECK( "k_faraday_center" );
     launches += 2;
@@ -1637,7 +1823,7 @@ int enqueue_step( sg_sim *S, cudaStream_t st )
     int launches = 0;
     SG_CUDA_TRY( cudaEventRecordWithFlags( S->ev[3], st, cudaEventRecordExternal ) );
     for( int c = 9; c < 12; c++ ) SG_CUDA_TRY( cudaMemsetAsync( S->fptr[c], 0, S->fsize[c] * S->esz, st ) );
-    SG_CUDA_TRY( cudaMemsetAsync( S->d_flags, 0, ( 1 + S->sp.size() ) * sizeof( int ), st ) );
+    SG_CUDA_TRY( cudaMemsetAsync( S->d_flags, 0, ( 1 + 2 * S->max_species ) * sizeof( int ), st ) );
     for( auto &s : S->sp ) SG_CUDA_TRY( cudaMemsetAsync( s.count[1 - s.cur], 0, S->g.ntiles * sizeof( int ), st ) );
     SG_CUDA_TRY( cudaEventRecordWithFlags( S->ev[0], st, cudaEventRecordExternal ) );
     for( auto &s : S->sp ) {
@@ -1651,7 +1837,7 @@ int enqueue_step( sg_sim *S, cudaStream_t st )
     else r = S->mixed ? launch_fields<2, float>( S, st, launches ) : launch_fields<2, double>( S, st, launches );
     if( r ) return r;
     SG_CUDA_TRY( cudaEventRecordWithFlags( S->ev[2], st, cudaEventRecordExternal ) );
-    SG_CUDA_TRY( cudaMemcpyAsync( S->h_flags, S->d_flags, ( 1 + S->sp.size() ) * sizeof( int ), cudaMemcpyDeviceToHost, st ) );
+    SG_CUDA_TRY( cudaMemcpyAsync( S->h_flags, S->d_flags, ( 1 + 2 * S->max_species ) * sizeof( int ), cudaMemcpyDeviceToHost, st ) );
     S->launches_per_step = launches;
     return SG_OK;
 }
@@ -1789,7 +1975,8 @@ int choose_tiles( sg_sim *S )
         }
         if( g.N[d] % t ) return set_error( SG_ERR_ARG, "tile size %d does not divide %d cells in dimension %d", t, g.N[d], d );
         g.T[d] = t;
-        g.nt[d] = g.N[d] / t;
+        // an open axis has N + 1 nodes (a particle in [L - dx/2, L) is nearest to node N): one more tile
+        g.nt[d] = g.N[d] / t + g.open[d];
         g.tshift[d] = ( t & ( t - 1 ) ) == 0 ? __builtin_ctz( ( unsigned )t ) : -1;
     }
     g.ntiles = g.nt[0] * g.nt[1] * ( g.ndim == 3 ? g.nt[2] : 1 );
@@ -1814,7 +2001,10 @@ int sg_sim_create( const sg_sim_config *cfg, sg_sim **out )
         SG_REQUIRE( cfg->n_cells[d] >= 8, "at least 8 cells per dimension are needed (dimension %d has %d)", d, cfg->n_cells[d] );
         SG_REQUIRE( cfg->cell_length[d] > 0.0, "cell_length[%d] must be positive", d );
         if( cfg->form == SG_FORM_MIXED )
-            SG_REQUIRE( cfg->n_cells[d] <= ( cfg->ndim == 3 ? ( d == 0 ? 2048 : 1024 ) : 65536 ), "mixed form: too many cells in dimension %d", d );
+            SG_REQUIRE( cfg->n_cells[d] + ( cfg->bc[d] == SG_BC_OPEN ) <= ( cfg->ndim == 3 ? ( d == 0 ? 2048 : 1024 ) : 65536 ),
+                        "mixed form: too many cells in dimension %d", d );
+        SG_REQUIRE( cfg->bc[d] == SG_BC_PERIODIC || cfg->bc[d] == SG_BC_OPEN, "unknown boundary %d in dimension %d", cfg->bc[d], d );
+        SG_REQUIRE( cfg->bc[d] == SG_BC_PERIODIC || cfg->ndim == 2, "open boundaries are implemented in 2D" );
         SG_REQUIRE( cfg->dt < cfg->cell_length[d], "dt must be below every cell length (a particle may cross at most one cell per step)" );
     }
     sg_sim *S = new sg_sim();
@@ -1825,6 +2015,7 @@ int sg_sim_create( const sg_sim_config *cfg, sg_sim **out )
     g.ndim = cfg->ndim;
     g.dt = cfg->dt;
     for( int d = 0; d < 3; d++ ) {
+        g.open[d] = d < g.ndim && cfg->bc[d] == SG_BC_OPEN ? 1 : 0;
         g.N[d] = d < g.ndim ? cfg->n_cells[d] : 1;
         g.np[d] = d < g.ndim ? g.N[d] + 1 + 2 * OS : 1;
         g.dx[d] = d < g.ndim ? cfg->cell_length[d] : 1.0;
@@ -1833,6 +2024,22 @@ int sg_sim_create( const sg_sim_config *cfg, sg_sim **out )
     }
     int r = choose_tiles( S );
     if( r ) { delete S; return r; }
+    // Silver-Mueller coefficients (ElectroMagnBC2D_SM constructor, ElectroMagnBC2D_SM.cpp:18-66)
+    // with the default incoming directions +x, -x, +y, -y (Params.cpp:476-493)
+    for( int side = 0; side < 4 && g.ndim == 2; side++ ) {
+        const int a0 = side / 2, a1 = a0 == 0 ? 1 : 0;
+        const double sgn = ( double )( side % 2 ) * 2.0 - 1.0;
+        const double k[2] = { a0 == 0 ? -sgn : 0.0, a0 == 1 ? -sgn : 0.0 };
+        const double k0 = k[a0], k1 = k[a1];
+        const double dt0 = g.dt / g.dx[a0], dt1 = g.dt / g.dx[a1];
+        const double factor = 1.0 / ( k0 - sgn * dt0 );
+        double *c = S->obc.coef[side];
+        c[0] = 2.0 * factor;
+        c[1] = -( k0 + sgn * dt0 ) * factor;
+        c[2] = 4.0 * k0 * factor;
+        c[3] = -( k1 + dt1 ) * factor;
+        c[4] = -( k1 - dt1 ) * factor;
+    }
     // fields
     size_t total = 0;
     for( int c = 0; c < 12; c++ ) {
@@ -1860,8 +2067,10 @@ int sg_sim_create( const sg_sim_config *cfg, sg_sim **out )
             p += ( ( S->fsize[c] * S->esz + 255 ) / 256 ) * 256;
         }
     const int nt = g.ntiles;
-    e = cudaMalloc( &S->d_flags, ( 1 + S->max_species ) * sizeof( int ) );
-    if( e == cudaSuccess ) e = cudaMallocHost( &S->h_flags, ( 1 + S->max_species ) * sizeof( int ) );
+    e = cudaMalloc( &S->d_step, sizeof( int64_t ) );
+    if( e == cudaSuccess ) e = cudaMemset( S->d_step, 0, sizeof( int64_t ) );
+    if( e == cudaSuccess ) e = cudaMalloc( &S->d_flags, ( 1 + 2 * S->max_species ) * sizeof( int ) );
+    if( e == cudaSuccess ) e = cudaMallocHost( &S->h_flags, ( 1 + 2 * S->max_species ) * sizeof( int ) );
     if( e == cudaSuccess ) e = cudaMalloc( &S->scan_scratch, scan_scratch_elems( nt ) * sizeof( int64_t ) );
     if( e == cudaSuccess ) e = cudaMalloc( &S->tmp_start, nt * sizeof( int64_t ) );
     if( e == cudaSuccess ) e = cudaMalloc( &S->tmp_cap, nt * sizeof( int ) );
@@ -1895,6 +2104,7 @@ int sg_sim_destroy( sg_sim *S )
     }
     release( S->fmem );
     release( S->d_flags );
+    release( S->d_step );
     if( S->h_flags ) cudaFreeHost( S->h_flags );
     release( S->scan_scratch );
     release( S->tmp_start );
@@ -2101,6 +2311,7 @@ int sg_sim_step( sg_sim *S, int nsteps )
             return set_error( status, status == SG_ERR_BOUNDS ? "a particle moved more than one cell in a step or left its tile"
                                                               : "the spill list overflowed (capacity too small)" );
         }
+        for( size_t k = 0; k < S->sp.size(); k++ ) S->sp[k].npart -= S->h_flags[1 + S->max_species + k];
         for( size_t k = 0; k < S->sp.size(); k++ ) {
             const int nspill = S->h_flags[1 + k];
             if( nspill > 0 ) {
@@ -2111,6 +2322,44 @@ int sg_sim_step( sg_sim *S, int nsteps )
             }
         }
     }
+    return SG_OK;
+}
+
+int sg_sim_add_laser_gaussian2d( sg_sim *S, const double *p )
+{
+    SG_REQUIRE( S && p, "NULL argument" );
+    SG_REQUIRE( S->g.ndim == 2 && S->g.open[0], "a Gaussian 2D laser needs a 2D grid with an open x axis" );
+    SG_REQUIRE( S->obc.nlaser < MAX_LASERS, "at most %d lasers", MAX_LASERS );
+    const double a0 = p[0], omega = p[1], waist = p[2], fx = p[3], fy = p[4], pphi = p[5], ell = p[6];
+    SG_REQUIRE( omega > 0.0 && waist > 0.0 && p[11] > 0.0, "omega, waist and fwhm must be positive" );
+    // LaserGaussian2D (pyprofiles.py:507-569) with transformPolarization (:458-468): its
+    // [dephasing, A1, A2] is unpacked as (dephasing, amplitudeZ, amplitudeY), so the By
+    // profile takes A2 and the Bz profile A1
+    const double e2 = ell * ell;
+    const double pp = ( 1.0 - e2 ) * std::sin( 2.0 * pphi ) / 2.0;
+    const double dephasing = std::atan2( ell, pp );
+    const double amplitude = std::sqrt( 1.0 / ( 1.0 + e2 ) );
+    const double c2 = std::cos( pphi ) * std::cos( pphi ), s2 = 1.0 - c2;
+    LaserG2 L{};
+    L.omega = omega;
+    L.fy = fy;
+    L.amp[0] = amplitude * std::sqrt( s2 + e2 * c2 ) * a0 * omega;
+    L.amp[1] = amplitude * std::sqrt( c2 + e2 * s2 ) * a0 * omega;
+    L.delay[0] = 0.0;
+    L.delay[1] = dephasing;
+    L.phase_offset = p[7];
+    const double Zr = omega * waist * waist / 2.0;
+    const double w = std::sqrt( 1.0 / ( 1.0 + ( fx / Zr ) * ( fx / Zr ) ) );
+    L.invWaist2 = ( w / waist ) * ( w / waist );
+    L.coeff = -omega * fx * w * w / ( 2.0 * Zr * Zr );
+    L.sqrtw = std::sqrt( w );
+    L.t_start = p[8];
+    L.t_end = p[8] + p[9];
+    L.t_center = p[10];
+    L.t_order = p[12];
+    L.t_invsigma = 1.0 / ( std::pow( 0.5 * p[11], p[12] ) / std::log( 2.0 ) );
+    S->obc.laser[S->obc.nlaser++] = L;
+    drop_graphs( S ); // the boundary kernel takes the lasers by value
     return SG_OK;
 }
 
@@ -2608,6 +2857,7 @@ extern "C" {
 int sg_sim_get_rho( sg_sim *S, double *host )
 {
     SG_REQUIRE( S && host, "NULL argument" );
+    SG_REQUIRE( !S->g.open[0] && !S->g.open[1] && !S->g.open[2], "charge density, Poisson and residual need a periodic grid" );
     const GridInfo &g = S->g;
     const size_t n = ( size_t )ext( g, 0, 0 ) * ext( g, 1, 0 ) * ext( g, 2, 0 );
     double *rho = nullptr;
@@ -2624,6 +2874,7 @@ int sg_sim_get_rho( sg_sim *S, double *host )
 int sg_sim_solve_poisson( sg_sim *S, double max_error, int max_iter, int *iterations, double *ctrl_out )
 {
     SG_REQUIRE( S, "NULL simulation" );
+    SG_REQUIRE( !S->g.open[0] && !S->g.open[1] && !S->g.open[2], "charge density, Poisson and residual need a periodic grid" );
     SG_REQUIRE( max_iter >= 0, "max_iter < 0" );
     const GridInfo &g = S->g;
     cudaStream_t st = S->stream;
@@ -2687,6 +2938,7 @@ int sg_sim_solve_poisson( sg_sim *S, double max_error, int max_iter, int *iterat
 int sg_sim_charge_residual( sg_sim *S, double *residual, double *rho_max )
 {
     SG_REQUIRE( S && residual, "NULL argument" );
+    SG_REQUIRE( !S->g.open[0] && !S->g.open[1] && !S->g.open[2], "charge density, Poisson and residual need a periodic grid" );
     const GridInfo &g = S->g;
     cudaStream_t st = S->stream;
     const int64_t n = phys_nodes( g );

@@ -18,7 +18,10 @@ FIELD_INDEX = {"Ex": 0, "Ey": 1, "Ez": 2, "Bx": 3, "By": 4, "Bz": 5, "Bx_m": 6, 
 
 
 class Simulation:
-    def __init__(self, n_cells, cell_length, dt, form="mixed", tile=None, capacity_slack=0.25, use_graph=True):
+    def __init__(self, n_cells, cell_length, dt, form="mixed", tile=None, capacity_slack=0.25, use_graph=True,
+                 boundaries=None):
+        """boundaries: per dimension "periodic" (default) or "open" (2D: Silver-Mueller fields,
+        particles removed when they leave)."""
         self.ndim = len(n_cells)
         self.n_cells = [int(n) for n in n_cells]
         self.cell_length = [float(c) for c in cell_length]
@@ -34,6 +37,9 @@ class Simulation:
         cfg.dt = self.dt
         cfg.capacity_slack = float(capacity_slack)
         cfg.use_graph = int(bool(use_graph))
+        self.boundaries = list(boundaries) if boundaries else ["periodic"] * self.ndim
+        for d, b in enumerate(self.boundaries):
+            cfg.bc[d] = {"periodic": _lib.BC_PERIODIC, "open": _lib.BC_OPEN}[b]
         h = ctypes.c_void_p()
         check(_lib.lib().sg_sim_create(ctypes.byref(cfg), ctypes.byref(h)), "sg_sim_create")
         self._h = h
@@ -158,6 +164,21 @@ class Simulation:
         r, m = ctypes.c_double(), ctypes.c_double()
         check(_lib.lib().sg_sim_charge_residual(self._h, ctypes.byref(r), ctypes.byref(m)), "charge_residual")
         return r.value
+
+    LASER_KEYS = ["a0", "omega", "waist", "focus_x", "focus_y", "polarization_phi", "ellipticity", "phase_offset",
+                  "t_start", "t_duration", "t_center", "t_fwhm", "t_order"]
+
+    def add_laser_gaussian2d(self, a0, waist, focus, t_fwhm, t_center=None, t_start=0.0, t_duration=1e300,
+                             omega=1.0, polarization_phi=0.0, ellipticity=0.0, phase_offset=0.0, t_order=2.0):
+        """Gaussian 2D laser entering through xmin (the reference's LaserGaussian2D with a
+        tgaussian time envelope; t_center defaults to sqrt(2) * t_fwhm as in its LWFA example)."""
+        vals = dict(a0=a0, omega=omega, waist=waist, focus_x=focus[0], focus_y=focus[1],
+                    polarization_phi=polarization_phi, ellipticity=ellipticity, phase_offset=phase_offset,
+                    t_start=t_start, t_duration=t_duration, t_center=t_center if t_center is not None else 2 ** 0.5 * t_fwhm,
+                    t_fwhm=t_fwhm, t_order=t_order)
+        a = np.array([float(vals[k]) for k in self.LASER_KEYS])
+        check(_lib.lib().sg_sim_add_laser_gaussian2d(self._h, a.ctypes.data), "add_laser_gaussian2d")
+        return vals
 
     def layout_stats(self):
         """(segment re-layouts so far, particles that went through the spill list)."""
