@@ -145,17 +145,35 @@ struct MlpView {
 
 __host__ __device__ inline int mlp_nparams( int H ) { return H * H + 5 * H + 1; }
 
-// Forward pass of one sample; optional activations out.
+// Activation of the inference paths: the hardware tanh approximation (relative error
+// below 2^-10, far under the network's own error against the table).  Training uses
+// tanhf, whose derivative 1 - h^2 the back-propagation relies on.
+__device__ __forceinline__ float tanh_fast( float x )
+{
+    float y;
+    asm( "tanh.approx.f32 %0, %1;" : "=f"( y ) : "f"( x ) );
+    return y;
+}
+
+template <bool FAST>
+__device__ __forceinline__ float act( float x )
+{
+    if constexpr( FAST ) return tanh_fast( x );
+    else return tanhf( x );
+}
+
+// Forward pass of one sample; optional activations out.  FAST: inference activation.
+template <bool FAST = false>
 __device__ __forceinline__ float mlp_forward( const MlpView &m, float u0, float u1, float *h1, float *h2 )
 {
     const int H = m.H;
-    for( int i = 0; i < H; i++ ) h1[i] = tanhf( m.W1[2 * i] * u0 + m.W1[2 * i + 1] * u1 + m.b1[i] );
+    for( int i = 0; i < H; i++ ) h1[i] = act<FAST>( m.W1[2 * i] * u0 + m.W1[2 * i + 1] * u1 + m.b1[i] );
     float y = m.b3[0];
     for( int i = 0; i < H; i++ ) {
         float a = m.b2[i];
         const float *w = m.W2 + i * H;
         for( int j = 0; j < H; j++ ) a = fmaf( w[j], h1[j], a );
-        h2[i] = tanhf( a );
+        h2[i] = act<FAST>( a );
         y = fmaf( m.W3[i], h2[i], y );
     }
     return y;
@@ -172,8 +190,8 @@ __device__ double mlp_photon_chi( const MlpView &m, double chi, double xi )
     float h1[MLP_MAX_H], h2[MLP_MAX_H];
     float u0, u1;
     mlp_inputs( m, chi, xi, u0, u1 );
-    const float y = mlp_forward( m, u0, u1, h1, h2 );
-    return chi * pow( 10.0, ( double )( y * m.out_scale ) );
+    const float y = mlp_forward<true>( m, u0, u1, h1, h2 );
+    return chi * ( double )exp10f( y * m.out_scale );
 }
 
 __device__ __forceinline__ bool mlp_masked( const MlpView &m, double chi, double xi )
@@ -205,6 +223,52 @@ __global__ void k_mlp_photon_chi( MlpView m, int64_t n, const double *__restrict
 {
     const int64_t i = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x;
     if( i < n ) out[i] = mlp_photon_chi( m, chi[i], xi[i] );
+}
+
+// Batched inference for a compile-time width: the parameters are staged once per
+// block in shared memory (every thread reads the same weight: broadcasts), the
+// hidden activations stay in registers, and the output power is taken in FP32
+// (FP64 is slow on this GPU; the network's own error is far above FP32 rounding).
+template <int H>
+__global__ void __launch_bounds__( 256 ) k_mlp_photon_chi_fast( MlpView m, int64_t n, const double *__restrict__ chi,
+                                                                const double *__restrict__ xi, double *__restrict__ out )
+{
+    __shared__ float sW1[2 * H], sb1[H], sb2[H], sW3[H], sb3;
+    __shared__ float4 sW2v[H * H / 4]; // row r, columns 4c..4c+3 at r * H / 4 + c
+    float *sW2 = reinterpret_cast<float *>( sW2v );
+    for( int k = threadIdx.x; k < H * H; k += blockDim.x ) sW2[k] = m.W2[k];
+    for( int k = threadIdx.x; k < H; k += blockDim.x ) {
+        sW1[2 * k] = m.W1[2 * k];
+        sW1[2 * k + 1] = m.W1[2 * k + 1];
+        sb1[k] = m.b1[k];
+        sb2[k] = m.b2[k];
+        sW3[k] = m.W3[k];
+    }
+    if( threadIdx.x == 0 ) sb3 = m.b3[0];
+    __syncthreads();
+    for( int64_t i = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x; i < n; i += ( int64_t )gridDim.x * blockDim.x ) {
+        const float c = ( float )chi[i];
+        const float u0 = 2.0f * ( log10f( c ) - m.lmin ) / m.lspan - 1.0f;
+        const float u1 = 2.0f * ( float )xi[i] - 1.0f;
+        float h1[H];
+#pragma unroll
+        for( int k = 0; k < H; k++ ) h1[k] = tanh_fast( fmaf( sW1[2 * k], u0, fmaf( sW1[2 * k + 1], u1, sb1[k] ) ) );
+        float y = sb3;
+#pragma unroll( H >= 64 ? 1 : 2 )
+        for( int r = 0; r < H; r++ ) {
+            float a = sb2[r];
+#pragma unroll
+            for( int c = 0; c < H / 4; c++ ) {
+                const float4 wv = sW2v[r * ( H / 4 ) + c];
+                a = fmaf( wv.x, h1[4 * c], a );
+                a = fmaf( wv.y, h1[4 * c + 1], a );
+                a = fmaf( wv.z, h1[4 * c + 2], a );
+                a = fmaf( wv.w, h1[4 * c + 3], a );
+            }
+            y = fmaf( sW3[r], tanh_fast( a ), y );
+        }
+        out[i] = chi[i] * ( double )exp10f( y * m.out_scale );
+    }
 }
 
 // RadiationMonteCarlo::operator() per particle (see the file header).
@@ -708,7 +772,11 @@ int sg_mlp_photon_chi( const sg_mlp *m, int64_t n, const double *chi, const doub
 {
     SG_REQUIRE( m && chi && xi && out, "NULL argument" );
     if( n <= 0 ) return SG_OK;
-    k_mlp_photon_chi<<<grid_for( n, 128 ), 128, 0, as_stream( stream )>>>( view( m ), n, chi, xi, out );
+    const unsigned blocks = ( unsigned )std::min<int64_t>( ( n + 255 ) / 256, 152 * 8 );
+    if( m->H == 64 ) k_mlp_photon_chi_fast<64><<<blocks, 256, 0, as_stream( stream )>>>( view( m ), n, chi, xi, out );
+    else if( m->H == 32 ) k_mlp_photon_chi_fast<32><<<blocks, 256, 0, as_stream( stream )>>>( view( m ), n, chi, xi, out );
+    else if( m->H == 16 ) k_mlp_photon_chi_fast<16><<<blocks, 256, 0, as_stream( stream )>>>( view( m ), n, chi, xi, out );
+    else k_mlp_photon_chi<<<grid_for( n, 128 ), 128, 0, as_stream( stream )>>>( view( m ), n, chi, xi, out );
     SG_LAUNCH_CHECK( "k_mlp_photon_chi" );
     return SG_OK;
 }

@@ -122,3 +122,49 @@ def test_trained_mlp_with_table_fallback(rad):
     h_mlp, _ = np.histogram(np.log10(g_mlp), bins=edges)
     assert np.abs(h_mlp - h_tab).sum() / h_tab.sum() < 0.1  # final energy spectrum
     net.close()
+
+
+def test_what_the_trained_network_gains_over_the_table(rad):
+    """The learned inverse CDF against the table it was trained on, on this GPU.
+
+    Gain 1, memory: the network's FP32 parameters are a small fraction of the table's
+    FP64 entries (and fit in a block's shared memory).  Gain 2, speed: a 32-wide network
+    evaluates 4M samples several times faster than the table, which needs two binary
+    searches and FP64 log/exp interpolation (FP64 is slow on this GPU).  Price, accuracy:
+    the network passes the 0.05-decade validation on a third or more of the (chi, xi)
+    bins (the table serves the rest), and its median deviation from the table over all
+    samples, masked bins included, is about 5 % (asserted under 8 %).  Training: Adam with
+    a step-down learning rate."""
+    radiation, T, _ = rad
+    net = radiation.PhotonChiMLP(hidden=32, seed=3)
+    for steps, lr in ((4000, 2e-3), (6000, 1e-3), (6000, 3e-4), (6000, 1e-4)):
+        net.train(T, steps=steps, batch=8192, lr=lr)
+    err, n_masked = net.validate(T, tol=0.05)
+    table_bytes = T.nbytes
+    net_bytes = net.nparams * 4
+    assert net_bytes * 50 < table_bytes, (net_bytes, table_bytes)
+    n = 1 << 22
+    rng = np.random.default_rng(11)
+    chi = cu(10.0 ** rng.uniform(-1.0, 1.0, n))
+    xi = cu(rng.uniform(0.0, 1.0, n))
+    times = {}
+    for name, fn in (("table", T.photon_chi), ("mlp", net.photon_chi)):
+        fn(chi, xi)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(10):
+            fn(chi, xi)
+        e1.record()
+        torch.cuda.synchronize()
+        times[name] = e0.elapsed_time(e1) / 10
+    ref = T.photon_chi(chi, xi)
+    got = net.photon_chi(chi, xi)
+    used = err.size - n_masked
+    assert used * 3 >= err.size, (used, err.size)
+    rel = (torch.abs(got - ref) / torch.abs(ref)).median().item()
+    assert rel < 0.08, rel
+    assert times["mlp"] * 2 <= times["table"], times
+    print(f"\nMLP inverse CDF: {net_bytes} B vs table {table_bytes} B; 4M samples: mlp {times['mlp']:.3f} ms, "
+          f"table {times['table']:.3f} ms; median rel dev {rel:.4f}; network used on {used}/{err.size} bins")
+    net.close()
