@@ -226,8 +226,6 @@ int sg_sim_charge_residual( sg_sim *sim, double *residual, double *rho_max );
 int sg_sim_state_bytes( sg_sim *sim, int species, size_t *bytes );
 int sg_sim_copy_state( sg_sim *sim, int species, void *host, int to_device );
 
-/* Device time of the last sg_sim_step call split by stage (ms): particles, fold,
- * maxwell, total; and the number of kernel launches per step. */
 /* Adds a Gaussian 2D laser injected through the Silver-Mueller condition on xmin
  * (LaserGaussian2D, src/Python/pyprofiles.py:507; ElectroMagnBC2D_SM::apply,
  * src/ElectroMagnBC/ElectroMagnBC2D_SM.cpp:118).  p = {a0, omega, waist, focus_x,
@@ -241,6 +239,37 @@ int sg_sim_add_laser_gaussian2d( sg_sim *sim, const double *params );
  * up) and the particles that went through the spill list.  No reference counterpart:
  * the reference re-sorts every step. */
 int sg_sim_layout_stats( sg_sim *sim, int64_t *relayouts, int64_t *spilled );
+
+/* Moving window (SimWindow, src/MovWindow/SimWindow.cpp:30-96; shift :98-560).  At
+ * the end of step k, when ((k + 1.5) dt - time_start) velocity_x > x_moved, the
+ * window moves shift_cells cells towards +x (the reference's patch width along x):
+ * that step skips its x boundaries; then every field moves shift_cells cells
+ * towards xmin with zeros in the fresh cells, Silver-Mueller is applied on xmin,
+ * lasers are switched off for good, particles that fall below x = 0 are removed,
+ * the rest follow the window (positions stay window-relative: the reference keeps
+ * absolute ones), the fresh cells are filled from each species' profile
+ * (sg_sim_set_species_profile), and x_moved grows by shift_cells dx.  Needs a 2D
+ * grid with an open x axis. */
+int sg_sim_set_moving_window( sg_sim *sim, double time_start, double velocity_x, int shift_cells );
+/* Cells and distance moved so far, and the number of shifts. */
+int sg_sim_window_state( sg_sim *sim, int64_t *n_moved, double *x_moved, int64_t *shifts );
+
+/* Density profile of a species for particle creation (ParticleCreator::create,
+ * src/Particles/ParticleCreator.cpp:110-345): profile = {n0, x_vacuum, x_slope1,
+ * x_plateau, x_slope2}, the reference's trapezoidal profile along x
+ * (src/Profiles/Function.cpp:291-314) evaluated at absolute cell centres; ppc = c^ndim
+ * particles per cell at regular positions (createPosition, :661-667); weight
+ * n dV / ppc (createWeight, :933-939); momenta zero when temperature == 0, else
+ * sqrt(temperature) times standard normals from a counter-based generator keyed on
+ * (seed, absolute cell, particle). */
+int sg_sim_set_species_profile( sg_sim *sim, int species, const double *profile, int ppc, double temperature,
+                                uint64_t seed );
+/* Creates the particles of the species' profile in window cells [x0_cell, x1_cell)
+ * x every cell along y (z), as the reference does for its initial plasma. */
+int sg_sim_fill_species( sg_sim *sim, int species, int x0_cell, int x1_cell );
+
+/* Device time of the last sg_sim_step call split by stage (ms): particles, fold,
+ * maxwell, total; and the number of kernel launches per step. */
 int sg_sim_last_timing( sg_sim *sim, double *ms_particles, double *ms_fields, double *ms_total, int *launches_per_step );
 
 /* Sets the stream the simulation runs on (default: a stream it creates). */

@@ -142,6 +142,8 @@ class Oracle(_Backend):
     def __init__(self):
         build()
         self.lib = ctypes.CDLL(LIB_PATH)
+        self.lib.or_window_shift_particles.restype = ctypes.c_int64
+        self.lib.or_create_particles.restype = ctypes.c_int64
 
     @staticmethod
     def _n(n):
@@ -198,10 +200,12 @@ class Oracle(_Backend):
                              _ptrs([_f64(s["weight"]) for s in species]),
                              _ptrs([np.ascontiguousarray(s["charge"], dtype=np.int16) for s in species]))
 
-    def pic_step_bc(self, n_cells, oversize, cell_length, dt, fields, species, periodic, laser=None, time_dual=0.0):
+    def pic_step_bc(self, n_cells, oversize, cell_length, dt, fields, species, periodic, laser=None, time_dual=0.0,
+                    skip_x=False):
         """2D step with open boundaries (bc_oracle.c or_pic_step_bc).  periodic: (px, py) flags;
-        laser: LASER_KEYS dict for a Gaussian laser on xmin, or None.  Species arrays are
-        replaced by their compacted survivors (pos, mom, weight, charge)."""
+        laser: LASER_KEYS dict for a Gaussian laser on xmin, or None; skip_x: the window moves
+        at the end of this step (no x boundary).  Species arrays are replaced by their
+        compacted survivors (pos, mom, weight, charge)."""
         order = ["Ex", "Ey", "Ez", "Bx", "By", "Bz", "Bx_m", "By_m", "Bz_m", "Jx", "Jy", "Jz"]
         farr = [fields[k] for k in order]
         for a in farr:
@@ -221,7 +225,7 @@ class Oracle(_Backend):
         self.lib.or_pic_step_bc(_i32(n_cells), oversize, _d(cell_length), ctypes.c_double(dt), _ptrs(farr), ns, npart,
                                 mass, pusher, _ptrs([s["pos"] for s in arrs]), _ptrs([s["mom"] for s in arrs]),
                                 _ptrs([s["weight"] for s in arrs]), _ptrs([s["charge"] for s in arrs]),
-                                _i32(list(periodic)), lz, ctypes.c_double(time_dual))
+                                _i32(list(periodic)), lz, ctypes.c_double(time_dual), int(skip_x))
         for k, s in enumerate(arrs):
             m = int(npart[k])
             nd = s["pos"].shape[0]
@@ -229,6 +233,81 @@ class Oracle(_Backend):
             s["mom"] = s["mom"].ravel()[: 3 * m].reshape(3, m).copy()
             s["weight"] = s["weight"][:m].copy()
             s["charge"] = s["charge"][:m].copy()
+
+    def window_shift(self, n_cells, oversize, cell_length, dt, fields, species, shift, periodic):
+        """The moving window's shift by ``shift`` cells (bc_oracle.c or_window_shift_fields and
+        or_window_shift_particles), then Silver-Mueller on xmin without laser, as
+        SimWindow::shift does after building its new patches (SimWindow.cpp:420-431)."""
+        order = ["Ex", "Ey", "Ez", "Bx", "By", "Bz", "Bx_m", "By_m", "Bz_m", "Jx", "Jy", "Jz"]
+        ndim = len(n_cells)
+        farr = [fields[k] for k in order]
+        for a in farr:
+            assert a.dtype == np.float64 and a.flags.c_contiguous
+        assert self.lib.or_window_shift_fields(ndim, _i32(n_cells), oversize, shift, _ptrs(farr)) == 0
+        n_prim = [n + 1 + 2 * oversize for n in n_cells]
+        self.sm_apply_2d(0, n_prim, cell_length, dt, farr[:6], tmin=int(not periodic[1]), tmax=int(not periodic[1]))
+        for s in species:
+            n = s["weight"].size
+            pos = np.ascontiguousarray(s["pos"], dtype=np.float64)
+            mom = np.ascontiguousarray(s["mom"], dtype=np.float64)
+            w = np.ascontiguousarray(s["weight"], dtype=np.float64)
+            q = np.ascontiguousarray(s["charge"], dtype=np.int16)
+            m = self.lib.or_window_shift_particles(ndim, ctypes.c_double(cell_length[0]), shift, ctypes.c_int64(n),
+                                                   _ptr(pos), _ptr(mom), _ptr(w), q.ctypes.data_as(ctypes.c_void_p))
+            s["pos"] = pos.ravel()[: ndim * m].reshape(ndim, m).copy()
+            s["mom"] = mom.ravel()[: 3 * m].reshape(3, m).copy()
+            s["weight"] = w[:m].copy()
+            s["charge"] = q[:m].copy()
+
+    def create_particles(self, n_cells, cell_length, x0, x1, n_moved, profile, ppc, temperature=0.0, seed=0):
+        """Regular-position particles in window cells [x0, x1) (bc_oracle.c or_create_particles);
+        profile = (n0, x_vacuum, x_slope1, x_plateau, x_slope2).  Returns (pos, mom, weight)."""
+        ndim = len(n_cells)
+        cap = max(1, (x1 - x0) * int(np.prod(n_cells[1:])) * ppc)
+        pos = np.zeros((ndim, cap)); mom = np.zeros((3, cap)); w = np.zeros(cap)
+        n = self.lib.or_create_particles(ndim, _i32(n_cells), _d(cell_length), x0, x1, ctypes.c_int64(n_moved),
+                                         _d(list(profile)), ppc, ctypes.c_double(temperature),
+                                         ctypes.c_uint64(seed), _ptr(pos), _ptr(mom), _ptr(w), ctypes.c_int64(cap))
+        assert n >= 0, "ppc must be a square (2D) or a cube (3D)"
+        return pos[:, :n].copy(), mom[:, :n].copy(), w[:n].copy()
+
+    def run_window(self, n_cells, cell_length, dt, fields, species, periodic, nsteps, window, laser=None,
+                   profiles=None, state=None):
+        """``nsteps`` 2D steps with open boundaries and a moving window, in the order of the
+        reference's main loop (Smilei.cpp:483-680): the step at time_dual = (k + 1.5) dt skips
+        its x boundaries when the window is due to move (SimWindow::isMoving,
+        SimWindow.cpp:93-96), then the window shifts by window["shift"] cells, lasers are
+        switched off for good (laserDisabled, SimWindow.cpp:138-145) and the fresh cells
+        are filled from each species' profile.  window = {t_start, velocity, shift};
+        profiles[s] = (profile, ppc, temperature, seed) or None; state (dict, updated)
+        carries step, n_moved, x_moved and laser_off between calls."""
+        st = state if state is not None else {}
+        st.setdefault("step", 0); st.setdefault("n_moved", 0); st.setdefault("x_moved", 0.0)
+        st.setdefault("laser_off", False)
+        P = window["shift"]
+        for _ in range(nsteps):
+            td = (st["step"] + 1.5) * dt
+            moving = (td - window["t_start"]) * window["velocity"] > st["x_moved"]
+            self.pic_step_bc(n_cells, 2, cell_length, dt, fields, species, periodic,
+                             None if st["laser_off"] else laser, td, skip_x=moving)
+            if moving:
+                st["n_moved"] += P
+                st["laser_off"] = True
+                self.window_shift(n_cells, 2, cell_length, dt, fields, species, P, periodic)
+                for s, pr in zip(species, profiles or [None] * len(species)):
+                    if pr is None:
+                        continue
+                    profile, ppc, temp, seed = pr
+                    pos, mom, w = self.create_particles(n_cells, cell_length, n_cells[0] - P, n_cells[0],
+                                                        st["n_moved"], profile, ppc, temp, seed)
+                    s["pos"] = np.concatenate([s["pos"], pos], axis=1)
+                    s["mom"] = np.concatenate([s["mom"], mom], axis=1)
+                    s["weight"] = np.concatenate([s["weight"], w])
+                    q = int(s["charge"][0]) if s["charge"].size else int(s.get("q", -1))
+                    s["charge"] = np.concatenate([s["charge"], np.full(w.size, q, np.int16)])
+                st["x_moved"] += cell_length[0] * P
+            st["step"] += 1
+        return st
 
     def sm_apply_2d(self, side, n_prim, cell_length, dt, F, b1=None, b2=None, tmin=1, tmax=1, k=None):
         """One Silver-Mueller side on F = [Ex, Ey, Ez, Bx, By, Bz] (updated in place)."""

@@ -221,12 +221,14 @@ static void fold_dims( const int *dims, const int *dual, const int *n_cells, int
 /*   sides in the order xmin, xmax, ymin, ymax (ElectroMagn::boundaryConditions, */
 /*   ElectroMagn.cpp:371-394) with the laser of `laser` (NULL: none) on xmin  */
 /*   at time_dual; B_m <- (B + B_m)/2.                                        */
+/* skip_x: the moving window shifts at the end of this step, so the x sides  */
+/*   are skipped (ElectroMagn.cpp:374, SimWindow::isMoving).                  */
 /* npart[s] is updated; the arrays of species s are compacted in place.      */
 /* ------------------------------------------------------------------------- */
 int or_pic_step_bc( const int *n_cells, int oversize, const double *cell_length, double dt, double *const *fields,
                     int nspecies, int64_t *npart, const double *mass, const int *pusher, double *const *pos,
                     double *const *mom, double *const *weight, short *const *charge, const int *periodic,
-                    const double *laser, double time_dual )
+                    const double *laser, double time_dual, int skip_x )
 {
     const int ndim = 2;
     int n_prim[3], domain_begin[3], dims[12][3];
@@ -306,7 +308,7 @@ int or_pic_step_bc( const int *n_cells, int oversize, const double *cell_length,
     static const double kdef[4][2] = { { 1.0, 0.0 }, { -1.0, 0.0 }, { 0.0, 1.0 }, { 0.0, -1.0 } };
     for( int side = 0; side < 4; side++ ) {
         const int ax = side / 2, tan = ax == 0 ? 1 : 0;
-        if( periodic[ax] ) continue;
+        if( periodic[ax] || ( ax == 0 && skip_x ) ) continue;
         double *b1 = NULL, *b2 = NULL;
         if( side == 0 && laser ) {
             const int n1p = n_prim[1], n1d = n1p + 1;
@@ -325,4 +327,157 @@ int or_pic_step_bc( const int *n_cells, int oversize, const double *cell_length,
     }
     or_center_b( &sizes[3], B, Bm );
     return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Moving window on one grid (SimWindow::shift, src/MovWindow/SimWindow.cpp:  */
+/* 98-560).  The reference drops its xmin patch and appends a fresh patch at   */
+/* xmax: fields of the fresh patch start at zero, the particles of the dropped */
+/* patch are lost, and particles keep absolute positions while the grid origin */
+/* advances by `shift` cells.  Here the grid stays put and its contents move:  */
+/* a point at window index i takes the value of point i + shift when it lies   */
+/* in front of the fresh region (position < (N - shift) dx), else 0; primal    */
+/* index i sits at (i - oversize) dx, dual at (i - oversize - 1/2) dx along x. */
+/* All 12 arrays (E, B, B_m, J) move.                                          */
+/* ------------------------------------------------------------------------- */
+int or_window_shift_fields( int ndim, const int *n_cells, int oversize, int shift, double *const *fields )
+{
+    static const int stag[12][3] = { {1,0,0}, {0,1,0}, {0,0,1}, {0,1,1}, {1,0,1}, {1,1,0},
+                                     {0,1,1}, {1,0,1}, {1,1,0}, {1,0,0}, {0,1,0}, {0,0,1} };
+    if( shift <= 0 || shift > n_cells[0] ) return -1;
+    for( int f = 0; f < 12; f++ ) {
+        int64_t dims[3];
+        for( int d = 0; d < 3; d++ ) dims[d] = d < ndim ? n_cells[d] + 1 + 2 * oversize + stag[f][d] : 1;
+        const int64_t plane = dims[1] * dims[2];
+        const int64_t keep = ( int64_t )n_cells[0] - shift + oversize + stag[f][0]; /* first index of the fresh region */
+        double *a = fields[f];
+        for( int64_t i = 0; i < dims[0]; i++ )
+            for( int64_t t = 0; t < plane; t++ )
+                a[i * plane + t] = i < keep ? a[( i + shift ) * plane + t] : 0.0;
+    }
+    return 0;
+}
+
+/* Particles of one species follow the window: x -= shift dx (the FP64 form keeps  */
+/* window positions; the reference keeps absolute ones and moves the origin), and */
+/* a particle now at x < 0 was in the dropped patch and is removed.  The arrays   */
+/* are compacted in place, order kept; returns the survivors' count.              */
+int64_t or_window_shift_particles( int ndim, double dx, int shift, int64_t n, double *pos, double *mom, double *weight,
+                                   short *charge )
+{
+    const double sx = ( double )shift * dx;
+    int64_t m = 0;
+    for( int64_t p = 0; p < n; p++ ) {
+        const double x = pos[p] - sx;
+        if( x < 0.0 ) continue;
+        pos[m] = x;
+        for( int d = 1; d < ndim; d++ ) pos[d * n + m] = pos[d * n + p];
+        for( int c = 0; c < 3; c++ ) mom[c * n + m] = mom[c * n + p];
+        weight[m] = weight[p];
+        if( charge ) charge[m] = charge[p];
+        m++;
+    }
+    for( int d = 1; d < ndim; d++ ) memmove( &pos[d * m], &pos[d * n], ( size_t )m * sizeof( double ) );
+    for( int c = 1; c < 3; c++ ) memmove( &mom[c * m], &mom[c * n], ( size_t )m * sizeof( double ) );
+    return m;
+}
+
+/* Trapezoidal profile (trapeze, src/Profiles/Function.cpp:291-310). */
+static double trapeze( double x, double plateau, double slope1, double slope2 )
+{
+    double r = 0.0;
+    if( x > 0.0 ) {
+        if( x < slope1 ) {
+            r = x / slope1;
+        } else {
+            x -= slope1 + plateau;
+            if( x < 0.0 ) {
+                r = 1.0;
+            } else {
+                x -= slope2;
+                if( x < 0.0 ) r = -x / slope2;
+            }
+        }
+    }
+    return r;
+}
+
+/* Counter-based random numbers for the momenta of created particles: the     */
+/* splitmix64 output function (Steele, Lea and Flood 2014, as published by    */
+/* Vigna) applied to a key built from (seed, absolute cell, particle, draw).   */
+/* Not the reference's generator: the reference draws from one stream per      */
+/* patch; a counter-based key makes every particle's draw independent of the   */
+/* order of creation, which is what a parallel creator needs.                  */
+static inline uint64_t mix64( uint64_t z )
+{
+    z += 0x9E3779B97F4A7C15ull;
+    z = ( z ^ ( z >> 30 ) ) * 0xBF58476D1CE4E5B9ull;
+    z = ( z ^ ( z >> 27 ) ) * 0x94D049BB133111EBull;
+    return z ^ ( z >> 31 );
+}
+
+static inline double uniform_open0( uint64_t seed, uint64_t cell, uint64_t k )
+{
+    const uint64_t h = mix64( mix64( seed ^ mix64( cell ) ) + k );
+    return ( double )( ( h >> 11 ) + 1 ) * ( 1.0 / 9007199254740992.0 ); /* (0, 1] */
+}
+
+/* Particle creation in window cells [x0, x1) x all y (x all z), regular       */
+/* positions (ParticleCreator::create and createPosition, src/Particles/        */
+/* ParticleCreator.cpp:110-345, 615-667): ppc = c^ndim particles per cell where */
+/* the density is non-zero, at x = i dx + dx 0.975 / c (0.5 + m), m the          */
+/* particle's index along x (fastest), then y, z; weight = n(x_centre) dx dy    */
+/* (dz) / ppc (createWeight, :933-939) with n evaluated at the absolute cell    */
+/* centre (n_moved + i + 1/2) dx of a trapezoidal profile in x;                  */
+/* prof = {n0, x_vacuum, x_slope1, x_plateau, x_slope2}.  Momenta: zero when     */
+/* temperature == 0, else sqrt(temperature) times standard normals (Box-Muller), */
+/* the non-relativistic limit of the reference's Maxwell-Juettner sampling.      */
+/* Cells x-major, then y, z; returns the number created (at most cap; -1 when   */
+/* cap is too small or ppc is not a power ndim).                                 */
+int64_t or_create_particles( int ndim, const int *n_cells, const double *cell_length, int x0, int x1,
+                             int64_t n_moved, const double *prof, int ppc, double temperature, uint64_t seed,
+                             double *pos, double *mom, double *weight, int64_t cap )
+{
+    int c = 1;
+    while( ( ndim == 2 ? c * c : c * c * c ) < ppc ) c++;
+    if( ( ndim == 2 ? c * c : c * c * c ) != ppc ) return -1;
+    const double invc = 1.0 / ( double )c;
+    const int ny = n_cells[1], nz = ndim == 3 ? n_cells[2] : 1;
+    double vol = 1.0;
+    for( int d = 0; d < ndim; d++ ) vol *= cell_length[d];
+    const double sq = sqrt( temperature );
+    int64_t n = 0;
+    for( int i = x0; i < x1; i++ ) {
+        const double xc = ( ( double )( n_moved + i ) + 0.5 ) * cell_length[0];
+        const double dens = prof[0] * trapeze( xc - prof[1], prof[3], prof[2], prof[4] );
+        if( !( dens > 0.0 ) ) continue;
+        const double w = dens * vol / ( double )ppc;
+        for( int j = 0; j < ny; j++ )
+            for( int k = 0; k < nz; k++ ) {
+                const int ci[3] = { i, j, k };
+                const uint64_t cell = ( ( uint64_t )( n_moved + i ) * ( uint64_t )ny + ( uint64_t )j ) * ( uint64_t )nz + ( uint64_t )k;
+                for( int p = 0; p < ppc; p++ ) {
+                    if( n >= cap ) return -1;
+                    int m = p;
+                    for( int d = 0; d < ndim; d++ ) {
+                        pos[d * cap + n] = ( double )ci[d] * cell_length[d] + cell_length[d] * 0.975 * invc * ( 0.5 + ( double )( m % c ) );
+                        m /= c;
+                    }
+                    for( int q = 0; q < 3; q++ ) mom[q * cap + n] = 0.0;
+                    if( temperature > 0.0 ) {
+                        const uint64_t base = ( uint64_t )p * 4u;
+                        const double r1 = sqrt( -2.0 * log( uniform_open0( seed, cell, base ) ) );
+                        const double a1 = 6.283185307179586 * uniform_open0( seed, cell, base + 1 );
+                        const double r2 = sqrt( -2.0 * log( uniform_open0( seed, cell, base + 2 ) ) );
+                        const double a2 = 6.283185307179586 * uniform_open0( seed, cell, base + 3 );
+                        mom[n] = sq * r1 * cos( a1 );
+                        mom[cap + n] = sq * r1 * sin( a1 );
+                        mom[2 * cap + n] = sq * r2 * cos( a2 );
+                    }
+                    weight[n] = w;
+                    n++;
+                }
+            }
+    }
+    return n;
 }

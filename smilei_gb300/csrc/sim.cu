@@ -1207,6 +1207,7 @@ __device__ inline double laser_amp( const LaserG2 &L, int profile, double y, dou
 constexpr int MAX_LASERS = 4;
 struct OpenBC {
     double coef[4][5];      // Silver-Mueller Alpha..Epsilon per side (xmin, xmax, ymin, ymax)
+    int side_mask;          // bit s: side s is applied (the x sides are skipped when the window moves)
     int nlaser;             // lasers on xmin
     LaserG2 laser[MAX_LASERS];
 };
@@ -1219,7 +1220,7 @@ template <class T>
 __global__ void k_silver_mueller2d( GridInfo g, Fields<T> f, OpenBC bc, const int64_t *__restrict__ step )
 {
     const int side = blockIdx.y, ax = side / 2, tan = ax == 0 ? 1 : 0;
-    if( !g.open[ax] ) return;
+    if( !g.open[ax] || !( ( bc.side_mask >> side ) & 1 ) ) return;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const int nxp = g.np[0], nyp = g.np[1], nyd = nyp + 1;
     const int mx = side % 2, sgn = mx ? 1 : -1;
@@ -1473,6 +1474,222 @@ __global__ void k_relayout_tiles( int ndim, int nt, const int64_t *__restrict__ 
 }
 
 // ------------------------------------------------------------------------------
+// Moving window (SimWindow::shift, src/MovWindow/SimWindow.cpp:98-560) and
+// particle creation from a density profile (ParticleCreator::create,
+// src/Particles/ParticleCreator.cpp:110-345).  The reference drops its xmin patch
+// and appends a zeroed patch at xmax, keeping absolute particle positions; here
+// the one grid keeps its place and its contents move `shift` cells towards xmin.
+// These run on the (rare) steps at which the window moves, outside the graphs.
+// ------------------------------------------------------------------------------
+
+// dst[i] = src[i + shift] for the points in front of the fresh region, 0 in it;
+// one thread per point, x the slowest index (plane = points per x index).
+template <class T>
+__global__ void k_window_shift_field( const T *__restrict__ src, T *__restrict__ dst, int64_t ex, int64_t plane,
+                                      int64_t keep, int shift )
+{
+    const int64_t n = ex * plane;
+    for( int64_t t = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x; t < n; t += ( int64_t )gridDim.x * blockDim.x ) {
+        const int64_t i = t / plane;
+        dst[t] = i < keep ? src[t + ( int64_t )shift * plane] : T( 0 );
+    }
+}
+
+// Nearest node of an FP64 position, as the initial placement computes it.
+__device__ __forceinline__ int node_fp64( const GridInfo &g, double x, int d )
+{
+    int ip = round_half_away( x * g.dxi[d] );
+    if( g.open[d] ) {
+        if( ip < 0 || ip > g.N[d] ) ip = 0;
+    } else {
+        if( ip >= g.N[d] ) ip -= g.N[d];
+        if( ip < 0 ) ip += g.N[d];
+        if( ip < 0 || ip >= g.N[d] ) ip = 0;
+    }
+    return ip;
+}
+
+// Every live particle moves `shift` cells towards xmin in place (mixed form: the
+// x node of the key, exact; FP64 form: x -= shift dx); one now at x < 0 lay in
+// the dropped cells and is removed (slot_tile = -1).  Else slot_tile = its tile,
+// counted in newcount.  shift = 0 only re-bins.  One block per tile.
+template <int DIM, bool MIXED>
+__global__ void k_window_particles( GridInfo g, const int64_t *__restrict__ seg_start, const int *__restrict__ count,
+                                    PBuf<MIXED> b, int shift, int *__restrict__ slot_tile, int *__restrict__ newcount,
+                                    unsigned long long *__restrict__ removed )
+{
+    const int t = blockIdx.x;
+    const int n = count[t];
+    const int64_t s0 = seg_start[t];
+    unsigned gone_here = 0;
+    for( int i = threadIdx.x; i < n; i += blockDim.x ) {
+        const int64_t o = s0 + i;
+        int node[3] = { 0, 0, 0 };
+        bool gone;
+        if constexpr( MIXED ) {
+            unpack_key( DIM, b.key[o], node[0], node[1], node[2] );
+            node[0] -= shift;
+            gone = node[0] < 0 || ( node[0] == 0 && b.d[0][o] < 0.0f );
+            if( !gone ) b.key[o] = pack_key( DIM, node[0], node[1], node[2] );
+        } else {
+            const double x = b.x[0][o] - ( double )shift * g.dx[0];
+            gone = x < 0.0;
+            b.x[0][o] = x;
+#pragma unroll
+            for( int d = 0; d < DIM; d++ ) node[d] = node_fp64( g, b.x[d][o], d );
+        }
+        if( gone ) {
+            slot_tile[o] = -1;
+            gone_here++;
+        } else {
+            const int nt = tile_of( g, node[0], node[1], node[2] );
+            slot_tile[o] = nt;
+            atomicAdd( &newcount[nt], 1 );
+        }
+    }
+    if( gone_here ) atomicAdd( removed, ( unsigned long long )gone_here );
+}
+
+// Survivors of k_window_particles -> next free slot of their tile in dst.
+template <bool MIXED>
+__global__ void k_window_place( int ndim, const int64_t *__restrict__ seg_start, const int *__restrict__ count,
+                                PBuf<MIXED> src, const int *__restrict__ slot_tile, const int64_t *__restrict__ new_start,
+                                int *__restrict__ fill, PBuf<MIXED> dst )
+{
+    const int t = blockIdx.x;
+    const int n = count[t];
+    const int64_t s0 = seg_start[t];
+    for( int i = threadIdx.x; i < n; i += blockDim.x ) {
+        const int64_t o = s0 + i;
+        const int nt = slot_tile[o];
+        if( nt < 0 ) continue;
+        const int slot = atomicAdd( &fill[nt], 1 );
+        copy_particle<MIXED>( src, o, dst, new_start[nt] + slot, ndim );
+    }
+}
+
+// Density profile and particle layout of created plasma.
+struct InjectParams {
+    double prof[5];      // n0, x_vacuum, x_slope1, x_plateau, x_slope2 (trapezoidal in x)
+    double vol;          // cell volume
+    double invc;         // 1 / particles per cell per dimension
+    double sqrt_temp;    // sqrt(temperature); 0: cold
+    unsigned long long seed;
+    long long n_moved;   // cells the window has moved: absolute cell = n_moved + window cell
+    int ppc, c;          // particles per cell = c^ndim
+    int x0, x1;          // window cells [x0, x1) along x, every cell along y (z)
+};
+
+// trapeze (src/Profiles/Function.cpp:291-310)
+__device__ inline double trapeze( double x, double plateau, double slope1, double slope2 )
+{
+    double r = 0.0;
+    if( x > 0.0 ) {
+        if( x < slope1 ) {
+            r = x / slope1;
+        } else {
+            x -= slope1 + plateau;
+            if( x < 0.0 ) {
+                r = 1.0;
+            } else {
+                x -= slope2;
+                if( x < 0.0 ) r = -x / slope2;
+            }
+        }
+    }
+    return r;
+}
+
+// splitmix64 output function (Steele, Lea and Flood 2014) over a key of
+// (seed, absolute cell, draw): each particle's momentum draw is independent of
+// the order in which particles are created.
+__device__ __forceinline__ unsigned long long mix64( unsigned long long z )
+{
+    z += 0x9E3779B97F4A7C15ull;
+    z = ( z ^ ( z >> 30 ) ) * 0xBF58476D1CE4E5B9ull;
+    z = ( z ^ ( z >> 27 ) ) * 0x94D049BB133111EBull;
+    return z ^ ( z >> 31 );
+}
+
+__device__ __forceinline__ double uniform_open0( unsigned long long seed, unsigned long long cell, unsigned long long k )
+{
+    const unsigned long long h = mix64( mix64( seed ^ mix64( cell ) ) + k );
+    return ( double )( ( h >> 11 ) + 1 ) * ( 1.0 / 9007199254740992.0 ); // (0, 1]
+}
+
+// One thread per cell of the region.  pass 0 counts the new particles per tile
+// (newcount, created); pass 1 writes them to the next free slots of their tiles
+// (fill, new_start) of dst.  Regular positions x = i dx + dx 0.975 / c (0.5 + m)
+// (ParticleCreator::createPosition, ParticleCreator.cpp:661-667), weight
+// n(x_centre) dV / ppc (createWeight, :933-939); rounded products and sums (no
+// contraction) so that positions and weights are those of the FP64 restatement.
+template <int DIM, bool MIXED>
+__global__ void k_inject( GridInfo g, InjectParams ip, int pass, int *__restrict__ newcount,
+                          unsigned long long *__restrict__ created, const int64_t *__restrict__ new_start,
+                          int *__restrict__ fill, PBuf<MIXED> dst )
+{
+    const int ny = g.N[1], nz = DIM == 3 ? g.N[2] : 1;
+    const int64_t ncell = ( int64_t )( ip.x1 - ip.x0 ) * ny * nz;
+    const int64_t cidx = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x;
+    if( cidx >= ncell ) return;
+    const int k = ( int )( cidx % nz ), j = ( int )( ( cidx / nz ) % ny ), i = ip.x0 + ( int )( cidx / ( ( int64_t )ny * nz ) );
+    const double xc = __dmul_rn( ( double )( ip.n_moved + i ) + 0.5, g.dx[0] );
+    const double dens = __dmul_rn( ip.prof[0], trapeze( __dadd_rn( xc, -ip.prof[1] ), ip.prof[3], ip.prof[2], ip.prof[4] ) );
+    if( !( dens > 0.0 ) ) return;
+    const double w = __dmul_rn( dens, ip.vol ) / ( double )ip.ppc;
+    const int ci[3] = { i, j, k };
+    const unsigned long long cell =
+        ( ( unsigned long long )( ip.n_moved + i ) * ( unsigned long long )ny + ( unsigned long long )j ) * ( unsigned long long )nz + ( unsigned long long )k;
+    for( int p = 0; p < ip.ppc; p++ ) {
+        double x[3] = { 0.0, 0.0, 0.0 };
+        int node[3] = { 0, 0, 0 };
+        int m = p;
+#pragma unroll
+        for( int d = 0; d < DIM; d++ ) {
+            const double off = __dmul_rn( __dmul_rn( __dmul_rn( g.dx[d], 0.975 ), ip.invc ), 0.5 + ( double )( m % ip.c ) );
+            x[d] = __dadd_rn( __dmul_rn( ( double )ci[d], g.dx[d] ), off );
+            m /= ip.c;
+            node[d] = node_fp64( g, x[d], d );
+        }
+        const int t = tile_of( g, node[0], node[1], node[2] );
+        if( pass == 0 ) {
+            atomicAdd( &newcount[t], 1 );
+            continue;
+        }
+        double pm[3] = { 0.0, 0.0, 0.0 };
+        if( ip.sqrt_temp > 0.0 ) {
+            const unsigned long long base = ( unsigned long long )p * 4ull;
+            const double r1 = sqrt( -2.0 * log( uniform_open0( ip.seed, cell, base ) ) );
+            const double a1 = 6.283185307179586 * uniform_open0( ip.seed, cell, base + 1 );
+            const double r2 = sqrt( -2.0 * log( uniform_open0( ip.seed, cell, base + 2 ) ) );
+            const double a2 = 6.283185307179586 * uniform_open0( ip.seed, cell, base + 3 );
+            pm[0] = ip.sqrt_temp * r1 * cos( a1 );
+            pm[1] = ip.sqrt_temp * r1 * sin( a1 );
+            pm[2] = ip.sqrt_temp * r2 * cos( a2 );
+        }
+        const int slot = atomicAdd( &fill[t], 1 );
+        const int64_t o = new_start[t] + slot;
+        if constexpr( MIXED ) {
+            dst.key[o] = pack_key( DIM, node[0], node[1], node[2] );
+#pragma unroll
+            for( int d = 0; d < DIM; d++ ) { // offset from the nearest node before a periodic wrap
+                const double xn = __dmul_rn( x[d], g.dxi[d] );
+                dst.d[d][o] = ( float )( xn - ( double )round_half_away( xn ) );
+            }
+        } else {
+#pragma unroll
+            for( int d = 0; d < DIM; d++ ) dst.x[d][o] = x[d];
+        }
+        using PT = typename std::conditional<MIXED, float, double>::type;
+        dst.p[0][o] = ( PT )pm[0];
+        dst.p[1][o] = ( PT )pm[1];
+        dst.p[2][o] = ( PT )pm[2];
+        dst.w[o] = ( PT )w;
+    }
+    if( pass == 0 ) atomicAdd( created, ( unsigned long long )ip.ppc );
+}
+
+// ------------------------------------------------------------------------------
 // FP64 reductions for the energy diagnostics.
 // ------------------------------------------------------------------------------
 __device__ __forceinline__ double block_sum( double v )
@@ -1616,6 +1833,8 @@ struct SpeciesState {
     PBuf<true> om{};
     int *ovf_tile = nullptr;
     int max_cap = 0; // largest tile segment of the current layout
+    bool inject = false;       // fresh window cells are filled from this profile
+    InjectParams inj{};        // its profile (x0, x1, n_moved set per call)
 };
 
 // Carves a particle SoA of `n` elements out of one allocation.
@@ -1687,6 +1906,17 @@ struct sg_sim {
     int64_t relayouts = 0;       // segment re-layouts after a spill
     int64_t spilled = 0;         // particles that went through the spill list
     size_t smem_bytes = 0;
+    int64_t hstep = 0;           // steps done (host copy)
+    // moving window (SimWindow.cpp:93-96): moves `shift` cells when (time_dual - t_start) v > x_moved
+    bool win_on = false;
+    double win_t_start = 0.0, win_velocity = 0.0, win_x_moved = 0.0;
+    int win_shift = 0;
+    int64_t win_n_moved = 0;
+    int64_t win_shifts = 0;
+    void *win_scratch = nullptr;         // one field array
+    int *slot_tile = nullptr;            // per particle slot: its tile after a shift (-1: removed)
+    int64_t slot_cap = 0;
+    unsigned long long *d_wcount = nullptr; // [0] removed, [1] created
 };
 
 namespace sg {
@@ -1821,22 +2051,26 @@ int launch_fields( sg_sim *S, cudaStream_t st, int &launches )
 int enqueue_step( sg_sim *S, cudaStream_t st )
 {
     int launches = 0;
-    SG_CUDA_TRY( cudaEventRecordWithFlags( S->ev[3], st, cudaEventRecordExternal ) );
+    // inside a capture the stage events become external event nodes; outside, plain records
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    SG_CUDA_TRY( cudaStreamIsCapturing( st, &cs ) );
+    const unsigned evflags = cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
+    SG_CUDA_TRY( cudaEventRecordWithFlags( S->ev[3], st, evflags ) );
     for( int c = 9; c < 12; c++ ) SG_CUDA_TRY( cudaMemsetAsync( S->fptr[c], 0, S->fsize[c] * S->esz, st ) );
     SG_CUDA_TRY( cudaMemsetAsync( S->d_flags, 0, ( 1 + 2 * S->max_species ) * sizeof( int ), st ) );
     for( auto &s : S->sp ) SG_CUDA_TRY( cudaMemsetAsync( s.count[1 - s.cur], 0, S->g.ntiles * sizeof( int ), st ) );
-    SG_CUDA_TRY( cudaEventRecordWithFlags( S->ev[0], st, cudaEventRecordExternal ) );
+    SG_CUDA_TRY( cudaEventRecordWithFlags( S->ev[0], st, evflags ) );
     for( auto &s : S->sp ) {
         int r = launch_particles_any( S, s, st );
         if( r ) return r;
         launches++;
     }
-    SG_CUDA_TRY( cudaEventRecordWithFlags( S->ev[1], st, cudaEventRecordExternal ) );
+    SG_CUDA_TRY( cudaEventRecordWithFlags( S->ev[1], st, evflags ) );
     int r;
     if( S->g.ndim == 3 ) r = S->mixed ? launch_fields<3, float>( S, st, launches ) : launch_fields<3, double>( S, st, launches );
     else r = S->mixed ? launch_fields<2, float>( S, st, launches ) : launch_fields<2, double>( S, st, launches );
     if( r ) return r;
-    SG_CUDA_TRY( cudaEventRecordWithFlags( S->ev[2], st, cudaEventRecordExternal ) );
+    SG_CUDA_TRY( cudaEventRecordWithFlags( S->ev[2], st, evflags ) );
     SG_CUDA_TRY( cudaMemcpyAsync( S->h_flags, S->d_flags, ( 1 + 2 * S->max_species ) * sizeof( int ), cudaMemcpyDeviceToHost, st ) );
     S->launches_per_step = launches;
     return SG_OK;
@@ -1962,6 +2196,145 @@ int relayout( sg_sim *S, SpeciesState &s, int nspill )
     return SG_OK;
 }
 
+// Moves species s `shift` cells towards xmin (0: none), drops what left through
+// xmin, adds the particles of its profile in window cells [x0, x1) (x0 == x1:
+// none) and lays the species out anew.  Synchronises the stream.
+int rebuild_species( sg_sim *S, SpeciesState &s, int shift, int x0, int x1 )
+{
+    const int nt = S->g.ntiles, nd = S->g.ndim;
+    cudaStream_t st = S->stream;
+    if( S->slot_cap < s.capacity ) {
+        release( S->slot_tile );
+        S->slot_tile = nullptr;
+        S->slot_cap = 0;
+        SG_CUDA_TRY( cudaMalloc( &S->slot_tile, s.capacity * sizeof( int ) ) );
+        S->slot_cap = s.capacity;
+    }
+    if( !S->d_wcount ) SG_CUDA_TRY( cudaMalloc( &S->d_wcount, 2 * sizeof( unsigned long long ) ) );
+    int *newcount = s.count[1 - s.cur];
+    SG_CUDA_TRY( cudaMemsetAsync( newcount, 0, nt * sizeof( int ), st ) );
+    SG_CUDA_TRY( cudaMemsetAsync( S->d_wcount, 0, 2 * sizeof( unsigned long long ), st ) );
+    const int *cnt = s.count[s.cur];
+    if( S->mixed ) {
+        if( nd == 3 ) k_window_particles<3, true><<<nt, 128, 0, st>>>( S->g, s.seg_start, cnt, s.bm[s.cur], shift, S->slot_tile, newcount, S->d_wcount );
+        else k_window_particles<2, true><<<nt, 128, 0, st>>>( S->g, s.seg_start, cnt, s.bm[s.cur], shift, S->slot_tile, newcount, S->d_wcount );
+    } else {
+        if( nd == 3 ) k_window_particles<3, false><<<nt, 128, 0, st>>>( S->g, s.seg_start, cnt, s.bd[s.cur], shift, S->slot_tile, newcount, S->d_wcount );
+        else k_window_particles<2, false><<<nt, 128, 0, st>>>( S->g, s.seg_start, cnt, s.bd[s.cur], shift, S->slot_tile, newcount, S->d_wcount );
+    }
+    SG_LAUNCH_CHECK( "k_window_particles" );
+    const bool inject = s.inject && x1 > x0;
+    InjectParams ip = s.inj;
+    ip.x0 = x0;
+    ip.x1 = x1;
+    ip.n_moved = ( long long )S->win_n_moved;
+    const int64_t ncell = inject ? ( int64_t )( x1 - x0 ) * S->g.N[1] * ( nd == 3 ? S->g.N[2] : 1 ) : 0;
+    const unsigned iblocks = ( unsigned )( ( ncell + 127 ) / 128 );
+    auto launch_inject = [&]( int pass, PBuf<true> dm, PBuf<false> dd ) {
+        if( S->mixed ) {
+            if( nd == 3 ) k_inject<3, true><<<iblocks, 128, 0, st>>>( S->g, ip, pass, newcount, S->d_wcount + 1, S->tmp_start, S->fill, dm );
+            else k_inject<2, true><<<iblocks, 128, 0, st>>>( S->g, ip, pass, newcount, S->d_wcount + 1, S->tmp_start, S->fill, dm );
+        } else {
+            if( nd == 3 ) k_inject<3, false><<<iblocks, 128, 0, st>>>( S->g, ip, pass, newcount, S->d_wcount + 1, S->tmp_start, S->fill, dd );
+            else k_inject<2, false><<<iblocks, 128, 0, st>>>( S->g, ip, pass, newcount, S->d_wcount + 1, S->tmp_start, S->fill, dd );
+        }
+    };
+    if( inject ) {
+        launch_inject( 0, s.bm[s.cur], s.bd[s.cur] );
+        SG_LAUNCH_CHECK( "k_inject (count)" );
+    }
+    int64_t total = 0;
+    int new_max_cap = 0;
+    int r = layout_from_counts( S, newcount, S->tmp_cap, S->tmp_start, &total, &new_max_cap ); // synchronises
+    if( r ) return r;
+    unsigned long long wc[2] = { 0, 0 };
+    SG_CUDA_TRY( cudaMemcpyAsync( wc, S->d_wcount, sizeof( wc ), cudaMemcpyDeviceToHost, st ) );
+    SG_CUDA_TRY( cudaStreamSynchronize( st ) );
+    void *old_mem[2] = { s.mem[0], s.mem[1] };
+    const PBuf<false> old_bd = s.bd[s.cur];
+    const PBuf<true> old_bm = s.bm[s.cur];
+    int dst = 1 - s.cur;
+    const bool realloc = total > s.capacity;
+    if( realloc ) {
+        r = alloc_species_buffers( S, s, total + total / 8 );
+        if( r ) return r;
+        dst = s.cur;
+    }
+    SG_CUDA_TRY( cudaMemsetAsync( S->fill, 0, nt * sizeof( int ), st ) );
+    if( S->mixed ) k_window_place<true><<<nt, 128, 0, st>>>( nd, s.seg_start, cnt, old_bm, S->slot_tile, S->tmp_start, S->fill, s.bm[dst] );
+    else k_window_place<false><<<nt, 128, 0, st>>>( nd, s.seg_start, cnt, old_bd, S->slot_tile, S->tmp_start, S->fill, s.bd[dst] );
+    SG_LAUNCH_CHECK( "k_window_place" );
+    if( inject ) {
+        launch_inject( 1, s.bm[dst], s.bd[dst] );
+        SG_LAUNCH_CHECK( "k_inject (place)" );
+    }
+    SG_CUDA_TRY( cudaMemcpyAsync( s.count[dst], S->fill, nt * sizeof( int ), cudaMemcpyDeviceToDevice, st ) );
+    SG_CUDA_TRY( cudaStreamSynchronize( st ) );
+    std::swap( s.seg_start, S->tmp_start );
+    std::swap( s.cap, S->tmp_cap );
+    s.max_cap = new_max_cap;
+    s.cur = dst;
+    s.npart += ( int64_t )wc[1] - ( int64_t )wc[0];
+    if( realloc ) {
+        release( old_mem[0] );
+        release( old_mem[1] );
+    }
+    drop_graphs( S );
+    return SG_OK;
+}
+
+// The window's shift at the end of a step (SimWindow::shift): fields move
+// `shift` cells towards xmin with zeros in the fresh cells, Silver-Mueller on
+// xmin without laser (SimWindow.cpp:420-431), lasers off for good
+// (laserDisabled, :138-145), particles follow and the fresh cells are filled.
+int window_shift( sg_sim *S )
+{
+    const int P = S->win_shift;
+    const GridInfo &g = S->g;
+    cudaStream_t st = S->stream;
+    std::vector<void *> arrays;
+    std::vector<int> stag;
+    for( int c = 0; c < 12; c++ ) {
+        arrays.push_back( S->fptr[c] );
+        stag.push_back( S->fshape[c][0] - g.np[0] );
+    }
+    for( int c = 0; c < 3; c++ )
+        if( S->ecomp[c] ) {
+            arrays.push_back( S->ecomp[c] );
+            stag.push_back( S->fshape[c][0] - g.np[0] );
+        }
+    for( size_t a = 0; a < arrays.size(); a++ ) {
+        const int c = a < 12 ? ( int )a : ( int )a - 12;
+        const int64_t ex = S->fshape[c][0], plane = S->fsize[c] / ex;
+        const int64_t keep = ( int64_t )g.N[0] - P + OS + stag[a];
+        const int64_t n = S->fsize[c];
+        const unsigned blocks = ( unsigned )std::min<int64_t>( ( n + 255 ) / 256, 152 * 16 );
+        if( S->mixed ) {
+            k_window_shift_field<float><<<blocks, 256, 0, st>>>( static_cast<const float *>( arrays[a] ), static_cast<float *>( S->win_scratch ), ex, plane, keep, P );
+        } else {
+            k_window_shift_field<double><<<blocks, 256, 0, st>>>( static_cast<const double *>( arrays[a] ), static_cast<double *>( S->win_scratch ), ex, plane, keep, P );
+        }
+        SG_LAUNCH_CHECK( "k_window_shift_field" );
+        SG_CUDA_TRY( cudaMemcpyAsync( arrays[a], S->win_scratch, n * S->esz, cudaMemcpyDeviceToDevice, st ) );
+    }
+    S->obc.nlaser = 0;
+    OpenBC xmin = S->obc;
+    xmin.side_mask = 1;
+    const int nside = std::max( g.np[0], g.np[1] ) + 1;
+    if( S->mixed ) k_silver_mueller2d<float><<<dim3( ( nside + 127 ) / 128, 4 ), 128, 0, st>>>( g, field_view<float>( S ), xmin, S->d_step );
+    else k_silver_mueller2d<double><<<dim3( ( nside + 127 ) / 128, 4 ), 128, 0, st>>>( g, field_view<double>( S ), xmin, S->d_step );
+    SG_LAUNCH_CHECK( "k_silver_mueller2d" );
+    S->win_n_moved += P;
+    for( auto &s : S->sp ) {
+        int r = rebuild_species( S, s, P, g.N[0] - P, g.N[0] );
+        if( r ) return r;
+    }
+    SG_CUDA_TRY( cudaStreamSynchronize( st ) );
+    S->win_shifts++;
+    drop_graphs( S );
+    return SG_OK;
+}
+
 int choose_tiles( sg_sim *S )
 {
     GridInfo &g = S->g;
@@ -2024,6 +2397,7 @@ int sg_sim_create( const sg_sim_config *cfg, sg_sim **out )
     }
     int r = choose_tiles( S );
     if( r ) { delete S; return r; }
+    S->obc.side_mask = 0xF;
     // Silver-Mueller coefficients (ElectroMagnBC2D_SM constructor, ElectroMagnBC2D_SM.cpp:18-66)
     // with the default incoming directions +x, -x, +y, -y (Params.cpp:476-493)
     for( int side = 0; side < 4 && g.ndim == 2; side++ ) {
@@ -2111,6 +2485,9 @@ int sg_sim_destroy( sg_sim *S )
     release( S->tmp_cap );
     release( S->fill );
     release( S->d_red );
+    release( S->win_scratch );
+    release( S->slot_tile );
+    release( S->d_wcount );
     for( int i = 0; i < 4; i++ )
         if( S->ev[i] ) cudaEventDestroy( S->ev[i] );
     if( S->own_stream && S->stream ) cudaStreamDestroy( S->stream );
@@ -2281,7 +2658,16 @@ int sg_sim_step( sg_sim *S, int nsteps )
     SG_REQUIRE( nsteps >= 0, "nsteps < 0" );
     for( int it = 0; it < nsteps; it++ ) {
         const int parity = S->sp.empty() ? 0 : S->sp[0].cur;
-        if( S->cfg.use_graph ) {
+        // the window moves at the end of this step (SimWindow::isMoving, SimWindow.cpp:93-96);
+        // the x boundaries of this step are then skipped (ElectroMagn.cpp:374)
+        const double time_dual = ( ( double )S->hstep + 1.5 ) * S->g.dt;
+        const bool moving = S->win_on && ( time_dual - S->win_t_start ) * S->win_velocity > S->win_x_moved;
+        if( moving ) {
+            S->obc.side_mask = 0xC;
+            int r = enqueue_step( S, S->stream );
+            S->obc.side_mask = 0xF;
+            if( r ) return r;
+        } else if( S->cfg.use_graph ) {
             if( S->graph_parity < 0 ) {
                 // capture both parities: the step from the current state and the one after it
                 int r = capture( S, &S->graph[0] );
@@ -2321,8 +2707,80 @@ int sg_sim_step( sg_sim *S, int nsteps )
                 if( r ) return r;
             }
         }
+        if( moving ) {
+            int r = window_shift( S );
+            if( r ) return r;
+            S->win_x_moved += S->g.dx[0] * S->win_shift;
+        }
+        S->hstep++;
     }
     return SG_OK;
+}
+
+int sg_sim_set_moving_window( sg_sim *S, double time_start, double velocity_x, int shift_cells )
+{
+    SG_REQUIRE( S, "NULL simulation" );
+    SG_REQUIRE( S->g.ndim == 2 && S->g.open[0], "the moving window needs a 2D grid with an open x axis" );
+    SG_REQUIRE( shift_cells > 0 && shift_cells < S->g.N[0], "shift_cells must be in [1, %d)", S->g.N[0] );
+    SG_REQUIRE( velocity_x >= 0.0, "velocity_x must not be negative" );
+    if( !S->win_scratch ) {
+        int64_t mx = 0;
+        for( int c = 0; c < 12; c++ ) mx = std::max( mx, S->fsize[c] );
+        SG_CUDA_TRY( cudaMalloc( &S->win_scratch, ( size_t )mx * S->esz ) );
+    }
+    S->win_on = true;
+    S->win_t_start = time_start;
+    S->win_velocity = velocity_x;
+    S->win_shift = shift_cells;
+    return SG_OK;
+}
+
+int sg_sim_window_state( sg_sim *S, int64_t *n_moved, double *x_moved, int64_t *shifts )
+{
+    SG_REQUIRE( S, "NULL simulation" );
+    if( n_moved ) *n_moved = S->win_n_moved;
+    if( x_moved ) *x_moved = S->win_x_moved;
+    if( shifts ) *shifts = S->win_shifts;
+    return SG_OK;
+}
+
+int sg_sim_set_species_profile( sg_sim *S, int species, const double *profile, int ppc, double temperature,
+                                uint64_t seed )
+{
+    SG_REQUIRE( S && profile, "NULL argument" );
+    SG_REQUIRE( species >= 0 && species < ( int )S->sp.size(), "species %d out of range", species );
+    const int nd = S->g.ndim;
+    int c = 1;
+    while( ( nd == 2 ? c * c : c * c * c ) < ppc ) c++;
+    SG_REQUIRE( ppc > 0 && ( nd == 2 ? c * c : c * c * c ) == ppc,
+                "regular positions need ppc = c^%d particles per cell (got %d)", nd, ppc );
+    SG_REQUIRE( temperature >= 0.0, "temperature must not be negative" );
+    SG_REQUIRE( profile[2] >= 0.0 && profile[4] >= 0.0, "slopes must not be negative" );
+    SpeciesState &s = S->sp[species];
+    InjectParams &ip = s.inj;
+    for( int k = 0; k < 5; k++ ) ip.prof[k] = profile[k];
+    double vol = 1.0;
+    for( int d = 0; d < nd; d++ ) vol *= S->g.dx[d];
+    ip.vol = vol;
+    ip.ppc = ppc;
+    ip.c = c;
+    ip.invc = 1.0 / ( double )c;
+    ip.sqrt_temp = std::sqrt( temperature );
+    ip.seed = ( unsigned long long )seed;
+    s.inject = true;
+    return SG_OK;
+}
+
+int sg_sim_fill_species( sg_sim *S, int species, int x0_cell, int x1_cell )
+{
+    SG_REQUIRE( S, "NULL simulation" );
+    SG_REQUIRE( species >= 0 && species < ( int )S->sp.size(), "species %d out of range", species );
+    SpeciesState &s = S->sp[species];
+    SG_REQUIRE( s.inject, "species %d has no profile (sg_sim_set_species_profile)", species );
+    SG_REQUIRE( 0 <= x0_cell && x0_cell <= x1_cell && x1_cell <= S->g.N[0], "cells [%d, %d) out of [0, %d]", x0_cell,
+                x1_cell, S->g.N[0] );
+    SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
+    return rebuild_species( S, s, 0, x0_cell, x1_cell );
 }
 
 int sg_sim_add_laser_gaussian2d( sg_sim *S, const double *p )

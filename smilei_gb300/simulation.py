@@ -180,6 +180,36 @@ class Simulation:
         check(_lib.lib().sg_sim_add_laser_gaussian2d(self._h, a.ctypes.data), "add_laser_gaussian2d")
         return vals
 
+    def set_moving_window(self, time_start, velocity_x, shift_cells):
+        """The reference's MovingWindow(time_start, velocity_x) moving by ``shift_cells``
+        cells (its patch width along x) whenever (time_dual - time_start) * velocity_x
+        exceeds the distance already moved."""
+        check(_lib.lib().sg_sim_set_moving_window(self._h, float(time_start), float(velocity_x), int(shift_cells)),
+              "set_moving_window")
+
+    def window_state(self):
+        """(cells moved, distance moved, number of shifts)."""
+        n, s = ctypes.c_int64(), ctypes.c_int64()
+        x = ctypes.c_double()
+        check(_lib.lib().sg_sim_window_state(self._h, ctypes.byref(n), ctypes.byref(x), ctypes.byref(s)),
+              "window_state")
+        return n.value, x.value, s.value
+
+    def set_species_profile(self, species, n0, ppc, x_vacuum=0.0, x_slope1=0.0, x_plateau=1e300, x_slope2=0.0,
+                            temperature=0.0, seed=0):
+        """Density profile for particle creation: the reference's trapezoidal(n0, xvacuum,
+        xplateau, xslope1, xslope2) along x, ``ppc`` particles per cell at regular
+        positions.  Returns the profile tuple (n0, x_vacuum, x_slope1, x_plateau, x_slope2)."""
+        prof = np.array([n0, x_vacuum, x_slope1, x_plateau, x_slope2], dtype=np.float64)
+        check(_lib.lib().sg_sim_set_species_profile(self._h, int(species), prof.ctypes.data, int(ppc),
+                                                    float(temperature), int(seed)), "set_species_profile")
+        return tuple(float(v) for v in prof)
+
+    def fill_species(self, species, x0=0, x1=None):
+        """Creates the species' particles in window cells [x0, x1) (default: the whole grid)."""
+        x1 = self.n_cells[0] if x1 is None else x1
+        check(_lib.lib().sg_sim_fill_species(self._h, int(species), int(x0), int(x1)), "fill_species")
+
     def layout_stats(self):
         """(segment re-layouts so far, particles that went through the spill list)."""
         a, b = ctypes.c_int64(), ctypes.c_int64()
