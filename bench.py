@@ -282,6 +282,109 @@ def run_gpu(args, rank, world, local_rank):
                 tuning=tuning, relayouts=relayouts)
 
 
+LWFA = dict(n_cells=[3840, 512], cell_length=[0.1, 1.5], dt=0.095, ppc=4, pusher="vay", n0=0.003, ramp=100.0,
+            a0=2.0, waist=30.0, t_fwhm=60.0, shift=32)
+
+
+def lwfa_t_start():
+    """The window starts once the pulse has entered: 2 x its envelope centre sqrt(2) x FWHM."""
+    return 2.0 * 2 ** 0.5 * LWFA["t_fwhm"]
+
+
+def run_gpu_lwfa(args, rank, world, local_rank):
+    """2D laser wakefield with a moving window: the Gaussian pulse is injected from xmin,
+    the window starts moving at c once the pulse is in (laser then off, as in the
+    reference), and the timed steps run with the window moving and plasma injected."""
+    import torch
+    from smilei_gb300 import simulation, _lib
+    device = f"cuda:{local_rank}"
+    torch.cuda.set_device(local_rank)
+    stream = torch.cuda.Stream(device=device)
+    torch.cuda.set_stream(stream)
+    c = LWFA
+    sim = simulation.Simulation(c["n_cells"], c["cell_length"], c["dt"], form=args.form, boundaries=("open", "open"),
+                                use_graph=True)
+    _lib.check(_lib.lib().sg_sim_set_stream(sim._h, stream.cuda_stream), "set_stream")
+    ly = c["n_cells"][1] * c["cell_length"][1]
+    sim.add_laser_gaussian2d(a0=c["a0"], waist=c["waist"], focus=[0.0, ly / 2], t_fwhm=c["t_fwhm"])
+    sim.add_species(1.0, -1.0, c["pusher"], np.zeros((2, 0)), np.zeros((3, 0)), np.zeros(0))
+    sim.set_species_profile(0, c["n0"], c["ppc"], x_vacuum=0.0, x_slope1=c["ramp"])
+    sim.fill_species(0)
+    t_start = lwfa_t_start()
+    sim.set_moving_window(t_start, 1.0, c["shift"])
+    # untimed: run until the window moves, then the warm-up steps
+    pre = int(np.ceil(t_start / c["dt"])) + 1
+    sim.step(pre)
+    for _ in range(args.warmup):
+        sim.step(1)
+    torch.cuda.synchronize()
+    n0 = sim.species_count(0)
+    t_part, counts = [], []
+    with ClockSampler(local_rank) as clk:
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        wall0 = time.perf_counter()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            counts.append(sim.species_count(0))
+            sim.step(1)
+            tp, tf, tt, launches = sim.last_timing()
+            t_part.append(tp)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        wall1 = time.perf_counter()
+    ms = max_over_ranks(ev0.elapsed_time(ev1), device)
+    n_moved, x_moved, shifts = sim.window_state()
+    particle_steps = float(sum(counts))
+    sim.close()
+    ncell = int(np.prod(c["n_cells"]))
+    s_state = 52.0 if args.form == "mixed" else 88.0
+    s = 4 if args.form == "mixed" else 8
+    n_mean = particle_steps / args.steps
+    kernel_bytes = n_mean * s_state + ncell * 9 * s
+    t_kernel = float(np.mean(t_part)) / 1e3
+    peak, peak_kind = measured_peak()
+    return dict(n=int(round(n_mean)), ms=ms, value=particle_steps * world / (ms / 1e3),
+                wall_ms_per_step=(wall1 - wall0) * 1e3 / args.steps, kernel_bytes=kernel_bytes, t_kernel=t_kernel,
+                peak=peak, peak_kind=peak_kind, B_alg=s_state + 24 * s / c["ppc"], launches=launches,
+                clocks=clk.summary(), window=dict(n_moved=n_moved, x_moved=x_moved, shifts=shifts, pre_steps=pre,
+                                                  particles_at_start=n0),
+                cfg=c, energy=None, tile="default 8x8", tuning=None, relayouts=None,
+                e2e=None, e2e_note="not measured for this workload: the state size changes at every window shift")
+
+
+def run_cpu_sample_lwfa(args):
+    """The oracle's 2D open-boundary step with the moving window on a bounded sample: the
+    first 1920 x 256 cells of the workload (same cell size, density ramp, 4 ppc), window moving."""
+    import oracle
+    c = LWFA
+    n_cells = [1920, 256]
+    O = oracle.Oracle()
+    prof = (c["n0"], 0.0, c["ramp"], 1e300, 0.0)
+    pos, mom, w = O.create_particles(n_cells, c["cell_length"], 0, n_cells[0], 0, prof, c["ppc"])
+    sp = [dict(pos=pos, mom=mom, weight=w, charge=np.full(w.shape, -1, np.int16), mass=1.0, pusher="vay")]
+    from smilei_gb300 import synthetic
+    st = synthetic.STAGGER
+    fields = {k: np.zeros(tuple(n_cells[d] + 5 + st[k.replace("_m", "")][d] for d in range(2)))
+              for k in ["Ex", "Ey", "Ez", "Bx", "By", "Bz", "Bx_m", "By_m", "Bz_m", "Jx", "Jy", "Jz"]}
+    win = dict(t_start=0.0, velocity=1.0, shift=c["shift"])
+    steps = args.cpu_steps * 3
+    state = {}
+    O.run_window(n_cells, c["cell_length"], c["dt"], fields, sp, (False, False), 1, win,
+                 profiles=[(prof, c["ppc"], 0.0, 0)], state=state)
+    t0 = time.perf_counter()
+    npart = 0
+    for _ in range(steps):
+        npart += sp[0]["weight"].size
+        O.run_window(n_cells, c["cell_length"], c["dt"], fields, sp, (False, False), 1, win,
+                     profiles=[(prof, c["ppc"], 0.0, 0)], state=state)
+    t1 = time.perf_counter()
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return dict(value=npart / (t1 - t0), unit=UNIT, cores=cores, kind="port",
+                sample=f"2D wakefield sample 1920x256 cells x 4 ppc ({w.size} electrons), Vay, window moving, "
+                       f"{steps} FP64 steps of oracle/bc_oracle.c + pic_oracle.c")
+
+
 def run_cpu_sample(args, steps=None):
     """The oracle's FP64 timestep on a bounded sample of the workload (all host cores)."""
     import oracle
@@ -329,14 +432,20 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="thermal", choices=["thermal", "uneven"])
+    ap.add_argument("--workload", default="thermal", choices=["thermal", "uneven", "lwfa"])
     ap.add_argument("--autotune", action="store_true", help="pick the tile shape by timing candidates first")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-    if args.workload == "uneven":
+    if args.workload == "lwfa":
+        c = LWFA
+        workload = (f"2D laser wakefield with a moving window: {c['n_cells'][0]}x{c['n_cells'][1]} cells, dx=0.1, "
+                    f"dy=1.5, dt=0.095, Gaussian laser a0=2 waist 30 FWHM 60 from xmin, electrons n=0.003 with a "
+                    f"100-long ramp then plateau at 4 ppc (regular positions), Vay, window at c from "
+                    f"t={lwfa_t_start():.1f} moving {c['shift']} cells per shift, Silver-Mueller on all sides")
+    elif args.workload == "uneven":
         workload = ("3D uneven patches: 512x256x256 cells in 1024 patches of 32^3, particles per cell per patch "
                     "8*exp(N(0,1.5)) floored and clipped to [0,64], T=5 keV electrons, Boris, dt=0.95 CFL, periodic")
     else:
@@ -346,7 +455,7 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        r = run_cpu_sample(args)
+        r = run_cpu_sample_lwfa(args) if args.workload == "lwfa" else run_cpu_sample(args)
         line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
                 "steps": args.cpu_steps, "warmup": 1, "ms_per_step": None, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, host)",
@@ -359,11 +468,14 @@ def main():
     if world > 1:
         import torch.distributed as td
         td.init_process_group("nccl")
-    res = run_gpu(args, rank, world, local_rank)
+    if args.workload == "lwfa":
+        res = run_gpu_lwfa(args, rank, world, local_rank)
+    else:
+        res = run_gpu(args, rank, world, local_rank)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
-            cpu = run_cpu_sample(args)
+            cpu = run_cpu_sample_lwfa(args) if args.workload == "lwfa" else run_cpu_sample(args)
         except Exception as e:  # the baseline is reported, not required
             cpu = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {e}"}
     if rank != 0:
@@ -386,7 +498,8 @@ def main():
                    "hbm_fraction_of_step": step_gbs / res["peak"], "wall_ms_per_step": res["wall_ms_per_step"],
                    "energy_ukin_uelm_before_after": res["energy"], "tile": res["tile"] or "default 4x4x4",
                    "autotune_ms_per_step": res["tuning"],
-                   "relayouts_spilled_over_run": res["relayouts"]},
+                   "relayouts_spilled_over_run": res["relayouts"],
+                   **({"window": res["window"], "e2e_note": res["e2e_note"]} if "window" in res else {})},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": res["peak"], "unit": "GB/s",
                      "frac": achieved / res["peak"], "traffic": traffic, "kernel": "k_step_particles",
                      "algorithmic_bytes_per_launch": res["kernel_bytes"], "peak_source": res["peak_kind"]},
