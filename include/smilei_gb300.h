@@ -315,6 +315,33 @@ int sg_rad_monte_carlo( const sg_rad_tables *tables, const sg_mlp *mlp, int64_t 
                         const double *Epart, const double *Bpart, uint32_t seed, uint32_t first_id, uint32_t step,
                         double *radiated, unsigned long long *n_emissions, sg_stream_t stream );
 
+/* The same pass creating macro-photons (RadiationMonteCarlo.cpp:425-545), as a species
+ * with radiation_photon_species set: an emission whose photon gamma is at least
+ * gamma_threshold (radiation_photon_gamma_threshold), while the particle has made
+ * fewer than max_emissions photon groups (radiation_max_emissions) in this call,
+ * appends `sampling` photons (radiation_photon_sampling) at the particle's position
+ * (pos[d * n + i], ndim rows) with momentum photon_gamma p / |p| (p after the recoil),
+ * weight w / sampling, chi = the photon's chi and tau = -1; the energy of such an
+ * emission is not added to *radiated.  Photon k goes to ph_pos[d * photon_capacity + k],
+ * ph_mom[c * photon_capacity + k], ph_weight[k], ph_chi[k], ph_tau[k] in the order the
+ * slots are taken (atomically: not the particle order); *n_photons (device) is
+ * incremented by the number of photons wanted, and slots at or past photon_capacity are
+ * not written.  A capacity of n * max_emissions * sampling never overflows, like the
+ * reference's per-particle GPU buffers. */
+int sg_rad_monte_carlo_photons( const sg_rad_tables *tables, const sg_mlp *mlp, int ndim, int64_t n, double dt,
+                                double mass, double charge, const double *pos, double *mom, const double *weight,
+                                double *tau, double *chi_out, const double *Epart, const double *Bpart,
+                                uint32_t seed, uint32_t first_id, uint32_t step, int sampling,
+                                double gamma_threshold, int max_emissions, int64_t photon_capacity, double *ph_pos,
+                                double *ph_mom, double *ph_weight, double *ph_chi, double *ph_tau,
+                                unsigned long long *n_photons, double *radiated, unsigned long long *n_emissions,
+                                sg_stream_t stream );
+
+/* Rectilinear photon push (PusherPhoton::operator(), src/Pusher/PusherPhoton.cpp:30):
+ * invgf[i] = 1 / |p_i| (optional), pos[d * n + i] += dt p_d invgf.  Device pointers. */
+int sg_push_photons( int ndim, int64_t n, double dt, double *pos, const double *mom, double *invgf,
+                     sg_stream_t stream );
+
 /* The learned inverse CDF: an FP32 MLP 2 -> hidden -> hidden -> 1 (tanh) from
  * (log10 chi normalised to [log10_chi_min, log10_chi_max], xi) to
  * log10(photon chi / chi) / 8.  Trained on the GPU (forward, backward, batch

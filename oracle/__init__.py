@@ -497,6 +497,46 @@ def rad_photon_chi(tables: RadTables, chi, xi):
     return out
 
 
+def rad_monte_carlo_photons(tables: RadTables, dt, mass, charge, pos, mom, weight, tau, E, B, seed, first_id=0,
+                            step=0, sampling=1, threshold=2.0, max_emissions=10):
+    """Monte-Carlo pass creating macro-photons (rad_oracle.c or_rad_monte_carlo_photons).
+    Returns (radiated, n_emissions, chi, photons) with photons = dict(pos, mom, weight, chi, tau)
+    in particle order."""
+    n = mom.shape[1]
+    ndim = pos.shape[0]
+    assert mom.dtype == np.float64 and mom.flags.c_contiguous and tau.dtype == np.float64
+    chi = np.zeros(n)
+    nem, nph = ctypes.c_int64(), ctypes.c_int64()
+    cap = max(1, n * max_emissions * sampling)
+    ph_pos = np.zeros((ndim, cap)); ph_mom = np.zeros((3, cap)); ph_w = np.zeros(cap)
+    ph_chi = np.zeros(cap); ph_tau = np.zeros(cap)
+    ts = tables.c_struct()
+    L = _rad_lib()
+    L.or_rad_monte_carlo_photons.restype = ctypes.c_double
+    rad = L.or_rad_monte_carlo_photons(ctypes.byref(ts), ndim, ctypes.c_int64(n), ctypes.c_double(dt),
+                                       ctypes.c_double(mass), ctypes.c_double(charge), _ptr(_f64(pos)), _ptr(mom),
+                                       _ptr(_f64(weight)), _ptr(tau), _ptr(chi), _ptr(_f64(E)), _ptr(_f64(B)),
+                                       ctypes.c_uint32(seed), ctypes.c_uint32(first_id), ctypes.c_uint32(step),
+                                       sampling, ctypes.c_double(threshold), max_emissions, ctypes.c_int64(cap),
+                                       _ptr(ph_pos), _ptr(ph_mom), _ptr(ph_w), _ptr(ph_chi), _ptr(ph_tau),
+                                       ctypes.byref(nph), ctypes.byref(nem))
+    k = int(nph.value)
+    assert k <= cap
+    photons = dict(pos=ph_pos[:, :k].copy(), mom=ph_mom[:, :k].copy(), weight=ph_w[:k].copy(),
+                   chi=ph_chi[:k].copy(), tau=ph_tau[:k].copy())
+    return rad, nem.value, chi, photons
+
+
+def push_photons(dt, pos, mom):
+    """Rectilinear photon push (rad_oracle.c or_push_photons); pos updated in place, returns 1/|p|."""
+    n = mom.shape[1]
+    assert pos.dtype == np.float64 and pos.flags.c_contiguous
+    inv = np.zeros(n)
+    _rad_lib().or_push_photons(pos.shape[0], ctypes.c_int64(n), ctypes.c_double(dt), _ptr(pos), _ptr(_f64(mom)),
+                               _ptr(inv))
+    return inv
+
+
 def rad_monte_carlo(tables: RadTables, dt, mass, charge, mom, weight, tau, E, B, seed, first_id=0, step=0):
     """One Monte-Carlo radiation pass; mom and tau updated in place.  Returns (radiated, n_emissions, chi)."""
     n = mom.shape[1]

@@ -11,6 +11,7 @@
  * each mapped to [0, 1) by x * (1 - 1e-11) / 2^32 (Random.h:21-24).
  */
 #include <math.h>
+#include <stddef.h>
 #include <stdint.h>
 
 static inline uint32_t fmix32( uint32_t h )
@@ -152,10 +153,55 @@ static inline double ridgers_energy( const or_rad_tables *t, double chi, double 
  * stream (id = first_id + index, step).  Returns the radiated energy sum_p w * dgamma
  * (times mass is up to the caller) and stores each particle's chi.
  * photon_chi_fn: 0 = table, else user callback (not used by the oracle). */
+/* Macro-photon output of a Monte-Carlo pass (RadiationMonteCarlo.cpp:425-545): an
+ * emission whose photon_gamma >= threshold, while the particle has made fewer than
+ * max_emissions photons in this pass, creates `sampling` photons at the particle's
+ * position with momentum photon_gamma * p / |p| (p after the recoil), weight
+ * w / sampling, chi = photon_chi, tau = -1; its energy is then not added to the
+ * radiated tally.  Photons are appended in particle order; count may exceed cap
+ * (nothing is written past cap). */
+typedef struct {
+    int ndim;
+    const double *pos;           /* particle positions, pos[d * n + p] */
+    int sampling, max_emissions;
+    double threshold;
+    int64_t cap, count;
+    double *ph_pos, *ph_mom, *ph_w, *ph_chi, *ph_tau; /* ph_pos[d * cap + k], ph_mom[c * cap + k] */
+} or_photon_out;
+
+static double mc_pass( const or_rad_tables *t, int64_t n, double dt, double mass, double charge,
+                       double *mom, const double *weight, double *tau, double *chi_out,
+                       const double *Epart, const double *Bpart, uint32_t seed, uint32_t first_id,
+                       uint32_t step, int64_t *n_emissions, or_photon_out *ph );
+
 double or_rad_monte_carlo( const or_rad_tables *t, int64_t n, double dt, double mass, double charge,
                            double *mom, const double *weight, double *tau, double *chi_out,
                            const double *Epart, const double *Bpart, uint32_t seed, uint32_t first_id,
                            uint32_t step, int64_t *n_emissions )
+{
+    return mc_pass( t, n, dt, mass, charge, mom, weight, tau, chi_out, Epart, Bpart, seed, first_id, step,
+                    n_emissions, NULL );
+}
+
+double or_rad_monte_carlo_photons( const or_rad_tables *t, int ndim, int64_t n, double dt, double mass,
+                                   double charge, const double *pos, double *mom, const double *weight,
+                                   double *tau, double *chi_out, const double *Epart, const double *Bpart,
+                                   uint32_t seed, uint32_t first_id, uint32_t step, int sampling,
+                                   double threshold, int max_emissions, int64_t cap, double *ph_pos,
+                                   double *ph_mom, double *ph_w, double *ph_chi, double *ph_tau,
+                                   int64_t *n_photons, int64_t *n_emissions )
+{
+    or_photon_out ph = { ndim, pos, sampling, max_emissions, threshold, cap, 0, ph_pos, ph_mom, ph_w, ph_chi, ph_tau };
+    const double r = mc_pass( t, n, dt, mass, charge, mom, weight, tau, chi_out, Epart, Bpart, seed, first_id, step,
+                              n_emissions, &ph );
+    if( n_photons ) *n_photons = ph.count;
+    return r;
+}
+
+static double mc_pass( const or_rad_tables *t, int64_t n, double dt, double mass, double charge,
+                       double *mom, const double *weight, double *tau, double *chi_out,
+                       const double *Epart, const double *Bpart, uint32_t seed, uint32_t first_id,
+                       uint32_t step, int64_t *n_emissions, or_photon_out *ph )
 {
     const double oom = 1.0 / mass;
     const double qm2 = charge * oom * oom;
@@ -169,7 +215,7 @@ double or_rad_monte_carlo( const or_rad_tables *t, int64_t n, double dt, double 
         const double Bx = Bpart[p], By = Bpart[n + p], Bz = Bpart[2 * n + p];
         uint32_t rs = or_rng_init( seed, first_id + ( uint32_t )p, step );
         double local_time = 0.0, emission_time = 0.0;
-        int it = 0;
+        int it = 0, i_photon = 0;
         double last_chi = 0.0;
         while( local_time < dt && it < max_it ) {
             const double g = sqrt( 1.0 + px * px + py * py + pz * pz );
@@ -191,8 +237,24 @@ double or_rad_monte_carlo( const or_rad_tables *t, int64_t n, double dt, double 
                     px -= px * f;
                     py -= py * f;
                     pz -= pz * f;
-                    const double gn = sqrt( 1.0 + px * px + py * py + pz * pz );
-                    radiated += weight[p] * ( g - gn );
+                    if( ph && pg >= ph->threshold && i_photon < ph->max_emissions ) {
+                        const double inv = 1.0 / sqrt( px * px + py * py + pz * pz );
+                        for( int k = 0; k < ph->sampling; k++ ) {
+                            const int64_t o = ph->count++;
+                            if( o >= ph->cap ) continue;
+                            for( int d = 0; d < ph->ndim; d++ ) ph->ph_pos[d * ph->cap + o] = ph->pos[d * n + p];
+                            ph->ph_mom[o] = pg * px * inv;
+                            ph->ph_mom[ph->cap + o] = pg * py * inv;
+                            ph->ph_mom[2 * ph->cap + o] = pg * pz * inv;
+                            ph->ph_w[o] = weight[p] * ( 1.0 / ph->sampling );
+                            ph->ph_chi[o] = pchi;
+                            ph->ph_tau[o] = -1.0;
+                        }
+                        i_photon++;
+                    } else {
+                        const double gn = sqrt( 1.0 + px * px + py * py + pz * pz );
+                        radiated += weight[p] * ( g - gn );
+                    }
                     nem++;
                     tau[p] = -1.0;
                 }
@@ -229,4 +291,17 @@ void or_rad_yield_n( const or_rad_tables *t, int64_t n, const double *chi, const
 void or_rad_photon_chi_n( const or_rad_tables *t, int64_t n, const double *chi, const double *xi, double *out )
 {
     for( int64_t i = 0; i < n; i++ ) out[i] = or_rad_photon_chi( t, chi[i], xi[i] );
+}
+
+/* Rectilinear photon push (PusherPhoton::operator(), src/Pusher/PusherPhoton.cpp:30-85):
+ * invgf = 1 / |p|, x += dt p invgf. */
+void or_push_photons( int ndim, int64_t n, double dt, double *pos, const double *mom, double *invgf )
+{
+    for( int64_t p = 0; p < n; p++ ) {
+        const double px = mom[p], py = mom[n + p], pz = mom[2 * n + p];
+        const double inv = 1.0 / sqrt( px * px + py * py + pz * pz );
+        if( invgf ) invgf[p] = inv;
+        const double m[3] = { px, py, pz };
+        for( int d = 0; d < ndim; d++ ) pos[d * n + p] += dt * m[d] * inv;
+    }
 }

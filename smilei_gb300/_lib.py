@@ -94,6 +94,10 @@ _SIGNATURES = {
     "sg_rad_production_yield": (_I, [_VP, _I64, _VP, _VP, _VP, _VP]),
     "sg_rad_monte_carlo": (_I, [_VP, _VP, _I64, _D, _D, _D, _VP, _VP, _VP, _VP, _VP, _VP, ctypes.c_uint32,
                                 ctypes.c_uint32, ctypes.c_uint32, _VP, _VP, _VP]),
+    "sg_rad_monte_carlo_photons": (_I, [_VP, _VP, _I, _I64, _D, _D, _D, _VP, _VP, _VP, _VP, _VP, _VP, _VP,
+                                        ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _I, _D, _I, _I64,
+                                        _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
+    "sg_push_photons": (_I, [_I, _I64, _D, _VP, _VP, _VP, _VP]),
     "sg_mlp_create": (_I, [_I, ctypes.c_uint32, _D, _D, ctypes.POINTER(_VP)]),
     "sg_mlp_destroy": (_I, [_VP]),
     "sg_mlp_nparams": (_I, [_VP, ctypes.POINTER(_I)]),

@@ -271,12 +271,28 @@ __global__ void __launch_bounds__( 256 ) k_mlp_photon_chi_fast( MlpView m, int64
     }
 }
 
+// Macro-photon output (RadiationMonteCarlo.cpp:425-545): an emission with
+// photon_gamma >= threshold, while the particle has made fewer than max_emissions
+// photons in this pass, appends `sampling` photons (slots from one atomicAdd on
+// count) at the particle's position, momentum photon_gamma p / |p| with p after
+// the recoil, weight w / sampling, chi = photon chi, tau = -1; its energy is then
+// not tallied as radiated.  Slots at or past cap are not written.  count == null:
+// no photons.
+struct PhotonOut {
+    const double *pos;
+    int ndim, sampling, max_emissions;
+    double threshold;
+    int64_t cap;
+    unsigned long long *count;
+    double *ph_pos, *ph_mom, *ph_w, *ph_chi, *ph_tau; // ph_pos[d * cap + k], ph_mom[c * cap + k]
+};
+
 // RadiationMonteCarlo::operator() per particle (see the file header).
 __global__ void k_monte_carlo( RadTab t, MlpView m, int use_mlp, int64_t n, double dt, double qm2,
                                double *__restrict__ mom, const double *__restrict__ w, double *__restrict__ tau,
                                double *__restrict__ chi_out, const double *__restrict__ Ep,
                                const double *__restrict__ Bp, uint32_t seed, uint32_t first_id, uint32_t step,
-                               double *__restrict__ radiated, unsigned long long *__restrict__ n_emit )
+                               double *__restrict__ radiated, unsigned long long *__restrict__ n_emit, PhotonOut ph )
 {
     const int64_t p = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x;
     double rad = 0.0;
@@ -288,7 +304,7 @@ __global__ void k_monte_carlo( RadTab t, MlpView m, int use_mlp, int64_t n, doub
         double tp = tau[p];
         uint32_t rs = rng_init( seed, first_id + ( uint32_t )p, step );
         double local_time = 0.0, emission_time = 0.0, last_chi = 0.0;
-        int it = 0;
+        int it = 0, i_photon = 0;
         const double eps_tau = 1e-100;
         while( local_time < dt && it < 100 ) {
             const double g = sqrt( 1.0 + px * px + py * py + pz * pz );
@@ -315,7 +331,24 @@ __global__ void k_monte_carlo( RadTab t, MlpView m, int use_mlp, int64_t n, doub
                     px -= px * f;
                     py -= py * f;
                     pz -= pz * f;
-                    rad += w[p] * ( g - sqrt( 1.0 + px * px + py * py + pz * pz ) );
+                    if( ph.count && pg >= ph.threshold && i_photon < ph.max_emissions ) {
+                        const double inv = 1.0 / sqrt( px * px + py * py + pz * pz );
+                        const unsigned long long o0 = atomicAdd( ph.count, ( unsigned long long )ph.sampling );
+                        for( int k = 0; k < ph.sampling; k++ ) {
+                            const unsigned long long o = o0 + ( unsigned long long )k;
+                            if( o >= ( unsigned long long )ph.cap ) break;
+                            for( int d = 0; d < ph.ndim; d++ ) ph.ph_pos[d * ph.cap + o] = ph.pos[d * n + p];
+                            ph.ph_mom[o] = pg * px * inv;
+                            ph.ph_mom[ph.cap + o] = pg * py * inv;
+                            ph.ph_mom[2 * ph.cap + o] = pg * pz * inv;
+                            ph.ph_w[o] = w[p] * ( 1.0 / ph.sampling );
+                            ph.ph_chi[o] = pchi;
+                            ph.ph_tau[o] = -1.0;
+                        }
+                        i_photon++;
+                    } else {
+                        rad += w[p] * ( g - sqrt( 1.0 + px * px + py * py + pz * pz ) );
+                    }
                     nem++;
                     tp = -1.0;
                 }
@@ -358,6 +391,20 @@ __global__ void k_monte_carlo( RadTab t, MlpView m, int use_mlp, int64_t n, doub
         if( r != 0.0 ) atomicAdd( radiated, r );
         if( e ) atomicAdd( n_emit, e );
     }
+}
+
+// PusherPhoton::operator() (src/Pusher/PusherPhoton.cpp:30-85): x += dt p / |p|.
+__global__ void k_push_photons( int ndim, int64_t n, double dt, double *__restrict__ pos,
+                                const double *__restrict__ mom, double *__restrict__ invgf )
+{
+    const int64_t p = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x;
+    if( p >= n ) return;
+    const double px = mom[p], py = mom[n + p], pz = mom[2 * n + p];
+    const double inv = 1.0 / sqrt( px * px + py * py + pz * pz );
+    if( invgf ) invgf[p] = inv;
+    pos[p] += dt * px * inv;
+    if( ndim > 1 ) pos[n + p] += dt * py * inv;
+    if( ndim > 2 ) pos[2 * n + p] += dt * pz * inv;
 }
 
 // ---- MLP training ------------------------------------------------------------
@@ -626,8 +673,48 @@ int sg_rad_monte_carlo( const sg_rad_tables *T, const sg_mlp *mlp, int64_t n, do
     if( mlp ) v = view( mlp );
     k_monte_carlo<<<grid_for( n, 256 ), 256, 0, as_stream( stream )>>>( T->t, v, mlp ? 1 : 0, n, dt, charge * oom * oom, mom,
                                                                           weight, tau, chi_out, Epart, Bpart, seed,
-                                                                          first_id, step, radiated, n_emissions );
+                                                                          first_id, step, radiated, n_emissions, PhotonOut{} );
     SG_LAUNCH_CHECK( "k_monte_carlo" );
+    return SG_OK;
+}
+
+int sg_rad_monte_carlo_photons( const sg_rad_tables *T, const sg_mlp *mlp, int ndim, int64_t n, double dt,
+                                double mass, double charge, const double *pos, double *mom, const double *weight,
+                                double *tau, double *chi_out, const double *Epart, const double *Bpart, uint32_t seed,
+                                uint32_t first_id, uint32_t step, int sampling, double gamma_threshold,
+                                int max_emissions, int64_t photon_capacity, double *ph_pos, double *ph_mom,
+                                double *ph_weight, double *ph_chi, double *ph_tau, unsigned long long *n_photons,
+                                double *radiated, unsigned long long *n_emissions, sg_stream_t stream )
+{
+    SG_REQUIRE( T && pos && mom && weight && tau && Epart && Bpart && radiated && n_emissions && n_photons,
+                "NULL argument" );
+    SG_REQUIRE( ndim >= 1 && ndim <= 3, "ndim must be 1, 2 or 3" );
+    SG_REQUIRE( mass > 0.0, "mass must be positive" );
+    SG_REQUIRE( sampling >= 1 && max_emissions >= 1, "sampling and max_emissions must be at least 1" );
+    SG_REQUIRE( photon_capacity >= 0, "photon_capacity < 0" );
+    if( photon_capacity > 0 ) SG_REQUIRE( ph_pos && ph_mom && ph_weight && ph_chi && ph_tau, "NULL photon array" );
+    if( mlp ) SG_REQUIRE( mlp->mask != nullptr, "the network has not been validated (sg_mlp_validate)" );
+    if( n <= 0 ) return SG_OK;
+    const double oom = 1.0 / mass;
+    MlpView v{};
+    if( mlp ) v = view( mlp );
+    PhotonOut ph{ pos, ndim, sampling, max_emissions, gamma_threshold, photon_capacity, n_photons,
+                  ph_pos, ph_mom, ph_weight, ph_chi, ph_tau };
+    k_monte_carlo<<<grid_for( n, 256 ), 256, 0, as_stream( stream )>>>( T->t, v, mlp ? 1 : 0, n, dt, charge * oom * oom, mom,
+                                                                          weight, tau, chi_out, Epart, Bpart, seed,
+                                                                          first_id, step, radiated, n_emissions, ph );
+    SG_LAUNCH_CHECK( "k_monte_carlo" );
+    return SG_OK;
+}
+
+int sg_push_photons( int ndim, int64_t n, double dt, double *pos, const double *mom, double *invgf,
+                     sg_stream_t stream )
+{
+    SG_REQUIRE( ndim >= 1 && ndim <= 3, "ndim must be 1, 2 or 3" );
+    if( n <= 0 ) return SG_OK;
+    SG_REQUIRE( pos && mom, "NULL argument" );
+    k_push_photons<<<grid_for( n, 256 ), 256, 0, as_stream( stream )>>>( ndim, n, dt, pos, mom, invgf );
+    SG_LAUNCH_CHECK( "k_push_photons" );
     return SG_OK;
 }
 

@@ -156,3 +156,41 @@ def monte_carlo(tables: RadiationTables, dt, mass, charge, mom, weight, tau, E, 
           "monte_carlo")
     torch.cuda.current_stream().synchronize()
     return float(acc[0].item()), int(cnt.item())
+
+
+def monte_carlo_photons(tables: RadiationTables, dt, mass, charge, pos, mom, weight, tau, E, B, seed, first_id=0,
+                        step=0, sampling=1, gamma_threshold=2.0, max_emissions=10,
+                        mlp: PhotonChiMLP | None = None, chi_out=None):
+    """RadiationMonteCarlo::operator() with macro-photon creation (a species whose
+    radiation_photon_species is set), on CUDA tensors.  Returns (radiated energy of the
+    emissions that made no photon, number of emissions, photons) where photons =
+    dict(pos[ndim, k], mom[3, k], weight[k], chi[k], tau[k]) in slot order."""
+    n = weight.numel()
+    ndim = pos.shape[0]
+    cap = max(1, n * max_emissions * sampling)
+    dev = mom.device
+    ph_pos = torch.empty((ndim, cap), dtype=torch.float64, device=dev)
+    ph_mom = torch.empty((3, cap), dtype=torch.float64, device=dev)
+    ph = torch.empty((3, cap), dtype=torch.float64, device=dev)  # weight, chi, tau
+    acc = torch.zeros(3, dtype=torch.float64, device=dev)
+    check(_lib.lib().sg_rad_monte_carlo_photons(
+        tables._h, mlp._h if mlp is not None else None, ndim, n, float(dt), float(mass), float(charge), ptr(pos),
+        ptr(mom), ptr(weight), ptr(tau), ptr(chi_out) if chi_out is not None else None, ptr(E), ptr(B),
+        int(seed) & 0xffffffff, int(first_id), int(step), int(sampling), float(gamma_threshold), int(max_emissions),
+        cap, ptr(ph_pos), ptr(ph_mom), ph[0].data_ptr(), ph[1].data_ptr(), ph[2].data_ptr(),
+        acc.data_ptr() + 16, acc.data_ptr(), acc.data_ptr() + 8, torch.cuda.current_stream().cuda_stream),
+        "monte_carlo_photons")
+    torch.cuda.current_stream().synchronize()
+    cnt = acc[1:].view(torch.int64)
+    k = int(cnt[1].item())
+    assert k <= cap
+    photons = dict(pos=ph_pos[:, :k], mom=ph_mom[:, :k], weight=ph[0, :k], chi=ph[1, :k], tau=ph[2, :k])
+    return float(acc[0].item()), int(cnt[0].item()), photons
+
+
+def push_photons(dt, pos, mom, invgf=None):
+    """PusherPhoton::operator() on CUDA tensors: pos[ndim, n] += dt p / |p| in place."""
+    n = mom.shape[1]
+    check(_lib.lib().sg_push_photons(pos.shape[0], n, float(dt), ptr(pos), ptr(mom),
+                                     ptr(invgf) if invgf is not None else None,
+                                     torch.cuda.current_stream().cuda_stream), "push_photons")

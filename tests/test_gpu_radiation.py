@@ -76,6 +76,39 @@ def test_monte_carlo_pass_matches_oracle(rad):
     assert 0.05 < chi_o.mean() < 20.0
 
 
+def test_monte_carlo_photons_match_oracle(rad):
+    """Macro-photon creation: the same emissions, photons and recoils as the oracle
+    (photons come out in slot order on the GPU: compared sorted by chi)."""
+    radiation, T, Tc = rad
+    n = 20000
+    mom, E, B, w = beam(n, 3)
+    rng = np.random.default_rng(4)
+    pos = np.ascontiguousarray(np.stack([rng.uniform(0, 10, n), rng.uniform(0, 5, n)]))
+    w = rng.uniform(0.5, 1.5, n)
+    tau = np.full(n, -1.0)
+    m_gpu, tau_gpu = cu(mom), cu(tau)
+    for step in range(2):
+        r_g, e_g, ph_g = radiation.monte_carlo_photons(T, 0.1, 1.0, -1.0, cu(pos), m_gpu, cu(w), tau_gpu, cu(E), cu(B),
+                                                       seed=5, step=step, sampling=2, gamma_threshold=20.0,
+                                                       max_emissions=3)
+        r_o, e_o, _, ph_o = oracle.rad_monte_carlo_photons(Tc, 0.1, 1.0, -1.0, pos, mom, w, tau, E, B, seed=5,
+                                                           step=step, sampling=2, threshold=20.0, max_emissions=3)
+        assert e_g == e_o and ph_o["weight"].size == ph_g["weight"].numel() > 1000
+        assert abs(r_g - r_o) <= 1e-10 * max(abs(r_o), 1.0)
+        og = np.lexsort((ph_g["weight"].cpu().numpy(), ph_g["chi"].cpu().numpy()))
+        oo = np.lexsort((ph_o["weight"], ph_o["chi"]))
+        for k in ["pos", "mom", "weight", "chi", "tau"]:
+            a = ph_g[k].cpu().numpy()[..., og]
+            assert rel_err(a, ph_o[k][..., oo]) <= 1e-12, k
+    assert rel_err(m_gpu.cpu().numpy(), mom) <= 1e-12
+    # photons then move in straight lines at c
+    p_gpu = ph_g["pos"].contiguous().clone()
+    radiation.push_photons(0.5, p_gpu, ph_g["mom"].contiguous())
+    p_ref = ph_g["pos"].cpu().numpy().copy()
+    oracle.push_photons(0.5, p_ref, ph_g["mom"].cpu().numpy())
+    assert rel_err(p_gpu.cpu().numpy(), p_ref) <= 1e-15
+
+
 def test_mlp_gradients_match_cpu_oracle(rad):
     radiation, _, _ = rad
     from oracle import mlp as M
