@@ -1,4 +1,4 @@
-"""The scalar diagnostic: ``scalars.txt`` in the reference's text layout.
+"""Diagnostics: ``scalars.txt`` in the reference's text layout, and field dumps.
 
 DiagScalar mirrors the reference's DiagnosticScalar (src/Diagnostic/
 DiagnosticScalar.cpp): the same scalar names in the same order, the same
@@ -173,4 +173,72 @@ def read_scalars(path: str) -> dict:
     return {n: data[:, i] for i, n in enumerate(names)}
 
 
-__all__ = ["DiagScalar", "read_scalars", "column_width", "GENERAL", "SPECIES", "ENERGY_FIELDS", "MINMAX_FIELDS"]
+FIELD_NAMES = ["Ex", "Ey", "Ez", "Bx", "By", "Bz", "Bx_m", "By_m", "Bz_m", "Jx", "Jy", "Jz", "Rho"]
+
+
+class DiagFields:
+    """Field dumps in the reference's DiagFields layout, as .npz instead of HDF5.
+
+    The reference (src/Diagnostic/DiagnosticFields2D.cpp:20-55,150-190 and its 3D
+    twin) writes, for every field whatever its staggering, the N + 1 points per
+    dimension that start at array index oversize (the patches' own points, the
+    first patch contributing its lower border), into group ``data/<itime>`` of
+    Fields<n>.h5 with the attribute ``x_moved``.  Here each dump is one file
+    ``<path>/<itime>.npz`` holding one array per field and ``x_moved``;
+    ``time_average`` = T > 1 sums the fields of the T steps that start at each
+    selected step k * every and writes their sum times 1/T at step k * every + T - 1
+    (DiagnosticFields::prepare and run, src/Diagnostic/DiagnosticFields.cpp:262-292);
+    ``subgrid`` is a tuple of slices applied to the dumped (N + 1)-point arrays."""
+
+    def __init__(self, sim, path="Fields0", every=1, fields=None, time_average=1, subgrid=None):
+        import os
+        self.sim = sim
+        self.path = path
+        self.every = int(every)
+        self.fields = list(fields) if fields else [f for f in FIELD_NAMES if f != "Rho"]
+        self.time_average = max(1, int(time_average))
+        self.subgrid = subgrid
+        self._acc = {}
+        os.makedirs(path, exist_ok=True)
+
+    def _grab(self, name):
+        a = self.sim.rho() if name == "Rho" else self.sim.get_field(name)
+        nd = len(self.sim.n_cells)
+        sl = tuple(slice(OVERSIZE, OVERSIZE + self.sim.n_cells[d] + 1) for d in range(nd))
+        out = np.ascontiguousarray(a[sl])
+        return out[self.subgrid] if self.subgrid is not None else out
+
+    def __call__(self, itime: int):
+        """Accumulates (time average) and writes the dump of step ``itime`` when it is due."""
+        phase = itime % self.every
+        if phase >= self.time_average:
+            return None
+        if self.time_average > 1:
+            for f in self.fields:
+                self._acc[f] = self._acc.get(f, 0.0) + self._grab(f)
+            if phase != self.time_average - 1:
+                return None
+            inv = 1.0 / self.time_average
+            data = {f: self._acc[f] * inv for f in self.fields}
+            self._acc = {}
+        else:
+            data = {f: self._grab(f) for f in self.fields}
+        x_moved = self.sim.window_state()[1] if hasattr(self.sim, "window_state") else 0.0
+        import os
+        np.savez(os.path.join(self.path, f"{itime}.npz"), x_moved=np.float64(x_moved), **data)
+        return data
+
+
+def read_fields(path: str) -> dict:
+    """{itime: {field: array, "x_moved": float}} of a DiagFields directory."""
+    import os
+    out = {}
+    for fn in os.listdir(path):
+        if fn.endswith(".npz") and fn[:-4].isdigit():
+            z = np.load(os.path.join(path, fn))
+            out[int(fn[:-4])] = {k: (float(z[k]) if k == "x_moved" else z[k]) for k in z.files}
+    return dict(sorted(out.items()))
+
+
+__all__ = ["DiagScalar", "read_scalars", "column_width", "GENERAL", "SPECIES", "ENERGY_FIELDS", "MINMAX_FIELDS",
+           "DiagFields", "read_fields", "FIELD_NAMES"]

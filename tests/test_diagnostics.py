@@ -107,3 +107,45 @@ def test_scalar_values_match_numpy_on_gpu(tmp_path):
     ex = d._interior(sim.get_field("Ex"))
     assert v["ExMax"] == ex.max() and np.unravel_index(v["ExMaxCell"], ex.shape) == np.unravel_index(ex.argmax(), ex.shape)
     sim.close()
+
+
+class FieldSim:
+    """A stand-in simulation whose fields encode their array indices."""
+    n_cells = [4, 3]
+
+    def __init__(self):
+        self.t = 0
+
+    def get_field(self, name):
+        from smilei_gb300 import synthetic
+        st = synthetic.STAGGER[name.replace("_m", "")]
+        shape = tuple(self.n_cells[d] + 5 + st[d] for d in range(2))
+        i, j = np.indices(shape)
+        return 100.0 * i + j + 1000.0 * self.t
+
+    def window_state(self):
+        return (8, 0.8, 2)
+
+
+def test_field_dump_layout_and_time_average(tmp_path):
+    """N + 1 points per dimension from array index oversize, whatever the staggering
+    (DiagnosticFields2D.cpp:20-55,150-190); time_average T sums the T steps from each
+    selected step and writes at step k*every + T - 1 (DiagnosticFields.cpp:262-292)."""
+    sim = FieldSim()
+    d = D.DiagFields(sim, path=str(tmp_path / "F"), every=5, fields=["Ex", "By_m", "Jz"])
+    for t in range(11):
+        sim.t = t
+        d(t)
+    got = D.read_fields(str(tmp_path / "F"))
+    assert sorted(got) == [0, 5, 10]
+    a = got[5]["Ex"]
+    assert a.shape == (5, 4)
+    assert a[0, 0] == 100.0 * 2 + 2 + 5000.0 and a[4, 3] == 100.0 * 6 + 5 + 5000.0
+    assert got[5]["By_m"].shape == (5, 4) and got[10]["x_moved"] == 0.8
+    d2 = D.DiagFields(sim, path=str(tmp_path / "G"), every=5, fields=["Ex"], time_average=3)
+    for t in range(11):
+        sim.t = t
+        d2(t)
+    got = D.read_fields(str(tmp_path / "G"))
+    assert sorted(got) == [2, 7]
+    np.testing.assert_allclose(got[7]["Ex"][0, 0], 100.0 * 2 + 2 + 1000.0 * (5 + 6 + 7) / 3)
