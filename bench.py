@@ -202,7 +202,7 @@ def run_gpu(args, rank, world, local_rank):
 
     def build(tile):
         sm = simulation.Simulation(cfg["n_cells"], cfg["cell_length"], cfg["dt"], form=args.form,
-                                   tile=list(tile) if tile else None, use_graph=True)
+                                   tile=list(tile) if tile else None, use_graph=True, capacity_slack=args.slack)
         _lib.check(_lib.lib().sg_sim_set_stream(sm._h, stream.cuda_stream), "set_stream")
         sm.add_species(1.0, -1.0, cfg["pusher"], pos, mom, w)
         return sm
@@ -302,18 +302,29 @@ def run_gpu_lwfa(args, rank, world, local_rank):
     stream = torch.cuda.Stream(device=device)
     torch.cuda.set_stream(stream)
     c = LWFA
-    sim = simulation.Simulation(c["n_cells"], c["cell_length"], c["dt"], form=args.form, boundaries=("open", "open"),
-                                use_graph=True)
-    _lib.check(_lib.lib().sg_sim_set_stream(sim._h, stream.cuda_stream), "set_stream")
-    ly = c["n_cells"][1] * c["cell_length"][1]
-    sim.add_laser_gaussian2d(a0=c["a0"], waist=c["waist"], focus=[0.0, ly / 2], t_fwhm=c["t_fwhm"])
-    sim.add_species(1.0, -1.0, c["pusher"], np.zeros((2, 0)), np.zeros((3, 0)), np.zeros(0))
-    sim.set_species_profile(0, c["n0"], c["ppc"], x_vacuum=0.0, x_slope1=c["ramp"])
-    sim.fill_species(0)
+
+    def make(tile):
+        sm = simulation.Simulation(c["n_cells"], c["cell_length"], c["dt"], form=args.form,
+                                   boundaries=("open", "open"), tile=list(tile) if tile else None, use_graph=True,
+                                   capacity_slack=args.slack)
+        _lib.check(_lib.lib().sg_sim_set_stream(sm._h, stream.cuda_stream), "set_stream")
+        ly = c["n_cells"][1] * c["cell_length"][1]
+        sm.add_laser_gaussian2d(a0=c["a0"], waist=c["waist"], focus=[0.0, ly / 2], t_fwhm=c["t_fwhm"])
+        sm.add_species(1.0, -1.0, c["pusher"], np.zeros((2, 0)), np.zeros((3, 0)), np.zeros(0))
+        sm.set_species_profile(0, c["n0"], c["ppc"], x_vacuum=0.0, x_slope1=c["ramp"])
+        sm.fill_species(0)
+        return sm
+
+    tile, tuning = ([args.tile] * 2 if args.tile else None), None
+    if args.autotune:
+        from smilei_gb300 import autotune
+        best, times = autotune.tune_tiles(make, ndim=2)
+        tile, tuning = list(best), {"x".join(map(str, k)): round(v, 3) for k, v in times.items()}
+    sim = make(tile)
     t_start = lwfa_t_start()
     sim.set_moving_window(t_start, 1.0, c["shift"])
-    # untimed: run until the window moves, then the warm-up steps
-    pre = int(np.ceil(t_start / c["dt"])) + 1
+    # untimed: run until the window moves (or --preroll-steps, for small profiling runs), then the warm-up steps
+    pre = int(np.ceil(t_start / c["dt"])) + 1 if args.preroll_steps < 0 else args.preroll_steps
     sim.step(pre)
     for _ in range(args.warmup):
         sim.step(1)
@@ -335,6 +346,7 @@ def run_gpu_lwfa(args, rank, world, local_rank):
         wall1 = time.perf_counter()
     ms = max_over_ranks(ev0.elapsed_time(ev1), device)
     n_moved, x_moved, shifts = sim.window_state()
+    relayouts = sim.layout_stats()
     particle_steps = float(sum(counts))
     sim.close()
     ncell = int(np.prod(c["n_cells"]))
@@ -349,7 +361,7 @@ def run_gpu_lwfa(args, rank, world, local_rank):
                 peak=peak, peak_kind=peak_kind, B_alg=s_state + 24 * s / c["ppc"], launches=launches,
                 clocks=clk.summary(), window=dict(n_moved=n_moved, x_moved=x_moved, shifts=shifts, pre_steps=pre,
                                                   particles_at_start=n0),
-                cfg=c, energy=None, tile="default 8x8", tuning=None, relayouts=None,
+                cfg=c, energy=None, tile=tile or "default 8x8", tuning=tuning, relayouts=relayouts,
                 e2e=None, e2e_note="not measured for this workload: the state size changes at every window shift")
 
 
@@ -434,6 +446,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="thermal", choices=["thermal", "uneven", "lwfa"])
     ap.add_argument("--autotune", action="store_true", help="pick the tile shape by timing candidates first")
+    ap.add_argument("--slack", type=float, default=0.25,
+                    help="segment capacity slack: room per tile beyond its particle count, as a fraction")
+    ap.add_argument("--preroll-steps", type=int, default=-1,
+                    help="wakefield workload: untimed steps before the warm-up (default: until the window moves)")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -493,6 +509,7 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+i32" if args.form == "mixed" else "f64",
         "data": "synthetic (seeded Maxwellian, generated on device)",
         "config": {"workload": workload, "form": args.form, "global_particles": res["n"] * world,
+                   "capacity_slack": args.slack,
                    "cells": int(np.prod(res["cfg"]["n_cells"])), "parallelism": f"replicas x{world}", "l2": "inputs larger than L2",
                    "B_alg_bytes_per_particle_step": res["B_alg"],
                    "hbm_fraction_of_step": step_gbs / res["peak"], "wall_ms_per_step": res["wall_ms_per_step"],

@@ -1833,6 +1833,8 @@ struct SpeciesState {
     PBuf<true> om{};
     int *ovf_tile = nullptr;
     int max_cap = 0; // largest tile segment of the current layout
+    double slack = 0.0;        // capacity slack of this species' layout (0: the configuration's)
+    int64_t last_relayout = -1; // step of its last re-layout after a spill
     bool inject = false;       // fresh window cells are filled from this profile
     InjectParams inj{};        // its profile (x0, x1, n_moved set per call)
 };
@@ -2119,10 +2121,12 @@ int alloc_species_buffers( sg_sim *S, SpeciesState &s, int64_t capacity )
 }
 
 // New segment layout from counts: cap, seg_start into (new_cap, new_start); returns the total.
-int layout_from_counts( sg_sim *S, const int *count, int *new_cap, int64_t *new_start, int64_t *total, int *max_cap )
+int layout_from_counts( sg_sim *S, const int *count, int *new_cap, int64_t *new_start, int64_t *total, int *max_cap,
+                        double slack_override = 0.0 )
 {
     const int nt = S->g.ntiles;
-    const float slack = ( float )( S->cfg.capacity_slack > 0.0 ? S->cfg.capacity_slack : 0.25 );
+    const float slack = ( float )( slack_override > 0.0 ? slack_override
+                                                        : ( S->cfg.capacity_slack > 0.0 ? S->cfg.capacity_slack : 0.25 ) );
     // room beyond the slack fraction: 16 particles at the default slack of 0.25, less when the slack is smaller
     const int min_extra = ( int )std::ceil( 16.0 * std::min( 1.0, slack / 0.25 ) );
     k_caps<<<grid_for( nt, 256 ), 256, 0, S->stream>>>( S->g, count, new_cap, slack, min_extra );
@@ -2154,13 +2158,22 @@ int place_staged( sg_sim *S, SpeciesState &s, int64_t n, PBuf<MIXED> st, const i
     return SG_OK;
 }
 
+// Steps within which a second spill doubles a species' capacity slack.
+constexpr int64_t RELAYOUT_WINDOW = 64;
+
 // Re-lays species s out after a spill: counts come from the step just done.
 int relayout( sg_sim *S, SpeciesState &s, int nspill )
 {
     const int nt = S->g.ntiles;
     int64_t total = 0;
     int new_max_cap = 0;
-    int r = layout_from_counts( S, s.count[s.cur], S->tmp_cap, S->tmp_start, &total, &new_max_cap );
+    // a species that spills again soon after its last re-layout gets twice the room per
+    // tile (up to 2x its count): its density moves faster than the slack absorbs
+    const double base = S->cfg.capacity_slack > 0.0 ? S->cfg.capacity_slack : 0.25;
+    if( s.slack <= 0.0 ) s.slack = base;
+    if( s.last_relayout >= 0 && S->hstep - s.last_relayout < RELAYOUT_WINDOW ) s.slack = std::min( 2.0, 2.0 * s.slack );
+    s.last_relayout = S->hstep;
+    int r = layout_from_counts( S, s.count[s.cur], S->tmp_cap, S->tmp_start, &total, &new_max_cap, s.slack );
     if( r ) return r;
     // destination: the idle buffer, or fresh buffers when the layout no longer fits
     void *old_mem[2] = { s.mem[0], s.mem[1] };
@@ -2245,7 +2258,7 @@ int rebuild_species( sg_sim *S, SpeciesState &s, int shift, int x0, int x1 )
     }
     int64_t total = 0;
     int new_max_cap = 0;
-    int r = layout_from_counts( S, newcount, S->tmp_cap, S->tmp_start, &total, &new_max_cap ); // synchronises
+    int r = layout_from_counts( S, newcount, S->tmp_cap, S->tmp_start, &total, &new_max_cap, s.slack ); // synchronises
     if( r ) return r;
     unsigned long long wc[2] = { 0, 0 };
     SG_CUDA_TRY( cudaMemcpyAsync( wc, S->d_wcount, sizeof( wc ), cudaMemcpyDeviceToHost, st ) );
