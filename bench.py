@@ -397,6 +397,160 @@ def run_cpu_sample_lwfa(args):
                        f"{steps} FP64 steps of oracle/bc_oracle.c + pic_oracle.c")
 
 
+RAD = dict(n_cells=[2048, 512], ppw=16, npart=10_000_000, gamma=2000.0, sigma_wavelengths=2.0, a0=100.0)
+
+
+def rad_setup(n_cells, npart, seed):
+    """Head-on collision: a Gaussian electron bunch (gamma 2000, sigma_x = sigma_y = 2 lambda)
+    moving towards -x through a plane wave of a0 = 100 moving towards +x; 16 cells per
+    wavelength (lambda = 2 pi), dt = 0.95 CFL."""
+    lam = 2.0 * np.pi
+    dx = lam / RAD["ppw"]
+    dt = 0.95 / np.sqrt(2.0 / dx ** 2)
+    rng = np.random.default_rng(seed)
+    L = [n_cells[0] * dx, n_cells[1] * dx]
+    sig = RAD["sigma_wavelengths"] * lam
+    pos = np.stack([np.clip(rng.normal(L[0] / 2, sig, npart), 4 * dx, L[0] - 4 * dx),
+                    np.clip(rng.normal(L[1] / 2, sig, npart), 4 * dx, L[1] - 4 * dx)])
+    p0 = np.sqrt(RAD["gamma"] ** 2 - 1.0)
+    mom = np.stack([np.full(npart, -p0), np.zeros(npart), np.zeros(npart)])
+    return dict(dx=dx, dt=dt, pos=np.ascontiguousarray(pos), mom=np.ascontiguousarray(mom),
+                w=np.ones(npart), lam=lam)
+
+
+def plane_wave(shape_fn, n_cells, dx, a0):
+    """Ey = Bz = a0 sin(k x) on their own staggered x positions (a wave moving towards +x)."""
+    out = {}
+    for comp, stag_x in (("Ey", 0), ("Bz", 1)):
+        shp = shape_fn(comp)
+        x = (np.arange(shp[0]) - 2 - 0.5 * stag_x) * dx
+        out[comp] = np.repeat((a0 * np.sin(x))[:, None], shp[1], axis=1)
+    return out
+
+
+def run_gpu_radiation(args, rank, world, local_rank):
+    """Monte-Carlo radiation reaction in the PIC loop through the drop-in operators (FP64):
+    per step interpolate, radiate (RadiationMonteCarlo), push (Vay), deposit (Esirkepov),
+    then B save, Ampere, Faraday, B centring, in the order of Species::dynamics.  Photon
+    chi from the table, or from the MLP where its validation passed (--mlp)."""
+    import torch
+    from smilei_gb300 import operators as O, radiation as R, _lib
+    device = f"cuda:{local_rank}"
+    torch.cuda.set_device(local_rank)
+    n_cells = RAD["n_cells"]
+    st = rad_setup(n_cells, RAD["npart"], args.seed + rank)
+    geom = O.PatchGeometry(n_cells, [st["dx"], st["dx"]])
+    EM = O.ElectroMagn(geom, device=device)
+    for comp, arr in plane_wave(geom.shape, n_cells, st["dx"], RAD["a0"]).items():
+        getattr(EM, comp + "_").copy_(torch.as_tensor(arr, device=device))
+    EM.Bz_m.copy_(EM.Bz_)
+    cu = lambda a: torch.as_tensor(a, dtype=torch.float64, device=device).contiguous()
+    P = O.Particles(cu(st["pos"]), cu(st["mom"]), cu(st["w"]), torch.full((RAD["npart"],), -1, device=device))
+    del st["pos"], st["mom"]
+    smpi = O.SmileiMPI(2, P.size(), device=device)
+    tau = torch.full((P.size(),), -1.0, dtype=torch.float64, device=device)
+    g = np.load(os.path.join(ROOT, "tests", "golden", "radiation.npz"))
+    f_dn, f_cl, inv_es = R.normalised_factors(2.0 * np.pi * 299792458.0 / 1e-6)
+    T = R.RadiationTables(g["integfochi"], g["integfochi_min"], g["integfochi_max"], g["xi_table"], g["xi_min"],
+                          g["xi_max"], g["xi_axis1_min"], f_dn, f_cl, inv_es)
+    if args.rad_math == "fp32":
+        T.set_fp32_math(True)
+    mlp, used = None, None
+    if args.mlp:
+        mlp = R.PhotonChiMLP(hidden=64, seed=3)
+        for steps, lr in ((4000, 2e-3), (4000, 1e-3), (4000, 3e-4)):
+            mlp.train(T, steps=steps, batch=8192, lr=lr)
+        err, n_masked = mlp.validate(T, tol=0.05)
+        used = f"{err.size - n_masked}/{err.size} (chi, xi) bins"
+    dt = st["dt"]
+    interp = O.Interpolator2D2Order(geom)
+    push = O.PusherVay(dt, 1.0, 2)
+    proj = O.Projector2D2Order(geom, dt)
+    ma, mf = O.MA_Solver_norm(dt), O.MF_Solver_Yee(dt)
+    acc = torch.zeros(2, dtype=torch.float64, device=device)
+    stream = torch.cuda.current_stream()
+    L = _lib.lib()
+
+    def step(it):
+        interp.fieldsWrapper(EM, P, smpi)
+        _lib.check(L.sg_rad_monte_carlo(T._h, mlp._h if mlp is not None else None, P.size(), dt, 1.0, -1.0,
+                                        P.momentum.data_ptr(), P.weight.data_ptr(), tau.data_ptr(), None,
+                                        smpi.dynamics_Epart.data_ptr(), smpi.dynamics_Bpart.data_ptr(), 7, 0, it,
+                                        acc.data_ptr(), acc.data_ptr() + 8, stream.cuda_stream), "monte_carlo")
+        push(P, smpi)
+        EM.restartRhoJ()
+        proj.currentsAndDensityWrapper(EM, P, smpi)
+        EM.saveMagneticFields()
+        ma(EM)
+        mf(EM)
+        EM.centerMagneticFields()
+
+    for it in range(args.warmup):
+        step(it)
+    torch.cuda.synchronize()
+    acc.zero_()
+    with ClockSampler(local_rank) as clk:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        wall0 = time.perf_counter()
+        e0.record()
+        for it in range(args.steps):
+            step(args.warmup + it)
+        e1.record()
+        torch.cuda.synchronize()
+        wall1 = time.perf_counter()
+    ms = max_over_ranks(e0.elapsed_time(e1), device)
+    radiated = float(acc[0].item())
+    n_emit = int(acc[1:].view(torch.int64).item())
+    n = P.size()
+    # bytes the operator chain moves per particle-step (FP64): interpolate 88, radiate 120, push 138, deposit 82
+    b_per = 88.0 + 120.0 + 138.0 + 82.0
+    peak, peak_kind = measured_peak()
+    value = whole_job_rate(n, world, args.steps, ms)
+    if mlp is not None:
+        mlp.close()
+    return dict(n=n, ms=ms, value=value, wall_ms_per_step=(wall1 - wall0) * 1e3 / args.steps, clocks=clk.summary(),
+                b_per=b_per, peak=peak, peak_kind=peak_kind, radiated=radiated, emissions=n_emit, mlp_used=used)
+
+
+def run_cpu_sample_radiation(args):
+    """The oracle's interpolate, Monte-Carlo radiation, Vay push and deposit on a bounded
+    sample: 200,000 electrons of the same bunch on a 512 x 128-cell grid (FP64)."""
+    import oracle
+    n_cells = [512, 128]
+    st = rad_setup(n_cells, 200_000, args.seed)
+    O = oracle.Oracle()
+    from smilei_gb300 import synthetic
+    stag = synthetic.STAGGER
+    shape = lambda c: tuple(n_cells[d] + 5 + stag[c.replace("_m", "")][d] for d in range(2))
+    f = {c: np.zeros(shape(c)) for c in ["Ex", "Ey", "Ez", "Bx", "By", "Bz", "Jx", "Jy", "Jz"]}
+    f.update(plane_wave(shape, n_cells, st["dx"], RAD["a0"]))
+    n_prim = [n + 5 for n in n_cells]
+    dom = [-2, -2]
+    cl = [st["dx"], st["dx"]]
+    g = np.load(os.path.join(ROOT, "tests", "golden", "radiation.npz"))
+    from smilei_gb300.radiation import normalised_factors
+    f_dn, f_cl, inv_es = normalised_factors(2.0 * np.pi * 299792458.0 / 1e-6)
+    Tc = oracle.RadTables.from_golden(g, factor_dNph_dt=f_dn, factor_classical=f_cl, inv_norm_E_schwinger=inv_es)
+    pos, mom, w = st["pos"], st["mom"], st["w"]
+    q = np.full(w.size, -1, np.int16)
+    tau = np.full(w.size, -1.0)
+    steps = max(2, args.cpu_steps)
+    t0 = time.perf_counter()
+    for it in range(steps):
+        E, B, iold, delta = O.interpolate(2, n_prim, dom, cl, [f["Ex"], f["Ey"], f["Ez"], f["Bx"], f["By"], f["Bz"]],
+                                          pos)
+        oracle.rad_monte_carlo(Tc, st["dt"], 1.0, -1.0, mom, w, tau, E, B, seed=7, step=it)
+        pos, mom, invgf = O.push("vay", 2, st["dt"], 1.0, pos, mom, q, E, B)
+        J = [np.zeros_like(f["Jx"]), np.zeros_like(f["Jy"]), np.zeros_like(f["Jz"]), None]
+        O.project(0, 2, n_prim, dom, cl, st["dt"], pos, mom, w, q, invgf, iold, delta, J)
+    t1 = time.perf_counter()
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return dict(value=w.size * steps / (t1 - t0), unit=UNIT, cores=cores, kind="port",
+                sample=f"radiation sample: 200000 electrons (gamma 2000, a0 = 100 plane wave) on 512x128 cells, "
+                       f"{steps} FP64 steps of interpolate + Monte-Carlo radiation + Vay push + Esirkepov "
+                       f"(oracle/pic_oracle.c, rad_oracle.c; fields held fixed)")
+
+
 def run_cpu_sample(args, steps=None):
     """The oracle's FP64 timestep on a bounded sample of the workload (all host cores)."""
     import oracle
@@ -444,7 +598,10 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="thermal", choices=["thermal", "uneven", "lwfa"])
+    ap.add_argument("--workload", default="thermal", choices=["thermal", "uneven", "lwfa", "radiation"])
+    ap.add_argument("--mlp", action="store_true", help="radiation workload: photon chi from the trained MLP")
+    ap.add_argument("--rad-math", default="fp32", choices=["fp32", "fp64"],
+                    help="radiation workload: arithmetic of the Monte-Carlo table lookups and draws")
     ap.add_argument("--autotune", action="store_true", help="pick the tile shape by timing candidates first")
     ap.add_argument("--slack", type=float, default=0.25,
                     help="segment capacity slack: room per tile beyond its particle count, as a fraction")
@@ -455,7 +612,12 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-    if args.workload == "lwfa":
+    if args.workload == "radiation":
+        workload = ("2D Monte-Carlo radiation reaction: 2048x512 cells (16 per wavelength), 1e7 electrons gamma=2000 "
+                    "in a Gaussian bunch (sigma_x = sigma_y = 2 lambda) head-on with a plane wave a0=100, Vay, "
+                    "drop-in FP64 operators, Monte-Carlo lookups in " + args.rad_math + ", photon chi from the " +
+                    ("MLP (table where its validation failed)" if args.mlp else "table"))
+    elif args.workload == "lwfa":
         c = LWFA
         workload = (f"2D laser wakefield with a moving window: {c['n_cells'][0]}x{c['n_cells'][1]} cells, dx=0.1, "
                     f"dy=1.5, dt=0.095, Gaussian laser a0=2 waist 30 FWHM 60 from xmin, electrons n=0.003 with a "
@@ -471,7 +633,8 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        r = run_cpu_sample_lwfa(args) if args.workload == "lwfa" else run_cpu_sample(args)
+        r = (run_cpu_sample_lwfa(args) if args.workload == "lwfa" else
+             run_cpu_sample_radiation(args) if args.workload == "radiation" else run_cpu_sample(args))
         line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
                 "steps": args.cpu_steps, "warmup": 1, "ms_per_step": None, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, host)",
@@ -484,6 +647,30 @@ def main():
     if world > 1:
         import torch.distributed as td
         td.init_process_group("nccl")
+    if args.workload == "radiation":
+        res = run_gpu_radiation(args, rank, world, local_rank)
+        cpu = None
+        if rank == 0 and world == 1 and not args.no_cpu_baseline:
+            cpu = run_cpu_sample_radiation(args)
+        if rank == 0:
+            achieved = res["b_per"] * res["value"] / 1e9
+            print(json.dumps({
+                "metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": res["ms"] / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded bunch, host)",
+                "config": {"workload": workload, "form": "fp64 operators", "global_particles": res["n"] * world,
+                           "wall_ms_per_step": res["wall_ms_per_step"], "radiated_energy": res["radiated"],
+                           "emissions": res["emissions"], "mlp_used_on": res["mlp_used"],
+                           "l2": "inputs larger than L2"},
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": res["peak"], "unit": "GB/s",
+                             "frac": achieved / res["peak"], "traffic": None, "kernel": "operator chain",
+                             "algorithmic_bytes_per_particle_step": res["b_per"],
+                             "peak_source": res["peak_kind"]},
+                "cpu_baseline": cpu, "e2e": None, "gpu_launches": 9 * args.steps, "clocks": res["clocks"]}))
+        if world > 1:
+            import torch.distributed as td
+            td.destroy_process_group()
+        return
     if args.workload == "lwfa":
         res = run_gpu_lwfa(args, rank, world, local_rank)
     else:

@@ -292,6 +292,13 @@ int sg_rad_tables_create( const double *integ, int n_integ, double integ_min, do
                           const double *factors, sg_rad_tables **out );
 int sg_rad_tables_destroy( sg_rad_tables *tables );
 
+/* Arithmetic of the Monte-Carlo passes that use these tables: 0 (default) FP64, as the
+ * reference; 1 FP32 for the table lookups, the optical-depth draw and the continuous
+ * loss (chi, gamma, times and momenta stay FP64).  FP64 runs at a small fraction of the
+ * FP32 rate on GB300; the FP32 pass draws the same random numbers and agrees with the
+ * FP64 pass statistically, not bit for bit. */
+int sg_rad_tables_set_fp32_math( sg_rad_tables *tables, int on );
+
 /* Inverse CDF (particle chi, xi) -> photon chi: replaces
  * RadiationTables::computeRandomPhotonChiWithInterpolation (RadiationTables.cpp:375). */
 int sg_rad_photon_chi( const sg_rad_tables *tables, int64_t n, const double *chi, const double *xi, double *out,

@@ -90,6 +90,7 @@ _SIGNATURES = {
     "sg_sim_get_rho": (_I, [_VP, _VP]),
     "sg_rad_tables_create": (_I, [_VP, _I, _D, _D, _VP, _I, _I, _D, _D, _VP, _VP, ctypes.POINTER(_VP)]),
     "sg_rad_tables_destroy": (_I, [_VP]),
+    "sg_rad_tables_set_fp32_math": (_I, [_VP, _I]),
     "sg_rad_photon_chi": (_I, [_VP, _I64, _VP, _VP, _VP, _VP]),
     "sg_rad_production_yield": (_I, [_VP, _I64, _VP, _VP, _VP, _VP]),
     "sg_rad_monte_carlo": (_I, [_VP, _VP, _I64, _D, _D, _D, _VP, _VP, _VP, _VP, _VP, _VP, ctypes.c_uint32,

@@ -39,6 +39,7 @@ struct RadTab {
     double xi_l0, xi_d, xi_id, inv_nph_m1;
     const double *axis1_min;
     double factor_dNph_dt, factor_classical, min_cont, min_disc, inv_es;
+    const float *integf, *xif, *axis1_minf; // FP32 copies for the FP32-math Monte Carlo
 };
 
 __host__ __device__ inline uint32_t fmix32( uint32_t h )
@@ -132,6 +133,76 @@ __device__ double tab_photon_chi( const RadTab &t, double chi, double xi )
 }
 
 // ---- the MLP ----------------------------------------------------------------
+// The two lookups in FP32 arithmetic (same interpolation rules as above): the
+// table itself is a piecewise-linear fit in log space, far coarser than FP32.
+__device__ float tab_yield32( const RadTab &t, float chi, float gamma )
+{
+    const float lc = log10f( chi );
+    const float l0 = ( float )t.integ_l0, d = ( float )t.integ_d, id = ( float )t.integ_id;
+    const int i = ( int )floorf( ( lc - l0 ) * id );
+    float v;
+    if( i < 0 ) v = t.integf[0];
+    else if( i >= t.n_integ - 1 ) v = t.integf[t.n_integ - 2];
+    else {
+        const float lm = i * d + l0, lp = lm + d;
+        v = ( t.integf[i + 1] * fabsf( lc - lm ) + t.integf[i] * fabsf( lp - lc ) ) * id;
+    }
+    return ( float )t.factor_dNph_dt * v * chi / gamma;
+}
+
+__device__ __forceinline__ int search_monotonic32( const float *__restrict__ a, float v, int n )
+{
+    int imin = 0, imax = n - 1;
+    if( v == a[0] ) return 0;
+    if( v == a[n - 1] ) return n - 2;
+    while( imax - imin > 1 ) {
+        const int imid = ( imin + imax ) / 2;
+        if( v >= a[imid] ) imin = imid;
+        else imax = imid;
+    }
+    return imin;
+}
+
+__device__ float tab_photon_chi32( const RadTab &t, float chi, float xi )
+{
+    const int n1 = t.n_ph;
+    const float lc = log10f( chi );
+    const float l0 = ( float )t.xi_l0, d0 = ( float )t.xi_d, id0 = ( float )t.xi_id, inm1 = ( float )t.inv_nph_m1;
+    int ic = ( int )floorf( ( lc - l0 ) * id0 );
+    if( ic < 0 ) ic = 0;
+    else if( ic > t.n_chi - 2 ) ic = t.n_chi - 2;
+    const float *X = t.xif;
+    int i1, i2;
+    if( xi <= X[ic * n1] ) {
+        i1 = 0;
+        i2 = 0;
+        xi = X[ic * n1];
+    } else {
+        i1 = search_monotonic32( &X[ic * n1], xi, n1 );
+        i2 = search_monotonic32( &X[( ic + 1 ) * n1], xi, n1 );
+    }
+    const float dchi = ( lc - ( ic * d0 + l0 ) ) * id0;
+    const float d1 = ( ic * d0 + l0 - t.axis1_minf[ic] ) * inm1;
+    const float d2 = ( ( ic + 1 ) * d0 + l0 - t.axis1_minf[ic + 1] ) * inm1;
+    const int x1 = ic * n1 + i1, x2 = ( ic + 1 ) * n1 + i2;
+    float p1, p2;
+    if( X[x1] < 1.0f && X[x1 + 1] - X[x1] > 1e-15f ) {
+        const float lm = i1 * d1 + t.axis1_minf[ic], lp = lm + d1;
+        const float d = ( xi - X[x1] ) / ( X[x1 + 1] - X[x1] );
+        p1 = lm * ( 1.0f - d ) + lp * d;
+    } else {
+        p1 = i1 * d1 + t.axis1_minf[ic];
+    }
+    if( X[x2] < 1.0f && X[x2 + 1] - X[x2] > 1e-15f ) {
+        const float lm = i2 * d2 + t.axis1_minf[ic + 1], lp = lm + d2;
+        const float d = ( xi - X[x2] ) / ( X[x2 + 1] - X[x2] );
+        p2 = lm * ( 1.0f - d ) + lp * d;
+    } else {
+        p2 = i2 * d2 + t.axis1_minf[ic + 1];
+    }
+    return exp10f( p1 * ( 1.0f - dchi ) + p2 * dchi );
+}
+
 constexpr int MLP_MAX_H = 128;
 
 struct MlpView {
@@ -288,12 +359,71 @@ struct PhotonOut {
 };
 
 // RadiationMonteCarlo::operator() per particle (see the file header).
+// The network's weights in shared memory, for kernels that evaluate it per thread.
+template <int H>
+struct MlpShared {
+    float W1[2 * H], b1[H], b2[H], W3[H], b3;
+    float4 W2v[H * H / 4]; // row r, columns 4c..4c+3 at r * H / 4 + c
+};
+
+template <int H>
+__device__ __forceinline__ void mlp_stage( const MlpView &m, MlpShared<H> &w )
+{
+    float *W2 = reinterpret_cast<float *>( w.W2v );
+    for( int k = threadIdx.x; k < H * H; k += blockDim.x ) W2[k] = m.W2[k];
+    for( int k = threadIdx.x; k < H; k += blockDim.x ) {
+        w.W1[2 * k] = m.W1[2 * k];
+        w.W1[2 * k + 1] = m.W1[2 * k + 1];
+        w.b1[k] = m.b1[k];
+        w.b2[k] = m.b2[k];
+        w.W3[k] = m.W3[k];
+    }
+    if( threadIdx.x == 0 ) w.b3 = m.b3[0];
+}
+
+// photon chi = chi 10^(out_scale * network(log10 chi, xi)), hidden layer in registers
+template <int H>
+__device__ __forceinline__ double mlp_photon_chi_smem( const MlpView &m, const MlpShared<H> &w, double chi, double xi )
+{
+    const float u0 = 2.0f * ( log10f( ( float )chi ) - m.lmin ) / m.lspan - 1.0f;
+    const float u1 = 2.0f * ( float )xi - 1.0f;
+    float h1[H];
+#pragma unroll
+    for( int k = 0; k < H; k++ ) h1[k] = tanh_fast( fmaf( w.W1[2 * k], u0, fmaf( w.W1[2 * k + 1], u1, w.b1[k] ) ) );
+    float y = w.b3;
+#pragma unroll( H >= 64 ? 1 : 2 )
+    for( int r = 0; r < H; r++ ) {
+        float a = w.b2[r];
+#pragma unroll
+        for( int c = 0; c < H / 4; c++ ) {
+            const float4 wv = w.W2v[r * ( H / 4 ) + c];
+            a = fmaf( wv.x, h1[4 * c], a );
+            a = fmaf( wv.y, h1[4 * c + 1], a );
+            a = fmaf( wv.z, h1[4 * c + 2], a );
+            a = fmaf( wv.w, h1[4 * c + 3], a );
+        }
+        y = fmaf( w.W3[r], tanh_fast( a ), y );
+    }
+    return chi * ( double )exp10f( y * m.out_scale );
+}
+
+// F32: the table lookups, the optical-depth draw and the continuous-loss formula in
+// FP32 arithmetic (FP64 is a small fraction of FP32 throughput on this GPU); chi,
+// gamma, times and momenta stay FP64.  The random stream is the FP64 pass's.
+// H > 0: the network (H hidden units) evaluated from shared memory; H == 0 with
+// use_mlp: any width, weights read from global memory.
+template <bool F32, int H>
 __global__ void k_monte_carlo( RadTab t, MlpView m, int use_mlp, int64_t n, double dt, double qm2,
                                double *__restrict__ mom, const double *__restrict__ w, double *__restrict__ tau,
                                double *__restrict__ chi_out, const double *__restrict__ Ep,
                                const double *__restrict__ Bp, uint32_t seed, uint32_t first_id, uint32_t step,
                                double *__restrict__ radiated, unsigned long long *__restrict__ n_emit, PhotonOut ph )
 {
+    __shared__ MlpShared<H == 0 ? 4 : H> sw;
+    if constexpr( H > 0 ) {
+        mlp_stage<H>( m, sw );
+        __syncthreads();
+    }
     const int64_t p = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x;
     double rad = 0.0;
     unsigned long long nem = 0;
@@ -316,16 +446,25 @@ __global__ void k_monte_carlo( RadTab t, MlpView m, int use_mlp, int64_t n, doub
             const double chi = fabs( qm2 ) * t.inv_es * sqrt( fabs( a * a - b * b - c * c - d * d ) );
             last_chi = chi;
             if( chi > t.min_disc && tp <= eps_tau ) {
-                while( tp <= eps_tau ) tp = -log( 1.0 - rng_uniform( rs ) );
+                if constexpr( F32 ) {
+                    while( tp <= eps_tau ) tp = -( double )logf( fmaxf( 1.0f - ( float )rng_uniform( rs ), 5.9604645e-8f ) );
+                } else {
+                    while( tp <= eps_tau ) tp = -log( 1.0 - rng_uniform( rs ) );
+                }
             }
             if( tp > eps_tau ) {
-                const double rate = tab_yield( t, chi, g );
+                const double rate = F32 ? ( double )tab_yield32( t, ( float )chi, ( float )g ) : tab_yield( t, chi, g );
                 emission_time = fmin( tp / rate, dt - local_time );
                 tp -= rate * emission_time;
                 if( tp <= eps_tau ) {
                     const double u = rng_uniform( rs );
-                    const double pchi = ( use_mlp && !mlp_masked( m, chi, u ) ) ? mlp_photon_chi( m, chi, u )
-                                                                               : tab_photon_chi( t, chi, u );
+                    double pchi;
+                    if( use_mlp && !mlp_masked( m, chi, u ) ) {
+                        if constexpr( H > 0 ) pchi = mlp_photon_chi_smem<H>( m, sw, chi, u );
+                        else pchi = mlp_photon_chi( m, chi, u );
+                    } else {
+                        pchi = F32 ? ( double )tab_photon_chi32( t, ( float )chi, ( float )u ) : tab_photon_chi( t, chi, u );
+                    }
                     const double pg = pchi / chi * ( g - 1.0 );
                     const double f = pg / sqrt( g * g - 1.0 );
                     px -= px * f;
@@ -356,8 +495,15 @@ __global__ void k_monte_carlo( RadTab t, MlpView m, int use_mlp, int64_t n, doub
                 local_time += emission_time;
             } else if( chi <= t.min_disc && tp <= eps_tau && chi > t.min_cont ) {
                 emission_time = dt - local_time;
-                const double aa = 1.0 + 4.8 * ( 1.0 + chi ) * log( 1.0 + 1.7 * chi ) + 2.44 * chi * chi;
-                const double e = ( 1.0 / cbrt( aa * aa ) ) * emission_time * chi * chi * t.factor_classical;
+                double e;
+                if constexpr( F32 ) {
+                    const float c = ( float )chi;
+                    const float aa = 1.0f + 4.8f * ( 1.0f + c ) * logf( 1.0f + 1.7f * c ) + 2.44f * c * c;
+                    e = ( double )( 1.0f / cbrtf( aa * aa ) ) * emission_time * chi * chi * t.factor_classical;
+                } else {
+                    const double aa = 1.0 + 4.8 * ( 1.0 + chi ) * log( 1.0 + 1.7 * chi ) + 2.44 * chi * chi;
+                    e = ( 1.0 / cbrt( aa * aa ) ) * emission_time * chi * chi * t.factor_classical;
+                }
                 const double tmp = e * g / ( g * g - 1.0 );
                 px -= tmp * px;
                 py -= tmp * py;
@@ -538,6 +684,8 @@ using namespace sg;
 struct sg_rad_tables {
     RadTab t;
     double *mem = nullptr;
+    float *memf = nullptr; // FP32 copies of the tables
+    int fp32 = 0;          // Monte-Carlo arithmetic: 0 FP64, 1 FP32 (sg_rad_tables_set_fp32_math)
 };
 
 struct sg_mlp {
@@ -587,7 +735,25 @@ int ensure_scratch( sg_mlp *m, int B )
 
 } // namespace
 
+namespace sg {
+namespace {
+// The Monte-Carlo kernel for the tables' arithmetic and the network's width.
+using McKernel = void ( * )( RadTab, MlpView, int, int64_t, double, double, double *, const double *, double *,
+                             double *, const double *, const double *, uint32_t, uint32_t, uint32_t, double *,
+                             unsigned long long *, PhotonOut );
+template <bool F32>
+McKernel mc_kernel_for( int H )
+{
+    if( H == 64 ) return k_monte_carlo<F32, 64>;
+    if( H == 32 ) return k_monte_carlo<F32, 32>;
+    if( H == 16 ) return k_monte_carlo<F32, 16>;
+    return k_monte_carlo<F32, 0>;
+}
+} // namespace
+} // namespace sg
+
 extern "C" {
+
 
 int sg_rad_tables_create( const double *integ, int n_integ, double integ_min, double integ_max, const double *xi,
                           int n_chi, int n_ph, double xi_min, double xi_max, const double *axis1_min,
@@ -627,7 +793,30 @@ int sg_rad_tables_create( const double *integ, int n_integ, double integ_min, do
     t.inv_es = factors[2];
     t.min_cont = factors[3];
     t.min_disc = factors[4];
+    {
+        std::vector<float> hf( n );
+        for( int i = 0; i < n_integ; i++ ) hf[i] = ( float )integ[i];
+        for( size_t i = 0; i < ( size_t )n_chi * n_ph; i++ ) hf[n_integ + i] = ( float )xi[i];
+        for( int i = 0; i < n_chi; i++ ) hf[n_integ + ( size_t )n_chi * n_ph + i] = ( float )axis1_min[i];
+        if( cudaMalloc( &T->memf, n * sizeof( float ) ) != cudaSuccess ||
+            cudaMemcpy( T->memf, hf.data(), n * sizeof( float ), cudaMemcpyHostToDevice ) != cudaSuccess ) {
+            release( T->mem );
+            release( T->memf );
+            delete T;
+            return set_error( SG_ERR_NOMEM, "cannot allocate the FP32 radiation tables" );
+        }
+        t.integf = T->memf;
+        t.xif = T->memf + n_integ;
+        t.axis1_minf = T->memf + n_integ + ( size_t )n_chi * n_ph;
+    }
     *out = T;
+    return SG_OK;
+}
+
+int sg_rad_tables_set_fp32_math( sg_rad_tables *T, int on )
+{
+    SG_REQUIRE( T, "NULL tables" );
+    T->fp32 = on ? 1 : 0;
     return SG_OK;
 }
 
@@ -635,6 +824,7 @@ int sg_rad_tables_destroy( sg_rad_tables *T )
 {
     if( !T ) return SG_OK;
     release( T->mem );
+    release( T->memf );
     delete T;
     return SG_OK;
 }
@@ -671,9 +861,11 @@ int sg_rad_monte_carlo( const sg_rad_tables *T, const sg_mlp *mlp, int64_t n, do
     const double oom = 1.0 / mass;
     MlpView v{};
     if( mlp ) v = view( mlp );
-    k_monte_carlo<<<grid_for( n, 256 ), 256, 0, as_stream( stream )>>>( T->t, v, mlp ? 1 : 0, n, dt, charge * oom * oom, mom,
-                                                                          weight, tau, chi_out, Epart, Bpart, seed,
-                                                                          first_id, step, radiated, n_emissions, PhotonOut{} );
+    const int H = mlp ? v.H : 0;
+    McKernel kern = T->fp32 ? mc_kernel_for<true>( H ) : mc_kernel_for<false>( H );
+    kern<<<grid_for( n, 256 ), 256, 0, as_stream( stream )>>>( T->t, v, mlp ? 1 : 0, n, dt, charge * oom * oom, mom, weight,
+                                                                tau, chi_out, Epart, Bpart, seed, first_id, step, radiated,
+                                                                n_emissions, PhotonOut{} );
     SG_LAUNCH_CHECK( "k_monte_carlo" );
     return SG_OK;
 }
@@ -700,9 +892,11 @@ int sg_rad_monte_carlo_photons( const sg_rad_tables *T, const sg_mlp *mlp, int n
     if( mlp ) v = view( mlp );
     PhotonOut ph{ pos, ndim, sampling, max_emissions, gamma_threshold, photon_capacity, n_photons,
                   ph_pos, ph_mom, ph_weight, ph_chi, ph_tau };
-    k_monte_carlo<<<grid_for( n, 256 ), 256, 0, as_stream( stream )>>>( T->t, v, mlp ? 1 : 0, n, dt, charge * oom * oom, mom,
-                                                                          weight, tau, chi_out, Epart, Bpart, seed,
-                                                                          first_id, step, radiated, n_emissions, ph );
+    const int H = mlp ? v.H : 0;
+    McKernel kern = T->fp32 ? mc_kernel_for<true>( H ) : mc_kernel_for<false>( H );
+    kern<<<grid_for( n, 256 ), 256, 0, as_stream( stream )>>>( T->t, v, mlp ? 1 : 0, n, dt, charge * oom * oom, mom, weight,
+                                                                tau, chi_out, Epart, Bpart, seed, first_id, step, radiated,
+                                                                n_emissions, ph );
     SG_LAUNCH_CHECK( "k_monte_carlo" );
     return SG_OK;
 }

@@ -52,6 +52,11 @@ class RadiationTables:
         self.chi_range = (float(xi_min), float(xi_max))
         self.nbytes = integ.nbytes + xi.nbytes + ax.nbytes
 
+
+    def set_fp32_math(self, on: bool = True):
+        """Monte-Carlo passes with these tables in FP32 arithmetic for the lookups, the
+        optical-depth draw and the continuous loss (chi, gamma, momenta stay FP64)."""
+        check(_lib.lib().sg_rad_tables_set_fp32_math(self._h, int(bool(on))), "set_fp32_math")
     def close(self):
         if getattr(self, "_h", None):
             _lib.lib().sg_rad_tables_destroy(self._h)

@@ -109,6 +109,50 @@ def test_monte_carlo_photons_match_oracle(rad):
     assert rel_err(p_gpu.cpu().numpy(), p_ref) <= 1e-15
 
 
+def test_fp32_math_pass_agrees_with_fp64(rad):
+    """The FP32-math pass draws the same random numbers as the FP64 pass and uses the
+    same tables in FP32: the same emissions up to rare threshold flips, the same radiated
+    energy and spectrum to well under a percent, and most particles' momenta at FP32
+    rounding level.  It is also faster (FP64 is slow on this GPU)."""
+    from smilei_gb300 import radiation as R
+    radiation, T, _ = rad
+    g = np.load(__import__("os").path.join(__import__("os").path.dirname(__file__), "golden", "radiation.npz"))
+    f_dn, f_cl, inv_es = R.normalised_factors(2.0 * np.pi * 299792458.0 / 1e-6)
+    T32 = R.RadiationTables(g["integfochi"], g["integfochi_min"], g["integfochi_max"], g["xi_table"], g["xi_min"],
+                            g["xi_max"], g["xi_axis1_min"], f_dn, f_cl, inv_es)
+    T32.set_fp32_math(True)
+    n = 400000
+    mom, E, B, w = beam(n, 5)
+    res, times = {}, {}
+    for name, tab in (("fp64", T), ("fp32", T32)):
+        m, tau = cu(mom), cu(np.full(n, -1.0))
+        tot, nem = 0.0, 0
+        radiation.monte_carlo(tab, 0.1, 1.0, -1.0, m.clone(), cu(w), tau.clone(), cu(E), cu(B), seed=3, step=99)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for step in range(3):
+            r, e = radiation.monte_carlo(tab, 0.1, 1.0, -1.0, m, cu(w), tau, cu(E), cu(B), seed=3, step=step)
+            tot += r
+            nem += e
+        e1.record()
+        torch.cuda.synchronize()
+        times[name] = e0.elapsed_time(e1)
+        res[name] = (tot, nem, m.cpu().numpy())
+    (t64, n64, m64), (t32, n32, m32) = res["fp64"], res["fp32"]
+    assert abs(n32 - n64) <= 0.002 * n64, (n32, n64)
+    assert abs(t32 - t64) <= 0.005 * t64, (t32, t64)
+    dp = np.abs(m32 - m64).max(axis=0) / np.abs(m64).max(axis=0)
+    assert np.mean(dp < 1e-4) > 0.95, np.mean(dp < 1e-4)
+    g64 = np.sqrt(1 + (m64 ** 2).sum(axis=0))
+    g32 = np.sqrt(1 + (m32 ** 2).sum(axis=0))
+    h64, edges = np.histogram(g64, bins=40)
+    h32, _ = np.histogram(g32, bins=edges)
+    assert np.abs(h32 - h64).sum() <= 0.02 * n
+    assert times["fp32"] < times["fp64"], times
+    print(f"\nMonte Carlo 3 passes over {n}: fp64 {times['fp64']:.2f} ms, fp32 math {times['fp32']:.2f} ms")
+    T32.close()
+
+
 def test_mlp_gradients_match_cpu_oracle(rad):
     radiation, _, _ = rad
     from oracle import mlp as M

@@ -16,16 +16,10 @@ import oracle
 
 @pytest.fixture(scope="module")
 def tables(golden_rad):
-    g = golden_rad
-    c = 299792458.0
-    omega = 2.0 * np.pi * c / 1e-6
-    # rate factors of the order of those at lambda_r = 1 um; the properties tested hold for any positive factors
-    re = 2.8179403262e-15
-    lam_c = 3.8615926796e-13
-    f_cl = 2.0 / 3.0 * re * omega / c
-    f_dn = np.sqrt(3.0) * 1.0 / 137.035999084 / (2.0 * np.pi * lam_c * omega / c) / (np.sqrt(3.0) / (2.0 * np.pi))
-    inv_es = 1.0 / (1.32e18 / (9.109e-31 * c * omega / 1.602e-19))
-    return oracle.RadTables.from_golden(g, factor_dNph_dt=f_dn, factor_classical=f_cl, inv_norm_E_schwinger=inv_es)
+    from smilei_gb300.radiation import normalised_factors
+    f_dn, f_cl, inv_es = normalised_factors(2.0 * np.pi * 299792458.0 / 1e-6)  # lambda_r = 1 um
+    return oracle.RadTables.from_golden(golden_rad, factor_dNph_dt=f_dn, factor_classical=f_cl,
+                                        inv_norm_E_schwinger=inv_es)
 
 
 def beam(n, seed):
