@@ -402,14 +402,26 @@ constexpr int REC = 8;
 constexpr int NO_SHIFT = 1 | ( 1 << 2 ) | ( 1 << 4 ); // packed shifts (s + 1 per 2 bits) of a particle that keeps its node
 constexpr int GONE_RECORD = 1 << 8;                  // record of a particle removed at an open boundary: deposits nothing
 
-template <int DIM, bool MIXED, int KIND, bool CELLS>
+// FIXT: the tile is the default shape (4x4x4 in 3D, 8x8 in 2D), known at compile
+// time, so tile and stencil offsets fold into immediates.
+template <int DIM, bool MIXED, int KIND, bool CELLS, bool FIXT = false>
 __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_particles(
-    GridInfo g, Fields<typename std::conditional<MIXED, float, double>::type> f, SpecParams sp, PBuf<MIXED> in,
+    GridInfo g_arg, Fields<typename std::conditional<MIXED, float, double>::type> f, SpecParams sp, PBuf<MIXED> in,
     PBuf<MIXED> out, const int64_t *__restrict__ seg_start, const int *__restrict__ cap,
     const int *__restrict__ count_in, int *__restrict__ count_out, PBuf<MIXED> ovf, int *__restrict__ ovf_tile,
     int *__restrict__ ovf_count, int ovf_cap, int *__restrict__ status, int nmax, int *__restrict__ removed )
 {
     using T = typename std::conditional<MIXED, float, double>::type;
+    GridInfo g = g_arg;
+    if constexpr( FIXT ) {
+        constexpr int t = DIM == 3 ? 4 : 8, ts = DIM == 3 ? 2 : 3;
+        g.T[0] = t;
+        g.T[1] = t;
+        g.T[2] = DIM == 3 ? t : 1;
+        g.tshift[0] = ts;
+        g.tshift[1] = ts;
+        g.tshift[2] = DIM == 3 ? ts : 0;
+    }
     extern __shared__ __align__( 16 ) unsigned char smem_raw[];
     T *sF = reinterpret_cast<T *>( smem_raw );
     const TileDims td = tile_dims( g );
@@ -1983,7 +1995,9 @@ int launch_particles( sg_sim *S, SpeciesState &s, cudaStream_t st )
         const int fit = fixed < CELLS_SMEM_TARGET ? ( int )( ( CELLS_SMEM_TARGET - fixed ) / per ) : 0;
         chunk = std::max( 1, std::min( s.max_cap, fit & ~31 ) );
         if( tc <= ( DIM == 3 ? 64 : 128 ) && fit >= 128 ) {
-            kern = k_step_particles<DIM, MIXED, KIND, true>;
+            const GridInfo &g = S->g;
+            const bool fixt = DIM == 3 ? ( g.T[0] == 4 && g.T[1] == 4 && g.T[2] == 4 ) : ( g.T[0] == 8 && g.T[1] == 8 );
+            kern = fixt ? k_step_particles<DIM, MIXED, KIND, true, true> : k_step_particles<DIM, MIXED, KIND, true>;
             smem += cells_smem_bytes( tc, chunk );
         }
     }
