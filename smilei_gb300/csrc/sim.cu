@@ -402,16 +402,43 @@ constexpr int REC = 8;
 constexpr int NO_SHIFT = 1 | ( 1 << 2 ) | ( 1 << 4 ); // packed shifts (s + 1 per 2 bits) of a particle that keeps its node
 constexpr int GONE_RECORD = 1 << 8;                  // record of a particle removed at an open boundary: deposits nothing
 
+// Shared memory of the per-cell mode: REC planes of nmax floats, a count and a
+// start per cell, a packed (cell, rank) word and a list word per particle, a
+// cell byte per slot.
+constexpr size_t CELLS_SMEM_TARGET = 44 * 1024; // five 128-thread blocks per SM
+constexpr size_t cells_smem_bytes( int tc, int nmax )
+{
+    return ( size_t )REC * 4 * nmax + ( size_t )8 * tc + ( size_t )8 * nmax + ( ( ( size_t )nmax + 15 ) & ~( size_t )15 );
+}
+
+// Particles per chunk of the per-cell mode that fit CELLS_SMEM_TARGET with a tile
+// of tc cells whose field and current tiles take tile_bytes (0: none fit).
+constexpr int cells_chunk_fit( size_t tile_bytes, int tc )
+{
+    const size_t fixed = tile_bytes + cells_smem_bytes( tc, 0 ) + 16;
+    const size_t per = ( size_t )REC * 4 + 8 + 1; // planes, rank and list words, cell byte
+    return fixed < CELLS_SMEM_TARGET ? ( int )( ( CELLS_SMEM_TARGET - fixed ) / per ) : 0;
+}
+
+// The chunk of the default tile shapes (4x4x4 in 3D, 8x8 in 2D; FP32 tiles of
+// 6 field and 3 current components with T + 3 and T + 4 points per dimension).
+constexpr int fixt_chunk( int dim )
+{
+    return dim == 3 ? cells_chunk_fit( ( size_t )( 6 * 7 * 7 * 7 + 3 * 8 * 8 * 8 ) * 4, 64 ) & ~31
+                    : cells_chunk_fit( ( size_t )( 6 * 11 * 11 + 3 * 12 * 12 ) * 4, 64 ) & ~31;
+}
+
 // FIXT: the tile is the default shape (4x4x4 in 3D, 8x8 in 2D), known at compile
-// time, so tile and stencil offsets fold into immediates.
+// time, so tile and stencil offsets fold into immediates; its chunk is fixt_chunk.
 template <int DIM, bool MIXED, int KIND, bool CELLS, bool FIXT = false>
 __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_particles(
     GridInfo g_arg, Fields<typename std::conditional<MIXED, float, double>::type> f, SpecParams sp, PBuf<MIXED> in,
     PBuf<MIXED> out, const int64_t *__restrict__ seg_start, const int *__restrict__ cap,
     const int *__restrict__ count_in, int *__restrict__ count_out, PBuf<MIXED> ovf, int *__restrict__ ovf_tile,
-    int *__restrict__ ovf_count, int ovf_cap, int *__restrict__ status, int nmax, int *__restrict__ removed )
+    int *__restrict__ ovf_count, int ovf_cap, int *__restrict__ status, int nmax_arg, int *__restrict__ removed )
 {
     using T = typename std::conditional<MIXED, float, double>::type;
+    const int nmax = FIXT ? fixt_chunk( DIM ) : nmax_arg;
     GridInfo g = g_arg;
     if constexpr( FIXT ) {
         constexpr int t = DIM == 3 ? 4 : 8, ts = DIM == 3 ? 2 : 3;
@@ -1953,14 +1980,6 @@ Fields<T> field_view( sg_sim *S )
 // comp 0..2 E, 3..5 B, 6..8 B_m, 9..11 J -> staggering flags
 inline int comp_stag( int comp, int d ) { return comp < 3 ? stag( comp, d ) : ( comp < 9 ? stag( 3 + ( comp % 3 ), d ) : stag( comp - 9, d ) ); }
 
-// Shared memory of the per-cell mode: REC planes of nmax floats, a count and a
-// start per cell, a packed (cell, rank) word and a list word per particle, a
-// cell byte per slot.
-constexpr size_t CELLS_SMEM_TARGET = 44 * 1024; // five 128-thread blocks per SM
-inline size_t cells_smem_bytes( int tc, int nmax )
-{
-    return ( size_t )REC * 4 * nmax + ( size_t )8 * tc + ( size_t )8 * nmax + ( ( ( size_t )nmax + 15 ) & ~( size_t )15 );
-}
 
 template <int DIM, bool MIXED, int KIND>
 int launch_particles( sg_sim *S, SpeciesState &s, cudaStream_t st )
@@ -1990,13 +2009,16 @@ int launch_particles( sg_sim *S, SpeciesState &s, cudaStream_t st )
     int chunk = s.max_cap;
     if constexpr( MIXED ) {
         const int tc = S->g.T[0] * S->g.T[1] * ( DIM == 3 ? S->g.T[2] : 1 );
-        const size_t per = ( size_t )REC * 4 + 8 + 1; // planes, rank and list words, cell byte
-        const size_t fixed = smem + cells_smem_bytes( tc, 0 ) + 16;
-        const int fit = fixed < CELLS_SMEM_TARGET ? ( int )( ( CELLS_SMEM_TARGET - fixed ) / per ) : 0;
+        const int fit = cells_chunk_fit( smem, tc );
         chunk = std::max( 1, std::min( s.max_cap, fit & ~31 ) );
         if( tc <= ( DIM == 3 ? 64 : 128 ) && fit >= 128 ) {
             const GridInfo &g = S->g;
             const bool fixt = DIM == 3 ? ( g.T[0] == 4 && g.T[1] == 4 && g.T[2] == 4 ) : ( g.T[0] == 8 && g.T[1] == 8 );
+            if( fixt ) {
+                // the chunk is a compile-time constant of the kernel
+                chunk = fixt_chunk( DIM );
+                if( chunk != ( fit & ~31 ) ) return set_error( SG_ERR_ARG, "per-cell chunk mismatch (%d, %d)", chunk, fit & ~31 );
+            }
             kern = fixt ? k_step_particles<DIM, MIXED, KIND, true, true> : k_step_particles<DIM, MIXED, KIND, true>;
             smem += cells_smem_bytes( tc, chunk );
         }
