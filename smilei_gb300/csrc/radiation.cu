@@ -427,7 +427,7 @@ __global__ void k_monte_carlo( RadTab t, MlpView m, int use_mlp, int64_t n, doub
     const int64_t p = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x;
     double rad = 0.0;
     unsigned long long nem = 0;
-    if( p < n ) {
+    if( !F32 && p < n ) {
         double px = mom[p], py = mom[n + p], pz = mom[2 * n + p];
         const double Ex = Ep[p], Ey = Ep[n + p], Ez = Ep[2 * n + p];
         const double Bx = Bp[p], By = Bp[n + p], Bz = Bp[2 * n + p];
@@ -519,6 +519,98 @@ __global__ void k_monte_carlo( RadTab t, MlpView m, int use_mlp, int64_t n, doub
         mom[2 * n + p] = pz;
         tau[p] = tp;
         if( chi_out ) chi_out[p] = last_chi;
+    }
+    if( F32 && p < n ) {
+        // FP32 arithmetic for gamma, chi, the rates, times and the optical depth; the
+        // momenta and the radiated-energy tally stay FP64
+        double px = mom[p], py = mom[n + p], pz = mom[2 * n + p];
+        const float Ex = ( float )Ep[p], Ey = ( float )Ep[n + p], Ez = ( float )Ep[2 * n + p];
+        const float Bx = ( float )Bp[p], By = ( float )Bp[n + p], Bz = ( float )Bp[2 * n + p];
+        const float k_chi = ( float )( fabs( qm2 ) * t.inv_es );
+        const float dtf = ( float )dt, min_disc = ( float )t.min_disc, min_cont = ( float )t.min_cont;
+        float tp = ( float )tau[p];
+        uint32_t rs = rng_init( seed, first_id + ( uint32_t )p, step );
+        float local_time = 0.0f, emission_time = 0.0f, last_chi = 0.0f;
+        int it = 0, i_photon = 0;
+        // the optical depth counts as spent at or below eps_tau (the FP64 pass uses 1e-100):
+        // a residual of the subtraction below it would otherwise never reach zero and
+        // stall the particle's emissions
+        const float eps_tau = 1e-30f;
+        while( local_time < dtf && it < 100 ) {
+            const float fx = ( float )px, fy = ( float )py, fz = ( float )pz;
+            const float g = sqrtf( 1.0f + fx * fx + fy * fy + fz * fz );
+            if( g < 1.1f ) break;
+            const float a = Ex * fx + Ey * fy + Ez * fz;
+            const float b = g * Ex - By * fz + Bz * fy;
+            const float c = g * Ey - Bz * fx + Bx * fz;
+            const float d = g * Ez - Bx * fy + By * fx;
+            const float chi = k_chi * sqrtf( fabsf( a * a - b * b - c * c - d * d ) );
+            last_chi = chi;
+            if( chi > min_disc && tp <= eps_tau ) {
+                while( tp <= eps_tau ) tp = -logf( fmaxf( 1.0f - ( float )rng_uniform( rs ), 5.9604645e-8f ) );
+            }
+            if( tp > eps_tau ) {
+                const float rate = tab_yield32( t, chi, g );
+                emission_time = fminf( tp / rate, dtf - local_time );
+                tp -= rate * emission_time;
+                if( tp <= eps_tau ) {
+                    const double u = rng_uniform( rs );
+                    double pchi;
+                    if( use_mlp && !mlp_masked( m, chi, u ) ) {
+                        if constexpr( H > 0 ) pchi = mlp_photon_chi_smem<H>( m, sw, chi, u );
+                        else pchi = mlp_photon_chi( m, chi, u );
+                    } else {
+                        pchi = ( double )tab_photon_chi32( t, chi, ( float )u );
+                    }
+                    const double gd = sqrt( 1.0 + px * px + py * py + pz * pz );
+                    const double pg = pchi / ( double )chi * ( gd - 1.0 );
+                    const double f = ( double )( ( float )pg / sqrtf( g * g - 1.0f ) );
+                    px -= px * f;
+                    py -= py * f;
+                    pz -= pz * f;
+                    if( ph.count && pg >= ph.threshold && i_photon < ph.max_emissions ) {
+                        const double inv = 1.0 / sqrt( px * px + py * py + pz * pz );
+                        const unsigned long long o0 = atomicAdd( ph.count, ( unsigned long long )ph.sampling );
+                        for( int k = 0; k < ph.sampling; k++ ) {
+                            const unsigned long long o = o0 + ( unsigned long long )k;
+                            if( o >= ( unsigned long long )ph.cap ) break;
+                            for( int dd = 0; dd < ph.ndim; dd++ ) ph.ph_pos[dd * ph.cap + o] = ph.pos[dd * n + p];
+                            ph.ph_mom[o] = pg * px * inv;
+                            ph.ph_mom[ph.cap + o] = pg * py * inv;
+                            ph.ph_mom[2 * ph.cap + o] = pg * pz * inv;
+                            ph.ph_w[o] = w[p] * ( 1.0 / ph.sampling );
+                            ph.ph_chi[o] = pchi;
+                            ph.ph_tau[o] = -1.0;
+                        }
+                        i_photon++;
+                    } else {
+                        rad += w[p] * ( gd - sqrt( 1.0 + px * px + py * py + pz * pz ) );
+                    }
+                    nem++;
+                    tp = -1.0f;
+                }
+                it++;
+                local_time += emission_time;
+            } else if( chi <= min_disc && tp <= eps_tau && chi > min_cont ) {
+                emission_time = dtf - local_time;
+                const float aa = 1.0f + 4.8f * ( 1.0f + chi ) * logf( 1.0f + 1.7f * chi ) + 2.44f * chi * chi;
+                const float e = ( 1.0f / cbrtf( aa * aa ) ) * emission_time * chi * chi * ( float )t.factor_classical;
+                const double tmp = ( double )( e * g / ( g * g - 1.0f ) );
+                const double gd = sqrt( 1.0 + px * px + py * py + pz * pz );
+                px -= tmp * px;
+                py -= tmp * py;
+                pz -= tmp * pz;
+                rad += w[p] * ( gd - sqrt( 1.0 + px * px + py * py + pz * pz ) );
+                local_time = dtf;
+            } else {
+                local_time = dtf;
+            }
+        }
+        mom[p] = px;
+        mom[n + p] = py;
+        mom[2 * n + p] = pz;
+        tau[p] = ( double )tp;
+        if( chi_out ) chi_out[p] = ( double )last_chi;
     }
     // block reduction of the tallies
     __shared__ double srad[32];
