@@ -366,11 +366,16 @@ struct MlpShared {
     float4 W2v[H * H / 4]; // row r, columns 4c..4c+3 at r * H / 4 + c
 };
 
-template <int H>
+// TRANSPOSED: W2 stored column-major (W2T[i * H + r] = W2[r][i]) for the
+// warp-cooperative evaluation, where lane r reads row r of consecutive columns.
+template <int H, bool TRANSPOSED = false>
 __device__ __forceinline__ void mlp_stage( const MlpView &m, MlpShared<H> &w )
 {
     float *W2 = reinterpret_cast<float *>( w.W2v );
-    for( int k = threadIdx.x; k < H * H; k += blockDim.x ) W2[k] = m.W2[k];
+    for( int k = threadIdx.x; k < H * H; k += blockDim.x ) {
+        if constexpr( TRANSPOSED ) W2[( k % H ) * H + k / H] = m.W2[k];
+        else W2[k] = m.W2[k];
+    }
     for( int k = threadIdx.x; k < H; k += blockDim.x ) {
         w.W1[2 * k] = m.W1[2 * k];
         w.W1[2 * k + 1] = m.W1[2 * k + 1];
@@ -407,6 +412,44 @@ __device__ __forceinline__ double mlp_photon_chi_smem( const MlpView &m, const M
     return chi * ( double )exp10f( y * m.out_scale );
 }
 
+// The network evaluated by a whole warp for one (chi, xi) (every lane passes the
+// same values; W2 staged transposed): lane l owns hidden units l and l + 32, the
+// first layer's outputs travel by shuffles, the last layer is a warp sum.  About
+// H shuffles and 2H FMAs per lane instead of H^2 FMAs in one thread.
+template <int H>
+__device__ __forceinline__ float mlp_coop( const MlpView &m, const MlpShared<H> &w, float chi, float xi, int lane )
+{
+    constexpr int K = H >= 32 ? H / 32 : 1;
+    const float u0 = 2.0f * ( log10f( chi ) - m.lmin ) / m.lspan - 1.0f;
+    const float u1 = 2.0f * xi - 1.0f;
+    const float *W2T = reinterpret_cast<const float *>( w.W2v );
+    float h[K], acc[K];
+#pragma unroll
+    for( int k = 0; k < K; k++ ) {
+        const int j = lane + 32 * k;
+        h[k] = j < H ? tanh_fast( fmaf( w.W1[2 * j], u0, fmaf( w.W1[2 * j + 1], u1, w.b1[j] ) ) ) : 0.0f;
+        acc[k] = j < H ? w.b2[j] : 0.0f;
+    }
+#pragma unroll 8
+    for( int i = 0; i < H; i++ ) {
+        const float hv = __shfl_sync( 0xffffffffu, h[i >> 5], i & 31 );
+#pragma unroll
+        for( int k = 0; k < K; k++ ) {
+            const int r = lane + 32 * k;
+            if( r < H ) acc[k] = fmaf( W2T[i * H + r], hv, acc[k] );
+        }
+    }
+    float y = 0.0f;
+#pragma unroll
+    for( int k = 0; k < K; k++ ) {
+        const int r = lane + 32 * k;
+        if( r < H ) y = fmaf( w.W3[r], tanh_fast( acc[k] ), y );
+    }
+#pragma unroll
+    for( int o = 16; o > 0; o >>= 1 ) y += __shfl_xor_sync( 0xffffffffu, y, o );
+    return y + w.b3;
+}
+
 // F32: the table lookups, the optical-depth draw and the continuous-loss formula in
 // FP32 arithmetic (FP64 is a small fraction of FP32 throughput on this GPU); chi,
 // gamma, times and momenta stay FP64.  The random stream is the FP64 pass's.
@@ -421,7 +464,7 @@ __global__ void k_monte_carlo( RadTab t, MlpView m, int use_mlp, int64_t n, doub
 {
     __shared__ MlpShared<H == 0 ? 4 : H> sw;
     if constexpr( H > 0 ) {
-        mlp_stage<H>( m, sw );
+        mlp_stage<H, F32>( m, sw );
         __syncthreads();
     }
     const int64_t p = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x;
@@ -520,97 +563,140 @@ __global__ void k_monte_carlo( RadTab t, MlpView m, int use_mlp, int64_t n, doub
         tau[p] = tp;
         if( chi_out ) chi_out[p] = last_chi;
     }
-    if( F32 && p < n ) {
+    if constexpr( F32 ) {
         // FP32 arithmetic for gamma, chi, the rates, times and the optical depth; the
-        // momenta and the radiated-energy tally stay FP64
-        double px = mom[p], py = mom[n + p], pz = mom[2 * n + p];
-        const float Ex = ( float )Ep[p], Ey = ( float )Ep[n + p], Ez = ( float )Ep[2 * n + p];
-        const float Bx = ( float )Bp[p], By = ( float )Bp[n + p], Bz = ( float )Bp[2 * n + p];
+        // momenta and the radiated-energy tally stay FP64.  The loop is warp-synchronous
+        // (every lane steps until all are done) so that the lanes that emit through the
+        // network can evaluate it together, one emission after another.
+        const int lane = threadIdx.x & 31;
+        bool active = p < n;
+        const int64_t q = active ? p : 0;
+        double px = 0.0, py = 0.0, pz = 0.0;
+        float Ex = 0.0f, Ey = 0.0f, Ez = 0.0f, Bx = 0.0f, By = 0.0f, Bz = 0.0f, tp = 0.0f;
+        if( active ) {
+            px = mom[q];
+            py = mom[n + q];
+            pz = mom[2 * n + q];
+            Ex = ( float )Ep[q];
+            Ey = ( float )Ep[n + q];
+            Ez = ( float )Ep[2 * n + q];
+            Bx = ( float )Bp[q];
+            By = ( float )Bp[n + q];
+            Bz = ( float )Bp[2 * n + q];
+            tp = ( float )tau[q];
+        }
         const float k_chi = ( float )( fabs( qm2 ) * t.inv_es );
         const float dtf = ( float )dt, min_disc = ( float )t.min_disc, min_cont = ( float )t.min_cont;
-        float tp = ( float )tau[p];
-        uint32_t rs = rng_init( seed, first_id + ( uint32_t )p, step );
-        float local_time = 0.0f, emission_time = 0.0f, last_chi = 0.0f;
-        int it = 0, i_photon = 0;
         // the optical depth counts as spent at or below eps_tau (the FP64 pass uses 1e-100):
         // a residual of the subtraction below it would otherwise never reach zero and
         // stall the particle's emissions
         const float eps_tau = 1e-30f;
-        while( local_time < dtf && it < 100 ) {
-            const float fx = ( float )px, fy = ( float )py, fz = ( float )pz;
-            const float g = sqrtf( 1.0f + fx * fx + fy * fy + fz * fz );
-            if( g < 1.1f ) break;
-            const float a = Ex * fx + Ey * fy + Ez * fz;
-            const float b = g * Ex - By * fz + Bz * fy;
-            const float c = g * Ey - Bz * fx + Bx * fz;
-            const float d = g * Ez - Bx * fy + By * fx;
-            const float chi = k_chi * sqrtf( fabsf( a * a - b * b - c * c - d * d ) );
-            last_chi = chi;
-            if( chi > min_disc && tp <= eps_tau ) {
-                while( tp <= eps_tau ) tp = -logf( fmaxf( 1.0f - ( float )rng_uniform( rs ), 5.9604645e-8f ) );
-            }
-            if( tp > eps_tau ) {
-                const float rate = tab_yield32( t, chi, g );
-                emission_time = fminf( tp / rate, dtf - local_time );
-                tp -= rate * emission_time;
-                if( tp <= eps_tau ) {
-                    const double u = rng_uniform( rs );
-                    double pchi;
-                    if( use_mlp && !mlp_masked( m, chi, u ) ) {
-                        if constexpr( H > 0 ) pchi = mlp_photon_chi_smem<H>( m, sw, chi, u );
-                        else pchi = mlp_photon_chi( m, chi, u );
-                    } else {
-                        pchi = ( double )tab_photon_chi32( t, chi, ( float )u );
+        uint32_t rs = rng_init( seed, first_id + ( uint32_t )q, step );
+        float local_time = 0.0f, last_chi = 0.0f;
+        int it = 0, i_photon = 0;
+        while( __any_sync( 0xffffffffu, active ) ) {
+            bool emit = false, net = false;
+            float g = 0.0f, chi = 0.0f, u32 = 0.0f;
+            double pchi = 0.0;
+            if( active && !( local_time < dtf && it < 100 ) ) active = false;
+            if( active ) {
+                const float fx = ( float )px, fy = ( float )py, fz = ( float )pz;
+                g = sqrtf( 1.0f + fx * fx + fy * fy + fz * fz );
+                if( g < 1.1f ) {
+                    active = false;
+                } else {
+                    const float a = Ex * fx + Ey * fy + Ez * fz;
+                    const float b = g * Ex - By * fz + Bz * fy;
+                    const float c = g * Ey - Bz * fx + Bx * fz;
+                    const float d = g * Ez - Bx * fy + By * fx;
+                    chi = k_chi * sqrtf( fabsf( a * a - b * b - c * c - d * d ) );
+                    last_chi = chi;
+                    if( chi > min_disc && tp <= eps_tau ) {
+                        while( tp <= eps_tau ) tp = -logf( fmaxf( 1.0f - ( float )rng_uniform( rs ), 5.9604645e-8f ) );
                     }
-                    const double gd = sqrt( 1.0 + px * px + py * py + pz * pz );
-                    const double pg = pchi / ( double )chi * ( gd - 1.0 );
-                    const double f = ( double )( ( float )pg / sqrtf( g * g - 1.0f ) );
-                    px -= px * f;
-                    py -= py * f;
-                    pz -= pz * f;
-                    if( ph.count && pg >= ph.threshold && i_photon < ph.max_emissions ) {
-                        const double inv = 1.0 / sqrt( px * px + py * py + pz * pz );
-                        const unsigned long long o0 = atomicAdd( ph.count, ( unsigned long long )ph.sampling );
-                        for( int k = 0; k < ph.sampling; k++ ) {
-                            const unsigned long long o = o0 + ( unsigned long long )k;
-                            if( o >= ( unsigned long long )ph.cap ) break;
-                            for( int dd = 0; dd < ph.ndim; dd++ ) ph.ph_pos[dd * ph.cap + o] = ph.pos[dd * n + p];
-                            ph.ph_mom[o] = pg * px * inv;
-                            ph.ph_mom[ph.cap + o] = pg * py * inv;
-                            ph.ph_mom[2 * ph.cap + o] = pg * pz * inv;
-                            ph.ph_w[o] = w[p] * ( 1.0 / ph.sampling );
-                            ph.ph_chi[o] = pchi;
-                            ph.ph_tau[o] = -1.0;
+                    if( tp > eps_tau ) {
+                        const float rate = tab_yield32( t, chi, g );
+                        const float emission_time = fminf( tp / rate, dtf - local_time );
+                        tp -= rate * emission_time;
+                        if( tp <= eps_tau ) {
+                            const double u = rng_uniform( rs );
+                            emit = true;
+                            if( use_mlp && !mlp_masked( m, chi, u ) ) {
+                                if constexpr( H > 0 ) {
+                                    net = true;
+                                    u32 = ( float )u;
+                                } else {
+                                    pchi = mlp_photon_chi( m, chi, u );
+                                }
+                            } else {
+                                pchi = ( double )tab_photon_chi32( t, chi, ( float )u );
+                            }
                         }
-                        i_photon++;
+                        it++;
+                        local_time += emission_time;
+                    } else if( chi <= min_disc && tp <= eps_tau && chi > min_cont ) {
+                        const float emission_time = dtf - local_time;
+                        const float aa = 1.0f + 4.8f * ( 1.0f + chi ) * logf( 1.0f + 1.7f * chi ) + 2.44f * chi * chi;
+                        const float e = ( 1.0f / cbrtf( aa * aa ) ) * emission_time * chi * chi * ( float )t.factor_classical;
+                        const double tmp = ( double )( e * g / ( g * g - 1.0f ) );
+                        const double gd = sqrt( 1.0 + px * px + py * py + pz * pz );
+                        px -= tmp * px;
+                        py -= tmp * py;
+                        pz -= tmp * pz;
+                        rad += w[q] * ( gd - sqrt( 1.0 + px * px + py * py + pz * pz ) );
+                        local_time = dtf;
                     } else {
-                        rad += w[p] * ( gd - sqrt( 1.0 + px * px + py * py + pz * pz ) );
+                        local_time = dtf;
                     }
-                    nem++;
-                    tp = -1.0f;
                 }
-                it++;
-                local_time += emission_time;
-            } else if( chi <= min_disc && tp <= eps_tau && chi > min_cont ) {
-                emission_time = dtf - local_time;
-                const float aa = 1.0f + 4.8f * ( 1.0f + chi ) * logf( 1.0f + 1.7f * chi ) + 2.44f * chi * chi;
-                const float e = ( 1.0f / cbrtf( aa * aa ) ) * emission_time * chi * chi * ( float )t.factor_classical;
-                const double tmp = ( double )( e * g / ( g * g - 1.0f ) );
+            }
+            if constexpr( H > 0 ) {
+                // the emitting lanes' network evaluations, by the whole warp
+                unsigned req = __ballot_sync( 0xffffffffu, net );
+                while( req ) {
+                    const int src = __ffs( req ) - 1;
+                    req &= req - 1;
+                    const float cs = __shfl_sync( 0xffffffffu, chi, src ), us = __shfl_sync( 0xffffffffu, u32, src );
+                    const float y = mlp_coop<H>( m, sw, cs, us, lane );
+                    if( lane == src ) pchi = ( double )chi * ( double )exp10f( y * m.out_scale );
+                }
+            }
+            if( emit ) {
                 const double gd = sqrt( 1.0 + px * px + py * py + pz * pz );
-                px -= tmp * px;
-                py -= tmp * py;
-                pz -= tmp * pz;
-                rad += w[p] * ( gd - sqrt( 1.0 + px * px + py * py + pz * pz ) );
-                local_time = dtf;
-            } else {
-                local_time = dtf;
+                const double pg = pchi / ( double )chi * ( gd - 1.0 );
+                const double f = ( double )( ( float )pg / sqrtf( g * g - 1.0f ) );
+                px -= px * f;
+                py -= py * f;
+                pz -= pz * f;
+                if( ph.count && pg >= ph.threshold && i_photon < ph.max_emissions ) {
+                    const double inv = 1.0 / sqrt( px * px + py * py + pz * pz );
+                    const unsigned long long o0 = atomicAdd( ph.count, ( unsigned long long )ph.sampling );
+                    for( int k = 0; k < ph.sampling; k++ ) {
+                        const unsigned long long o = o0 + ( unsigned long long )k;
+                        if( o >= ( unsigned long long )ph.cap ) break;
+                        for( int dd = 0; dd < ph.ndim; dd++ ) ph.ph_pos[dd * ph.cap + o] = ph.pos[dd * n + q];
+                        ph.ph_mom[o] = pg * px * inv;
+                        ph.ph_mom[ph.cap + o] = pg * py * inv;
+                        ph.ph_mom[2 * ph.cap + o] = pg * pz * inv;
+                        ph.ph_w[o] = w[q] * ( 1.0 / ph.sampling );
+                        ph.ph_chi[o] = pchi;
+                        ph.ph_tau[o] = -1.0;
+                    }
+                    i_photon++;
+                } else {
+                    rad += w[q] * ( gd - sqrt( 1.0 + px * px + py * py + pz * pz ) );
+                }
+                nem++;
+                tp = -1.0f;
             }
         }
-        mom[p] = px;
-        mom[n + p] = py;
-        mom[2 * n + p] = pz;
-        tau[p] = ( double )tp;
-        if( chi_out ) chi_out[p] = ( double )last_chi;
+        if( p < n ) {
+            mom[p] = px;
+            mom[n + p] = py;
+            mom[2 * n + p] = pz;
+            tau[p] = ( double )tp;
+            if( chi_out ) chi_out[p] = ( double )last_chi;
+        }
     }
     // block reduction of the tallies
     __shared__ double srad[32];
