@@ -154,3 +154,44 @@ def test_sort_rejects_particles_outside_the_patch(ops):
     part = ops.Particles(cu(pos), cu(np.zeros((3, 2))), cu(np.ones(2)), cu(np.ones(2), torch.int16))
     with pytest.raises(SmileiGPUError, match="outside"):
         ops.sortParticles(part, [8], [0.0], [0.1])
+
+
+def test_empty_inputs_are_no_ops(ops):
+    """Zero particles (an empty bin or species): every operator returns without touching
+    the fields; the sort returns empty bins."""
+    geom = ops.PatchGeometry([8, 8, 8], [0.1, 0.1, 0.1])
+    em = ops.ElectroMagn(geom)
+    for comp in ("Ex_", "By_m", "Jx_"):
+        getattr(em, comp).fill_(1.5)
+    part = ops.Particles(torch.zeros((3, 0), dtype=torch.float64, device="cuda"),
+                         torch.zeros((3, 0), dtype=torch.float64, device="cuda"),
+                         torch.zeros(0, dtype=torch.float64, device="cuda"),
+                         torch.zeros(0, dtype=torch.int16, device="cuda"))
+    smpi = ops.SmileiMPI(3, 0)
+    ops.Interpolator3D2Order(geom).fieldsWrapper(em, part, smpi)
+    ops.PusherFactory("boris", 0.05, 1.0, 3)(part, smpi)
+    ops.Projector3D2Order(geom, 0.05).currentsAndDensityWrapper(em, part, smpi)
+    first, last, keys = ops.sortParticles(part, [8, 8, 8], [0.0, 0.0, 0.0], [0.1, 0.1, 0.1])
+    torch.cuda.synchronize()
+    assert float(em.Jx_.min()) == 1.5 and float(em.Jx_.max()) == 1.5
+    assert keys.numel() == 0 and int(first.sum()) == 0 and int(last.sum()) == 0
+
+
+def test_resident_step_with_an_empty_species(ops):
+    """A species without particles steps alongside a populated one; the result equals
+    the populated species alone."""
+    from smilei_gb300 import simulation, synthetic
+    n_cells, cl = [16, 16], [0.1, 0.1]
+    dt = 0.95 / np.sqrt(2 / 0.01)
+    pos, mom, w = synthetic.thermal_plasma(n_cells, cl, 4, 0.1, 3)
+    out = []
+    for with_empty in (False, True):
+        sim = simulation.Simulation(n_cells, cl, dt, form="fp64")
+        if with_empty:
+            sim.add_species(1.0, -1.0, "boris", np.zeros((2, 0)), np.zeros((3, 0)), np.zeros(0))
+        sim.add_species(1.0, -1.0, "boris", pos, mom, w)
+        sim.step(5)
+        out.append(sim.get_field("Jx"))
+        assert sim.species_count(1 if with_empty else 0) == w.size
+        sim.close()
+    assert rel_err(out[1], out[0]) <= 1e-12
