@@ -154,6 +154,8 @@ typedef struct sg_sim_config {
 #define SG_BC_OPEN 1
 
 typedef struct sg_sim sg_sim;
+typedef struct sg_rad_tables sg_rad_tables; /* radiation tables (below) */
+typedef struct sg_mlp sg_mlp;               /* learned inverse CDF (below) */
 
 int sg_sim_create( const sg_sim_config *cfg, sg_sim **out );
 int sg_sim_destroy( sg_sim *sim );
@@ -268,6 +270,21 @@ int sg_sim_set_species_profile( sg_sim *sim, int species, const double *profile,
  * x every cell along y (z), as the reference does for its initial plasma. */
 int sg_sim_fill_species( sg_sim *sim, int species, int x0_cell, int x1_cell );
 
+/* Monte-Carlo radiation reaction of a species inside the resident step (2D mixed form):
+ * before each push (Species::dynamics, src/Species/Species.cpp:583-640) every particle of
+ * the species gets its E and B_m by the order-2 gather and one FP32-arithmetic pass of
+ * RadiationMonteCarlo::operator() (sg_rad_tables_set_fp32_math) with `tables`, and with
+ * the network `mlp` (may be NULL; validated) where its validation passed.  The species
+ * then carries an optical depth per particle (starting spent, -1).  The random stream of
+ * the particle in buffer slot o at step k is (seed, o, k): not the operator pass's.
+ * Photons are tallied, not created.  The tables and the network must outlive the
+ * simulation or the next call. */
+int sg_sim_set_species_radiation( sg_sim *sim, int species, const sg_rad_tables *tables, const sg_mlp *mlp,
+                                  uint32_t seed );
+/* Radiated energy (sum of w (gamma_before - gamma_after)) and number of emissions of a
+ * radiating species since sg_sim_set_species_radiation. */
+int sg_sim_radiation_stats( sg_sim *sim, int species, double *radiated, unsigned long long *emissions );
+
 /* Device time of the last sg_sim_step call split by stage (ms): particles, fold,
  * maxwell, total; and the number of kernel launches per step. */
 int sg_sim_last_timing( sg_sim *sim, double *ms_particles, double *ms_fields, double *ms_total, int *launches_per_step );
@@ -277,8 +294,6 @@ int sg_sim_set_stream( sg_sim *sim, sg_stream_t stream );
 
 /* ---- Monte-Carlo radiation reaction ---- */
 
-typedef struct sg_rad_tables sg_rad_tables;
-typedef struct sg_mlp sg_mlp;
 
 /* Uploads the radiation tables (host arrays, FP64) in the reference's conventions
  * (src/Radiation/Table.cpp:77-110; RadiationTables::initialization,

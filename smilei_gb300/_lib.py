@@ -82,6 +82,8 @@ _SIGNATURES = {
     "sg_sim_window_state": (_I, [_VP, ctypes.POINTER(_I64), ctypes.POINTER(_D), ctypes.POINTER(_I64)]),
     "sg_sim_set_species_profile": (_I, [_VP, _I, _VP, _I, _D, ctypes.c_uint64]),
     "sg_sim_fill_species": (_I, [_VP, _I, _I, _I]),
+    "sg_sim_set_species_radiation": (_I, [_VP, _I, _VP, _VP, ctypes.c_uint32]),
+    "sg_sim_radiation_stats": (_I, [_VP, _I, ctypes.POINTER(_D), ctypes.POINTER(ctypes.c_ulonglong)]),
     "sg_sim_energy": (_I, [_VP, ctypes.POINTER(_D), ctypes.POINTER(_D)]),
     "sg_sim_last_timing": (_I, [_VP, ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.POINTER(_D),
                                 ctypes.POINTER(_I)]),

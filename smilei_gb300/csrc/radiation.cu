@@ -23,6 +23,7 @@
 // src/Tools/Random.h:9-20) and mapped to [0, 1) by x * (1 - 1e-11) / 2^32.
 
 #include "common.cuh"
+#include "resident_rad.cuh"
 
 #include <cmath>
 #include <vector>
@@ -450,6 +451,127 @@ __device__ __forceinline__ float mlp_coop( const MlpView &m, const MlpShared<H> 
     return y + w.b3;
 }
 
+// One particle's Monte-Carlo steps over dt in FP32 arithmetic for gamma, chi, the
+// rates, times and the optical depth (the momenta and the radiated-energy tally stay
+// FP64), RadiationMonteCarlo::operator() (RadiationMonteCarlo.cpp:62-611).  Called by
+// every lane of a warp (inactive lanes too): the loop is warp-synchronous, so that the
+// lanes that emit through the network evaluate it together, one emission after another.
+// ph.count == null: no macro-photons (then q and n are unused).
+template <int H>
+__device__ __forceinline__ void mc_pass_f32( const RadTab &t, const MlpView &m, int use_mlp,
+                                             const MlpShared<H == 0 ? 4 : H> &sw, bool active, double dt, double qm2,
+                                             const float *E3, const float *B3, double &px, double &py, double &pz,
+                                             float &tp, uint32_t &rs, double wgt, double &rad, unsigned long long &nem,
+                                             float &last_chi, const PhotonOut &ph, int64_t q, int64_t n )
+{
+    const int lane = threadIdx.x & 31;
+    const float Ex = E3[0], Ey = E3[1], Ez = E3[2], Bx = B3[0], By = B3[1], Bz = B3[2];
+    const float k_chi = ( float )( fabs( qm2 ) * t.inv_es );
+    const float dtf = ( float )dt, min_disc = ( float )t.min_disc, min_cont = ( float )t.min_cont;
+    // the optical depth counts as spent at or below eps_tau (the FP64 pass uses 1e-100):
+    // a residual of the subtraction below it would otherwise never reach zero and
+    // stall the particle's emissions
+    const float eps_tau = 1e-30f;
+    float local_time = 0.0f;
+    int it = 0, i_photon = 0;
+    while( __any_sync( 0xffffffffu, active ) ) {
+        bool emit = false, net = false;
+        float g = 0.0f, chi = 0.0f, u32 = 0.0f;
+        double pchi = 0.0;
+        if( active && !( local_time < dtf && it < 100 ) ) active = false;
+        if( active ) {
+            const float fx = ( float )px, fy = ( float )py, fz = ( float )pz;
+            g = sqrtf( 1.0f + fx * fx + fy * fy + fz * fz );
+            if( g < 1.1f ) {
+                active = false;
+            } else {
+                const float a = Ex * fx + Ey * fy + Ez * fz;
+                const float b = g * Ex - By * fz + Bz * fy;
+                const float c = g * Ey - Bz * fx + Bx * fz;
+                const float d = g * Ez - Bx * fy + By * fx;
+                chi = k_chi * sqrtf( fabsf( a * a - b * b - c * c - d * d ) );
+                last_chi = chi;
+                if( chi > min_disc && tp <= eps_tau ) {
+                    while( tp <= eps_tau ) tp = -logf( fmaxf( 1.0f - ( float )rng_uniform( rs ), 5.9604645e-8f ) );
+                }
+                if( tp > eps_tau ) {
+                    const float rate = tab_yield32( t, chi, g );
+                    const float emission_time = fminf( tp / rate, dtf - local_time );
+                    tp -= rate * emission_time;
+                    if( tp <= eps_tau ) {
+                        const double u = rng_uniform( rs );
+                        emit = true;
+                        if( use_mlp && !mlp_masked( m, chi, u ) ) {
+                            if constexpr( H > 0 ) {
+                                net = true;
+                                u32 = ( float )u;
+                            } else {
+                                pchi = mlp_photon_chi( m, chi, u );
+                            }
+                        } else {
+                            pchi = ( double )tab_photon_chi32( t, chi, ( float )u );
+                        }
+                    }
+                    it++;
+                    local_time += emission_time;
+                } else if( chi <= min_disc && tp <= eps_tau && chi > min_cont ) {
+                    const float emission_time = dtf - local_time;
+                    const float aa = 1.0f + 4.8f * ( 1.0f + chi ) * logf( 1.0f + 1.7f * chi ) + 2.44f * chi * chi;
+                    const float e = ( 1.0f / cbrtf( aa * aa ) ) * emission_time * chi * chi * ( float )t.factor_classical;
+                    const double tmp = ( double )( e * g / ( g * g - 1.0f ) );
+                    const double gd = sqrt( 1.0 + px * px + py * py + pz * pz );
+                    px -= tmp * px;
+                    py -= tmp * py;
+                    pz -= tmp * pz;
+                    rad += wgt * ( gd - sqrt( 1.0 + px * px + py * py + pz * pz ) );
+                    local_time = dtf;
+                } else {
+                    local_time = dtf;
+                }
+            }
+        }
+        if constexpr( H > 0 ) {
+            // the emitting lanes' network evaluations, by the whole warp
+            unsigned req = __ballot_sync( 0xffffffffu, net );
+            while( req ) {
+                const int src = __ffs( req ) - 1;
+                req &= req - 1;
+                const float cs = __shfl_sync( 0xffffffffu, chi, src ), us = __shfl_sync( 0xffffffffu, u32, src );
+                const float y = mlp_coop<H>( m, sw, cs, us, lane );
+                if( lane == src ) pchi = ( double )chi * ( double )exp10f( y * m.out_scale );
+            }
+        }
+        if( emit ) {
+            const double gd = sqrt( 1.0 + px * px + py * py + pz * pz );
+            const double pg = pchi / ( double )chi * ( gd - 1.0 );
+            const double f = ( double )( ( float )pg / sqrtf( g * g - 1.0f ) );
+            px -= px * f;
+            py -= py * f;
+            pz -= pz * f;
+            if( ph.count && pg >= ph.threshold && i_photon < ph.max_emissions ) {
+                const double inv = 1.0 / sqrt( px * px + py * py + pz * pz );
+                const unsigned long long o0 = atomicAdd( ph.count, ( unsigned long long )ph.sampling );
+                for( int k = 0; k < ph.sampling; k++ ) {
+                    const unsigned long long o = o0 + ( unsigned long long )k;
+                    if( o >= ( unsigned long long )ph.cap ) break;
+                    for( int dd = 0; dd < ph.ndim; dd++ ) ph.ph_pos[dd * ph.cap + o] = ph.pos[dd * n + q];
+                    ph.ph_mom[o] = pg * px * inv;
+                    ph.ph_mom[ph.cap + o] = pg * py * inv;
+                    ph.ph_mom[2 * ph.cap + o] = pg * pz * inv;
+                    ph.ph_w[o] = wgt * ( 1.0 / ph.sampling );
+                    ph.ph_chi[o] = pchi;
+                    ph.ph_tau[o] = -1.0;
+                }
+                i_photon++;
+            } else {
+                rad += wgt * ( gd - sqrt( 1.0 + px * px + py * py + pz * pz ) );
+            }
+            nem++;
+            tp = -1.0f;
+        }
+    }
+}
+
 // F32: the table lookups, the optical-depth draw and the continuous-loss formula in
 // FP32 arithmetic (FP64 is a small fraction of FP32 throughput on this GPU); chi,
 // gamma, times and momenta stay FP64.  The random stream is the FP64 pass's.
@@ -564,133 +686,23 @@ __global__ void k_monte_carlo( RadTab t, MlpView m, int use_mlp, int64_t n, doub
         if( chi_out ) chi_out[p] = last_chi;
     }
     if constexpr( F32 ) {
-        // FP32 arithmetic for gamma, chi, the rates, times and the optical depth; the
-        // momenta and the radiated-energy tally stay FP64.  The loop is warp-synchronous
-        // (every lane steps until all are done) so that the lanes that emit through the
-        // network can evaluate it together, one emission after another.
-        const int lane = threadIdx.x & 31;
-        bool active = p < n;
+        const bool active = p < n;
         const int64_t q = active ? p : 0;
         double px = 0.0, py = 0.0, pz = 0.0;
-        float Ex = 0.0f, Ey = 0.0f, Ez = 0.0f, Bx = 0.0f, By = 0.0f, Bz = 0.0f, tp = 0.0f;
+        float E3[3] = { 0.0f, 0.0f, 0.0f }, B3[3] = { 0.0f, 0.0f, 0.0f }, tp = 0.0f, last_chi = 0.0f;
         if( active ) {
             px = mom[q];
             py = mom[n + q];
             pz = mom[2 * n + q];
-            Ex = ( float )Ep[q];
-            Ey = ( float )Ep[n + q];
-            Ez = ( float )Ep[2 * n + q];
-            Bx = ( float )Bp[q];
-            By = ( float )Bp[n + q];
-            Bz = ( float )Bp[2 * n + q];
+            for( int c = 0; c < 3; c++ ) {
+                E3[c] = ( float )Ep[c * n + q];
+                B3[c] = ( float )Bp[c * n + q];
+            }
             tp = ( float )tau[q];
         }
-        const float k_chi = ( float )( fabs( qm2 ) * t.inv_es );
-        const float dtf = ( float )dt, min_disc = ( float )t.min_disc, min_cont = ( float )t.min_cont;
-        // the optical depth counts as spent at or below eps_tau (the FP64 pass uses 1e-100):
-        // a residual of the subtraction below it would otherwise never reach zero and
-        // stall the particle's emissions
-        const float eps_tau = 1e-30f;
         uint32_t rs = rng_init( seed, first_id + ( uint32_t )q, step );
-        float local_time = 0.0f, last_chi = 0.0f;
-        int it = 0, i_photon = 0;
-        while( __any_sync( 0xffffffffu, active ) ) {
-            bool emit = false, net = false;
-            float g = 0.0f, chi = 0.0f, u32 = 0.0f;
-            double pchi = 0.0;
-            if( active && !( local_time < dtf && it < 100 ) ) active = false;
-            if( active ) {
-                const float fx = ( float )px, fy = ( float )py, fz = ( float )pz;
-                g = sqrtf( 1.0f + fx * fx + fy * fy + fz * fz );
-                if( g < 1.1f ) {
-                    active = false;
-                } else {
-                    const float a = Ex * fx + Ey * fy + Ez * fz;
-                    const float b = g * Ex - By * fz + Bz * fy;
-                    const float c = g * Ey - Bz * fx + Bx * fz;
-                    const float d = g * Ez - Bx * fy + By * fx;
-                    chi = k_chi * sqrtf( fabsf( a * a - b * b - c * c - d * d ) );
-                    last_chi = chi;
-                    if( chi > min_disc && tp <= eps_tau ) {
-                        while( tp <= eps_tau ) tp = -logf( fmaxf( 1.0f - ( float )rng_uniform( rs ), 5.9604645e-8f ) );
-                    }
-                    if( tp > eps_tau ) {
-                        const float rate = tab_yield32( t, chi, g );
-                        const float emission_time = fminf( tp / rate, dtf - local_time );
-                        tp -= rate * emission_time;
-                        if( tp <= eps_tau ) {
-                            const double u = rng_uniform( rs );
-                            emit = true;
-                            if( use_mlp && !mlp_masked( m, chi, u ) ) {
-                                if constexpr( H > 0 ) {
-                                    net = true;
-                                    u32 = ( float )u;
-                                } else {
-                                    pchi = mlp_photon_chi( m, chi, u );
-                                }
-                            } else {
-                                pchi = ( double )tab_photon_chi32( t, chi, ( float )u );
-                            }
-                        }
-                        it++;
-                        local_time += emission_time;
-                    } else if( chi <= min_disc && tp <= eps_tau && chi > min_cont ) {
-                        const float emission_time = dtf - local_time;
-                        const float aa = 1.0f + 4.8f * ( 1.0f + chi ) * logf( 1.0f + 1.7f * chi ) + 2.44f * chi * chi;
-                        const float e = ( 1.0f / cbrtf( aa * aa ) ) * emission_time * chi * chi * ( float )t.factor_classical;
-                        const double tmp = ( double )( e * g / ( g * g - 1.0f ) );
-                        const double gd = sqrt( 1.0 + px * px + py * py + pz * pz );
-                        px -= tmp * px;
-                        py -= tmp * py;
-                        pz -= tmp * pz;
-                        rad += w[q] * ( gd - sqrt( 1.0 + px * px + py * py + pz * pz ) );
-                        local_time = dtf;
-                    } else {
-                        local_time = dtf;
-                    }
-                }
-            }
-            if constexpr( H > 0 ) {
-                // the emitting lanes' network evaluations, by the whole warp
-                unsigned req = __ballot_sync( 0xffffffffu, net );
-                while( req ) {
-                    const int src = __ffs( req ) - 1;
-                    req &= req - 1;
-                    const float cs = __shfl_sync( 0xffffffffu, chi, src ), us = __shfl_sync( 0xffffffffu, u32, src );
-                    const float y = mlp_coop<H>( m, sw, cs, us, lane );
-                    if( lane == src ) pchi = ( double )chi * ( double )exp10f( y * m.out_scale );
-                }
-            }
-            if( emit ) {
-                const double gd = sqrt( 1.0 + px * px + py * py + pz * pz );
-                const double pg = pchi / ( double )chi * ( gd - 1.0 );
-                const double f = ( double )( ( float )pg / sqrtf( g * g - 1.0f ) );
-                px -= px * f;
-                py -= py * f;
-                pz -= pz * f;
-                if( ph.count && pg >= ph.threshold && i_photon < ph.max_emissions ) {
-                    const double inv = 1.0 / sqrt( px * px + py * py + pz * pz );
-                    const unsigned long long o0 = atomicAdd( ph.count, ( unsigned long long )ph.sampling );
-                    for( int k = 0; k < ph.sampling; k++ ) {
-                        const unsigned long long o = o0 + ( unsigned long long )k;
-                        if( o >= ( unsigned long long )ph.cap ) break;
-                        for( int dd = 0; dd < ph.ndim; dd++ ) ph.ph_pos[dd * ph.cap + o] = ph.pos[dd * n + q];
-                        ph.ph_mom[o] = pg * px * inv;
-                        ph.ph_mom[ph.cap + o] = pg * py * inv;
-                        ph.ph_mom[2 * ph.cap + o] = pg * pz * inv;
-                        ph.ph_w[o] = w[q] * ( 1.0 / ph.sampling );
-                        ph.ph_chi[o] = pchi;
-                        ph.ph_tau[o] = -1.0;
-                    }
-                    i_photon++;
-                } else {
-                    rad += w[q] * ( gd - sqrt( 1.0 + px * px + py * py + pz * pz ) );
-                }
-                nem++;
-                tp = -1.0f;
-            }
-        }
-        if( p < n ) {
+        mc_pass_f32<H>( t, m, use_mlp, sw, active, dt, qm2, E3, B3, px, py, pz, tp, rs, w[q], rad, nem, last_chi, ph, q, n );
+        if( active ) {
             mom[p] = px;
             mom[n + p] = py;
             mom[2 * n + p] = pz;
@@ -729,6 +741,111 @@ __global__ void k_push_photons( int ndim, int64_t n, double dt, double *__restri
     pos[p] += dt * px * inv;
     if( ndim > 1 ) pos[n + p] += dt * py * inv;
     if( ndim > 2 ) pos[2 * n + p] += dt * pz * inv;
+}
+
+// The pass over a resident 2D mixed-form species, one block per tile: each
+// particle's E and B_m come from an order-2 gather of the global field arrays (the
+// gather of the step kernel, here from global memory), then mc_pass_f32 updates its
+// momentum and optical depth in place.  The random stream of the particle in slot o at
+// step k is (seed, o, k).  Runs before the step, as Radiate before the push in
+// Species::dynamics (Species.cpp:583-640).
+__device__ __forceinline__ void bspl2( float x, float &c0, float &c1, float &c2 )
+{
+    c0 = 0.5f * ( 0.5f - x ) * ( 0.5f - x );
+    c1 = 0.75f - x * x;
+    c2 = 0.5f * ( 0.5f + x ) * ( 0.5f + x );
+}
+
+__device__ __forceinline__ float gather2( const float *__restrict__ F, int ny, int bx, int by, const float *cx,
+                                          const float *cy )
+{
+    float r = 0.0f;
+#pragma unroll
+    for( int a = 0; a < 3; a++ ) {
+        const float *row = F + ( int64_t )( bx + a ) * ny + by;
+        r = fmaf( cx[a], cy[0] * row[0] + cy[1] * row[1] + cy[2] * row[2], r );
+    }
+    return r;
+}
+
+template <int H>
+__global__ void __launch_bounds__( 128 ) k_radiate_resident( RadTab t, MlpView m, int use_mlp, ResidentRad r )
+{
+    __shared__ MlpShared<H == 0 ? 4 : H> sw;
+    if constexpr( H > 0 ) {
+        mlp_stage<H, true>( m, sw );
+        __syncthreads();
+    }
+    const int tile = blockIdx.x;
+    const int n = r.count[tile];
+    const int64_t s0 = r.seg_start[tile];
+    const uint32_t step = ( uint32_t )*r.step;
+    const int nyp = r.np[1], nyd = nyp + 1;
+    double rad = 0.0;
+    unsigned long long nem = 0;
+    for( int base = 0; base < n; base += blockDim.x ) { // the same trip count for every thread
+        const int i = base + threadIdx.x;
+        const bool active = i < n;
+        const int64_t o = s0 + ( active ? i : 0 );
+        double px = 0.0, py = 0.0, pz = 0.0;
+        float E3[3] = { 0.0f, 0.0f, 0.0f }, B3[3] = { 0.0f, 0.0f, 0.0f }, tp = 0.0f, last_chi = 0.0f, wq = 0.0f;
+        if( active ) {
+            const unsigned k = r.key[o];
+            const int gx = ( int )( k >> 16 ), gy = ( int )( k & 65535u );
+            const float dxl = r.d[0][o], dyl = r.d[1][o];
+            float cpx[3], cpy[3], cdx[3], cdy[3];
+            bspl2( dxl, cpx[0], cpx[1], cpx[2] );
+            bspl2( dyl, cpy[0], cpy[1], cpy[2] );
+            const int sx = dxl >= 0.0f ? 1 : 0, sy = dyl >= 0.0f ? 1 : 0;
+            bspl2( dxl + 0.5f - ( float )sx, cdx[0], cdx[1], cdx[2] );
+            bspl2( dyl + 0.5f - ( float )sy, cdy[0], cdy[1], cdy[2] );
+            // primal node gx sits at array index gx + 2; the stencil starts one node below
+            const int bxp = gx + 1, byp = gy + 1, bxd = gx + 1 + sx, byd = gy + 1 + sy;
+            // Ex(d,p) Ey(p,d) Ez(p,p) Bx(p,d) By(d,p) Bz(d,d)
+            E3[0] = gather2( r.E[0], nyp, bxd, byp, cdx, cpy );
+            E3[1] = gather2( r.E[1], nyd, bxp, byd, cpx, cdy );
+            E3[2] = gather2( r.E[2], nyp, bxp, byp, cpx, cpy );
+            B3[0] = gather2( r.Bm[0], nyd, bxp, byd, cpx, cdy );
+            B3[1] = gather2( r.Bm[1], nyp, bxd, byp, cdx, cpy );
+            B3[2] = gather2( r.Bm[2], nyd, bxd, byd, cdx, cdy );
+            px = r.p[0][o];
+            py = r.p[1][o];
+            pz = r.p[2][o];
+            tp = r.tau[o];
+            wq = r.w[o];
+        }
+        uint32_t rs = rng_init( r.seed, ( uint32_t )o, step );
+        mc_pass_f32<H>( t, m, use_mlp, sw, active, r.dt, r.qm2, E3, B3, px, py, pz, tp, rs, ( double )wq, rad, nem,
+                        last_chi, PhotonOut{}, 0, 0 );
+        if( active ) {
+            r.p[0][o] = ( float )px;
+            r.p[1][o] = ( float )py;
+            r.p[2][o] = ( float )pz;
+            r.tau[o] = tp;
+        }
+    }
+    __shared__ double srad[4];
+    __shared__ unsigned long long snem[4];
+    for( int k = 16; k > 0; k >>= 1 ) {
+        rad += __shfl_down_sync( 0xffffffffu, rad, k );
+        nem += __shfl_down_sync( 0xffffffffu, nem, k );
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if( lane == 0 ) {
+        srad[warp] = rad;
+        snem[warp] = nem;
+    }
+    __syncthreads();
+    if( threadIdx.x == 0 ) {
+        double a = 0.0;
+        unsigned long long e = 0;
+        for( int k = 0; k < ( int )( blockDim.x >> 5 ); k++ ) {
+            a += srad[k];
+            e += snem[k];
+        }
+        if( a != 0.0 ) atomicAdd( r.radiated, a );
+        if( e ) atomicAdd( r.emissions, e );
+    }
 }
 
 // ---- MLP training ------------------------------------------------------------
@@ -928,6 +1045,22 @@ McKernel mc_kernel_for( int H )
     return k_monte_carlo<F32, 0>;
 }
 } // namespace
+} // namespace sg
+
+namespace sg {
+int launch_radiate_resident( const sg_rad_tables *T, const sg_mlp *mlp, const ResidentRad &r, cudaStream_t st )
+{
+    if( mlp ) SG_REQUIRE( mlp->mask != nullptr, "the network has not been validated (sg_mlp_validate)" );
+    MlpView v{};
+    if( mlp ) v = view( mlp );
+    const int H = mlp ? v.H : 0;
+    if( H == 64 ) k_radiate_resident<64><<<r.ntiles, 128, 0, st>>>( T->t, v, 1, r );
+    else if( H == 32 ) k_radiate_resident<32><<<r.ntiles, 128, 0, st>>>( T->t, v, 1, r );
+    else if( H == 16 ) k_radiate_resident<16><<<r.ntiles, 128, 0, st>>>( T->t, v, 1, r );
+    else k_radiate_resident<0><<<r.ntiles, 128, 0, st>>>( T->t, v, mlp ? 1 : 0, r );
+    SG_LAUNCH_CHECK( "k_radiate_resident" );
+    return SG_OK;
+}
 } // namespace sg
 
 extern "C" {

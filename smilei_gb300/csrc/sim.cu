@@ -28,6 +28,7 @@
 // sees the spill after the step and re-lays the segments out (rare).
 
 #include "common.cuh"
+#include "resident_rad.cuh"
 #include "scan.cuh"
 
 #include <algorithm>
@@ -76,6 +77,7 @@ struct PBuf<false> {
     double *x[3];
     double *p[3];
     double *w;
+    double *tau; // optical depth of a radiating species, else null
 };
 template <>
 struct PBuf<true> {
@@ -83,6 +85,7 @@ struct PBuf<true> {
     float *d[3];
     float *p[3];
     float *w;
+    float *tau; // optical depth of a radiating species, else null
 };
 
 struct SpecParams {
@@ -583,6 +586,8 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
 #pragma unroll
             for( int k = 0; k < 3; k++ ) cp_async_word( &sRec[( 3 + k ) * nmax + slot], &in.p[k][src], true );
             cp_async_word( &sRec[7 * nmax + slot], &in.w[src], true );
+            // a radiating species' optical depth rides in the record plane until the record is written
+            if( in.tau ) cp_async_word( &sRec[6 * nmax + slot], &in.tau[src], true );
             sSlotCell[slot] = ( unsigned char )lc;
         }
         if( threadIdx.x == 0 ) {
@@ -604,7 +609,11 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
         int img[3] = { 0, 0, 0 }; // FP64 form: N when the old node was wrapped to its image 0
         double xabs[3] = { 0.0, 0.0, 0.0 };
         double xpn[3] = { 0.0, 0.0, 0.0 };
-        T px = T( 0 ), py = T( 0 ), pz = T( 0 ), w = T( 0 );
+        T px = T( 0 ), py = T( 0 ), pz = T( 0 ), w = T( 0 ), tauv = T( 0 );
+        if( valid && in.tau ) {
+            if constexpr( CELLS ) tauv = ( T )sRec[6 * nmax + q];
+            else tauv = in.tau[src];
+        }
         if( valid ) {
             if constexpr( CELLS ) {
                 // slot q of the cell-ordered planes
@@ -860,6 +869,7 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
                 dst.p[1][o] = py;
                 dst.p[2][o] = pz;
                 dst.w[o] = w;
+                if( dst.tau ) dst.tau[o] = tauv;
             }
         }
     }
@@ -1434,6 +1444,7 @@ __global__ void k_stage( GridInfo g, int64_t n, const double *__restrict__ pos, 
     st.p[1][p] = ( PT )mom[n + p];
     st.p[2][p] = ( PT )mom[2 * n + p];
     st.w[p] = ( PT )wgt[p];
+    if( st.tau ) st.tau[p] = ( PT )-1.0;
     const int t = tile_of( g, node[0], node[1], node[2] );
     st_tile[p] = t;
     atomicAdd( &count[t], 1 );
@@ -1478,6 +1489,7 @@ __device__ __forceinline__ void copy_particle( const PBuf<MIXED> &s, int64_t i, 
     d.p[1][o] = s.p[1][i];
     d.p[2][o] = s.p[2][i];
     d.w[o] = s.w[i];
+    if( s.tau ) d.tau[o] = s.tau[i];
 }
 
 // Staged (or spilled) particle -> next free slot of its tile in the destination buffer.
@@ -1724,6 +1736,7 @@ __global__ void k_inject( GridInfo g, InjectParams ip, int pass, int *__restrict
         dst.p[1][o] = ( PT )pm[1];
         dst.p[2][o] = ( PT )pm[2];
         dst.w[o] = ( PT )w;
+        if( dst.tau ) dst.tau[o] = ( PT )-1.0;
     }
     if( pass == 0 ) atomicAdd( created, ( unsigned long long )ip.ppc );
 }
@@ -1808,6 +1821,15 @@ __global__ void k_norm2( GridInfo g, const T *__restrict__ a, int sx, int sy, in
     if( threadIdx.x == 0 ) atomicAdd( out, acc );
 }
 
+__global__ void k_bump_step( int64_t *step ) { *step += 1; }
+
+template <class T>
+__global__ void k_fill( int64_t n, T *__restrict__ a, T v )
+{
+    const int64_t i = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x;
+    if( i < n ) a[i] = v;
+}
+
 template <class Src, class Dst>
 __global__ void k_convert( int64_t n, const Src *__restrict__ s, Dst *__restrict__ d )
 {
@@ -1872,6 +1894,13 @@ struct SpeciesState {
     PBuf<true> om{};
     int *ovf_tile = nullptr;
     int max_cap = 0; // largest tile segment of the current layout
+    bool radiates = false;     // carries an optical-depth plane (Monte-Carlo radiation)
+    void *tau_mem[2] = { nullptr, nullptr };
+    void *ovf_tau = nullptr;
+    const sg_rad_tables *rad_tables = nullptr; // its radiation tables and network (not owned)
+    const sg_mlp *rad_mlp = nullptr;
+    uint32_t rad_seed = 0;
+    double *d_rad = nullptr;   // device tallies: radiated energy, emissions (as unsigned long long)
     double slack = 0.0;        // capacity slack of this species' layout (0: the configuration's)
     int64_t last_relayout = -1; // step of its last re-layout after a spill
     bool inject = false;       // fresh window cells are filled from this profile
@@ -1896,6 +1925,7 @@ void carve( void *mem, int ndim, int64_t n, PBuf<false> &b )
     }
     for( int d = 0; d < 3; d++ ) { b.p[d] = reinterpret_cast<double *>( p ); p = align256( p + 8 * n ); }
     b.w = reinterpret_cast<double *>( p );
+    b.tau = nullptr;
 }
 
 void carve( void *mem, int ndim, int64_t n, PBuf<true> &b )
@@ -1909,6 +1939,7 @@ void carve( void *mem, int ndim, int64_t n, PBuf<true> &b )
     }
     for( int d = 0; d < 3; d++ ) { b.p[d] = reinterpret_cast<float *>( p ); p = align256( p + 4 * n ); }
     b.w = reinterpret_cast<float *>( p );
+    b.tau = nullptr;
 }
 
 } // namespace
@@ -1948,6 +1979,7 @@ struct sg_sim {
     int64_t spilled = 0;         // particles that went through the spill list
     size_t smem_bytes = 0;
     int64_t hstep = 0;           // steps done (host copy)
+    int64_t *d_rad_step = nullptr; // steps done (device), the radiation's random streams
     // moving window (SimWindow.cpp:93-96): moves `shift` cells when (time_dual - t_start) v > x_moved
     bool win_on = false;
     double win_t_start = 0.0, win_velocity = 0.0, win_x_moved = 0.0;
@@ -2085,6 +2117,42 @@ int launch_fields( sg_sim *S, cudaStream_t st, int &launches )
     return SG_OK;
 }
 
+// The radiation pass over species s (2D mixed form) on its current buffer.
+int launch_radiation( sg_sim *S, SpeciesState &s, cudaStream_t st )
+{
+    const GridInfo &g = S->g;
+    ResidentRad r{};
+    for( int d = 0; d < 2; d++ ) {
+        r.N[d] = g.N[d];
+        r.np[d] = g.np[d];
+        r.T[d] = g.T[d];
+        r.nt[d] = g.nt[d];
+        r.dx[d] = g.dx[d];
+        r.dxi[d] = g.dxi[d];
+    }
+    r.ntiles = g.ntiles;
+    for( int c = 0; c < 3; c++ ) {
+        r.E[c] = static_cast<const float *>( S->fptr[c] );
+        r.Bm[c] = static_cast<const float *>( S->fptr[6 + c] );
+    }
+    const PBuf<true> &b = s.bm[s.cur];
+    r.seg_start = s.seg_start;
+    r.count = s.count[s.cur];
+    r.key = b.key;
+    r.d[0] = b.d[0];
+    r.d[1] = b.d[1];
+    for( int c = 0; c < 3; c++ ) r.p[c] = b.p[c];
+    r.w = b.w;
+    r.tau = b.tau;
+    r.dt = g.dt;
+    r.qm2 = s.charge / ( s.mass * s.mass );
+    r.seed = s.rad_seed;
+    r.step = S->d_rad_step;
+    r.radiated = s.d_rad;
+    r.emissions = reinterpret_cast<unsigned long long *>( s.d_rad + 1 );
+    return launch_radiate_resident( s.rad_tables, s.rad_mlp, r, st );
+}
+
 // Enqueues one full timestep on `st` (no host synchronisation).
 int enqueue_step( sg_sim *S, cudaStream_t st )
 {
@@ -2098,6 +2166,20 @@ int enqueue_step( sg_sim *S, cudaStream_t st )
     SG_CUDA_TRY( cudaMemsetAsync( S->d_flags, 0, ( 1 + 2 * S->max_species ) * sizeof( int ), st ) );
     for( auto &s : S->sp ) SG_CUDA_TRY( cudaMemsetAsync( s.count[1 - s.cur], 0, S->g.ntiles * sizeof( int ), st ) );
     SG_CUDA_TRY( cudaEventRecordWithFlags( S->ev[0], st, evflags ) );
+    // Monte-Carlo radiation of the radiating species, before their push (Species.cpp:583-640)
+    bool radiated = false;
+    for( auto &s : S->sp ) {
+        if( !s.radiates ) continue;
+        int r = launch_radiation( S, s, st );
+        if( r ) return r;
+        launches++;
+        radiated = true;
+    }
+    if( radiated ) {
+        k_bump_step<<<1, 1, 0, st>>>( S->d_rad_step );
+        SG_LAUNCH_CHECK( "k_bump_step" );
+        launches++;
+    }
     for( auto &s : S->sp ) {
         int r = launch_particles_any( S, s, st );
         if( r ) return r;
@@ -2140,6 +2222,21 @@ int capture( sg_sim *S, cudaGraphExec_t *out )
     return SG_OK;
 }
 
+// Optical-depth planes of a radiating species for both buffers (the old ones are
+// left to the caller, who may still be reading them).
+int alloc_tau( sg_sim *S, SpeciesState &s, int64_t capacity )
+{
+    for( int b = 0; b < 2; b++ ) {
+        void *m = nullptr;
+        if( cudaMalloc( &m, ( size_t )std::max<int64_t>( capacity, 1 ) * S->esz ) != cudaSuccess )
+            return set_error( SG_ERR_NOMEM, "cannot allocate the optical-depth plane" );
+        s.tau_mem[b] = m;
+        if( S->mixed ) s.bm[b].tau = static_cast<float *>( m );
+        else s.bd[b].tau = static_cast<double *>( m );
+    }
+    return SG_OK;
+}
+
 int alloc_species_buffers( sg_sim *S, SpeciesState &s, int64_t capacity )
 {
     const int nd = S->g.ndim;
@@ -2153,6 +2250,7 @@ int alloc_species_buffers( sg_sim *S, SpeciesState &s, int64_t capacity )
         else carve( m, nd, capacity, s.bd[b] );
     }
     s.capacity = capacity;
+    if( s.radiates ) return alloc_tau( S, s, capacity );
     return SG_OK;
 }
 
@@ -2212,7 +2310,7 @@ int relayout( sg_sim *S, SpeciesState &s, int nspill )
     int r = layout_from_counts( S, s.count[s.cur], S->tmp_cap, S->tmp_start, &total, &new_max_cap, s.slack );
     if( r ) return r;
     // destination: the idle buffer, or fresh buffers when the layout no longer fits
-    void *old_mem[2] = { s.mem[0], s.mem[1] };
+    void *old_mem[2] = { s.mem[0], s.mem[1] }, *old_tau[2] = { s.tau_mem[0], s.tau_mem[1] };
     PBuf<false> old_bd = s.bd[s.cur];
     PBuf<true> old_bm = s.bm[s.cur];
     int dst_buf = 1 - s.cur;
@@ -2239,6 +2337,10 @@ int relayout( sg_sim *S, SpeciesState &s, int nspill )
     if( realloc ) {
         release( old_mem[0] );
         release( old_mem[1] );
+        if( s.radiates ) {
+            release( old_tau[0] );
+            release( old_tau[1] );
+        }
     }
     s.cur = dst_buf;
     drop_graphs( S );
@@ -2299,7 +2401,7 @@ int rebuild_species( sg_sim *S, SpeciesState &s, int shift, int x0, int x1 )
     unsigned long long wc[2] = { 0, 0 };
     SG_CUDA_TRY( cudaMemcpyAsync( wc, S->d_wcount, sizeof( wc ), cudaMemcpyDeviceToHost, st ) );
     SG_CUDA_TRY( cudaStreamSynchronize( st ) );
-    void *old_mem[2] = { s.mem[0], s.mem[1] };
+    void *old_mem[2] = { s.mem[0], s.mem[1] }, *old_tau[2] = { s.tau_mem[0], s.tau_mem[1] };
     const PBuf<false> old_bd = s.bd[s.cur];
     const PBuf<true> old_bm = s.bm[s.cur];
     int dst = 1 - s.cur;
@@ -2327,6 +2429,10 @@ int rebuild_species( sg_sim *S, SpeciesState &s, int shift, int x0, int x1 )
     if( realloc ) {
         release( old_mem[0] );
         release( old_mem[1] );
+        if( s.radiates ) {
+            release( old_tau[0] );
+            release( old_tau[1] );
+        }
     }
     drop_graphs( S );
     return SG_OK;
@@ -2524,7 +2630,12 @@ int sg_sim_destroy( sg_sim *S )
         release( s.count[1] );
         release( s.ovf_mem );
         release( s.ovf_tile );
+        release( s.tau_mem[0] );
+        release( s.tau_mem[1] );
+        release( s.ovf_tau );
+        release( s.d_rad );
     }
+    release( S->d_rad_step );
     release( S->fmem );
     release( S->d_flags );
     release( S->d_step );
@@ -2817,6 +2928,54 @@ int sg_sim_set_species_profile( sg_sim *S, int species, const double *profile, i
     ip.sqrt_temp = std::sqrt( temperature );
     ip.seed = ( unsigned long long )seed;
     s.inject = true;
+    return SG_OK;
+}
+
+int sg_sim_set_species_radiation( sg_sim *S, int species, const sg_rad_tables *tables, const sg_mlp *mlp,
+                                  uint32_t seed )
+{
+    SG_REQUIRE( S && tables, "NULL argument" );
+    SG_REQUIRE( species >= 0 && species < ( int )S->sp.size(), "species %d out of range", species );
+    SG_REQUIRE( S->mixed && S->g.ndim == 2, "radiation in the resident step needs the 2D mixed form" );
+    SpeciesState &s = S->sp[species];
+    SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
+    if( !s.radiates ) {
+        s.radiates = true;
+        int r = alloc_tau( S, s, s.capacity );
+        if( r ) return r;
+        SG_CUDA_TRY( cudaMalloc( &s.ovf_tau, ( size_t )std::max<int64_t>( s.ovf_capacity, 1 ) * sizeof( float ) ) );
+        s.om.tau = static_cast<float *>( s.ovf_tau );
+        // optical depths start spent: the first step draws them (tau = -1, RadiationMonteCarlo.cpp:337)
+        for( int b = 0; b < 2; b++ ) {
+            k_fill<float><<<grid_for( std::max<int64_t>( s.capacity, 1 ), 256 ), 256, 0, S->stream>>>( s.capacity, s.bm[b].tau, -1.0f );
+            SG_LAUNCH_CHECK( "k_fill" );
+        }
+        SG_CUDA_TRY( cudaMalloc( &s.d_rad, 2 * sizeof( double ) ) );
+        SG_CUDA_TRY( cudaMemsetAsync( s.d_rad, 0, 2 * sizeof( double ), S->stream ) );
+        if( !S->d_rad_step ) {
+            SG_CUDA_TRY( cudaMalloc( &S->d_rad_step, sizeof( int64_t ) ) );
+            SG_CUDA_TRY( cudaMemsetAsync( S->d_rad_step, 0, sizeof( int64_t ), S->stream ) );
+        }
+        SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
+    }
+    s.rad_tables = tables;
+    s.rad_mlp = mlp;
+    s.rad_seed = seed;
+    drop_graphs( S );
+    return SG_OK;
+}
+
+int sg_sim_radiation_stats( sg_sim *S, int species, double *radiated, unsigned long long *emissions )
+{
+    SG_REQUIRE( S, "NULL simulation" );
+    SG_REQUIRE( species >= 0 && species < ( int )S->sp.size(), "species %d out of range", species );
+    const SpeciesState &s = S->sp[species];
+    SG_REQUIRE( s.radiates, "species %d does not radiate", species );
+    double h[2] = { 0.0, 0.0 };
+    SG_CUDA_TRY( cudaMemcpyAsync( h, s.d_rad, sizeof( h ), cudaMemcpyDeviceToHost, S->stream ) );
+    SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
+    if( radiated ) *radiated = h[0];
+    if( emissions ) std::memcpy( emissions, &h[1], sizeof( unsigned long long ) );
     return SG_OK;
 }
 

@@ -205,6 +205,23 @@ class Simulation:
                                                     float(temperature), int(seed)), "set_species_profile")
         return tuple(float(v) for v in prof)
 
+    def set_species_radiation(self, species, tables, mlp=None, seed=0):
+        """Monte-Carlo radiation reaction of ``species`` in every step (2D mixed form):
+        ``tables`` a radiation.RadiationTables, ``mlp`` a validated radiation.PhotonChiMLP
+        or None.  Both must stay alive while the simulation runs."""
+        self._rad_refs = getattr(self, "_rad_refs", {})
+        self._rad_refs[species] = (tables, mlp)
+        check(_lib.lib().sg_sim_set_species_radiation(self._h, int(species), tables._h,
+                                                      mlp._h if mlp is not None else None, int(seed) & 0xffffffff),
+              "set_species_radiation")
+
+    def radiation_stats(self, species):
+        """(radiated energy, number of emissions) of a radiating species so far."""
+        r, e = ctypes.c_double(), ctypes.c_ulonglong()
+        check(_lib.lib().sg_sim_radiation_stats(self._h, int(species), ctypes.byref(r), ctypes.byref(e)),
+              "radiation_stats")
+        return r.value, e.value
+
     def fill_species(self, species, x0=0, x1=None):
         """Creates the species' particles in window cells [x0, x1) (default: the whole grid)."""
         x1 = self.n_cells[0] if x1 is None else x1

@@ -248,3 +248,82 @@ def test_what_the_trained_network_gains_over_the_table(rad):
     print(f"\nMLP inverse CDF: {net_bytes} B vs table {table_bytes} B; 4M samples: mlp {times['mlp']:.3f} ms, "
           f"table {times['table']:.3f} ms; median rel dev {rel:.4f}; network used on {used}/{err.size} bins")
     net.close()
+
+
+def test_resident_radiation_matches_the_operator_loop(rad):
+    """Radiation inside the resident 2D mixed step against the drop-in operator loop
+    (FP64 interpolate, Monte Carlo, push, deposit, Maxwell) on the same electrons in the
+    same uniform crossed fields (E_y = B_z = 50, electrons at gamma 1000 moving towards
+    -x: chi about 0.25).  Different random streams (the resident pass keys them on the
+    buffer slot): emissions and radiated energy agree to 2 %, and the tallies of a run
+    whose fields make chi zero are zero with the momenta untouched by radiation."""
+    radiation, _, _ = rad
+    from smilei_gb300 import operators as O, simulation
+    g = np.load(__import__("os").path.join(__import__("os").path.dirname(__file__), "golden", "radiation.npz"))
+    f_dn, f_cl, inv_es = radiation.normalised_factors(2.0 * np.pi * 299792458.0 / 1e-6)
+    T32 = radiation.RadiationTables(g["integfochi"], g["integfochi_min"], g["integfochi_max"], g["xi_table"],
+                                    g["xi_min"], g["xi_max"], g["xi_axis1_min"], f_dn, f_cl, inv_es)
+    T32.set_fp32_math(True)
+    n_cells, cl, dt, steps = [32, 32], [0.5, 0.5], 0.3, 8
+    rng = np.random.default_rng(21)
+    n = 200000
+    L = [n_cells[0] * cl[0], n_cells[1] * cl[1]]
+    pos = np.stack([rng.uniform(0, L[0], n), rng.uniform(0, L[1], n)])
+    mom = np.stack([np.full(n, -1000.0), rng.normal(0, 1, n), np.zeros(n)])
+    w = np.full(n, 1e-9)  # test particles: their current does not disturb the fields
+
+    def uniform_fields(E0):
+        from smilei_gb300 import synthetic
+        st = synthetic.STAGGER
+        f = {}
+        for k in ["Ex", "Ey", "Ez", "Bx", "By", "Bz", "Bx_m", "By_m", "Bz_m", "Jx", "Jy", "Jz"]:
+            f[k] = np.zeros(tuple(n_cells[d] + 5 + st[k.replace("_m", "")][d] for d in range(2)))
+        for k in ("Ey", "Bz", "Bz_m"):
+            f[k][:] = E0
+        return f
+
+    def resident(E0):
+        sim = simulation.Simulation(n_cells, cl, dt, form="mixed")
+        for k, a in uniform_fields(E0).items():
+            sim.set_field(k, a)
+        sim.add_species(1.0, -1.0, "vay", pos, mom, w)
+        sim.set_species_radiation(0, T32, None, seed=5)
+        sim.step(steps)
+        r, e = sim.radiation_stats(0)
+        p, m, _ = sim.get_species(0)
+        sim.close()
+        return r, e, m
+
+    def operators(E0):
+        geom = O.PatchGeometry(n_cells, cl)
+        em = O.ElectroMagn(geom)
+        for k, a in uniform_fields(E0).items():
+            name = k + "_" if not k.endswith("_m") else k
+            if hasattr(em, name):
+                getattr(em, name).copy_(torch.as_tensor(a, device="cuda"))
+        part = O.Particles(cu(pos), cu(mom), cu(w), torch.full((n,), -1, device="cuda"))
+        smpi = O.SmileiMPI(2, n)
+        tau = cu(np.full(n, -1.0))
+        interp, push = O.Interpolator2D2Order(geom), O.PusherVay(dt, 1.0, 2)
+        tot, nem = 0.0, 0
+        for it in range(steps):
+            interp.fieldsWrapper(em, part, smpi)
+            r, e = radiation.monte_carlo(T32, dt, 1.0, -1.0, part.momentum, part.weight, tau, smpi.dynamics_Epart,
+                                         smpi.dynamics_Bpart, seed=5, step=it)
+            tot += r
+            nem += e
+            push(part, smpi)
+            # periodic wrap (the operators act on one patch)
+            for d in range(2):
+                part.position[d] = torch.remainder(part.position[d], L[d])
+        return tot, nem
+
+    r_res, e_res, _ = resident(50.0)
+    r_op, e_op = operators(50.0)
+    assert e_op > 100000
+    assert abs(e_res - e_op) <= 0.02 * e_op, (e_res, e_op)
+    assert abs(r_res - r_op) <= 0.02 * r_op, (r_res, r_op)
+    r0, e0, m0 = resident(0.0)
+    assert r0 == 0.0 and e0 == 0
+    assert np.allclose(np.sort(m0[0]), np.sort(mom[0]), rtol=1e-6)
+    T32.close()
