@@ -512,6 +512,82 @@ def run_gpu_radiation(args, rank, world, local_rank):
                 b_per=b_per, peak=peak, peak_kind=peak_kind, radiated=radiated, emissions=n_emit, mlp_used=used)
 
 
+def run_gpu_radiation_resident(args, rank, world, local_rank):
+    """The same collision in the resident 2D mixed-form step: FP32 push and deposit, the
+    radiation pass of the species (FP32 arithmetic, table or network) before each push."""
+    import torch
+    from smilei_gb300 import simulation, radiation as R, _lib, synthetic
+    device = f"cuda:{local_rank}"
+    torch.cuda.set_device(local_rank)
+    stream = torch.cuda.Stream(device=device)
+    torch.cuda.set_stream(stream)
+    n_cells = RAD["n_cells"]
+    st = rad_setup(n_cells, RAD["npart"], args.seed + rank)
+    stag = synthetic.STAGGER
+    shape = lambda c: tuple(n_cells[d] + 5 + stag[c.replace("_m", "")][d] for d in range(2))
+    wave = plane_wave(shape, n_cells, st["dx"], RAD["a0"])
+
+    def make(tile, tables=None, net=None):
+        sm = simulation.Simulation(n_cells, [st["dx"], st["dx"]], st["dt"], form="mixed", use_graph=True,
+                                   tile=list(tile) if tile else None)
+        _lib.check(_lib.lib().sg_sim_set_stream(sm._h, stream.cuda_stream), "set_stream")
+        for comp in ("Ey", "Bz"):
+            sm.set_field(comp, wave[comp])
+        sm.set_field("Bz_m", wave["Bz"])
+        sm.add_species(1.0, -1.0, "vay", st["pos"], st["mom"], st["w"])
+        if tables is not None:
+            sm.set_species_radiation(0, tables, net, seed=7)
+        return sm
+
+    g = np.load(os.path.join(ROOT, "tests", "golden", "radiation.npz"))
+    f_dn, f_cl, inv_es = R.normalised_factors(2.0 * np.pi * 299792458.0 / 1e-6)
+    T = R.RadiationTables(g["integfochi"], g["integfochi_min"], g["integfochi_max"], g["xi_table"], g["xi_min"],
+                          g["xi_max"], g["xi_axis1_min"], f_dn, f_cl, inv_es)
+    T.set_fp32_math(True)
+    mlp, used = None, None
+    if args.mlp:
+        mlp = R.PhotonChiMLP(hidden=64, seed=3)
+        for steps, lr in ((4000, 2e-3), (4000, 1e-3), (4000, 3e-4)):
+            mlp.train(T, steps=steps, batch=8192, lr=lr)
+        err, n_masked = mlp.validate(T, tol=0.05)
+        used = f"{err.size - n_masked}/{err.size} (chi, xi) bins"
+    tile, tuning = ([args.tile] * 2 if args.tile else None), None
+    if args.autotune:
+        from smilei_gb300 import autotune
+        best, times = autotune.tune_tiles(lambda t: make(t, T, mlp), ndim=2)
+        tile, tuning = list(best), {"x".join(map(str, k)): round(v, 3) for k, v in times.items()}
+    sim = make(tile, T, mlp)
+    del st["pos"], st["mom"]
+    for _ in range(args.warmup):
+        sim.step(1)
+    torch.cuda.synchronize()
+    r0, e0 = sim.radiation_stats(0)
+    n = sim.species_count(0)
+    t_part = []
+    with ClockSampler(local_rank) as clk:
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        wall0 = time.perf_counter()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            sim.step(1)
+            tp, tf, tt, launches = sim.last_timing()
+            t_part.append(tp)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        wall1 = time.perf_counter()
+    ms = max_over_ranks(ev0.elapsed_time(ev1), device)
+    r1, e1 = sim.radiation_stats(0)
+    sim.close()
+    if mlp is not None:
+        mlp.close()
+    peak, peak_kind = measured_peak()
+    return dict(n=n, ms=ms, value=whole_job_rate(n, world, args.steps, ms),
+                wall_ms_per_step=(wall1 - wall0) * 1e3 / args.steps, clocks=clk.summary(),
+                b_per=52.0 + 8.0 + 24 * 4 / (n / float(np.prod(n_cells))), peak=peak, peak_kind=peak_kind,
+                radiated=r1 - r0, emissions=e1 - e0, mlp_used=used, launches=launches, tile=tile or "default 8x8",
+                tuning=tuning)
+
+
 def run_cpu_sample_radiation(args):
     """The oracle's interpolate, Monte-Carlo radiation, Vay push and deposit on a bounded
     sample: 200,000 electrons of the same bunch on a 512 x 128-cell grid (FP64)."""
@@ -600,6 +676,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="thermal", choices=["thermal", "uneven", "lwfa", "radiation"])
     ap.add_argument("--mlp", action="store_true", help="radiation workload: photon chi from the trained MLP")
+    ap.add_argument("--resident", action="store_true",
+                    help="radiation workload: the resident mixed-form step instead of the drop-in operators")
     ap.add_argument("--rad-math", default="fp32", choices=["fp32", "fp64"],
                     help="radiation workload: arithmetic of the Monte-Carlo table lookups and draws")
     ap.add_argument("--autotune", action="store_true", help="pick the tile shape by timing candidates first")
@@ -614,8 +692,9 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.workload == "radiation":
         workload = ("2D Monte-Carlo radiation reaction: 2048x512 cells (16 per wavelength), 1e7 electrons gamma=2000 "
-                    "in a Gaussian bunch (sigma_x = sigma_y = 2 lambda) head-on with a plane wave a0=100, Vay, "
-                    "drop-in FP64 operators, Monte-Carlo lookups in " + args.rad_math + ", photon chi from the " +
+                    "in a Gaussian bunch (sigma_x = sigma_y = 2 lambda) head-on with a plane wave a0=100, Vay, " +
+                    ("resident mixed-form step (FP32 push, deposit and Monte Carlo)" if args.resident else
+                     "drop-in FP64 operators, Monte-Carlo lookups in " + args.rad_math) + ", photon chi from the " +
                     ("MLP (table where its validation failed)" if args.mlp else "table"))
     elif args.workload == "lwfa":
         c = LWFA
@@ -648,7 +727,7 @@ def main():
         import torch.distributed as td
         td.init_process_group("nccl")
     if args.workload == "radiation":
-        res = run_gpu_radiation(args, rank, world, local_rank)
+        res = (run_gpu_radiation_resident if args.resident else run_gpu_radiation)(args, rank, world, local_rank)
         cpu = None
         if rank == 0 and world == 1 and not args.no_cpu_baseline:
             cpu = run_cpu_sample_radiation(args)
@@ -658,15 +737,18 @@ def main():
                 "metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": res["ms"] / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded bunch, host)",
-                "config": {"workload": workload, "form": "fp64 operators", "global_particles": res["n"] * world,
+                "config": {"workload": workload, "form": "mixed, resident step" if args.resident else "fp64 operators",
+                           "global_particles": res["n"] * world,
                            "wall_ms_per_step": res["wall_ms_per_step"], "radiated_energy": res["radiated"],
                            "emissions": res["emissions"], "mlp_used_on": res["mlp_used"],
+                           "tile": res.get("tile"), "autotune_ms_per_step": res.get("tuning"),
                            "l2": "inputs larger than L2"},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": res["peak"], "unit": "GB/s",
                              "frac": achieved / res["peak"], "traffic": None, "kernel": "operator chain",
                              "algorithmic_bytes_per_particle_step": res["b_per"],
                              "peak_source": res["peak_kind"]},
-                "cpu_baseline": cpu, "e2e": None, "gpu_launches": 9 * args.steps, "clocks": res["clocks"]}))
+                "cpu_baseline": cpu, "e2e": None,
+                "gpu_launches": res.get("launches", 9) * args.steps, "clocks": res["clocks"]}))
         if world > 1:
             import torch.distributed as td
             td.destroy_process_group()

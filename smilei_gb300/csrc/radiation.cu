@@ -769,24 +769,33 @@ __device__ __forceinline__ float gather2( const float *__restrict__ F, int ny, i
 }
 
 template <int H>
-__global__ void __launch_bounds__( 128 ) k_radiate_resident( RadTab t, MlpView m, int use_mlp, ResidentRad r )
+__global__ void __launch_bounds__( 128 ) k_radiate_resident( RadTab t, MlpView m, int use_mlp, ResidentRad r,
+                                                             int64_t nslots )
 {
     __shared__ MlpShared<H == 0 ? 4 : H> sw;
     if constexpr( H > 0 ) {
         mlp_stage<H, true>( m, sw );
         __syncthreads();
     }
-    const int tile = blockIdx.x;
-    const int n = r.count[tile];
-    const int64_t s0 = r.seg_start[tile];
     const uint32_t step = ( uint32_t )*r.step;
     const int nyp = r.np[1], nyd = nyp + 1;
     double rad = 0.0;
     unsigned long long nem = 0;
-    for( int base = 0; base < n; base += blockDim.x ) { // the same trip count for every thread
-        const int i = base + threadIdx.x;
-        const bool active = i < n;
-        const int64_t o = s0 + ( active ? i : 0 );
+    // one thread per buffer slot (all tiles' segments, holes included), so that a few
+    // dense tiles still spread over the whole GPU; a slot's tile is found by a binary
+    // search of the segment starts
+    for( int64_t o0 = ( int64_t )blockIdx.x * blockDim.x; o0 < nslots; o0 += ( int64_t )gridDim.x * blockDim.x ) {
+        const int64_t o = o0 + threadIdx.x;
+        bool active = false;
+        if( o < nslots ) {
+            int lo = 0, hi = r.ntiles - 1; // last tile whose segment starts at or before o
+            while( lo < hi ) {
+                const int mid = ( lo + hi + 1 ) >> 1;
+                if( r.seg_start[mid] <= o ) lo = mid;
+                else hi = mid - 1;
+            }
+            active = o - r.seg_start[lo] < r.count[lo];
+        }
         double px = 0.0, py = 0.0, pz = 0.0;
         float E3[3] = { 0.0f, 0.0f, 0.0f }, B3[3] = { 0.0f, 0.0f, 0.0f }, tp = 0.0f, last_chi = 0.0f, wq = 0.0f;
         if( active ) {
@@ -1054,10 +1063,12 @@ int launch_radiate_resident( const sg_rad_tables *T, const sg_mlp *mlp, const Re
     MlpView v{};
     if( mlp ) v = view( mlp );
     const int H = mlp ? v.H : 0;
-    if( H == 64 ) k_radiate_resident<64><<<r.ntiles, 128, 0, st>>>( T->t, v, 1, r );
-    else if( H == 32 ) k_radiate_resident<32><<<r.ntiles, 128, 0, st>>>( T->t, v, 1, r );
-    else if( H == 16 ) k_radiate_resident<16><<<r.ntiles, 128, 0, st>>>( T->t, v, 1, r );
-    else k_radiate_resident<0><<<r.ntiles, 128, 0, st>>>( T->t, v, mlp ? 1 : 0, r );
+    const unsigned blocks = ( unsigned )std::min<int64_t>( ( r.nslots + 127 ) / 128, 152 * 64 );
+    if( r.nslots <= 0 ) return SG_OK;
+    if( H == 64 ) k_radiate_resident<64><<<blocks, 128, 0, st>>>( T->t, v, 1, r, r.nslots );
+    else if( H == 32 ) k_radiate_resident<32><<<blocks, 128, 0, st>>>( T->t, v, 1, r, r.nslots );
+    else if( H == 16 ) k_radiate_resident<16><<<blocks, 128, 0, st>>>( T->t, v, 1, r, r.nslots );
+    else k_radiate_resident<0><<<blocks, 128, 0, st>>>( T->t, v, mlp ? 1 : 0, r, r.nslots );
     SG_LAUNCH_CHECK( "k_radiate_resident" );
     return SG_OK;
 }

@@ -18,6 +18,7 @@ struct ResidentRad {
     const float *E[3], *Bm[3];
     const int64_t *seg_start;
     const int *count;
+    int64_t nslots;   // buffer slots covered by the segments (last start + last capacity)
     const unsigned *key;
     const float *d[2];
     float *p[3];

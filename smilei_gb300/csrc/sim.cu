@@ -2138,6 +2138,7 @@ int launch_radiation( sg_sim *S, SpeciesState &s, cudaStream_t st )
     const PBuf<true> &b = s.bm[s.cur];
     r.seg_start = s.seg_start;
     r.count = s.count[s.cur];
+    r.nslots = s.capacity; // slots past the last segment find no particle
     r.key = b.key;
     r.d[0] = b.d[0];
     r.d[1] = b.d[1];
