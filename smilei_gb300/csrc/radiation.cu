@@ -592,7 +592,7 @@ __global__ void k_monte_carlo( RadTab t, MlpView m, int use_mlp, int64_t n, doub
     const int64_t p = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x;
     double rad = 0.0;
     unsigned long long nem = 0;
-    if( !F32 && p < n ) {
+    if( !F32 && p < n ) { // the reference's FP64 arithmetic
         double px = mom[p], py = mom[n + p], pz = mom[2 * n + p];
         const double Ex = Ep[p], Ey = Ep[n + p], Ez = Ep[2 * n + p];
         const double Bx = Bp[p], By = Bp[n + p], Bz = Bp[2 * n + p];
@@ -611,14 +611,10 @@ __global__ void k_monte_carlo( RadTab t, MlpView m, int use_mlp, int64_t n, doub
             const double chi = fabs( qm2 ) * t.inv_es * sqrt( fabs( a * a - b * b - c * c - d * d ) );
             last_chi = chi;
             if( chi > t.min_disc && tp <= eps_tau ) {
-                if constexpr( F32 ) {
-                    while( tp <= eps_tau ) tp = -( double )logf( fmaxf( 1.0f - ( float )rng_uniform( rs ), 5.9604645e-8f ) );
-                } else {
-                    while( tp <= eps_tau ) tp = -log( 1.0 - rng_uniform( rs ) );
-                }
+                while( tp <= eps_tau ) tp = -log( 1.0 - rng_uniform( rs ) );
             }
             if( tp > eps_tau ) {
-                const double rate = F32 ? ( double )tab_yield32( t, ( float )chi, ( float )g ) : tab_yield( t, chi, g );
+                const double rate = tab_yield( t, chi, g );
                 emission_time = fmin( tp / rate, dt - local_time );
                 tp -= rate * emission_time;
                 if( tp <= eps_tau ) {
@@ -628,7 +624,7 @@ __global__ void k_monte_carlo( RadTab t, MlpView m, int use_mlp, int64_t n, doub
                         if constexpr( H > 0 ) pchi = mlp_photon_chi_smem<H>( m, sw, chi, u );
                         else pchi = mlp_photon_chi( m, chi, u );
                     } else {
-                        pchi = F32 ? ( double )tab_photon_chi32( t, ( float )chi, ( float )u ) : tab_photon_chi( t, chi, u );
+                        pchi = tab_photon_chi( t, chi, u );
                     }
                     const double pg = pchi / chi * ( g - 1.0 );
                     const double f = pg / sqrt( g * g - 1.0 );
@@ -660,15 +656,8 @@ __global__ void k_monte_carlo( RadTab t, MlpView m, int use_mlp, int64_t n, doub
                 local_time += emission_time;
             } else if( chi <= t.min_disc && tp <= eps_tau && chi > t.min_cont ) {
                 emission_time = dt - local_time;
-                double e;
-                if constexpr( F32 ) {
-                    const float c = ( float )chi;
-                    const float aa = 1.0f + 4.8f * ( 1.0f + c ) * logf( 1.0f + 1.7f * c ) + 2.44f * c * c;
-                    e = ( double )( 1.0f / cbrtf( aa * aa ) ) * emission_time * chi * chi * t.factor_classical;
-                } else {
-                    const double aa = 1.0 + 4.8 * ( 1.0 + chi ) * log( 1.0 + 1.7 * chi ) + 2.44 * chi * chi;
-                    e = ( 1.0 / cbrt( aa * aa ) ) * emission_time * chi * chi * t.factor_classical;
-                }
+                const double aa = 1.0 + 4.8 * ( 1.0 + chi ) * log( 1.0 + 1.7 * chi ) + 2.44 * chi * chi;
+                const double e = ( 1.0 / cbrt( aa * aa ) ) * emission_time * chi * chi * t.factor_classical;
                 const double tmp = e * g / ( g * g - 1.0 );
                 px -= tmp * px;
                 py -= tmp * py;
