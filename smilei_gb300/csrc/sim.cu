@@ -191,8 +191,17 @@ template <class T>
 __device__ __forceinline__ T rsqrt_t( T x );
 template <>
 __device__ __forceinline__ double rsqrt_t<double>( double x ) { return 1.0 / sqrt( x ); }
+// FP32 (mixed form): the hardware approximations (a few ulp), well inside the form's
+// 1e-5 parity bar, instead of the IEEE-rounded sequences
 template <>
-__device__ __forceinline__ float rsqrt_t<float>( float x ) { return 1.0f / sqrtf( x ); }
+__device__ __forceinline__ float rsqrt_t<float>( float x ) { return rsqrtf( x ); }
+
+template <class T>
+__device__ __forceinline__ T rcp_t( T x );
+template <>
+__device__ __forceinline__ double rcp_t<double>( double x ) { return 1.0 / x; }
+template <>
+__device__ __forceinline__ float rcp_t<float>( float x ) { return __fdividef( 1.0f, x ); }
 
 template <int KIND, class T>
 __device__ __forceinline__ T push_t( T qm, T Ex, T Ey, T Ez, T Bx, T By, T Bz, T &px, T &py, T &pz )
@@ -202,7 +211,7 @@ __device__ __forceinline__ T push_t( T qm, T Ex, T Ey, T Ez, T Bx, T By, T Bz, T
         const T umx = px + pxsm, umy = py + pysm, umz = pz + pzsm;
         const T lg = qm * rsqrt_t<T>( T( 1 ) + umx * umx + umy * umy + umz * umz );
         const T Tx = lg * Bx, Ty = lg * By, Tz = lg * Bz;
-        const T inv_det = T( 1 ) / ( T( 1 ) + Tx * Tx + Ty * Ty + Tz * Tz );
+        const T inv_det = rcp_t<T>( T( 1 ) + Tx * Tx + Ty * Ty + Tz * Tz );
         pxsm += ( ( T( 1 ) + Tx * Tx - Ty * Ty - Tz * Tz ) * umx + T( 2 ) * ( Tx * Ty + Tz ) * umy + T( 2 ) * ( Tz * Tx - Ty ) * umz ) * inv_det;
         pysm += ( T( 2 ) * ( Tx * Ty - Tz ) * umx + ( T( 1 ) - Tx * Tx + Ty * Ty - Tz * Tz ) * umy + T( 2 ) * ( Ty * Tz + Tx ) * umz ) * inv_det;
         pzsm += ( T( 2 ) * ( Tz * Tx + Ty ) * umx + T( 2 ) * ( Ty * Tz - Tx ) * umy + ( T( 1 ) - Tx * Tx - Ty * Ty + Tz * Tz ) * umz ) * inv_det;
@@ -221,7 +230,7 @@ __device__ __forceinline__ T push_t( T qm, T Ex, T Ey, T Ez, T Bx, T By, T Bz, T
         us2 = us2 * us2;
         alpha = rsqrt_t<T>( T( 0.5 ) * ( s + sqrt( s * s + T( 4 ) * ( T2 + us2 ) ) ) );
         Tx *= alpha; Ty *= alpha; Tz *= alpha;
-        s = T( 1 ) / ( T( 1 ) + Tx * Tx + Ty * Ty + Tz * Tz );
+        s = rcp_t<T>( T( 1 ) + Tx * Tx + Ty * Ty + Tz * Tz );
         alpha = upx * Tx + upy * Ty + upz * Tz;
         px = s * ( upx + alpha * Tx + Tz * upy - Ty * upz );
         py = s * ( upy + alpha * Ty + Tx * upz - Tz * upx );
@@ -237,7 +246,7 @@ __device__ __forceinline__ T push_t( T qm, T Ex, T Ey, T Ez, T Bx, T By, T Bz, T
         Tx *= lg; Ty *= lg; Tz *= lg;
         const T Tx2 = Tx * Tx, Ty2 = Ty * Ty, Tz2 = Tz * Tz;
         const T TxTy = Tx * Ty, TyTz = Ty * Tz, TzTx = Tz * Tx;
-        const T inv_det = T( 1 ) / ( T( 1 ) + Tx2 + Ty2 + Tz2 );
+        const T inv_det = rcp_t<T>( T( 1 ) + Tx2 + Ty2 + Tz2 );
         const T upx = ( ( T( 1 ) + Tx2 - Ty2 - Tz2 ) * umx + T( 2 ) * ( TxTy + Tz ) * umy + T( 2 ) * ( TzTx - Ty ) * umz ) * inv_det;
         const T upy = ( T( 2 ) * ( TxTy - Tz ) * umx + ( T( 1 ) - Tx2 + Ty2 - Tz2 ) * umy + T( 2 ) * ( TyTz + Tx ) * umz ) * inv_det;
         const T upz = ( T( 2 ) * ( TzTx + Ty ) * umx + T( 2 ) * ( TyTz - Tx ) * umy + ( T( 1 ) - Tx2 - Ty2 + Tz2 ) * umz ) * inv_det;
