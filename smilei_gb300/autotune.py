@@ -15,7 +15,7 @@ import time
 # 3D shapes of at most 64 cells (the per-cell deposit's limit with two thread
 # groups per cell) and 2D shapes of at most 128 cells.
 CANDIDATES_3D = [(4, 4, 4), (2, 4, 8), (8, 4, 2), (4, 4, 2), (4, 2, 4)]
-CANDIDATES_2D = [(8, 8), (4, 16), (16, 4), (8, 16), (4, 8)]
+CANDIDATES_2D = [(8, 8), (4, 16), (16, 4), (8, 16), (4, 8), (4, 4)]
 
 
 def tune_tiles(build, candidates=None, ndim=3, warmup=2, steps=3, log=None):
