@@ -457,10 +457,12 @@ __device__ __forceinline__ float mlp_coop( const MlpView &m, const MlpShared<H> 
 // every lane of a warp (inactive lanes too): the loop is warp-synchronous, so that the
 // lanes that emit through the network evaluate it together, one emission after another.
 // ph.count == null: no macro-photons (then q and n are unused).
-template <int H>
+// P: the arithmetic of the momenta and of the recoil (double for FP64 momenta, float
+// for the mixed form's FP32 momenta).
+template <int H, class P>
 __device__ __forceinline__ void mc_pass_f32( const RadTab &t, const MlpView &m, int use_mlp,
                                              const MlpShared<H == 0 ? 4 : H> &sw, bool active, double dt, double qm2,
-                                             const float *E3, const float *B3, double &px, double &py, double &pz,
+                                             const float *E3, const float *B3, P &px, P &py, P &pz,
                                              float &tp, uint32_t &rs, double wgt, double &rad, unsigned long long &nem,
                                              float &last_chi, const PhotonOut &ph, int64_t q, int64_t n )
 {
@@ -518,12 +520,12 @@ __device__ __forceinline__ void mc_pass_f32( const RadTab &t, const MlpView &m, 
                     const float emission_time = dtf - local_time;
                     const float aa = 1.0f + 4.8f * ( 1.0f + chi ) * logf( 1.0f + 1.7f * chi ) + 2.44f * chi * chi;
                     const float e = ( 1.0f / cbrtf( aa * aa ) ) * emission_time * chi * chi * ( float )t.factor_classical;
-                    const double tmp = ( double )( e * g / ( g * g - 1.0f ) );
-                    const double gd = sqrt( 1.0 + px * px + py * py + pz * pz );
+                    const P tmp = ( P )( e * g / ( g * g - 1.0f ) );
+                    const P gd = sqrt( P( 1 ) + px * px + py * py + pz * pz );
                     px -= tmp * px;
                     py -= tmp * py;
                     pz -= tmp * pz;
-                    rad += wgt * ( gd - sqrt( 1.0 + px * px + py * py + pz * pz ) );
+                    rad += wgt * ( double )( gd - sqrt( P( 1 ) + px * px + py * py + pz * pz ) );
                     local_time = dtf;
                 } else {
                     local_time = dtf;
@@ -542,14 +544,14 @@ __device__ __forceinline__ void mc_pass_f32( const RadTab &t, const MlpView &m, 
             }
         }
         if( emit ) {
-            const double gd = sqrt( 1.0 + px * px + py * py + pz * pz );
-            const double pg = pchi / ( double )chi * ( gd - 1.0 );
-            const double f = ( double )( ( float )pg / sqrtf( g * g - 1.0f ) );
+            const P gd = sqrt( P( 1 ) + px * px + py * py + pz * pz );
+            const double pg = pchi / ( double )chi * ( double )( gd - P( 1 ) );
+            const P f = ( P )( ( float )pg / sqrtf( g * g - 1.0f ) );
             px -= px * f;
             py -= py * f;
             pz -= pz * f;
             if( ph.count && pg >= ph.threshold && i_photon < ph.max_emissions ) {
-                const double inv = 1.0 / sqrt( px * px + py * py + pz * pz );
+                const double inv = 1.0 / sqrt( ( double )( px * px + py * py + pz * pz ) );
                 const unsigned long long o0 = atomicAdd( ph.count, ( unsigned long long )ph.sampling );
                 for( int k = 0; k < ph.sampling; k++ ) {
                     const unsigned long long o = o0 + ( unsigned long long )k;
@@ -564,7 +566,7 @@ __device__ __forceinline__ void mc_pass_f32( const RadTab &t, const MlpView &m, 
                 }
                 i_photon++;
             } else {
-                rad += wgt * ( gd - sqrt( 1.0 + px * px + py * py + pz * pz ) );
+                rad += wgt * ( double )( gd - sqrt( P( 1 ) + px * px + py * py + pz * pz ) );
             }
             nem++;
             tp = -1.0f;
@@ -690,7 +692,8 @@ __global__ void k_monte_carlo( RadTab t, MlpView m, int use_mlp, int64_t n, doub
             tp = ( float )tau[q];
         }
         uint32_t rs = rng_init( seed, first_id + ( uint32_t )q, step );
-        mc_pass_f32<H>( t, m, use_mlp, sw, active, dt, qm2, E3, B3, px, py, pz, tp, rs, w[q], rad, nem, last_chi, ph, q, n );
+        mc_pass_f32<H, double>( t, m, use_mlp, sw, active, dt, qm2, E3, B3, px, py, pz, tp, rs, w[q], rad, nem, last_chi, ph, q,
+                                n );
         if( active ) {
             mom[p] = px;
             mom[n + p] = py;
@@ -785,7 +788,7 @@ __global__ void __launch_bounds__( 128 ) k_radiate_resident( RadTab t, MlpView m
             }
             active = o - r.seg_start[lo] < r.count[lo];
         }
-        double px = 0.0, py = 0.0, pz = 0.0;
+        float px = 0.0f, py = 0.0f, pz = 0.0f;
         float E3[3] = { 0.0f, 0.0f, 0.0f }, B3[3] = { 0.0f, 0.0f, 0.0f }, tp = 0.0f, last_chi = 0.0f, wq = 0.0f;
         if( active ) {
             const unsigned k = r.key[o];
@@ -813,12 +816,12 @@ __global__ void __launch_bounds__( 128 ) k_radiate_resident( RadTab t, MlpView m
             wq = r.w[o];
         }
         uint32_t rs = rng_init( r.seed, ( uint32_t )o, step );
-        mc_pass_f32<H>( t, m, use_mlp, sw, active, r.dt, r.qm2, E3, B3, px, py, pz, tp, rs, ( double )wq, rad, nem,
-                        last_chi, PhotonOut{}, 0, 0 );
+        mc_pass_f32<H, float>( t, m, use_mlp, sw, active, r.dt, r.qm2, E3, B3, px, py, pz, tp, rs, ( double )wq, rad, nem,
+                               last_chi, PhotonOut{}, 0, 0 );
         if( active ) {
-            r.p[0][o] = ( float )px;
-            r.p[1][o] = ( float )py;
-            r.p[2][o] = ( float )pz;
+            r.p[0][o] = px;
+            r.p[1][o] = py;
+            r.p[2][o] = pz;
             r.tau[o] = tp;
         }
     }
