@@ -246,9 +246,9 @@ def run_gpu(args, rank, world, local_rank):
     # e2e: the same step driven from host buffers through the C ABI
     e2e = None
     if not args.no_e2e:
-        nbytes = sim.state_bytes(0)
+        nbytes = sim.packed_bytes(0)
         host = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
-        sim.copy_state(0, host.data_ptr(), False)
+        sim.pack_state(0, host.data_ptr())
         torch.cuda.synchronize()
         ke = max(1, min(args.steps, args.e2e_steps))
         e0 = torch.cuda.Event(enable_timing=True)
@@ -258,9 +258,9 @@ def run_gpu(args, rank, world, local_rank):
         torch.cuda.synchronize()
         e0.record(stream)
         for _ in range(ke):
-            sim.copy_state(0, host.data_ptr(), True)
+            sim.unpack_state(0, host.data_ptr())
             sim.step(1)
-            sim.copy_state(0, host.data_ptr(), False)
+            sim.pack_state(0, host.data_ptr())
             sim.energy()
         e1.record(stream)
         torch.cuda.synchronize()

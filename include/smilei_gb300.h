@@ -228,6 +228,17 @@ int sg_sim_charge_residual( sg_sim *sim, double *residual, double *rho_max );
 int sg_sim_state_bytes( sg_sim *sim, int species, size_t *bytes );
 int sg_sim_copy_state( sg_sim *sim, int species, void *host, int to_device );
 
+/* The same state packed: an int64 particle count, the per-tile counts, then every
+ * tile's particles back to back, plane by plane (no segment slack or holes, about 20 %
+ * fewer bytes than the raw state).  pack copies it device -> host (asynchronous with
+ * pinned memory); unpack copies it host -> device into the current layout, where every
+ * tile's count must fit its segment (it synchronises to check that; a species'
+ * optical depths stay on the device).  Restoring what was packed leaves the simulation
+ * as it was. */
+int sg_sim_packed_bytes( sg_sim *sim, int species, size_t *bytes );
+int sg_sim_pack_state( sg_sim *sim, int species, void *host );
+int sg_sim_unpack_state( sg_sim *sim, int species, const void *host );
+
 /* Adds a Gaussian 2D laser injected through the Silver-Mueller condition on xmin
  * (LaserGaussian2D, src/Python/pyprofiles.py:507; ElectroMagnBC2D_SM::apply,
  * src/ElectroMagnBC/ElectroMagnBC2D_SM.cpp:118).  p = {a0, omega, waist, focus_x,

@@ -1846,6 +1846,66 @@ __global__ void k_convert( int64_t n, const Src *__restrict__ s, Dst *__restrict
     if( i < n ) d[i] = ( Dst )s[i];
 }
 
+__host__ __device__ inline size_t packed_header_bytes( int nt ) { return ( 8 + 4 * ( size_t )nt + 255 ) & ~( size_t )255; }
+
+// Packed state: the particles of every tile back to back (tile order), plane by plane,
+// behind the per-tile counts; pack reads the segments, unpack writes them back into the
+// current layout (a tile's count must fit its segment).
+template <bool MIXED>
+__device__ __forceinline__ void packed_planes( const PBuf<MIXED> &, int ndim, int64_t n, char *base, PBuf<MIXED> &pk )
+{
+    using PT = typename std::conditional<MIXED, float, double>::type;
+    char *q = base;
+    if constexpr( MIXED ) {
+        pk.key = reinterpret_cast<unsigned *>( q );
+        q += 4 * n;
+        for( int d = 0; d < 3; d++ ) {
+            pk.d[d] = d < ndim ? reinterpret_cast<float *>( q ) : nullptr;
+            if( d < ndim ) q += 4 * n;
+        }
+    } else {
+        for( int d = 0; d < 3; d++ ) {
+            pk.x[d] = d < ndim ? reinterpret_cast<double *>( q ) : nullptr;
+            if( d < ndim ) q += 8 * n;
+        }
+    }
+    for( int c = 0; c < 3; c++ ) {
+        pk.p[c] = reinterpret_cast<PT *>( q );
+        q += sizeof( PT ) * n;
+    }
+    pk.w = reinterpret_cast<PT *>( q );
+    pk.tau = nullptr;
+}
+
+template <bool MIXED, bool PACK>
+__global__ void k_pack( int ndim, int nt, const int64_t *__restrict__ seg_start, const int *__restrict__ cap,
+                        int *__restrict__ count, const int64_t *__restrict__ off, PBuf<MIXED> b, int64_t n,
+                        char *__restrict__ packed, int *__restrict__ status )
+{
+    const int t = blockIdx.x;
+    if( t >= nt ) return;
+    int *counts = reinterpret_cast<int *>( packed + 8 ); // behind the particle count (int64)
+    PBuf<MIXED> pk;
+    packed_planes<MIXED>( b, ndim, n, packed + packed_header_bytes( nt ), pk );
+    b.tau = nullptr; // the optical depth stays in place
+    int c;
+    if constexpr( PACK ) {
+        c = count[t];
+        if( threadIdx.x == 0 ) counts[t] = c;
+    } else {
+        c = counts[t];
+        if( c > cap[t] || c < 0 ) {
+            if( threadIdx.x == 0 ) atomicCAS( status, 0, SG_ERR_ARG );
+            return;
+        }
+        if( threadIdx.x == 0 ) count[t] = c;
+    }
+    for( int i = threadIdx.x; i < c; i += blockDim.x ) {
+        if constexpr( PACK ) copy_particle<MIXED>( b, seg_start[t] + i, pk, off[t] + i, ndim );
+        else copy_particle<MIXED>( pk, off[t] + i, b, seg_start[t] + i, ndim );
+    }
+}
+
 // Back to absolute FP64 positions (tile-sorted order) for output.
 template <int DIM, bool MIXED>
 __global__ void k_export( GridInfo g, int nt, const int64_t *__restrict__ seg_start, const int *__restrict__ count,
@@ -1999,6 +2059,8 @@ struct sg_sim {
     int *slot_tile = nullptr;            // per particle slot: its tile after a shift (-1: removed)
     int64_t slot_cap = 0;
     unsigned long long *d_wcount = nullptr; // [0] removed, [1] created
+    void *pack_mem = nullptr;    // staging of the packed state
+    size_t pack_bytes = 0;
 };
 
 namespace sg {
@@ -2656,6 +2718,7 @@ int sg_sim_destroy( sg_sim *S )
     release( S->fill );
     release( S->d_red );
     release( S->win_scratch );
+    release( S->pack_mem );
     release( S->slot_tile );
     release( S->d_wcount );
     for( int i = 0; i < 4; i++ )
@@ -3122,6 +3185,80 @@ int sg_sim_copy_state( sg_sim *S, int species, void *host, int to_device )
     sg_sim_state_bytes( S, species, &bytes );
     if( to_device ) SG_CUDA_TRY( cudaMemcpyAsync( s.mem[s.cur], host, bytes, cudaMemcpyHostToDevice, S->stream ) );
     else SG_CUDA_TRY( cudaMemcpyAsync( host, s.mem[s.cur], bytes, cudaMemcpyDeviceToHost, S->stream ) );
+    return SG_OK;
+}
+
+int sg_sim_packed_bytes( sg_sim *S, int species, size_t *bytes )
+{
+    SG_REQUIRE( S && bytes, "NULL argument" );
+    SG_REQUIRE( species >= 0 && species < ( int )S->sp.size(), "no species %d", species );
+    const int nd = S->g.ndim;
+    const size_t per = S->mixed ? ( size_t )( 4 + 4 * nd + 16 ) : ( size_t )( 8 * nd + 32 );
+    *bytes = packed_header_bytes( S->g.ntiles ) + per * ( size_t )S->sp[species].npart;
+    return SG_OK;
+}
+
+// staging buffer of at least `bytes` on the device
+static int packed_staging( sg_sim *S, size_t bytes )
+{
+    if( S->pack_bytes >= bytes ) return SG_OK;
+    release( S->pack_mem );
+    S->pack_mem = nullptr;
+    S->pack_bytes = 0;
+    SG_CUDA_TRY( cudaMalloc( &S->pack_mem, bytes ) );
+    S->pack_bytes = bytes;
+    return SG_OK;
+}
+
+int sg_sim_pack_state( sg_sim *S, int species, void *host )
+{
+    SG_REQUIRE( S && host, "NULL argument" );
+    SG_REQUIRE( species >= 0 && species < ( int )S->sp.size(), "no species %d", species );
+    SpeciesState &s = S->sp[species];
+    const int nt = S->g.ntiles, nd = S->g.ndim;
+    size_t bytes = 0;
+    int r = sg_sim_packed_bytes( S, species, &bytes );
+    if( r ) return r;
+    r = packed_staging( S, bytes );
+    if( r ) return r;
+    char *stg = static_cast<char *>( S->pack_mem );
+    const int64_t n = s.npart;
+    r = exclusive_scan<int>( s.count[s.cur], nt, S->tmp_start, S->scan_scratch, S->stream );
+    if( r ) return r;
+    SG_CUDA_TRY( cudaMemcpyAsync( stg, &s.npart, 8, cudaMemcpyHostToDevice, S->stream ) );
+    if( S->mixed ) k_pack<true, true><<<nt, 128, 0, S->stream>>>( nd, nt, s.seg_start, s.cap, s.count[s.cur], S->tmp_start, s.bm[s.cur], n, stg, S->d_flags );
+    else k_pack<false, true><<<nt, 128, 0, S->stream>>>( nd, nt, s.seg_start, s.cap, s.count[s.cur], S->tmp_start, s.bd[s.cur], n, stg, S->d_flags );
+    SG_LAUNCH_CHECK( "k_pack" );
+    SG_CUDA_TRY( cudaMemcpyAsync( host, stg, bytes, cudaMemcpyDeviceToHost, S->stream ) );
+    return SG_OK;
+}
+
+int sg_sim_unpack_state( sg_sim *S, int species, const void *host )
+{
+    SG_REQUIRE( S && host, "NULL argument" );
+    SG_REQUIRE( species >= 0 && species < ( int )S->sp.size(), "no species %d", species );
+    SpeciesState &s = S->sp[species];
+    const int nt = S->g.ntiles, nd = S->g.ndim;
+    int64_t n = 0;
+    std::memcpy( &n, host, 8 );
+    SG_REQUIRE( n == s.npart, "the packed state holds %lld particles, the species %lld", ( long long )n,
+                ( long long )s.npart );
+    size_t bytes = 0;
+    int r = sg_sim_packed_bytes( S, species, &bytes );
+    if( r ) return r;
+    r = packed_staging( S, bytes );
+    if( r ) return r;
+    char *stg = static_cast<char *>( S->pack_mem );
+    SG_CUDA_TRY( cudaMemcpyAsync( stg, host, bytes, cudaMemcpyHostToDevice, S->stream ) );
+    r = exclusive_scan<int>( reinterpret_cast<const int *>( stg + 8 ), nt, S->tmp_start, S->scan_scratch, S->stream );
+    if( r ) return r;
+    SG_CUDA_TRY( cudaMemsetAsync( S->d_flags, 0, sizeof( int ), S->stream ) );
+    if( S->mixed ) k_pack<true, false><<<nt, 128, 0, S->stream>>>( nd, nt, s.seg_start, s.cap, s.count[s.cur], S->tmp_start, s.bm[s.cur], n, stg, S->d_flags );
+    else k_pack<false, false><<<nt, 128, 0, S->stream>>>( nd, nt, s.seg_start, s.cap, s.count[s.cur], S->tmp_start, s.bd[s.cur], n, stg, S->d_flags );
+    SG_LAUNCH_CHECK( "k_pack" );
+    SG_CUDA_TRY( cudaMemcpyAsync( S->h_flags, S->d_flags, sizeof( int ), cudaMemcpyDeviceToHost, S->stream ) );
+    SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
+    if( S->h_flags[0] ) return set_error( SG_ERR_ARG, "a tile of the packed state exceeds its segment in the current layout" );
     return SG_OK;
 }
 

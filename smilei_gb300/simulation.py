@@ -103,6 +103,19 @@ class Simulation:
         check(_lib.lib().sg_sim_state_bytes(self._h, s, ctypes.byref(b)), "state_bytes")
         return b.value
 
+    def packed_bytes(self, s: int) -> int:
+        b = ctypes.c_size_t()
+        check(_lib.lib().sg_sim_packed_bytes(self._h, s, ctypes.byref(b)), "packed_bytes")
+        return b.value
+
+    def pack_state(self, s: int, host_ptr: int):
+        """Packed state of species s (tile counts + particles, no slack) to a host buffer of packed_bytes(s)."""
+        check(_lib.lib().sg_sim_pack_state(self._h, s, host_ptr), "pack_state")
+
+    def unpack_state(self, s: int, host_ptr: int):
+        """Restores a packed state of species s into the current layout."""
+        check(_lib.lib().sg_sim_unpack_state(self._h, s, host_ptr), "unpack_state")
+
     def copy_state(self, s: int, host_ptr: int, to_device: bool):
         """Raw state of species s to/from a host buffer of state_bytes(s) bytes (pinned for async)."""
         check(_lib.lib().sg_sim_copy_state(self._h, s, host_ptr, int(bool(to_device))), "copy_state")
