@@ -133,3 +133,37 @@ def test_eager_steps_match_graph_steps(mods):
         sim.close()
     for k in FIELDS:
         assert rel_err(out[1][k], out[0][k]) <= 1e-12, k
+
+
+def test_window_with_a_radiating_species(mods):
+    """The optical depth travels with the particles through window shifts, creation and
+    re-layouts: a radiating species in a moving window runs, keeps its count in the
+    plateau, and its new particles start with a spent optical depth (they emit like the
+    others: the emission count grows every step)."""
+    from smilei_gb300 import radiation
+    g = np.load(__import__("os").path.join(__import__("os").path.dirname(__file__), "golden", "radiation.npz"))
+    f_dn, f_cl, inv_es = radiation.normalised_factors(2.0 * np.pi * 299792458.0 / 1e-6)
+    T = radiation.RadiationTables(g["integfochi"], g["integfochi_min"], g["integfochi_max"], g["xi_table"],
+                                  g["xi_min"], g["xi_max"], g["xi_axis1_min"], f_dn, f_cl, inv_es)
+    T.set_fp32_math(True)
+    sim = mods.Simulation(N_CELLS, CL, DT, form="mixed", boundaries=("open", "periodic"))
+    sim.add_species(1.0, -1.0, "vay", np.zeros((2, 0)), np.zeros((3, 0)), np.zeros(0))
+    sim.set_species_profile(0, 0.5, 4, temperature=0.0)
+    sim.fill_species(0)
+    # crossed fields in which electrons at rest stay at rest would not radiate: give the
+    # plasma a strong uniform E_y so that it is accelerated and emits
+    e = sim.get_field("Ey")
+    e[:] = 400.0
+    sim.set_field("Ey", e)
+    sim.set_species_radiation(0, T, None, seed=3)
+    sim.set_moving_window(0.0, 1.0, 4)
+    counts, emissions = [], []
+    for _ in range(12):
+        sim.step(1)
+        counts.append(sim.species_count(0))
+        emissions.append(sim.radiation_stats(0)[1])
+    assert sim.window_state()[2] >= 2
+    assert all(c == counts[0] for c in counts), counts
+    assert emissions[-1] > 0 and all(b >= a for a, b in zip(emissions, emissions[1:]))
+    sim.close()
+    T.close()
