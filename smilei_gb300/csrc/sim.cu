@@ -432,17 +432,28 @@ constexpr int cells_chunk_fit( size_t tile_bytes, int tc )
     return fixed < CELLS_SMEM_TARGET ? ( int )( ( CELLS_SMEM_TARGET - fixed ) / per ) : 0;
 }
 
-// The chunk of the default tile shapes (4x4x4 in 3D, 8x8 in 2D; FP32 tiles of
-// 6 field and 3 current components with T + 3 and T + 4 points per dimension).
-constexpr int fixt_chunk( int dim )
+// Tile shapes with their own kernel instances (code FT): 0 any shape (runtime), 1 the
+// default (4x4x4 in 3D, 8x8 in 2D), 2 8x16 (2D), 3 4x4 (2D); the 2D ones are the shapes
+// the autotuner picks for the wakefield and for dense bunches.
+constexpr int ft_tile( int dim, int ft, int d )
+{
+    return dim == 3 ? ( d < 3 ? 4 : 1 ) : ( d == 2 ? 1 : ( ft == 2 ? ( d == 0 ? 8 : 16 ) : ( ft == 3 ? 4 : 8 ) ) );
+}
+constexpr int ft_shift( int t ) { return t == 16 ? 4 : ( t == 8 ? 3 : ( t == 4 ? 2 : 0 ) ); }
+
+// The chunk of such a shape: FP32 tiles of 6 field and 3 current components with
+// T + 3 and T + 4 points per dimension.
+constexpr int fixt_chunk( int dim, int ft )
 {
     return dim == 3 ? cells_chunk_fit( ( size_t )( 6 * 7 * 7 * 7 + 3 * 8 * 8 * 8 ) * 4, 64 ) & ~31
-                    : cells_chunk_fit( ( size_t )( 6 * 11 * 11 + 3 * 12 * 12 ) * 4, 64 ) & ~31;
+                    : cells_chunk_fit( ( size_t )( 6 * ( ft_tile( 2, ft, 0 ) + 3 ) * ( ft_tile( 2, ft, 1 ) + 3 ) +
+                                                   3 * ( ft_tile( 2, ft, 0 ) + 4 ) * ( ft_tile( 2, ft, 1 ) + 4 ) ) * 4,
+                                       ft_tile( 2, ft, 0 ) * ft_tile( 2, ft, 1 ) ) & ~31;
 }
 
-// FIXT: the tile is the default shape (4x4x4 in 3D, 8x8 in 2D), known at compile
-// time, so tile and stencil offsets fold into immediates; its chunk is fixt_chunk.
-template <int DIM, bool MIXED, int KIND, bool CELLS, bool FIXT = false>
+// FT > 0: the tile shape is known at compile time, so tile and stencil offsets fold into
+// immediates; the chunk is fixt_chunk.
+template <int DIM, bool MIXED, int KIND, bool CELLS, int FT = 0>
 __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_particles(
     GridInfo g_arg, Fields<typename std::conditional<MIXED, float, double>::type> f, SpecParams sp, PBuf<MIXED> in,
     PBuf<MIXED> out, const int64_t *__restrict__ seg_start, const int *__restrict__ cap,
@@ -450,16 +461,14 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
     int *__restrict__ ovf_count, int ovf_cap, int *__restrict__ status, int nmax_arg, int *__restrict__ removed )
 {
     using T = typename std::conditional<MIXED, float, double>::type;
-    const int nmax = FIXT ? fixt_chunk( DIM ) : nmax_arg;
+    const int nmax = FT ? fixt_chunk( DIM, FT ) : nmax_arg;
     GridInfo g = g_arg;
-    if constexpr( FIXT ) {
-        constexpr int t = DIM == 3 ? 4 : 8, ts = DIM == 3 ? 2 : 3;
-        g.T[0] = t;
-        g.T[1] = t;
-        g.T[2] = DIM == 3 ? t : 1;
-        g.tshift[0] = ts;
-        g.tshift[1] = ts;
-        g.tshift[2] = DIM == 3 ? ts : 0;
+    if constexpr( FT > 0 ) {
+#pragma unroll
+        for( int d = 0; d < 3; d++ ) {
+            g.T[d] = ft_tile( DIM, FT, d );
+            g.tshift[d] = ft_shift( ft_tile( DIM, FT, d ) );
+        }
     }
     extern __shared__ __align__( 16 ) unsigned char smem_raw[];
     T *sF = reinterpret_cast<T *>( smem_raw );
@@ -2116,13 +2125,22 @@ int launch_particles( sg_sim *S, SpeciesState &s, cudaStream_t st )
         chunk = std::max( 1, std::min( s.max_cap, fit & ~31 ) );
         if( tc <= ( DIM == 3 ? 64 : 128 ) && fit >= 128 ) {
             const GridInfo &g = S->g;
-            const bool fixt = DIM == 3 ? ( g.T[0] == 4 && g.T[1] == 4 && g.T[2] == 4 ) : ( g.T[0] == 8 && g.T[1] == 8 );
-            if( fixt ) {
+            int ft = 0;
+            if( DIM == 3 ) ft = ( g.T[0] == 4 && g.T[1] == 4 && g.T[2] == 4 ) ? 1 : 0;
+            else if( g.T[0] == 8 && g.T[1] == 8 ) ft = 1;
+            else if( g.T[0] == 8 && g.T[1] == 16 ) ft = 2;
+            else if( g.T[0] == 4 && g.T[1] == 4 ) ft = 3;
+            if( ft ) {
                 // the chunk is a compile-time constant of the kernel
-                chunk = fixt_chunk( DIM );
+                chunk = fixt_chunk( DIM, ft );
                 if( chunk != ( fit & ~31 ) ) return set_error( SG_ERR_ARG, "per-cell chunk mismatch (%d, %d)", chunk, fit & ~31 );
             }
-            kern = fixt ? k_step_particles<DIM, MIXED, KIND, true, true> : k_step_particles<DIM, MIXED, KIND, true>;
+            kern = k_step_particles<DIM, MIXED, KIND, true>;
+            if( ft == 1 ) kern = k_step_particles<DIM, MIXED, KIND, true, 1>;
+            if constexpr( DIM == 2 ) {
+                if( ft == 2 ) kern = k_step_particles<DIM, MIXED, KIND, true, 2>;
+                if( ft == 3 ) kern = k_step_particles<DIM, MIXED, KIND, true, 3>;
+            }
             smem += cells_smem_bytes( tc, chunk );
         }
     }
