@@ -2382,6 +2382,33 @@ int place_staged( sg_sim *S, SpeciesState &s, int64_t n, PBuf<MIXED> st, const i
     return SG_OK;
 }
 
+// The per-cell chunk launch_particles passes for a largest segment of max_cap (0 for
+// the FP64 form, whose kernel does not use it).  A new layout that keeps it, the
+// segment tables and the buffers keeps the captured graphs valid.
+template <int DIM>
+int launch_chunk_dim( const sg_sim *S, int max_cap )
+{
+    if( !S->mixed ) return 0;
+    const GridInfo &g = S->g;
+    const int tc = g.T[0] * g.T[1] * ( DIM == 3 ? g.T[2] : 1 );
+    const int fit = cells_chunk_fit( S->smem_bytes, tc );
+    int chunk = std::max( 1, std::min( max_cap, fit & ~31 ) );
+    if( tc <= ( DIM == 3 ? 64 : 128 ) && fit >= 128 ) {
+        int ft = 0;
+        if( DIM == 3 ) ft = ( g.T[0] == 4 && g.T[1] == 4 && g.T[2] == 4 ) ? 1 : 0;
+        else if( g.T[0] == 8 && g.T[1] == 8 ) ft = 1;
+        else if( g.T[0] == 8 && g.T[1] == 16 ) ft = 2;
+        else if( g.T[0] == 4 && g.T[1] == 4 ) ft = 3;
+        if( ft ) chunk = fixt_chunk( DIM, ft );
+    }
+    return chunk;
+}
+
+int launch_chunk( const sg_sim *S, int max_cap )
+{
+    return S->g.ndim == 3 ? launch_chunk_dim<3>( S, max_cap ) : launch_chunk_dim<2>( S, max_cap );
+}
+
 // Steps within which a second spill doubles a species' capacity slack.
 constexpr int64_t RELAYOUT_WINDOW = 64;
 
@@ -2415,9 +2442,10 @@ int relayout( sg_sim *S, SpeciesState &s, int nspill )
     else
         k_relayout_tiles<false><<<nt, 128, 0, S->stream>>>( S->g.ndim, nt, s.seg_start, s.cap, s.count[s.cur], old_bd, S->tmp_start, s.bd[dst_buf], S->fill );
     SG_LAUNCH_CHECK( "k_relayout_tiles" );
-    // new layout becomes current
-    std::swap( s.seg_start, S->tmp_start );
-    std::swap( s.cap, S->tmp_cap );
+    // new layout becomes current (copied into the same tables, which the graphs hold)
+    const int old_chunk = launch_chunk( S, s.max_cap );
+    SG_CUDA_TRY( cudaMemcpyAsync( s.seg_start, S->tmp_start, nt * sizeof( int64_t ), cudaMemcpyDeviceToDevice, S->stream ) );
+    SG_CUDA_TRY( cudaMemcpyAsync( s.cap, S->tmp_cap, nt * sizeof( int ), cudaMemcpyDeviceToDevice, S->stream ) );
     s.max_cap = new_max_cap;
     if( S->mixed ) r = place_staged<true>( S, s, nspill, s.om, s.ovf_tile, dst_buf );
     else r = place_staged<false>( S, s, nspill, s.od, s.ovf_tile, dst_buf );
@@ -2433,7 +2461,9 @@ int relayout( sg_sim *S, SpeciesState &s, int nspill )
         }
     }
     s.cur = dst_buf;
-    drop_graphs( S );
+    // the graphs hold one buffer parity for all species together: a re-layout of one
+    // species among several breaks it
+    if( realloc || S->sp.size() > 1 || launch_chunk( S, s.max_cap ) != old_chunk ) drop_graphs( S );
     return SG_OK;
 }
 
@@ -2510,9 +2540,11 @@ int rebuild_species( sg_sim *S, SpeciesState &s, int shift, int x0, int x1 )
         SG_LAUNCH_CHECK( "k_inject (place)" );
     }
     SG_CUDA_TRY( cudaMemcpyAsync( s.count[dst], S->fill, nt * sizeof( int ), cudaMemcpyDeviceToDevice, st ) );
+    // new layout into the same tables, which the graphs hold
+    SG_CUDA_TRY( cudaMemcpyAsync( s.seg_start, S->tmp_start, nt * sizeof( int64_t ), cudaMemcpyDeviceToDevice, st ) );
+    SG_CUDA_TRY( cudaMemcpyAsync( s.cap, S->tmp_cap, nt * sizeof( int ), cudaMemcpyDeviceToDevice, st ) );
     SG_CUDA_TRY( cudaStreamSynchronize( st ) );
-    std::swap( s.seg_start, S->tmp_start );
-    std::swap( s.cap, S->tmp_cap );
+    const int old_chunk = launch_chunk( S, s.max_cap );
     s.max_cap = new_max_cap;
     s.cur = dst;
     s.npart += ( int64_t )wc[1] - ( int64_t )wc[0];
@@ -2524,7 +2556,7 @@ int rebuild_species( sg_sim *S, SpeciesState &s, int shift, int x0, int x1 )
             release( old_tau[1] );
         }
     }
-    drop_graphs( S );
+    if( realloc || launch_chunk( S, s.max_cap ) != old_chunk ) drop_graphs( S );
     return SG_OK;
 }
 
@@ -2562,6 +2594,7 @@ int window_shift( sg_sim *S )
         SG_LAUNCH_CHECK( "k_window_shift_field" );
         SG_CUDA_TRY( cudaMemcpyAsync( arrays[a], S->win_scratch, n * S->esz, cudaMemcpyDeviceToDevice, st ) );
     }
+    const bool lasers_were_on = S->obc.nlaser > 0;
     S->obc.nlaser = 0;
     OpenBC xmin = S->obc;
     xmin.side_mask = 1;
@@ -2576,7 +2609,7 @@ int window_shift( sg_sim *S )
     }
     SG_CUDA_TRY( cudaStreamSynchronize( st ) );
     S->win_shifts++;
-    drop_graphs( S );
+    if( lasers_were_on ) drop_graphs( S ); // the boundary kernel holds the lasers by value
     return SG_OK;
 }
 
