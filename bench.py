@@ -315,7 +315,8 @@ def run_gpu_lwfa(args, rank, world, local_rank):
         sm.fill_species(0)
         return sm
 
-    tile, tuning = ([args.tile] * 2 if args.tile else None), None
+    # 8x16 tiles unless asked otherwise: the autotuner's pick for this workload
+    tile, tuning = ([args.tile] * 2 if args.tile else [8, 16]), None
     if args.autotune:
         from smilei_gb300 import autotune
         best, times = autotune.tune_tiles(make, ndim=2)
