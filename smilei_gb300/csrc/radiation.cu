@@ -545,21 +545,21 @@ __device__ __forceinline__ void mc_pass_f32( const RadTab &t, const MlpView &m, 
         }
         if( emit ) {
             const P gd = sqrt( P( 1 ) + px * px + py * py + pz * pz );
-            const double pg = pchi / ( double )chi * ( double )( gd - P( 1 ) );
+            const P pg = ( P )pchi / ( P )chi * ( gd - P( 1 ) );
             const P f = ( P )( ( float )pg / sqrtf( g * g - 1.0f ) );
             px -= px * f;
             py -= py * f;
             pz -= pz * f;
-            if( ph.count && pg >= ph.threshold && i_photon < ph.max_emissions ) {
+            if( ph.count && ( double )pg >= ph.threshold && i_photon < ph.max_emissions ) {
                 const double inv = 1.0 / sqrt( ( double )( px * px + py * py + pz * pz ) );
                 const unsigned long long o0 = atomicAdd( ph.count, ( unsigned long long )ph.sampling );
                 for( int k = 0; k < ph.sampling; k++ ) {
                     const unsigned long long o = o0 + ( unsigned long long )k;
                     if( o >= ( unsigned long long )ph.cap ) break;
                     for( int dd = 0; dd < ph.ndim; dd++ ) ph.ph_pos[dd * ph.cap + o] = ph.pos[dd * n + q];
-                    ph.ph_mom[o] = pg * px * inv;
-                    ph.ph_mom[ph.cap + o] = pg * py * inv;
-                    ph.ph_mom[2 * ph.cap + o] = pg * pz * inv;
+                    ph.ph_mom[o] = ( double )pg * px * inv;
+                    ph.ph_mom[ph.cap + o] = ( double )pg * py * inv;
+                    ph.ph_mom[2 * ph.cap + o] = ( double )pg * pz * inv;
                     ph.ph_w[o] = wgt * ( 1.0 / ph.sampling );
                     ph.ph_chi[o] = pchi;
                     ph.ph_tau[o] = -1.0;
@@ -755,7 +755,7 @@ __device__ __forceinline__ float gather2( const float *__restrict__ F, int ny, i
 #pragma unroll
     for( int a = 0; a < 3; a++ ) {
         const float *row = F + ( int64_t )( bx + a ) * ny + by;
-        r = fmaf( cx[a], cy[0] * row[0] + cy[1] * row[1] + cy[2] * row[2], r );
+        r = fmaf( cx[a], cy[0] * __ldg( row ) + cy[1] * __ldg( row + 1 ) + cy[2] * __ldg( row + 2 ), r );
     }
     return r;
 }
