@@ -737,7 +737,8 @@ def main():
             print(json.dumps({
                 "metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": res["ms"] / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded bunch, host)",
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.resident else "f64",
+                "data": "synthetic (seeded bunch, host)",
                 "config": {"workload": workload, "form": "mixed, resident step" if args.resident else "fp64 operators",
                            "global_particles": res["n"] * world,
                            "wall_ms_per_step": res["wall_ms_per_step"], "radiated_energy": res["radiated"],
@@ -745,7 +746,9 @@ def main():
                            "tile": res.get("tile"), "autotune_ms_per_step": res.get("tuning"),
                            "l2": "inputs larger than L2"},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": res["peak"], "unit": "GB/s",
-                             "frac": achieved / res["peak"], "traffic": None, "kernel": "operator chain",
+                             "frac": achieved / res["peak"], "traffic": None,
+                             "kernel": "resident step (radiation pass, particle kernel, fields)" if args.resident
+                             else "operator chain",
                              "algorithmic_bytes_per_particle_step": res["b_per"],
                              "peak_source": res["peak_kind"]},
                 "cpu_baseline": cpu, "e2e": None,
