@@ -258,9 +258,13 @@ def run_gpu(args, rank, world, local_rank):
         torch.cuda.synchronize()
         e0.record(stream)
         for _ in range(ke):
-            sim.unpack_state(0, host.data_ptr())
-            sim.step(1)
-            sim.pack_state(0, host.data_ptr())
+            if args.e2e_chunks > 0:
+                # the copy in overlaps the particle kernel over tile ranges
+                sim.step_host(0, host.data_ptr(), chunks=args.e2e_chunks)
+            else:
+                sim.unpack_state(0, host.data_ptr())
+                sim.step(1)
+                sim.pack_state(0, host.data_ptr())
             sim.energy()
         e1.record(stream)
         torch.cuda.synchronize()
@@ -673,6 +677,8 @@ def main():
     ap.add_argument("--cpu-cells", type=int, default=64)
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--e2e-chunks", type=int, default=32,
+                    help="tile ranges of the streamed host step (0: unpack, step, pack one after another)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="thermal", choices=["thermal", "uneven", "lwfa", "radiation"])

@@ -239,6 +239,18 @@ int sg_sim_packed_bytes( sg_sim *sim, int species, size_t *bytes );
 int sg_sim_pack_state( sg_sim *sim, int species, void *host );
 int sg_sim_unpack_state( sg_sim *sim, int species, const void *host );
 
+/* One step of a species whose particles live in host memory between steps (the
+ * reference's Particles vectors on the host, src/Particles/Particles.h:48): reads the
+ * packed state from host_in, steps the whole simulation, and writes the new packed
+ * state to host_out (host_out may equal host_in; it needs packed_bytes() bytes, and
+ * particles removed at open boundaries only shrink it).  The copy in runs in `chunks`
+ * tile ranges of about equal particle counts on a second stream, and each range is
+ * stepped as soon as it is in, so the copies overlap the particle kernel.  Same result
+ * as unpack_state, step(1), pack_state (up to the order of floating-point atomics in
+ * the current deposit).  Not for a radiating species or a step in which the window
+ * moves.  Returns after host_out is written. */
+int sg_sim_step_host( sg_sim *sim, int species, const void *host_in, void *host_out, int chunks );
+
 /* Adds a Gaussian 2D laser injected through the Silver-Mueller condition on xmin
  * (LaserGaussian2D, src/Python/pyprofiles.py:507; ElectroMagnBC2D_SM::apply,
  * src/ElectroMagnBC/ElectroMagnBC2D_SM.cpp:118).  p = {a0, omega, waist, focus_x,

@@ -33,6 +33,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <vector>
 
@@ -95,6 +96,7 @@ struct SpecParams {
     double cw;       // charge * inverse cell volume (per unit weight)
     double cr[3];    // cw * dx_d / dt: Esirkepov current factor per unit weight
     double vs[3];    // dt / dx_d: displacement in cells per unit velocity
+    int tile0;       // first tile of the launch (block b steps tile tile0 + b)
 };
 
 // Packed node index of the mixed form: 3D x:11 y:10 z:10 bits, 2D x:16 y:16 bits.
@@ -488,7 +490,7 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
     __shared__ int sNX;         // length of that list
     __shared__ int sXc[4];      // node-changing particles per class (x, y, z only; several)
 
-    const int tile = blockIdx.x;
+    const int tile = blockIdx.x + sp.tile0;
     int tz = 0, ty, tx;
     if( DIM == 3 ) {
         tz = tile % g.nt[2];
@@ -1889,9 +1891,9 @@ __device__ __forceinline__ void packed_planes( const PBuf<MIXED> &, int ndim, in
 template <bool MIXED, bool PACK>
 __global__ void k_pack( int ndim, int nt, const int64_t *__restrict__ seg_start, const int *__restrict__ cap,
                         int *__restrict__ count, const int64_t *__restrict__ off, PBuf<MIXED> b, int64_t n,
-                        char *__restrict__ packed, int *__restrict__ status )
+                        char *__restrict__ packed, int *__restrict__ status, int t0 )
 {
-    const int t = blockIdx.x;
+    const int t = blockIdx.x + t0;
     if( t >= nt ) return;
     int *counts = reinterpret_cast<int *>( packed + 8 ); // behind the particle count (int64)
     PBuf<MIXED> pk;
@@ -2070,6 +2072,14 @@ struct sg_sim {
     unsigned long long *d_wcount = nullptr; // [0] removed, [1] created
     void *pack_mem = nullptr;    // staging of the packed state
     size_t pack_bytes = 0;
+    cudaStream_t copy_stream = nullptr; // host-to-device copies of a streamed step
+    cudaStream_t out_stream = nullptr;  // its device-to-host copies
+    std::vector<cudaEvent_t> copy_ev;   // [0] staging free, [1] header copied, [2 + c] chunk c copied,
+                                        // [2 + chunks + c] chunk c packed
+    void *pack_out_mem = nullptr;       // staging of the packed state a streamed step writes
+    size_t pack_out_cap = 0;
+    int64_t *pack_off = nullptr;        // its per-tile offsets
+    int64_t *h_chunk_end = nullptr;     // pinned: first and end packed particle of each range
 };
 
 namespace sg {
@@ -2094,7 +2104,7 @@ inline int comp_stag( int comp, int d ) { return comp < 3 ? stag( comp, d ) : ( 
 
 
 template <int DIM, bool MIXED, int KIND>
-int launch_particles( sg_sim *S, SpeciesState &s, cudaStream_t st )
+int launch_particles( sg_sim *S, SpeciesState &s, cudaStream_t st, int t0, int t1 )
 {
     using T = typename std::conditional<MIXED, float, double>::type;
     const int in = s.cur, out = 1 - s.cur;
@@ -2112,6 +2122,8 @@ int launch_particles( sg_sim *S, SpeciesState &s, cudaStream_t st )
         sp.cr[d] = sp.cw * S->g.dx[d] / S->g.dt;
         sp.vs[d] = S->g.dt * S->g.dxi[d];
     }
+    sp.tile0 = t0;
+    if( t1 <= t0 ) return SG_OK;
     // The mixed form deposits per cell (one tile = at most 64 cells in 3D, where two
     // thread groups split a cell's footprint, 128 in 2D).  Its particles go through
     // shared memory in chunks: the chunk is the largest segment when that fits the
@@ -2146,7 +2158,7 @@ int launch_particles( sg_sim *S, SpeciesState &s, cudaStream_t st )
     }
     if( smem > 48 * 1024 ) SG_CUDA_TRY( cudaFuncSetAttribute( kern, cudaFuncAttributeMaxDynamicSharedMemorySize, ( int )smem ) );
     const int sidx = ( int )( &s - &S->sp[0] );
-    kern<<<S->g.ntiles, 128, smem, st>>>( S->g, field_view<T>( S ), sp, bin, bout, s.seg_start, s.cap, s.count[in],
+    kern<<<t1 - t0, 128, smem, st>>>( S->g, field_view<T>( S ), sp, bin, bout, s.seg_start, s.cap, s.count[in],
                                           s.count[out], bov, s.ovf_tile, S->d_flags + 1 + sidx, ( int )s.ovf_capacity,
                                           S->d_flags, chunk, S->d_flags + 1 + S->max_species + sidx );
     SG_LAUNCH_CHECK( "k_step_particles" );
@@ -2154,17 +2166,19 @@ int launch_particles( sg_sim *S, SpeciesState &s, cudaStream_t st )
 }
 
 template <int DIM, bool MIXED>
-int launch_particles_kind( sg_sim *S, SpeciesState &s, cudaStream_t st )
+int launch_particles_kind( sg_sim *S, SpeciesState &s, cudaStream_t st, int t0, int t1 )
 {
-    if( s.pusher == 0 ) return launch_particles<DIM, MIXED, 0>( S, s, st );
-    if( s.pusher == 1 ) return launch_particles<DIM, MIXED, 1>( S, s, st );
-    return launch_particles<DIM, MIXED, 2>( S, s, st );
+    if( s.pusher == 0 ) return launch_particles<DIM, MIXED, 0>( S, s, st, t0, t1 );
+    if( s.pusher == 1 ) return launch_particles<DIM, MIXED, 1>( S, s, st, t0, t1 );
+    return launch_particles<DIM, MIXED, 2>( S, s, st, t0, t1 );
 }
 
-int launch_particles_any( sg_sim *S, SpeciesState &s, cudaStream_t st )
+// The particle step of species s over tiles [t0, t1) (all tiles by default).
+int launch_particles_any( sg_sim *S, SpeciesState &s, cudaStream_t st, int t0 = 0, int t1 = -1 )
 {
-    if( S->g.ndim == 3 ) return S->mixed ? launch_particles_kind<3, true>( S, s, st ) : launch_particles_kind<3, false>( S, s, st );
-    return S->mixed ? launch_particles_kind<2, true>( S, s, st ) : launch_particles_kind<2, false>( S, s, st );
+    if( t1 < 0 ) t1 = S->g.ntiles;
+    if( S->g.ndim == 3 ) return S->mixed ? launch_particles_kind<3, true>( S, s, st, t0, t1 ) : launch_particles_kind<3, false>( S, s, st, t0, t1 );
+    return S->mixed ? launch_particles_kind<2, true>( S, s, st, t0, t1 ) : launch_particles_kind<2, false>( S, s, st, t0, t1 );
 }
 
 template <int DIM, class T>
@@ -2243,8 +2257,67 @@ int launch_radiation( sg_sim *S, SpeciesState &s, cudaStream_t st )
     return launch_radiate_resident( s.rad_tables, s.rad_mlp, r, st );
 }
 
+// One species whose packed state streams in from host memory during the step. Its
+// tiles go in ranges [ta[j], tb[j]), j in processing order; the copy stream has put
+// range j's particles in the staging buffer when copy_ev[2 + j] fires.
+//
+// With `pack` set, the new state is packed range by range as well. Range j's output
+// tiles are final once every tile within one tile of them has stepped, which is after
+// the kernel of range pack_after[j]; and the packed offsets of range j depend only on
+// tiles before it, which are final by then too.  Range j is then packed into the
+// output staging, its first and last packed particle go to h_chunk_end[2j], [2j + 1],
+// copy_ev[2 + nr + j] fires, and the host copies it out while later ranges still step.
+struct StreamIn {
+    int species = -1;
+    int64_t n = 0;
+    std::vector<int> ta, tb;
+    bool pack = false;
+    std::vector<int> pack_after;
+};
+
+// Unpacks the streamed species range by range and steps each range's tiles as soon as
+// their particles are in, so the copies of later ranges overlap the particle kernel.
+int stream_in_particles( sg_sim *S, SpeciesState &s, const StreamIn &in, cudaStream_t st, int &launches )
+{
+    const int nt = S->g.ntiles, nd = S->g.ndim, nr = ( int )in.ta.size();
+    char *stg = static_cast<char *>( S->pack_mem );
+    SG_CUDA_TRY( cudaStreamWaitEvent( st, S->copy_ev[1], 0 ) );
+    int r = exclusive_scan<int>( reinterpret_cast<const int *>( stg + 8 ), nt, S->tmp_start, S->scan_scratch, st );
+    if( r ) return r;
+    for( int j = 0; j < nr; j++ ) {
+        const int t0 = in.ta[j], t1 = in.tb[j];
+        if( t1 > t0 ) {
+            SG_CUDA_TRY( cudaStreamWaitEvent( st, S->copy_ev[2 + j], 0 ) );
+            // a tile over its segment raises SG_ERR_ARG in the step status and keeps its old, in-bounds count
+            if( S->mixed ) k_pack<true, false><<<t1 - t0, 128, 0, st>>>( nd, nt, s.seg_start, s.cap, s.count[s.cur], S->tmp_start, s.bm[s.cur], in.n, stg, S->d_flags, t0 );
+            else k_pack<false, false><<<t1 - t0, 128, 0, st>>>( nd, nt, s.seg_start, s.cap, s.count[s.cur], S->tmp_start, s.bd[s.cur], in.n, stg, S->d_flags, t0 );
+            SG_LAUNCH_CHECK( "k_pack" );
+            r = launch_particles_any( S, s, st, t0, t1 );
+            if( r ) return r;
+            launches += 2;
+        }
+        for( int q = 0; in.pack && q < nr; q++ ) {
+            if( in.pack_after[q] != j ) continue;
+            const int out = 1 - s.cur, q0 = in.ta[q], q1 = in.tb[q];
+            char *ostg = static_cast<char *>( S->pack_out_mem );
+            r = exclusive_scan<int>( s.count[out], nt, S->pack_off, S->scan_scratch, st );
+            if( r ) return r;
+            if( q1 > q0 ) {
+                if( S->mixed ) k_pack<true, true><<<q1 - q0, 128, 0, st>>>( nd, nt, s.seg_start, s.cap, s.count[out], S->pack_off, s.bm[out], in.n, ostg, S->d_flags, q0 );
+                else k_pack<false, true><<<q1 - q0, 128, 0, st>>>( nd, nt, s.seg_start, s.cap, s.count[out], S->pack_off, s.bd[out], in.n, ostg, S->d_flags, q0 );
+                SG_LAUNCH_CHECK( "k_pack" );
+                launches++;
+                SG_CUDA_TRY( cudaMemcpyAsync( S->h_chunk_end + 2 * q, S->pack_off + q0, 8, cudaMemcpyDeviceToHost, st ) );
+                if( q1 < nt ) SG_CUDA_TRY( cudaMemcpyAsync( S->h_chunk_end + 2 * q + 1, S->pack_off + q1, 8, cudaMemcpyDeviceToHost, st ) );
+            }
+            SG_CUDA_TRY( cudaEventRecord( S->copy_ev[2 + nr + q], st ) );
+        }
+    }
+    return SG_OK;
+}
+
 // Enqueues one full timestep on `st` (no host synchronisation).
-int enqueue_step( sg_sim *S, cudaStream_t st )
+int enqueue_step( sg_sim *S, cudaStream_t st, const StreamIn *in = nullptr )
 {
     int launches = 0;
     // inside a capture the stage events become external event nodes; outside, plain records
@@ -2271,6 +2344,11 @@ int enqueue_step( sg_sim *S, cudaStream_t st )
         launches++;
     }
     for( auto &s : S->sp ) {
+        if( in && &s == &S->sp[in->species] ) {
+            int r = stream_in_particles( S, s, *in, st, launches );
+            if( r ) return r;
+            continue;
+        }
         int r = launch_particles_any( S, s, st );
         if( r ) return r;
         launches++;
@@ -2774,6 +2852,15 @@ int sg_sim_destroy( sg_sim *S )
     release( S->d_wcount );
     for( int i = 0; i < 4; i++ )
         if( S->ev[i] ) cudaEventDestroy( S->ev[i] );
+    for( cudaEvent_t e : S->copy_ev ) cudaEventDestroy( e );
+    for( cudaStream_t x : { S->copy_stream, S->out_stream } )
+        if( x ) {
+            cudaStreamSynchronize( x );
+            cudaStreamDestroy( x );
+        }
+    release( S->pack_out_mem );
+    release( S->pack_off );
+    if( S->h_chunk_end ) cudaFreeHost( S->h_chunk_end );
     if( S->own_stream && S->stream ) cudaStreamDestroy( S->stream );
     delete S;
     return SG_OK;
@@ -2936,6 +3023,44 @@ int sg_sim_get_field( sg_sim *S, int comp, double *host )
     return SG_OK;
 }
 
+// After the step enqueued on S->stream: waits for it, swaps the buffers, reads the
+// status and removal counts, re-lays out spilled species and shifts the window.
+static int finish_step( sg_sim *S, bool moving )
+{
+    SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
+    for( auto &s : S->sp ) s.cur = 1 - s.cur;
+    const int status = S->h_flags[0];
+    // stage times from the events recorded inside the step (external event nodes in a graph)
+    if( cudaEventElapsedTime( &S->last_ms[0], S->ev[0], S->ev[1] ) != cudaSuccess ||
+        cudaEventElapsedTime( &S->last_ms[1], S->ev[1], S->ev[2] ) != cudaSuccess ||
+        cudaEventElapsedTime( &S->last_ms[2], S->ev[3], S->ev[2] ) != cudaSuccess ) {
+        cudaGetLastError(); // timing is informative only; do not leave the error pending
+        S->last_ms[0] = S->last_ms[1] = S->last_ms[2] = -1.0f;
+    }
+    if( status ) {
+        return set_error( status, status == SG_ERR_BOUNDS ? "a particle moved more than one cell in a step or left its tile"
+                                  : status == SG_ERR_ARG ? "a tile of the packed state exceeds its segment in the current layout"
+                                                         : "the spill list overflowed (capacity too small)" );
+    }
+    for( size_t k = 0; k < S->sp.size(); k++ ) S->sp[k].npart -= S->h_flags[1 + S->max_species + k];
+    for( size_t k = 0; k < S->sp.size(); k++ ) {
+        const int nspill = S->h_flags[1 + k];
+        if( nspill > 0 ) {
+            S->relayouts++;
+            S->spilled += nspill;
+            int r = relayout( S, S->sp[k], nspill );
+            if( r ) return r;
+        }
+    }
+    if( moving ) {
+        int r = window_shift( S );
+        if( r ) return r;
+        S->win_x_moved += S->g.dx[0] * S->win_shift;
+    }
+    S->hstep++;
+    return SG_OK;
+}
+
 int sg_sim_step( sg_sim *S, int nsteps )
 {
     SG_REQUIRE( S, "NULL simulation" );
@@ -2967,36 +3092,8 @@ int sg_sim_step( sg_sim *S, int nsteps )
             int r = enqueue_step( S, S->stream );
             if( r ) return r;
         }
-        SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
-        for( auto &s : S->sp ) s.cur = 1 - s.cur;
-        const int status = S->h_flags[0];
-        // stage times from the events recorded inside the step (external event nodes in a graph)
-        if( cudaEventElapsedTime( &S->last_ms[0], S->ev[0], S->ev[1] ) != cudaSuccess ||
-            cudaEventElapsedTime( &S->last_ms[1], S->ev[1], S->ev[2] ) != cudaSuccess ||
-            cudaEventElapsedTime( &S->last_ms[2], S->ev[3], S->ev[2] ) != cudaSuccess ) {
-            cudaGetLastError(); // timing is informative only; do not leave the error pending
-            S->last_ms[0] = S->last_ms[1] = S->last_ms[2] = -1.0f;
-        }
-        if( status ) {
-            return set_error( status, status == SG_ERR_BOUNDS ? "a particle moved more than one cell in a step or left its tile"
-                                                              : "the spill list overflowed (capacity too small)" );
-        }
-        for( size_t k = 0; k < S->sp.size(); k++ ) S->sp[k].npart -= S->h_flags[1 + S->max_species + k];
-        for( size_t k = 0; k < S->sp.size(); k++ ) {
-            const int nspill = S->h_flags[1 + k];
-            if( nspill > 0 ) {
-                S->relayouts++;
-                S->spilled += nspill;
-                int r = relayout( S, S->sp[k], nspill );
-                if( r ) return r;
-            }
-        }
-        if( moving ) {
-            int r = window_shift( S );
-            if( r ) return r;
-            S->win_x_moved += S->g.dx[0] * S->win_shift;
-        }
-        S->hstep++;
+        int r = finish_step( S, moving );
+        if( r ) return r;
     }
     return SG_OK;
 }
@@ -3277,8 +3374,8 @@ int sg_sim_pack_state( sg_sim *S, int species, void *host )
     r = exclusive_scan<int>( s.count[s.cur], nt, S->tmp_start, S->scan_scratch, S->stream );
     if( r ) return r;
     SG_CUDA_TRY( cudaMemcpyAsync( stg, &s.npart, 8, cudaMemcpyHostToDevice, S->stream ) );
-    if( S->mixed ) k_pack<true, true><<<nt, 128, 0, S->stream>>>( nd, nt, s.seg_start, s.cap, s.count[s.cur], S->tmp_start, s.bm[s.cur], n, stg, S->d_flags );
-    else k_pack<false, true><<<nt, 128, 0, S->stream>>>( nd, nt, s.seg_start, s.cap, s.count[s.cur], S->tmp_start, s.bd[s.cur], n, stg, S->d_flags );
+    if( S->mixed ) k_pack<true, true><<<nt, 128, 0, S->stream>>>( nd, nt, s.seg_start, s.cap, s.count[s.cur], S->tmp_start, s.bm[s.cur], n, stg, S->d_flags, 0 );
+    else k_pack<false, true><<<nt, 128, 0, S->stream>>>( nd, nt, s.seg_start, s.cap, s.count[s.cur], S->tmp_start, s.bd[s.cur], n, stg, S->d_flags, 0 );
     SG_LAUNCH_CHECK( "k_pack" );
     SG_CUDA_TRY( cudaMemcpyAsync( host, stg, bytes, cudaMemcpyDeviceToHost, S->stream ) );
     return SG_OK;
@@ -3304,12 +3401,173 @@ int sg_sim_unpack_state( sg_sim *S, int species, const void *host )
     r = exclusive_scan<int>( reinterpret_cast<const int *>( stg + 8 ), nt, S->tmp_start, S->scan_scratch, S->stream );
     if( r ) return r;
     SG_CUDA_TRY( cudaMemsetAsync( S->d_flags, 0, sizeof( int ), S->stream ) );
-    if( S->mixed ) k_pack<true, false><<<nt, 128, 0, S->stream>>>( nd, nt, s.seg_start, s.cap, s.count[s.cur], S->tmp_start, s.bm[s.cur], n, stg, S->d_flags );
-    else k_pack<false, false><<<nt, 128, 0, S->stream>>>( nd, nt, s.seg_start, s.cap, s.count[s.cur], S->tmp_start, s.bd[s.cur], n, stg, S->d_flags );
+    if( S->mixed ) k_pack<true, false><<<nt, 128, 0, S->stream>>>( nd, nt, s.seg_start, s.cap, s.count[s.cur], S->tmp_start, s.bm[s.cur], n, stg, S->d_flags, 0 );
+    else k_pack<false, false><<<nt, 128, 0, S->stream>>>( nd, nt, s.seg_start, s.cap, s.count[s.cur], S->tmp_start, s.bd[s.cur], n, stg, S->d_flags, 0 );
     SG_LAUNCH_CHECK( "k_pack" );
     SG_CUDA_TRY( cudaMemcpyAsync( S->h_flags, S->d_flags, sizeof( int ), cudaMemcpyDeviceToHost, S->stream ) );
     SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
     if( S->h_flags[0] ) return set_error( SG_ERR_ARG, "a tile of the packed state exceeds its segment in the current layout" );
+    return SG_OK;
+}
+
+int sg_sim_step_host( sg_sim *S, int species, const void *host_in, void *host_out, int chunks )
+{
+    SG_REQUIRE( S && host_in && host_out, "NULL argument" );
+    SG_REQUIRE( species >= 0 && species < ( int )S->sp.size(), "no species %d", species );
+    SG_REQUIRE( chunks >= 1 && chunks <= 64, "chunks must be in [1, 64], got %d", chunks );
+    SpeciesState &s = S->sp[species];
+    SG_REQUIRE( !s.radiates, "a radiating species does not stream: its radiation pass reads every particle before the push" );
+    const double time_dual = ( ( double )S->hstep + 1.5 ) * S->g.dt;
+    const bool moving = S->win_on && ( time_dual - S->win_t_start ) * S->win_velocity > S->win_x_moved;
+    SG_REQUIRE( !moving, "the window moves in this step (the state size changes): unpack, step and pack instead" );
+    const char *hin = static_cast<const char *>( host_in );
+    int64_t n = 0;
+    std::memcpy( &n, hin, 8 );
+    SG_REQUIRE( n == s.npart, "the packed state holds %lld particles, the species %lld", ( long long )n,
+                ( long long )s.npart );
+    const int nt = S->g.ntiles, nd = S->g.ndim;
+    const int *hc = reinterpret_cast<const int *>( hin + 8 );
+    std::vector<int64_t> hoff( nt + 1, 0 );
+    for( int t = 0; t < nt; t++ ) {
+        SG_REQUIRE( hc[t] >= 0, "tile %d of the packed state has a negative count", t );
+        hoff[t + 1] = hoff[t] + hc[t];
+    }
+    SG_REQUIRE( hoff[nt] == n, "the packed tile counts sum to %lld, the header says %lld", ( long long )hoff[nt], ( long long )n );
+
+    // Packing while stepping needs the particle count to stay (no open boundary removes
+    // any) and three x-slabs of tiles at least.  The last x-slab then steps first: the
+    // first slab receives from it across the periodic boundary, and would otherwise be
+    // final only at the end, with every packed offset behind it.
+    StreamIn in;
+    in.species = species;
+    in.n = n;
+    const int slab = nd == 3 ? S->g.nt[1] * S->g.nt[2] : S->g.nt[1];
+    in.pack = S->g.nt[0] >= 3;
+    for( int d = 0; d < nd; d++ ) in.pack = in.pack && !S->g.open[d];
+    const int body = in.pack ? nt - slab : nt; // tiles cut into `chunks` ranges of about equal particle counts
+    if( in.pack ) {
+        in.ta.push_back( body );
+        in.tb.push_back( nt );
+    }
+    for( int c = 0, t = 0; c < chunks; c++ ) {
+        const int t0 = t;
+        const int64_t target = hoff[body] / chunks * ( c + 1 );
+        while( t < body && ( c == chunks - 1 || hoff[t] < target ) ) t++;
+        in.ta.push_back( t0 );
+        in.tb.push_back( t );
+    }
+    const int nr = ( int )in.ta.size();
+    if( in.pack ) {
+        // range j is final after the first range q >= j whose end reaches one tile's reach past j's end
+        const int reach = nd == 3 ? S->g.nt[1] * S->g.nt[2] + S->g.nt[2] + 1 : S->g.nt[1] + 1;
+        in.pack_after.assign( nr, nr - 1 );
+        for( int j = 1; j < nr; j++ ) {
+            int q = j;
+            while( q < nr - 1 && in.tb[q] < std::min( body, in.tb[j] + reach ) ) q++;
+            in.pack_after[j] = q;
+        }
+        in.pack_after[0] = nr - 1; // the last slab receives from the range before it
+    }
+
+    size_t bytes = 0;
+    int r = sg_sim_packed_bytes( S, species, &bytes );
+    if( r ) return r;
+    r = packed_staging( S, bytes );
+    if( r ) return r;
+    if( !S->copy_stream ) SG_CUDA_TRY( cudaStreamCreateWithFlags( &S->copy_stream, cudaStreamNonBlocking ) );
+    while( ( int )S->copy_ev.size() < 2 * nr + 2 ) {
+        cudaEvent_t e = nullptr;
+        SG_CUDA_TRY( cudaEventCreateWithFlags( &e, cudaEventDisableTiming ) );
+        S->copy_ev.push_back( e );
+    }
+    if( in.pack ) {
+        if( S->pack_out_cap < bytes ) {
+            release( S->pack_out_mem );
+            S->pack_out_mem = nullptr;
+            S->pack_out_cap = 0;
+            SG_CUDA_TRY( cudaMalloc( &S->pack_out_mem, bytes ) );
+            S->pack_out_cap = bytes;
+        }
+        if( !S->pack_off ) SG_CUDA_TRY( cudaMalloc( &S->pack_off, ( size_t )nt * sizeof( int64_t ) ) );
+        if( !S->h_chunk_end ) SG_CUDA_TRY( cudaMallocHost( &S->h_chunk_end, 2 * 65 * sizeof( int64_t ) ) );
+        if( !S->out_stream ) SG_CUDA_TRY( cudaStreamCreateWithFlags( &S->out_stream, cudaStreamNonBlocking ) );
+        for( int j = 0; j < nr; j++ ) S->h_chunk_end[2 * j] = S->h_chunk_end[2 * j + 1] = n;
+    }
+    char *stg = static_cast<char *>( S->pack_mem );
+    const size_t hdr = packed_header_bytes( nt ), esz = S->mixed ? 4 : 8;
+    const int planes = S->mixed ? 1 + nd + 4 : nd + 4;
+    cudaStream_t cs = S->copy_stream;
+    // the staging buffer is free once the work already queued on the simulation's stream is done
+    SG_CUDA_TRY( cudaEventRecord( S->copy_ev[0], S->stream ) );
+    SG_CUDA_TRY( cudaStreamWaitEvent( cs, S->copy_ev[0], 0 ) );
+    SG_CUDA_TRY( cudaMemcpyAsync( stg, hin, 8 + 4 * ( size_t )nt, cudaMemcpyHostToDevice, cs ) );
+    SG_CUDA_TRY( cudaEventRecord( S->copy_ev[1], cs ) );
+    for( int j = 0; j < nr; j++ ) {
+        const int64_t p0 = hoff[in.ta[j]], p1 = hoff[in.tb[j]];
+        for( int k = 0; k < planes && p1 > p0; k++ ) {
+            const size_t o = hdr + ( ( size_t )k * ( size_t )n + ( size_t )p0 ) * esz;
+            SG_CUDA_TRY( cudaMemcpyAsync( stg + o, hin + o, ( size_t )( p1 - p0 ) * esz, cudaMemcpyHostToDevice, cs ) );
+        }
+        SG_CUDA_TRY( cudaEventRecord( S->copy_ev[2 + j], cs ) );
+    }
+    r = enqueue_step( S, S->stream, &in );
+    if( r ) {
+        cudaStreamSynchronize( cs );
+        cudaStreamSynchronize( S->stream );
+        return r;
+    }
+    char *hout = static_cast<char *>( host_out );
+    if( in.pack ) {
+        // copy each range out as soon as it is packed: the link carries both directions at once
+        std::vector<int> order( nr );
+        for( int j = 0; j < nr; j++ ) order[j] = j;
+        std::stable_sort( order.begin(), order.end(), [&]( int x, int y ) { return in.pack_after[x] < in.pack_after[y]; } );
+        const char *ostg = static_cast<const char *>( S->pack_out_mem );
+        int64_t copied = 0;
+        bool valid = true;
+        cudaError_t e = cudaSuccess;
+        for( int j : order ) {
+            e = cudaEventSynchronize( S->copy_ev[2 + nr + j] );
+            if( e != cudaSuccess ) break;
+            if( in.tb[j] <= in.ta[j] ) continue;
+            const int64_t p0 = S->h_chunk_end[2 * j], p1 = S->h_chunk_end[2 * j + 1];
+            if( p0 < 0 || p1 < p0 || p1 > n ) {
+                valid = false; // not a packing of n particles: the full pack below redoes it
+                continue;
+            }
+            copied += p1 - p0;
+            // host_out may be host_in: first finish the copy in of every range whose input this overwrites
+            int last_in = -1;
+            for( int i = 0; i < nr; i++ )
+                if( hoff[in.ta[i]] < p1 && hoff[in.tb[i]] > p0 ) last_in = std::max( last_in, i );
+            if( last_in >= 0 ) e = cudaStreamWaitEvent( S->out_stream, S->copy_ev[2 + last_in], 0 );
+            for( int k = 0; k < planes && p1 > p0 && e == cudaSuccess; k++ ) {
+                const size_t o = hdr + ( ( size_t )k * ( size_t )n + ( size_t )p0 ) * esz;
+                e = cudaMemcpyAsync( hout + o, ostg + o, ( size_t )( p1 - p0 ) * esz, cudaMemcpyDeviceToHost, S->out_stream );
+            }
+            if( e != cudaSuccess ) break;
+        }
+        if( e == cudaSuccess ) e = cudaMemcpyAsync( hout + 8, ostg + 8, 4 * ( size_t )nt, cudaMemcpyDeviceToHost, S->out_stream );
+        if( e == cudaSuccess ) e = cudaStreamSynchronize( S->out_stream );
+        if( e != cudaSuccess ) {
+            cudaStreamSynchronize( S->stream );
+            return cuda_fail( e, "streamed step copy-out", __FILE__, __LINE__ );
+        }
+        r = finish_step( S, false );
+        if( r ) return r;
+        // a spill re-laid the species out, or particles left: the ranges packed during the
+        // step are not the new state
+        if( valid && copied == n && S->h_flags[1 + species] == 0 && S->h_flags[1 + S->max_species + species] == 0 ) {
+            std::memcpy( hout, &n, 8 );
+            return SG_OK;
+        }
+    } else {
+        r = finish_step( S, false );
+        if( r ) return r;
+    }
+    r = sg_sim_pack_state( S, species, host_out );
+    if( r ) return r;
+    SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
     return SG_OK;
 }
 

@@ -116,6 +116,13 @@ class Simulation:
         """Restores a packed state of species s into the current layout."""
         check(_lib.lib().sg_sim_unpack_state(self._h, s, host_ptr), "unpack_state")
 
+    def step_host(self, s: int, host_in_ptr: int, host_out_ptr: int | None = None, chunks: int = 8):
+        """One step of species s kept in host memory as a packed state: reads it from
+        host_in_ptr, steps (the copy in overlaps the particle kernel over `chunks` tile
+        ranges) and writes the new packed state to host_out_ptr (default: in place)."""
+        out = host_in_ptr if host_out_ptr is None else host_out_ptr
+        check(_lib.lib().sg_sim_step_host(self._h, s, host_in_ptr, out, int(chunks)), "step_host")
+
     def copy_state(self, s: int, host_ptr: int, to_device: bool):
         """Raw state of species s to/from a host buffer of state_bytes(s) bytes (pinned for async)."""
         check(_lib.lib().sg_sim_copy_state(self._h, s, host_ptr, int(bool(to_device))), "copy_state")

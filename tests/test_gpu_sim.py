@@ -163,6 +163,64 @@ def test_autotune_times_every_candidate_and_keeps_the_fastest(sim_mod):
     assert best == min(times, key=times.get) and all(t > 0 for t in times.values())
 
 
+@pytest.mark.parametrize("form,n_cells", [("mixed", [16, 16, 16]), ("fp64", [16, 16, 16]), ("mixed", [8, 16, 16])])
+def test_step_host_matches_unpack_step_pack(sim_mod, form, n_cells):
+    """sg_sim_step_host (the copy in overlapped with the particle kernel over tile
+    ranges, and with 3 or more x-slabs of tiles the copy out overlapped too) gives the
+    particles of unpack -> step -> pack: identical after the first step, equal to
+    rounding afterwards (the order of the deposit's atomics differs)."""
+    simulation, synthetic = sim_mod
+    cl = [0.1, 0.1, 0.1]
+    dt = 0.95 * 0.1 / np.sqrt(3.0)
+    pos, mom, w = synthetic.thermal_plasma(n_cells, cl, 8, 0.14, 4, unique_weights=True)
+
+    def make():
+        sim = simulation.Simulation(n_cells, cl, dt, form=form)
+        sim.add_species(1.0, -1.0, "higueracary", pos, mom, w)
+        return sim
+
+    def particles(sim):
+        p, m, wt = sim.get_species(0)
+        o = np.argsort(wt)
+        return p[:, o], m[:, o], wt[o]
+
+    a, b = make(), make()
+    nb = a.packed_bytes(0)
+    ha = np.zeros(nb, dtype=np.uint8)
+    a.pack_state(0, ha.ctypes.data)
+    torch.cuda.synchronize()
+    hb = ha.copy()  # the order inside a tile is not deterministic: both start from the same one
+    b.unpack_state(0, hb.ctypes.data)
+    tol = dict(rtol=0, atol=1e-10) if form == "fp64" else dict(rtol=0, atol=2e-6)
+    for it, chunks in enumerate([5, 1, 64, 3]):
+        a.unpack_state(0, ha.ctypes.data)
+        a.step(1)
+        a.pack_state(0, ha.ctypes.data)
+        torch.cuda.synchronize()
+        b.step_host(0, hb.ctypes.data, chunks=chunks)
+        # the per-tile counts are deterministic
+        nt = int(np.prod(n_cells)) // 64
+        assert np.array_equal(ha[:8 + 4 * nt], hb[:8 + 4 * nt])
+        pa, ma, wa = particles(a)
+        pb, mb, wb = particles(b)
+        assert np.array_equal(wa, wb)
+        if it == 0:
+            assert np.array_equal(pa, pb) and np.array_equal(ma, mb)
+        else:
+            np.testing.assert_allclose(pb, pa, **tol)
+            np.testing.assert_allclose(mb, ma, **tol)
+    ua, ub = a.energy(), b.energy()
+    np.testing.assert_allclose(ub, ua, rtol=1e-5 if form == "mixed" else 1e-10)
+    with pytest.raises(RuntimeError):
+        b.step_host(0, hb.ctypes.data, chunks=0)
+    bad = hb.copy()
+    bad[:8] = np.frombuffer(np.int64(len(w) + 1).tobytes(), dtype=np.uint8)
+    with pytest.raises(RuntimeError):
+        b.step_host(0, bad.ctypes.data)
+    a.close()
+    b.close()
+
+
 @pytest.mark.parametrize("form", ["mixed", "fp64"])
 def test_packed_state_round_trip(sim_mod, form):
     """pack -> (one more step) -> unpack restores the packed particles exactly; the
