@@ -250,6 +250,9 @@ def run_gpu(args, rank, world, local_rank):
         host = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
         sim.pack_state(0, host.data_ptr())
         torch.cuda.synchronize()
+        if args.e2e_chunks > 0:
+            sim.step_host(0, host.data_ptr(), chunks=args.e2e_chunks)  # untimed: its staging buffers
+            torch.cuda.synchronize()
         ke = max(1, min(args.steps, args.e2e_steps))
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
@@ -271,6 +274,8 @@ def run_gpu(args, rank, world, local_rank):
         ems = max_over_ranks(e0.elapsed_time(e1), device)
         e2e = {"value": whole_job_rate(n, world, ke, ems), "unit": UNIT, "h2d_bytes_per_step": int(nbytes),
                "d2h_bytes_per_step": int(nbytes + 16), "steps": ke}
+        if args.e2e_chunks > 0:
+            e2e["last_step_stages_ms"] = sim.stream_timing()
         del host
     sim.close()
     ncell_all = int(np.prod(cfg["n_cells"]))

@@ -251,6 +251,11 @@ int sg_sim_unpack_state( sg_sim *sim, int species, const void *host );
  * moves.  Returns after host_out is written. */
 int sg_sim_step_host( sg_sim *sim, int species, const void *host_in, void *host_out, int chunks );
 
+/* Stage times of the last sg_sim_step_host that packed while stepping, in ms from its
+ * start (-1 where not measured): [0] copy in done, [1] particle kernels done, [2] copy
+ * out done, [3] field update done (the reference's Timers, src/Tools/Timers.cpp). */
+int sg_sim_stream_timing( sg_sim *sim, float *ms );
+
 /* Adds a Gaussian 2D laser injected through the Silver-Mueller condition on xmin
  * (LaserGaussian2D, src/Python/pyprofiles.py:507; ElectroMagnBC2D_SM::apply,
  * src/ElectroMagnBC/ElectroMagnBC2D_SM.cpp:118).  p = {a0, omega, waist, focus_x,

@@ -1917,6 +1917,16 @@ __global__ void k_pack( int ndim, int nt, const int64_t *__restrict__ seg_start,
     }
 }
 
+// First and end packed particle of tiles [q0, q1) into pinned host memory. A store from
+// the SMs, not a copy: a copy would queue on the copy engine behind the bulk copies out.
+__global__ void k_store_bounds( const int64_t *__restrict__ off, int q0, int q1, int nt, int64_t n,
+                                volatile int64_t *host )
+{
+    host[0] = off[q0];
+    host[1] = q1 < nt ? off[q1] : n;
+    __threadfence_system();
+}
+
 // Back to absolute FP64 positions (tile-sorted order) for output.
 template <int DIM, bool MIXED>
 __global__ void k_export( GridInfo g, int nt, const int64_t *__restrict__ seg_start, const int *__restrict__ count,
@@ -2080,6 +2090,8 @@ struct sg_sim {
     size_t pack_out_cap = 0;
     int64_t *pack_off = nullptr;        // its per-tile offsets
     int64_t *h_chunk_end = nullptr;     // pinned: first and end packed particle of each range
+    int64_t *d_chunk_end = nullptr;     // its device address
+    float stream_ms[4] = { -1, -1, -1, -1 }; // last streamed step: copy in, particles, copy out, fields done
 };
 
 namespace sg {
@@ -2307,8 +2319,8 @@ int stream_in_particles( sg_sim *S, SpeciesState &s, const StreamIn &in, cudaStr
                 else k_pack<false, true><<<q1 - q0, 128, 0, st>>>( nd, nt, s.seg_start, s.cap, s.count[out], S->pack_off, s.bd[out], in.n, ostg, S->d_flags, q0 );
                 SG_LAUNCH_CHECK( "k_pack" );
                 launches++;
-                SG_CUDA_TRY( cudaMemcpyAsync( S->h_chunk_end + 2 * q, S->pack_off + q0, 8, cudaMemcpyDeviceToHost, st ) );
-                if( q1 < nt ) SG_CUDA_TRY( cudaMemcpyAsync( S->h_chunk_end + 2 * q + 1, S->pack_off + q1, 8, cudaMemcpyDeviceToHost, st ) );
+                k_store_bounds<<<1, 1, 0, st>>>( S->pack_off, q0, q1, nt, in.n, S->d_chunk_end + 2 * q );
+                SG_LAUNCH_CHECK( "k_store_bounds" );
             }
             SG_CUDA_TRY( cudaEventRecord( S->copy_ev[2 + nr + q], st ) );
         }
@@ -3420,6 +3432,8 @@ int sg_sim_step_host( sg_sim *S, int species, const void *host_in, void *host_ou
     const double time_dual = ( ( double )S->hstep + 1.5 ) * S->g.dt;
     const bool moving = S->win_on && ( time_dual - S->win_t_start ) * S->win_velocity > S->win_x_moved;
     SG_REQUIRE( !moving, "the window moves in this step (the state size changes): unpack, step and pack instead" );
+    // a pack_state into host_in may still be in flight on the simulation's stream
+    SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
     const char *hin = static_cast<const char *>( host_in );
     int64_t n = 0;
     std::memcpy( &n, hin, 8 );
@@ -3475,9 +3489,9 @@ int sg_sim_step_host( sg_sim *S, int species, const void *host_in, void *host_ou
     r = packed_staging( S, bytes );
     if( r ) return r;
     if( !S->copy_stream ) SG_CUDA_TRY( cudaStreamCreateWithFlags( &S->copy_stream, cudaStreamNonBlocking ) );
-    while( ( int )S->copy_ev.size() < 2 * nr + 2 ) {
+    while( ( int )S->copy_ev.size() < 2 * nr + 3 ) {
         cudaEvent_t e = nullptr;
-        SG_CUDA_TRY( cudaEventCreateWithFlags( &e, cudaEventDisableTiming ) );
+        SG_CUDA_TRY( cudaEventCreate( &e ) ); // timed: the stage times of the step
         S->copy_ev.push_back( e );
     }
     if( in.pack ) {
@@ -3489,7 +3503,10 @@ int sg_sim_step_host( sg_sim *S, int species, const void *host_in, void *host_ou
             S->pack_out_cap = bytes;
         }
         if( !S->pack_off ) SG_CUDA_TRY( cudaMalloc( &S->pack_off, ( size_t )nt * sizeof( int64_t ) ) );
-        if( !S->h_chunk_end ) SG_CUDA_TRY( cudaMallocHost( &S->h_chunk_end, 2 * 65 * sizeof( int64_t ) ) );
+        if( !S->h_chunk_end ) {
+            SG_CUDA_TRY( cudaHostAlloc( &S->h_chunk_end, 2 * 65 * sizeof( int64_t ), cudaHostAllocMapped ) );
+            SG_CUDA_TRY( cudaHostGetDevicePointer( reinterpret_cast<void **>( &S->d_chunk_end ), S->h_chunk_end, 0 ) );
+        }
         if( !S->out_stream ) SG_CUDA_TRY( cudaStreamCreateWithFlags( &S->out_stream, cudaStreamNonBlocking ) );
         for( int j = 0; j < nr; j++ ) S->h_chunk_end[2 * j] = S->h_chunk_end[2 * j + 1] = n;
     }
@@ -3548,6 +3565,7 @@ int sg_sim_step_host( sg_sim *S, int species, const void *host_in, void *host_ou
             if( e != cudaSuccess ) break;
         }
         if( e == cudaSuccess ) e = cudaMemcpyAsync( hout + 8, ostg + 8, 4 * ( size_t )nt, cudaMemcpyDeviceToHost, S->out_stream );
+        if( e == cudaSuccess ) e = cudaEventRecord( S->copy_ev[2 + 2 * nr], S->out_stream );
         if( e == cudaSuccess ) e = cudaStreamSynchronize( S->out_stream );
         if( e != cudaSuccess ) {
             cudaStreamSynchronize( S->stream );
@@ -3555,6 +3573,12 @@ int sg_sim_step_host( sg_sim *S, int species, const void *host_in, void *host_ou
         }
         r = finish_step( S, false );
         if( r ) return r;
+        const cudaEvent_t marks[4] = { S->copy_ev[1 + nr], S->ev[1], S->copy_ev[2 + 2 * nr], S->ev[2] };
+        for( int k = 0; k < 4; k++ )
+            if( cudaEventElapsedTime( &S->stream_ms[k], S->copy_ev[0], marks[k] ) != cudaSuccess ) {
+                cudaGetLastError(); // informative only
+                S->stream_ms[k] = -1.0f;
+            }
         // a spill re-laid the species out, or particles left: the ranges packed during the
         // step are not the new state
         if( valid && copied == n && S->h_flags[1 + species] == 0 && S->h_flags[1 + S->max_species + species] == 0 ) {
@@ -3568,6 +3592,13 @@ int sg_sim_step_host( sg_sim *S, int species, const void *host_in, void *host_ou
     r = sg_sim_pack_state( S, species, host_out );
     if( r ) return r;
     SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
+    return SG_OK;
+}
+
+int sg_sim_stream_timing( sg_sim *S, float *ms )
+{
+    SG_REQUIRE( S && ms, "NULL argument" );
+    for( int k = 0; k < 4; k++ ) ms[k] = S->stream_ms[k];
     return SG_OK;
 }
 

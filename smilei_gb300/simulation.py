@@ -123,6 +123,13 @@ class Simulation:
         out = host_in_ptr if host_out_ptr is None else host_out_ptr
         check(_lib.lib().sg_sim_step_host(self._h, s, host_in_ptr, out, int(chunks)), "step_host")
 
+    def stream_timing(self):
+        """Stage times (ms from the start) of the last step_host that packed while stepping:
+        copy in, particle kernels, copy out and field update done."""
+        a = (ctypes.c_float * 4)()
+        check(_lib.lib().sg_sim_stream_timing(self._h, a), "stream_timing")
+        return dict(copy_in=a[0], particles=a[1], copy_out=a[2], fields=a[3])
+
     def copy_state(self, s: int, host_ptr: int, to_device: bool):
         """Raw state of species s to/from a host buffer of state_bytes(s) bytes (pinned for async)."""
         check(_lib.lib().sg_sim_copy_state(self._h, s, host_ptr, int(bool(to_device))), "copy_state")
