@@ -243,12 +243,16 @@ int sg_sim_unpack_state( sg_sim *sim, int species, const void *host );
  * reference's Particles vectors on the host, src/Particles/Particles.h:48): reads the
  * packed state from host_in, steps the whole simulation, and writes the new packed
  * state to host_out (host_out may equal host_in; it needs packed_bytes() bytes, and
- * particles removed at open boundaries only shrink it).  The copy in runs in `chunks`
- * tile ranges of about equal particle counts on a second stream, and each range is
- * stepped as soon as it is in, so the copies overlap the particle kernel.  Same result
- * as unpack_state, step(1), pack_state (up to the order of floating-point atomics in
- * the current deposit).  Not for a radiating species or a step in which the window
- * moves.  Returns after host_out is written. */
+ * particles removed at open boundaries only shrink it; it must not overlap host_in
+ * unless it is host_in).  The copy in runs in `chunks` (1..64) tile ranges of about
+ * equal particle counts on a second stream, and each range is stepped as soon as it is
+ * in.  On a grid periodic in every dimension with at least three x-slabs of tiles,
+ * each range is also packed once its neighbours have stepped and copied out on a third
+ * stream, so both directions of the host link and the kernel overlap; otherwise, or
+ * after a spill, the state is packed after the step.  Same result as unpack_state,
+ * step(1), pack_state (up to the order of floating-point atomics in the current
+ * deposit).  Not for a radiating species or a step in which the window moves.  Waits
+ * for the simulation's stream first and returns after host_out is written. */
 int sg_sim_step_host( sg_sim *sim, int species, const void *host_in, void *host_out, int chunks );
 
 /* Stage times of the last sg_sim_step_host that packed while stepping, in ms from its
