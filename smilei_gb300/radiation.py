@@ -4,7 +4,7 @@
 conventions, src/Radiation/RadiationTables.h); ``monte_carlo`` runs
 RadiationMonteCarlo::operator() over a species' particles;
 ``PhotonChiMLP`` is the learned inverse CDF (hand-written CUDA training and
-inference in csrc/radiation.cu) with the table as fallback and judge.
+inference in csrc/radiation.cu) with the table as fallback and as its check.
 All arrays are torch CUDA tensors (float64).
 """
 from __future__ import annotations

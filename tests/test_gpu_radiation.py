@@ -4,7 +4,7 @@ Tables are the reference's default tables (tests/golden/radiation.npz, dumped
 from the reference's RadiationTablesDefault).  Table kernels must reproduce the
 reference's outputs; the Monte-Carlo pass must reproduce the oracle's pass
 drawing the same per-particle random streams; the network's gradients must
-match the FP64 oracle's; the trained network is judged by the table: its
+match the FP64 oracle's; the trained network is checked against the table: its
 per-bin error decides where it is used, and the emitted spectrum and mean
 energy loss of a Monte-Carlo pass using it are compared with the table-only pass.
 """
