@@ -255,6 +255,15 @@ int sg_sim_unpack_state( sg_sim *sim, int species, const void *host );
  * for the simulation's stream first and returns after host_out is written. */
 int sg_sim_step_host( sg_sim *sim, int species, const void *host_in, void *host_out, int chunks );
 
+/* The tile ranges sg_sim_step_host uses, in processing order, for a grid of
+ * ntiles[0..ndim) tiles (x-major) holding counts[t] particles per tile: range j is
+ * tiles [ta[j], tb[j]).  pack_after[j] is the range after whose particle step range j's
+ * output is final (-1 for all when the step does not pack while stepping: a grid not
+ * periodic in every dimension, or fewer than three x-slabs of tiles).  Arrays of
+ * chunks + 1 entries; host only. */
+int sg_stream_ranges( int ndim, const int *ntiles, int periodic, const int *counts, int chunks, int *ta, int *tb,
+                      int *pack_after, int *nranges );
+
 /* Stage times of the last sg_sim_step_host that packed while stepping, in ms from its
  * start (-1 where not measured): [0] copy in done, [1] particle kernels done, [2] copy
  * out done, [3] field update done (the reference's Timers, src/Tools/Timers.cpp). */

@@ -94,6 +94,7 @@ _SIGNATURES = {
     "sg_sim_unpack_state": (_I, [_VP, _I, _VP]),
     "sg_sim_step_host": (_I, [_VP, _I, _VP, _VP, _I]),
     "sg_sim_stream_timing": (_I, [_VP, ctypes.POINTER(ctypes.c_float)]),
+    "sg_stream_ranges": (_I, [_I, _VP, _I, _VP, _I, _VP, _VP, _VP, ctypes.POINTER(_I)]),
     "sg_sim_get_rho": (_I, [_VP, _VP]),
     "sg_rad_tables_create": (_I, [_VP, _I, _D, _D, _VP, _I, _I, _D, _D, _VP, _VP, ctypes.POINTER(_VP)]),
     "sg_rad_tables_destroy": (_I, [_VP]),

@@ -3422,6 +3422,78 @@ int sg_sim_unpack_state( sg_sim *S, int species, const void *host )
     return SG_OK;
 }
 
+// Tile ranges of a streamed step, in processing order, from the packed particle offsets
+// hoff[0..nt] (tile order).  Returns whether the ranges can be packed while stepping:
+// that needs the particle count to stay (no open boundary removes any) and three x-slabs
+// of tiles at least.  The last x-slab is then range 0 and steps first: the first slab
+// receives from it across the periodic boundary, and would otherwise be final only at the
+// end, with every packed offset behind it.  The other `chunks` ranges cut the remaining
+// tiles at about equal particle counts.  A tile receives from its own x-slab and the two
+// beside it (the y and z wraps stay inside a slab), so range j is final once every tile
+// up to the end of the slab after its last tile has stepped: pack_after[j] is the first
+// range that reaches there.
+static bool plan_stream( int nd, const int *ntiles, bool periodic, const std::vector<int64_t> &hoff, int chunks,
+                         std::vector<int> &ta, std::vector<int> &tb, std::vector<int> &pack_after )
+{
+    const int nt = ( int )hoff.size() - 1;
+    const int slab = nd == 3 ? ntiles[1] * ntiles[2] : ntiles[1];
+    const bool pack = periodic && ntiles[0] >= 3;
+    const int body = pack ? nt - slab : nt;
+    ta.clear();
+    tb.clear();
+    pack_after.clear();
+    if( pack ) {
+        ta.push_back( body );
+        tb.push_back( nt );
+    }
+    for( int c = 0, t = 0; c < chunks; c++ ) {
+        const int t0 = t;
+        const int64_t target = hoff[body] / chunks * ( c + 1 );
+        while( t < body && ( c == chunks - 1 || hoff[t] < target ) ) t++;
+        ta.push_back( t0 );
+        tb.push_back( t );
+    }
+    if( !pack ) return false;
+    const int nr = ( int )ta.size();
+    pack_after.assign( nr, nr - 1 );
+    for( int j = 1; j < nr; j++ ) {
+        const int need = std::min( body, ( std::max( tb[j] - 1, 0 ) / slab + 2 ) * slab );
+        int q = j;
+        while( q < nr - 1 && tb[q] < need ) q++;
+        pack_after[j] = q;
+    }
+    pack_after[0] = nr - 1; // the last slab receives from the range before it
+    return true;
+}
+
+int sg_stream_ranges( int ndim, const int *ntiles, int periodic, const int *counts, int chunks, int *ta, int *tb,
+                      int *pack_after, int *nranges )
+{
+    SG_REQUIRE( ntiles && counts && ta && tb && pack_after && nranges, "NULL argument" );
+    SG_REQUIRE( ndim == 2 || ndim == 3, "ndim must be 2 or 3" );
+    SG_REQUIRE( chunks >= 1 && chunks <= 64, "chunks must be in [1, 64], got %d", chunks );
+    int64_t nt = 1;
+    for( int d = 0; d < ndim; d++ ) {
+        SG_REQUIRE( ntiles[d] >= 1, "ntiles[%d] < 1", d );
+        nt *= ntiles[d];
+    }
+    SG_REQUIRE( nt < ( int64_t )1 << 30, "too many tiles" );
+    std::vector<int64_t> hoff( nt + 1, 0 );
+    for( int64_t t = 0; t < nt; t++ ) {
+        SG_REQUIRE( counts[t] >= 0, "tile %lld has a negative count", ( long long )t );
+        hoff[t + 1] = hoff[t] + counts[t];
+    }
+    std::vector<int> a, b, p;
+    const bool pack = plan_stream( ndim, ntiles, periodic != 0, hoff, chunks, a, b, p );
+    for( size_t j = 0; j < a.size(); j++ ) {
+        ta[j] = a[j];
+        tb[j] = b[j];
+        pack_after[j] = pack ? p[j] : -1;
+    }
+    *nranges = ( int )a.size();
+    return SG_OK;
+}
+
 int sg_sim_step_host( sg_sim *S, int species, const void *host_in, void *host_out, int chunks )
 {
     SG_REQUIRE( S && host_in && host_out, "NULL argument" );
@@ -3448,40 +3520,13 @@ int sg_sim_step_host( sg_sim *S, int species, const void *host_in, void *host_ou
     }
     SG_REQUIRE( hoff[nt] == n, "the packed tile counts sum to %lld, the header says %lld", ( long long )hoff[nt], ( long long )n );
 
-    // Packing while stepping needs the particle count to stay (no open boundary removes
-    // any) and three x-slabs of tiles at least.  The last x-slab then steps first: the
-    // first slab receives from it across the periodic boundary, and would otherwise be
-    // final only at the end, with every packed offset behind it.
     StreamIn in;
     in.species = species;
     in.n = n;
-    const int slab = nd == 3 ? S->g.nt[1] * S->g.nt[2] : S->g.nt[1];
-    in.pack = S->g.nt[0] >= 3;
-    for( int d = 0; d < nd; d++ ) in.pack = in.pack && !S->g.open[d];
-    const int body = in.pack ? nt - slab : nt; // tiles cut into `chunks` ranges of about equal particle counts
-    if( in.pack ) {
-        in.ta.push_back( body );
-        in.tb.push_back( nt );
-    }
-    for( int c = 0, t = 0; c < chunks; c++ ) {
-        const int t0 = t;
-        const int64_t target = hoff[body] / chunks * ( c + 1 );
-        while( t < body && ( c == chunks - 1 || hoff[t] < target ) ) t++;
-        in.ta.push_back( t0 );
-        in.tb.push_back( t );
-    }
+    bool periodic = true;
+    for( int d = 0; d < nd; d++ ) periodic = periodic && !S->g.open[d];
+    in.pack = plan_stream( nd, S->g.nt, periodic, hoff, chunks, in.ta, in.tb, in.pack_after );
     const int nr = ( int )in.ta.size();
-    if( in.pack ) {
-        // range j is final after the first range q >= j whose end reaches one tile's reach past j's end
-        const int reach = nd == 3 ? S->g.nt[1] * S->g.nt[2] + S->g.nt[2] + 1 : S->g.nt[1] + 1;
-        in.pack_after.assign( nr, nr - 1 );
-        for( int j = 1; j < nr; j++ ) {
-            int q = j;
-            while( q < nr - 1 && in.tb[q] < std::min( body, in.tb[j] + reach ) ) q++;
-            in.pack_after[j] = q;
-        }
-        in.pack_after[0] = nr - 1; // the last slab receives from the range before it
-    }
 
     size_t bytes = 0;
     int r = sg_sim_packed_bytes( S, species, &bytes );

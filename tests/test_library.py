@@ -100,3 +100,60 @@ def test_other_configuration_errors():
     assert "dt must be below every cell length" in _lib.last_error()
     assert L.sg_sim_create(ctypes.byref(_cfg(2, 7, [16, 16])), ctypes.byref(h)) == -1
     assert "unknown form" in _lib.last_error()
+
+
+def _stream_ranges(nt3, counts, chunks, periodic=True):
+    L = _lib.lib()
+    nd = len(nt3)
+    ntiles = (ctypes.c_int * 3)(*(list(nt3) + [1] * (3 - nd)))
+    c = (ctypes.c_int * len(counts))(*[int(v) for v in counts])
+    ta, tb, pa = ((ctypes.c_int * (chunks + 1))() for _ in range(3))
+    nr = ctypes.c_int()
+    _lib.check(L.sg_stream_ranges(nd, ntiles, int(periodic), c, chunks, ta, tb, pa, ctypes.byref(nr)),
+               "sg_stream_ranges")
+    k = nr.value
+    return list(ta[:k]), list(tb[:k]), list(pa[:k])
+
+
+@pytest.mark.parametrize("nt3", [(4, 4, 4), (3, 4, 4), (5, 3, 7), (8, 2, 2), (6, 5), (3, 9)])
+@pytest.mark.parametrize("chunks", [1, 2, 3, 5, 8, 32, 64])
+def test_streamed_step_ranges_pack_only_final_tiles(nt3, chunks):
+    """The streamed host step packs a tile range only after every tile that can send it
+    particles (its 3^D neighbours, periodic wraps included) has stepped, and after every
+    range before it in tile order is final (their packed offsets come first).  Checked
+    by brute force over the library's own range plan (sg_stream_ranges, host only)."""
+    import itertools
+    import numpy as np
+    rng = np.random.default_rng(len(nt3) * 100 + chunks)
+    nt = int(np.prod(nt3))
+    for _ in range(3):
+        counts = rng.integers(0, 50, nt)
+        counts[rng.random(nt) < 0.2] = 0  # empty tiles
+        ta, tb, pa = _stream_ranges(nt3, counts, chunks)
+        owner = np.full(nt, -1)
+        for j, (a, b) in enumerate(zip(ta, tb)):
+            assert a <= b
+            owner[a:b] = j
+        assert (owner >= 0).all()  # every tile in exactly one range
+        assert all(0 <= p < len(ta) for p in pa)
+        dims = list(nt3)
+        for j, (a, b) in enumerate(zip(ta, tb)):
+            assert pa[j] >= j
+            for t in range(a, b):
+                idx = np.unravel_index(t, dims)
+                for off in itertools.product((-1, 0, 1), repeat=len(dims)):
+                    src = np.ravel_multi_index([(i + o) % n for i, o, n in zip(idx, off, dims)], dims)
+                    assert owner[src] <= pa[j], (j, t, int(src))
+            for i in range(len(ta)):
+                if i != j and tb[i] <= a and tb[i] > ta[i]:
+                    assert pa[i] <= pa[j]  # tiles before range j are final no later than it
+
+
+def test_streamed_step_ranges_without_packing():
+    """An open boundary, or fewer than three x-slabs, keeps the copy out after the step."""
+    ta, tb, pa = _stream_ranges((4, 4, 4), [1] * 64, 4, periodic=False)
+    assert pa == [-1] * 4 and ta[0] == 0 and tb[-1] == 64
+    ta, tb, pa = _stream_ranges((2, 4, 4), [1] * 32, 4)
+    assert pa == [-1] * 4 and tb[-1] == 32
+    with pytest.raises(RuntimeError):
+        _stream_ranges((4, 4, 4), [1] * 64, 0)
