@@ -402,7 +402,8 @@ def run_cpu_sample_lwfa(args):
                      profiles=[(prof, c["ppc"], 0.0, 0)], state=state)
     t1 = time.perf_counter()
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    return dict(value=npart / (t1 - t0), unit=UNIT, cores=cores, kind="port",
+    return dict(value=npart / (t1 - t0), unit=UNIT, cores=cores, kind="port", steps=steps, warmup=1,
+                ms_per_step=(t1 - t0) * 1e3 / steps,
                 sample=f"2D wakefield sample 1920x256 cells x 4 ppc ({w.size} electrons), Vay, window moving, "
                        f"{steps} FP64 steps of oracle/bc_oracle.c + pic_oracle.c")
 
@@ -631,13 +632,14 @@ def run_cpu_sample_radiation(args):
         O.project(0, 2, n_prim, dom, cl, st["dt"], pos, mom, w, q, invgf, iold, delta, J)
     t1 = time.perf_counter()
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    return dict(value=w.size * steps / (t1 - t0), unit=UNIT, cores=cores, kind="port",
+    return dict(value=w.size * steps / (t1 - t0), unit=UNIT, cores=cores, kind="port", steps=steps, warmup=0,
+                ms_per_step=(t1 - t0) * 1e3 / steps,
                 sample=f"radiation sample: 200000 electrons (gamma 2000, a0 = 100 plane wave) on 512x128 cells, "
                        f"{steps} FP64 steps of interpolate + Monte-Carlo radiation + Vay push + Esirkepov "
                        f"(oracle/pic_oracle.c, rad_oracle.c; fields held fixed)")
 
 
-def run_cpu_sample(args, steps=None):
+def run_cpu_sample(args, steps=None, warmup=1):
     """The oracle's FP64 timestep on a bounded sample of the workload (all host cores)."""
     import oracle
     n = args.cpu_cells
@@ -656,14 +658,16 @@ def run_cpu_sample(args, steps=None):
     sp = [dict(pos=pos, mom=mom, weight=w, charge=np.full(w.shape, -1, np.int16), mass=1.0, pusher=pusher)]
     O = oracle.Oracle()
     steps = steps or args.cpu_steps
-    O.pic_step(3, [n] * 3, 2, [dx] * 3, dt, fields, sp)  # warm-up
+    for _ in range(max(1, warmup)):
+        O.pic_step(3, [n] * 3, 2, [dx] * 3, dt, fields, sp)
     t0 = time.perf_counter()
     for _ in range(steps):
         O.pic_step(3, [n] * 3, 2, [dx] * 3, dt, fields, sp)
     t1 = time.perf_counter()
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     value = pos.shape[1] * steps / (t1 - t0)
-    return dict(value=value, unit=UNIT, cores=cores, kind="port",
+    return dict(value=value, unit=UNIT, cores=cores, kind="port", steps=steps, warmup=max(1, warmup),
+                ms_per_step=(t1 - t0) * 1e3 / steps,
                 sample=f"{what} ({pos.shape[1]} electrons), {pusher}, "
                        f"{steps} FP64 steps of oracle/pic_oracle.c (OpenMP)")
 
@@ -724,10 +728,13 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
+        # the 3D sample runs the requested warm-up and timed steps (each one FP64 step of the
+        # bounded sample); the 2D samples keep their own bounded step counts
         r = (run_cpu_sample_lwfa(args) if args.workload == "lwfa" else
-             run_cpu_sample_radiation(args) if args.workload == "radiation" else run_cpu_sample(args))
+             run_cpu_sample_radiation(args) if args.workload == "radiation" else
+             run_cpu_sample(args, steps=max(1, args.steps), warmup=args.warmup))
         line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
-                "steps": args.cpu_steps, "warmup": 1, "ms_per_step": None, "higher_is_better": True,
+                "steps": r["steps"], "warmup": r["warmup"], "ms_per_step": r["ms_per_step"], "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, host)",
                 "config": {"workload": workload, "sample": r["sample"], "form": "fp64"},
                 "cpu_baseline": r,
