@@ -1790,8 +1790,16 @@ __global__ void k_kinetic( int nt, const int64_t *__restrict__ seg_start, const 
         const int n = count[t];
         const int64_t s0 = seg_start[t];
         for( int i = threadIdx.x; i < n; i += blockDim.x ) {
-            const double px = b.p[0][s0 + i], py = b.p[1][s0 + i], pz = b.p[2][s0 + i];
-            acc += ( double )b.w[s0 + i] * ( sqrt( 1.0 + px * px + py * py + pz * pz ) - 1.0 );
+            if constexpr( MIXED ) {
+                // FP32 momenta: gamma - 1 = p^2 / (1 + gamma) in FP32 (no cancellation at small
+                // p; about 1e-8 relative on the sum), summed in FP64 -- one FP64 add per particle
+                const float px = b.p[0][s0 + i], py = b.p[1][s0 + i], pz = b.p[2][s0 + i];
+                const float p2 = fmaf( px, px, fmaf( py, py, pz * pz ) );
+                acc += ( double )b.w[s0 + i] * ( double )( p2 / ( 1.0f + sqrtf( 1.0f + p2 ) ) );
+            } else {
+                const double px = b.p[0][s0 + i], py = b.p[1][s0 + i], pz = b.p[2][s0 + i];
+                acc += ( double )b.w[s0 + i] * ( sqrt( 1.0 + px * px + py * py + pz * pz ) - 1.0 );
+            }
         }
     }
     acc = block_sum( acc );
