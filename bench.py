@@ -44,6 +44,13 @@ SIGMA_10KEV = float(np.sqrt(10.0 / 511.0))
 def workload_cfg(args):
     dx = 0.1
     dt = 0.95 * dx / np.sqrt(3.0)
+    if getattr(args, "workload", "thermal") == "thermal2d":
+        # 2D thermal plasma: 256 x 256 cells, electrons and protons (mass 1836) at 16 ppc each,
+        # T = 10 keV in each species' own momentum unit (sigma = sqrt(T / m c^2)), Boris
+        return dict(n_cells=[256, 256], cell_length=[dx, dx], dt=float(0.95 * dx / np.sqrt(2.0)), ppc=16,
+                    pusher="boris", sigma=SIGMA_10KEV,
+                    species=[dict(mass=1.0, charge=-1.0, sigma=SIGMA_10KEV),
+                             dict(mass=1836.0, charge=1.0, sigma=SIGMA_10KEV / np.sqrt(1836.0))])
     if getattr(args, "workload", "thermal") == "uneven":
         # batched uneven patches: 512 x 256 x 256 cells in 1024 patches of 32^3, particles per
         # cell per patch 8 * exp(N(0, 1.5)) floored and clipped to [0, 64], T = 5 keV, Boris
@@ -61,11 +68,14 @@ def workload_cfg(args):
 NCU_TRAFFIC_BYTES_PER_PARTICLE = {"mixed": (664.124160e6 + 530.128384e6) / 16777216, "fp64": None}
 
 
-def bytes_alg_per_particle_step(form, ppc):
-    """B_alg = S_state + 24 * s / ppc (state read+write once; 24 grid values per cell per step)."""
+def bytes_alg_per_particle_step(form, ppc, ndim=3):
+    """B_alg = S_state + 24 * s / ppc (state read+write once; 24 grid values per cell per step).
+    S_state: 3D 60 B mixed, 104 B FP64; 2D3V 52 B mixed, 88 B FP64."""
     if form == "mixed":
-        return 60.0 + 24 * 4 / ppc, 60.0, 4
-    return 104.0 + 24 * 8 / ppc, 104.0, 8
+        st = 60.0 if ndim == 3 else 52.0
+        return st + 24 * 4 / ppc, st, 4
+    st = 104.0 if ndim == 3 else 88.0
+    return st + 24 * 8 / ppc, st, 8
 
 
 def measured_peak():
@@ -135,6 +145,39 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def make_uniform_2d(cfg, sigma, seed, device):
+    """ppc particles per cell at uniform random positions, Maxwellian momenta of width sigma,
+    weight n0 dV / ppc (n0 = 1), 2D, on the device."""
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    n_cells, cl, ppc = cfg["n_cells"], cfg["cell_length"], cfg["ppc"]
+    n = int(np.prod(n_cells)) * ppc
+    cell = torch.arange(n, device=device, dtype=torch.int64) // ppc
+    pos = torch.empty((2, n), dtype=torch.float64, device=device)
+    pos[0] = ((cell // n_cells[1]).to(torch.float64) + torch.rand(n, generator=g, device=device,
+                                                                   dtype=torch.float64)) * cl[0]
+    pos[1] = ((cell % n_cells[1]).to(torch.float64) + torch.rand(n, generator=g, device=device,
+                                                                  dtype=torch.float64)) * cl[1]
+    mom = torch.randn((3, n), generator=g, device=device, dtype=torch.float64) * sigma
+    w = torch.full((n,), float(np.prod(cl)) / ppc, dtype=torch.float64, device=device)
+    return pos, mom, w
+
+
+def add_plasma(sim, cfg, seed, device):
+    """Adds the workload's species to sim; returns the particle count."""
+    if "species" in cfg:
+        n = 0
+        for k, sp in enumerate(cfg["species"]):
+            pos, mom, w = make_uniform_2d(cfg, sp["sigma"], seed + 7919 * k, device)
+            sim.add_species(sp["mass"], sp["charge"], cfg["pusher"], pos, mom, w)
+            n += int(w.shape[0])
+        return n
+    pos, mom, w = make_plasma(cfg, seed, device)
+    sim.add_species(1.0, -1.0, cfg["pusher"], pos, mom, w)
+    return int(w.shape[0])
+
+
 def make_plasma(cfg, seed, device):
     """Seeded plasma generated on the device (FP64 positions, momenta, weights).
 
@@ -193,8 +236,6 @@ def run_gpu(args, rank, world, local_rank):
     device = f"cuda:{local_rank}"
     torch.cuda.set_device(local_rank)
     cfg = workload_cfg(args)
-    pos, mom, w = make_plasma(cfg, args.seed + rank, device)
-    n = int(w.shape[0])
     # a dedicated stream: the step is captured as a CUDA graph, which the legacy default stream does not allow
     stream = torch.cuda.Stream(device=device)
     torch.cuda.set_stream(stream)
@@ -204,17 +245,23 @@ def run_gpu(args, rank, world, local_rank):
         sm = simulation.Simulation(cfg["n_cells"], cfg["cell_length"], cfg["dt"], form=args.form,
                                    tile=list(tile) if tile else None, use_graph=True, capacity_slack=args.slack)
         _lib.check(_lib.lib().sg_sim_set_stream(sm._h, stream.cuda_stream), "set_stream")
-        sm.add_species(1.0, -1.0, cfg["pusher"], pos, mom, w)
+        add_plasma(sm, cfg, args.seed + rank, device)
+        torch.cuda.empty_cache()
         return sm
 
-    tile, tuning = ([args.tile] * 3 if args.tile else None), None
+    ndim = len(cfg["n_cells"])
+    tile, tuning = ([args.tile] * ndim if args.tile else None), None
     if args.autotune:
         from smilei_gb300 import autotune
-        best, times = autotune.tune_tiles(build, ndim=3)
+        best, times = autotune.tune_tiles(build, ndim=ndim)
         tile, tuning = list(best), {"x".join(map(str, k)): round(v, 3) for k, v in times.items()}
     sim = build(tile)
-    del pos, mom, w
-    torch.cuda.empty_cache()
+    nspec = len(cfg.get("species", [None]))
+    n = sum(sim.species_count(k) for k in range(nspec))
+    # initial E from the charge (FP64 CG, as the reference's solve_poisson): the charge
+    # residual then measures what the steps add
+    poisson = sim.solve_poisson() if args.poisson else None
+    res0 = sim.charge_residual() if args.poisson else None
     uk0, ue0 = sim.energy()
     for _ in range(args.warmup):
         sim.step(1)
@@ -241,11 +288,41 @@ def run_gpu(args, rank, world, local_rank):
         td.barrier()
     ms = max_over_ranks(ev0.elapsed_time(ev1), device)
     uk1, ue1 = sim.energy()
+    res1 = sim.charge_residual() if args.poisson else None
     relayouts = sim.layout_stats()
+    # the run's fields after the warm-up and timed steps, for the comparison with the FP64 form
+    fields_mixed = None
+    if args.compare_fp64 and args.form == "mixed" and args.workload in ("thermal", "thermal2d"):
+        fields_mixed = {k: sim.get_field(k) for k in COMPARE_FIELDS}
 
     # e2e: the same step driven from host buffers through the C ABI
     e2e = None
-    if not args.no_e2e:
+    if not args.no_e2e and nspec > 1:
+        # every species' packed state host->device, the step, and back (no streamed variant
+        # for several species)
+        nb = [sim.packed_bytes(k) for k in range(nspec)]
+        hosts = [torch.empty(b, dtype=torch.uint8, pin_memory=True) for b in nb]
+        for k in range(nspec):
+            sim.pack_state(k, hosts[k].data_ptr())
+        torch.cuda.synchronize()
+        ke = max(1, min(args.steps, args.e2e_steps))
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(ke):
+            for k in range(nspec):
+                sim.unpack_state(k, hosts[k].data_ptr())
+            sim.step(1)
+            for k in range(nspec):
+                sim.pack_state(k, hosts[k].data_ptr())
+            sim.energy()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ems = max_over_ranks(e0.elapsed_time(e1), device)
+        e2e = {"value": whole_job_rate(n, world, ke, ems), "unit": UNIT, "h2d_bytes_per_step": int(sum(nb)),
+               "d2h_bytes_per_step": int(sum(nb) + 16), "steps": ke}
+        del hosts
+    elif not args.no_e2e:
         nbytes = sim.packed_bytes(0)
         host = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
         sim.pack_state(0, host.data_ptr())
@@ -278,8 +355,12 @@ def run_gpu(args, rank, world, local_rank):
             e2e["last_step_stages_ms"] = sim.stream_timing()
         del host
     sim.close()
+    fp64 = None
+    if fields_mixed is not None:
+        fp64 = run_fp64_compare(args, cfg, rank, device, stream, fields_mixed, (uk0 + ue0, uk1 + ue1))
+        del fields_mixed
     ncell_all = int(np.prod(cfg["n_cells"]))
-    B_alg, s_state, s = bytes_alg_per_particle_step(args.form, n / ncell_all)
+    B_alg, s_state, s = bytes_alg_per_particle_step(args.form, n / ncell_all, len(cfg["n_cells"]))
     ncell = int(np.prod(cfg["n_cells"]))
     kernel_bytes = n * s_state + ncell * 9 * s  # state read+write; gather E,B_m and J write per cell
     t_kernel = float(np.mean(t_part)) / 1e3
@@ -288,7 +369,59 @@ def run_gpu(args, rank, world, local_rank):
     return dict(n=n, ms=ms, value=value, wall_ms_per_step=(wall1 - wall0) * 1e3 / args.steps, e2e=e2e,
                 kernel_bytes=kernel_bytes, t_kernel=t_kernel, peak=peak, peak_kind=peak_kind, B_alg=B_alg,
                 launches=launches, clocks=clk.summary(), energy=(uk0, ue0, uk1, ue1), cfg=cfg, tile=tile,
-                tuning=tuning, relayouts=relayouts)
+                tuning=tuning, relayouts=relayouts, fp64=fp64,
+                residual=None if res0 is None else {"after_poisson": res0, "after_steps": res1,
+                                                    "poisson_iterations": poisson[0]})
+
+
+COMPARE_FIELDS = ["Ex", "Ey", "Ez", "Bx", "By", "Bz", "Jx", "Jy", "Jz"]
+
+
+def rel_l2(a_list, b_list):
+    """sqrt(sum |a - b|^2 / sum |b|^2) over a group of arrays (b the FP64 run)."""
+    num = sum(float(np.sum((a - b) ** 2)) for a, b in zip(a_list, b_list))
+    den = sum(float(np.sum(b ** 2)) for b in b_list)
+    return (num / den) ** 0.5 if den > 0 else num ** 0.5
+
+
+def run_fp64_compare(args, cfg, rank, device, stream, fields_mixed, utot_mixed):
+    """The plain FP64 form on the same seeded plasma, the same number of steps: its
+    throughput (the mixed form's target is 2x it) and the mixed run's errors against it
+    (relative L2 of E, B and J after the steps, energy drift, charge residual)."""
+    import torch
+    from smilei_gb300 import simulation, _lib
+    sim = simulation.Simulation(cfg["n_cells"], cfg["cell_length"], cfg["dt"], form="fp64", use_graph=True,
+                                capacity_slack=args.slack)
+    _lib.check(_lib.lib().sg_sim_set_stream(sim._h, stream.cuda_stream), "set_stream")
+    n = add_plasma(sim, cfg, args.seed + rank, device)
+    torch.cuda.empty_cache()
+    if args.poisson:
+        sim.solve_poisson()
+    uk0, ue0 = sim.energy()
+    for _ in range(args.warmup):
+        sim.step(1)
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        sim.step(1)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    uk1, ue1 = sim.energy()
+    res1 = sim.charge_residual() if args.poisson else None
+    f64 = {k: sim.get_field(k) for k in COMPARE_FIELDS}
+    sim.close()
+    err = {"E_rel_l2": rel_l2([fields_mixed[k] for k in COMPARE_FIELDS[:3]], [f64[k] for k in COMPARE_FIELDS[:3]]),
+           "B_rel_l2": rel_l2([fields_mixed[k] for k in COMPARE_FIELDS[3:6]], [f64[k] for k in COMPARE_FIELDS[3:6]]),
+           "J_rel_l2": rel_l2([fields_mixed[k] for k in COMPARE_FIELDS[6:]], [f64[k] for k in COMPARE_FIELDS[6:]]),
+           "energy_drift_mixed": (utot_mixed[1] - utot_mixed[0]) / utot_mixed[0],
+           "energy_drift_fp64": (uk1 + ue1 - uk0 - ue0) / (uk0 + ue0),
+           "energy_mixed_vs_fp64": (utot_mixed[1] - (uk1 + ue1)) / (uk1 + ue1),
+           "charge_residual_fp64": res1}
+    return {"value": n * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps, "steps": args.steps,
+            "warmup": args.warmup, "errors": err}
 
 
 LWFA = dict(n_cells=[3840, 512], cell_length=[0.1, 1.5], dt=0.095, ppc=4, pusher="vay", n0=0.003, ramp=100.0,
@@ -639,6 +772,36 @@ def run_cpu_sample_radiation(args):
                        f"(oracle/pic_oracle.c, rad_oracle.c; fields held fixed)")
 
 
+def run_cpu_sample_2d(args, steps=None, warmup=1):
+    """The oracle's FP64 2D timestep on the whole 2D thermal workload (electrons and protons,
+    256 x 256 cells, 16 ppc each; all host cores)."""
+    import oracle
+    from smilei_gb300 import synthetic
+    cfg = workload_cfg(args)
+    n_cells, cl = cfg["n_cells"], cfg["cell_length"]
+    sp = []
+    for k, spc in enumerate(cfg["species"]):
+        pos, mom, w = synthetic.thermal_plasma(n_cells, cl, cfg["ppc"], spc["sigma"], args.seed + 7919 * k)
+        sp.append(dict(pos=pos, mom=mom, weight=w, charge=np.full(w.shape, int(spc["charge"]), np.int16),
+                       mass=spc["mass"], pusher=cfg["pusher"]))
+    fields = synthetic.periodic_em(args.seed, n_cells, 0.0, 0.0)
+    O = oracle.Oracle()
+    steps = steps or args.cpu_steps
+    for _ in range(max(1, warmup)):
+        O.pic_step(2, n_cells, 2, cl, cfg["dt"], fields, sp)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        O.pic_step(2, n_cells, 2, cl, cfg["dt"], fields, sp)
+    t1 = time.perf_counter()
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    npart = sum(s_["weight"].size for s_ in sp)
+    return dict(value=npart * steps / (t1 - t0), unit=UNIT, cores=cores, kind="port", steps=steps,
+                warmup=max(1, warmup), ms_per_step=(t1 - t0) * 1e3 / steps, particles=int(npart),
+                cells=int(np.prod(n_cells)),
+                sample=f"2D thermal 256x256 cells, electrons + protons x 16 ppc ({npart} particles), Boris, "
+                       f"{steps} FP64 steps of oracle/pic_oracle.c (OpenMP)")
+
+
 def run_cpu_sample(args, steps=None, warmup=1):
     """The oracle's FP64 timestep on a bounded sample of the workload (all host cores)."""
     import oracle
@@ -646,6 +809,8 @@ def run_cpu_sample(args, steps=None, warmup=1):
     dx = 0.1
     dt = 0.95 * dx / np.sqrt(3.0)
     from smilei_gb300 import synthetic
+    if getattr(args, "workload", "thermal") == "thermal2d":
+        return run_cpu_sample_2d(args, steps, warmup)
     if getattr(args, "workload", "thermal") == "uneven":
         # the same patch statistics on an n^3 grid cut into 8^3-cell patches
         pos, mom, w, _ = synthetic.uneven_plasma([n, n, n], [dx] * 3, [8, 8, 8], 8, 1.5, 64, np.sqrt(5.0 / 511.0),
@@ -667,7 +832,7 @@ def run_cpu_sample(args, steps=None, warmup=1):
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     value = pos.shape[1] * steps / (t1 - t0)
     return dict(value=value, unit=UNIT, cores=cores, kind="port", steps=steps, warmup=max(1, warmup),
-                ms_per_step=(t1 - t0) * 1e3 / steps,
+                ms_per_step=(t1 - t0) * 1e3 / steps, particles=int(pos.shape[1]), cells=n ** 3,
                 sample=f"{what} ({pos.shape[1]} electrons), {pusher}, "
                        f"{steps} FP64 steps of oracle/pic_oracle.c (OpenMP)")
 
@@ -683,14 +848,20 @@ def main():
     ap.add_argument("--ppc", type=int, default=8)
     ap.add_argument("--tile", type=int, default=0)
     ap.add_argument("--seed", type=int, default=1234)
-    ap.add_argument("--cpu-cells", type=int, default=64)
+    ap.add_argument("--cpu-cells", type=int, default=0,
+                    help="cells per dimension of the 3D CPU legs (default: the thermal workload's own 256; "
+                         "a 64^3 sample for the uneven workload)")
+    ap.add_argument("--no-poisson", dest="poisson", action="store_false",
+                    help="3D workloads: skip the initial FP64 Poisson solve (and the charge residual)")
+    ap.add_argument("--no-compare-fp64", dest="compare_fp64", action="store_false",
+                    help="3D thermal, mixed form: skip the FP64-form run on the same plasma")
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--e2e-chunks", type=int, default=32,
                     help="tile ranges of the streamed host step (0: unpack, step, pack one after another)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="thermal", choices=["thermal", "uneven", "lwfa", "radiation"])
+    ap.add_argument("--workload", default="thermal", choices=["thermal", "thermal2d", "uneven", "lwfa", "radiation"])
     ap.add_argument("--mlp", action="store_true", help="radiation workload: photon chi from the trained MLP")
     ap.add_argument("--resident", action="store_true",
                     help="radiation workload: the resident mixed-form step instead of the drop-in operators")
@@ -702,6 +873,8 @@ def main():
     ap.add_argument("--preroll-steps", type=int, default=-1,
                     help="wakefield workload: untimed steps before the warm-up (default: until the window moves)")
     args = ap.parse_args()
+    if args.cpu_cells <= 0:
+        args.cpu_cells = args.cells if args.workload == "thermal" else 64
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -721,6 +894,9 @@ def main():
     elif args.workload == "uneven":
         workload = ("3D uneven patches: 512x256x256 cells in 1024 patches of 32^3, particles per cell per patch "
                     "8*exp(N(0,1.5)) floored and clipped to [0,64], T=5 keV electrons, Boris, dt=0.95 CFL, periodic")
+    elif args.workload == "thermal2d":
+        workload = ("2D thermal plasma 256x256 cells, dx=dy=0.1, dt=0.95 CFL, periodic, electrons and protons "
+                    "(mass 1836) at 16 ppc each (2097152 particles), T=10 keV, Boris")
     else:
         workload = (f"3D thermal plasma {args.cells}^3 cells, {args.ppc} ppc electrons "
                     f"({args.cells ** 3 * args.ppc} particles per GPU), Higuera-Cary, dt=0.95 CFL, periodic")
@@ -736,7 +912,8 @@ def main():
         line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
                 "steps": r["steps"], "warmup": r["warmup"], "ms_per_step": r["ms_per_step"], "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, host)",
-                "config": {"workload": workload, "sample": r["sample"], "form": "fp64"},
+                "config": {"workload": workload, "sample": r["sample"], "form": "fp64",
+                           **({"global_particles": r["particles"], "cells": r["cells"]} if "particles" in r else {})},
                 "cpu_baseline": r,
                 "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
@@ -807,6 +984,10 @@ def main():
                    "energy_ukin_uelm_before_after": res["energy"], "tile": res["tile"] or "default 4x4x4",
                    "autotune_ms_per_step": res["tuning"],
                    "relayouts_spilled_over_run": res["relayouts"],
+                   **({"charge_residual": res["residual"]} if res.get("residual") else {}),
+                   **({"fp64_value": res["fp64"]["value"], "fp64_ms_per_step": res["fp64"]["ms_per_step"],
+                       "fp64_steps": res["fp64"]["steps"], "mixed_over_fp64": res["value"] / res["fp64"]["value"],
+                       "errors_vs_fp64": res["fp64"]["errors"]} if res.get("fp64") else {}),
                    **({"window": res["window"], "e2e_note": res["e2e_note"]} if "window" in res else {})},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": res["peak"], "unit": "GB/s",
                      "frac": achieved / res["peak"], "traffic": traffic, "kernel": "k_step_particles",

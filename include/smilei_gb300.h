@@ -112,17 +112,19 @@ int sg_sort_particles( int ndim, const int *patch_size, const double *xmin, cons
                        int *last_index, int *cell_keys, sg_stream_t stream );
 
 /* The same per-cell sort with no device allocation.  It has no counterpart in the
- * reference: it is for callers that cannot call cudaMalloc (code running inside a
- * CUDA graph capture in global mode, which refuses allocation calls; hosts that give
- * the library a fixed device-memory budget; loops that cannot take an allocation's
- * synchronisation).  Its scratch is a fixed array in the library's device image
- * (SG_SORT_NOALLOC_SCRATCH_BYTES, held on every GPU that loads the library until the
- * process exits), so it accepts at most SG_SORT_NOALLOC_MAX_PARTICLES particles and
+ * reference.  It is for callers that cannot call cudaMalloc: a host code that takes
+ * the GPU's memory into its own pool at start-up leaves nothing for a library to
+ * allocate later, and one that gives each library a fixed device-memory budget
+ * cannot let a call grow it.  Its scratch is a fixed array in the library's device
+ * image (SG_SORT_NOALLOC_SCRATCH_BYTES, held on every GPU that loads the library until
+ * the process exits), so it accepts at most SG_SORT_NOALLOC_MAX_PARTICLES particles and
  * SG_SORT_NOALLOC_MAX_CELLS cells ((patch_size+1)^ndim) and returns SG_ERR_ARG beyond
- * them.  The first call on a device looks the array's device address up (with that
- * device current); make that first call before any stream capture.  All calls share
- * the one array: calls whose GPU work overlaps (other streams, other threads) race
- * and must be serialised by the caller.  Arguments and results as sg_sort_particles. */
+ * them, before any GPU work.  The first call on a device looks the array's device
+ * address up (with that device current); make that first call before any stream
+ * capture.  The call waits for its stream before it returns (it reads the status
+ * word).  All calls share the one array, which keeps the last call's contents: calls
+ * whose GPU work overlaps (other streams, other threads) race and must be serialised
+ * by the caller.  Arguments and results as sg_sort_particles. */
 #define SG_SORT_NOALLOC_MAX_PARTICLES 262144
 #define SG_SORT_NOALLOC_MAX_CELLS 32768
 #define SG_SORT_NOALLOC_SCRATCH_BYTES ( 5 * 1024 * 1024 )

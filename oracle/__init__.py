@@ -63,12 +63,25 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
-def build_ref() -> str | None:
+def reference_src() -> str | None:
+    """The reference's src/ directory: $SMILEI_REFERENCE_SRC, else the reference tree
+    beside this checkout's parent, when either exists (it exists only where the
+    reference was unpacked, never on a machine that only runs the tests)."""
+    cands = [os.environ.get("SMILEI_REFERENCE_SRC"),
+             os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference", "src")]
+    for c in cands:
+        if c and os.path.isdir(c):
+            return c
+    return None
+
+
+def build_ref(src: str | None = None) -> str | None:
     """Compile the reference's operator sources (only where the reference tree exists)."""
     script = os.path.join(HERE, "build_ref.sh")
-    if not os.path.isdir("/root/reference/src"):
+    src = src or reference_src()
+    if src is None:
         return None
-    subprocess.run(["bash", script], check=True, stdout=subprocess.DEVNULL)
+    subprocess.run(["bash", script, src], check=True, stdout=subprocess.DEVNULL)
     return REF_PATH if os.path.exists(REF_PATH) else None
 
 

@@ -10,10 +10,11 @@
 # operators calls either library.  The result is loaded only by tests/ and by
 # tests/golden/make_golden.py to pin the C restatement in oracle/pic_oracle.c.
 #
-# usage: oracle/build_ref.sh [reference_src_dir]   (default /root/reference/src)
+# usage: oracle/build_ref.sh [reference_src_dir]
+#   (default: $SMILEI_REFERENCE_SRC, else ../reference/src beside the checkout)
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-SRC="${1:-/root/reference/src}"
+SRC="${1:-${SMILEI_REFERENCE_SRC:-$HERE/../../reference/src}}"
 OUT="$HERE/_ref"
 if [ ! -d "$SRC" ]; then
     echo "build_ref: reference sources not found at $SRC; skipping" >&2

@@ -1992,6 +1992,7 @@ struct SpeciesState {
     PBuf<true> om{};
     int *ovf_tile = nullptr;
     int max_cap = 0; // largest tile segment of the current layout
+    std::vector<int> h_cap;    // host copy of cap (the current layout's segment capacities)
     bool radiates = false;     // carries an optical-depth plane (Monte-Carlo radiation)
     void *tau_mem[2] = { nullptr, nullptr };
     void *ovf_tau = nullptr;
@@ -2444,7 +2445,7 @@ int alloc_species_buffers( sg_sim *S, SpeciesState &s, int64_t capacity )
 
 // New segment layout from counts: cap, seg_start into (new_cap, new_start); returns the total.
 int layout_from_counts( sg_sim *S, const int *count, int *new_cap, int64_t *new_start, int64_t *total, int *max_cap,
-                        double slack_override = 0.0 )
+                        std::vector<int> &caps, double slack_override = 0.0 )
 {
     const int nt = S->g.ntiles;
     const float slack = ( float )( slack_override > 0.0 ? slack_override
@@ -2459,7 +2460,7 @@ int layout_from_counts( sg_sim *S, const int *count, int *new_cap, int64_t *new_
     int last_cap = 0;
     SG_CUDA_TRY( cudaMemcpyAsync( &last_start, new_start + nt - 1, sizeof( int64_t ), cudaMemcpyDeviceToHost, S->stream ) );
     SG_CUDA_TRY( cudaMemcpyAsync( &last_cap, new_cap + nt - 1, sizeof( int ), cudaMemcpyDeviceToHost, S->stream ) );
-    std::vector<int> caps( nt );
+    caps.assign( nt, 0 );
     SG_CUDA_TRY( cudaMemcpyAsync( caps.data(), new_cap, nt * sizeof( int ), cudaMemcpyDeviceToHost, S->stream ) );
     SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
     *total = last_start + last_cap;
@@ -2522,7 +2523,8 @@ int relayout( sg_sim *S, SpeciesState &s, int nspill )
     if( s.slack <= 0.0 ) s.slack = base;
     if( s.last_relayout >= 0 && S->hstep - s.last_relayout < RELAYOUT_WINDOW ) s.slack = std::min( 2.0, 2.0 * s.slack );
     s.last_relayout = S->hstep;
-    int r = layout_from_counts( S, s.count[s.cur], S->tmp_cap, S->tmp_start, &total, &new_max_cap, s.slack );
+    std::vector<int> new_caps;
+    int r = layout_from_counts( S, s.count[s.cur], S->tmp_cap, S->tmp_start, &total, &new_max_cap, new_caps, s.slack );
     if( r ) return r;
     // destination: the idle buffer, or fresh buffers when the layout no longer fits
     void *old_mem[2] = { s.mem[0], s.mem[1] }, *old_tau[2] = { s.tau_mem[0], s.tau_mem[1] };
@@ -2545,6 +2547,7 @@ int relayout( sg_sim *S, SpeciesState &s, int nspill )
     SG_CUDA_TRY( cudaMemcpyAsync( s.seg_start, S->tmp_start, nt * sizeof( int64_t ), cudaMemcpyDeviceToDevice, S->stream ) );
     SG_CUDA_TRY( cudaMemcpyAsync( s.cap, S->tmp_cap, nt * sizeof( int ), cudaMemcpyDeviceToDevice, S->stream ) );
     s.max_cap = new_max_cap;
+    s.h_cap.swap( new_caps );
     if( S->mixed ) r = place_staged<true>( S, s, nspill, s.om, s.ovf_tile, dst_buf );
     else r = place_staged<false>( S, s, nspill, s.od, s.ovf_tile, dst_buf );
     if( r ) return r;
@@ -2614,7 +2617,8 @@ int rebuild_species( sg_sim *S, SpeciesState &s, int shift, int x0, int x1 )
     }
     int64_t total = 0;
     int new_max_cap = 0;
-    int r = layout_from_counts( S, newcount, S->tmp_cap, S->tmp_start, &total, &new_max_cap, s.slack ); // synchronises
+    std::vector<int> new_caps;
+    int r = layout_from_counts( S, newcount, S->tmp_cap, S->tmp_start, &total, &new_max_cap, new_caps, s.slack ); // synchronises
     if( r ) return r;
     unsigned long long wc[2] = { 0, 0 };
     SG_CUDA_TRY( cudaMemcpyAsync( wc, S->d_wcount, sizeof( wc ), cudaMemcpyDeviceToHost, st ) );
@@ -2644,6 +2648,7 @@ int rebuild_species( sg_sim *S, SpeciesState &s, int shift, int x0, int x1 )
     SG_CUDA_TRY( cudaStreamSynchronize( st ) );
     const int old_chunk = launch_chunk( S, s.max_cap );
     s.max_cap = new_max_cap;
+    s.h_cap.swap( new_caps );
     s.cur = dst;
     s.npart += ( int64_t )wc[1] - ( int64_t )wc[0];
     if( realloc ) {
@@ -2938,7 +2943,7 @@ int sg_sim_add_species_device( sg_sim *S, double mass, double charge, int pusher
         SG_LAUNCH_CHECK( "k_stage" );
     }
     int64_t total = 0;
-    int r = layout_from_counts( S, s.count[1], s.cap, s.seg_start, &total, &s.max_cap );
+    int r = layout_from_counts( S, s.count[1], s.cap, s.seg_start, &total, &s.max_cap, s.h_cap );
     if( r ) return r;
     r = alloc_species_buffers( S, s, std::max<int64_t>( total, 1 ) );
     if( r ) return r;
@@ -3527,6 +3532,13 @@ int sg_sim_step_host( sg_sim *S, int species, const void *host_in, void *host_ou
         hoff[t + 1] = hoff[t] + hc[t];
     }
     SG_REQUIRE( hoff[nt] == n, "the packed tile counts sum to %lld, the header says %lld", ( long long )hoff[nt], ( long long )n );
+    // The unpack would refuse a tile over its segment, but only after the copy out of
+    // earlier ranges had begun, and host_out may be host_in: check before any copy.
+    SG_REQUIRE( ( int )s.h_cap.size() == nt, "no host copy of the segment layout" );
+    for( int t = 0; t < nt; t++ )
+        if( hc[t] > s.h_cap[t] )
+            return set_error( SG_ERR_ARG, "tile %d of the packed state holds %d particles, more than its segment (%d) in the current layout",
+                              t, hc[t], s.h_cap[t] );
 
     StreamIn in;
     in.species = species;

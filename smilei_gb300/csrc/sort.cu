@@ -297,7 +297,13 @@ extern "C" int sg_sort_particles_noalloc( int ndim, const int *patch_size, const
     int h_status = 0;
     rc = sort_with_scratch( g, ncell, npart, dprops, n_dprops, charge, first_index, last_index, cell_keys, off,
                             scan_tmp, keys, perm, count, fill, status, tmp, s, &h_status );
-    if( rc ) return rc;
+    if( rc ) {
+        // work queued before the failure may still use the shared array: let it end
+        // before the caller retries (perhaps on another stream)
+        cudaStreamSynchronize( s );
+        cudaGetLastError();
+        return rc;
+    }
     SG_CUDA_TRY( cudaStreamSynchronize( s ) );
     if( h_status ) return set_error( h_status, "a particle lies outside the patch's node lattice" );
     return SG_OK;

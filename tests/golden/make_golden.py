@@ -1,8 +1,10 @@
 """Generate the golden fixtures in tests/golden from the reference's own operators.
 
-Run here, where the reference tree is present:
+Run where the reference tree is present:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [reference_src_dir]
+
+(default: $SMILEI_REFERENCE_SRC, else ../reference/src beside the checkout).
 
 It compiles the reference's operator sources (oracle/build_ref.sh), feeds them
 seeded inputs, and stores inputs and outputs as .npz files next to this script.
@@ -21,6 +23,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
 import oracle  # noqa: E402
+
+REF_SRC = sys.argv[1] if len(sys.argv) > 1 else oracle.reference_src()
 
 FIELDS_EB = ["Ex", "Ey", "Ez", "Bx", "By", "Bz"]
 
@@ -142,7 +146,7 @@ def reference_laser_gaussian2d(cfg):
     tree) to build LaserGaussian2D and returns its Laser component."""
     ns = {}
     for f in ("pyinit.py", "pyprofiles.py"):
-        path = os.path.join("/root/reference/src/Python", f)
+        path = os.path.join(REF_SRC, "Python", f)
         exec(compile(open(path).read(), path, "exec"), ns)
     ns["Main"](geometry="2Dcartesian", interpolation_order=2, timestep=cfg["dt"], simulation_time=cfg["t_sim"],
                cell_length=list(cfg["cell_length"]), grid_length=list(cfg["grid_length"]), number_of_patches=[1, 1])
@@ -198,7 +202,7 @@ def boundary_cases(ref):
 
 
 def main():
-    path = oracle.build_ref()
+    path = oracle.build_ref(REF_SRC)
     if path is None:
         raise SystemExit("reference tree not found; the fixtures cannot be regenerated here")
     ref = oracle.RefOps(path)

@@ -221,6 +221,36 @@ def test_step_host_matches_unpack_step_pack(sim_mod, form, n_cells):
     b.close()
 
 
+def test_step_host_refuses_a_tile_over_its_segment_and_leaves_the_input(sim_mod):
+    """A packed state whose tile holds more particles than its segment in the current
+    layout is refused before anything is copied: host_in (here also host_out) keeps
+    its bytes, and the simulation can still step the valid state afterwards."""
+    simulation, synthetic = sim_mod
+    n_cells, cl = [16, 16, 16], [0.1, 0.1, 0.1]
+    dt = 0.95 * 0.1 / np.sqrt(3.0)
+    pos, mom, w = synthetic.thermal_plasma(n_cells, cl, 8, 0.14, 4, unique_weights=True)
+    sim = simulation.Simulation(n_cells, cl, dt, form="mixed")
+    sim.add_species(1.0, -1.0, "higueracary", pos, mom, w)
+    host = np.zeros(sim.packed_bytes(0), dtype=np.uint8)
+    sim.pack_state(0, host.ctypes.data)
+    torch.cuda.synchronize()
+    nt = int(np.prod(n_cells)) // 64
+    counts = host[8:8 + 4 * nt].view(np.int32)
+    bad = host.copy()
+    bc = bad[8:8 + 4 * nt].view(np.int32)
+    moved = int(counts[1]) // 2 + 300  # tile 0 far over its capacity; the total is unchanged
+    moved = min(moved, int(counts[1]))
+    bc[0] += moved
+    bc[1] -= moved
+    before = bad.copy()
+    with pytest.raises(RuntimeError, match="segment"):
+        sim.step_host(0, bad.ctypes.data, chunks=4)
+    assert np.array_equal(bad, before)
+    sim.step_host(0, host.ctypes.data, chunks=4)
+    assert sim.species_count(0) == len(w)
+    sim.close()
+
+
 @pytest.mark.parametrize("form", ["mixed", "fp64"])
 def test_packed_state_round_trip(sim_mod, form):
     """pack -> (one more step) -> unpack restores the packed particles exactly; the

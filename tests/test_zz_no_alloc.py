@@ -1,14 +1,14 @@
 """The per-cell sort entry point that allocates no device memory.
 
-sg_sort_particles_noalloc exists for callers that cannot call cudaMalloc: code
-running while a CUDA graph is captured in global mode (allocation calls are
-refused there), hosts that give the library a fixed device-memory budget, and
-loops that cannot take an allocation's synchronisation.  It sorts on a fixed
-scratch array in the library's device image instead.  These tests call it
-through the C ABI and require results identical to sg_sort_particles, the
-allocating entry point, on two calls in a row with different shapes (the
-shared array keeps the previous call's contents, which must not leak into the
-next result).  The file is named to be collected last.
+sg_sort_particles_noalloc exists for callers that cannot call cudaMalloc: a host
+code that takes all of the GPU's memory into its own pool at start-up leaves none
+for the library, and one that gives each library a fixed device-memory budget
+cannot let a call grow it.  It sorts on a fixed scratch array in the library's
+device image instead.  These tests call it through the C ABI and require results
+identical to sg_sort_particles, the allocating entry point, on two calls in a row
+with different shapes (the shared array keeps the previous call's contents, which
+must not leak into the next result), and at its stated limits.  The file is
+named to be collected last.
 """
 import ctypes
 
@@ -67,6 +67,18 @@ def test_noalloc_sort_matches_allocating_sort_twice_in_a_row(lib):
         for a, b in zip(got, ref):
             assert np.array_equal(a, b), (ndim, patch, n)
         assert np.all(np.diff(got[-1]) >= 0)
+
+
+def test_noalloc_sort_at_its_limits_matches_allocating_sort(lib):
+    """Exactly SG_SORT_NOALLOC_MAX_PARTICLES particles on a 32 x 32 x 32 node lattice,
+    exactly SG_SORT_NOALLOC_MAX_CELLS: the fixed scratch holds the whole layout."""
+    ndim, patch, n = 3, [31, 31, 31], 262144
+    cl, xmin, pos, mom, w, q = _inputs(13, ndim, patch, n)
+    for _ in range(2):
+        got = _sort(lib, "sg_sort_particles_noalloc", ndim, patch, cl, xmin, pos, mom, w, q)
+        ref = _sort(lib, "sg_sort_particles", ndim, patch, cl, xmin, pos, mom, w, q)
+        for a, b in zip(got, ref):
+            assert np.array_equal(a, b)
 
 
 def test_noalloc_sort_rejects_sizes_beyond_its_scratch(lib):
