@@ -250,17 +250,19 @@ def run_gpu(args, rank, world, local_rank):
         return sm
 
     ndim = len(cfg["n_cells"])
-    tile, tuning = ([args.tile] * ndim if args.tile else None), None
+    tile, tuning, queue = ([args.tile] * ndim if args.tile else None), None, args.tile_queue
     if args.autotune:
         from smilei_gb300 import autotune
-        best, times = autotune.tune_tiles(build, ndim=ndim)
-        tile, tuning = list(best), {"x".join(map(str, k)): round(v, 3) for k, v in times.items()}
+        (best, queue), times = autotune.tune(build, ndim=ndim)
+        tile = list(best)
+        tuning = {"x".join(map(str, k)) + (" queue" if q else ""): round(v, 3) for (k, q), v in times.items()}
     sim = build(tile)
+    sim.set_tile_queue(queue)
     nspec = len(cfg.get("species", [None]))
     n = sum(sim.species_count(k) for k in range(nspec))
     # initial E from the charge (FP64 CG, as the reference's solve_poisson): the charge
     # residual then measures what the steps add
-    poisson = sim.solve_poisson() if args.poisson else None
+    poisson = sim.solve_poisson(max_error=POISSON_MAX_ERROR) if args.poisson else None
     res0 = sim.charge_residual() if args.poisson else None
     uk0, ue0 = sim.energy()
     for _ in range(args.warmup):
@@ -369,12 +371,15 @@ def run_gpu(args, rank, world, local_rank):
     return dict(n=n, ms=ms, value=value, wall_ms_per_step=(wall1 - wall0) * 1e3 / args.steps, e2e=e2e,
                 kernel_bytes=kernel_bytes, t_kernel=t_kernel, peak=peak, peak_kind=peak_kind, B_alg=B_alg,
                 launches=launches, clocks=clk.summary(), energy=(uk0, ue0, uk1, ue1), cfg=cfg, tile=tile,
-                tuning=tuning, relayouts=relayouts, fp64=fp64,
+                tuning=tuning, relayouts=relayouts, fp64=fp64, queue=bool(queue),
                 residual=None if res0 is None else {"after_poisson": res0, "after_steps": res1,
                                                     "poisson_iterations": poisson[0]})
 
 
 COMPARE_FIELDS = ["Ex", "Ey", "Ez", "Bx", "By", "Bz", "Jx", "Jy", "Jz"]
+# r.r / n of the initial Poisson solve: far below the reference's default 1e-14, so that the
+# charge residual after the steps measures the steps, not the start
+POISSON_MAX_ERROR = 1e-24
 
 
 def rel_l2(a_list, b_list):
@@ -396,7 +401,7 @@ def run_fp64_compare(args, cfg, rank, device, stream, fields_mixed, utot_mixed):
     n = add_plasma(sim, cfg, args.seed + rank, device)
     torch.cuda.empty_cache()
     if args.poisson:
-        sim.solve_poisson()
+        sim.solve_poisson(max_error=POISSON_MAX_ERROR)
     uk0, ue0 = sim.energy()
     for _ in range(args.warmup):
         sim.step(1)
@@ -852,7 +857,7 @@ def main():
                     help="cells per dimension of the 3D CPU legs (default: the thermal workload's own 256; "
                          "a 64^3 sample for the uneven workload)")
     ap.add_argument("--no-poisson", dest="poisson", action="store_false",
-                    help="3D workloads: skip the initial FP64 Poisson solve (and the charge residual)")
+                    help="thermal workloads: skip the initial FP64 Poisson solve (and the charge residual)")
     ap.add_argument("--no-compare-fp64", dest="compare_fp64", action="store_false",
                     help="3D thermal, mixed form: skip the FP64-form run on the same plasma")
     ap.add_argument("--cpu-steps", type=int, default=3)
@@ -867,7 +872,11 @@ def main():
                     help="radiation workload: the resident mixed-form step instead of the drop-in operators")
     ap.add_argument("--rad-math", default="fp32", choices=["fp32", "fp64"],
                     help="radiation workload: arithmetic of the Monte-Carlo table lookups and draws")
-    ap.add_argument("--autotune", action="store_true", help="pick the tile shape by timing candidates first")
+    ap.add_argument("--autotune", action="store_true",
+                    help="pick the tile shape (and, for the 3D and 2D thermal and uneven workloads, the tile "
+                         "queue) by timing candidates first")
+    ap.add_argument("--tile-queue", action="store_true",
+                    help="particle kernel as a persistent grid draining a tile queue, densest tile first")
     ap.add_argument("--slack", type=float, default=0.25,
                     help="segment capacity slack: room per tile beyond its particle count, as a fraction")
     ap.add_argument("--preroll-steps", type=int, default=-1,
@@ -875,6 +884,10 @@ def main():
     args = ap.parse_args()
     if args.cpu_cells <= 0:
         args.cpu_cells = args.cells if args.workload == "thermal" else 64
+    # the uneven plasma is far from neutral patch by patch: a Poisson start would give it
+    # fields that empty the dense patches, another workload than the batched-patch one
+    if args.workload not in ("thermal", "thermal2d"):
+        args.poisson = False
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -982,6 +995,7 @@ def main():
                    "B_alg_bytes_per_particle_step": res["B_alg"],
                    "hbm_fraction_of_step": step_gbs / res["peak"], "wall_ms_per_step": res["wall_ms_per_step"],
                    "energy_ukin_uelm_before_after": res["energy"], "tile": res["tile"] or "default 4x4x4",
+                   "tile_queue": res.get("queue", False),
                    "autotune_ms_per_step": res["tuning"],
                    "relayouts_spilled_over_run": res["relayouts"],
                    **({"charge_residual": res["residual"]} if res.get("residual") else {}),

@@ -141,7 +141,11 @@ int sg_sort_particles_noalloc( int ndim, const int *patch_size, const double *xm
 typedef struct sg_sim_config {
     int ndim;              /* 2 or 3 */
     int form;              /* SG_FORM_FP64 or SG_FORM_MIXED */
-    int n_cells[3];        /* global cells per dimension */
+    int n_cells[3];        /* global cells per dimension, at least 8; the mixed form packs a
+                              particle's node into one 32-bit key (3D x:11 y:10 z:10 bits, 2D
+                              16:16), so it takes at most 2048 x 1024 x 1024 nodes in 3D and
+                              65536 x 65536 in 2D (an open axis has one node more than cells);
+                              sg_sim_create refuses larger grids in that form */
     double cell_length[3];
     double dt;
     int tile[3];           /* cells per tile (bin) per dimension; 0 = choose automatically */
@@ -162,17 +166,28 @@ typedef struct sg_mlp sg_mlp;               /* learned inverse CDF (below) */
 int sg_sim_create( const sg_sim_config *cfg, sg_sim **out );
 int sg_sim_destroy( sg_sim *sim );
 
+/* How the particle kernel's CTAs get their tiles.  on = 0 (default): one CTA per tile,
+ * handed out by the hardware block scheduler.  on = 1: a persistent grid (as many CTAs
+ * as fit on the GPU at once) whose CTAs take tiles from a device counter until none is
+ * left, densest tile first (order recomputed at every re-layout).  The reference hands
+ * patches to OpenMP threads with schedule(runtime) (src/Patch/VectorPatch.cpp:4777);
+ * this is the GPU's version of that work queue.  The results are the same either way.
+ * No reference counterpart as an entry point. */
+int sg_sim_set_tile_queue( sg_sim *sim, int on );
+
 /* Adds a species from host arrays (absolute FP64 positions pos[ndim*n],
  * momenta mom[3*n], weights[n]); pusher: 0 Boris, 1 Vay, 2 Higuera-Cary.
  * Returns the species index in *index. */
 int sg_sim_add_species( sg_sim *sim, double mass, double charge, int pusher, int64_t npart, const double *pos,
                         const double *mom, const double *weight, int *index );
 
-/* Same, from device arrays (same layout), without host copies. */
+/* Same, from device arrays (same layout), without host copies.  The call first waits
+ * for all work on the device, so arrays still being written on any stream are complete
+ * before they are read. */
 int sg_sim_add_species_device( sg_sim *sim, double mass, double charge, int pusher, int64_t npart,
                                const double *pos, const double *mom, const double *weight, int *index );
 
-/* Field access, reference layout with ghosts, FP64, host (set/get) or device (_device) buffers.
+/* Field access, reference layout with ghosts, FP64, host buffers.
  * comp: 0..2 Ex Ey Ez, 3..5 Bx By Bz, 6..8 Bx_m By_m Bz_m, 9..11 Jx Jy Jz. */
 int sg_sim_set_field( sg_sim *sim, int comp, const double *host );
 int sg_sim_get_field( sg_sim *sim, int comp, double *host );

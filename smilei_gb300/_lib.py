@@ -88,6 +88,7 @@ _SIGNATURES = {
     "sg_sim_last_timing": (_I, [_VP, ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.POINTER(_D),
                                 ctypes.POINTER(_I)]),
     "sg_sim_set_stream": (_I, [_VP, _VP]),
+    "sg_sim_set_tile_queue": (_I, [_VP, _I]),
     "sg_sim_state_bytes": (_I, [_VP, _I, ctypes.POINTER(ctypes.c_size_t)]),
     "sg_sim_packed_bytes": (_I, [_VP, _I, ctypes.POINTER(ctypes.c_size_t)]),
     "sg_sim_pack_state": (_I, [_VP, _I, _VP]),

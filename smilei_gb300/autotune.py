@@ -1,12 +1,14 @@
-"""Tile-shape autotuner for the resident step.
+"""Autotuner for the resident step: tile (bin) shape and how tiles reach the CTAs.
 
-The tile (bin) shape decides the work of one CTA of the particle kernel: the
-field and current tiles it stages, the cells the per-cell deposit walks, and
-how a dense region is cut into work items.  The best shape depends on the
-density and its spread, so it is measured: every candidate builds the same
-simulation, runs a few warm-up steps and a few timed steps (CUDA events on the
-simulation's stream), and the fastest is kept.  Candidates whose shape does not
-divide the grid are adjusted by the library exactly as a user's choice would be.
+The tile shape decides the work of one CTA of the particle kernel: the field and
+current tiles it stages, the cells the per-cell deposit walks, and how a dense
+region is cut into work items.  The tiles reach the CTAs either one CTA per tile
+through the hardware block scheduler, or through a device queue that a persistent
+grid drains, densest tile first (Simulation.set_tile_queue).  The best choice
+depends on the density and its spread, so it is measured: every candidate builds
+the same simulation, runs a few warm-up steps and a few timed steps (CUDA events
+on the simulation's stream), and the fastest is kept.  Candidates whose shape does
+not divide the grid are adjusted by the library exactly as a user's choice would be.
 """
 from __future__ import annotations
 
@@ -42,5 +44,35 @@ def tune_tiles(build, candidates=None, ndim=3, warmup=2, steps=3, log=None):
             torch.cuda.empty_cache()
         if log:
             log(f"tile {tile}: {times[tuple(tile)]:.3f} ms/step (trial {time.perf_counter() - t0:.1f} s)")
+    best = min(times, key=times.get)
+    return best, times
+
+
+def tune(build, ndim=3, tiles=None, queues=(False, True), warmup=2, steps=3, log=None):
+    """Every (tile shape, tile queue) pair: build(tile) -> Simulation, then the queue
+    setting, timed as in tune_tiles.  Returns ((best_tile, best_queue), {(tile, queue): ms})."""
+    import torch
+    cands = tiles or (CANDIDATES_3D if ndim == 3 else CANDIDATES_2D)
+    times = {}
+    for tile in cands:
+        for q in queues:
+            t0 = time.perf_counter()
+            sim = build(tuple(tile))
+            try:
+                sim.set_tile_queue(q)
+                for _ in range(warmup):
+                    sim.step(1)
+                torch.cuda.synchronize()
+                ms = []
+                for _ in range(steps):
+                    sim.step(1)
+                    ms.append(sim.last_timing()[2])
+                times[(tuple(tile), bool(q))] = sum(ms) / len(ms)
+            finally:
+                sim.close()
+                torch.cuda.empty_cache()
+            if log:
+                log(f"tile {tile} queue {q}: {times[(tuple(tile), bool(q))]:.3f} ms/step "
+                    f"(trial {time.perf_counter() - t0:.1f} s)")
     best = min(times, key=times.get)
     return best, times

@@ -65,9 +65,13 @@ __host__ __device__ inline int stag( int comp, int d )
     return d == comp - 3 ? 0 : 1;
 }
 
+// J is FP64 in both forms: the mixed form's per-tile FP32 currents are added into FP64
+// global arrays, so the sum over tiles and its storage add no FP32 rounding (each
+// rounding there breaks discrete charge conservation by the rounded amount).
 template <class T>
 struct Fields {
-    T *E[3], *B[3], *Bm[3], *J[3];
+    T *E[3], *B[3], *Bm[3];
+    double *J[3];
     T *Ec[3]; // compensation of E's FP32 sums (mixed form), else null
 };
 
@@ -97,6 +101,9 @@ struct SpecParams {
     double cr[3];    // cw * dx_d / dt: Esirkepov current factor per unit weight
     double vs[3];    // dt / dx_d: displacement in cells per unit velocity
     int tile0;       // first tile of the launch (block b steps tile tile0 + b)
+    int *queue;        // persistent launch: counter of the next item (null: one CTA per tile)
+    const int *order;  // tile of each item, relative to tile0 (null: item itself)
+    int nitems;        // items of a persistent launch
 };
 
 // Packed node index of the mixed form: 3D x:11 y:10 z:10 bits, 2D x:16 y:16 bits.
@@ -298,6 +305,39 @@ __device__ __forceinline__ T gather_tile( const T *__restrict__ F, const TileDim
     return r;
 }
 
+// Two components gathered at once with paired FP32 arithmetic (FFMA2: one instruction,
+// two independent IEEE fmas): the same operations as two gather_tile calls, half the
+// FMA instructions.  Each component has its own weights and tile origin.
+template <int DIM>
+__device__ __forceinline__ float2 gather_pair( const float *__restrict__ F1, const float *__restrict__ F2,
+                                               const TileDims &td, const float *cx1, const float *cx2,
+                                               const float *cy1, const float *cy2, const float *cz1,
+                                               const float *cz2, int bx1, int by1, int bz1, int bx2, int by2,
+                                               int bz2 )
+{
+    float2 r = make_float2( 0.f, 0.f );
+#pragma unroll
+    for( int a = 0; a < 3; a++ ) {
+        float2 ra = make_float2( 0.f, 0.f );
+#pragma unroll
+        for( int b = 0; b < 3; b++ ) {
+            const float *row1 = F1 + ( ( bx1 + a ) * td.FY + ( by1 + b ) ) * td.FZ + bz1;
+            const float *row2 = F2 + ( ( bx2 + a ) * td.FY + ( by2 + b ) ) * td.FZ + bz2;
+            float2 rb;
+            if( DIM == 3 ) {
+                rb = __fmul2_rn( make_float2( cz1[0], cz2[0] ), make_float2( row1[0], row2[0] ) );
+                rb = __ffma2_rn( make_float2( cz1[1], cz2[1] ), make_float2( row1[1], row2[1] ), rb );
+                rb = __ffma2_rn( make_float2( cz1[2], cz2[2] ), make_float2( row1[2], row2[2] ), rb );
+            } else {
+                rb = make_float2( row1[0], row2[0] );
+            }
+            ra = __ffma2_rn( make_float2( cy1[b], cy2[b] ), rb, ra );
+        }
+        r = __ffma2_rn( make_float2( cx1[a], cx2[a] ), ra, r );
+    }
+    return r;
+}
+
 template <class T>
 __device__ __forceinline__ void sh_add( T *a, T v )
 {
@@ -320,11 +360,28 @@ __device__ __forceinline__ T pick3( int j, T c0, T c1, T c2 )
     return j == 0 ? c0 : ( j == 1 ? c1 : ( j == 2 ? c2 : T( 0 ) ) );
 }
 
+// Deposit weights of the mixed form: the outer two on the 2^-24 grid, the middle one
+// 1 minus them.  They then sum to 1 exactly, S1 - S0 and its running sums are exact in
+// FP32, and the running sum over a whole window is exactly zero: the deposit breaks
+// charge conservation only by the rounding of the transverse weights and products.
+// (Plain FP32 weights sum to 1 only to a few ulp, a per-step error of that size at
+// the window's last node.)  The FP64 form keeps the reference's weights.
+template <class T>
+__device__ __forceinline__ void dep_spline( T d, T &c0, T &c1, T &c2 )
+{
+    bspline2( d, c0, c1, c2 );
+    if constexpr( sizeof( T ) == 4 ) {
+        c0 = rintf( c0 * 16777216.0f ) * ( 1.0f / 16777216.0f );
+        c2 = rintf( c2 * 16777216.0f ) * ( 1.0f / 16777216.0f );
+        c1 = ( 1.0f - c0 ) - c2;
+    }
+}
+
 template <class T>
 __device__ __forceinline__ void esir_win( T c0o, T c1o, T c2o, T dnew, int shift, EsirWin<T> &w )
 {
     T c0, c1, c2;
-    bspline2( dnew, c0, c1, c2 );
+    dep_spline( dnew, c0, c1, c2 );
     w.lo = shift < 0 ? 0 : 1;
     T run = T( 0 );
 #pragma unroll
@@ -490,7 +547,18 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
     __shared__ int sNX;         // length of that list
     __shared__ int sXc[4];      // node-changing particles per class (x, y, z only; several)
 
-    const int tile = blockIdx.x + sp.tile0;
+    // One tile per CTA, or (sp.queue set) a persistent grid whose CTAs take tiles from
+    // a device counter until none is left, in the order sp.order gives (densest first).
+    __shared__ int sItem;
+    for( int item = blockIdx.x;; ) {
+    if( sp.queue ) {
+        __syncthreads(); // the previous tile is done with shared memory
+        if( threadIdx.x == 0 ) sItem = atomicAdd( sp.queue, 1 );
+        __syncthreads();
+        item = sItem;
+        if( item >= sp.nitems ) break;
+    }
+    const int tile = sp.tile0 + ( sp.order ? sp.order[item] : item );
     int tz = 0, ty, tx;
     if( DIM == 3 ) {
         tz = tile % g.nt[2];
@@ -718,12 +786,26 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
         const int bz_p = DIM == 3 ? lx[2] : 0, bz_d = DIM == 3 ? lx[2] + sd[2] : 0;
         const int bx_p = lx[0], bx_d = lx[0] + sd[0], by_p = lx[1], by_d = lx[1] + sd[1];
         // Ex(d,p,p) Ey(p,d,p) Ez(p,p,d) Bx(p,d,d) By(d,p,d) Bz(d,d,p)
-        const T Ex = gather_tile<DIM, T>( sF + 0 * fsz, td, cd[0], cp[1], cp[2], bx_d, by_p, bz_p );
-        const T Ey = gather_tile<DIM, T>( sF + 1 * fsz, td, cp[0], cd[1], cp[2], bx_p, by_d, bz_p );
-        const T Ez = gather_tile<DIM, T>( sF + 2 * fsz, td, cp[0], cp[1], cd[2], bx_p, by_p, bz_d );
-        const T Bx = gather_tile<DIM, T>( sF + 3 * fsz, td, cp[0], cd[1], cd[2], bx_p, by_d, bz_d );
-        const T By = gather_tile<DIM, T>( sF + 4 * fsz, td, cd[0], cp[1], cd[2], bx_d, by_p, bz_d );
-        const T Bz = gather_tile<DIM, T>( sF + 5 * fsz, td, cd[0], cd[1], cp[2], bx_d, by_d, bz_p );
+        T Ex, Ey, Ez, Bx, By, Bz;
+        if constexpr( MIXED ) {
+            // paired: (Ex, By) share their x and y windows, (Ey, Bx) too
+            const float2 exby = gather_pair<DIM>( sF + 0 * fsz, sF + 4 * fsz, td, cd[0], cd[0], cp[1], cp[1], cp[2], cd[2],
+                                                  bx_d, by_p, bz_p, bx_d, by_p, bz_d );
+            const float2 eybx = gather_pair<DIM>( sF + 1 * fsz, sF + 3 * fsz, td, cp[0], cp[0], cd[1], cd[1], cp[2], cd[2],
+                                                  bx_p, by_d, bz_p, bx_p, by_d, bz_d );
+            const float2 ezbz = gather_pair<DIM>( sF + 2 * fsz, sF + 5 * fsz, td, cp[0], cd[0], cp[1], cd[1], cd[2], cp[2],
+                                                  bx_p, by_p, bz_d, bx_d, by_d, bz_p );
+            Ex = exby.x; By = exby.y;
+            Ey = eybx.x; Bx = eybx.y;
+            Ez = ezbz.x; Bz = ezbz.y;
+        } else {
+            Ex = gather_tile<DIM, T>( sF + 0 * fsz, td, cd[0], cp[1], cp[2], bx_d, by_p, bz_p );
+            Ey = gather_tile<DIM, T>( sF + 1 * fsz, td, cp[0], cd[1], cp[2], bx_p, by_d, bz_p );
+            Ez = gather_tile<DIM, T>( sF + 2 * fsz, td, cp[0], cp[1], cd[2], bx_p, by_p, bz_d );
+            Bx = gather_tile<DIM, T>( sF + 3 * fsz, td, cp[0], cd[1], cd[2], bx_p, by_d, bz_d );
+            By = gather_tile<DIM, T>( sF + 4 * fsz, td, cd[0], cp[1], cd[2], bx_d, by_p, bz_d );
+            Bz = gather_tile<DIM, T>( sF + 5 * fsz, td, cd[0], cd[1], cp[2], bx_d, by_d, bz_p );
+        }
 
         // ---- push -----------------------------------------------------------------
         const T ginv = push_t<KIND, T>( qm, Ex, Ey, Ez, Bx, By, Bz, px, py, pz );
@@ -790,7 +872,12 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
             } else if( !gone ) {
                 EsirWin<T> W[3];
 #pragma unroll
-                for( int d = 0; d < DIM; d++ ) esir_win<T>( cp[d][0], cp[d][1], cp[d][2], dnew[d], shift[d], W[d] );
+                for( int d = 0; d < DIM; d++ ) {
+                    // the old weights of the deposit (the gather's, requantised in the mixed form)
+                    T o0 = cp[d][0], o1 = cp[d][1], o2 = cp[d][2];
+                    if constexpr( MIXED ) dep_spline( dlt[d], o0, o1, o2 );
+                    esir_win<T>( o0, o1, o2, dnew[d], shift[d], W[d] );
+                }
                 const T cr[3] = { cr3[0] * w, cr3[1] * w, cr3[2] * w };
                 deposit_direct<DIM, T>( sJ, td, jsz, lx, W, cr, cw0 * w * pz * ginv );
             }
@@ -946,10 +1033,14 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
             // 3D: acc = along-axis current (m, u, v), accz = Jz plane hf (u, v)
             // 2D: acc = Jx (m, u) then Jy (u, m), accz = Jz (u, v)
             T acc[18], accz[9];
+            float2 acc2[9]; // 3D: the along-axis current's two planes (m = 0, 1) as a pair
 #pragma unroll
             for( int k = 0; k < 18; k++ ) acc[k] = T( 0 );
 #pragma unroll
-            for( int k = 0; k < 9; k++ ) accz[k] = T( 0 );
+            for( int k = 0; k < 9; k++ ) {
+                accz[k] = T( 0 );
+                acc2[k] = make_float2( 0.f, 0.f );
+            }
             const int end = sStart[c] + sCnt[c];
             for( int q = sStart[c] + q0; q < end; q += qstep ) {
                 if( __float_as_int( sRec[6 * nmax + q] ) != NO_SHIFT ) continue; // in the node-changing list
@@ -968,8 +1059,8 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
 #pragma unroll
                     for( int d = 0; d < DIM; d++ ) {
                         T o0, o1, o2, n0, n1, n2;
-                        bspline2( dold[d], o0, o1, o2 );
-                        bspline2( dn[d], n0, n1, n2 );
+                        dep_spline( dold[d], o0, o1, o2 );
+                        dep_spline( dn[d], n0, n1, n2 );
                         A[d][0] = T( 0.5 ) * ( o0 + n0 ); A[d][1] = T( 0.5 ) * ( o1 + n1 ); A[d][2] = T( 0.5 ) * ( o2 + n2 );
                         D[d][0] = n0 - o0; D[d][1] = n1 - o1; D[d][2] = n2 - o2;
                         P[d][0] = D[d][0];
@@ -980,16 +1071,21 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
                         const T cra = hf ? cr[1] : cr[0];
                         const T pa0 = hf ? P[1][0] : P[0][0], pa1 = hf ? P[1][1] : P[0][1];
                         const T pz = hf ? P[2][1] : P[2][0];
+                        // paired FP32 arithmetic (FFMA2): (wt, wz) together, then both planes
+                        // of the along-axis current in one instruction
+                        const float2 cpa = make_float2( -( cra * pa0 ), -( cra * pa1 ) );
+                        const T cpz = -( cr[2] * pz );
 #pragma unroll
                         for( int u = 0; u < 3; u++ ) {
                             const T ab = hf ? A[0][u] : A[1][u], db = hf ? D[0][u] : D[1][u];
+                            const float2 au = make_float2( ab, A[0][u] ), du = make_float2( twelfth * db, twelfth * D[0][u] );
 #pragma unroll
                             for( int v = 0; v < 3; v++ ) {
-                                const T wt = ab * A[2][v] + twelfth * db * D[2][v];
-                                acc[( 0 * 3 + u ) * 3 + v] -= cra * pa0 * wt;
-                                acc[( 1 * 3 + u ) * 3 + v] -= cra * pa1 * wt;
-                                const T wz = A[0][u] * A[1][v] + twelfth * D[0][u] * D[1][v];
-                                accz[u * 3 + v] -= cr[2] * pz * wz;
+                                // .x = wt = ab A_z + db D_z / 12, .y = wz = A_x A_y + D_x D_y / 12
+                                const float2 w2 = __ffma2_rn( au, make_float2( A[2][v], A[1][v] ),
+                                                              __fmul2_rn( du, make_float2( D[2][v], D[1][v] ) ) );
+                                acc2[u * 3 + v] = __ffma2_rn( cpa, make_float2( w2.x, w2.x ), acc2[u * 3 + v] );
+                                accz[u * 3 + v] = fmaf( cpz, w2.y, accz[u * 3 + v] );
                             }
                         }
                     } else {
@@ -1017,7 +1113,7 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
                         for( int m = 0; m < 2; m++ ) {
                             const int ia = ( hf ? cl[0] + 1 + u : cl[0] + 2 + m ), ib = ( hf ? cl[1] + 2 + m : cl[1] + 1 + u );
                             const int ea = ( ia * td.JY + ib ) * td.JZ + cl[2] + 1 + v;
-                            sh_add( &Ja[ea], acc[( m * 3 + u ) * 3 + v] );
+                            sh_add( &Ja[ea], m == 0 ? acc2[u * 3 + v].x : acc2[u * 3 + v].y );
                         }
                         const int ez = ( ( cl[0] + 1 + u ) * td.JY + cl[1] + 1 + v ) * td.JZ + cl[2] + 2 + hf;
                         sh_add( &Jz[ez], accz[u * 3 + v] );
@@ -1063,7 +1159,7 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
 #pragma unroll
             for( int d = 0; d < DIM; d++ ) {
                 T o0, o1, o2;
-                bspline2( ( T )sRec[d * nmax + q], o0, o1, o2 );
+                dep_spline( ( T )sRec[d * nmax + q], o0, o1, o2 );
                 esir_win<T>( o0, o1, o2, ( T )sRec[( 3 + d ) * nmax + q], sh[d], W[d] );
             }
             // the list is grouped by crossing dimension, so a warp's zero nodes mostly coincide
@@ -1080,7 +1176,7 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
     const TileMap jm = tile_map<DIM>( td.JY, td.JZ );
 #pragma unroll
     for( int c = 0; c < 3; c++ ) {
-        T *dstJ = f.J[c];
+        double *dstJ = f.J[c];
         const int ny = ext( g, 1, stag( c, 1 ) ), nz = ext( g, 2, stag( c, 2 ) );
         const int nx = ext( g, 0, stag( c, 0 ) );
         const T *srcJ = sJ + c * jsz;
@@ -1091,7 +1187,7 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
                     const int e = ( cx * td.JY + jm.cy ) * td.JZ + jm.cz;
                     const T v = srcJ[e];
                     const int gx = ix0 + OS - 2 + cx;
-                    if( v != T( 0 ) && gx < nx && gy < ny && gz < nz ) atomicAdd( &dstJ[( ( int64_t )gx * ny + gy ) * nz + gz], v );
+                    if( v != T( 0 ) && gx < nx && gy < ny && gz < nz ) atomicAdd( &dstJ[( ( int64_t )gx * ny + gy ) * nz + gz], ( double )v );
                 }
             }
         } else {
@@ -1100,10 +1196,12 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
                 if( v == T( 0 ) ) continue;
                 const int cz = e % td.JZ, cy = ( e / td.JZ ) % td.JY, cx = e / ( td.JZ * td.JY );
                 const int gx = ix0 + OS - 2 + cx, gy = iy0 + OS - 2 + cy, gz = DIM == 3 ? iz0 + OS - 2 + cz : 0;
-                if( gx < nx && gy < ny && gz < nz ) atomicAdd( &dstJ[( ( int64_t )gx * ny + gy ) * nz + gz], v );
+                if( gx < nx && gy < ny && gz < nz ) atomicAdd( &dstJ[( ( int64_t )gx * ny + gy ) * nz + gz], ( double )v );
             }
         }
     }
+    if( !sp.queue ) break;
+    } // tile
 }
 
 // ------------------------------------------------------------------------------
@@ -1118,7 +1216,7 @@ template <class T>
 __global__ void k_fold( GridInfo g, int d, Fields<T> f )
 {
     const int c = blockIdx.y;
-    T *a = f.J[c];
+    double *a = f.J[c];
     const int e0 = ext( g, 0, stag( c, 0 ) ), e1 = ext( g, 1, stag( c, 1 ) ), e2 = ext( g, 2, stag( c, 2 ) );
     int se[3] = { e0, e1, e2 };
     se[d] = 1 + 2 * OS + stag( c, d );
@@ -1133,7 +1231,7 @@ __global__ void k_fold( GridInfo g, int d, Fields<T> f )
         else k2 += g.N[2];
         const int64_t a1 = ( ( int64_t )i * e1 + j ) * e2 + k;
         const int64_t a2 = ( ( int64_t )i2 * e1 + j2 ) * e2 + k2;
-        const T v = a[a2] + a[a1];
+        const double v = a[a2] + a[a1];
         a[a2] = v;
         a[a1] = v;
     }
@@ -1142,23 +1240,55 @@ __global__ void k_fold( GridInfo g, int d, Fields<T> f )
 // Ampere on every point (MA_Solver3D_norm.cpp:18-115 / MA_Solver2D_norm.cpp:18-107).
 // One block per row of the last dimension; E stays consistent between a node and
 // its periodic image because J (folded) and B (synchronised) are.
-// E[t] += d.  With a compensation array C (FP32 fields) the add is Kahan's: the
-// part of d that the FP32 sum drops is kept in C[t] and added back on the next
-// step, so the stored E carries one rounding instead of one per step.  (An FP64
-// increment lowers the residual a little more but costs 2 ms per 256^3 step: FP64
-// arithmetic is slow on this GPU.)
+
+// Error-free transforms (Knuth's two-sum, the FMA two-product): a + b = s + e and
+// a * b = p + e exactly in floating point.
 template <class T>
-__device__ __forceinline__ void add_comp( T *E, T *C, int64_t t, T d )
+__device__ __forceinline__ void two_sum( T a, T b, T &s, T &e )
 {
-    if( C ) {
-        const T y = d - C[t];
-        const T e = E[t];
-        const T s = e + y;
-        C[t] = ( s - e ) - y;
-        E[t] = s;
-    } else {
-        E[t] += d;
+    s = a + b;
+    const T bb = s - a;
+    e = ( a - ( s - bb ) ) + ( b - bb );
+}
+template <class T>
+__device__ __forceinline__ void two_prod( T a, T b, T &p, T &e )
+{
+    p = a * b;
+    e = fma( a, b, -p );
+}
+
+// Ampere increment of one E point: -dt J + ca (b1 - b0) + cb (b3 - b2) (cb = 0: one curl
+// term).  FP64 form: plain arithmetic in the reference's order.  Mixed form (C given):
+// the increment is formed exactly as a pair (hi + lo) with error-free transforms, and E
+// is kept as the pair E - C (C the compensation), so an Ampere step adds no rounding
+// of its own to E: div E follows div J and the discrete curl of B exactly (the curl
+// part cancels in the divergence whatever B is).
+template <class T>
+__device__ __forceinline__ void ampere_point( T *E, T *C, int64_t t, T dt, double Jd, T ca, T b1, T b0, T cb, T b3, T b2 )
+{
+    if( !C ) {
+        const T J = ( T )Jd;
+        E[t] += -dt * J + ca * ( b1 - b0 ) + cb * ( b3 - b2 );
+        return;
     }
+    // the FP64 current as an FP32 pair J + Jl
+    const T J = ( T )Jd, Jl = ( T )( Jd - ( double )J );
+    T d1, e1, d2, e2, p1, q1, p2, q2, p3, q3, s, es, S, eS;
+    two_sum( b1, -b0, d1, e1 );
+    two_sum( b3, -b2, d2, e2 );
+    two_prod( -dt, J, p1, q1 );
+    q1 += -dt * Jl;
+    two_prod( ca, d1, p2, q2 );
+    two_prod( cb, d2, p3, q3 );
+    two_sum( p1, p2, s, es );
+    two_sum( s, p3, S, eS );
+    const T lo = ( ( q1 + q2 ) + ( q3 + ca * e1 ) ) + ( ( cb * e2 + es ) + eS );
+    T Es, eE;
+    two_sum( E[t], S, Es, eE );
+    const T low = ( eE + lo ) - C[t];
+    const T En = Es + low;
+    C[t] = ( En - Es ) - low;
+    E[t] = En;
 }
 
 template <int DIM, class T>
@@ -1172,18 +1302,18 @@ __global__ void k_ampere_all( GridInfo g, Fields<T> f, T dt, T dtdx, T dtdy, T d
         for( int k = threadIdx.x; k < nzd; k += blockDim.x ) {
             if( j < nyp && k < nzp ) {
                 const int64_t t = ( ( int64_t )i * nyp + j ) * nzp + k;
-                add_comp( f.E[0], f.Ec[0], t, -dt * f.J[0][t] + dtdy * ( f.B[2][( ( int64_t )i * nyd + j + 1 ) * nzp + k] - f.B[2][( ( int64_t )i * nyd + j ) * nzp + k] )
-                             - dtdz * ( f.B[1][( ( int64_t )i * nyp + j ) * nzd + k + 1] - f.B[1][( ( int64_t )i * nyp + j ) * nzd + k] ) );
+                ampere_point( f.E[0], f.Ec[0], t, dt, f.J[0][t], dtdy, f.B[2][( ( int64_t )i * nyd + j + 1 ) * nzp + k], f.B[2][( ( int64_t )i * nyd + j ) * nzp + k],
+                              -dtdz, f.B[1][( ( int64_t )i * nyp + j ) * nzd + k + 1], f.B[1][( ( int64_t )i * nyp + j ) * nzd + k] );
             }
             if( i < nxp && k < nzp ) {
                 const int64_t t = ( ( int64_t )i * nyd + j ) * nzp + k;
-                add_comp( f.E[1], f.Ec[1], t, -dt * f.J[1][t] - dtdx * ( f.B[2][( ( int64_t )( i + 1 ) * nyd + j ) * nzp + k] - f.B[2][t] )
-                             + dtdz * ( f.B[0][( ( int64_t )i * nyd + j ) * nzd + k + 1] - f.B[0][( ( int64_t )i * nyd + j ) * nzd + k] ) );
+                ampere_point( f.E[1], f.Ec[1], t, dt, f.J[1][t], -dtdx, f.B[2][( ( int64_t )( i + 1 ) * nyd + j ) * nzp + k], f.B[2][t],
+                              dtdz, f.B[0][( ( int64_t )i * nyd + j ) * nzd + k + 1], f.B[0][( ( int64_t )i * nyd + j ) * nzd + k] );
             }
             if( i < nxp && j < nyp ) {
                 const int64_t t = ( ( int64_t )i * nyp + j ) * nzd + k;
-                add_comp( f.E[2], f.Ec[2], t, -dt * f.J[2][t] + dtdx * ( f.B[1][( ( int64_t )( i + 1 ) * nyp + j ) * nzd + k] - f.B[1][t] )
-                             - dtdy * ( f.B[0][( ( int64_t )i * nyd + j + 1 ) * nzd + k] - f.B[0][( ( int64_t )i * nyd + j ) * nzd + k] ) );
+                ampere_point( f.E[2], f.Ec[2], t, dt, f.J[2][t], dtdx, f.B[1][( ( int64_t )( i + 1 ) * nyp + j ) * nzd + k], f.B[1][t],
+                              -dtdy, f.B[0][( ( int64_t )i * nyd + j + 1 ) * nzd + k], f.B[0][( ( int64_t )i * nyd + j ) * nzd + k] );
             }
         }
     } else {
@@ -1191,16 +1321,16 @@ __global__ void k_ampere_all( GridInfo g, Fields<T> f, T dt, T dtdx, T dtdy, T d
         for( int j = threadIdx.x; j < nyd; j += blockDim.x ) {
             if( j < nyp ) {
                 const int64_t t = ( int64_t )i * nyp + j;
-                add_comp( f.E[0], f.Ec[0], t, -dt * f.J[0][t] + dtdy * ( f.B[2][( int64_t )i * nyd + j + 1] - f.B[2][( int64_t )i * nyd + j] ) );
+                ampere_point( f.E[0], f.Ec[0], t, dt, f.J[0][t], dtdy, f.B[2][( int64_t )i * nyd + j + 1], f.B[2][( int64_t )i * nyd + j], T( 0 ), T( 0 ), T( 0 ) );
             }
             if( i < nxp ) {
                 const int64_t t = ( int64_t )i * nyd + j;
-                add_comp( f.E[1], f.Ec[1], t, -dt * f.J[1][t] - dtdx * ( f.B[2][( int64_t )( i + 1 ) * nyd + j] - f.B[2][t] ) );
+                ampere_point( f.E[1], f.Ec[1], t, dt, f.J[1][t], -dtdx, f.B[2][( int64_t )( i + 1 ) * nyd + j], f.B[2][t], T( 0 ), T( 0 ), T( 0 ) );
             }
             if( i < nxp && j < nyp ) {
                 const int64_t t = ( int64_t )i * nyp + j;
-                add_comp( f.E[2], f.Ec[2], t, -dt * f.J[2][t] + dtdx * ( f.B[1][( int64_t )( i + 1 ) * nyp + j] - f.B[1][t] )
-                             - dtdy * ( f.B[0][( int64_t )i * nyd + j + 1] - f.B[0][( int64_t )i * nyd + j] ) );
+                ampere_point( f.E[2], f.Ec[2], t, dt, f.J[2][t], dtdx, f.B[1][( int64_t )( i + 1 ) * nyp + j], f.B[1][t],
+                              -dtdy, f.B[0][( int64_t )i * nyd + j + 1], f.B[0][( int64_t )i * nyd + j] );
             }
         }
     }
@@ -1993,6 +2123,7 @@ struct SpeciesState {
     int *ovf_tile = nullptr;
     int max_cap = 0; // largest tile segment of the current layout
     std::vector<int> h_cap;    // host copy of cap (the current layout's segment capacities)
+    int *order = nullptr;      // tiles by decreasing capacity: the persistent kernel's queue order
     bool radiates = false;     // carries an optical-depth plane (Monte-Carlo radiation)
     void *tau_mem[2] = { nullptr, nullptr };
     void *ovf_tau = nullptr;
@@ -2059,6 +2190,8 @@ struct sg_sim {
     std::vector<SpeciesState> sp;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    bool tile_queue = false;  // particle kernel as a persistent grid over a tile queue
+    int *d_queue = nullptr;   // its item counter
     int *d_flags = nullptr; // [0] status, [1 + s] spill count of species s, [1 + max_species + s] removed
     int *h_flags = nullptr; // pinned copy
     int max_species = 16;
@@ -2106,6 +2239,9 @@ struct sg_sim {
 namespace sg {
 namespace {
 
+// Bytes per element of field component c: J (9..11) is FP64 in both forms.
+inline size_t felem( const sg_sim *S, int c ) { return c >= 9 ? 8 : S->esz; }
+
 template <class T>
 Fields<T> field_view( sg_sim *S )
 {
@@ -2114,7 +2250,7 @@ Fields<T> field_view( sg_sim *S )
         f.E[c] = static_cast<T *>( S->fptr[c] );
         f.B[c] = static_cast<T *>( S->fptr[3 + c] );
         f.Bm[c] = static_cast<T *>( S->fptr[6 + c] );
-        f.J[c] = static_cast<T *>( S->fptr[9 + c] );
+        f.J[c] = static_cast<double *>( S->fptr[9 + c] );
         f.Ec[c] = static_cast<T *>( S->ecomp[c] );
     }
     return f;
@@ -2179,7 +2315,23 @@ int launch_particles( sg_sim *S, SpeciesState &s, cudaStream_t st, int t0, int t
     }
     if( smem > 48 * 1024 ) SG_CUDA_TRY( cudaFuncSetAttribute( kern, cudaFuncAttributeMaxDynamicSharedMemorySize, ( int )smem ) );
     const int sidx = ( int )( &s - &S->sp[0] );
-    kern<<<t1 - t0, 128, smem, st>>>( S->g, field_view<T>( S ), sp, bin, bout, s.seg_start, s.cap, s.count[in],
+    sp.queue = nullptr;
+    sp.order = nullptr;
+    sp.nitems = t1 - t0;
+    int grid = t1 - t0;
+    if( S->tile_queue && t0 == 0 && t1 == S->g.ntiles && s.order ) {
+        // persistent grid: as many CTAs as fit on the GPU at once, each taking tiles
+        // from the queue, densest first
+        int per_sm = 0, sms = 0, dev = 0;
+        SG_CUDA_TRY( cudaGetDevice( &dev ) );
+        SG_CUDA_TRY( cudaDeviceGetAttribute( &sms, cudaDevAttrMultiProcessorCount, dev ) );
+        SG_CUDA_TRY( cudaOccupancyMaxActiveBlocksPerMultiprocessor( &per_sm, kern, 128, smem ) );
+        grid = std::max( 1, std::min( t1 - t0, per_sm * sms ) );
+        SG_CUDA_TRY( cudaMemsetAsync( S->d_queue, 0, sizeof( int ), st ) );
+        sp.queue = S->d_queue;
+        sp.order = s.order;
+    }
+    kern<<<grid, 128, smem, st>>>( S->g, field_view<T>( S ), sp, bin, bout, s.seg_start, s.cap, s.count[in],
                                           s.count[out], bov, s.ovf_tile, S->d_flags + 1 + sidx, ( int )s.ovf_capacity,
                                           S->d_flags, chunk, S->d_flags + 1 + S->max_species + sidx );
     SG_LAUNCH_CHECK( "k_step_particles" );
@@ -2346,7 +2498,7 @@ int enqueue_step( sg_sim *S, cudaStream_t st, const StreamIn *in = nullptr )
     SG_CUDA_TRY( cudaStreamIsCapturing( st, &cs ) );
     const unsigned evflags = cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
     SG_CUDA_TRY( cudaEventRecordWithFlags( S->ev[3], st, evflags ) );
-    for( int c = 9; c < 12; c++ ) SG_CUDA_TRY( cudaMemsetAsync( S->fptr[c], 0, S->fsize[c] * S->esz, st ) );
+    for( int c = 9; c < 12; c++ ) SG_CUDA_TRY( cudaMemsetAsync( S->fptr[c], 0, S->fsize[c] * felem( S, c ), st ) );
     SG_CUDA_TRY( cudaMemsetAsync( S->d_flags, 0, ( 1 + 2 * S->max_species ) * sizeof( int ), st ) );
     for( auto &s : S->sp ) SG_CUDA_TRY( cudaMemsetAsync( s.count[1 - s.cur], 0, S->g.ntiles * sizeof( int ), st ) );
     SG_CUDA_TRY( cudaEventRecordWithFlags( S->ev[0], st, evflags ) );
@@ -2382,6 +2534,23 @@ int enqueue_step( sg_sim *S, cudaStream_t st, const StreamIn *in = nullptr )
     SG_CUDA_TRY( cudaEventRecordWithFlags( S->ev[2], st, evflags ) );
     SG_CUDA_TRY( cudaMemcpyAsync( S->h_flags, S->d_flags, ( 1 + 2 * S->max_species ) * sizeof( int ), cudaMemcpyDeviceToHost, st ) );
     S->launches_per_step = launches;
+    return SG_OK;
+}
+
+// The persistent kernel's tile order for species s: tiles by decreasing segment
+// capacity (about their particle counts), so the densest tiles start first and the
+// short ones fill the end.  Recomputed whenever the layout changes.
+int refresh_order( sg_sim *S, SpeciesState &s )
+{
+    if( !S->tile_queue ) return SG_OK;
+    const int nt = S->g.ntiles;
+    if( ( int )s.h_cap.size() != nt ) return SG_OK;
+    std::vector<int> idx( nt );
+    for( int t = 0; t < nt; t++ ) idx[t] = t;
+    std::stable_sort( idx.begin(), idx.end(), [&]( int a, int b ) { return s.h_cap[a] > s.h_cap[b]; } );
+    if( !s.order ) SG_CUDA_TRY( cudaMalloc( &s.order, nt * sizeof( int ) ) );
+    SG_CUDA_TRY( cudaMemcpyAsync( s.order, idx.data(), nt * sizeof( int ), cudaMemcpyHostToDevice, S->stream ) );
+    SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
     return SG_OK;
 }
 
@@ -2548,6 +2717,7 @@ int relayout( sg_sim *S, SpeciesState &s, int nspill )
     SG_CUDA_TRY( cudaMemcpyAsync( s.cap, S->tmp_cap, nt * sizeof( int ), cudaMemcpyDeviceToDevice, S->stream ) );
     s.max_cap = new_max_cap;
     s.h_cap.swap( new_caps );
+    if( int ro = refresh_order( S, s ) ) return ro;
     if( S->mixed ) r = place_staged<true>( S, s, nspill, s.om, s.ovf_tile, dst_buf );
     else r = place_staged<false>( S, s, nspill, s.od, s.ovf_tile, dst_buf );
     if( r ) return r;
@@ -2649,6 +2819,7 @@ int rebuild_species( sg_sim *S, SpeciesState &s, int shift, int x0, int x1 )
     const int old_chunk = launch_chunk( S, s.max_cap );
     s.max_cap = new_max_cap;
     s.h_cap.swap( new_caps );
+    if( int ro = refresh_order( S, s ) ) return ro;
     s.cur = dst;
     s.npart += ( int64_t )wc[1] - ( int64_t )wc[0];
     if( realloc ) {
@@ -2689,13 +2860,14 @@ int window_shift( sg_sim *S )
         const int64_t keep = ( int64_t )g.N[0] - P + OS + stag[a];
         const int64_t n = S->fsize[c];
         const unsigned blocks = ( unsigned )std::min<int64_t>( ( n + 255 ) / 256, 152 * 16 );
-        if( S->mixed ) {
+        const size_t el = a < 12 ? felem( S, c ) : S->esz;
+        if( el == 4 ) {
             k_window_shift_field<float><<<blocks, 256, 0, st>>>( static_cast<const float *>( arrays[a] ), static_cast<float *>( S->win_scratch ), ex, plane, keep, P );
         } else {
             k_window_shift_field<double><<<blocks, 256, 0, st>>>( static_cast<const double *>( arrays[a] ), static_cast<double *>( S->win_scratch ), ex, plane, keep, P );
         }
         SG_LAUNCH_CHECK( "k_window_shift_field" );
-        SG_CUDA_TRY( cudaMemcpyAsync( arrays[a], S->win_scratch, n * S->esz, cudaMemcpyDeviceToDevice, st ) );
+        SG_CUDA_TRY( cudaMemcpyAsync( arrays[a], S->win_scratch, n * el, cudaMemcpyDeviceToDevice, st ) );
     }
     const bool lasers_were_on = S->obc.nlaser > 0;
     S->obc.nlaser = 0;
@@ -2804,7 +2976,7 @@ int sg_sim_create( const sg_sim_config *cfg, sg_sim **out )
             n *= S->fshape[c][d];
         }
         S->fsize[c] = n;
-        total += ( ( n * S->esz + 255 ) / 256 ) * 256;
+        total += ( ( n * felem( S, c ) + 255 ) / 256 ) * 256;
     }
     if( S->mixed )
         for( int c = 0; c < 3; c++ ) total += ( ( S->fsize[c] * S->esz + 255 ) / 256 ) * 256;
@@ -2814,7 +2986,7 @@ int sg_sim_create( const sg_sim_config *cfg, sg_sim **out )
     char *p = static_cast<char *>( S->fmem );
     for( int c = 0; c < 12; c++ ) {
         S->fptr[c] = p;
-        p += ( ( S->fsize[c] * S->esz + 255 ) / 256 ) * 256;
+        p += ( ( S->fsize[c] * felem( S, c ) + 255 ) / 256 ) * 256;
     }
     if( S->mixed )
         for( int c = 0; c < 3; c++ ) {
@@ -2852,6 +3024,7 @@ int sg_sim_destroy( sg_sim *S )
         release( s.mem[1] );
         release( s.seg_start );
         release( s.cap );
+        release( s.order );
         release( s.count[0] );
         release( s.count[1] );
         release( s.ovf_mem );
@@ -2864,6 +3037,7 @@ int sg_sim_destroy( sg_sim *S )
     release( S->d_rad_step );
     release( S->fmem );
     release( S->d_flags );
+    release( S->d_queue );
     release( S->d_step );
     if( S->h_flags ) cudaFreeHost( S->h_flags );
     release( S->scan_scratch );
@@ -2891,6 +3065,20 @@ int sg_sim_destroy( sg_sim *S )
     return SG_OK;
 }
 
+int sg_sim_set_tile_queue( sg_sim *S, int on )
+{
+    SG_REQUIRE( S, "NULL simulation" );
+    SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
+    S->tile_queue = on != 0;
+    if( S->tile_queue && !S->d_queue ) SG_CUDA_TRY( cudaMalloc( &S->d_queue, sizeof( int ) ) );
+    for( auto &s : S->sp ) {
+        int r = refresh_order( S, s );
+        if( r ) return r;
+    }
+    drop_graphs( S );
+    return SG_OK;
+}
+
 int sg_sim_set_stream( sg_sim *S, sg_stream_t stream )
 {
     SG_REQUIRE( S, "NULL simulation" );
@@ -2911,6 +3099,9 @@ int sg_sim_add_species_device( sg_sim *S, double mass, double charge, int pusher
     SG_REQUIRE( npart >= 0 && npart < ( int64_t )1 << 31, "npart out of range" );
     SG_REQUIRE( ( int )S->sp.size() < S->max_species, "too many species" );
     if( npart > 0 ) SG_REQUIRE( pos && mom && weight, "NULL particle array" );
+    // the arrays may still be being written on another stream (the simulation's own
+    // stream does not wait for the legacy default stream): let all device work end first
+    SG_CUDA_TRY( cudaDeviceSynchronize() );
     const int nt = S->g.ntiles, nd = S->g.ndim;
     S->sp.emplace_back();
     SpeciesState &s = S->sp.back();
@@ -2944,6 +3135,8 @@ int sg_sim_add_species_device( sg_sim *S, double mass, double charge, int pusher
     }
     int64_t total = 0;
     int r = layout_from_counts( S, s.count[1], s.cap, s.seg_start, &total, &s.max_cap, s.h_cap );
+    if( r ) return r;
+    r = refresh_order( S, s );
     if( r ) return r;
     r = alloc_species_buffers( S, s, std::max<int64_t>( total, 1 ) );
     if( r ) return r;
@@ -3013,7 +3206,7 @@ int sg_sim_set_field( sg_sim *S, int comp, const double *host )
     SG_REQUIRE( comp >= 0 && comp < 12, "component out of range" );
     const int64_t n = S->fsize[comp];
     SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
-    if( !S->mixed ) {
+    if( !S->mixed || felem( S, comp ) == 8 ) {
         SG_CUDA_TRY( cudaMemcpy( S->fptr[comp], host, n * 8, cudaMemcpyHostToDevice ) );
     } else {
         double *d = nullptr;
@@ -3034,7 +3227,7 @@ int sg_sim_get_field( sg_sim *S, int comp, double *host )
     SG_REQUIRE( comp >= 0 && comp < 12, "component out of range" );
     const int64_t n = S->fsize[comp];
     SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
-    if( !S->mixed ) {
+    if( !S->mixed || felem( S, comp ) == 8 ) {
         SG_CUDA_TRY( cudaMemcpy( host, S->fptr[comp], n * 8, cudaMemcpyDeviceToHost ) );
     } else {
         double *d = nullptr;
@@ -3132,7 +3325,7 @@ int sg_sim_set_moving_window( sg_sim *S, double time_start, double velocity_x, i
     if( !S->win_scratch ) {
         int64_t mx = 0;
         for( int c = 0; c < 12; c++ ) mx = std::max( mx, S->fsize[c] );
-        SG_CUDA_TRY( cudaMalloc( &S->win_scratch, ( size_t )mx * S->esz ) );
+        SG_CUDA_TRY( cudaMalloc( &S->win_scratch, ( size_t )mx * 8 ) );
     }
     S->win_on = true;
     S->win_t_start = time_start;
@@ -4003,9 +4196,12 @@ __global__ void k_efield_store( GridInfo g, const double *__restrict__ E, int64_
 // (as unsigned-long-long bit patterns of non-negative doubles, so atomicMax orders them).
 template <class T>
 __global__ void k_residual( GridInfo g, const T *__restrict__ Ex, const T *__restrict__ Ey, const T *__restrict__ Ez,
+                            const T *__restrict__ Cx, const T *__restrict__ Cy, const T *__restrict__ Cz,
                             const double *__restrict__ rho_g, const double *__restrict__ sums, int64_t n,
                             unsigned long long *__restrict__ out )
 {
+    // the mixed form's E is the pair E - C (C: compensation of the Ampere updates)
+    auto ev = []( const T *E, const T *C, int64_t i ) { return C ? ( double )E[i] - ( double )C[i] : ( double )E[i]; };
     const double mean = sums[0] / ( double )n;
     const int nyp = ext( g, 1, 0 ), nzp = ext( g, 2, 0 );
     double m0 = 0.0, m1 = 0.0;
@@ -4014,10 +4210,10 @@ __global__ void k_residual( GridInfo g, const T *__restrict__ Ex, const T *__res
         phys_ijk( g, t, i, j, k );
         const int a = i + OS, b = j + OS, c = g.ndim == 3 ? k + OS : 0;
         // primal node (a,b,c): Ex dual in x at a and a+1, etc.
-        double div = ( ( double )Ex[( ( int64_t )( a + 1 ) * nyp + b ) * nzp + c] - ( double )Ex[( ( int64_t )a * nyp + b ) * nzp + c] ) * g.dxi[0]
-                     + ( ( double )Ey[( ( int64_t )a * ( nyp + 1 ) + b + 1 ) * nzp + c] - ( double )Ey[( ( int64_t )a * ( nyp + 1 ) + b ) * nzp + c] ) * g.dxi[1];
+        double div = ( ev( Ex, Cx, ( ( int64_t )( a + 1 ) * nyp + b ) * nzp + c ) - ev( Ex, Cx, ( ( int64_t )a * nyp + b ) * nzp + c ) ) * g.dxi[0]
+                     + ( ev( Ey, Cy, ( ( int64_t )a * ( nyp + 1 ) + b + 1 ) * nzp + c ) - ev( Ey, Cy, ( ( int64_t )a * ( nyp + 1 ) + b ) * nzp + c ) ) * g.dxi[1];
         if( g.ndim == 3 )
-            div += ( ( double )Ez[( ( int64_t )a * nyp + b ) * ( nzp + 1 ) + c + 1] - ( double )Ez[( ( int64_t )a * nyp + b ) * ( nzp + 1 ) + c] ) * g.dxi[2];
+            div += ( ev( Ez, Cz, ( ( int64_t )a * nyp + b ) * ( nzp + 1 ) + c + 1 ) - ev( Ez, Cz, ( ( int64_t )a * nyp + b ) * ( nzp + 1 ) + c ) ) * g.dxi[2];
         const double rv = rho_g[( ( int64_t )a * nyp + b ) * nzp + c] - mean;
         m0 = fmax( m0, fabs( div - rv ) );
         m1 = fmax( m1, fabs( rv ) );
@@ -4171,9 +4367,11 @@ int sg_sim_charge_residual( sg_sim *S, double *residual, double *rho_max )
         if( ( rc = deposit_rho( S, rho ) ) ) break;
         k_rho_sum<<<1024, 256, 0, st>>>( g, rho, n, s );
         if( S->mixed )
-            k_residual<float><<<1024, 256, 0, st>>>( g, static_cast<float *>( S->fptr[0] ), static_cast<float *>( S->fptr[1] ), static_cast<float *>( S->fptr[2] ), rho, s, n, mx );
+            k_residual<float><<<1024, 256, 0, st>>>( g, static_cast<float *>( S->fptr[0] ), static_cast<float *>( S->fptr[1] ), static_cast<float *>( S->fptr[2] ),
+                                                      static_cast<float *>( S->ecomp[0] ), static_cast<float *>( S->ecomp[1] ), static_cast<float *>( S->ecomp[2] ), rho, s, n, mx );
         else
-            k_residual<double><<<1024, 256, 0, st>>>( g, static_cast<double *>( S->fptr[0] ), static_cast<double *>( S->fptr[1] ), static_cast<double *>( S->fptr[2] ), rho, s, n, mx );
+            k_residual<double><<<1024, 256, 0, st>>>( g, static_cast<double *>( S->fptr[0] ), static_cast<double *>( S->fptr[1] ), static_cast<double *>( S->fptr[2] ),
+                                                       nullptr, nullptr, nullptr, rho, s, n, mx );
         if( cudaGetLastError() != cudaSuccess ) { rc = set_error( SG_ERR_CUDA, "residual launch failed" ); break; }
     } while( 0 );
     unsigned long long h[2] = { 0, 0 };

@@ -62,6 +62,11 @@ class Simulation:
     def __exit__(self, *a):
         self.close()
 
+    def set_tile_queue(self, on: bool = True):
+        """Particle kernel as a persistent grid taking tiles from a queue, densest first
+        (on), or one CTA per tile (off, the default)."""
+        check(_lib.lib().sg_sim_set_tile_queue(self._h, int(bool(on))), "set_tile_queue")
+
     # -- species -----------------------------------------------------------
     def add_species(self, mass, charge, pusher, position, momentum, weight, name=None):
         """position[ndim, n], momentum[3, n], weight[n] as float64 numpy arrays (host) or CUDA tensors."""

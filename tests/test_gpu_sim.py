@@ -38,7 +38,7 @@ def make_case(synthetic, ndim, seed, species_spec):
     return n_cells, cl, dt, fields, species
 
 
-def run_pair(sim_mod, cpu_oracle, ndim, form, nsteps, species_spec, seed=5, tile=None):
+def run_pair(sim_mod, cpu_oracle, ndim, form, nsteps, species_spec, seed=5, tile=None, tile_queue=False):
     simulation, synthetic = sim_mod
     n_cells, cl, dt, fields, species = make_case(synthetic, ndim, seed, species_spec)
     sim = simulation.Simulation(n_cells, cl, dt, form=form, tile=tile, use_graph=True)
@@ -46,6 +46,8 @@ def run_pair(sim_mod, cpu_oracle, ndim, form, nsteps, species_spec, seed=5, tile
         sim.set_field(k, fields[k])
     for s in species:
         sim.add_species(s["mass"], s["q"], s["pusher"], s["pos"], s["mom"], s["weight"])
+    if tile_queue:
+        sim.set_tile_queue(True)
     sim.step(nsteps)
     ref = {k: v.copy() for k, v in fields.items()}
     ref_sp = [dict(s, pos=s["pos"].copy(), mom=s["mom"].copy()) for s in species]
@@ -277,3 +279,17 @@ def test_packed_state_round_trip(sim_mod, form):
     assert np.array_equal(w1[o1], w3[o3])
     assert np.array_equal(p1[:, o1], p3[:, o3]) and np.array_equal(m1[:, o1], m3[:, o3])
     sim.close()
+
+
+@pytest.mark.parametrize("ndim,form,tol", [(3, "mixed", 1e-5), (3, "fp64", 1e-12), (2, "mixed", 1e-5)])
+def test_tile_queue_step_matches_oracle(sim_mod, cpu_oracle, ndim, form, tol):
+    """The persistent particle kernel (CTAs take tiles from a device queue, densest first)
+    gives the oracle's step like the one-CTA-per-tile launch, over 3 steps (the third
+    and later steps replay the captured graph, with the queue counter reset inside it)."""
+    spec = [(1.0, -1.0, "higueracary" if ndim == 3 else "vay", 6, 0.14)]
+    got, ref, parts = run_pair(sim_mod, cpu_oracle, ndim, form, 3, spec, tile_queue=True)
+    for k in FIELDS:
+        assert rel_err(got[k], ref[k]) <= tol * 10, k
+    for pg, mg, pr, mr, cl, n_cells in parts:
+        assert rel_err(mg, mr) <= tol * 10
+        assert position_error(pg, pr, cl, n_cells) <= tol * 10
