@@ -441,9 +441,15 @@ int sg_mlp_train( sg_mlp *mlp, const sg_rad_tables *tables, int steps, int batch
  * above tol.  err_out[n_chi_bins * n_xi_bins] optional. */
 int sg_mlp_validate( sg_mlp *mlp, const sg_rad_tables *tables, int n_chi_bins, int n_xi_bins, int per_bin,
                      float tol, float *err_out, int *n_masked );
-/* Network inverse CDF alone (no fallback), device arrays. */
+/* Network inverse CDF alone (no fallback), device arrays.  A 64-wide network runs its
+ * 64 x 64 layer on the tensor cores (mma.sync, FP16 operands, FP32 accumulation); other
+ * widths, and sg_mlp_photon_chi_fp32 for every width, run on the FP32 cores.  No
+ * reference counterpart: the reference has the table only
+ * (RadiationTables::computeRandomPhotonChiWithInterpolation, RadiationTables.cpp:375). */
 int sg_mlp_photon_chi( const sg_mlp *mlp, int64_t n, const double *chi, const double *xi, double *out,
                        sg_stream_t stream );
+int sg_mlp_photon_chi_fp32( const sg_mlp *mlp, int64_t n, const double *chi, const double *xi, double *out,
+                            sg_stream_t stream );
 
 #ifdef __cplusplus
 }

@@ -3,7 +3,7 @@
 The compute path is libsmileigb300.so (hand-written CUDA behind the C ABI in
 include/smilei_gb300.h).  ``operators`` mirrors the reference's operator
 classes on one patch's arrays; ``simulation`` runs whole resident timesteps;
-``namelist`` reads Smilei-style namelists.
+``namelist`` executes Smilei namelists against them.
 """
 from ._lib import SmileiGPUError, lib, last_error  # noqa: F401
 

@@ -117,6 +117,7 @@ _SIGNATURES = {
     "sg_mlp_train": (_I, [_VP, _VP, _I, _I, ctypes.c_float, ctypes.c_uint32, _VP, _VP]),
     "sg_mlp_validate": (_I, [_VP, _VP, _I, _I, _I, ctypes.c_float, _VP, ctypes.POINTER(_I)]),
     "sg_mlp_photon_chi": (_I, [_VP, _I64, _VP, _VP, _VP, _VP]),
+    "sg_mlp_photon_chi_fp32": (_I, [_VP, _I64, _VP, _VP, _VP, _VP]),
     "sg_sim_solve_poisson": (_I, [_VP, _D, _I, ctypes.POINTER(_I), ctypes.POINTER(_D)]),
     "sg_sim_charge_residual": (_I, [_VP, ctypes.POINTER(_D), ctypes.POINTER(_D)]),
     "sg_sim_copy_state": (_I, [_VP, _I, _VP, _I]),

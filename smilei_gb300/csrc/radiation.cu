@@ -25,6 +25,8 @@
 #include "common.cuh"
 #include "resident_rad.cuh"
 
+#include <cuda_fp16.h>
+
 #include <cmath>
 #include <vector>
 
@@ -343,6 +345,144 @@ __global__ void __launch_bounds__( 256 ) k_mlp_photon_chi_fast( MlpView m, int64
     }
 }
 
+// Batched inference of the 64-wide network on the tensor cores (mma.sync
+// m16n8k16, FP16 operands, FP32 accumulation): a warp takes 32 samples at a time
+// (two 16-row tiles).  Layer 1 (2 -> 64) and both activations run on the FP32 cores,
+// each lane computing exactly the hidden values its operand fragments hold; layer 2
+// (64 x 64, 96 % of the network's arithmetic) is 64 mma instructions per 32 samples;
+// layer 3 is a sum over the accumulator fragments and two shuffles.  FP16 rounding of
+// the hidden values and of W2 (relative 2^-11) is far below the network's own error
+// against the table; the test bounds the difference to the FP32 network.
+constexpr int TC_H = 64;
+constexpr int TC_W2_STRIDE = TC_H + 8; // halves per row of W2 in shared memory: no bank conflicts
+
+__device__ __forceinline__ uint32_t pack_half2( float lo, float hi )
+{
+    const __half2 h = __floats2half2_rn( lo, hi );
+    return *reinterpret_cast<const uint32_t *>( &h );
+}
+
+// The 64-wide network on one warp for up to 32 rows (two 16-row tiles; mtiles = 1 uses
+// only the first): ru0/ru1 hold the inputs of rows 16 mt + gid + 8 hf, the rows this
+// lane's fragments hold (gid = lane / 4, tig = lane % 4).  Returns in y[mt][hf] the
+// output before b3 of those rows, complete in all four lanes of the group.  W2h: FP16
+// W2 (row = output unit) with rows TC_W2_STRIDE halves apart.
+__device__ __forceinline__ void tc_network( const __half *__restrict__ W2h, const float *__restrict__ W1,
+                                            const float *__restrict__ b1, const float *__restrict__ b2,
+                                            const float *__restrict__ W3, const float ( &ru0 )[2][2],
+                                            const float ( &ru1 )[2][2], int mtiles, float ( &y )[2][2] )
+{
+    const int lane = threadIdx.x & 31, gid = lane >> 2, tig = lane & 3;
+    float acc[2][8][4];
+#pragma unroll
+    for( int mt = 0; mt < 2; mt++ )
+#pragma unroll
+        for( int nt = 0; nt < 8; nt++ )
+#pragma unroll
+            for( int e = 0; e < 4; e++ ) acc[mt][nt][e] = 0.0f;
+#pragma unroll
+    for( int ks = 0; ks < 4; ks++ ) {
+        // layer 1 for the columns k = 16 ks + 2 tig + {0, 1} (+ 8) of this lane's rows
+        uint32_t a[2][4];
+#pragma unroll
+        for( int mt = 0; mt < 2; mt++ )
+#pragma unroll
+            for( int r = 0; r < 4; r++ ) { // r: (hf, kh) = (r & 1, r >> 1), the PTX order a0..a3
+                const int hf = r & 1, k0 = 16 * ks + 2 * tig + 8 * ( r >> 1 );
+                const float v0 = tanh_fast( fmaf( W1[2 * k0], ru0[mt][hf], fmaf( W1[2 * k0 + 1], ru1[mt][hf], b1[k0] ) ) );
+                const float v1 = tanh_fast( fmaf( W1[2 * k0 + 2], ru0[mt][hf], fmaf( W1[2 * k0 + 3], ru1[mt][hf], b1[k0 + 1] ) ) );
+                a[mt][r] = pack_half2( v0, v1 );
+            }
+#pragma unroll
+        for( int nt = 0; nt < 8; nt++ ) {
+            const __half *wrow = W2h + ( 8 * nt + gid ) * TC_W2_STRIDE + 16 * ks + 2 * tig;
+            const uint32_t b0 = *reinterpret_cast<const uint32_t *>( wrow );
+            const uint32_t bb = *reinterpret_cast<const uint32_t *>( wrow + 8 );
+#pragma unroll
+            for( int mt = 0; mt < 2; mt++ )
+                if( mt < mtiles )
+                    asm volatile( "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+                                  "{%8,%9}, {%0,%1,%2,%3};\n"
+                                  : "+f"( acc[mt][nt][0] ), "+f"( acc[mt][nt][1] ), "+f"( acc[mt][nt][2] ),
+                                    "+f"( acc[mt][nt][3] )
+                                  : "r"( a[mt][0] ), "r"( a[mt][1] ), "r"( a[mt][2] ), "r"( a[mt][3] ), "r"( b0 ),
+                                    "r"( bb ) );
+        }
+    }
+    // layer 2 activation and layer 3: rows gid (+ 8) of each tile, columns 8 nt + 2 tig + {0, 1}
+#pragma unroll
+    for( int mt = 0; mt < 2; mt++ ) {
+        y[mt][0] = y[mt][1] = 0.0f;
+#pragma unroll
+        for( int nt = 0; nt < 8; nt++ )
+#pragma unroll
+            for( int e = 0; e < 4; e++ ) {
+                const int col = 8 * nt + 2 * tig + ( e & 1 );
+                y[mt][e >> 1] = fmaf( W3[col], tanh_fast( acc[mt][nt][e] + b2[col] ), y[mt][e >> 1] );
+            }
+    }
+#pragma unroll
+    for( int mt = 0; mt < 2; mt++ )
+#pragma unroll
+        for( int hf = 0; hf < 2; hf++ ) {
+            y[mt][hf] += __shfl_xor_sync( 0xffffffffu, y[mt][hf], 1 );
+            y[mt][hf] += __shfl_xor_sync( 0xffffffffu, y[mt][hf], 2 );
+        }
+}
+
+// Row k's output (k < 32) from the group that holds it: lanes 4 (k % 8) .. + 3.
+__device__ __forceinline__ float tc_row( const float ( &y )[2][2], int k )
+{
+    const int src = 4 * ( k & 7 );
+    const float y00 = __shfl_sync( 0xffffffffu, y[0][0], src ), y01 = __shfl_sync( 0xffffffffu, y[0][1], src );
+    const float y10 = __shfl_sync( 0xffffffffu, y[1][0], src ), y11 = __shfl_sync( 0xffffffffu, y[1][1], src );
+    return ( k >> 4 ) ? ( ( k >> 3 ) & 1 ? y11 : y10 ) : ( ( k >> 3 ) & 1 ? y01 : y00 );
+}
+
+__global__ void __launch_bounds__( 128 ) k_mlp_photon_chi_tc( MlpView m, int64_t n, const double *__restrict__ chi,
+                                                              const double *__restrict__ xi, double *__restrict__ out )
+{
+    __shared__ __align__( 16 ) __half sW2[TC_H * TC_W2_STRIDE];
+    __shared__ float sW1[2 * TC_H], sb1[TC_H], sb2[TC_H], sW3[TC_H];
+    for( int k = threadIdx.x; k < TC_H * TC_H; k += blockDim.x )
+        sW2[( k / TC_H ) * TC_W2_STRIDE + ( k % TC_H )] = __float2half_rn( m.W2[k] );
+    for( int k = threadIdx.x; k < TC_H; k += blockDim.x ) {
+        sW1[2 * k] = m.W1[2 * k];
+        sW1[2 * k + 1] = m.W1[2 * k + 1];
+        sb1[k] = m.b1[k];
+        sb2[k] = m.b2[k];
+        sW3[k] = m.W3[k];
+    }
+    __syncthreads();
+    const float b3 = m.b3[0];
+    const int lane = threadIdx.x & 31, gid = lane >> 2, tig = lane & 3;
+    const int64_t warps = ( int64_t )gridDim.x * ( blockDim.x >> 5 );
+    for( int64_t base = ( ( int64_t )blockIdx.x * ( blockDim.x >> 5 ) + ( threadIdx.x >> 5 ) ) * 32; base < n;
+         base += warps * 32 ) {
+        // this lane's own sample (row `lane` of the 32)
+        const int64_t i = base + lane;
+        float c = 1.0f, u0 = 0.0f, u1 = 0.0f;
+        if( i < n ) {
+            c = ( float )chi[i];
+            u0 = 2.0f * ( log10f( c ) - m.lmin ) / m.lspan - 1.0f;
+            u1 = 2.0f * ( float )xi[i] - 1.0f;
+        }
+        // inputs of the four rows this lane's fragments hold: 16 mt + gid + 8 hf
+        float ru0[2][2], ru1[2][2];
+#pragma unroll
+        for( int mt = 0; mt < 2; mt++ )
+#pragma unroll
+            for( int hf = 0; hf < 2; hf++ ) {
+                ru0[mt][hf] = __shfl_sync( 0xffffffffu, u0, 16 * mt + gid + 8 * hf );
+                ru1[mt][hf] = __shfl_sync( 0xffffffffu, u1, 16 * mt + gid + 8 * hf );
+            }
+        float y[2][2];
+        tc_network( sW2, sW1, sb1, sb2, sW3, ru0, ru1, 2, y );
+        const float yl = tc_row( y, lane );
+        if( i < n ) out[i] = chi[i] * ( double )exp10f( ( yl + b3 ) * m.out_scale );
+    }
+}
+
 // Macro-photon output (RadiationMonteCarlo.cpp:425-545): an emission with
 // photon_gamma >= threshold, while the particle has made fewer than max_emissions
 // photons in this pass, appends `sampling` photons (slots from one atomicAdd on
@@ -366,16 +506,27 @@ struct MlpShared {
     float W1[2 * H], b1[H], b2[H], W3[H], b3;
     float4 W2v[H * H / 4]; // row r, columns 4c..4c+3 at r * H / 4 + c
 };
+// The 64-wide network is evaluated on the tensor cores (tc_network): W2 in FP16.
+template <>
+struct MlpShared<TC_H> {
+    float W1[2 * TC_H], b1[TC_H], b2[TC_H], W3[TC_H], b3;
+    __align__( 16 ) __half W2h[TC_H * TC_W2_STRIDE];
+};
 
 // TRANSPOSED: W2 stored column-major (W2T[i * H + r] = W2[r][i]) for the
 // warp-cooperative evaluation, where lane r reads row r of consecutive columns.
 template <int H, bool TRANSPOSED = false>
 __device__ __forceinline__ void mlp_stage( const MlpView &m, MlpShared<H> &w )
 {
-    float *W2 = reinterpret_cast<float *>( w.W2v );
-    for( int k = threadIdx.x; k < H * H; k += blockDim.x ) {
-        if constexpr( TRANSPOSED ) W2[( k % H ) * H + k / H] = m.W2[k];
-        else W2[k] = m.W2[k];
+    if constexpr( H == TC_H ) {
+        for( int k = threadIdx.x; k < H * H; k += blockDim.x )
+            w.W2h[( k / H ) * TC_W2_STRIDE + ( k % H )] = __float2half_rn( m.W2[k] );
+    } else {
+        float *W2 = reinterpret_cast<float *>( w.W2v );
+        for( int k = threadIdx.x; k < H * H; k += blockDim.x ) {
+            if constexpr( TRANSPOSED ) W2[( k % H ) * H + k / H] = m.W2[k];
+            else W2[k] = m.W2[k];
+        }
     }
     for( int k = threadIdx.x; k < H; k += blockDim.x ) {
         w.W1[2 * k] = m.W1[2 * k];
@@ -391,26 +542,31 @@ __device__ __forceinline__ void mlp_stage( const MlpView &m, MlpShared<H> &w )
 template <int H>
 __device__ __forceinline__ double mlp_photon_chi_smem( const MlpView &m, const MlpShared<H> &w, double chi, double xi )
 {
-    const float u0 = 2.0f * ( log10f( ( float )chi ) - m.lmin ) / m.lspan - 1.0f;
-    const float u1 = 2.0f * ( float )xi - 1.0f;
-    float h1[H];
+    // one sample per thread: the 64-wide network reads its FP32 weights from global memory
+    if constexpr( H == TC_H ) {
+        return mlp_photon_chi( m, chi, xi );
+    } else {
+        const float u0 = 2.0f * ( log10f( ( float )chi ) - m.lmin ) / m.lspan - 1.0f;
+        const float u1 = 2.0f * ( float )xi - 1.0f;
+        float h1[H];
 #pragma unroll
-    for( int k = 0; k < H; k++ ) h1[k] = tanh_fast( fmaf( w.W1[2 * k], u0, fmaf( w.W1[2 * k + 1], u1, w.b1[k] ) ) );
-    float y = w.b3;
+        for( int k = 0; k < H; k++ ) h1[k] = tanh_fast( fmaf( w.W1[2 * k], u0, fmaf( w.W1[2 * k + 1], u1, w.b1[k] ) ) );
+        float y = w.b3;
 #pragma unroll( H >= 64 ? 1 : 2 )
-    for( int r = 0; r < H; r++ ) {
-        float a = w.b2[r];
+        for( int r = 0; r < H; r++ ) {
+            float a = w.b2[r];
 #pragma unroll
-        for( int c = 0; c < H / 4; c++ ) {
-            const float4 wv = w.W2v[r * ( H / 4 ) + c];
-            a = fmaf( wv.x, h1[4 * c], a );
-            a = fmaf( wv.y, h1[4 * c + 1], a );
-            a = fmaf( wv.z, h1[4 * c + 2], a );
-            a = fmaf( wv.w, h1[4 * c + 3], a );
+            for( int c = 0; c < H / 4; c++ ) {
+                const float4 wv = w.W2v[r * ( H / 4 ) + c];
+                a = fmaf( wv.x, h1[4 * c], a );
+                a = fmaf( wv.y, h1[4 * c + 1], a );
+                a = fmaf( wv.z, h1[4 * c + 2], a );
+                a = fmaf( wv.w, h1[4 * c + 3], a );
+            }
+            y = fmaf( w.W3[r], tanh_fast( a ), y );
         }
-        y = fmaf( w.W3[r], tanh_fast( a ), y );
+        return chi * ( double )exp10f( y * m.out_scale );
     }
-    return chi * ( double )exp10f( y * m.out_scale );
 }
 
 // The network evaluated by a whole warp for one (chi, xi) (every lane passes the
@@ -532,7 +688,35 @@ __device__ __forceinline__ void mc_pass_f32( const RadTab &t, const MlpView &m, 
                 }
             }
         }
-        if constexpr( H > 0 ) {
+        if constexpr( H == TC_H ) {
+            // the emitting lanes' network evaluations as one batch on the tensor cores:
+            // row k is the lane with the k-th lowest index among them
+            const unsigned req = __ballot_sync( 0xffffffffu, net );
+            if( req ) {
+                const int nreq = __popc( req );
+                float u0 = 0.0f, u1 = 0.0f;
+                if( net ) {
+                    u0 = 2.0f * ( log10f( chi ) - m.lmin ) / m.lspan - 1.0f;
+                    u1 = 2.0f * u32 - 1.0f;
+                }
+                const int gid = lane >> 2;
+                float ru0[2][2], ru1[2][2];
+#pragma unroll
+                for( int mt = 0; mt < 2; mt++ )
+#pragma unroll
+                    for( int hf = 0; hf < 2; hf++ ) {
+                        const int row = 16 * mt + gid + 8 * hf;
+                        const int src = row < nreq ? ( int )__fns( req, 0, row + 1 ) : lane;
+                        const float a0 = __shfl_sync( 0xffffffffu, u0, src ), a1 = __shfl_sync( 0xffffffffu, u1, src );
+                        ru0[mt][hf] = row < nreq ? a0 : 0.0f;
+                        ru1[mt][hf] = row < nreq ? a1 : 0.0f;
+                    }
+                float yv[2][2];
+                tc_network( sw.W2h, sw.W1, sw.b1, sw.b2, sw.W3, ru0, ru1, nreq > 16 ? 2 : 1, yv );
+                const float y = tc_row( yv, __popc( req & ( ( 1u << lane ) - 1u ) ) );
+                if( net ) pchi = ( double )chi * ( double )exp10f( ( y + sw.b3 ) * m.out_scale );
+            }
+        } else if constexpr( H > 0 ) {
             // the emitting lanes' network evaluations, by the whole warp
             unsigned req = __ballot_sync( 0xffffffffu, net );
             while( req ) {
@@ -1364,6 +1548,19 @@ int sg_mlp_validate( sg_mlp *m, const sg_rad_tables *T, int n_chi_bins, int n_xi
 }
 
 int sg_mlp_photon_chi( const sg_mlp *m, int64_t n, const double *chi, const double *xi, double *out, sg_stream_t stream )
+{
+    SG_REQUIRE( m && chi && xi && out, "NULL argument" );
+    if( n <= 0 ) return SG_OK;
+    if( m->H != TC_H ) return sg_mlp_photon_chi_fp32( m, n, chi, xi, out, stream );
+    const int64_t tiles = ( n + 31 ) / 32;
+    const unsigned blocks = ( unsigned )std::min<int64_t>( ( tiles + 3 ) / 4, 152 * 8 );
+    k_mlp_photon_chi_tc<<<blocks, 128, 0, as_stream( stream )>>>( view( m ), n, chi, xi, out );
+    SG_LAUNCH_CHECK( "k_mlp_photon_chi_tc" );
+    return SG_OK;
+}
+
+int sg_mlp_photon_chi_fp32( const sg_mlp *m, int64_t n, const double *chi, const double *xi, double *out,
+                            sg_stream_t stream )
 {
     SG_REQUIRE( m && chi && xi && out, "NULL argument" );
     if( n <= 0 ) return SG_OK;

@@ -500,15 +500,19 @@ constexpr int ft_tile( int dim, int ft, int d )
 }
 constexpr int ft_shift( int t ) { return t == 16 ? 4 : ( t == 8 ? 3 : ( t == 4 ? 2 : 0 ) ); }
 
-// The chunk of such a shape: FP32 tiles of 6 field and 3 current components with
-// T + 3 and T + 4 points per dimension.
+// The chunk of such a shape: FP32 tiles of 6 field and 3 + 3 current components (the
+// per-cell sums' tile and the node-changing particles' tile) with T + 3 and T + 4
+// points per dimension.
 constexpr int fixt_chunk( int dim, int ft )
 {
-    return dim == 3 ? cells_chunk_fit( ( size_t )( 6 * 7 * 7 * 7 + 3 * 8 * 8 * 8 ) * 4, 64 ) & ~31
+    return dim == 3 ? cells_chunk_fit( ( size_t )( 6 * 7 * 7 * 7 + 6 * 8 * 8 * 8 ) * 4, 64 ) & ~31
                     : cells_chunk_fit( ( size_t )( 6 * ( ft_tile( 2, ft, 0 ) + 3 ) * ( ft_tile( 2, ft, 1 ) + 3 ) +
-                                                   3 * ( ft_tile( 2, ft, 0 ) + 4 ) * ( ft_tile( 2, ft, 1 ) + 4 ) ) * 4,
+                                                   6 * ( ft_tile( 2, ft, 0 ) + 4 ) * ( ft_tile( 2, ft, 1 ) + 4 ) ) * 4,
                                        ft_tile( 2, ft, 0 ) * ft_tile( 2, ft, 1 ) ) & ~31;
 }
+
+// The per-cell mode's second current tile (node-changing particles), FP32.
+inline size_t cells_j2_bytes( const TileDims &td ) { return ( size_t )3 * td.JX * td.JY * td.JZ * 4; }
 
 // FT > 0: the tile shape is known at compile time, so tile and stencil offsets fold into
 // immediates; the chunk is fixt_chunk.
@@ -538,7 +542,12 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
     // per-cell mode (CELLS): particle planes, per-cell counts and starts, each
     // particle's (cell << 16 | rank in cell), each slot's cell
     const int TC = g.T[0] * g.T[1] * ( DIM == 3 ? g.T[2] : 1 );
-    float *sRec = reinterpret_cast<float *>( sJ + 3 * jsz );
+    // per-cell mode: node-changing particles deposit into a second tile sJ2.  Their many
+    // single adds then round against their own small partial sums, not against the
+    // per-cell sums (an FP32 add's error is about an ulp of the partial sum); the two
+    // tiles are summed in FP64 at the flush.
+    T *sJ2 = sJ + 3 * jsz;
+    float *sRec = reinterpret_cast<float *>( sJ2 + ( CELLS ? 3 * jsz : 0 ) );
     int *sCnt = reinterpret_cast<int *>( sRec + ( CELLS ? REC * nmax : 0 ) );
     int *sStart = sCnt + TC;
     int *sRank = sStart + TC;   // reused after loading as the list of node-changing slots
@@ -598,7 +607,7 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
             }
         }
     }
-    for( int e = threadIdx.x; e < 3 * jsz; e += blockDim.x ) sJ[e] = T( 0 );
+    for( int e = threadIdx.x; e < ( CELLS ? 6 : 3 ) * jsz; e += blockDim.x ) sJ[e] = T( 0 );
     // per-cell mode keeps the field copies in flight through the ranking and waits
     // for them together with the particle copies
     if constexpr( !CELLS ) cp_async_wait_all();
@@ -1006,9 +1015,9 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
 
     // 3. per-cell deposit (CELLS).  Particles that stay on their node in every
     // dimension share their cell's fixed footprint: stencil points 1..3 across the
-    // current, 2..3 along it (point 4 carries only the rounding residue of a sum
-    // that is zero).  Their contributions are summed in registers and added once
-    // per cell; particles that change node are deposited directly.  3D: thread
+    // current, 2..3 along it (point 4 carries a sum that is exactly zero).  Their
+    // contributions are summed in registers and added once per cell; particles that
+    // change node are deposited directly (into sJ2).  3D: thread
     // t works on cell t % TC, group j = t / TC; even groups own Jx and the lower
     // Jz plane, odd groups Jy and the upper one; groups j>>1 split the records.
     // 2D: the groups split the records and own all three components.
@@ -1136,7 +1145,8 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
                 }
             }
         }
-        // node-changing particles, one per thread
+        // node-changing particles, one per thread, into their own tile (after the
+        // per-cell pass: warps that finish their cells early start on this list)
         for( int k = threadIdx.x; k < sNX; k += blockDim.x ) {
             const int q = sXs[k];
             const int lc = sSlotCell[q];
@@ -1164,7 +1174,7 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
             }
             // the list is grouped by crossing dimension, so a warp's zero nodes mostly coincide
             const T crz = cw0 * wq * vz;
-            deposit_direct<DIM, T>( sJ, td, jsz, cl, W, cr, crz );
+            deposit_direct<DIM, T>( sJ2, td, jsz, cl, W, cr, crz );
         }
         __syncthreads();
     }
@@ -1179,24 +1189,24 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
         double *dstJ = f.J[c];
         const int ny = ext( g, 1, stag( c, 1 ) ), nz = ext( g, 2, stag( c, 2 ) );
         const int nx = ext( g, 0, stag( c, 0 ) );
-        const T *srcJ = sJ + c * jsz;
+        const T *srcJ = sJ + c * jsz, *srcJ2 = sJ2 + c * jsz;
         if( jm.fast ) {
             if( jm.active ) {
                 const int gy = iy0 + OS - 2 + jm.cy, gz = DIM == 3 ? iz0 + OS - 2 + jm.cz : 0;
                 for( int cx = jm.cx0; cx < td.JX; cx += jm.step ) {
                     const int e = ( cx * td.JY + jm.cy ) * td.JZ + jm.cz;
-                    const T v = srcJ[e];
+                    const double v = CELLS ? ( double )srcJ[e] + ( double )srcJ2[e] : ( double )srcJ[e];
                     const int gx = ix0 + OS - 2 + cx;
-                    if( v != T( 0 ) && gx < nx && gy < ny && gz < nz ) atomicAdd( &dstJ[( ( int64_t )gx * ny + gy ) * nz + gz], ( double )v );
+                    if( v != 0.0 && gx < nx && gy < ny && gz < nz ) atomicAdd( &dstJ[( ( int64_t )gx * ny + gy ) * nz + gz], v );
                 }
             }
         } else {
             for( int e = threadIdx.x; e < jsz; e += blockDim.x ) {
-                const T v = srcJ[e];
-                if( v == T( 0 ) ) continue;
+                const double v = CELLS ? ( double )srcJ[e] + ( double )srcJ2[e] : ( double )srcJ[e];
+                if( v == 0.0 ) continue;
                 const int cz = e % td.JZ, cy = ( e / td.JZ ) % td.JY, cx = e / ( td.JZ * td.JY );
                 const int gx = ix0 + OS - 2 + cx, gy = iy0 + OS - 2 + cy, gz = DIM == 3 ? iz0 + OS - 2 + cz : 0;
-                if( gx < nx && gy < ny && gz < nz ) atomicAdd( &dstJ[( ( int64_t )gx * ny + gy ) * nz + gz], ( double )v );
+                if( gx < nx && gy < ny && gz < nz ) atomicAdd( &dstJ[( ( int64_t )gx * ny + gy ) * nz + gz], v );
             }
         }
     }
@@ -2290,7 +2300,8 @@ int launch_particles( sg_sim *S, SpeciesState &s, cudaStream_t st, int t0, int t
     int chunk = s.max_cap;
     if constexpr( MIXED ) {
         const int tc = S->g.T[0] * S->g.T[1] * ( DIM == 3 ? S->g.T[2] : 1 );
-        const int fit = cells_chunk_fit( smem, tc );
+        const size_t j2 = cells_j2_bytes( tile_dims( S->g ) );
+        const int fit = cells_chunk_fit( smem + j2, tc );
         chunk = std::max( 1, std::min( s.max_cap, fit & ~31 ) );
         if( tc <= ( DIM == 3 ? 64 : 128 ) && fit >= 128 ) {
             const GridInfo &g = S->g;
@@ -2310,7 +2321,7 @@ int launch_particles( sg_sim *S, SpeciesState &s, cudaStream_t st, int t0, int t
                 if( ft == 2 ) kern = k_step_particles<DIM, MIXED, KIND, true, 2>;
                 if( ft == 3 ) kern = k_step_particles<DIM, MIXED, KIND, true, 3>;
             }
-            smem += cells_smem_bytes( tc, chunk );
+            smem += j2 + cells_smem_bytes( tc, chunk );
         }
     }
     if( smem > 48 * 1024 ) SG_CUDA_TRY( cudaFuncSetAttribute( kern, cudaFuncAttributeMaxDynamicSharedMemorySize, ( int )smem ) );
@@ -2659,7 +2670,7 @@ int launch_chunk_dim( const sg_sim *S, int max_cap )
     if( !S->mixed ) return 0;
     const GridInfo &g = S->g;
     const int tc = g.T[0] * g.T[1] * ( DIM == 3 ? g.T[2] : 1 );
-    const int fit = cells_chunk_fit( S->smem_bytes, tc );
+    const int fit = cells_chunk_fit( S->smem_bytes + cells_j2_bytes( tile_dims( g ) ), tc );
     int chunk = std::max( 1, std::min( max_cap, fit & ~31 ) );
     if( tc <= ( DIM == 3 ? 64 : 128 ) && fit >= 128 ) {
         int ft = 0;

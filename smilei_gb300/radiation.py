@@ -138,10 +138,13 @@ class PhotonChiMLP:
         self.validated = True
         return err.reshape(n_chi_bins, n_xi_bins), nm.value
 
-    def photon_chi(self, chi: torch.Tensor, xi: torch.Tensor) -> torch.Tensor:
+    def photon_chi(self, chi: torch.Tensor, xi: torch.Tensor, tensor_cores: bool = True) -> torch.Tensor:
+        """Batched network inverse CDF; a 64-wide network uses the tensor cores unless
+        tensor_cores is False (then every layer runs on the FP32 cores)."""
         out = torch.empty_like(chi)
-        check(_lib.lib().sg_mlp_photon_chi(self._h, chi.numel(), ptr(chi), ptr(xi), ptr(out),
-                                           torch.cuda.current_stream().cuda_stream), "mlp photon_chi")
+        fn = _lib.lib().sg_mlp_photon_chi if tensor_cores else _lib.lib().sg_mlp_photon_chi_fp32
+        check(fn(self._h, chi.numel(), ptr(chi), ptr(xi), ptr(out), torch.cuda.current_stream().cuda_stream),
+              "mlp photon_chi")
         return out
 
 
