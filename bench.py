@@ -258,6 +258,8 @@ def run_gpu(args, rank, world, local_rank):
         tuning = {"x".join(map(str, k)) + (" queue" if q else ""): round(v, 3) for (k, q), v in times.items()}
     sim = build(tile)
     sim.set_tile_queue(queue)
+    if args.tma:
+        sim.set_tma_staging(True)
     nspec = len(cfg.get("species", [None]))
     n = sum(sim.species_count(k) for k in range(nspec))
     # initial E from the charge (FP64 CG, as the reference's solve_poisson): the charge
@@ -875,6 +877,8 @@ def main():
     ap.add_argument("--autotune", action="store_true",
                     help="pick the tile shape (and, for the 3D and 2D thermal and uneven workloads, the tile "
                          "queue) by timing candidates first")
+    ap.add_argument("--tma", action="store_true",
+                    help="3D mixed form, 4x4x4 tiles: stage the field tile with the tensor memory accelerator")
     ap.add_argument("--tile-queue", action="store_true",
                     help="particle kernel as a persistent grid draining a tile queue, densest tile first")
     ap.add_argument("--slack", type=float, default=0.25,
@@ -995,7 +999,7 @@ def main():
                    "B_alg_bytes_per_particle_step": res["B_alg"],
                    "hbm_fraction_of_step": step_gbs / res["peak"], "wall_ms_per_step": res["wall_ms_per_step"],
                    "energy_ukin_uelm_before_after": res["energy"], "tile": res["tile"] or "default 4x4x4",
-                   "tile_queue": res.get("queue", False),
+                   "tile_queue": res.get("queue", False), "tma_staging": bool(getattr(args, "tma", False)),
                    "autotune_ms_per_step": res["tuning"],
                    "relayouts_spilled_over_run": res["relayouts"],
                    **({"charge_residual": res["residual"]} if res.get("residual") else {}),

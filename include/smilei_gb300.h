@@ -175,6 +175,15 @@ int sg_sim_destroy( sg_sim *sim );
  * No reference counterpart as an entry point. */
 int sg_sim_set_tile_queue( sg_sim *sim, int on );
 
+/* How the particle kernel stages its tile of E and B_m in shared memory (3D mixed form
+ * with 4x4x4 tiles, periodic).  on = 0 (default): every thread copies words with
+ * cp.async.  on = 1: one thread issues a tensor-memory-accelerator copy
+ * (cp.async.bulk.tensor, completion on an mbarrier) per component; the tensor maps need
+ * rows of a multiple of 16 bytes, so every step first copies E and B_m into padded
+ * arrays.  The results are the same either way.  No reference counterpart (the
+ * reference's gather reads the field arrays directly, Interpolator3D2Order.cpp:225-245). */
+int sg_sim_set_tma_staging( sg_sim *sim, int on );
+
 /* Adds a species from host arrays (absolute FP64 positions pos[ndim*n],
  * momenta mom[3*n], weights[n]); pusher: 0 Boris, 1 Vay, 2 Higuera-Cary.
  * Returns the species index in *index. */

@@ -89,6 +89,7 @@ _SIGNATURES = {
                                 ctypes.POINTER(_I)]),
     "sg_sim_set_stream": (_I, [_VP, _VP]),
     "sg_sim_set_tile_queue": (_I, [_VP, _I]),
+    "sg_sim_set_tma_staging": (_I, [_VP, _I]),
     "sg_sim_state_bytes": (_I, [_VP, _I, ctypes.POINTER(ctypes.c_size_t)]),
     "sg_sim_packed_bytes": (_I, [_VP, _I, ctypes.POINTER(ctypes.c_size_t)]),
     "sg_sim_pack_state": (_I, [_VP, _I, _VP]),

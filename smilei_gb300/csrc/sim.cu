@@ -31,6 +31,9 @@
 #include "resident_rad.cuh"
 #include "scan.cuh"
 
+#include <cuda.h> // CUtensorMap (the encoder is looked up through the runtime: no libcuda link)
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -474,12 +477,15 @@ constexpr int NO_SHIFT = 1 | ( 1 << 2 ) | ( 1 << 4 ); // packed shifts (s + 1 pe
 constexpr int GONE_RECORD = 1 << 8;                  // record of a particle removed at an open boundary: deposits nothing
 
 // Shared memory of the per-cell mode: REC planes of nmax floats, a count and a
-// start per cell, a packed (cell, rank) word and a list word per particle, a
-// cell byte per slot.
+// start per cell, a packed (cell, rank) word per particle (later the node-changing
+// list), a cell byte per slot.  A chunk holds at most 128 XL particles (the in-place
+// grouping of the node-changing list keeps XL entries per thread in registers).
 constexpr size_t CELLS_SMEM_TARGET = 44 * 1024; // five 128-thread blocks per SM
+constexpr int XL = 8;
+constexpr int CELLS_MAX_CHUNK = 128 * XL;
 constexpr size_t cells_smem_bytes( int tc, int nmax )
 {
-    return ( size_t )REC * 4 * nmax + ( size_t )8 * tc + ( size_t )8 * nmax + ( ( ( size_t )nmax + 15 ) & ~( size_t )15 );
+    return ( size_t )REC * 4 * nmax + ( size_t )8 * tc + ( size_t )4 * nmax + ( ( ( size_t )nmax + 15 ) & ~( size_t )15 );
 }
 
 // Particles per chunk of the per-cell mode that fit CELLS_SMEM_TARGET with a tile
@@ -487,9 +493,25 @@ constexpr size_t cells_smem_bytes( int tc, int nmax )
 constexpr int cells_chunk_fit( size_t tile_bytes, int tc )
 {
     const size_t fixed = tile_bytes + cells_smem_bytes( tc, 0 ) + 16;
-    const size_t per = ( size_t )REC * 4 + 8 + 1; // planes, rank and list words, cell byte
-    return fixed < CELLS_SMEM_TARGET ? ( int )( ( CELLS_SMEM_TARGET - fixed ) / per ) : 0;
+    const size_t per = ( size_t )REC * 4 + 4 + 1; // planes, rank (list) word, cell byte
+    const int fit = fixed < CELLS_SMEM_TARGET ? ( int )( ( CELLS_SMEM_TARGET - fixed ) / per ) : 0;
+    return fit < CELLS_MAX_CHUNK ? fit : CELLS_MAX_CHUNK;
 }
+
+// Field tile staged by the tensor memory accelerator (TMA, 3D 4x4x4 tiles): one
+// cp.async.bulk.tensor per component copies a box of 8 (z) x 7 (y) x 7 (x) FP32 values.
+// The box's z extent must be a multiple of 16 bytes and its start 16-byte aligned, so it
+// starts at the tile's first node (4 tz) rather than one below (4 tz + 1 in array
+// indices) and is 8 wide; the gather then indexes z one further.  Each component's tile
+// starts on a 128-byte boundary of shared memory.  The global arrays need rows that are a
+// multiple of 16 bytes, which the reference layout's 261- or 262-value rows are not: the
+// step copies E and B_m into padded arrays (rows of a multiple of 4 values) first.
+constexpr int TMA_BOX_Z = 8, TMA_BOX_Y = 7, TMA_BOX_X = 7;
+constexpr int TMA_FSZ = 416; // floats per component tile: 8 x 7 x 7 = 392, rounded up to 128 bytes
+constexpr unsigned TMA_TX_BYTES = 6 * TMA_BOX_Z * TMA_BOX_Y * TMA_BOX_X * 4;
+struct TmaFields {
+    CUtensorMap m[6]; // Ex Ey Ez Bx_m By_m Bz_m over the padded arrays
+};
 
 // Tile shapes with their own kernel instances (code FT): 0 any shape (runtime), 1 the
 // default (4x4x4 in 3D, 8x8 in 2D), 2 8x16 (2D), 3 4x4 (2D); the 2D ones are the shapes
@@ -514,17 +536,41 @@ constexpr int fixt_chunk( int dim, int ft )
 // The per-cell mode's second current tile (node-changing particles), FP32.
 inline size_t cells_j2_bytes( const TileDims &td ) { return ( size_t )3 * td.JX * td.JY * td.JZ * 4; }
 
+// The 3D default tile's chunk with TMA staging: the padded field tile (6 TMA_FSZ floats)
+// and 128 bytes to align the dynamic shared memory.
+constexpr size_t TMA_TILE_BYTES = ( size_t )( 6 * TMA_FSZ + 6 * 8 * 8 * 8 ) * 4 + 128;
+constexpr int tma_chunk() { return cells_chunk_fit( TMA_TILE_BYTES, 64 ) & ~31; }
+
 // FT > 0: the tile shape is known at compile time, so tile and stencil offsets fold into
 // immediates; the chunk is fixt_chunk.
-template <int DIM, bool MIXED, int KIND, bool CELLS, int FT = 0>
+// Waits (every thread) for phase `phase` of the TMA barrier, at most a bounded number of
+// polls (each try_wait itself suspends for a while); a barrier that never completes
+// sets SG_ERR_STATE in the status word and returns, so the step reports the failure.
+__device__ __forceinline__ void tma_wait( unsigned long long *bar, unsigned phase, int *status )
+{
+    const unsigned mb = ( unsigned )__cvta_generic_to_shared( bar );
+    for( int it = 0; it < ( 1 << 22 ); it++ ) {
+        unsigned done;
+        asm volatile( "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                      : "=r"( done ) : "r"( mb ), "r"( phase ) : "memory" );
+        if( done ) return;
+    }
+    atomicCAS( status, 0, SG_ERR_STATE );
+}
+
+// TMA (3D, mixed, per-cell, FT 1 only): the field tile comes from the tensor maps in
+// `tma` (padded copies of E and B_m), not from word copies.
+template <int DIM, bool MIXED, int KIND, bool CELLS, int FT = 0, bool TMA = false>
 __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_particles(
     GridInfo g_arg, Fields<typename std::conditional<MIXED, float, double>::type> f, SpecParams sp, PBuf<MIXED> in,
     PBuf<MIXED> out, const int64_t *__restrict__ seg_start, const int *__restrict__ cap,
     const int *__restrict__ count_in, int *__restrict__ count_out, PBuf<MIXED> ovf, int *__restrict__ ovf_tile,
-    int *__restrict__ ovf_count, int ovf_cap, int *__restrict__ status, int nmax_arg, int *__restrict__ removed )
+    int *__restrict__ ovf_count, int ovf_cap, int *__restrict__ status, int nmax_arg, int *__restrict__ removed,
+    const __grid_constant__ TmaFields tma )
 {
     using T = typename std::conditional<MIXED, float, double>::type;
-    const int nmax = FT ? fixt_chunk( DIM, FT ) : nmax_arg;
+    static_assert( !TMA || ( DIM == 3 && MIXED && CELLS && FT == 1 ), "TMA staging: 3D mixed per-cell 4x4x4 tiles" );
+    const int nmax = FT ? ( TMA ? tma_chunk() : fixt_chunk( DIM, FT ) ) : nmax_arg;
     GridInfo g = g_arg;
     if constexpr( FT > 0 ) {
 #pragma unroll
@@ -534,9 +580,12 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
         }
     }
     extern __shared__ __align__( 16 ) unsigned char smem_raw[];
-    T *sF = reinterpret_cast<T *>( smem_raw );
-    const TileDims td = tile_dims( g );
-    const int fsz = td.FX * td.FY * td.FZ;
+    // TMA writes 128-byte aligned component tiles (the dynamic region is 16-byte aligned)
+    T *sF = reinterpret_cast<T *>( TMA ? ( smem_raw + ( ( 128 - ( ( unsigned )__cvta_generic_to_shared( smem_raw ) & 127u ) ) & 127u ) )
+                                       : smem_raw );
+    TileDims td = tile_dims( g );
+    if constexpr( TMA ) td.FZ = TMA_BOX_Z;
+    const int fsz = TMA ? TMA_FSZ : td.FX * td.FY * td.FZ;
     const int jsz = td.JX * td.JY * td.JZ;
     T *sJ = sF + 6 * fsz;
     // per-cell mode (CELLS): particle planes, per-cell counts and starts, each
@@ -550,11 +599,24 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
     float *sRec = reinterpret_cast<float *>( sJ2 + ( CELLS ? 3 * jsz : 0 ) );
     int *sCnt = reinterpret_cast<int *>( sRec + ( CELLS ? REC * nmax : 0 ) );
     int *sStart = sCnt + TC;
-    int *sRank = sStart + TC;   // reused after loading as the list of node-changing slots
-    int *sXs = sRank + ( CELLS ? nmax : 0 ); // that list grouped by crossing class
-    unsigned char *sSlotCell = reinterpret_cast<unsigned char *>( sXs + ( CELLS ? nmax : 0 ) );
+    int *sRank = sStart + TC;   // reused after loading as the list of node-changing slots (then grouped by crossing class)
+    unsigned char *sSlotCell = reinterpret_cast<unsigned char *>( sRank + ( CELLS ? nmax : 0 ) );
     __shared__ int sNX;         // length of that list
     __shared__ int sXc[4];      // node-changing particles per class (x, y, z only; several)
+
+    // TMA completion barrier: thread 0 arms it per tile with the bytes to expect, the
+    // copies complete it, every thread waits on its phase (bounded)
+    __shared__ __align__( 8 ) unsigned long long sTmaBar;
+    unsigned tma_phase = 0;
+    if constexpr( TMA ) {
+        if( threadIdx.x == 0 ) {
+            const unsigned mb = ( unsigned )__cvta_generic_to_shared( &sTmaBar );
+            asm volatile( "mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"( mb ) : "memory" );
+            asm volatile( "fence.mbarrier_init.release.cluster;\n" ::: "memory" );
+        }
+        __syncthreads();
+    }
+    bool tma_pending = false;
 
     // One tile per CTA, or (sp.queue set) a persistent grid whose CTAs take tiles from
     // a device counter until none is left, in the order sp.order gives (densest first).
@@ -580,9 +642,27 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
     const int ix0 = tx * g.T[0], iy0 = ty * g.T[1], iz0 = DIM == 3 ? tz * g.T[2] : 0;
 
     // 1. stage E and B_m (field tile origin = array index (i0 + OS - 1)) and clear J
+    if constexpr( TMA ) {
+        if( threadIdx.x == 0 ) {
+            const unsigned mb = ( unsigned )__cvta_generic_to_shared( &sTmaBar );
+            // the previous tile's reads of sF come before these asynchronous writes
+            asm volatile( "fence.proxy.async.shared::cta;\n" ::: "memory" );
+            asm volatile( "mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"( mb ), "r"( TMA_TX_BYTES ) : "memory" );
+            // box origin: z at the tile's first node (16-byte aligned), y and x one node below
+            const int z0 = iz0, y0 = iy0 + OS - 1, x0 = ix0 + OS - 1;
+#pragma unroll
+            for( int c = 0; c < 6; c++ ) {
+                const unsigned dst = ( unsigned )__cvta_generic_to_shared( sF + c * fsz );
+                asm volatile( "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n"
+                              ::"r"( dst ), "l"( reinterpret_cast<uint64_t>( &tma.m[c] ) ), "r"( z0 ), "r"( y0 ), "r"( x0 ), "r"( mb )
+                              : "memory" );
+            }
+        }
+        tma_pending = true;
+    }
     const TileMap fm = tile_map<DIM>( td.FY, td.FZ );
 #pragma unroll
-    for( int c = 0; c < 6; c++ ) {
+    for( int c = 0; c < ( TMA ? 0 : 6 ); c++ ) {
         const T *src = c < 3 ? f.E[c] : f.Bm[c - 3];
         const int ny = ext( g, 1, stag( c, 1 ) ), nz = ext( g, 2, stag( c, 2 ) );
         const int nx = ext( g, 0, stag( c, 0 ) );
@@ -692,6 +772,13 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
         }
         if( threadIdx.x < 4 ) sXc[threadIdx.x] = 0;
         cp_async_wait_all(); // the particle planes (and, on the first chunk, the field tile)
+        if constexpr( TMA ) {
+            if( tma_pending ) {
+                tma_wait( &sTmaBar, tma_phase, status );
+                tma_phase ^= 1u;
+                tma_pending = false;
+            }
+        }
         __syncthreads();
     }
 
@@ -792,7 +879,8 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
         // clamp the dual shift for safety (0 or 1 by construction)
 #pragma unroll
         for( int d = 0; d < 3; d++ ) sd[d] = sd[d] < 0 ? 0 : ( sd[d] > 1 ? 1 : sd[d] );
-        const int bz_p = DIM == 3 ? lx[2] : 0, bz_d = DIM == 3 ? lx[2] + sd[2] : 0;
+        // (TMA's box starts one z node lower)
+        const int bz_p = DIM == 3 ? lx[2] + ( TMA ? 1 : 0 ) : 0, bz_d = DIM == 3 ? lx[2] + sd[2] + ( TMA ? 1 : 0 ) : 0;
         const int bx_p = lx[0], bx_d = lx[0] + sd[0], by_p = lx[1], by_d = lx[1] + sd[1];
         // Ex(d,p,p) Ey(p,d,p) Ez(p,p,d) Bx(p,d,d) By(d,p,d) Bz(d,d,p)
         T Ex, Ey, Ez, Bx, By, Bz;
@@ -1001,15 +1089,26 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
                 run += c;
             }
         }
-        __syncthreads();
-        for( int k = threadIdx.x; k < sNX; k += blockDim.x ) {
-            const int q = sRank[k];
-            const int sb = __float_as_int( sRec[6 * nmax + q] );
-            const int h0 = ( sb & 3 ) - 1, h1 = ( ( sb >> 2 ) & 3 ) - 1, h2 = ( ( sb >> 4 ) & 3 ) - 1;
-            const int nsh = ( h0 != 0 ) + ( h1 != 0 ) + ( h2 != 0 );
-            const int cls = nsh == 1 ? ( h0 != 0 ? 0 : ( h1 != 0 ? 1 : 2 ) ) : 3;
-            sXs[atomicAdd( &sXc[cls], 1 )] = q;
+        // in place: every thread holds its entries (at most XL of them: nmax <= 128 XL)
+        // while the list is rewritten grouped
+        int xq[XL], xc[XL];
+#pragma unroll
+        for( int j = 0; j < XL; j++ ) {
+            const int k = ( int )threadIdx.x + j * ( int )blockDim.x;
+            xq[j] = -1;
+            if( k < sNX ) {
+                const int q = sRank[k];
+                const int sb = __float_as_int( sRec[6 * nmax + q] );
+                const int h0 = ( sb & 3 ) - 1, h1 = ( ( sb >> 2 ) & 3 ) - 1, h2 = ( ( sb >> 4 ) & 3 ) - 1;
+                const int nsh = ( h0 != 0 ) + ( h1 != 0 ) + ( h2 != 0 );
+                xq[j] = q;
+                xc[j] = nsh == 1 ? ( h0 != 0 ? 0 : ( h1 != 0 ? 1 : 2 ) ) : 3;
+            }
         }
+        __syncthreads();
+#pragma unroll
+        for( int j = 0; j < XL; j++ )
+            if( xq[j] >= 0 ) sRank[atomicAdd( &sXc[xc[j]], 1 )] = xq[j];
         __syncthreads();
     }
 
@@ -1148,7 +1247,7 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
         // node-changing particles, one per thread, into their own tile (after the
         // per-cell pass: warps that finish their cells early start on this list)
         for( int k = threadIdx.x; k < sNX; k += blockDim.x ) {
-            const int q = sXs[k];
+            const int q = sRank[k];
             const int lc = sSlotCell[q];
             int cl[3];
             if( DIM == 3 ) {
@@ -1181,6 +1280,13 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
     } // chunk
     // a tile without particles still waits for its field copies before the CTA ends
     if constexpr( CELLS ) cp_async_wait_all();
+    if constexpr( TMA ) {
+        if( tma_pending ) {
+            tma_wait( &sTmaBar, tma_phase, status );
+            tma_phase ^= 1u;
+            tma_pending = false;
+        }
+    }
 
     // 4. flush the J tile (origin = array index i0 + OS - 2) with global atomics
     const TileMap jm = tile_map<DIM>( td.JY, td.JZ );
@@ -1217,6 +1323,18 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
 // ------------------------------------------------------------------------------
 // Field kernels of the periodic single-grid step.
 // ------------------------------------------------------------------------------
+
+// dst rows of nz4 values (zeros past nz) from src rows of nz: the padded layout the TMA
+// tensor maps need (rows a multiple of 16 bytes).  One thread per padded value.
+__global__ void k_pad_rows( const float *__restrict__ src, float *__restrict__ dst, int64_t rows, int nz, int nz4 )
+{
+    const int64_t n = rows * nz4;
+    for( int64_t t = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x; t < n; t += ( int64_t )gridDim.x * blockDim.x ) {
+        const int64_t r = t / nz4;
+        const int k = ( int )( t - r * nz4 );
+        dst[t] = k < nz ? src[r * nz + k] : 0.0f;
+    }
+}
 
 // Periodic J ghost fold along dimension d (the same-process branch of
 // SyncVectorPatch::sumAllComponents, SyncVectorPatch.cpp:203-330): the first
@@ -2202,6 +2320,10 @@ struct sg_sim {
     bool own_stream = false;
     bool tile_queue = false;  // particle kernel as a persistent grid over a tile queue
     int *d_queue = nullptr;   // its item counter
+    bool tma = false;         // field tile staged by TMA (3D mixed, 4x4x4 tiles)
+    float *tma_pad[6] = {};   // E, B_m with rows padded to a multiple of 4 values
+    int tma_nz4[6] = {};      // their padded row lengths
+    TmaFields tma_maps{};     // tensor maps over them
     int *d_flags = nullptr; // [0] status, [1 + s] spill count of species s, [1 + max_species + s] removed
     int *h_flags = nullptr; // pinned copy
     int max_species = 16;
@@ -2322,6 +2444,13 @@ int launch_particles( sg_sim *S, SpeciesState &s, cudaStream_t st, int t0, int t
                 if( ft == 3 ) kern = k_step_particles<DIM, MIXED, KIND, true, 3>;
             }
             smem += j2 + cells_smem_bytes( tc, chunk );
+            if constexpr( DIM == 3 ) {
+                if( S->tma && ft == 1 ) {
+                    kern = k_step_particles<3, true, KIND, true, 1, true>;
+                    chunk = tma_chunk();
+                    smem = TMA_TILE_BYTES + cells_smem_bytes( tc, chunk );
+                }
+            }
         }
     }
     if( smem > 48 * 1024 ) SG_CUDA_TRY( cudaFuncSetAttribute( kern, cudaFuncAttributeMaxDynamicSharedMemorySize, ( int )smem ) );
@@ -2344,7 +2473,7 @@ int launch_particles( sg_sim *S, SpeciesState &s, cudaStream_t st, int t0, int t
     }
     kern<<<grid, 128, smem, st>>>( S->g, field_view<T>( S ), sp, bin, bout, s.seg_start, s.cap, s.count[in],
                                           s.count[out], bov, s.ovf_tile, S->d_flags + 1 + sidx, ( int )s.ovf_capacity,
-                                          S->d_flags, chunk, S->d_flags + 1 + S->max_species + sidx );
+                                          S->d_flags, chunk, S->d_flags + 1 + S->max_species + sidx, S->tma_maps );
     SG_LAUNCH_CHECK( "k_step_particles" );
     return SG_OK;
 }
@@ -2526,6 +2655,18 @@ int enqueue_step( sg_sim *S, cudaStream_t st, const StreamIn *in = nullptr )
         k_bump_step<<<1, 1, 0, st>>>( S->d_rad_step );
         SG_LAUNCH_CHECK( "k_bump_step" );
         launches++;
+    }
+    if( S->tma ) {
+        // the padded copies of E and B_m that the tensor maps read
+        Fields<float> f = field_view<float>( S );
+        for( int c = 0; c < 6; c++ ) {
+            const float *src = c < 3 ? f.E[c] : f.Bm[c - 3];
+            const int64_t rows = S->fsize[c] / S->fshape[c][2];
+            k_pad_rows<<<( unsigned )std::min<int64_t>( ( rows * S->tma_nz4[c] + 255 ) / 256, 152 * 32 ), 256, 0, st>>>(
+                src, S->tma_pad[c], rows, S->fshape[c][2], S->tma_nz4[c] );
+            SG_LAUNCH_CHECK( "k_pad_rows" );
+            launches++;
+        }
     }
     for( auto &s : S->sp ) {
         if( in && &s == &S->sp[in->species] ) {
@@ -3049,6 +3190,7 @@ int sg_sim_destroy( sg_sim *S )
     release( S->fmem );
     release( S->d_flags );
     release( S->d_queue );
+    for( int c = 0; c < 6; c++ ) release( S->tma_pad[c] );
     release( S->d_step );
     if( S->h_flags ) cudaFreeHost( S->h_flags );
     release( S->scan_scratch );
@@ -3073,6 +3215,42 @@ int sg_sim_destroy( sg_sim *S )
     if( S->h_chunk_end ) cudaFreeHost( S->h_chunk_end );
     if( S->own_stream && S->stream ) cudaStreamDestroy( S->stream );
     delete S;
+    return SG_OK;
+}
+
+int sg_sim_set_tma_staging( sg_sim *S, int on )
+{
+    SG_REQUIRE( S, "NULL simulation" );
+    SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
+    if( !on ) {
+        S->tma = false;
+        drop_graphs( S );
+        return SG_OK;
+    }
+    const GridInfo &g = S->g;
+    SG_REQUIRE( g.ndim == 3 && S->mixed && g.T[0] == 4 && g.T[1] == 4 && g.T[2] == 4,
+                "TMA staging needs the 3D mixed form with 4x4x4 tiles" );
+    SG_REQUIRE( !g.open[0] && !g.open[1] && !g.open[2], "TMA staging needs a periodic grid" );
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    SG_CUDA_TRY( cudaGetDriverEntryPointByVersion( "cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q ) );
+    SG_REQUIRE( fn && q == cudaDriverEntryPointSuccess, "cuTensorMapEncodeTiled is not available" );
+    auto encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>( fn );
+    for( int c = 0; c < 6; c++ ) {
+        const int field = c < 3 ? c : 6 + ( c - 3 ); // E, then B_m
+        const int nx = S->fshape[field][0], ny = S->fshape[field][1], nz = S->fshape[field][2];
+        S->tma_nz4[c] = ( nz + 3 ) & ~3;
+        if( !S->tma_pad[c] ) SG_CUDA_TRY( cudaMalloc( &S->tma_pad[c], ( size_t )nx * ny * S->tma_nz4[c] * sizeof( float ) ) );
+        const cuuint64_t dims[3] = { ( cuuint64_t )nz, ( cuuint64_t )ny, ( cuuint64_t )nx };
+        const cuuint64_t strides[2] = { ( cuuint64_t )S->tma_nz4[c] * 4, ( cuuint64_t )S->tma_nz4[c] * 4 * ny };
+        const cuuint32_t box[3] = { TMA_BOX_Z, TMA_BOX_Y, TMA_BOX_X }, estr[3] = { 1, 1, 1 };
+        const CUresult r = encode( &S->tma_maps.m[c], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, S->tma_pad[c], dims, strides, box, estr,
+                                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE );
+        if( r != CUDA_SUCCESS ) return set_error( SG_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d) for field %d", ( int )r, field );
+    }
+    S->tma = true;
+    drop_graphs( S );
     return SG_OK;
 }
 

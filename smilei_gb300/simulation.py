@@ -67,6 +67,11 @@ class Simulation:
         (on), or one CTA per tile (off, the default)."""
         check(_lib.lib().sg_sim_set_tile_queue(self._h, int(bool(on))), "set_tile_queue")
 
+    def set_tma_staging(self, on: bool = True):
+        """Field tile staged by the tensor memory accelerator (3D mixed form, 4x4x4 tiles)
+        instead of word copies (the default)."""
+        check(_lib.lib().sg_sim_set_tma_staging(self._h, int(bool(on))), "set_tma_staging")
+
     # -- species -----------------------------------------------------------
     def add_species(self, mass, charge, pusher, position, momentum, weight, name=None):
         """position[ndim, n], momentum[3, n], weight[n] as float64 numpy arrays (host) or CUDA tensors."""

@@ -38,7 +38,7 @@ def make_case(synthetic, ndim, seed, species_spec):
     return n_cells, cl, dt, fields, species
 
 
-def run_pair(sim_mod, cpu_oracle, ndim, form, nsteps, species_spec, seed=5, tile=None, tile_queue=False):
+def run_pair(sim_mod, cpu_oracle, ndim, form, nsteps, species_spec, seed=5, tile=None, tile_queue=False, tma=False):
     simulation, synthetic = sim_mod
     n_cells, cl, dt, fields, species = make_case(synthetic, ndim, seed, species_spec)
     sim = simulation.Simulation(n_cells, cl, dt, form=form, tile=tile, use_graph=True)
@@ -48,6 +48,8 @@ def run_pair(sim_mod, cpu_oracle, ndim, form, nsteps, species_spec, seed=5, tile
         sim.add_species(s["mass"], s["q"], s["pusher"], s["pos"], s["mom"], s["weight"])
     if tile_queue:
         sim.set_tile_queue(True)
+    if tma:
+        sim.set_tma_staging(True)
     sim.step(nsteps)
     ref = {k: v.copy() for k, v in fields.items()}
     ref_sp = [dict(s, pos=s["pos"].copy(), mom=s["mom"].copy()) for s in species]
@@ -293,3 +295,19 @@ def test_tile_queue_step_matches_oracle(sim_mod, cpu_oracle, ndim, form, tol):
     for pg, mg, pr, mr, cl, n_cells in parts:
         assert rel_err(mg, mr) <= tol * 10
         assert position_error(pg, pr, cl, n_cells) <= tol * 10
+
+
+@pytest.mark.parametrize("pusher,ppc", [("higueracary", 6), ("boris", 64)])
+def test_tma_staging_step_matches_oracle(sim_mod, cpu_oracle, pusher, ppc):
+    """The field tile staged by TMA (tensor copies of padded E and B_m, one mbarrier per
+    tile) gives the oracle's step like the word copies: 3 graph-replayed steps of the
+    16 x 12 x 8 grid (tiles at every grid edge, so boxes reach past the arrays and read
+    the tensor maps' zero fill), and a dense case whose tiles take several chunks."""
+    spec = [(1.0, -1.0, pusher, ppc, 0.14)]
+    got, ref, parts = run_pair(sim_mod, cpu_oracle, 3, "mixed", 3 if ppc < 32 else 1, spec, tma=True)
+    tol = 1e-4 if ppc < 32 else 1e-5
+    for k in FIELDS:
+        assert rel_err(got[k], ref[k]) <= tol, k
+    for pg, mg, pr, mr, cl, n_cells in parts:
+        assert rel_err(mg, mr) <= tol
+        assert position_error(pg, pr, cl, n_cells) <= tol
