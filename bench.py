@@ -258,8 +258,11 @@ def run_gpu(args, rank, world, local_rank):
         tuning = {"x".join(map(str, k)) + (" queue" if q else ""): round(v, 3) for (k, q), v in times.items()}
     sim = build(tile)
     sim.set_tile_queue(queue)
-    if args.tma:
-        sim.set_tma_staging(True)
+    # TMA staging is the default of the 3D mixed form with 4x4x4 tiles; --no-tma turns it off
+    tma = len(cfg["n_cells"]) == 3 and args.form == "mixed" and list(tile or [4, 4, 4]) == [4, 4, 4]
+    if tma and args.no_tma:
+        sim.set_tma_staging(False)
+        tma = False
     nspec = len(cfg.get("species", [None]))
     n = sum(sim.species_count(k) for k in range(nspec))
     # initial E from the charge (FP64 CG, as the reference's solve_poisson): the charge
@@ -373,7 +376,7 @@ def run_gpu(args, rank, world, local_rank):
     return dict(n=n, ms=ms, value=value, wall_ms_per_step=(wall1 - wall0) * 1e3 / args.steps, e2e=e2e,
                 kernel_bytes=kernel_bytes, t_kernel=t_kernel, peak=peak, peak_kind=peak_kind, B_alg=B_alg,
                 launches=launches, clocks=clk.summary(), energy=(uk0, ue0, uk1, ue1), cfg=cfg, tile=tile,
-                tuning=tuning, relayouts=relayouts, fp64=fp64, queue=bool(queue),
+                tuning=tuning, relayouts=relayouts, fp64=fp64, queue=bool(queue), tma=tma,
                 residual=None if res0 is None else {"after_poisson": res0, "after_steps": res1,
                                                     "poisson_iterations": poisson[0]})
 
@@ -877,8 +880,9 @@ def main():
     ap.add_argument("--autotune", action="store_true",
                     help="pick the tile shape (and, for the 3D and 2D thermal and uneven workloads, the tile "
                          "queue) by timing candidates first")
-    ap.add_argument("--tma", action="store_true",
-                    help="3D mixed form, 4x4x4 tiles: stage the field tile with the tensor memory accelerator")
+    ap.add_argument("--no-tma", action="store_true",
+                    help="3D mixed form, 4x4x4 tiles: stage the field tile with word copies instead of the "
+                         "tensor memory accelerator")
     ap.add_argument("--tile-queue", action="store_true",
                     help="particle kernel as a persistent grid draining a tile queue, densest tile first")
     ap.add_argument("--slack", type=float, default=0.25,
@@ -999,7 +1003,7 @@ def main():
                    "B_alg_bytes_per_particle_step": res["B_alg"],
                    "hbm_fraction_of_step": step_gbs / res["peak"], "wall_ms_per_step": res["wall_ms_per_step"],
                    "energy_ukin_uelm_before_after": res["energy"], "tile": res["tile"] or "default 4x4x4",
-                   "tile_queue": res.get("queue", False), "tma_staging": bool(getattr(args, "tma", False)),
+                   "tile_queue": res.get("queue", False), "tma_staging": res.get("tma", False),
                    "autotune_ms_per_step": res["tuning"],
                    "relayouts_spilled_over_run": res["relayouts"],
                    **({"charge_residual": res["residual"]} if res.get("residual") else {}),

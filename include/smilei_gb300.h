@@ -176,12 +176,14 @@ int sg_sim_destroy( sg_sim *sim );
 int sg_sim_set_tile_queue( sg_sim *sim, int on );
 
 /* How the particle kernel stages its tile of E and B_m in shared memory (3D mixed form
- * with 4x4x4 tiles, periodic).  on = 0 (default): every thread copies words with
- * cp.async.  on = 1: one thread issues a tensor-memory-accelerator copy
+ * with 4x4x4 tiles, periodic).  on = 1 (the default for such a simulation, set by
+ * sg_sim_create): one thread issues a tensor-memory-accelerator copy
  * (cp.async.bulk.tensor, completion on an mbarrier) per component; the tensor maps need
  * rows of a multiple of 16 bytes, so every step first copies E and B_m into padded
- * arrays.  The results are the same either way.  No reference counterpart (the
- * reference's gather reads the field arrays directly, Interpolator3D2Order.cpp:225-245). */
+ * arrays (six more field arrays of device memory).  on = 0: every thread copies words
+ * with cp.async; no padded arrays are written.  The results are the same either way.
+ * Any other simulation refuses on = 1.  No reference counterpart (the reference's
+ * gather reads the field arrays directly, Interpolator3D2Order.cpp:225-245). */
 int sg_sim_set_tma_staging( sg_sim *sim, int on );
 
 /* Adds a species from host arrays (absolute FP64 positions pos[ndim*n],

@@ -477,25 +477,22 @@ constexpr int NO_SHIFT = 1 | ( 1 << 2 ) | ( 1 << 4 ); // packed shifts (s + 1 pe
 constexpr int GONE_RECORD = 1 << 8;                  // record of a particle removed at an open boundary: deposits nothing
 
 // Shared memory of the per-cell mode: REC planes of nmax floats, a count and a
-// start per cell, a packed (cell, rank) word per particle (later the node-changing
-// list), a cell byte per slot.  A chunk holds at most 128 XL particles (the in-place
-// grouping of the node-changing list keeps XL entries per thread in registers).
+// start per cell, a packed (cell, rank) word and a list word per particle (with TMA
+// staging the list uses the field tile instead), a cell byte per slot.
 constexpr size_t CELLS_SMEM_TARGET = 44 * 1024; // five 128-thread blocks per SM
-constexpr int XL = 8;
-constexpr int CELLS_MAX_CHUNK = 128 * XL;
-constexpr size_t cells_smem_bytes( int tc, int nmax )
+constexpr size_t cells_smem_bytes( int tc, int nmax, bool list_in_fields = false )
 {
-    return ( size_t )REC * 4 * nmax + ( size_t )8 * tc + ( size_t )4 * nmax + ( ( ( size_t )nmax + 15 ) & ~( size_t )15 );
+    return ( size_t )REC * 4 * nmax + ( size_t )8 * tc + ( size_t )( list_in_fields ? 4 : 8 ) * nmax +
+           ( ( ( size_t )nmax + 15 ) & ~( size_t )15 );
 }
 
 // Particles per chunk of the per-cell mode that fit CELLS_SMEM_TARGET with a tile
 // of tc cells whose field and current tiles take tile_bytes (0: none fit).
-constexpr int cells_chunk_fit( size_t tile_bytes, int tc )
+constexpr int cells_chunk_fit( size_t tile_bytes, int tc, bool list_in_fields = false )
 {
     const size_t fixed = tile_bytes + cells_smem_bytes( tc, 0 ) + 16;
-    const size_t per = ( size_t )REC * 4 + 4 + 1; // planes, rank (list) word, cell byte
-    const int fit = fixed < CELLS_SMEM_TARGET ? ( int )( ( CELLS_SMEM_TARGET - fixed ) / per ) : 0;
-    return fit < CELLS_MAX_CHUNK ? fit : CELLS_MAX_CHUNK;
+    const size_t per = ( size_t )REC * 4 + ( list_in_fields ? 4 : 8 ) + 1; // planes, rank and list words, cell byte
+    return fixed < CELLS_SMEM_TARGET ? ( int )( ( CELLS_SMEM_TARGET - fixed ) / per ) : 0;
 }
 
 // Field tile staged by the tensor memory accelerator (TMA, 3D 4x4x4 tiles): one
@@ -539,7 +536,7 @@ inline size_t cells_j2_bytes( const TileDims &td ) { return ( size_t )3 * td.JX 
 // The 3D default tile's chunk with TMA staging: the padded field tile (6 TMA_FSZ floats)
 // and 128 bytes to align the dynamic shared memory.
 constexpr size_t TMA_TILE_BYTES = ( size_t )( 6 * TMA_FSZ + 6 * 8 * 8 * 8 ) * 4 + 128;
-constexpr int tma_chunk() { return cells_chunk_fit( TMA_TILE_BYTES, 64 ) & ~31; }
+constexpr int tma_chunk() { return cells_chunk_fit( TMA_TILE_BYTES, 64, true ) & ~31; }
 
 // FT > 0: the tile shape is known at compile time, so tile and stencil offsets fold into
 // immediates; the chunk is fixt_chunk.
@@ -556,6 +553,26 @@ __device__ __forceinline__ void tma_wait( unsigned long long *bar, unsigned phas
         if( done ) return;
     }
     atomicCAS( status, 0, SG_ERR_STATE );
+}
+
+// One thread arms the TMA barrier with the tile's bytes and issues the six tensor
+// copies of E and B_m into sF (component c at c * fsz floats, 128-byte aligned).
+__device__ __forceinline__ void tma_issue( const TmaFields &tma, unsigned long long *bar, float *sF, int fsz, int ix0,
+                                           int iy0, int iz0 )
+{
+    const unsigned mb = ( unsigned )__cvta_generic_to_shared( bar );
+    // earlier reads and writes of sF by the threads come before these asynchronous writes
+    asm volatile( "fence.proxy.async.shared::cta;\n" ::: "memory" );
+    asm volatile( "mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"( mb ), "r"( TMA_TX_BYTES ) : "memory" );
+    // box origin: z at the tile's first node (16-byte aligned), y and x one node below
+    const int z0 = iz0, y0 = iy0 + OS - 1, x0 = ix0 + OS - 1;
+#pragma unroll
+    for( int c = 0; c < 6; c++ ) {
+        const unsigned dst = ( unsigned )__cvta_generic_to_shared( sF + c * fsz );
+        asm volatile( "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n"
+                      ::"r"( dst ), "l"( reinterpret_cast<uint64_t>( &tma.m[c] ) ), "r"( z0 ), "r"( y0 ), "r"( x0 ), "r"( mb )
+                      : "memory" );
+    }
 }
 
 // TMA (3D, mixed, per-cell, FT 1 only): the field tile comes from the tensor maps in
@@ -599,8 +616,11 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
     float *sRec = reinterpret_cast<float *>( sJ2 + ( CELLS ? 3 * jsz : 0 ) );
     int *sCnt = reinterpret_cast<int *>( sRec + ( CELLS ? REC * nmax : 0 ) );
     int *sStart = sCnt + TC;
-    int *sRank = sStart + TC;   // reused after loading as the list of node-changing slots (then grouped by crossing class)
-    unsigned char *sSlotCell = reinterpret_cast<unsigned char *>( sRank + ( CELLS ? nmax : 0 ) );
+    int *sRank = sStart + TC;   // reused after loading as the list of node-changing slots
+    // that list grouped by crossing class: its own array, or with TMA staging the field
+    // tile, which the deposit no longer reads (a tile's next chunk stages it again)
+    int *sXs = TMA ? reinterpret_cast<int *>( sF ) : sRank + ( CELLS ? nmax : 0 );
+    unsigned char *sSlotCell = reinterpret_cast<unsigned char *>( ( TMA ? sRank : sXs ) + ( CELLS ? nmax : 0 ) );
     __shared__ int sNX;         // length of that list
     __shared__ int sXc[4];      // node-changing particles per class (x, y, z only; several)
 
@@ -643,21 +663,7 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
 
     // 1. stage E and B_m (field tile origin = array index (i0 + OS - 1)) and clear J
     if constexpr( TMA ) {
-        if( threadIdx.x == 0 ) {
-            const unsigned mb = ( unsigned )__cvta_generic_to_shared( &sTmaBar );
-            // the previous tile's reads of sF come before these asynchronous writes
-            asm volatile( "fence.proxy.async.shared::cta;\n" ::: "memory" );
-            asm volatile( "mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"( mb ), "r"( TMA_TX_BYTES ) : "memory" );
-            // box origin: z at the tile's first node (16-byte aligned), y and x one node below
-            const int z0 = iz0, y0 = iy0 + OS - 1, x0 = ix0 + OS - 1;
-#pragma unroll
-            for( int c = 0; c < 6; c++ ) {
-                const unsigned dst = ( unsigned )__cvta_generic_to_shared( sF + c * fsz );
-                asm volatile( "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n"
-                              ::"r"( dst ), "l"( reinterpret_cast<uint64_t>( &tma.m[c] ) ), "r"( z0 ), "r"( y0 ), "r"( x0 ), "r"( mb )
-                              : "memory" );
-            }
-        }
+        if( threadIdx.x == 0 ) tma_issue( tma, &sTmaBar, sF, fsz, ix0, iy0, iz0 );
         tma_pending = true;
     }
     const TileMap fm = tile_map<DIM>( td.FY, td.FZ );
@@ -708,6 +714,13 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
     for( int c0 = 0; c0 < ( CELLS ? ntot : 1 ); c0 += ( CELLS ? nmax : 1 ) ) {
     const int n = CELLS ? min( nmax, ntot - c0 ) : ntot;
     const int64_t s0 = seg0 + c0;
+    if constexpr( TMA ) {
+        // the previous chunk kept its node-changing list in the field tile: stage it again
+        if( c0 > 0 ) {
+            if( threadIdx.x == 0 ) tma_issue( tma, &sTmaBar, sF, fsz, ix0, iy0, iz0 );
+            tma_pending = true;
+        }
+    }
     if constexpr( CELLS ) {
         // rank of every particle inside its cell, then the cells' start offsets
         for( int c = threadIdx.x; c < TC; c += blockDim.x ) sCnt[c] = 0;
@@ -1089,26 +1102,15 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
                 run += c;
             }
         }
-        // in place: every thread holds its entries (at most XL of them: nmax <= 128 XL)
-        // while the list is rewritten grouped
-        int xq[XL], xc[XL];
-#pragma unroll
-        for( int j = 0; j < XL; j++ ) {
-            const int k = ( int )threadIdx.x + j * ( int )blockDim.x;
-            xq[j] = -1;
-            if( k < sNX ) {
-                const int q = sRank[k];
-                const int sb = __float_as_int( sRec[6 * nmax + q] );
-                const int h0 = ( sb & 3 ) - 1, h1 = ( ( sb >> 2 ) & 3 ) - 1, h2 = ( ( sb >> 4 ) & 3 ) - 1;
-                const int nsh = ( h0 != 0 ) + ( h1 != 0 ) + ( h2 != 0 );
-                xq[j] = q;
-                xc[j] = nsh == 1 ? ( h0 != 0 ? 0 : ( h1 != 0 ? 1 : 2 ) ) : 3;
-            }
-        }
         __syncthreads();
-#pragma unroll
-        for( int j = 0; j < XL; j++ )
-            if( xq[j] >= 0 ) sRank[atomicAdd( &sXc[xc[j]], 1 )] = xq[j];
+        for( int k = threadIdx.x; k < sNX; k += blockDim.x ) {
+            const int q = sRank[k];
+            const int sb = __float_as_int( sRec[6 * nmax + q] );
+            const int h0 = ( sb & 3 ) - 1, h1 = ( ( sb >> 2 ) & 3 ) - 1, h2 = ( ( sb >> 4 ) & 3 ) - 1;
+            const int nsh = ( h0 != 0 ) + ( h1 != 0 ) + ( h2 != 0 );
+            const int cls = nsh == 1 ? ( h0 != 0 ? 0 : ( h1 != 0 ? 1 : 2 ) ) : 3;
+            sXs[atomicAdd( &sXc[cls], 1 )] = q;
+        }
         __syncthreads();
     }
 
@@ -1247,7 +1249,7 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
         // node-changing particles, one per thread, into their own tile (after the
         // per-cell pass: warps that finish their cells early start on this list)
         for( int k = threadIdx.x; k < sNX; k += blockDim.x ) {
-            const int q = sRank[k];
+            const int q = sXs[k];
             const int lc = sSlotCell[q];
             int cl[3];
             if( DIM == 3 ) {
@@ -1275,6 +1277,8 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
             const T crz = cw0 * wq * vz;
             deposit_direct<DIM, T>( sJ2, td, jsz, cl, W, cr, crz );
         }
+        // the list's reads of the field tile come before the next staging's writes
+        if constexpr( TMA ) asm volatile( "fence.proxy.async.shared::cta;\n" ::: "memory" );
         __syncthreads();
     }
     } // chunk
@@ -2448,7 +2452,7 @@ int launch_particles( sg_sim *S, SpeciesState &s, cudaStream_t st, int t0, int t
                 if( S->tma && ft == 1 ) {
                     kern = k_step_particles<3, true, KIND, true, 1, true>;
                     chunk = tma_chunk();
-                    smem = TMA_TILE_BYTES + cells_smem_bytes( tc, chunk );
+                    smem = TMA_TILE_BYTES + cells_smem_bytes( tc, chunk, true );
                 }
             }
         }
@@ -3162,6 +3166,14 @@ int sg_sim_create( const sg_sim_config *cfg, sg_sim **out )
         return cuda_fail( e, "sg_sim_create allocations", __FILE__, __LINE__ );
     }
     S->own_stream = true;
+    // the 3D mixed form with 4x4x4 tiles on a periodic grid stages its field tile by TMA
+    if( g.ndim == 3 && S->mixed && g.T[0] == 4 && g.T[1] == 4 && g.T[2] == 4 && !g.open[0] && !g.open[1] && !g.open[2] ) {
+        const int r = sg_sim_set_tma_staging( S, 1 );
+        if( r ) {
+            sg_sim_destroy( S );
+            return r;
+        }
+    }
     *out = S;
     return SG_OK;
 }

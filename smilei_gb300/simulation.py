@@ -68,8 +68,8 @@ class Simulation:
         check(_lib.lib().sg_sim_set_tile_queue(self._h, int(bool(on))), "set_tile_queue")
 
     def set_tma_staging(self, on: bool = True):
-        """Field tile staged by the tensor memory accelerator (3D mixed form, 4x4x4 tiles)
-        instead of word copies (the default)."""
+        """Field tile staged by the tensor memory accelerator (on: the default of the 3D
+        mixed form with 4x4x4 periodic tiles) or by word copies (off)."""
         check(_lib.lib().sg_sim_set_tma_staging(self._h, int(bool(on))), "set_tma_staging")
 
     # -- species -----------------------------------------------------------

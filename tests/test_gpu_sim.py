@@ -48,8 +48,8 @@ def run_pair(sim_mod, cpu_oracle, ndim, form, nsteps, species_spec, seed=5, tile
         sim.add_species(s["mass"], s["q"], s["pusher"], s["pos"], s["mom"], s["weight"])
     if tile_queue:
         sim.set_tile_queue(True)
-    if tma:
-        sim.set_tma_staging(True)
+    if ndim == 3 and form == "mixed" and tile in (None, [4, 4, 4]):
+        sim.set_tma_staging(tma)  # TMA is this case's default: off tests the word copies
     sim.step(nsteps)
     ref = {k: v.copy() for k, v in fields.items()}
     ref_sp = [dict(s, pos=s["pos"].copy(), mom=s["mom"].copy()) for s in species]
@@ -297,14 +297,17 @@ def test_tile_queue_step_matches_oracle(sim_mod, cpu_oracle, ndim, form, tol):
         assert position_error(pg, pr, cl, n_cells) <= tol * 10
 
 
-@pytest.mark.parametrize("pusher,ppc", [("higueracary", 6), ("boris", 64)])
-def test_tma_staging_step_matches_oracle(sim_mod, cpu_oracle, pusher, ppc):
+@pytest.mark.parametrize("pusher,ppc,queue", [("higueracary", 6, False), ("boris", 64, False), ("vay", 40, True)])
+def test_tma_staging_step_matches_oracle(sim_mod, cpu_oracle, pusher, ppc, queue):
     """The field tile staged by TMA (tensor copies of padded E and B_m, one mbarrier per
     tile) gives the oracle's step like the word copies: 3 graph-replayed steps of the
     16 x 12 x 8 grid (tiles at every grid edge, so boxes reach past the arrays and read
-    the tensor maps' zero fill), and a dense case whose tiles take several chunks."""
+    the tensor maps' zero fill), and dense cases whose tiles take several chunks (each
+    chunk after the first stages the field tile again: the previous chunk kept its
+    node-changing list there), one of them with the persistent tile queue."""
     spec = [(1.0, -1.0, pusher, ppc, 0.14)]
-    got, ref, parts = run_pair(sim_mod, cpu_oracle, 3, "mixed", 3 if ppc < 32 else 1, spec, tma=True)
+    got, ref, parts = run_pair(sim_mod, cpu_oracle, 3, "mixed", 3 if ppc < 32 else 1, spec, tma=True,
+                               tile_queue=queue)
     tol = 1e-4 if ppc < 32 else 1e-5
     for k in FIELDS:
         assert rel_err(got[k], ref[k]) <= tol, k
