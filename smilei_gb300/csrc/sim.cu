@@ -270,6 +270,7 @@ __device__ __forceinline__ T push_t( T qm, T Ex, T Ey, T Ez, T Bx, T By, T Bz, T
 struct TileDims {
     int FX, FY, FZ; // field tile extents (T + 3)
     int JX, JY, JZ; // current tile extents (T + 4)
+    int JXS;        // current tile x stride: JY JZ, in 3D plus 4 words (below)
 };
 
 __host__ __device__ inline TileDims tile_dims( const GridInfo &g )
@@ -281,8 +282,16 @@ __host__ __device__ inline TileDims tile_dims( const GridInfo &g )
     t.JX = g.T[0] + 4;
     t.JY = g.T[1] + 4;
     t.JZ = g.ndim == 3 ? g.T[2] + 4 : 1;
+    // 3D: an x stride of 4 (mod 32) words puts the 4 x 4 x 4 cells of a 4^3 tile on the
+    // 32 banks two by two (4 cx + 8 cy + cz), where JY JZ = 64 put them four by four
+    // (8 cy + cz): the deposit's lanes, one per particle or per cell, conflict less
+    t.JXS = t.JY * t.JZ + ( g.ndim == 3 ? 4 : 0 );
     return t;
 }
+
+// Words of one current component tile (the last x plane is not padded).
+__host__ __device__ inline int jtile_size( const TileDims &t ) { return ( t.JX - 1 ) * t.JXS + t.JY * t.JZ; }
+constexpr int jtile3_size( int t ) { return ( t + 3 ) * ( ( t + 4 ) * ( t + 4 ) + 4 ) + ( t + 4 ) * ( t + 4 ); }
 
 // Gather one component from the shared tile: sum_a cx[a] sum_b cy[b] sum_c cz[c] F.
 template <int DIM, class T>
@@ -339,6 +348,27 @@ __device__ __forceinline__ float2 gather_pair( const float *__restrict__ F1, con
         r = __ffma2_rn( make_float2( cx1[a], cx2[a] ), ra, r );
     }
     return r;
+}
+
+// FP32 to FP64 with integer operations: this GPU runs FP64 adds and conversions on its
+// FP64 pipe at 1/64 of the FP32 rate.  Zeros, subnormals, infinities and NaNs take the
+// conversion instruction.
+__device__ __forceinline__ double widen( float x )
+{
+    const unsigned u = __float_as_uint( x ), ex = ( u >> 23 ) & 0xffu;
+    if( ( u << 1 ) == 0u ) return __hiloint2double( ( int )( u & 0x80000000u ), 0 );
+    if( ex == 0u || ex == 0xffu ) return ( double )x;
+    const unsigned hi = ( u & 0x80000000u ) | ( ( ex + 896u ) << 20 ) | ( ( u & 0x7fffffu ) >> 3 );
+    return __hiloint2double( ( int )hi, ( int )( u << 29 ) );
+}
+
+// A current-tile value for the FP64 arrays.  The per-cell mode's two FP32 tiles (cell
+// sums, node-changing particles) are summed in FP32, one rounding, and widened.
+template <bool CELLS, class T>
+__device__ __forceinline__ double tile_value( const T *a, const T *b, int e )
+{
+    if constexpr( CELLS && sizeof( T ) == 4 ) return widen( a[e] + b[e] );
+    else return ( double )a[e];
 }
 
 template <class T>
@@ -415,25 +445,36 @@ __device__ __forceinline__ void deposit_direct( T *sJ, const TileDims &td, int j
 {
     const T twelfth = T( 1.0 / 12.0 );
     if( DIM == 3 ) {
-#pragma unroll
+        // one component per pass of a loop that is not unrolled (a small body: this code
+        // runs once per tile); after each pass the dimensions rotate, (a, b, e) ->
+        // (b, e, a), so the current's dimension a is always Wa
+        EsirWin<T> Wa = W[0], Wb = W[1], We = W[2];
+        int la = lx[0], lb = lx[1], le = lx[2];
+        int sa = td.JXS, sb = td.JZ, se = 1;
+        T ca = cr[0], cb = cr[1], ce = cr[2];
+        T *J = sJ;
+#pragma unroll 1
         for( int c = 0; c < 3; c++ ) {
-            if( !( ( cmask >> c ) & 1u ) ) continue;
-            const int a = c, b = ( c + 1 ) % 3, e = ( c + 2 ) % 3;
-            T *J = sJ + c * jsz;
+            if( ( cmask >> c ) & 1u ) {
 #pragma unroll
-            for( int u = 0; u < 4; u++ )
+                for( int u = 0; u < 4; u++ )
 #pragma unroll
-                for( int v = 0; v < 4; v++ ) {
-                    const T wgt = W[b].A[u] * W[e].A[v] + twelfth * W[b].D[u] * W[e].D[v];
-                    int idx[3];
-                    idx[b] = lx[b] + W[b].lo + u;
-                    idx[e] = lx[e] + W[e].lo + v;
+                    for( int v = 0; v < 4; v++ ) {
+                        const T wgt = Wb.A[u] * We.A[v] + twelfth * Wb.D[u] * We.D[v];
+                        const int base = ( la + Wa.lo + 1 ) * sa + ( lb + Wb.lo + u ) * sb + ( le + We.lo + v ) * se;
 #pragma unroll
-                    for( int m = 0; m < 3; m++ ) {
-                        idx[a] = lx[a] + W[a].lo + 1 + m;
-                        sh_add( &J[( idx[0] * td.JY + idx[1] ) * td.JZ + idx[2]], -cr[a] * W[a].P[m] * wgt );
+                        for( int m = 0; m < 3; m++ ) sh_add( &J[base + m * sa], -ca * Wa.P[m] * wgt );
                     }
-                }
+            }
+            const EsirWin<T> tw = Wa;
+            Wa = Wb; Wb = We; We = tw;
+            int ti = la;
+            la = lb; lb = le; le = ti;
+            ti = sa;
+            sa = sb; sb = se; se = ti;
+            const T tc = ca;
+            ca = cb; cb = ce; ce = tc;
+            J += jsz;
         }
     } else {
         T *J0 = sJ, *J1 = sJ + jsz, *J2 = sJ + 2 * jsz;
@@ -443,7 +484,7 @@ __device__ __forceinline__ void deposit_direct( T *sJ, const TileDims &td, int j
                 const T ay = W[1].A[u];
 #pragma unroll
                 for( int m = 0; m < 3; m++ )
-                    sh_add( &J0[( lx[0] + W[0].lo + 1 + m ) * td.JY + lx[1] + W[1].lo + u], -cr[0] * W[0].P[m] * ay );
+                    sh_add( &J0[( lx[0] + W[0].lo + 1 + m ) * td.JXS + lx[1] + W[1].lo + u], -cr[0] * W[0].P[m] * ay );
             }
         }
         if( cmask & 2u ) {
@@ -452,7 +493,7 @@ __device__ __forceinline__ void deposit_direct( T *sJ, const TileDims &td, int j
                 const T ax = W[0].A[u];
 #pragma unroll
                 for( int m = 0; m < 3; m++ )
-                    sh_add( &J1[( lx[0] + W[0].lo + u ) * td.JY + lx[1] + W[1].lo + 1 + m], -cr[1] * W[1].P[m] * ax );
+                    sh_add( &J1[( lx[0] + W[0].lo + u ) * td.JXS + lx[1] + W[1].lo + 1 + m], -cr[1] * W[1].P[m] * ax );
             }
         }
         if( cmask & 4u ) {
@@ -461,8 +502,93 @@ __device__ __forceinline__ void deposit_direct( T *sJ, const TileDims &td, int j
 #pragma unroll
                 for( int v = 0; v < 4; v++ ) {
                     const T wz = W[0].A[u] * W[1].A[v] + twelfth * W[0].D[u] * W[1].D[v];
-                    sh_add( &J2[( lx[0] + W[0].lo + u ) * td.JY + lx[1] + W[1].lo + v], crz * wz );
+                    sh_add( &J2[( lx[0] + W[0].lo + u ) * td.JXS + lx[1] + W[1].lo + v], crz * wz );
                 }
+        }
+    }
+}
+
+// Footprint weights of one dimension for the per-cell deposit: S0 (old weights o) and
+// S1 (new weights n, on the new node) on the old node's stencil points 1..3.  A shift
+// s = +-1 moves S1 by s; the weight it moves out of the footprint (to point 4 for s = 1,
+// 0 for s = -1) is returned in nov.  A = (S0 + S1) / 2, D = S1 - S0, P = the running
+// sums of S1 - S0 up to points 1 and 2 (the current at points 2 and 3; point 0 holds
+// nov when s = -1).
+template <class T>
+__device__ __forceinline__ void footprint_weights( T dold, T dnew, int s, T *A, T *D, T *P, T &nov )
+{
+    T o0, o1, o2, n0, n1, n2;
+    dep_spline( dold, o0, o1, o2 );
+    dep_spline( dnew, n0, n1, n2 );
+    const T f0 = s > 0 ? T( 0 ) : ( s < 0 ? n1 : n0 );
+    const T f1 = s > 0 ? n0 : ( s < 0 ? n2 : n1 );
+    const T f2 = s > 0 ? n1 : ( s < 0 ? T( 0 ) : n2 );
+    nov = s > 0 ? n2 : n0;
+    A[0] = T( 0.5 ) * ( o0 + f0 ); A[1] = T( 0.5 ) * ( o1 + f1 ); A[2] = T( 0.5 ) * ( o2 + f2 );
+    D[0] = f0 - o0; D[1] = f1 - o1; D[2] = f2 - o2;
+    P[0] = D[0] + ( s < 0 ? nov : T( 0 ) );
+    P[1] = P[0] + D[1];
+}
+
+// The part of a 3D Esirkepov deposit outside the old cell's footprint, for a particle
+// that changes node in dimension DS only (shift sg): the window reaches one plane
+// further, stencil point 4 for sg = 1, for sg = -1 point 0 across the current and
+// point 1 along it.  Along DS: J_DS at that point over the (B, E) footprint gets
+// -cr Q (A_B A_E + D_B D_E / 12), Q = the sum of S1 - S0 before it (-nov or nov).
+// Across: J_C (C != DS) at its two footprint points along C, plane pt of DS, the
+// footprint of the third dimension, gets -cr_C P_C (A_ov A_t + D_ov D_t / 12) with
+// A_ov = nov / 2, D_ov = nov (S0 is zero there).  21 points in all; the per-cell
+// pass adds the footprint part.
+template <class T>
+__device__ __forceinline__ void deposit_overhang( T *J2, const TileDims &td, int jsz, const int *cl, const T ( *A )[3],
+                                                  const T ( *D )[3], const T ( *P )[2], const T *cr, const T *nov,
+                                                  const int *sh )
+{
+    // the frame (a, b, e) = (DS, DS + 1, DS + 2) mod 3, selected once: one body serves
+    // the three dimensions (this code runs once per tile, so it is kept small)
+    const int ds = sh[0] != 0 ? 0 : ( sh[1] != 0 ? 1 : 2 );
+    const int sg = ds == 0 ? sh[0] : ( ds == 1 ? sh[1] : sh[2] );
+    const T nv = ds == 0 ? nov[0] : ( ds == 1 ? nov[1] : nov[2] );
+#define SG_ROT( x0, x1, x2, k ) ( ds == 0 ? ( k == 0 ? x0 : k == 1 ? x1 : x2 ) : ds == 1 ? ( k == 0 ? x1 : k == 1 ? x2 : x0 ) : ( k == 0 ? x2 : k == 1 ? x0 : x1 ) )
+    const int stride[3] = { td.JXS, td.JZ, 1 };
+    const int sa = SG_ROT( stride[0], stride[1], stride[2], 0 ), sb = SG_ROT( stride[0], stride[1], stride[2], 1 ),
+              se = SG_ROT( stride[0], stride[1], stride[2], 2 );
+    const int la = SG_ROT( cl[0], cl[1], cl[2], 0 ), lb = SG_ROT( cl[0], cl[1], cl[2], 1 ), le = SG_ROT( cl[0], cl[1], cl[2], 2 );
+    const T cra = SG_ROT( cr[0], cr[1], cr[2], 0 ), crb = SG_ROT( cr[0], cr[1], cr[2], 1 ), cre = SG_ROT( cr[0], cr[1], cr[2], 2 );
+    T *Ja = J2 + SG_ROT( 0, 1, 2, 0 ) * jsz, *Jb = J2 + SG_ROT( 0, 1, 2, 1 ) * jsz, *Je = J2 + SG_ROT( 0, 1, 2, 2 ) * jsz;
+    T Ab[3], Db[3], Ae[3], De[3], Pb[2], Pe[2];
+#pragma unroll
+    for( int i = 0; i < 3; i++ ) {
+        Ab[i] = SG_ROT( A[0][i], A[1][i], A[2][i], 1 );
+        Db[i] = SG_ROT( D[0][i], D[1][i], D[2][i], 1 );
+        Ae[i] = SG_ROT( A[0][i], A[1][i], A[2][i], 2 );
+        De[i] = SG_ROT( D[0][i], D[1][i], D[2][i], 2 );
+    }
+#pragma unroll
+    for( int i = 0; i < 2; i++ ) {
+        Pb[i] = SG_ROT( P[0][i], P[1][i], P[2][i], 1 );
+        Pe[i] = SG_ROT( P[0][i], P[1][i], P[2][i], 2 );
+    }
+#undef SG_ROT
+    const T twelfth = T( 1.0 / 12.0 );
+    const int pt = sg > 0 ? 4 : 0, pa = sg > 0 ? 4 : 1;
+    const T qov = sg > 0 ? -nv : nv, aov = T( 0.5 ) * nv, dov = twelfth * nv;
+    // along a: the (b, e) footprint at point pa
+    const T ca = -( cra * qov );
+#pragma unroll
+    for( int u = 0; u < 3; u++ )
+#pragma unroll
+        for( int v = 0; v < 3; v++ )
+            sh_add( &Ja[( la + pa ) * sa + ( lb + 1 + u ) * sb + ( le + 1 + v ) * se],
+                    ca * ( Ab[u] * Ae[v] + twelfth * Db[u] * De[v] ) );
+    // across: J_b at its points 2, 3 along b, plane pt of a, the footprint of e; J_e the same with b and e swapped
+#pragma unroll
+    for( int w = 0; w < 3; w++ ) {
+        const T wte = aov * Ae[w] + dov * De[w], wtb = aov * Ab[w] + dov * Db[w];
+#pragma unroll
+        for( int m = 0; m < 2; m++ ) {
+            sh_add( &Jb[( lb + 2 + m ) * sb + ( la + pt ) * sa + ( le + 1 + w ) * se], -( crb * Pb[m] ) * wte );
+            sh_add( &Je[( le + 2 + m ) * se + ( la + pt ) * sa + ( lb + 1 + w ) * sb], -( cre * Pe[m] ) * wtb );
         }
     }
 }
@@ -524,18 +650,18 @@ constexpr int ft_shift( int t ) { return t == 16 ? 4 : ( t == 8 ? 3 : ( t == 4 ?
 // points per dimension.
 constexpr int fixt_chunk( int dim, int ft )
 {
-    return dim == 3 ? cells_chunk_fit( ( size_t )( 6 * 7 * 7 * 7 + 6 * 8 * 8 * 8 ) * 4, 64 ) & ~31
+    return dim == 3 ? cells_chunk_fit( ( size_t )( 6 * 7 * 7 * 7 + 6 * jtile3_size( 4 ) ) * 4, 64 ) & ~31
                     : cells_chunk_fit( ( size_t )( 6 * ( ft_tile( 2, ft, 0 ) + 3 ) * ( ft_tile( 2, ft, 1 ) + 3 ) +
                                                    6 * ( ft_tile( 2, ft, 0 ) + 4 ) * ( ft_tile( 2, ft, 1 ) + 4 ) ) * 4,
                                        ft_tile( 2, ft, 0 ) * ft_tile( 2, ft, 1 ) ) & ~31;
 }
 
 // The per-cell mode's second current tile (node-changing particles), FP32.
-inline size_t cells_j2_bytes( const TileDims &td ) { return ( size_t )3 * td.JX * td.JY * td.JZ * 4; }
+inline size_t cells_j2_bytes( const TileDims &td ) { return ( size_t )3 * jtile_size( td ) * 4; }
 
 // The 3D default tile's chunk with TMA staging: the padded field tile (6 TMA_FSZ floats)
 // and 128 bytes to align the dynamic shared memory.
-constexpr size_t TMA_TILE_BYTES = ( size_t )( 6 * TMA_FSZ + 6 * 8 * 8 * 8 ) * 4 + 128;
+constexpr size_t TMA_TILE_BYTES = ( size_t )( 6 * TMA_FSZ + 6 * jtile3_size( 4 ) ) * 4 + 128;
 constexpr int tma_chunk() { return cells_chunk_fit( TMA_TILE_BYTES, 64, true ) & ~31; }
 
 // FT > 0: the tile shape is known at compile time, so tile and stencil offsets fold into
@@ -603,15 +729,15 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
     TileDims td = tile_dims( g );
     if constexpr( TMA ) td.FZ = TMA_BOX_Z;
     const int fsz = TMA ? TMA_FSZ : td.FX * td.FY * td.FZ;
-    const int jsz = td.JX * td.JY * td.JZ;
+    const int jsz = jtile_size( td );
     T *sJ = sF + 6 * fsz;
     // per-cell mode (CELLS): particle planes, per-cell counts and starts, each
     // particle's (cell << 16 | rank in cell), each slot's cell
     const int TC = g.T[0] * g.T[1] * ( DIM == 3 ? g.T[2] : 1 );
-    // per-cell mode: node-changing particles deposit into a second tile sJ2.  Their many
-    // single adds then round against their own small partial sums, not against the
-    // per-cell sums (an FP32 add's error is about an ulp of the partial sum); the two
-    // tiles are summed in FP64 at the flush.
+    // per-cell mode: node-changing particles deposit into a second tile sJ2 (in 3D the
+    // part of their window outside the cell's footprint).  Their single adds then round
+    // against their own small partial sums, not against the per-cell sums (an FP32 add's
+    // error is about an ulp of the partial sum); the flush adds the two tiles.
     T *sJ2 = sJ + 3 * jsz;
     float *sRec = reinterpret_cast<float *>( sJ2 + ( CELLS ? 3 * jsz : 0 ) );
     int *sCnt = reinterpret_cast<int *>( sRec + ( CELLS ? REC * nmax : 0 ) );
@@ -994,12 +1120,12 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
         }
 
         if constexpr( CELLS ) {
-            // node-changing particles go to a list deposited with full warps later
-            const bool cross = valid && !gone && ( shift[0] | shift[1] | shift[2] ) != 0;
-            if( cross ) {
-                const int nsh = ( shift[0] != 0 ) + ( shift[1] != 0 ) + ( shift[2] != 0 );
-                atomicAdd( &sXc[nsh == 1 ? ( shift[0] != 0 ? 0 : ( shift[1] != 0 ? 1 : 2 ) ) : 3], 1 );
-            }
+            // node-changing particles go to a list deposited with full warps later (3D: the
+            // per-cell pass takes the footprint part of those that change node in one
+            // dimension, the list the plane beyond it)
+            const int nshift = ( shift[0] != 0 ) + ( shift[1] != 0 ) + ( shift[2] != 0 );
+            const bool cross = valid && !gone && nshift > 0;
+            if( cross ) atomicAdd( &sXc[nshift == 1 ? ( shift[0] != 0 ? 0 : ( shift[1] != 0 ? 1 : 2 ) ) : 3], 1 );
             const unsigned xm = __ballot_sync( 0xffffffffu, cross );
             if( xm ) {
                 int xb = 0;
@@ -1117,8 +1243,11 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
     // 3. per-cell deposit (CELLS).  Particles that stay on their node in every
     // dimension share their cell's fixed footprint: stencil points 1..3 across the
     // current, 2..3 along it (point 4 carries a sum that is exactly zero).  Their
-    // contributions are summed in registers and added once per cell; particles that
-    // change node are deposited directly (into sJ2).  3D: thread
+    // contributions are summed in registers and added once per cell.  In 3D so is the
+    // footprint part of a particle that changes node in one dimension (its new weights
+    // moved by the shift); the node-changing pass adds the plane beyond.  Particles
+    // that change node in more dimensions (3D) or at all (2D) are deposited directly
+    // (into sJ2).  3D: thread
     // t works on cell t % TC, group j = t / TC; even groups own Jx and the lower
     // Jz plane, odd groups Jy and the upper one; groups j>>1 split the records.
     // 2D: the groups split the records and own all three components.
@@ -1153,7 +1282,18 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
             }
             const int end = sStart[c] + sCnt[c];
             for( int q = sStart[c] + q0; q < end; q += qstep ) {
-                if( __float_as_int( sRec[6 * nmax + q] ) != NO_SHIFT ) continue; // in the node-changing list
+                const int sb = __float_as_int( sRec[6 * nmax + q] );
+                int sh[3] = { 0, 0, 0 };
+                if constexpr( DIM == 3 ) {
+                    // a particle that changes node in one dimension stays here (the rest
+                    // are in the node-changing list, and a removed one deposits nothing)
+                    sh[0] = ( sb & 3 ) - 1;
+                    sh[1] = ( ( sb >> 2 ) & 3 ) - 1;
+                    sh[2] = ( ( sb >> 4 ) & 3 ) - 1;
+                    if( sb == GONE_RECORD || ( sh[0] != 0 ) + ( sh[1] != 0 ) + ( sh[2] != 0 ) > 1 ) continue;
+                } else {
+                    if( sb != NO_SHIFT ) continue; // in the node-changing list
+                }
                 T dold[3], dn[3];
                 dold[0] = sRec[q];
                 dold[1] = sRec[nmax + q];
@@ -1168,13 +1308,8 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
                     T A[3][3], D[3][3], P[3][2];
 #pragma unroll
                     for( int d = 0; d < DIM; d++ ) {
-                        T o0, o1, o2, n0, n1, n2;
-                        dep_spline( dold[d], o0, o1, o2 );
-                        dep_spline( dn[d], n0, n1, n2 );
-                        A[d][0] = T( 0.5 ) * ( o0 + n0 ); A[d][1] = T( 0.5 ) * ( o1 + n1 ); A[d][2] = T( 0.5 ) * ( o2 + n2 );
-                        D[d][0] = n0 - o0; D[d][1] = n1 - o1; D[d][2] = n2 - o2;
-                        P[d][0] = D[d][0];
-                        P[d][1] = D[d][0] + D[d][1];
+                        T nov; // (the node-changing pass deposits the plane beyond the footprint)
+                        footprint_weights<T>( dold[d], dn[d], sh[d], A[d], D[d], P[d], nov );
                     }
                     if( DIM == 3 ) {
                         // along-axis a = hf, transverse b = 1 - hf and 2
@@ -1222,10 +1357,10 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
 #pragma unroll
                         for( int m = 0; m < 2; m++ ) {
                             const int ia = ( hf ? cl[0] + 1 + u : cl[0] + 2 + m ), ib = ( hf ? cl[1] + 2 + m : cl[1] + 1 + u );
-                            const int ea = ( ia * td.JY + ib ) * td.JZ + cl[2] + 1 + v;
+                            const int ea = ia * td.JXS + ib * td.JZ + cl[2] + 1 + v;
                             sh_add( &Ja[ea], m == 0 ? acc2[u * 3 + v].x : acc2[u * 3 + v].y );
                         }
-                        const int ez = ( ( cl[0] + 1 + u ) * td.JY + cl[1] + 1 + v ) * td.JZ + cl[2] + 2 + hf;
+                        const int ez = ( cl[0] + 1 + u ) * td.JXS + ( cl[1] + 1 + v ) * td.JZ + cl[2] + 2 + hf;
                         sh_add( &Jz[ez], accz[u * 3 + v] );
                     }
             } else {
@@ -1234,13 +1369,13 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
                 for( int u = 0; u < 3; u++ ) {
 #pragma unroll
                     for( int m = 0; m < 2; m++ ) {
-                        const int e0 = ( cl[0] + 2 + m ) * td.JY + cl[1] + 1 + u, e1 = ( cl[0] + 1 + u ) * td.JY + cl[1] + 2 + m;
+                        const int e0 = ( cl[0] + 2 + m ) * td.JXS + cl[1] + 1 + u, e1 = ( cl[0] + 1 + u ) * td.JXS + cl[1] + 2 + m;
                         sh_add( &J0[e0], acc[m * 3 + u] );
                         sh_add( &J1[e1], acc[6 + u * 2 + m] );
                     }
 #pragma unroll
                     for( int v = 0; v < 3; v++ ) {
-                        const int e2 = ( cl[0] + 1 + u ) * td.JY + cl[1] + 1 + v;
+                        const int e2 = ( cl[0] + 1 + u ) * td.JXS + cl[1] + 1 + v;
                         sh_add( &J2[e2], accz[u * 3 + v] );
                     }
                 }
@@ -1265,6 +1400,17 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
             const int sh[3] = { ( sbits & 3 ) - 1, ( ( sbits >> 2 ) & 3 ) - 1, ( ( sbits >> 4 ) & 3 ) - 1 };
             const T wq = sRec[7 * nmax + q];
             const T cr[3] = { cr3[0] * wq, cr3[1] * wq, cr3[2] * wq };
+            if constexpr( DIM == 3 ) {
+                if( ( sh[0] != 0 ) + ( sh[1] != 0 ) + ( sh[2] != 0 ) == 1 ) {
+                    // one dimension: the per-cell pass took the footprint, this the plane beyond
+                    T A[3][3], D[3][3], P[3][2], nov[3];
+#pragma unroll
+                    for( int d = 0; d < 3; d++ )
+                        footprint_weights<T>( ( T )sRec[d * nmax + q], ( T )sRec[( 3 + d ) * nmax + q], sh[d], A[d], D[d], P[d], nov[d] );
+                    deposit_overhang<T>( sJ2, td, jsz, cl, A, D, P, cr, nov, sh );
+                    continue;
+                }
+            }
             const T vz = DIM == 3 ? T( 0 ) : sRec[5 * nmax + q];
             EsirWin<T> W[3];
 #pragma unroll
@@ -1304,19 +1450,19 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
             if( jm.active ) {
                 const int gy = iy0 + OS - 2 + jm.cy, gz = DIM == 3 ? iz0 + OS - 2 + jm.cz : 0;
                 for( int cx = jm.cx0; cx < td.JX; cx += jm.step ) {
-                    const int e = ( cx * td.JY + jm.cy ) * td.JZ + jm.cz;
-                    const double v = CELLS ? ( double )srcJ[e] + ( double )srcJ2[e] : ( double )srcJ[e];
+                    const int e = cx * td.JXS + jm.cy * td.JZ + jm.cz;
+                    const double v = tile_value<CELLS, T>( srcJ, srcJ2, e );
                     const int gx = ix0 + OS - 2 + cx;
                     if( v != 0.0 && gx < nx && gy < ny && gz < nz ) atomicAdd( &dstJ[( ( int64_t )gx * ny + gy ) * nz + gz], v );
                 }
             }
         } else {
             for( int e = threadIdx.x; e < jsz; e += blockDim.x ) {
-                const double v = CELLS ? ( double )srcJ[e] + ( double )srcJ2[e] : ( double )srcJ[e];
+                const double v = tile_value<CELLS, T>( srcJ, srcJ2, e );
                 if( v == 0.0 ) continue;
-                const int cz = e % td.JZ, cy = ( e / td.JZ ) % td.JY, cx = e / ( td.JZ * td.JY );
+                const int cx = e / td.JXS, r = e - cx * td.JXS, cy = r / td.JZ, cz = r - cy * td.JZ;
                 const int gx = ix0 + OS - 2 + cx, gy = iy0 + OS - 2 + cy, gz = DIM == 3 ? iz0 + OS - 2 + cz : 0;
-                if( gx < nx && gy < ny && gz < nz ) atomicAdd( &dstJ[( ( int64_t )gx * ny + gy ) * nz + gz], v );
+                if( cy < td.JY && gx < nx && gy < ny && gz < nz ) atomicAdd( &dstJ[( ( int64_t )gx * ny + gy ) * nz + gz], v );
             }
         }
     }
@@ -3063,7 +3209,7 @@ int choose_tiles( sg_sim *S )
     }
     g.ntiles = g.nt[0] * g.nt[1] * ( g.ndim == 3 ? g.nt[2] : 1 );
     const TileDims td = tile_dims( g );
-    S->smem_bytes = ( size_t )( 6 * td.FX * td.FY * td.FZ + 3 * td.JX * td.JY * td.JZ ) * S->esz;
+    S->smem_bytes = ( size_t )( 6 * td.FX * td.FY * td.FZ + 3 * jtile_size( td ) ) * S->esz;
     if( S->smem_bytes > 200 * 1024 ) return set_error( SG_ERR_ARG, "tile too large for shared memory (%zu bytes)", S->smem_bytes );
     return SG_OK;
 }
