@@ -103,6 +103,7 @@ struct SpecParams {
     double cw;       // charge * inverse cell volume (per unit weight)
     double cr[3];    // cw * dx_d / dt: Esirkepov current factor per unit weight
     double vs[3];    // dt / dx_d: displacement in cells per unit velocity
+    float f_qm_dts2, f_cw, f_cr[3], f_vs[3]; // the same in FP32 (the mixed form's kernel reads these)
     int tile0;       // first tile of the launch (block b steps tile tile0 + b)
     int *queue;        // persistent launch: counter of the next item (null: one CTA per tile)
     const int *order;  // tile of each item, relative to tile0 (null: item itself)
@@ -350,26 +351,41 @@ __device__ __forceinline__ float2 gather_pair( const float *__restrict__ F1, con
     return r;
 }
 
-// FP32 to FP64 with integer operations: this GPU runs FP64 adds and conversions on its
-// FP64 pipe at 1/64 of the FP32 rate.  Zeros, subnormals, infinities and NaNs take the
-// conversion instruction.
+// FP32 to FP64 with integer operations (exact, every class of value): this GPU runs
+// FP64 adds, compares and conversions on its FP64 pipe at 1/64 of the FP32 rate.
 __device__ __forceinline__ double widen( float x )
 {
-    const unsigned u = __float_as_uint( x ), ex = ( u >> 23 ) & 0xffu;
-    if( ( u << 1 ) == 0u ) return __hiloint2double( ( int )( u & 0x80000000u ), 0 );
-    if( ex == 0u || ex == 0xffu ) return ( double )x;
-    const unsigned hi = ( u & 0x80000000u ) | ( ( ex + 896u ) << 20 ) | ( ( u & 0x7fffffu ) >> 3 );
-    return __hiloint2double( ( int )hi, ( int )( u << 29 ) );
+    const unsigned u = __float_as_uint( x ), sgn = u & 0x80000000u, ex = ( u >> 23 ) & 0xffu, man = u & 0x7fffffu;
+    unsigned e64, frac; // FP64 exponent field, 23-bit fraction
+    if( ex - 1u < 254u ) {
+        e64 = ex + 896u; // normal: 1023 - 127
+        frac = man;
+    } else if( ex == 0xffu ) {
+        e64 = 0x7ffu; // infinity, NaN
+        frac = man;
+    } else if( man == 0u ) {
+        e64 = 0u; // zero
+        frac = 0u;
+    } else {
+        // subnormal: man 2^-149 = 1.f 2^(p - 149), p = the leading bit of man
+        const int p = 31 - __clz( man );
+        e64 = ( unsigned )( p + 874 );
+        frac = ( man << ( 23 - p ) ) & 0x7fffffu;
+    }
+    return __hiloint2double( ( int )( sgn | ( e64 << 20 ) | ( frac >> 3 ) ), ( int )( frac << 29 ) );
 }
 
-// A current-tile value for the FP64 arrays.  The per-cell mode's two FP32 tiles (cell
-// sums, node-changing particles) are summed in FP32, one rounding, and widened.
+// A current-tile value: the per-cell mode's two FP32 tiles (cell sums, node-changing
+// particles) summed in FP32, one rounding.  to_global widens it for the FP64 arrays
+// (the zero test stays in the tile's type: an FP64 compare also takes the FP64 pipe).
 template <bool CELLS, class T>
-__device__ __forceinline__ double tile_value( const T *a, const T *b, int e )
+__device__ __forceinline__ T tile_value( const T *a, const T *b, int e )
 {
-    if constexpr( CELLS && sizeof( T ) == 4 ) return widen( a[e] + b[e] );
-    else return ( double )a[e];
+    if constexpr( CELLS ) return a[e] + b[e];
+    else return a[e];
 }
+__device__ __forceinline__ double to_global( float v ) { return widen( v ); }
+__device__ __forceinline__ double to_global( double v ) { return v; }
 
 template <class T>
 __device__ __forceinline__ void sh_add( T *a, T v )
@@ -404,8 +420,10 @@ __device__ __forceinline__ void dep_spline( T d, T &c0, T &c1, T &c2 )
 {
     bspline2( d, c0, c1, c2 );
     if constexpr( sizeof( T ) == 4 ) {
-        c0 = rintf( c0 * 16777216.0f ) * ( 1.0f / 16777216.0f );
-        c2 = rintf( c2 * 16777216.0f ) * ( 1.0f / 16777216.0f );
+        // c0, c2 lie in [0, 1/2]: adding 1/2 rounds them to the 2^-24 grid (to nearest,
+        // ties to even, as rint(c 2^24) 2^-24) with one FP32 add
+        c0 = __fsub_rn( __fadd_rn( c0, 0.5f ), 0.5f );
+        c2 = __fsub_rn( __fadd_rn( c2, 0.5f ), 0.5f );
         c1 = ( 1.0f - c0 ) - c2;
     }
 }
@@ -825,10 +843,13 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
     if constexpr( !CELLS ) cp_async_wait_all();
     __syncthreads();
 
-    const T qm = T( sp.qm_dts2 );
-    const T vs[3] = { T( sp.vs[0] ), T( sp.vs[1] ), T( sp.vs[2] ) };
-    const T cr3[3] = { T( sp.cr[0] ), T( sp.cr[1] ), T( sp.cr[2] ) };
-    const T cw0 = T( sp.cw );
+    // (FP32 copies for the mixed form: a conversion from FP64 takes the FP64 pipe)
+    const T qm = MIXED ? T( sp.f_qm_dts2 ) : T( sp.qm_dts2 );
+    const T vs[3] = { MIXED ? T( sp.f_vs[0] ) : T( sp.vs[0] ), MIXED ? T( sp.f_vs[1] ) : T( sp.vs[1] ),
+                      MIXED ? T( sp.f_vs[2] ) : T( sp.vs[2] ) };
+    const T cr3[3] = { MIXED ? T( sp.f_cr[0] ) : T( sp.cr[0] ), MIXED ? T( sp.f_cr[1] ) : T( sp.cr[1] ),
+                       MIXED ? T( sp.f_cr[2] ) : T( sp.cr[2] ) };
+    const T cw0 = MIXED ? T( sp.f_cw ) : T( sp.cw );
     const unsigned lane = threadIdx.x & 31u;
 
     // Per-cell mode takes the tile's particles in chunks of at most nmax (the
@@ -1451,18 +1472,19 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
                 const int gy = iy0 + OS - 2 + jm.cy, gz = DIM == 3 ? iz0 + OS - 2 + jm.cz : 0;
                 for( int cx = jm.cx0; cx < td.JX; cx += jm.step ) {
                     const int e = cx * td.JXS + jm.cy * td.JZ + jm.cz;
-                    const double v = tile_value<CELLS, T>( srcJ, srcJ2, e );
+                    const T v = tile_value<CELLS, T>( srcJ, srcJ2, e );
                     const int gx = ix0 + OS - 2 + cx;
-                    if( v != 0.0 && gx < nx && gy < ny && gz < nz ) atomicAdd( &dstJ[( ( int64_t )gx * ny + gy ) * nz + gz], v );
+                    if( v != T( 0 ) && gx < nx && gy < ny && gz < nz )
+                        atomicAdd( &dstJ[( ( int64_t )gx * ny + gy ) * nz + gz], to_global( v ) );
                 }
             }
         } else {
             for( int e = threadIdx.x; e < jsz; e += blockDim.x ) {
-                const double v = tile_value<CELLS, T>( srcJ, srcJ2, e );
-                if( v == 0.0 ) continue;
+                const T v = tile_value<CELLS, T>( srcJ, srcJ2, e );
+                if( v == T( 0 ) ) continue;
                 const int cx = e / td.JXS, r = e - cx * td.JXS, cy = r / td.JZ, cz = r - cy * td.JZ;
                 const int gx = ix0 + OS - 2 + cx, gy = iy0 + OS - 2 + cy, gz = DIM == 3 ? iz0 + OS - 2 + cz : 0;
-                if( cy < td.JY && gx < nx && gy < ny && gz < nz ) atomicAdd( &dstJ[( ( int64_t )gx * ny + gy ) * nz + gz], v );
+                if( cy < td.JY && gx < nx && gy < ny && gz < nz ) atomicAdd( &dstJ[( ( int64_t )gx * ny + gy ) * nz + gz], to_global( v ) );
             }
         }
     }
@@ -2560,6 +2582,12 @@ int launch_particles( sg_sim *S, SpeciesState &s, cudaStream_t st, int t0, int t
     for( int d = 0; d < 3; d++ ) {
         sp.cr[d] = sp.cw * S->g.dx[d] / S->g.dt;
         sp.vs[d] = S->g.dt * S->g.dxi[d];
+    }
+    sp.f_qm_dts2 = ( float )sp.qm_dts2;
+    sp.f_cw = ( float )sp.cw;
+    for( int d = 0; d < 3; d++ ) {
+        sp.f_cr[d] = ( float )sp.cr[d];
+        sp.f_vs[d] = ( float )sp.vs[d];
     }
     sp.tile0 = t0;
     if( t1 <= t0 ) return SG_OK;
