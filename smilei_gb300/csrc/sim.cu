@@ -621,21 +621,22 @@ constexpr int NO_SHIFT = 1 | ( 1 << 2 ) | ( 1 << 4 ); // packed shifts (s + 1 pe
 constexpr int GONE_RECORD = 1 << 8;                  // record of a particle removed at an open boundary: deposits nothing
 
 // Shared memory of the per-cell mode: REC planes of nmax floats, a count and a
-// start per cell, a packed (cell, rank) word and a list word per particle (with TMA
-// staging the list uses the field tile instead), a cell byte per slot.
+// start per cell, a packed (cell, rank) word per particle (later the node-changing
+// list), in 2D a word per particle for that list grouped by crossing dimension, a
+// cell byte per slot.
 constexpr size_t CELLS_SMEM_TARGET = 44 * 1024; // five 128-thread blocks per SM
-constexpr size_t cells_smem_bytes( int tc, int nmax, bool list_in_fields = false )
+constexpr size_t cells_smem_bytes( int tc, int nmax, bool grouped )
 {
-    return ( size_t )REC * 4 * nmax + ( size_t )8 * tc + ( size_t )( list_in_fields ? 4 : 8 ) * nmax +
+    return ( size_t )REC * 4 * nmax + ( size_t )8 * tc + ( size_t )( grouped ? 8 : 4 ) * nmax +
            ( ( ( size_t )nmax + 15 ) & ~( size_t )15 );
 }
 
 // Particles per chunk of the per-cell mode that fit CELLS_SMEM_TARGET with a tile
 // of tc cells whose field and current tiles take tile_bytes (0: none fit).
-constexpr int cells_chunk_fit( size_t tile_bytes, int tc, bool list_in_fields = false )
+constexpr int cells_chunk_fit( size_t tile_bytes, int tc, bool grouped )
 {
-    const size_t fixed = tile_bytes + cells_smem_bytes( tc, 0 ) + 16;
-    const size_t per = ( size_t )REC * 4 + ( list_in_fields ? 4 : 8 ) + 1; // planes, rank and list words, cell byte
+    const size_t fixed = tile_bytes + cells_smem_bytes( tc, 0, grouped ) + 16;
+    const size_t per = ( size_t )REC * 4 + ( grouped ? 8 : 4 ) + 1; // planes, rank (and list) words, cell byte
     return fixed < CELLS_SMEM_TARGET ? ( int )( ( CELLS_SMEM_TARGET - fixed ) / per ) : 0;
 }
 
@@ -668,10 +669,10 @@ constexpr int ft_shift( int t ) { return t == 16 ? 4 : ( t == 8 ? 3 : ( t == 4 ?
 // points per dimension.
 constexpr int fixt_chunk( int dim, int ft )
 {
-    return dim == 3 ? cells_chunk_fit( ( size_t )( 6 * 7 * 7 * 7 + 6 * jtile3_size( 4 ) ) * 4, 64 ) & ~31
+    return dim == 3 ? cells_chunk_fit( ( size_t )( 6 * 7 * 7 * 7 + 6 * jtile3_size( 4 ) ) * 4, 64, false ) & ~31
                     : cells_chunk_fit( ( size_t )( 6 * ( ft_tile( 2, ft, 0 ) + 3 ) * ( ft_tile( 2, ft, 1 ) + 3 ) +
                                                    6 * ( ft_tile( 2, ft, 0 ) + 4 ) * ( ft_tile( 2, ft, 1 ) + 4 ) ) * 4,
-                                       ft_tile( 2, ft, 0 ) * ft_tile( 2, ft, 1 ) ) & ~31;
+                                       ft_tile( 2, ft, 0 ) * ft_tile( 2, ft, 1 ), true ) & ~31;
 }
 
 // The per-cell mode's second current tile (node-changing particles), FP32.
@@ -680,7 +681,7 @@ inline size_t cells_j2_bytes( const TileDims &td ) { return ( size_t )3 * jtile_
 // The 3D default tile's chunk with TMA staging: the padded field tile (6 TMA_FSZ floats)
 // and 128 bytes to align the dynamic shared memory.
 constexpr size_t TMA_TILE_BYTES = ( size_t )( 6 * TMA_FSZ + 6 * jtile3_size( 4 ) ) * 4 + 128;
-constexpr int tma_chunk() { return cells_chunk_fit( TMA_TILE_BYTES, 64, true ) & ~31; }
+constexpr int tma_chunk() { return cells_chunk_fit( TMA_TILE_BYTES, 64, false ) & ~31; }
 
 // FT > 0: the tile shape is known at compile time, so tile and stencil offsets fold into
 // immediates; the chunk is fixt_chunk.
@@ -760,13 +761,15 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
     float *sRec = reinterpret_cast<float *>( sJ2 + ( CELLS ? 3 * jsz : 0 ) );
     int *sCnt = reinterpret_cast<int *>( sRec + ( CELLS ? REC * nmax : 0 ) );
     int *sStart = sCnt + TC;
-    int *sRank = sStart + TC;   // reused after loading as the list of node-changing slots
-    // that list grouped by crossing class: its own array, or with TMA staging the field
-    // tile, which the deposit no longer reads (a tile's next chunk stages it again)
-    int *sXs = TMA ? reinterpret_cast<int *>( sF ) : sRank + ( CELLS ? nmax : 0 );
-    unsigned char *sSlotCell = reinterpret_cast<unsigned char *>( ( TMA ? sRank : sXs ) + ( CELLS ? nmax : 0 ) );
-    __shared__ int sNX;         // length of that list
-    __shared__ int sXc[4];      // node-changing particles per class (x, y, z only; several)
+    // reused after loading as the list of node-changing slots: in 3D those that change
+    // node in one dimension from the front, the others from the back (so no grouping
+    // pass); in 2D grouped by crossing dimension into sXs after the particle loop
+    int *sRank = sStart + TC;
+    int *sXs = DIM == 2 ? sRank + ( CELLS ? nmax : 0 ) : sRank;
+    unsigned char *sSlotCell = reinterpret_cast<unsigned char *>( sXs + ( CELLS ? nmax : 0 ) );
+    __shared__ int sNX;         // length of that list (3D: its front part)
+    __shared__ int sNM;         // 3D: length of its back part
+    __shared__ int sXc[4];      // 2D: node-changing particles per class (x, y only; both)
 
     // TMA completion barrier: thread 0 arms it per tile with the bytes to expect, the
     // copies complete it, every thread waits on its phase (bounded)
@@ -861,13 +864,6 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
     for( int c0 = 0; c0 < ( CELLS ? ntot : 1 ); c0 += ( CELLS ? nmax : 1 ) ) {
     const int n = CELLS ? min( nmax, ntot - c0 ) : ntot;
     const int64_t s0 = seg0 + c0;
-    if constexpr( TMA ) {
-        // the previous chunk kept its node-changing list in the field tile: stage it again
-        if( c0 > 0 ) {
-            if( threadIdx.x == 0 ) tma_issue( tma, &sTmaBar, sF, fsz, ix0, iy0, iz0 );
-            tma_pending = true;
-        }
-    }
     if constexpr( CELLS ) {
         // rank of every particle inside its cell, then the cells' start offsets
         for( int c = threadIdx.x; c < TC; c += blockDim.x ) sCnt[c] = 0;
@@ -929,6 +925,7 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
         }
         if( threadIdx.x == 0 ) {
             sNX = 0;
+            sNM = 0;
         }
         if( threadIdx.x < 4 ) sXc[threadIdx.x] = 0;
         cp_async_wait_all(); // the particle planes (and, on the first chunk, the field tile)
@@ -1146,13 +1143,24 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
             // dimension, the list the plane beyond it)
             const int nshift = ( shift[0] != 0 ) + ( shift[1] != 0 ) + ( shift[2] != 0 );
             const bool cross = valid && !gone && nshift > 0;
-            if( cross ) atomicAdd( &sXc[nshift == 1 ? ( shift[0] != 0 ? 0 : ( shift[1] != 0 ? 1 : 2 ) ) : 3], 1 );
-            const unsigned xm = __ballot_sync( 0xffffffffu, cross );
+            const bool front = DIM == 2 || nshift == 1;
+            if( DIM == 2 && cross ) atomicAdd( &sXc[nshift == 1 ? ( shift[0] != 0 ? 0 : 1 ) : 3], 1 );
+            const unsigned lt = ( 1u << lane ) - 1u;
+            const unsigned xm = __ballot_sync( 0xffffffffu, cross && front );
             if( xm ) {
                 int xb = 0;
                 if( lane == 0 ) xb = atomicAdd( &sNX, __popc( xm ) );
                 xb = __shfl_sync( 0xffffffffu, xb, 0 );
-                if( cross ) sRank[xb + __popc( xm & ( ( 1u << lane ) - 1u ) )] = q;
+                if( cross && front ) sRank[xb + __popc( xm & lt )] = q;
+            }
+            if constexpr( DIM == 3 ) {
+                const unsigned mm = __ballot_sync( 0xffffffffu, cross && !front );
+                if( mm ) {
+                    int mb = 0;
+                    if( lane == 0 ) mb = atomicAdd( &sNM, __popc( mm ) );
+                    mb = __shfl_sync( 0xffffffffu, mb, 0 );
+                    if( cross && !front ) sRank[nmax - 1 - ( mb + __popc( mm & lt ) )] = q;
+                }
             }
         }
 
@@ -1239,7 +1247,7 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
     }
     __syncthreads();
 
-    if constexpr( CELLS ) {
+    if constexpr( CELLS && DIM == 2 ) {
         // group the node-changing list by class (counting sort); class starts in sXc
         if( threadIdx.x == 0 ) {
             int run = 0;
@@ -1404,8 +1412,8 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
         }
         // node-changing particles, one per thread, into their own tile (after the
         // per-cell pass: warps that finish their cells early start on this list)
-        for( int k = threadIdx.x; k < sNX; k += blockDim.x ) {
-            const int q = sXs[k];
+        for( int k = threadIdx.x; k < sNX + ( DIM == 3 ? sNM : 0 ); k += blockDim.x ) {
+            const int q = DIM == 2 ? sXs[k] : ( k < sNX ? sRank[k] : sRank[nmax - 1 - ( k - sNX )] );
             const int lc = sSlotCell[q];
             int cl[3];
             if( DIM == 3 ) {
@@ -1444,8 +1452,6 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
             const T crz = cw0 * wq * vz;
             deposit_direct<DIM, T>( sJ2, td, jsz, cl, W, cr, crz );
         }
-        // the list's reads of the field tile come before the next staging's writes
-        if constexpr( TMA ) asm volatile( "fence.proxy.async.shared::cta;\n" ::: "memory" );
         __syncthreads();
     }
     } // chunk
@@ -2601,7 +2607,7 @@ int launch_particles( sg_sim *S, SpeciesState &s, cudaStream_t st, int t0, int t
     if constexpr( MIXED ) {
         const int tc = S->g.T[0] * S->g.T[1] * ( DIM == 3 ? S->g.T[2] : 1 );
         const size_t j2 = cells_j2_bytes( tile_dims( S->g ) );
-        const int fit = cells_chunk_fit( smem + j2, tc );
+        const int fit = cells_chunk_fit( smem + j2, tc, DIM == 2 );
         chunk = std::max( 1, std::min( s.max_cap, fit & ~31 ) );
         if( tc <= ( DIM == 3 ? 64 : 128 ) && fit >= 128 ) {
             const GridInfo &g = S->g;
@@ -2621,12 +2627,12 @@ int launch_particles( sg_sim *S, SpeciesState &s, cudaStream_t st, int t0, int t
                 if( ft == 2 ) kern = k_step_particles<DIM, MIXED, KIND, true, 2>;
                 if( ft == 3 ) kern = k_step_particles<DIM, MIXED, KIND, true, 3>;
             }
-            smem += j2 + cells_smem_bytes( tc, chunk );
+            smem += j2 + cells_smem_bytes( tc, chunk, DIM == 2 );
             if constexpr( DIM == 3 ) {
                 if( S->tma && ft == 1 ) {
                     kern = k_step_particles<3, true, KIND, true, 1, true>;
                     chunk = tma_chunk();
-                    smem = TMA_TILE_BYTES + cells_smem_bytes( tc, chunk, true );
+                    smem = TMA_TILE_BYTES + cells_smem_bytes( tc, chunk, false );
                 }
             }
         }
@@ -2989,7 +2995,7 @@ int launch_chunk_dim( const sg_sim *S, int max_cap )
     if( !S->mixed ) return 0;
     const GridInfo &g = S->g;
     const int tc = g.T[0] * g.T[1] * ( DIM == 3 ? g.T[2] : 1 );
-    const int fit = cells_chunk_fit( S->smem_bytes + cells_j2_bytes( tile_dims( g ) ), tc );
+    const int fit = cells_chunk_fit( S->smem_bytes + cells_j2_bytes( tile_dims( g ) ), tc, DIM == 2 );
     int chunk = std::max( 1, std::min( max_cap, fit & ~31 ) );
     if( tc <= ( DIM == 3 ? 64 : 128 ) && fit >= 128 ) {
         int ft = 0;
