@@ -548,65 +548,91 @@ __device__ __forceinline__ void footprint_weights( T dold, T dnew, int s, T *A, 
     P[1] = P[0] + D[1];
 }
 
-// The part of a 3D Esirkepov deposit outside the old cell's footprint, for a particle
-// that changes node in dimension DS only (shift sg): the window reaches one plane
-// further, stencil point 4 for sg = 1, for sg = -1 point 0 across the current and
-// point 1 along it.  Along DS: J_DS at that point over the (B, E) footprint gets
-// -cr Q (A_B A_E + D_B D_E / 12), Q = the sum of S1 - S0 before it (-nov or nov).
-// Across: J_C (C != DS) at its two footprint points along C, plane pt of DS, the
-// footprint of the third dimension, gets -cr_C P_C (A_ov A_t + D_ov D_t / 12) with
-// A_ov = nov / 2, D_ov = nov (S0 is zero there).  21 points in all; the per-cell
-// pass adds the footprint part.
 template <class T>
-__device__ __forceinline__ void deposit_overhang( T *J2, const TileDims &td, int jsz, const int *cl, const T ( *A )[3],
-                                                  const T ( *D )[3], const T ( *P )[2], const T *cr, const T *nov,
-                                                  const int *sh )
+__device__ __forceinline__ T pick4( int i, T a0, T a1, T a2, T a3 )
 {
-    // the frame (a, b, e) = (DS, DS + 1, DS + 2) mod 3, selected once: one body serves
-    // the three dimensions (this code runs once per tile, so it is kept small)
-    const int ds = sh[0] != 0 ? 0 : ( sh[1] != 0 ? 1 : 2 );
-    const int sg = ds == 0 ? sh[0] : ( ds == 1 ? sh[1] : sh[2] );
-    const T nv = ds == 0 ? nov[0] : ( ds == 1 ? nov[1] : nov[2] );
-#define SG_ROT( x0, x1, x2, k ) ( ds == 0 ? ( k == 0 ? x0 : k == 1 ? x1 : x2 ) : ds == 1 ? ( k == 0 ? x1 : k == 1 ? x2 : x0 ) : ( k == 0 ? x2 : k == 1 ? x0 : x1 ) )
-    const int stride[3] = { td.JXS, td.JZ, 1 };
-    const int sa = SG_ROT( stride[0], stride[1], stride[2], 0 ), sb = SG_ROT( stride[0], stride[1], stride[2], 1 ),
-              se = SG_ROT( stride[0], stride[1], stride[2], 2 );
-    const int la = SG_ROT( cl[0], cl[1], cl[2], 0 ), lb = SG_ROT( cl[0], cl[1], cl[2], 1 ), le = SG_ROT( cl[0], cl[1], cl[2], 2 );
-    const T cra = SG_ROT( cr[0], cr[1], cr[2], 0 ), crb = SG_ROT( cr[0], cr[1], cr[2], 1 ), cre = SG_ROT( cr[0], cr[1], cr[2], 2 );
-    T *Ja = J2 + SG_ROT( 0, 1, 2, 0 ) * jsz, *Jb = J2 + SG_ROT( 0, 1, 2, 1 ) * jsz, *Je = J2 + SG_ROT( 0, 1, 2, 2 ) * jsz;
-    T Ab[3], Db[3], Ae[3], De[3], Pb[2], Pe[2];
-#pragma unroll
-    for( int i = 0; i < 3; i++ ) {
-        Ab[i] = SG_ROT( A[0][i], A[1][i], A[2][i], 1 );
-        Db[i] = SG_ROT( D[0][i], D[1][i], D[2][i], 1 );
-        Ae[i] = SG_ROT( A[0][i], A[1][i], A[2][i], 2 );
-        De[i] = SG_ROT( D[0][i], D[1][i], D[2][i], 2 );
-    }
-#pragma unroll
-    for( int i = 0; i < 2; i++ ) {
-        Pb[i] = SG_ROT( P[0][i], P[1][i], P[2][i], 1 );
-        Pe[i] = SG_ROT( P[0][i], P[1][i], P[2][i], 2 );
-    }
-#undef SG_ROT
+    return i == 0 ? a0 : ( i == 1 ? a1 : ( i == 2 ? a2 : a3 ) );
+}
+
+// The part of a 3D Esirkepov deposit outside the old cell's footprint, for a particle
+// that changes node (shift sh[d] in dimension d; the per-cell pass adds the footprint
+// part).  A shifted dimension's window reaches one plane further: stencil point 4 for
+// s = 1; for s = -1 point 0 across a current and point 1 along it.  In the frame of
+// current component a (transverse b, e), window index 3 (across) or 2 (along) is that
+// plane, with A = nov / 2, D = nov (S0 is zero there) across and Q = -s nov (the sum of
+// S1 - S0 before it) along.  J_a gets -cr_a P_a (A_b A_e + D_b D_e / 12) on the points
+// with at least one index beyond the footprint: 21 for a shift in one dimension.  The
+// loops are not unrolled (this code runs about once per tile per warp, where fetching a
+// long unrolled body costs more than running a short loop).
+template <class T>
+__device__ __forceinline__ void deposit_beyond( T *J2, int jsz, int jxs, int jz, const int *cl, const T ( *A )[3],
+                                                const T ( *D )[3], const T ( *P )[2], const T *cr, const T *nov,
+                                                const int *sh )
+{
     const T twelfth = T( 1.0 / 12.0 );
-    const int pt = sg > 0 ? 4 : 0, pa = sg > 0 ? 4 : 1;
-    const T qov = sg > 0 ? -nv : nv, aov = T( 0.5 ) * nv, dov = twelfth * nv;
-    // along a: the (b, e) footprint at point pa
-    const T ca = -( cra * qov );
+#pragma unroll 1
+    for( int c = 0; c < 3; c++ ) {
+        const int b = c == 2 ? 0 : c + 1, e = c == 0 ? 2 : c - 1;
+#define SG_SEL( x, i ) ( ( i ) == 0 ? x[0] : ( ( i ) == 1 ? x[1] : x[2] ) )
+        const int sa = c == 0 ? jxs : ( c == 1 ? jz : 1 ), sb = b == 0 ? jxs : ( b == 1 ? jz : 1 ), se = e == 0 ? jxs : ( e == 1 ? jz : 1 );
+        const int la = SG_SEL( cl, c ), lb = SG_SEL( cl, b ), le = SG_SEL( cl, e );
+        const int s_a = SG_SEL( sh, c ), s_b = SG_SEL( sh, b ), s_e = SG_SEL( sh, e );
+        const T cra = SG_SEL( cr, c ), nva = SG_SEL( nov, c ), nvb = SG_SEL( nov, b ), nve = SG_SEL( nov, e );
+        T Ab[3], Db[3], Ae[3], De[3], Pa[2];
 #pragma unroll
-    for( int u = 0; u < 3; u++ )
-#pragma unroll
-        for( int v = 0; v < 3; v++ )
-            sh_add( &Ja[( la + pa ) * sa + ( lb + 1 + u ) * sb + ( le + 1 + v ) * se],
-                    ca * ( Ab[u] * Ae[v] + twelfth * Db[u] * De[v] ) );
-    // across: J_b at its points 2, 3 along b, plane pt of a, the footprint of e; J_e the same with b and e swapped
-#pragma unroll
-    for( int w = 0; w < 3; w++ ) {
-        const T wte = aov * Ae[w] + dov * De[w], wtb = aov * Ab[w] + dov * Db[w];
-#pragma unroll
-        for( int m = 0; m < 2; m++ ) {
-            sh_add( &Jb[( lb + 2 + m ) * sb + ( la + pt ) * sa + ( le + 1 + w ) * se], -( crb * Pb[m] ) * wte );
-            sh_add( &Je[( le + 2 + m ) * se + ( la + pt ) * sa + ( lb + 1 + w ) * sb], -( cre * Pe[m] ) * wtb );
+        for( int i = 0; i < 3; i++ ) {
+            Ab[i] = b == 0 ? A[0][i] : ( b == 1 ? A[1][i] : A[2][i] );
+            Db[i] = b == 0 ? D[0][i] : ( b == 1 ? D[1][i] : D[2][i] );
+            Ae[i] = e == 0 ? A[0][i] : ( e == 1 ? A[1][i] : A[2][i] );
+            De[i] = e == 0 ? D[0][i] : ( e == 1 ? D[1][i] : D[2][i] );
+        }
+        Pa[0] = SG_SEL( P, c )[0];
+        Pa[1] = SG_SEL( P, c )[1];
+#undef SG_SEL
+        const T Ab3 = T( 0.5 ) * nvb, Db3 = twelfth * nvb, Ae3 = T( 0.5 ) * nve, De3 = nve;
+        const T qa = s_a > 0 ? -nva : nva;
+        const int pa = la + ( s_a > 0 ? 4 : 1 ), pb = lb + ( s_b > 0 ? 4 : 0 ), pe = le + ( s_e > 0 ? 4 : 0 );
+        const int nu = s_b != 0 ? 4 : 3, nv = s_e != 0 ? 4 : 3;
+        T *J = J2 + c * jsz;
+        // the along plane beyond (index 2): every (b, e) point of the window
+        if( s_a != 0 ) {
+            const T ca = -( cra * qa );
+#pragma unroll 1
+            for( int u = 0; u < nu; u++ ) {
+                const T ab = pick4( u, Ab[0], Ab[1], Ab[2], Ab3 ), db = pick4( u, twelfth * Db[0], twelfth * Db[1], twelfth * Db[2], Db3 );
+                const int ib = u < 3 ? lb + 1 + u : pb;
+#pragma unroll 1
+                for( int v = 0; v < nv; v++ ) {
+                    const T ae = pick4( v, Ae[0], Ae[1], Ae[2], Ae3 ), de = pick4( v, De[0], De[1], De[2], De3 );
+                    const int ie = v < 3 ? le + 1 + v : pe;
+                    sh_add( &J[pa * sa + ib * sb + ie * se], ca * ( ab * ae + db * de ) );
+                }
+            }
+        }
+        // the across-b plane beyond (index 3) at the two footprint points along
+        if( s_b != 0 ) {
+#pragma unroll 1
+            for( int m = 0; m < 2; m++ ) {
+                const T cm = -( cra * ( m ? Pa[1] : Pa[0] ) );
+#pragma unroll 1
+                for( int v = 0; v < nv; v++ ) {
+                    const T ae = pick4( v, Ae[0], Ae[1], Ae[2], Ae3 ), de = pick4( v, De[0], De[1], De[2], De3 );
+                    const int ie = v < 3 ? le + 1 + v : pe;
+                    sh_add( &J[( la + 2 + m ) * sa + pb * sb + ie * se], cm * ( Ab3 * ae + Db3 * de ) );
+                }
+            }
+        }
+        // the across-e plane beyond, footprint points of b (the corner is in the plane above)
+        if( s_e != 0 ) {
+#pragma unroll 1
+            for( int m = 0; m < 2; m++ ) {
+                const T cm = -( cra * ( m ? Pa[1] : Pa[0] ) );
+#pragma unroll 1
+                for( int u = 0; u < 3; u++ ) {
+                    const T ab = u == 0 ? Ab[0] : ( u == 1 ? Ab[1] : Ab[2] ), db = u == 0 ? Db[0] : ( u == 1 ? Db[1] : Db[2] );
+                    sh_add( &J[( la + 2 + m ) * sa + ( lb + 1 + u ) * sb + pe * se], cm * ( ab * Ae3 + twelfth * db * De3 ) );
+                }
+            }
         }
     }
 }
@@ -761,14 +787,12 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
     float *sRec = reinterpret_cast<float *>( sJ2 + ( CELLS ? 3 * jsz : 0 ) );
     int *sCnt = reinterpret_cast<int *>( sRec + ( CELLS ? REC * nmax : 0 ) );
     int *sStart = sCnt + TC;
-    // reused after loading as the list of node-changing slots: in 3D those that change
-    // node in one dimension from the front, the others from the back (so no grouping
-    // pass); in 2D grouped by crossing dimension into sXs after the particle loop
+    // reused after loading as the list of node-changing slots; in 2D grouped by crossing
+    // dimension into sXs after the particle loop
     int *sRank = sStart + TC;
     int *sXs = DIM == 2 ? sRank + ( CELLS ? nmax : 0 ) : sRank;
     unsigned char *sSlotCell = reinterpret_cast<unsigned char *>( sXs + ( CELLS ? nmax : 0 ) );
-    __shared__ int sNX;         // length of that list (3D: its front part)
-    __shared__ int sNM;         // 3D: length of its back part
+    __shared__ int sNX;         // length of that list
     __shared__ int sXc[4];      // 2D: node-changing particles per class (x, y only; both)
 
     // TMA completion barrier: thread 0 arms it per tile with the bytes to expect, the
@@ -925,7 +949,6 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
         }
         if( threadIdx.x == 0 ) {
             sNX = 0;
-            sNM = 0;
         }
         if( threadIdx.x < 4 ) sXc[threadIdx.x] = 0;
         cp_async_wait_all(); // the particle planes (and, on the first chunk, the field tile)
@@ -1139,28 +1162,16 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
 
         if constexpr( CELLS ) {
             // node-changing particles go to a list deposited with full warps later (3D: the
-            // per-cell pass takes the footprint part of those that change node in one
-            // dimension, the list the plane beyond it)
+            // per-cell pass takes their footprint part, the list the planes beyond it)
             const int nshift = ( shift[0] != 0 ) + ( shift[1] != 0 ) + ( shift[2] != 0 );
             const bool cross = valid && !gone && nshift > 0;
-            const bool front = DIM == 2 || nshift == 1;
             if( DIM == 2 && cross ) atomicAdd( &sXc[nshift == 1 ? ( shift[0] != 0 ? 0 : 1 ) : 3], 1 );
-            const unsigned lt = ( 1u << lane ) - 1u;
-            const unsigned xm = __ballot_sync( 0xffffffffu, cross && front );
+            const unsigned xm = __ballot_sync( 0xffffffffu, cross );
             if( xm ) {
                 int xb = 0;
                 if( lane == 0 ) xb = atomicAdd( &sNX, __popc( xm ) );
                 xb = __shfl_sync( 0xffffffffu, xb, 0 );
-                if( cross && front ) sRank[xb + __popc( xm & lt )] = q;
-            }
-            if constexpr( DIM == 3 ) {
-                const unsigned mm = __ballot_sync( 0xffffffffu, cross && !front );
-                if( mm ) {
-                    int mb = 0;
-                    if( lane == 0 ) mb = atomicAdd( &sNM, __popc( mm ) );
-                    mb = __shfl_sync( 0xffffffffu, mb, 0 );
-                    if( cross && !front ) sRank[nmax - 1 - ( mb + __popc( mm & lt ) )] = q;
-                }
+                if( cross ) sRank[xb + __popc( xm & ( ( 1u << lane ) - 1u ) )] = q;
             }
         }
 
@@ -1314,12 +1325,12 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
                 const int sb = __float_as_int( sRec[6 * nmax + q] );
                 int sh[3] = { 0, 0, 0 };
                 if constexpr( DIM == 3 ) {
-                    // a particle that changes node in one dimension stays here (the rest
-                    // are in the node-changing list, and a removed one deposits nothing)
+                    // every particle: one that changes node adds its footprint part here
+                    // (the node-changing pass the rest); a removed one deposits nothing
+                    if( sb == GONE_RECORD ) continue;
                     sh[0] = ( sb & 3 ) - 1;
                     sh[1] = ( ( sb >> 2 ) & 3 ) - 1;
                     sh[2] = ( ( sb >> 4 ) & 3 ) - 1;
-                    if( sb == GONE_RECORD || ( sh[0] != 0 ) + ( sh[1] != 0 ) + ( sh[2] != 0 ) > 1 ) continue;
                 } else {
                     if( sb != NO_SHIFT ) continue; // in the node-changing list
                 }
@@ -1412,8 +1423,8 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
         }
         // node-changing particles, one per thread, into their own tile (after the
         // per-cell pass: warps that finish their cells early start on this list)
-        for( int k = threadIdx.x; k < sNX + ( DIM == 3 ? sNM : 0 ); k += blockDim.x ) {
-            const int q = DIM == 2 ? sXs[k] : ( k < sNX ? sRank[k] : sRank[nmax - 1 - ( k - sNX )] );
+        for( int k = threadIdx.x; k < sNX; k += blockDim.x ) {
+            const int q = sXs[k];
             const int lc = sSlotCell[q];
             int cl[3];
             if( DIM == 3 ) {
@@ -1430,15 +1441,13 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
             const T wq = sRec[7 * nmax + q];
             const T cr[3] = { cr3[0] * wq, cr3[1] * wq, cr3[2] * wq };
             if constexpr( DIM == 3 ) {
-                if( ( sh[0] != 0 ) + ( sh[1] != 0 ) + ( sh[2] != 0 ) == 1 ) {
-                    // one dimension: the per-cell pass took the footprint, this the plane beyond
-                    T A[3][3], D[3][3], P[3][2], nov[3];
+                // the per-cell pass took the footprint part, this the planes beyond
+                T A[3][3], D[3][3], P[3][2], nov[3];
 #pragma unroll
-                    for( int d = 0; d < 3; d++ )
-                        footprint_weights<T>( ( T )sRec[d * nmax + q], ( T )sRec[( 3 + d ) * nmax + q], sh[d], A[d], D[d], P[d], nov[d] );
-                    deposit_overhang<T>( sJ2, td, jsz, cl, A, D, P, cr, nov, sh );
-                    continue;
-                }
+                for( int d = 0; d < 3; d++ )
+                    footprint_weights<T>( ( T )sRec[d * nmax + q], ( T )sRec[( 3 + d ) * nmax + q], sh[d], A[d], D[d], P[d], nov[d] );
+                deposit_beyond<T>( sJ2, jsz, td.JXS, td.JZ, cl, A, D, P, cr, nov, sh );
+                continue;
             }
             const T vz = DIM == 3 ? T( 0 ) : sRec[5 * nmax + q];
             EsirWin<T> W[3];
