@@ -648,12 +648,14 @@ constexpr int GONE_RECORD = 1 << 8;                  // record of a particle rem
 
 // Shared memory of the per-cell mode: REC planes of nmax floats, a count and a
 // start per cell, a packed (cell, rank) word per particle (later the node-changing
-// list), in 2D a word per particle for that list grouped by crossing dimension, a
-// cell byte per slot.
+// list), the list grouped by crossing dimension with each group padded to whole warps
+// (nmax + LIST_PAD words; with TMA staging it uses the field tile instead), a cell
+// byte per slot.
 constexpr size_t CELLS_SMEM_TARGET = 44 * 1024; // five 128-thread blocks per SM
+constexpr int LIST_PAD = 128;                   // four groups, each padded by at most 31
 constexpr size_t cells_smem_bytes( int tc, int nmax, bool grouped )
 {
-    return ( size_t )REC * 4 * nmax + ( size_t )8 * tc + ( size_t )( grouped ? 8 : 4 ) * nmax +
+    return ( size_t )REC * 4 * nmax + ( size_t )8 * tc + ( size_t )4 * nmax + ( grouped ? ( size_t )4 * ( nmax + LIST_PAD ) : 0 ) +
            ( ( ( size_t )nmax + 15 ) & ~( size_t )15 );
 }
 
@@ -662,7 +664,7 @@ constexpr size_t cells_smem_bytes( int tc, int nmax, bool grouped )
 constexpr int cells_chunk_fit( size_t tile_bytes, int tc, bool grouped )
 {
     const size_t fixed = tile_bytes + cells_smem_bytes( tc, 0, grouped ) + 16;
-    const size_t per = ( size_t )REC * 4 + ( grouped ? 8 : 4 ) + 1; // planes, rank (and list) words, cell byte
+    const size_t per = ( size_t )REC * 4 + ( grouped ? 8 : 4 ) + 1; // planes, rank (and grouped list) words, cell byte
     return fixed < CELLS_SMEM_TARGET ? ( int )( ( CELLS_SMEM_TARGET - fixed ) / per ) : 0;
 }
 
@@ -695,7 +697,7 @@ constexpr int ft_shift( int t ) { return t == 16 ? 4 : ( t == 8 ? 3 : ( t == 4 ?
 // points per dimension.
 constexpr int fixt_chunk( int dim, int ft )
 {
-    return dim == 3 ? cells_chunk_fit( ( size_t )( 6 * 7 * 7 * 7 + 6 * jtile3_size( 4 ) ) * 4, 64, false ) & ~31
+    return dim == 3 ? cells_chunk_fit( ( size_t )( 6 * 7 * 7 * 7 + 6 * jtile3_size( 4 ) ) * 4, 64, true ) & ~31
                     : cells_chunk_fit( ( size_t )( 6 * ( ft_tile( 2, ft, 0 ) + 3 ) * ( ft_tile( 2, ft, 1 ) + 3 ) +
                                                    6 * ( ft_tile( 2, ft, 0 ) + 4 ) * ( ft_tile( 2, ft, 1 ) + 4 ) ) * 4,
                                        ft_tile( 2, ft, 0 ) * ft_tile( 2, ft, 1 ), true ) & ~31;
@@ -787,13 +789,20 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
     float *sRec = reinterpret_cast<float *>( sJ2 + ( CELLS ? 3 * jsz : 0 ) );
     int *sCnt = reinterpret_cast<int *>( sRec + ( CELLS ? REC * nmax : 0 ) );
     int *sStart = sCnt + TC;
-    // reused after loading as the list of node-changing slots; in 2D grouped by crossing
-    // dimension into sXs after the particle loop
+    // reused after loading as the list of node-changing slots, which the particle
+    // loop's end groups by crossing dimension into sXs, each group padded to whole
+    // warps (slot -1) so that a warp takes one kind only: its own array, or with TMA
+    // staging the field tile, which the deposit no longer reads (a tile's next chunk
+    // stages it again)
     int *sRank = sStart + TC;
-    int *sXs = DIM == 2 ? sRank + ( CELLS ? nmax : 0 ) : sRank;
-    unsigned char *sSlotCell = reinterpret_cast<unsigned char *>( sXs + ( CELLS ? nmax : 0 ) );
+    int *sXs = TMA ? reinterpret_cast<int *>( sF ) : sRank + ( CELLS ? nmax : 0 );
+    unsigned char *sSlotCell = reinterpret_cast<unsigned char *>( TMA ? sRank + ( CELLS ? nmax : 0 )
+                                                                      : sXs + ( CELLS ? nmax + LIST_PAD : 0 ) );
     __shared__ int sNX;         // length of that list
-    __shared__ int sXc[4];      // 2D: node-changing particles per class (x, y only; both)
+    __shared__ int sNT;         // length of the grouped, padded list
+    __shared__ int sXc[4];      // node-changing particles per class (one dimension x, y, z; several)
+    __shared__ int sXn[4];      // the same counts, kept
+    __shared__ int sXb[4];      // class starts, kept
 
     // TMA completion barrier: thread 0 arms it per tile with the bytes to expect, the
     // copies complete it, every thread waits on its phase (bounded)
@@ -888,6 +897,13 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
     for( int c0 = 0; c0 < ( CELLS ? ntot : 1 ); c0 += ( CELLS ? nmax : 1 ) ) {
     const int n = CELLS ? min( nmax, ntot - c0 ) : ntot;
     const int64_t s0 = seg0 + c0;
+    if constexpr( TMA ) {
+        // the previous chunk kept its node-changing list in the field tile: stage it again
+        if( c0 > 0 ) {
+            if( threadIdx.x == 0 ) tma_issue( tma, &sTmaBar, sF, fsz, ix0, iy0, iz0 );
+            tma_pending = true;
+        }
+    }
     if constexpr( CELLS ) {
         // rank of every particle inside its cell, then the cells' start offsets
         for( int c = threadIdx.x; c < TC; c += blockDim.x ) sCnt[c] = 0;
@@ -1165,7 +1181,7 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
             // per-cell pass takes their footprint part, the list the planes beyond it)
             const int nshift = ( shift[0] != 0 ) + ( shift[1] != 0 ) + ( shift[2] != 0 );
             const bool cross = valid && !gone && nshift > 0;
-            if( DIM == 2 && cross ) atomicAdd( &sXc[nshift == 1 ? ( shift[0] != 0 ? 0 : 1 ) : 3], 1 );
+            if( cross ) atomicAdd( &sXc[nshift == 1 ? ( shift[0] != 0 ? 0 : ( shift[1] != 0 ? 1 : 2 ) ) : 3], 1 );
             const unsigned xm = __ballot_sync( 0xffffffffu, cross );
             if( xm ) {
                 int xb = 0;
@@ -1258,17 +1274,25 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
     }
     __syncthreads();
 
-    if constexpr( CELLS && DIM == 2 ) {
-        // group the node-changing list by class (counting sort); class starts in sXc
+    if constexpr( CELLS ) {
+        // group the node-changing list by class (counting sort), each class from a warp
+        // boundary; class starts in sXc, the padding slots hold -1
         if( threadIdx.x == 0 ) {
             int run = 0;
             for( int k = 0; k < 4; k++ ) {
                 const int c = sXc[k];
+                sXn[k] = c;
+                sXb[k] = run;
                 sXc[k] = run;
-                run += c;
+                run += ( c + 31 ) & ~31;
             }
+            sNT = run;
         }
         __syncthreads();
+        for( int i = threadIdx.x; i < 128; i += blockDim.x ) {
+            const int k = i >> 5, l = i & 31;
+            if( l < ( ( sXn[k] + 31 ) & ~31 ) - sXn[k] ) sXs[sXb[k] + sXn[k] + l] = -1;
+        }
         for( int k = threadIdx.x; k < sNX; k += blockDim.x ) {
             const int q = sRank[k];
             const int sb = __float_as_int( sRec[6 * nmax + q] );
@@ -1423,8 +1447,9 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
         }
         // node-changing particles, one per thread, into their own tile (after the
         // per-cell pass: warps that finish their cells early start on this list)
-        for( int k = threadIdx.x; k < sNX; k += blockDim.x ) {
+        for( int k = threadIdx.x; k < sNT; k += blockDim.x ) {
             const int q = sXs[k];
+            if( q < 0 ) continue; // padding
             const int lc = sSlotCell[q];
             int cl[3];
             if( DIM == 3 ) {
@@ -1461,6 +1486,8 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
             const T crz = cw0 * wq * vz;
             deposit_direct<DIM, T>( sJ2, td, jsz, cl, W, cr, crz );
         }
+        // the list's reads of the field tile come before the next staging's writes
+        if constexpr( TMA ) asm volatile( "fence.proxy.async.shared::cta;\n" ::: "memory" );
         __syncthreads();
     }
     } // chunk
@@ -2616,7 +2643,7 @@ int launch_particles( sg_sim *S, SpeciesState &s, cudaStream_t st, int t0, int t
     if constexpr( MIXED ) {
         const int tc = S->g.T[0] * S->g.T[1] * ( DIM == 3 ? S->g.T[2] : 1 );
         const size_t j2 = cells_j2_bytes( tile_dims( S->g ) );
-        const int fit = cells_chunk_fit( smem + j2, tc, DIM == 2 );
+        const int fit = cells_chunk_fit( smem + j2, tc, true );
         chunk = std::max( 1, std::min( s.max_cap, fit & ~31 ) );
         if( tc <= ( DIM == 3 ? 64 : 128 ) && fit >= 128 ) {
             const GridInfo &g = S->g;
@@ -2636,7 +2663,7 @@ int launch_particles( sg_sim *S, SpeciesState &s, cudaStream_t st, int t0, int t
                 if( ft == 2 ) kern = k_step_particles<DIM, MIXED, KIND, true, 2>;
                 if( ft == 3 ) kern = k_step_particles<DIM, MIXED, KIND, true, 3>;
             }
-            smem += j2 + cells_smem_bytes( tc, chunk, DIM == 2 );
+            smem += j2 + cells_smem_bytes( tc, chunk, true );
             if constexpr( DIM == 3 ) {
                 if( S->tma && ft == 1 ) {
                     kern = k_step_particles<3, true, KIND, true, 1, true>;
@@ -3004,7 +3031,7 @@ int launch_chunk_dim( const sg_sim *S, int max_cap )
     if( !S->mixed ) return 0;
     const GridInfo &g = S->g;
     const int tc = g.T[0] * g.T[1] * ( DIM == 3 ? g.T[2] : 1 );
-    const int fit = cells_chunk_fit( S->smem_bytes + cells_j2_bytes( tile_dims( g ) ), tc, DIM == 2 );
+    const int fit = cells_chunk_fit( S->smem_bytes + cells_j2_bytes( tile_dims( g ) ), tc, true );
     int chunk = std::max( 1, std::min( max_cap, fit & ~31 ) );
     if( tc <= ( DIM == 3 ? 64 : 128 ) && fit >= 128 ) {
         int ft = 0;
