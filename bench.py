@@ -65,7 +65,7 @@ def workload_cfg(args):
 # capture (dram__bytes_read.sum + dram__bytes_write.sum) of the 3D thermal case at
 # 128^3 cells x 8 ppc, divided by its 16,777,216 particles; a launch over N particles
 # at the same ppc moves N times this.  None where no capture has been taken.
-NCU_TRAFFIC_BYTES_PER_PARTICLE = {"mixed": (664.124160e6 + 530.128384e6) / 16777216, "fp64": None}
+NCU_TRAFFIC_BYTES_PER_PARTICLE = {"mixed": (693.389568e6 + 557.328640e6) / 16777216, "fp64": None}
 
 
 def bytes_alg_per_particle_step(form, ppc, ndim=3):

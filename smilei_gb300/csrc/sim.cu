@@ -1605,6 +1605,34 @@ __device__ __forceinline__ void two_prod( T a, T b, T &p, T &e )
 // is kept as the pair E - C (C the compensation), so an Ampere step adds no rounding
 // of its own to E: div E follows div J and the discrete curl of B exactly (the curl
 // part cancels in the divergence whatever B is).
+// FP64 to an FP32 pair hi + lo with integer operations: hi is d with its fraction cut
+// to 23 bits, lo the next 24 bits of the rest (hi + lo is d to about 2^-47 relative for
+// |d| above 2^-98; below, lo is 0).  Magnitudes beyond the FP32 range give +-infinity
+// (NaN stays NaN), below 2^-126 +-0.
+__device__ __forceinline__ void split_fp64( double d, float &hi, float &lo )
+{
+    const unsigned long long b = ( unsigned long long )__double_as_longlong( d );
+    const unsigned sgn = ( unsigned )( b >> 32 ) & 0x80000000u;
+    const int e = ( int )( ( b >> 52 ) & 0x7ffu ) - 1023;
+    const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+    lo = 0.f;
+    if( e > 127 ) {
+        hi = __uint_as_float( sgn | 0x7f800000u | ( e == 1024 && m ? 0x400000u : 0u ) );
+        return;
+    }
+    if( e < -126 ) {
+        hi = __uint_as_float( sgn );
+        return;
+    }
+    hi = __uint_as_float( sgn | ( ( unsigned )( e + 127 ) << 23 ) | ( unsigned )( m >> 29 ) );
+    const unsigned low = ( unsigned )( m & 0x1FFFFFFFull );
+    if( low == 0u ) return;
+    const int p = 31 - __clz( low ), fe = e - 52 + p;
+    if( fe < -126 ) return;
+    const unsigned frac = ( p >= 23 ? low >> ( p - 23 ) : low << ( 23 - p ) ) & 0x7fffffu;
+    lo = __uint_as_float( sgn | ( ( unsigned )( fe + 127 ) << 23 ) | frac );
+}
+
 template <class T>
 __device__ __forceinline__ void ampere_point( T *E, T *C, int64_t t, T dt, double Jd, T ca, T b1, T b0, T cb, T b3, T b2 )
 {
@@ -1613,8 +1641,14 @@ __device__ __forceinline__ void ampere_point( T *E, T *C, int64_t t, T dt, doubl
         E[t] += -dt * J + ca * ( b1 - b0 ) + cb * ( b3 - b2 );
         return;
     }
-    // the FP64 current as an FP32 pair J + Jl
-    const T J = ( T )Jd, Jl = ( T )( Jd - ( double )J );
+    // the FP64 current as an FP32 pair J + Jl (integer operations: FP64 conversions and
+    // adds take this GPU's FP64 pipe, 1/64 of the FP32 rate)
+    T J, Jl;
+    if constexpr( sizeof( T ) == 4 ) split_fp64( Jd, J, Jl );
+    else {
+        J = ( T )Jd;
+        Jl = T( 0 );
+    }
     T d1, e1, d2, e2, p1, q1, p2, q2, p3, q3, s, es, S, eS;
     two_sum( b1, -b0, d1, e1 );
     two_sum( b3, -b2, d2, e2 );
