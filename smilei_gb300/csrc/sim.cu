@@ -601,8 +601,10 @@ __device__ __forceinline__ void deposit_beyond( T *J2, int jsz, int jxs, int jz,
             for( int u = 0; u < nu; u++ ) {
                 const T ab = pick4( u, Ab[0], Ab[1], Ab[2], Ab3 ), db = pick4( u, twelfth * Db[0], twelfth * Db[1], twelfth * Db[2], Db3 );
                 const int ib = u < 3 ? lb + 1 + u : pb;
-#pragma unroll 1
-                for( int v = 0; v < nv; v++ ) {
+                // (the innermost loops are unrolled: independent adds in flight together)
+#pragma unroll
+                for( int v = 0; v < 4; v++ ) {
+                    if( v >= nv ) break;
                     const T ae = pick4( v, Ae[0], Ae[1], Ae[2], Ae3 ), de = pick4( v, De[0], De[1], De[2], De3 );
                     const int ie = v < 3 ? le + 1 + v : pe;
                     sh_add( &J[pa * sa + ib * sb + ie * se], ca * ( ab * ae + db * de ) );
@@ -614,8 +616,9 @@ __device__ __forceinline__ void deposit_beyond( T *J2, int jsz, int jxs, int jz,
 #pragma unroll 1
             for( int m = 0; m < 2; m++ ) {
                 const T cm = -( cra * ( m ? Pa[1] : Pa[0] ) );
-#pragma unroll 1
-                for( int v = 0; v < nv; v++ ) {
+#pragma unroll
+                for( int v = 0; v < 4; v++ ) {
+                    if( v >= nv ) break;
                     const T ae = pick4( v, Ae[0], Ae[1], Ae[2], Ae3 ), de = pick4( v, De[0], De[1], De[2], De3 );
                     const int ie = v < 3 ? le + 1 + v : pe;
                     sh_add( &J[( la + 2 + m ) * sa + pb * sb + ie * se], cm * ( Ab3 * ae + Db3 * de ) );
@@ -627,7 +630,7 @@ __device__ __forceinline__ void deposit_beyond( T *J2, int jsz, int jxs, int jz,
 #pragma unroll 1
             for( int m = 0; m < 2; m++ ) {
                 const T cm = -( cra * ( m ? Pa[1] : Pa[0] ) );
-#pragma unroll 1
+#pragma unroll
                 for( int u = 0; u < 3; u++ ) {
                     const T ab = u == 0 ? Ab[0] : ( u == 1 ? Ab[1] : Ab[2] ), db = u == 0 ? Db[0] : ( u == 1 ? Db[1] : Db[2] );
                     sh_add( &J[( la + 2 + m ) * sa + ( lb + 1 + u ) * sb + pe * se], cm * ( ab * Ae3 + twelfth * db * De3 ) );
