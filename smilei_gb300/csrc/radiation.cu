@@ -10,7 +10,7 @@
 //   production yield         computePhotonProductionYield (:225-262)
 //   Monte-Carlo pass         RadiationMonteCarlo::operator() (src/Radiation/RadiationMonteCarlo.cpp:62-611),
 //                            emitted energy tallied (no macro-photons)
-// Learned part: an FP32 MLP 2 -> H -> H -> 1 (tanh) maps (log10 chi, xi) to
+// Learned part: an FP32 MLP 2 -> H -> H -> 1 (tanh) maps (log10 chi, logit10(xi) / 3) to
 // log10(photon chi / chi).  It is trained on the GPU by the kernels below
 // (forward, backward, batch-reduced weight gradients, Adam) on samples whose
 // targets come from the table kernel, validated per (chi, xi) bin against the
@@ -253,10 +253,19 @@ __device__ __forceinline__ float mlp_forward( const MlpView &m, float u0, float 
     return y;
 }
 
+// The network's xi input: log10(xi / (1 - xi)) / 3, xi clamped to [1e-7, 1 - 2^-23].  The
+// inverse CDF is steep in xi at both ends (about 3 log10 xi near 0, a log of 1 - xi near
+// 1) and nearly linear in this coordinate.
+__device__ __forceinline__ float mlp_xi_input( float xi )
+{
+    xi = fminf( fmaxf( xi, 1e-7f ), 1.0f - 1.1920929e-7f );
+    return ( log10f( xi ) - log10f( 1.0f - xi ) ) * ( 1.0f / 3.0f );
+}
+
 __device__ __forceinline__ void mlp_inputs( const MlpView &m, double chi, double xi, float &u0, float &u1 )
 {
     u0 = 2.0f * ( ( float )log10( chi ) - m.lmin ) / m.lspan - 1.0f;
-    u1 = 2.0f * ( float )xi - 1.0f;
+    u1 = mlp_xi_input( ( float )xi );
 }
 
 __device__ double mlp_photon_chi( const MlpView &m, double chi, double xi )
@@ -323,7 +332,7 @@ __global__ void __launch_bounds__( 256 ) k_mlp_photon_chi_fast( MlpView m, int64
     for( int64_t i = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x; i < n; i += ( int64_t )gridDim.x * blockDim.x ) {
         const float c = ( float )chi[i];
         const float u0 = 2.0f * ( log10f( c ) - m.lmin ) / m.lspan - 1.0f;
-        const float u1 = 2.0f * ( float )xi[i] - 1.0f;
+        const float u1 = mlp_xi_input( ( float )xi[i] );
         float h1[H];
 #pragma unroll
         for( int k = 0; k < H; k++ ) h1[k] = tanh_fast( fmaf( sW1[2 * k], u0, fmaf( sW1[2 * k + 1], u1, sb1[k] ) ) );
@@ -465,7 +474,7 @@ __global__ void __launch_bounds__( 128 ) k_mlp_photon_chi_tc( MlpView m, int64_t
         if( i < n ) {
             c = ( float )chi[i];
             u0 = 2.0f * ( log10f( c ) - m.lmin ) / m.lspan - 1.0f;
-            u1 = 2.0f * ( float )xi[i] - 1.0f;
+            u1 = mlp_xi_input( ( float )xi[i] );
         }
         // inputs of the four rows this lane's fragments hold: 16 mt + gid + 8 hf
         float ru0[2][2], ru1[2][2];
@@ -547,7 +556,7 @@ __device__ __forceinline__ double mlp_photon_chi_smem( const MlpView &m, const M
         return mlp_photon_chi( m, chi, xi );
     } else {
         const float u0 = 2.0f * ( log10f( ( float )chi ) - m.lmin ) / m.lspan - 1.0f;
-        const float u1 = 2.0f * ( float )xi - 1.0f;
+        const float u1 = mlp_xi_input( ( float )xi );
         float h1[H];
 #pragma unroll
         for( int k = 0; k < H; k++ ) h1[k] = tanh_fast( fmaf( w.W1[2 * k], u0, fmaf( w.W1[2 * k + 1], u1, w.b1[k] ) ) );
@@ -578,7 +587,7 @@ __device__ __forceinline__ float mlp_coop( const MlpView &m, const MlpShared<H> 
 {
     constexpr int K = H >= 32 ? H / 32 : 1;
     const float u0 = 2.0f * ( log10f( chi ) - m.lmin ) / m.lspan - 1.0f;
-    const float u1 = 2.0f * xi - 1.0f;
+    const float u1 = mlp_xi_input( xi );
     const float *W2T = reinterpret_cast<const float *>( w.W2v );
     float h[K], acc[K];
 #pragma unroll
@@ -697,7 +706,7 @@ __device__ __forceinline__ void mc_pass_f32( const RadTab &t, const MlpView &m, 
                 float u0 = 0.0f, u1 = 0.0f;
                 if( net ) {
                     u0 = 2.0f * ( log10f( chi ) - m.lmin ) / m.lspan - 1.0f;
-                    u1 = 2.0f * u32 - 1.0f;
+                    u1 = mlp_xi_input( u32 );
                 }
                 const int gid = lane >> 2;
                 float ru0[2][2], ru1[2][2];
@@ -1034,7 +1043,8 @@ __global__ void __launch_bounds__( 128 ) k_radiate_resident( RadTab t, MlpView m
 }
 
 // ---- MLP training ------------------------------------------------------------
-// Samples: log10 chi uniform in [lmin, lmin + lspan], xi uniform in [0, 1);
+// Samples: log10 chi uniform in [lmin, lmin + lspan], xi uniform in [0, 1) (input
+// mlp_xi_input(xi));
 // target = log10(table photon chi / chi) / out_scale.
 __global__ void k_mlp_samples( RadTab t, int B, float lmin, float lspan, float out_scale, uint32_t seed,
                                uint32_t step, float *__restrict__ X, float *__restrict__ Y )
@@ -1047,7 +1057,7 @@ __global__ void k_mlp_samples( RadTab t, int B, float lmin, float lspan, float o
     const double chi = pow( 10.0, l );
     const double pc = tab_photon_chi( t, chi, xi );
     X[2 * b] = 2.0f * ( float )( ( l - lmin ) / lspan ) - 1.0f;
-    X[2 * b + 1] = 2.0f * ( float )xi - 1.0f;
+    X[2 * b + 1] = mlp_xi_input( ( float )xi );
     Y[b] = ( float )( log10( pc / chi ) / out_scale );
 }
 

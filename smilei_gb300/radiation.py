@@ -82,7 +82,8 @@ class RadiationTables:
 
 
 class PhotonChiMLP:
-    """FP32 2 -> H -> H -> 1 network for log10(photon chi / chi) given (log10 chi, xi)."""
+    """FP32 2 -> H -> H -> 1 network for log10(photon chi / chi) given log10 chi and
+    log10(xi / (1 - xi)) / 3 (the inverse CDF is steep in xi at both ends)."""
 
     def __init__(self, hidden=64, seed=1, log10_chi_range=(-4.0, 3.0)):
         h = ctypes.c_void_p()
