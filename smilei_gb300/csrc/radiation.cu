@@ -371,20 +371,21 @@ __device__ __forceinline__ uint32_t pack_half2( float lo, float hi )
     return *reinterpret_cast<const uint32_t *>( &h );
 }
 
-// The 64-wide network on one warp for up to 32 rows (two 16-row tiles; mtiles = 1 uses
-// only the first): ru0/ru1 hold the inputs of rows 16 mt + gid + 8 hf, the rows this
+// The 64-wide network on one warp for up to 16 MT rows (MT 16-row tiles together; mtiles
+// < MT uses only the first mtiles): ru0/ru1 hold the inputs of rows 16 mt + gid + 8 hf, the rows this
 // lane's fragments hold (gid = lane / 4, tig = lane % 4).  Returns in y[mt][hf] the
 // output before b3 of those rows, complete in all four lanes of the group.  W2h: FP16
 // W2 (row = output unit) with rows TC_W2_STRIDE halves apart.
+template <int MT>
 __device__ __forceinline__ void tc_network( const __half *__restrict__ W2h, const float *__restrict__ W1,
                                             const float *__restrict__ b1, const float *__restrict__ b2,
-                                            const float *__restrict__ W3, const float ( &ru0 )[2][2],
-                                            const float ( &ru1 )[2][2], int mtiles, float ( &y )[2][2] )
+                                            const float *__restrict__ W3, const float ( &ru0 )[MT][2],
+                                            const float ( &ru1 )[MT][2], int mtiles, float ( &y )[MT][2] )
 {
     const int lane = threadIdx.x & 31, gid = lane >> 2, tig = lane & 3;
-    float acc[2][8][4];
+    float acc[MT][8][4];
 #pragma unroll
-    for( int mt = 0; mt < 2; mt++ )
+    for( int mt = 0; mt < MT; mt++ )
 #pragma unroll
         for( int nt = 0; nt < 8; nt++ )
 #pragma unroll
@@ -392,9 +393,9 @@ __device__ __forceinline__ void tc_network( const __half *__restrict__ W2h, cons
 #pragma unroll
     for( int ks = 0; ks < 4; ks++ ) {
         // layer 1 for the columns k = 16 ks + 2 tig + {0, 1} (+ 8) of this lane's rows
-        uint32_t a[2][4];
+        uint32_t a[MT][4];
 #pragma unroll
-        for( int mt = 0; mt < 2; mt++ )
+        for( int mt = 0; mt < MT; mt++ )
 #pragma unroll
             for( int r = 0; r < 4; r++ ) { // r: (hf, kh) = (r & 1, r >> 1), the PTX order a0..a3
                 const int hf = r & 1, k0 = 16 * ks + 2 * tig + 8 * ( r >> 1 );
@@ -408,7 +409,7 @@ __device__ __forceinline__ void tc_network( const __half *__restrict__ W2h, cons
             const uint32_t b0 = *reinterpret_cast<const uint32_t *>( wrow );
             const uint32_t bb = *reinterpret_cast<const uint32_t *>( wrow + 8 );
 #pragma unroll
-            for( int mt = 0; mt < 2; mt++ )
+            for( int mt = 0; mt < MT; mt++ )
                 if( mt < mtiles )
                     asm volatile( "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
                                   "{%8,%9}, {%0,%1,%2,%3};\n"
@@ -420,7 +421,7 @@ __device__ __forceinline__ void tc_network( const __half *__restrict__ W2h, cons
     }
     // layer 2 activation and layer 3: rows gid (+ 8) of each tile, columns 8 nt + 2 tig + {0, 1}
 #pragma unroll
-    for( int mt = 0; mt < 2; mt++ ) {
+    for( int mt = 0; mt < MT; mt++ ) {
         y[mt][0] = y[mt][1] = 0.0f;
 #pragma unroll
         for( int nt = 0; nt < 8; nt++ )
@@ -431,7 +432,7 @@ __device__ __forceinline__ void tc_network( const __half *__restrict__ W2h, cons
             }
     }
 #pragma unroll
-    for( int mt = 0; mt < 2; mt++ )
+    for( int mt = 0; mt < MT; mt++ )
 #pragma unroll
         for( int hf = 0; hf < 2; hf++ ) {
             y[mt][hf] += __shfl_xor_sync( 0xffffffffu, y[mt][hf], 1 );
@@ -486,7 +487,7 @@ __global__ void __launch_bounds__( 128 ) k_mlp_photon_chi_tc( MlpView m, int64_t
                 ru1[mt][hf] = __shfl_sync( 0xffffffffu, u1, 16 * mt + gid + 8 * hf );
             }
         float y[2][2];
-        tc_network( sW2, sW1, sb1, sb2, sW3, ru0, ru1, 2, y );
+        tc_network<2>( sW2, sW1, sb1, sb2, sW3, ru0, ru1, 2, y );
         const float yl = tc_row( y, lane );
         if( i < n ) out[i] = chi[i] * ( double )exp10f( ( yl + b3 ) * m.out_scale );
     }
@@ -709,19 +710,32 @@ __device__ __forceinline__ void mc_pass_f32( const RadTab &t, const MlpView &m, 
                     u1 = mlp_xi_input( u32 );
                 }
                 const int gid = lane >> 2;
-                float ru0[2][2], ru1[2][2];
-#pragma unroll
-                for( int mt = 0; mt < 2; mt++ )
+                // one 16-row tile at a time (a second only past 16 rows): the accumulators
+                // of one tile, not two, stay live in this long loop
+                float y00 = 0.0f, y01 = 0.0f, y10 = 0.0f, y11 = 0.0f;
+#pragma unroll 1
+                for( int mt = 0; mt < 2; mt++ ) {
+                    if( mt * 16 >= nreq ) break;
+                    float ru0[1][2], ru1[1][2];
 #pragma unroll
                     for( int hf = 0; hf < 2; hf++ ) {
                         const int row = 16 * mt + gid + 8 * hf;
                         const int src = row < nreq ? ( int )__fns( req, 0, row + 1 ) : lane;
                         const float a0 = __shfl_sync( 0xffffffffu, u0, src ), a1 = __shfl_sync( 0xffffffffu, u1, src );
-                        ru0[mt][hf] = row < nreq ? a0 : 0.0f;
-                        ru1[mt][hf] = row < nreq ? a1 : 0.0f;
+                        ru0[0][hf] = row < nreq ? a0 : 0.0f;
+                        ru1[0][hf] = row < nreq ? a1 : 0.0f;
                     }
-                float yv[2][2];
-                tc_network( sw.W2h, sw.W1, sw.b1, sw.b2, sw.W3, ru0, ru1, nreq > 16 ? 2 : 1, yv );
+                    float y1[1][2];
+                    tc_network<1>( sw.W2h, sw.W1, sw.b1, sw.b2, sw.W3, ru0, ru1, 1, y1 );
+                    if( mt == 0 ) {
+                        y00 = y1[0][0];
+                        y01 = y1[0][1];
+                    } else {
+                        y10 = y1[0][0];
+                        y11 = y1[0][1];
+                    }
+                }
+                const float yv[2][2] = { { y00, y01 }, { y10, y11 } };
                 const float y = tc_row( yv, __popc( req & ( ( 1u << lane ) - 1u ) ) );
                 if( net ) pchi = ( double )chi * ( double )exp10f( ( y + sw.b3 ) * m.out_scale );
             }
