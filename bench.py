@@ -251,16 +251,19 @@ def run_gpu(args, rank, world, local_rank):
 
     ndim = len(cfg["n_cells"])
     tile, tuning, queue = ([args.tile] * ndim if args.tile else None), None, args.tile_queue
+    # TMA staging is the default of the 3D mixed form with 4x4x4 tiles; --no-tma turns it off
+    tma_choice = not args.no_tma
     if args.autotune:
         from smilei_gb300 import autotune
-        (best, queue), times = autotune.tune(build, ndim=ndim)
+        (best, queue, tma_choice), times = autotune.tune(build, ndim=ndim,
+                                                         stagings=(False,) if args.no_tma else (True, False))
         tile = list(best)
-        tuning = {"x".join(map(str, k)) + (" queue" if q else ""): round(v, 3) for (k, q), v in times.items()}
+        tuning = {"x".join(map(str, k)) + (" queue" if q else "") + (" tma" if t else ""): round(v, 3)
+                  for (k, q, t), v in times.items()}
     sim = build(tile)
     sim.set_tile_queue(queue)
-    # TMA staging is the default of the 3D mixed form with 4x4x4 tiles; --no-tma turns it off
     tma = len(cfg["n_cells"]) == 3 and args.form == "mixed" and list(tile or [4, 4, 4]) == [4, 4, 4]
-    if tma and args.no_tma:
+    if tma and not tma_choice:
         sim.set_tma_staging(False)
         tma = False
     nspec = len(cfg.get("species", [None]))

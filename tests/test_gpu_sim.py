@@ -165,6 +165,11 @@ def test_autotune_times_every_candidate_and_keeps_the_fastest(sim_mod):
     best, times = autotune.tune_tiles(build, ndim=3, warmup=1, steps=2)
     assert set(times) == set(autotune.CANDIDATES_3D)
     assert best == min(times, key=times.get) and all(t > 0 for t in times.values())
+    # the (tile, queue, staging) search: TMA staging is tried for the 4x4x4 tile only
+    best3, times3 = autotune.tune(build, ndim=3, tiles=[(4, 4, 4), (8, 4, 2)], warmup=1, steps=1)
+    assert set(times3) == {((4, 4, 4), q, t) for q in (False, True) for t in (True, False)} | \
+        {((8, 4, 2), q, False) for q in (False, True)}
+    assert best3 == min(times3, key=times3.get)
 
 
 @pytest.mark.parametrize("form,n_cells", [("mixed", [16, 16, 16]), ("fp64", [16, 16, 16]), ("mixed", [8, 16, 16])])
