@@ -1608,6 +1608,14 @@ __device__ __forceinline__ void two_prod( T a, T b, T &p, T &e )
 // is kept as the pair E - C (C the compensation), so an Ampere step adds no rounding
 // of its own to E: div E follows div J and the discrete curl of B exactly (the curl
 // part cancels in the divergence whatever B is).
+// The padded copies of E (p[0..2]) and B_m (p[3..5]) that the TMA tensor maps read:
+// rows of nz4[c] floats, a multiple of 16 bytes.  The field kernels write them beside
+// the arrays (null pointers: no TMA staging).
+struct PadOut {
+    float *p[6];
+    int nz4[6];
+};
+
 // FP64 to an FP32 pair hi + lo with integer operations: hi is d with its fraction cut
 // to 23 bits, lo the next 24 bits of the rest (hi + lo is d to about 2^-47 relative for
 // |d| above 2^-98; below, lo is 0).  Magnitudes beyond the FP32 range give +-infinity
@@ -1637,12 +1645,13 @@ __device__ __forceinline__ void split_fp64( double d, float &hi, float &lo )
 }
 
 template <class T>
-__device__ __forceinline__ void ampere_point( T *E, T *C, int64_t t, T dt, double Jd, T ca, T b1, T b0, T cb, T b3, T b2 )
+__device__ __forceinline__ T ampere_point( T *E, T *C, int64_t t, T dt, double Jd, T ca, T b1, T b0, T cb, T b3, T b2 )
 {
     if( !C ) {
         const T J = ( T )Jd;
-        E[t] += -dt * J + ca * ( b1 - b0 ) + cb * ( b3 - b2 );
-        return;
+        const T En = E[t] + ( -dt * J + ca * ( b1 - b0 ) + cb * ( b3 - b2 ) );
+        E[t] = En;
+        return En;
     }
     // the FP64 current as an FP32 pair J + Jl (integer operations: FP64 conversions and
     // adds take this GPU's FP64 pipe, 1/64 of the FP32 rate)
@@ -1668,10 +1677,11 @@ __device__ __forceinline__ void ampere_point( T *E, T *C, int64_t t, T dt, doubl
     const T En = Es + low;
     C[t] = ( En - Es ) - low;
     E[t] = En;
+    return En;
 }
 
 template <int DIM, class T>
-__global__ void k_ampere_all( GridInfo g, Fields<T> f, T dt, T dtdx, T dtdy, T dtdz )
+__global__ void k_ampere_all( GridInfo g, Fields<T> f, T dt, T dtdx, T dtdy, T dtdz, PadOut po )
 {
     const int nxp = g.np[0], nyp = g.np[1], nyd = nyp + 1;
     if( DIM == 3 ) {
@@ -1680,19 +1690,25 @@ __global__ void k_ampere_all( GridInfo g, Fields<T> f, T dt, T dtdx, T dtdy, T d
         const int i = row / nyd, j = row % nyd;
         for( int k = threadIdx.x; k < nzd; k += blockDim.x ) {
             if( j < nyp && k < nzp ) {
-                const int64_t t = ( ( int64_t )i * nyp + j ) * nzp + k;
-                ampere_point( f.E[0], f.Ec[0], t, dt, f.J[0][t], dtdy, f.B[2][( ( int64_t )i * nyd + j + 1 ) * nzp + k], f.B[2][( ( int64_t )i * nyd + j ) * nzp + k],
-                              -dtdz, f.B[1][( ( int64_t )i * nyp + j ) * nzd + k + 1], f.B[1][( ( int64_t )i * nyp + j ) * nzd + k] );
+                const int64_t r = ( int64_t )i * nyp + j, t = r * nzp + k;
+                const T e = ampere_point( f.E[0], f.Ec[0], t, dt, f.J[0][t], dtdy, f.B[2][( ( int64_t )i * nyd + j + 1 ) * nzp + k], f.B[2][( ( int64_t )i * nyd + j ) * nzp + k],
+                                          -dtdz, f.B[1][( ( int64_t )i * nyp + j ) * nzd + k + 1], f.B[1][( ( int64_t )i * nyp + j ) * nzd + k] );
+                if constexpr( sizeof( T ) == 4 )
+                    if( po.p[0] ) po.p[0][r * po.nz4[0] + k] = e;
             }
             if( i < nxp && k < nzp ) {
-                const int64_t t = ( ( int64_t )i * nyd + j ) * nzp + k;
-                ampere_point( f.E[1], f.Ec[1], t, dt, f.J[1][t], -dtdx, f.B[2][( ( int64_t )( i + 1 ) * nyd + j ) * nzp + k], f.B[2][t],
-                              dtdz, f.B[0][( ( int64_t )i * nyd + j ) * nzd + k + 1], f.B[0][( ( int64_t )i * nyd + j ) * nzd + k] );
+                const int64_t r = ( int64_t )i * nyd + j, t = r * nzp + k;
+                const T e = ampere_point( f.E[1], f.Ec[1], t, dt, f.J[1][t], -dtdx, f.B[2][( ( int64_t )( i + 1 ) * nyd + j ) * nzp + k], f.B[2][t],
+                                          dtdz, f.B[0][( ( int64_t )i * nyd + j ) * nzd + k + 1], f.B[0][( ( int64_t )i * nyd + j ) * nzd + k] );
+                if constexpr( sizeof( T ) == 4 )
+                    if( po.p[1] ) po.p[1][r * po.nz4[1] + k] = e;
             }
             if( i < nxp && j < nyp ) {
-                const int64_t t = ( ( int64_t )i * nyp + j ) * nzd + k;
-                ampere_point( f.E[2], f.Ec[2], t, dt, f.J[2][t], dtdx, f.B[1][( ( int64_t )( i + 1 ) * nyp + j ) * nzd + k], f.B[1][t],
-                              -dtdy, f.B[0][( ( int64_t )i * nyd + j + 1 ) * nzd + k], f.B[0][( ( int64_t )i * nyd + j ) * nzd + k] );
+                const int64_t r = ( int64_t )i * nyp + j, t = r * nzd + k;
+                const T e = ampere_point( f.E[2], f.Ec[2], t, dt, f.J[2][t], dtdx, f.B[1][( ( int64_t )( i + 1 ) * nyp + j ) * nzd + k], f.B[1][t],
+                                          -dtdy, f.B[0][( ( int64_t )i * nyd + j + 1 ) * nzd + k], f.B[0][( ( int64_t )i * nyd + j ) * nzd + k] );
+                if constexpr( sizeof( T ) == 4 )
+                    if( po.p[2] ) po.p[2][r * po.nz4[2] + k] = e;
             }
         }
     } else {
@@ -1861,7 +1877,7 @@ __global__ void k_center_b2d( GridInfo g, Fields<T> f, int64_t *__restrict__ ste
 }
 
 template <int DIM, class T>
-__global__ void k_faraday_center( GridInfo g, Fields<T> f, T dtdx, T dtdy, T dtdz )
+__global__ void k_faraday_center( GridInfo g, Fields<T> f, T dtdx, T dtdy, T dtdz, PadOut po )
 {
     const int nxp = g.np[0], nyp = g.np[1], nxd = nxp + 1, nyd = nyp + 1;
     const int Nx = g.N[0], Ny = g.N[1];
@@ -1878,7 +1894,10 @@ __global__ void k_faraday_center( GridInfo g, Fields<T> f, T dtdx, T dtdy, T dtd
                 const T nw = old + ( -dtdy * ( Ez[( ( int64_t )i * nyp + jc ) * nzd + k] - Ez[( ( int64_t )i * nyp + jc - 1 ) * nzd + k] )
                                      + dtdz * ( Ey[( ( int64_t )i * nyd + j ) * nzp + kc] - Ey[( ( int64_t )i * nyd + j ) * nzp + kc - 1] ) );
                 f.B[0][t] = nw;
-                f.Bm[0][t] = ( nw + old ) * T( 0.5 );
+                const T bm = ( nw + old ) * T( 0.5 );
+                f.Bm[0][t] = bm;
+                if constexpr( sizeof( T ) == 4 )
+                    if( po.p[3] ) po.p[3][( ( int64_t )i * nyd + j ) * po.nz4[3] + k] = bm;
             }
             if( j < nyp ) { // By(d,p,d)
                 const int ic = canon( i, nxd, Nx ), kc = canon( k, nzd, Nz );
@@ -1887,7 +1906,10 @@ __global__ void k_faraday_center( GridInfo g, Fields<T> f, T dtdx, T dtdy, T dtd
                 const T nw = old + ( -dtdz * ( Ex[( ( int64_t )i * nyp + j ) * nzp + kc] - Ex[( ( int64_t )i * nyp + j ) * nzp + kc - 1] )
                                      + dtdx * ( Ez[( ( int64_t )ic * nyp + j ) * nzd + k] - Ez[( ( int64_t )( ic - 1 ) * nyp + j ) * nzd + k] ) );
                 f.B[1][t] = nw;
-                f.Bm[1][t] = ( nw + old ) * T( 0.5 );
+                const T bm = ( nw + old ) * T( 0.5 );
+                f.Bm[1][t] = bm;
+                if constexpr( sizeof( T ) == 4 )
+                    if( po.p[4] ) po.p[4][( ( int64_t )i * nyp + j ) * po.nz4[4] + k] = bm;
             }
             if( k < nzp ) { // Bz(d,d,p)
                 const int ic = canon( i, nxd, Nx ), jc = canon( j, nyd, Ny );
@@ -1896,7 +1918,10 @@ __global__ void k_faraday_center( GridInfo g, Fields<T> f, T dtdx, T dtdy, T dtd
                 const T nw = old + ( -dtdx * ( Ey[( ( int64_t )ic * nyd + j ) * nzp + k] - Ey[( ( int64_t )( ic - 1 ) * nyd + j ) * nzp + k] )
                                      + dtdy * ( Ex[( ( int64_t )i * nyp + jc ) * nzp + k] - Ex[( ( int64_t )i * nyp + jc - 1 ) * nzp + k] ) );
                 f.B[2][t] = nw;
-                f.Bm[2][t] = ( nw + old ) * T( 0.5 );
+                const T bm = ( nw + old ) * T( 0.5 );
+                f.Bm[2][t] = bm;
+                if constexpr( sizeof( T ) == 4 )
+                    if( po.p[5] ) po.p[5][( ( int64_t )i * nyd + j ) * po.nz4[5] + k] = bm;
             }
         }
     } else {
@@ -2573,6 +2598,7 @@ struct sg_sim {
     int *d_queue = nullptr;   // its item counter
     bool tma = false;         // field tile staged by TMA (3D mixed, 4x4x4 tiles)
     float *tma_pad[6] = {};   // E, B_m with rows padded to a multiple of 4 values
+    bool pad_dirty = true;    // E or B_m changed outside the field kernels (which keep the copies)
     int tma_nz4[6] = {};      // their padded row lengths
     TmaFields tma_maps{};     // tensor maps over them
     int *d_flags = nullptr; // [0] status, [1 + s] spill count of species s, [1 + max_species + s] removed
@@ -2637,6 +2663,36 @@ Fields<T> field_view( sg_sim *S )
         f.Ec[c] = static_cast<T *>( S->ecomp[c] );
     }
     return f;
+}
+
+// Where the field kernels write the padded copies of E and B_m (TMA staging only).
+inline PadOut pad_out( const sg_sim *S )
+{
+    PadOut po{};
+    if( S->tma )
+        for( int c = 0; c < 6; c++ ) {
+            po.p[c] = S->tma_pad[c];
+            po.nz4[c] = S->tma_nz4[c];
+        }
+    return po;
+}
+
+// The padded copies from the arrays, where E or B_m changed outside the field kernels
+// (a field set from the host, the Poisson solve, TMA staging switched on): each step's
+// Ampere and Faraday kernels keep them current after that.
+int pad_fields( sg_sim *S, cudaStream_t st )
+{
+    if( !S->tma || !S->pad_dirty ) return SG_OK;
+    Fields<float> f = field_view<float>( S );
+    for( int c = 0; c < 6; c++ ) {
+        const float *src = c < 3 ? f.E[c] : f.Bm[c - 3];
+        const int64_t rows = S->fsize[c] / S->fshape[c][2];
+        k_pad_rows<<<( unsigned )std::min<int64_t>( ( rows * S->tma_nz4[c] + 255 ) / 256, 152 * 32 ), 256, 0, st>>>(
+            src, S->tma_pad[c], rows, S->fshape[c][2], S->tma_nz4[c] );
+        SG_LAUNCH_CHECK( "k_pad_rows" );
+    }
+    S->pad_dirty = false;
+    return SG_OK;
 }
 
 // comp 0..2 E, 3..5 B, 6..8 B_m, 9..11 J -> staggering flags
@@ -2769,7 +2825,7 @@ int launch_fields( sg_sim *S, cudaStream_t st, int &launches )
     const T dt = T( g.dt ), dtdx = T( g.dt / g.dx[0] ), dtdy = T( g.dt / g.dx[1] ), dtdz = T( DIM == 3 ? g.dt / g.dx[2] : 0.0 );
     const unsigned rows = DIM == 3 ? ( unsigned )( ( g.np[0] + 1 ) * ( g.np[1] + 1 ) ) : ( unsigned )( g.np[0] + 1 );
     const int tpb = DIM == 3 ? ( g.np[2] + 1 <= 128 ? 128 : 256 ) : 256;
-    k_ampere_all<DIM, T><<<rows, tpb, 0, st>>>( g, f, dt, dtdx, dtdy, dtdz );
+    k_ampere_all<DIM, T><<<rows, tpb, 0, st>>>( g, f, dt, dtdx, dtdy, dtdz, pad_out( S ) );
     SG_LAUNCH_CHECK( "k_ampere_all" );
     if( DIM == 2 && ( g.open[0] || g.open[1] ) ) {
         const int64_t pts = ( int64_t )( g.np[0] + 1 ) * ( g.np[1] + 1 );
@@ -2784,7 +2840,7 @@ int launch_fields( sg_sim *S, cudaStream_t st, int &launches )
         launches += 4;
         return SG_OK;
     }
-    k_faraday_center<DIM, T><<<rows, tpb, 0, st>>>( g, f, dtdx, dtdy, dtdz );
+    k_faraday_center<DIM, T><<<rows, tpb, 0, st>>>( g, f, dtdx, dtdy, dtdz, pad_out( S ) );
     SG_LAUNCH_CHECK( "k_faraday_center" );
     launches += 2;
     return SG_OK;
@@ -2912,18 +2968,6 @@ int enqueue_step( sg_sim *S, cudaStream_t st, const StreamIn *in = nullptr )
         k_bump_step<<<1, 1, 0, st>>>( S->d_rad_step );
         SG_LAUNCH_CHECK( "k_bump_step" );
         launches++;
-    }
-    if( S->tma ) {
-        // the padded copies of E and B_m that the tensor maps read
-        Fields<float> f = field_view<float>( S );
-        for( int c = 0; c < 6; c++ ) {
-            const float *src = c < 3 ? f.E[c] : f.Bm[c - 3];
-            const int64_t rows = S->fsize[c] / S->fshape[c][2];
-            k_pad_rows<<<( unsigned )std::min<int64_t>( ( rows * S->tma_nz4[c] + 255 ) / 256, 152 * 32 ), 256, 0, st>>>(
-                src, S->tma_pad[c], rows, S->fshape[c][2], S->tma_nz4[c] );
-            SG_LAUNCH_CHECK( "k_pad_rows" );
-            launches++;
-        }
     }
     for( auto &s : S->sp ) {
         if( in && &s == &S->sp[in->species] ) {
@@ -3249,6 +3293,7 @@ int rebuild_species( sg_sim *S, SpeciesState &s, int shift, int x0, int x1 )
 // (laserDisabled, :138-145), particles follow and the fresh cells are filled.
 int window_shift( sg_sim *S )
 {
+    S->pad_dirty = true; // the fields move
     const int P = S->win_shift;
     const GridInfo &g = S->g;
     cudaStream_t st = S->stream;
@@ -3515,6 +3560,7 @@ int sg_sim_set_tma_staging( sg_sim *S, int on )
         if( r != CUDA_SUCCESS ) return set_error( SG_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d) for field %d", ( int )r, field );
     }
     S->tma = true;
+    S->pad_dirty = true;
     drop_graphs( S );
     return SG_OK;
 }
@@ -3660,6 +3706,7 @@ int sg_sim_set_field( sg_sim *S, int comp, const double *host )
     SG_REQUIRE( comp >= 0 && comp < 12, "component out of range" );
     const int64_t n = S->fsize[comp];
     SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
+    S->pad_dirty = true;
     if( !S->mixed || felem( S, comp ) == 8 ) {
         SG_CUDA_TRY( cudaMemcpy( S->fptr[comp], host, n * 8, cudaMemcpyHostToDevice ) );
     } else {
@@ -3738,6 +3785,8 @@ int sg_sim_step( sg_sim *S, int nsteps )
     SG_REQUIRE( S, "NULL simulation" );
     SG_REQUIRE( nsteps >= 0, "nsteps < 0" );
     for( int it = 0; it < nsteps; it++ ) {
+        int rp = pad_fields( S, S->stream );
+        if( rp ) return rp;
         const int parity = S->sp.empty() ? 0 : S->sp[0].cur;
         // the window moves at the end of this step (SimWindow::isMoving, SimWindow.cpp:93-96);
         // the x boundaries of this step are then skipped (ElectroMagn.cpp:374)
@@ -4239,7 +4288,8 @@ int sg_sim_step_host( sg_sim *S, int species, const void *host_in, void *host_ou
         }
         SG_CUDA_TRY( cudaEventRecord( S->copy_ev[2 + j], cs ) );
     }
-    r = enqueue_step( S, S->stream, &in );
+    r = pad_fields( S, S->stream );
+    if( r == SG_OK ) r = enqueue_step( S, S->stream, &in );
     if( r ) {
         cudaStreamSynchronize( cs );
         cudaStreamSynchronize( S->stream );
@@ -4746,6 +4796,7 @@ int sg_sim_solve_poisson( sg_sim *S, double max_error, int max_iter, int *iterat
     SG_REQUIRE( max_iter >= 0, "max_iter < 0" );
     const GridInfo &g = S->g;
     cudaStream_t st = S->stream;
+    S->pad_dirty = true; // E is replaced
     const int64_t n = phys_nodes( g );
     const size_t nrho = ( size_t )ext( g, 0, 0 ) * ext( g, 1, 0 ) * ext( g, 2, 0 );
     // scratch: rho (ghosted) + phi, r, p, Ap (physical) + E (ndim x physical) + scalars
