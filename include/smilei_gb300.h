@@ -179,8 +179,9 @@ int sg_sim_set_tile_queue( sg_sim *sim, int on );
  * with 4x4x4 tiles, periodic).  on = 1 (the default for such a simulation, set by
  * sg_sim_create): one thread issues a tensor-memory-accelerator copy
  * (cp.async.bulk.tensor, completion on an mbarrier) per component; the tensor maps need
- * rows of a multiple of 16 bytes, so every step first copies E and B_m into padded
- * arrays (six more field arrays of device memory).  on = 0: every thread copies words
+ * rows of a multiple of 16 bytes, so the field kernels also write E and B_m into padded
+ * arrays (six more field arrays of device memory; a copy pass refreshes them after E or
+ * B_m change outside a step).  on = 0: every thread copies words
  * with cp.async; no padded arrays are written.  The results are the same either way.
  * Any other simulation refuses on = 1.  No reference counterpart (the reference's
  * gather reads the field arrays directly, Interpolator3D2Order.cpp:225-245). */
