@@ -319,3 +319,34 @@ def test_tma_staging_step_matches_oracle(sim_mod, cpu_oracle, pusher, ppc, queue
     for pg, mg, pr, mr, cl, n_cells in parts:
         assert rel_err(mg, mr) <= tol
         assert position_error(pg, pr, cl, n_cells) <= tol
+
+
+def test_tma_copies_follow_fields_set_between_steps(sim_mod):
+    """With TMA staging the field kernels keep the padded copies of E and B_m that the
+    tensor maps read; a field set from the host between (graph-replayed) steps makes the
+    next step copy them again.  The same sequence with word copies (which read the arrays
+    themselves) must give the same fields and momenta: 2 steps, new E and B_m from the
+    host, 2 more steps (1e-5: the deposit's atomics add in another order)."""
+    simulation, synthetic = sim_mod
+    n_cells, cl, dt, fields, species = make_case(synthetic, 3, 9, [(1.0, -1.0, "boris", 6, 0.14)])
+    fields2 = synthetic.periodic_em(17, n_cells)
+    out = []
+    for tma in (True, False):
+        sim = simulation.Simulation(n_cells, cl, dt, form="mixed", use_graph=True)
+        sim.set_tma_staging(tma)
+        for k in FIELDS:
+            sim.set_field(k, fields[k])
+        s = species[0]
+        sim.add_species(s["mass"], s["q"], s["pusher"], s["pos"], s["mom"], s["weight"])
+        sim.step(2)
+        for k in ("Ex", "Ey", "Ez", "Bx_m", "By_m", "Bz_m"):
+            sim.set_field(k, fields2[k])
+        sim.step(2)
+        p, m, w = sim.get_species(0)
+        o = np.argsort(w)
+        out.append(({k: sim.get_field(k) for k in FIELDS}, m[:, o]))
+        sim.close()
+    (fa, ma), (fb, mb) = out
+    for k in FIELDS:
+        assert rel_err(fa[k], fb[k]) <= 1e-5, k
+    assert rel_err(ma, mb) <= 1e-5
