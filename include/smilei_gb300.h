@@ -394,11 +394,13 @@ int sg_rad_production_yield( const sg_rad_tables *tables, int64_t n, const doubl
                              double *out, sg_stream_t stream );
 
 /* One Monte-Carlo radiation pass over n particles (device arrays: mom[3n] updated,
- * weight[n], tau[n] optical depth updated, chi_out[n] optional, Epart/Bpart[3n] the
- * interpolated fields): replaces RadiationMonteCarlo::operator()
- * (src/Radiation/RadiationMonteCarlo.cpp:62, called from Species.cpp:615) with the
- * emitted energy tallied instead of macro-photons created.  Particle p draws from its
- * own counter-based stream (seed, first_id + p, step).  radiated (device double) and
+ * weight[n], tau[n] optical depth updated, chi_out[n] optional: chi of the final
+ * momentum, RadiationMonteCarlo.cpp:642-655; Epart/Bpart[3n] the interpolated fields):
+ * replaces RadiationMonteCarlo::operator() (src/Radiation/RadiationMonteCarlo.cpp:62,
+ * called from Species.cpp:615) with the emitted energy tallied instead of macro-photons
+ * created.  Particle p draws from its own counter-based stream (seed, first_id + p,
+ * step): xorshift32 from that state with x / 2^32 per draw, the stream a reference
+ * Random seeded with the same state gives (src/Tools/Random.h:74-75).  radiated (device double) and
  * n_emissions (device) are accumulated.  mlp: NULL for the table inverse CDF, or a
  * validated network (sg_mlp_validate) used wherever its checked error is within
  * tolerance. */

@@ -425,6 +425,38 @@ class RefOps(_Backend):
         self.lib.ref_rad_photon_chi(len(chi), _ptr(chi), _ptr(xi), _ptr(out))
         return out
 
+    def rad_monte_carlo(self, factors, dt, mass, charge, pos, mom, weight, tau, E, B, seeds, sampling=0,
+                        threshold=2.0, max_emissions=10):
+        """The reference's RadiationMonteCarlo::operator() with the default tables, particle p
+        drawing from Random(seeds[p]).  factors: dict(factor_dNph_dt, factor_classical,
+        min_chi_continuous, min_chi_discontinuous, inv_norm_E_schwinger).  mom and tau are
+        updated in place.  Returns (radiated, chi, photons) with photons = dict(pos, mom,
+        weight, chi, tau) in creation order (None without a photon species, sampling = 0)."""
+        pos = _f64(pos); ndim, n = pos.shape
+        assert mom.dtype == np.float64 and mom.flags.c_contiguous and tau.dtype == np.float64
+        chi = np.zeros(n)
+        cap = max(1, n * max_emissions * max(sampling, 1))
+        ph_pos = np.zeros((ndim, cap)); ph_mom = np.zeros((3, cap)); ph_w = np.zeros(cap)
+        ph_chi = np.zeros(cap); ph_tau = np.zeros(cap)
+        nph = ctypes.c_long(); rad = ctypes.c_double()
+        seeds = np.ascontiguousarray(seeds, dtype=np.uint32)
+        f = factors
+        self.lib.ref_monte_carlo(ndim, n, ctypes.c_double(dt), ctypes.c_double(mass), ctypes.c_double(charge),
+                                 ctypes.c_double(f["factor_dNph_dt"]), ctypes.c_double(f["factor_classical"]),
+                                 ctypes.c_double(f["min_chi_continuous"]), ctypes.c_double(f["min_chi_discontinuous"]),
+                                 ctypes.c_double(f["inv_norm_E_schwinger"]), _ptr(pos), _ptr(mom),
+                                 _ptr(_f64(weight)), _ptr(tau), _ptr(chi), _ptr(_f64(E)), _ptr(_f64(B)),
+                                 _ptr(seeds), sampling, ctypes.c_double(threshold), max_emissions,
+                                 ctypes.c_long(cap), _ptr(ph_pos), _ptr(ph_mom), _ptr(ph_w), _ptr(ph_chi),
+                                 _ptr(ph_tau), ctypes.byref(nph), ctypes.byref(rad))
+        photons = None
+        if sampling > 0:
+            k = int(nph.value)
+            assert k <= cap
+            photons = dict(pos=ph_pos[:, :k].copy(), mom=ph_mom[:, :k].copy(), weight=ph_w[:k].copy(),
+                           chi=ph_chi[:k].copy(), tau=ph_tau[:k].copy())
+        return rad.value, chi, photons
+
 
 class RadTablesC(ctypes.Structure):
     """Mirror of or_rad_tables in rad_oracle.c."""
@@ -494,6 +526,13 @@ def _rad_lib():
     L.or_rad_monte_carlo.restype = ctypes.c_double
     L.or_rng_init.restype = ctypes.c_uint32
     return L
+
+
+def rng_seeds(seed, first_id, step, n):
+    """Initial xorshift32 state of each particle's random stream (rad_oracle.c or_rng_init)."""
+    L = _rad_lib()
+    return np.array([L.or_rng_init(ctypes.c_uint32(seed), ctypes.c_uint32((first_id + p) & 0xFFFFFFFF),
+                                   ctypes.c_uint32(step)) for p in range(n)], dtype=np.uint32)
 
 
 def rad_yield(tables: RadTables, chi, gamma):

@@ -3,7 +3,8 @@
 # they lie in the reference tree, into oracle/_ref/libsmilei_ref_ops.so.
 #
 # Only the files the hot path needs are compiled (interpolators, pushers,
-# projectors, Yee solvers, fields, particles, radiation tables), directly with
+# projectors, Yee solvers, fields, particles, radiation tables and the
+# Monte-Carlo radiation operator), directly with
 # g++; the reference's own build system is not used.  The reference headers
 # name MPI and HDF5 types, so oracle/shims supplies declaration-level,
 # single-rank stand-ins for <mpi.h> and <hdf5.h>; none of the compiled
@@ -36,7 +37,7 @@ Projector/Projector2D2Order.cpp Projector/Projector3D2Order.cpp
 ElectroMagnSolver/MA_Solver2D_norm.cpp ElectroMagnSolver/MA_Solver3D_norm.cpp
 ElectroMagnSolver/MF_Solver2D_Yee.cpp ElectroMagnSolver/MF_Solver3D_Yee.cpp
 Field/Field.cpp Field/Field2D.cpp Field/Field3D.cpp Particles/Particles.cpp
-Radiation/RadiationTables.cpp Radiation/RadiationTablesDefault.cpp Radiation/Table.cpp Radiation/Table2D.cpp
+Radiation/RadiationTables.cpp Radiation/RadiationTablesDefault.cpp Radiation/Radiation.cpp Radiation/RadiationMonteCarlo.cpp Radiation/Table.cpp Radiation/Table2D.cpp
 SmileiMPI/AsyncMPIbuffers.cpp Tools/H5.cpp Particles/Particle.cpp
 ElectroMagnBC/ElectroMagnBC.cpp ElectroMagnBC/ElectroMagnBC2D.cpp ElectroMagnBC/ElectroMagnBC2D_SM.cpp
 ElectroMagn/Laser.cpp Profiles/Function.cpp Profiles/Profile.cpp Tools/gpu.cpp

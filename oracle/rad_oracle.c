@@ -8,7 +8,9 @@
  * this oracle draw identical numbers: state = fmix32(seed ^ fmix32(id) ^
  * fmix32(step + 0x9e3779b9)) (MurmurHash3's 32-bit finaliser), then
  * successive xorshift32 steps (Marsaglia 2003, as src/Tools/Random.h:9-20),
- * each mapped to [0, 1) by x * (1 - 1e-11) / 2^32 (Random.h:21-24).
+ * each mapped to (0, 1) by x / 2^32 (Random::uniform, Random.h:74-75,129, the
+ * draw RadiationMonteCarlo::operator() makes).  A reference Random seeded with
+ * a particle's initial state draws that particle's stream.
  */
 #include <math.h>
 #include <stddef.h>
@@ -41,7 +43,7 @@ uint32_t or_rng_init( uint32_t seed, uint32_t id, uint32_t step )
 static inline double rng_uniform( uint32_t *s )
 {
     *s = xorshift32( *s );
-    return ( double )( *s ) * ( ( 1.0 - 1e-11 ) / 4294967296.0 );
+    return ( double )( *s ) * ( 1.0 / 4294967296.0 );
 }
 
 typedef struct {
@@ -151,7 +153,7 @@ static inline double ridgers_energy( const or_rad_tables *t, double chi, double 
  * creation: the emitted energy is tallied (the branch taken when no photon species is
  * given, :545-551).  Per particle, the random draws come from its own counter-based
  * stream (id = first_id + index, step).  Returns the radiated energy sum_p w * dgamma
- * (times mass is up to the caller) and stores each particle's chi.
+ * (times mass is up to the caller) and stores each particle's chi after the pass.
  * photon_chi_fn: 0 = table, else user callback (not used by the oracle). */
 /* Macro-photon output of a Monte-Carlo pass (RadiationMonteCarlo.cpp:425-545): an
  * emission whose photon_gamma >= threshold, while the particle has made fewer than
@@ -216,12 +218,10 @@ static double mc_pass( const or_rad_tables *t, int64_t n, double dt, double mass
         uint32_t rs = or_rng_init( seed, first_id + ( uint32_t )p, step );
         double local_time = 0.0, emission_time = 0.0;
         int it = 0, i_photon = 0;
-        double last_chi = 0.0;
         while( local_time < dt && it < max_it ) {
             const double g = sqrt( 1.0 + px * px + py * py + pz * pz );
             if( g < 1.1 ) break;
             const double chi = particle_chi( qm2, px, py, pz, g, Ex, Ey, Ez, Bx, By, Bz, t->inv_norm_E_schwinger );
-            last_chi = chi;
             if( chi > t->min_chi_discontinuous && tau[p] <= eps_tau ) {
                 while( tau[p] <= eps_tau ) tau[p] = -log( 1.0 - rng_uniform( &rs ) );
             }
@@ -276,7 +276,10 @@ static double mc_pass( const or_rad_tables *t, int64_t n, double dt, double mass
         mom[p] = px;
         mom[n + p] = py;
         mom[2 * n + p] = pz;
-        if( chi_out ) chi_out[p] = last_chi;
+        if( chi_out ) { /* chi of the final momentum (RadiationMonteCarlo.cpp:642-655) */
+            const double gf = sqrt( 1.0 + px * px + py * py + pz * pz );
+            chi_out[p] = particle_chi( qm2, px, py, pz, gf, Ex, Ey, Ez, Bx, By, Bz, t->inv_norm_E_schwinger );
+        }
     }
     if( n_emissions ) *n_emissions = nem;
     return radiated;

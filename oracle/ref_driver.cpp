@@ -3,7 +3,7 @@
 // oracle/build_ref.sh compiles a handful of the reference's operator sources
 // (Interpolator{2D,3D}2Order, Pusher{Boris,Vay,HigueraCary},
 // Projector{2D,3D}2Order, MA_Solver{2D,3D}_norm, MF_Solver{2D,3D}_Yee,
-// RadiationTables) straight from the reference tree and links them with this
+// RadiationTables, RadiationMonteCarlo) straight from the reference tree and links them with this
 // file into oracle/_ref/libsmilei_ref_ops.so.  The extern "C" entry points
 // below build the minimum reference objects those operators read (Params,
 // Patch, Species, ElectroMagn, SmileiMPI), call the operator exactly the way
@@ -62,6 +62,8 @@
 #include "MF_Solver3D_Yee.h"
 #include "RadiationTables.h"
 #include "RadiationTablesDefault.h"
+#include "RadiationMonteCarlo.h"
+#include "Random.h"
 #include "ElectroMagnBC2D_SM.h"
 #include "Laser.h"
 #include "Profile.h"
@@ -383,6 +385,84 @@ int ref_rad_photon_chi( int n, const double *chi, const double *xi, double *out 
 {
     RadiationTables *r = rad();
     for( int i = 0; i < n; i++ ) out[i] = r->computeRandomPhotonChiWithInterpolation( chi[i], xi[i] );
+    return 0;
+}
+
+// RadiationMonteCarlo::operator() (RadiationMonteCarlo.cpp:62-656) with the default
+// tables, as Species::dynamics calls it (Species.cpp:615): particle p alone in each call
+// (istart = p, iend = p + 1) and with its own Random(seeds[p]), so that its draws are the
+// xorshift32 stream started from seeds[p].  The table factors, the chi thresholds and
+// 1/E_Schwinger are given (RadiationTables::initialization and the Radiation constructor
+// read them from the namelist).  sampling > 0 passes a photon species with chi and tau
+// (Species.cpp:615 with a radiation_photon_species); its photons, in creation order, are
+// copied out up to cap (ph_pos[d * cap + k], ph_mom[c * cap + k]) and *n_photons counts
+// them all.  mom[c * n + p], Epart/Bpart[c * n + p]; mom, tau and chi are updated.
+int ref_monte_carlo( int ndim, int n, double dt, double mass, double charge, double factor_dNph_dt,
+                     double factor_classical, double min_chi_continuous, double min_chi_discontinuous,
+                     double inv_norm_E_schwinger, const double *pos, double *mom, const double *weight, double *tau,
+                     double *chi, const double *Epart, const double *Bpart, const unsigned *seeds, int sampling,
+                     double threshold, int max_emissions, long cap, double *ph_pos, double *ph_mom, double *ph_w,
+                     double *ph_chi, double *ph_tau, long *n_photons, double *radiated )
+{
+    RadiationTables *r = rad();
+    r->factor_dNph_dt_ = factor_dNph_dt;
+    r->factor_classical_radiated_power_ = factor_classical;
+    r->minimum_chi_continuous_ = min_chi_continuous;
+    r->minimum_chi_discontinuous_ = min_chi_discontinuous;
+    Params *params = zeroed<Params>();
+    params->nDim_particle = ndim;
+    params->timestep = dt;
+    Species *sp = zeroed<Species>();
+    sp->mass_ = mass;
+    sp->radiation_photon_sampling_ = sampling > 0 ? sampling : 1;
+    sp->radiation_max_emissions_ = max_emissions;
+    sp->radiation_photon_gamma_threshold_ = threshold;
+    Random seed0( 1u );
+    RadiationMonteCarlo mc( *params, sp, &seed0 );
+    // the Params constants behind E_Schwinger are not constructed in the zero-filled Params
+    mc.inv_norm_E_Schwinger_ = inv_norm_E_schwinger;
+    mc.norm_E_Schwinger_ = 1.0 / inv_norm_E_schwinger;
+
+    SmileiMPI *smpi = make_smpi( ndim, n );
+    std::memcpy( smpi->dynamics_Epart[0].data(), Epart, 3 * ( std::size_t )n * sizeof( double ) );
+    std::memcpy( smpi->dynamics_Bpart[0].data(), Bpart, 3 * ( std::size_t )n * sizeof( double ) );
+    std::vector<short> q( n, ( short )charge );
+    Particles part;
+    part.has_quantum_parameter = true;
+    part.has_Monte_Carlo_process = true;
+    fill_particles( part, ndim, n, pos, mom, weight, q.data() );
+    for( int p = 0; p < n; p++ ) {
+        part.Tau[p] = tau[p];
+        part.Chi[p] = 0.0;
+    }
+    Particles photons;
+    photons.has_quantum_parameter = true;
+    photons.has_Monte_Carlo_process = true;
+    photons.initialize( 0, ndim, false );
+
+    double total = 0.0;
+    for( int p = 0; p < n; p++ ) {
+        Random rnd( seeds[p] );
+        mc.rand_ = &rnd;
+        mc( part, sampling > 0 ? &photons : nullptr, smpi, *r, total, p, p + 1, 0, 0, 0 );
+    }
+    mc.rand_ = &seed0;
+    *radiated = total;
+    for( int c = 0; c < 3; c++ )
+        for( int p = 0; p < n; p++ ) mom[c * n + p] = part.Momentum[c][p];
+    for( int p = 0; p < n; p++ ) {
+        tau[p] = part.Tau[p];
+        chi[p] = part.Chi[p];
+    }
+    const long np = sampling > 0 ? ( long )photons.size() : 0;
+    *n_photons = np;
+    for( long k = 0; k < np && k < cap; k++ ) {
+        for( int d = 0; d < ndim; d++ ) ph_pos[d * cap + k] = photons.Position[d][k];
+        for( int c = 0; c < 3; c++ ) ph_mom[c * cap + k] = photons.Momentum[c][k];
+        ph_w[k] = photons.Weight[k];
+        ph_chi[k] = photons.Chi[k];
+        ph_tau[k] = photons.Tau[k];
+    }
     return 0;
 }
 

@@ -20,7 +20,8 @@
 // Random numbers: each particle draws from its own counter-based stream,
 // fmix32(seed ^ fmix32(id) ^ fmix32(step + 0x9e3779b9)) (MurmurHash3's 32-bit
 // finaliser) advanced by xorshift32 (Marsaglia 2003, as the reference's
-// src/Tools/Random.h:9-20) and mapped to [0, 1) by x * (1 - 1e-11) / 2^32.
+// src/Tools/Random.h:9-20) and mapped to (0, 1) by x / 2^32 (Random::uniform,
+// Random.h:74-75,129, the draw of RadiationMonteCarlo::operator()).
 
 #include "common.cuh"
 #include "resident_rad.cuh"
@@ -66,7 +67,19 @@ __device__ __forceinline__ double rng_uniform( uint32_t &s )
     s ^= s << 13;
     s ^= s >> 17;
     s ^= s << 5;
-    return ( double )s * ( ( 1.0 - 1e-11 ) / 4294967296.0 );
+    return ( double )s * ( 1.0 / 4294967296.0 );
+}
+
+// Radiation::computeParticleChi (src/Radiation/Radiation.h:71-80) in FP64; k = |q/m^2| / E_Schwinger.
+__device__ __forceinline__ double particle_chi64( double k, double px, double py, double pz, double Ex, double Ey,
+                                                  double Ez, double Bx, double By, double Bz )
+{
+    const double g = sqrt( 1.0 + px * px + py * py + pz * pz );
+    const double a = Ex * px + Ey * py + Ez * pz;
+    const double b = g * Ex - By * pz + Bz * py;
+    const double c = g * Ey - Bz * px + Bx * pz;
+    const double d = g * Ez - Bx * py + By * px;
+    return k * sqrt( fabs( a * a - b * b - c * c - d * d ) );
 }
 
 // userFunctions::searchValuesInMonotonicArray (src/Tools/userFunctions.h:248-272)
@@ -630,7 +643,7 @@ __device__ __forceinline__ void mc_pass_f32( const RadTab &t, const MlpView &m, 
                                              const MlpShared<H == 0 ? 4 : H> &sw, bool active, double dt, double qm2,
                                              const float *E3, const float *B3, P &px, P &py, P &pz,
                                              float &tp, uint32_t &rs, double wgt, double &rad, unsigned long long &nem,
-                                             float &last_chi, const PhotonOut &ph, int64_t q, int64_t n )
+                                             const PhotonOut &ph, int64_t q, int64_t n )
 {
     const int lane = threadIdx.x & 31;
     const float Ex = E3[0], Ey = E3[1], Ez = E3[2], Bx = B3[0], By = B3[1], Bz = B3[2];
@@ -658,7 +671,6 @@ __device__ __forceinline__ void mc_pass_f32( const RadTab &t, const MlpView &m, 
                 const float c = g * Ey - Bz * fx + Bx * fz;
                 const float d = g * Ez - Bx * fy + By * fx;
                 chi = k_chi * sqrtf( fabsf( a * a - b * b - c * c - d * d ) );
-                last_chi = chi;
                 if( chi > min_disc && tp <= eps_tau ) {
                     while( tp <= eps_tau ) tp = -logf( fmaxf( 1.0f - ( float )rng_uniform( rs ), 5.9604645e-8f ) );
                 }
@@ -807,7 +819,7 @@ __global__ void k_monte_carlo( RadTab t, MlpView m, int use_mlp, int64_t n, doub
         const double Bx = Bp[p], By = Bp[n + p], Bz = Bp[2 * n + p];
         double tp = tau[p];
         uint32_t rs = rng_init( seed, first_id + ( uint32_t )p, step );
-        double local_time = 0.0, emission_time = 0.0, last_chi = 0.0;
+        double local_time = 0.0, emission_time = 0.0;
         int it = 0, i_photon = 0;
         const double eps_tau = 1e-100;
         while( local_time < dt && it < 100 ) {
@@ -818,7 +830,6 @@ __global__ void k_monte_carlo( RadTab t, MlpView m, int use_mlp, int64_t n, doub
             const double c = g * Ey - Bz * px + Bx * pz;
             const double d = g * Ez - Bx * py + By * px;
             const double chi = fabs( qm2 ) * t.inv_es * sqrt( fabs( a * a - b * b - c * c - d * d ) );
-            last_chi = chi;
             if( chi > t.min_disc && tp <= eps_tau ) {
                 while( tp <= eps_tau ) tp = -log( 1.0 - rng_uniform( rs ) );
             }
@@ -881,13 +892,14 @@ __global__ void k_monte_carlo( RadTab t, MlpView m, int use_mlp, int64_t n, doub
         mom[n + p] = py;
         mom[2 * n + p] = pz;
         tau[p] = tp;
-        if( chi_out ) chi_out[p] = last_chi;
+        // chi of the final momentum (RadiationMonteCarlo.cpp:642-655)
+        if( chi_out ) chi_out[p] = particle_chi64( fabs( qm2 ) * t.inv_es, px, py, pz, Ex, Ey, Ez, Bx, By, Bz );
     }
     if constexpr( F32 ) {
         const bool active = p < n;
         const int64_t q = active ? p : 0;
         double px = 0.0, py = 0.0, pz = 0.0;
-        float E3[3] = { 0.0f, 0.0f, 0.0f }, B3[3] = { 0.0f, 0.0f, 0.0f }, tp = 0.0f, last_chi = 0.0f;
+        float E3[3] = { 0.0f, 0.0f, 0.0f }, B3[3] = { 0.0f, 0.0f, 0.0f }, tp = 0.0f;
         if( active ) {
             px = mom[q];
             py = mom[n + q];
@@ -899,14 +911,14 @@ __global__ void k_monte_carlo( RadTab t, MlpView m, int use_mlp, int64_t n, doub
             tp = ( float )tau[q];
         }
         uint32_t rs = rng_init( seed, first_id + ( uint32_t )q, step );
-        mc_pass_f32<H, double>( t, m, use_mlp, sw, active, dt, qm2, E3, B3, px, py, pz, tp, rs, w[q], rad, nem, last_chi, ph, q,
-                                n );
+        mc_pass_f32<H, double>( t, m, use_mlp, sw, active, dt, qm2, E3, B3, px, py, pz, tp, rs, w[q], rad, nem, ph, q, n );
         if( active ) {
             mom[p] = px;
             mom[n + p] = py;
             mom[2 * n + p] = pz;
             tau[p] = ( double )tp;
-            if( chi_out ) chi_out[p] = ( double )last_chi;
+            if( chi_out )
+                chi_out[p] = particle_chi64( fabs( qm2 ) * t.inv_es, px, py, pz, E3[0], E3[1], E3[2], B3[0], B3[1], B3[2] );
         }
     }
     // block reduction of the tallies
@@ -996,7 +1008,7 @@ __global__ void __launch_bounds__( 128 ) k_radiate_resident( RadTab t, MlpView m
             active = o - r.seg_start[lo] < r.count[lo];
         }
         float px = 0.0f, py = 0.0f, pz = 0.0f;
-        float E3[3] = { 0.0f, 0.0f, 0.0f }, B3[3] = { 0.0f, 0.0f, 0.0f }, tp = 0.0f, last_chi = 0.0f, wq = 0.0f;
+        float E3[3] = { 0.0f, 0.0f, 0.0f }, B3[3] = { 0.0f, 0.0f, 0.0f }, tp = 0.0f, wq = 0.0f;
         if( active ) {
             const unsigned k = r.key[o];
             const int gx = ( int )( k >> 16 ), gy = ( int )( k & 65535u );
@@ -1024,7 +1036,7 @@ __global__ void __launch_bounds__( 128 ) k_radiate_resident( RadTab t, MlpView m
         }
         uint32_t rs = rng_init( r.seed, ( uint32_t )o, step );
         mc_pass_f32<H, float>( t, m, use_mlp, sw, active, r.dt, r.qm2, E3, B3, px, py, pz, tp, rs, ( double )wq, rad, nem,
-                               last_chi, PhotonOut{}, 0, 0 );
+                               PhotonOut{}, 0, 0 );
         if( active ) {
             r.p[0][o] = px;
             r.p[1][o] = py;

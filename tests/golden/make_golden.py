@@ -141,6 +141,45 @@ def case_radiation(ref, rng):
                 xi_axis1_min=t["xi_axis1_min"])
 
 
+MC_FACTORS = dict(factor_dNph_dt=5e3, factor_classical=2e-3, min_chi_continuous=1e-3, min_chi_discontinuous=1e-2,
+                  inv_norm_E_schwinger=2e-6)
+
+
+def case_monte_carlo(ref):
+    """The reference's RadiationMonteCarlo::operator() on seeded particles, particle p drawing
+    from Random(state p) with state p = oracle.rng_seeds(seed, first_id, step)[p], so that the
+    oracle's per-particle streams are the same draws.  A third of the particles sit in strong
+    fields (discontinuous emissions, several per step), a third in weak ones (continuous loss
+    and no emission), a few are slow (gamma < 1.1); half start with a spent optical depth.
+    Run once without and once with a photon species (sampling 2, threshold 50, at most 3
+    photon groups per particle)."""
+    rng = np.random.default_rng(1234)
+    n = 1500
+    mom = np.stack([rng.normal(-2000, 800, n), rng.normal(0, 50, n), rng.normal(0, 50, n)])
+    E = rng.normal(0, 50, (3, n))
+    B = rng.normal(0, 50, (3, n))
+    k = n // 3
+    E[:, k:2 * k] *= 0.02
+    B[:, k:2 * k] *= 0.02
+    mom[:, 2 * k:2 * k + 40] *= 1e-4
+    w = rng.uniform(0.5, 2.0, n)
+    tau = np.where(rng.uniform(size=n) < 0.5, -1.0, rng.exponential(1.0, n))
+    pos = rng.uniform(0.0, 10.0, (2, n))
+    seed, first_id, step, dt = 7, 100, 3, 0.05
+    seeds = oracle.rng_seeds(seed, first_id, step, n)
+    out = dict(mom=mom, E=E, B=B, weight=w, tau=tau, pos=pos, seed=seed, first_id=first_id, step=step, dt=dt,
+               mass=1.0, charge=-1.0, sampling=2, threshold=50.0, max_emissions=3,
+               **{"f_" + a: b for a, b in MC_FACTORS.items()})
+    for tag, sampling in (("rad", 0), ("ph", 2)):
+        m, t = np.ascontiguousarray(mom.copy()), tau.copy()
+        r, chi, ph = ref.rad_monte_carlo(MC_FACTORS, dt, 1.0, -1.0, pos, m, w, t, E, B, seeds, sampling=sampling,
+                                         threshold=50.0, max_emissions=3)
+        out.update({f"{tag}_mom": m, f"{tag}_tau": t, f"{tag}_chi": chi, f"{tag}_radiated": r})
+        if ph is not None:
+            out.update({f"{tag}_photon_{a}": b for a, b in ph.items()})
+    return out
+
+
 def reference_laser_gaussian2d(cfg):
     """Runs the reference's own pyinit.py and pyprofiles.py (pure Python, from the reference
     tree) to build LaserGaussian2D and returns its Laser component."""
@@ -221,10 +260,12 @@ def main():
                         **{f"{c}/{k}": np.asarray(v) for c, d in cases.items() for k, v in d.items()})
     rad = case_radiation(ref, rng)
     np.savez_compressed(os.path.join(HERE, "radiation.npz"), **{k: np.asarray(v) for k, v in rad.items()})
+    mc = case_monte_carlo(ref)
+    np.savez_compressed(os.path.join(HERE, "monte_carlo.npz"), **{k: np.asarray(v) for k, v in mc.items()})
     bcases = boundary_cases(ref)
     np.savez_compressed(os.path.join(HERE, "boundaries.npz"),
                         **{f"{c}/{k}": np.asarray(v) for c, d in bcases.items() for k, v in d.items()})
-    print("wrote", len(cases), "operator cases, the radiation case and", len(bcases), "boundary cases")
+    print("wrote", len(cases), "operator cases, the radiation and Monte-Carlo cases and", len(bcases), "boundary cases")
 
 
 if __name__ == "__main__":

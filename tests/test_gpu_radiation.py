@@ -3,7 +3,8 @@
 Tables are the reference's default tables (tests/golden/radiation.npz, dumped
 from the reference's RadiationTablesDefault).  Table kernels must reproduce the
 reference's outputs; the Monte-Carlo pass must reproduce the oracle's pass
-drawing the same per-particle random streams; the network's gradients must
+drawing the same per-particle random streams, and the reference's own operator
+(tests/golden/monte_carlo.npz); the network's gradients must
 match the FP64 oracle's; the trained network is checked against the table: its
 per-bin error decides where it is used, and the emitted spectrum and mean
 energy loss of a Monte-Carlo pass using it are compared with the table-only pass.
@@ -107,6 +108,51 @@ def test_monte_carlo_photons_match_oracle(rad):
     p_ref = ph_g["pos"].cpu().numpy().copy()
     oracle.push_photons(0.5, p_ref, ph_g["mom"].cpu().numpy())
     assert rel_err(p_gpu.cpu().numpy(), p_ref) <= 1e-15
+
+
+@pytest.fixture(scope="module")
+def golden_mc():
+    import os
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "monte_carlo.npz"))
+    return {k: z[k] for k in z.files}
+
+
+def test_monte_carlo_pass_matches_reference_operator(rad, golden_rad, golden_mc):
+    """The FP64 pass against the reference's own RadiationMonteCarlo::operator() outputs
+    (tests/golden/monte_carlo.npz: each particle drew from a reference Random started at its
+    stream's state): momenta, optical depths, final chi, radiated energy and the photons of the
+    photon-species run (compared sorted by chi, the GPU takes slots atomically)."""
+    radiation = rad[0]
+    g, gr = golden_mc, golden_rad
+    T = radiation.RadiationTables(gr["integfochi"], gr["integfochi_min"], gr["integfochi_max"], gr["xi_table"],
+                                  gr["xi_min"], gr["xi_max"], gr["xi_axis1_min"], float(g["f_factor_dNph_dt"]),
+                                  float(g["f_factor_classical"]), float(g["f_inv_norm_E_schwinger"]),
+                                  float(g["f_min_chi_continuous"]), float(g["f_min_chi_discontinuous"]))
+    n = g["weight"].size
+    kw = dict(seed=int(g["seed"]), first_id=int(g["first_id"]), step=int(g["step"]))
+    args = (float(g["dt"]), float(g["mass"]), float(g["charge"]))
+    m_gpu, tau_gpu = cu(g["mom"]), cu(g["tau"])
+    chi_gpu = torch.zeros(n, dtype=torch.float64, device="cuda")
+    r_g, _ = radiation.monte_carlo(T, *args, m_gpu, cu(g["weight"]), tau_gpu, cu(g["E"]), cu(g["B"]), chi_out=chi_gpu,
+                                   **kw)
+    assert rel_err(m_gpu.cpu().numpy(), g["rad_mom"]) <= 1e-12
+    assert np.max(np.abs(tau_gpu.cpu().numpy() - g["rad_tau"])) <= 1e-10
+    assert rel_err(chi_gpu.cpu().numpy(), g["rad_chi"]) <= 1e-12
+    assert abs(r_g - float(g["rad_radiated"])) <= 1e-11 * abs(float(g["rad_radiated"]))
+
+    m_gpu, tau_gpu = cu(g["mom"]), cu(g["tau"])
+    r_g, _, ph = radiation.monte_carlo_photons(T, *args, cu(g["pos"]), m_gpu, cu(g["weight"]), tau_gpu, cu(g["E"]),
+                                               cu(g["B"]), sampling=int(g["sampling"]),
+                                               gamma_threshold=float(g["threshold"]),
+                                               max_emissions=int(g["max_emissions"]), **kw)
+    assert ph["weight"].numel() == g["ph_photon_weight"].size > 100
+    og = np.lexsort((ph["weight"].cpu().numpy(), ph["chi"].cpu().numpy()))
+    oo = np.lexsort((g["ph_photon_weight"], g["ph_photon_chi"]))
+    for k in ["pos", "mom", "weight", "chi", "tau"]:
+        assert rel_err(ph[k].cpu().numpy()[..., og], g["ph_photon_" + k][..., oo]) <= 1e-12, k
+    assert rel_err(m_gpu.cpu().numpy(), g["ph_mom"]) <= 1e-12
+    assert abs(r_g - float(g["ph_radiated"])) <= 1e-11 * abs(float(g["ph_radiated"]))
+    T.close()
 
 
 def test_fp32_math_pass_agrees_with_fp64(rad):
