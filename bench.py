@@ -230,6 +230,21 @@ def whole_job_rate(particles_per_rank: int, world: int, steps: int, ms: float) -
     return particles_per_rank * world * steps / (ms / 1e3)
 
 
+def time_batched(sim, steps, stream, device):
+    """The same steps through one sg_sim_step(steps) call: batched graphs of up to 8 steps,
+    one host wait per batch (the timed loops above wait after every step, to read each
+    step's stage times).  Returns (ms per step, batched graphs launched)."""
+    import torch
+    b0 = sim.batch_stats()[0]
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    sim.step(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return max_over_ranks(e0.elapsed_time(e1), device) / steps, sim.batch_stats()[0] - b0
+
+
 def run_gpu(args, rank, world, local_rank):
     import torch
     from smilei_gb300 import simulation
@@ -364,6 +379,8 @@ def run_gpu(args, rank, world, local_rank):
         if args.e2e_chunks > 0:
             e2e["last_step_stages_ms"] = sim.stream_timing()
         del host
+    bms, nb = time_batched(sim, args.steps, stream, device)
+    batched = {"ms_per_step": bms, "value": whole_job_rate(n, world, 1, bms), "steps": args.steps, "graphs": nb}
     sim.close()
     fp64 = None
     if fields_mixed is not None:
@@ -379,7 +396,7 @@ def run_gpu(args, rank, world, local_rank):
     return dict(n=n, ms=ms, value=value, wall_ms_per_step=(wall1 - wall0) * 1e3 / args.steps, e2e=e2e,
                 kernel_bytes=kernel_bytes, t_kernel=t_kernel, peak=peak, peak_kind=peak_kind, B_alg=B_alg,
                 launches=launches, clocks=clk.summary(), energy=(uk0, ue0, uk1, ue1), cfg=cfg, tile=tile,
-                tuning=tuning, relayouts=relayouts, fp64=fp64, queue=bool(queue), tma=tma,
+                tuning=tuning, relayouts=relayouts, fp64=fp64, queue=bool(queue), tma=tma, batched=batched,
                 residual=None if res0 is None else {"after_poisson": res0, "after_steps": res1,
                                                     "poisson_iterations": poisson[0]})
 
@@ -504,6 +521,10 @@ def run_gpu_lwfa(args, rank, world, local_rank):
     n_moved, x_moved, shifts = sim.window_state()
     relayouts = sim.layout_stats()
     particle_steps = float(sum(counts))
+    nb0 = sim.species_count(0)
+    bms, nb = time_batched(sim, args.steps, stream, device)
+    nb_mean = 0.5 * (nb0 + sim.species_count(0))
+    batched = {"ms_per_step": bms, "value": nb_mean * world / (bms / 1e3), "steps": args.steps, "graphs": nb}
     sim.close()
     ncell = int(np.prod(c["n_cells"]))
     s_state = 52.0 if args.form == "mixed" else 88.0
@@ -517,7 +538,7 @@ def run_gpu_lwfa(args, rank, world, local_rank):
                 peak=peak, peak_kind=peak_kind, B_alg=s_state + 24 * s / c["ppc"], launches=launches,
                 clocks=clk.summary(), window=dict(n_moved=n_moved, x_moved=x_moved, shifts=shifts, pre_steps=pre,
                                                   particles_at_start=n0),
-                cfg=c, energy=None, tile=tile or "default 8x8", tuning=tuning, relayouts=relayouts,
+                cfg=c, energy=None, tile=tile or "default 8x8", tuning=tuning, relayouts=relayouts, batched=batched,
                 e2e=None, e2e_note="not measured for this workload: the state size changes at every window shift")
 
 
@@ -1009,6 +1030,7 @@ def main():
                    "tile_queue": res.get("queue", False), "tma_staging": res.get("tma", False),
                    "autotune_ms_per_step": res["tuning"],
                    "relayouts_spilled_over_run": res["relayouts"],
+                   "batched_steps": res.get("batched"),
                    **({"charge_residual": res["residual"]} if res.get("residual") else {}),
                    **({"fp64_value": res["fp64"]["value"], "fp64_ms_per_step": res["fp64"]["ms_per_step"],
                        "fp64_steps": res["fp64"]["steps"], "mixed_over_fp64": res["value"] / res["fp64"]["value"],

@@ -206,8 +206,18 @@ int sg_sim_get_field( sg_sim *sim, int comp, double *host );
 int sg_sim_field_shape( sg_sim *sim, int comp, int *shape3 );
 
 /* Runs nsteps full timesteps (gather, push, deposit, bin sort, J ghost fold,
- * Ampere, Faraday, B centring) on the simulation's stream. */
+ * Ampere, Faraday, B centring) on the simulation's stream.  With graphs on
+ * (use_graph), steps go in batches of up to 8 as one graph: each step sits behind a
+ * conditional node that a one-thread gate kernel arms from the previous step's device
+ * flags, so a spill or an error stops the batch on the device and the host waits once
+ * per batch; the host then re-lays out a spilled species and goes on.  Steps at which
+ * the moving window shifts run one by one.  After a batch, sg_sim_last_timing reports
+ * -1 for the stage times (a batch records no stage events). */
 int sg_sim_step( sg_sim *sim, int nsteps );
+
+/* Batched graphs launched so far and the steps they made (sg_sim_step); *unsupported
+ * is 1 when the runtime refused a batched graph and steps run one by one. */
+int sg_sim_batch_stats( sg_sim *sim, int64_t *batches, int64_t *steps, int *unsupported );
 
 /* Synchronises and copies a species back as absolute FP64 positions, momenta and
  * weights (sorted by tile; the order is not the input order).  *npart receives the

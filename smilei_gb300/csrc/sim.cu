@@ -2385,6 +2385,38 @@ __global__ void k_norm2( GridInfo g, const T *__restrict__ a, int sx, int sy, in
 
 __global__ void k_bump_step( int64_t *step ) { *step += 1; }
 
+// Steps in one batched graph.
+constexpr int BATCH_STEPS = 8;
+
+// Ints of the batch record: [0] stop, [1] steps done, [2] step limit (from the host),
+// [3 + s] particles removed from species s over the batch, then the flags of the last
+// step done (1 + 2 * max_species ints, layout of d_flags).
+__host__ __device__ constexpr int batch_record_ints( int max_species ) { return 3 + max_species + 1 + 2 * max_species; }
+
+// Gate k of a batched graph (one thread): accounts for step k - 1 if it ran (its removals
+// summed, its flags kept; a spill or an error stops the batch) and, unless it is the last
+// gate, sets the condition of step k's node: run while not stopped and k < the limit.
+// Gate 0 clears the record.  The flags are reset at the start of every step.
+__global__ void k_batch_gate( cudaGraphConditionalHandle h, int arm, int k, int *__restrict__ rec,
+                              const int *__restrict__ flags, int nsp, int max_species )
+{
+    if( k == 0 ) {
+        rec[0] = 0;
+        rec[1] = 0;
+        for( int i = 0; i < max_species; i++ ) rec[3 + i] = 0;
+    } else if( !rec[0] && k - 1 < rec[2] ) {
+        rec[1] = k;
+        bool stop = flags[0] != 0;
+        for( int i = 0; i < nsp; i++ ) {
+            rec[3 + i] += flags[1 + max_species + i];
+            stop = stop || flags[1 + i] > 0;
+        }
+        for( int i = 0; i < 1 + 2 * max_species; i++ ) rec[3 + max_species + i] = flags[i];
+        if( stop ) rec[0] = 1;
+    }
+    if( arm ) cudaGraphSetConditional( h, ( !rec[0] && k < rec[2] ) ? 1u : 0u );
+}
+
 template <class T>
 __global__ void k_fill( int64_t n, T *__restrict__ a, T v )
 {
@@ -2611,6 +2643,15 @@ struct sg_sim {
     double *d_red = nullptr;
     cudaGraphExec_t graph[2] = { nullptr, nullptr };
     int graph_parity = -1; // parity of species 0 that graph[0] starts from
+    // batched steps: BATCH_STEPS steps in one graph, each behind a conditional node that a
+    // gate kernel arms while no earlier step of the batch spilled or failed, so that the
+    // host waits for the device once per batch instead of once per step
+    cudaGraphExec_t batch[2] = { nullptr, nullptr };
+    int batch_parity = -1;        // parity of species 0 that batch[0] starts from
+    bool batch_unsupported = false; // the runtime refused a batched graph: steps one by one
+    int *d_batch = nullptr;       // gate record, layout at k_batch_gate
+    int *h_batch = nullptr;       // its pinned copy (written by the graph's last node), then the step limit
+    int64_t batches = 0, batched_steps = 0;
     cudaEvent_t ev[4] = { nullptr, nullptr, nullptr, nullptr }; // step start, particles start/end, step end
     float last_ms[3] = { 0, 0, 0 };
     int launches_per_step = 0;
@@ -2942,19 +2983,22 @@ int stream_in_particles( sg_sim *S, SpeciesState &s, const StreamIn &in, cudaStr
     return SG_OK;
 }
 
-// Enqueues one full timestep on `st` (no host synchronisation).
-int enqueue_step( sg_sim *S, cudaStream_t st, const StreamIn *in = nullptr )
+// Enqueues one full timestep on `st` (no host synchronisation).  batched: the step is
+// captured into the body of a conditional node, which holds no event records, so the
+// stage events and the flags' copy to the host are left out (the batch's gates read the
+// flags on the device).
+int enqueue_step( sg_sim *S, cudaStream_t st, const StreamIn *in = nullptr, bool batched = false )
 {
     int launches = 0;
     // inside a capture the stage events become external event nodes; outside, plain records
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     SG_CUDA_TRY( cudaStreamIsCapturing( st, &cs ) );
     const unsigned evflags = cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
-    SG_CUDA_TRY( cudaEventRecordWithFlags( S->ev[3], st, evflags ) );
+    if( !batched ) SG_CUDA_TRY( cudaEventRecordWithFlags( S->ev[3], st, evflags ) );
     for( int c = 9; c < 12; c++ ) SG_CUDA_TRY( cudaMemsetAsync( S->fptr[c], 0, S->fsize[c] * felem( S, c ), st ) );
     SG_CUDA_TRY( cudaMemsetAsync( S->d_flags, 0, ( 1 + 2 * S->max_species ) * sizeof( int ), st ) );
     for( auto &s : S->sp ) SG_CUDA_TRY( cudaMemsetAsync( s.count[1 - s.cur], 0, S->g.ntiles * sizeof( int ), st ) );
-    SG_CUDA_TRY( cudaEventRecordWithFlags( S->ev[0], st, evflags ) );
+    if( !batched ) SG_CUDA_TRY( cudaEventRecordWithFlags( S->ev[0], st, evflags ) );
     // Monte-Carlo radiation of the radiating species, before their push (Species.cpp:583-640)
     bool radiated = false;
     for( auto &s : S->sp ) {
@@ -2979,11 +3023,12 @@ int enqueue_step( sg_sim *S, cudaStream_t st, const StreamIn *in = nullptr )
         if( r ) return r;
         launches++;
     }
-    SG_CUDA_TRY( cudaEventRecordWithFlags( S->ev[1], st, evflags ) );
+    if( !batched ) SG_CUDA_TRY( cudaEventRecordWithFlags( S->ev[1], st, evflags ) );
     int r;
     if( S->g.ndim == 3 ) r = S->mixed ? launch_fields<3, float>( S, st, launches ) : launch_fields<3, double>( S, st, launches );
     else r = S->mixed ? launch_fields<2, float>( S, st, launches ) : launch_fields<2, double>( S, st, launches );
     if( r ) return r;
+    if( batched ) return SG_OK;
     SG_CUDA_TRY( cudaEventRecordWithFlags( S->ev[2], st, evflags ) );
     SG_CUDA_TRY( cudaMemcpyAsync( S->h_flags, S->d_flags, ( 1 + 2 * S->max_species ) * sizeof( int ), cudaMemcpyDeviceToHost, st ) );
     S->launches_per_step = launches;
@@ -3012,8 +3057,11 @@ void drop_graphs( sg_sim *S )
     for( int i = 0; i < 2; i++ ) {
         if( S->graph[i] ) cudaGraphExecDestroy( S->graph[i] );
         S->graph[i] = nullptr;
+        if( S->batch[i] ) cudaGraphExecDestroy( S->batch[i] );
+        S->batch[i] = nullptr;
     }
     S->graph_parity = -1;
+    S->batch_parity = -1;
 }
 
 int capture( sg_sim *S, cudaGraphExec_t *out )
@@ -3031,6 +3079,72 @@ int capture( sg_sim *S, cudaGraphExec_t *out )
     cudaGraphDestroy( graph );
     if( e != cudaSuccess ) return cuda_fail( e, "cudaGraphInstantiate", __FILE__, __LINE__ );
     return SG_OK;
+}
+
+// Builds a graph of BATCH_STEPS steps from the species' current buffers: gate 0, step 0
+// behind its conditional node, gate 1, step 1, ..., gate BATCH_STEPS (which accounts for
+// the last step), then the record's copy to the host.  SG_OK with *out = null when the
+// runtime refuses any part of it (the caller then steps one by one).
+int build_batch( sg_sim *S, cudaGraphExec_t *out )
+{
+    *out = nullptr;
+    cudaGraph_t g = nullptr;
+    if( cudaGraphCreate( &g, 0 ) != cudaSuccess ) {
+        cudaGetLastError();
+        return SG_OK;
+    }
+    std::vector<int> cur0;
+    for( auto &s : S->sp ) cur0.push_back( s.cur );
+    const int nsp = ( int )S->sp.size();
+    cudaGraphNode_t prev = nullptr;
+    bool ok = true;
+    int r = SG_OK;
+    for( int k = 0; ok && r == SG_OK; k++ ) {
+        const int arm = k < BATCH_STEPS ? 1 : 0;
+        cudaGraphConditionalHandle h = 0;
+        if( arm ) ok = cudaGraphConditionalHandleCreate( &h, g, 0, 0 ) == cudaSuccess;
+        if( !ok ) break;
+        void *args[] = { &h, ( void * )&arm, &k, &S->d_batch, &S->d_flags, ( void * )&nsp, &S->max_species };
+        cudaKernelNodeParams kp{};
+        kp.func = ( void * )k_batch_gate;
+        kp.gridDim = dim3( 1 );
+        kp.blockDim = dim3( 1 );
+        kp.kernelParams = args;
+        cudaGraphNode_t gate = nullptr;
+        ok = cudaGraphAddKernelNode( &gate, g, prev ? &prev : nullptr, prev ? 1 : 0, &kp ) == cudaSuccess;
+        prev = gate;
+        if( !ok || !arm ) break;
+        cudaGraphNodeParams cp{};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeIf;
+        cp.conditional.size = 1;
+        cudaGraphNode_t cn = nullptr;
+        ok = cudaGraphAddNode( &cn, g, &prev, nullptr, 1, &cp ) == cudaSuccess;
+        if( !ok ) break;
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        ok = cudaStreamBeginCaptureToGraph( S->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal ) ==
+             cudaSuccess;
+        if( !ok ) break;
+        r = enqueue_step( S, S->stream, nullptr, true );
+        ok = cudaStreamEndCapture( S->stream, &body ) == cudaSuccess;
+        prev = cn;
+        for( auto &s : S->sp ) s.cur = 1 - s.cur;
+    }
+    for( size_t i = 0; i < S->sp.size(); i++ ) S->sp[i].cur = cur0[i];
+    cudaGraphNode_t cpy = nullptr;
+    if( ok && r == SG_OK )
+        ok = cudaGraphAddMemcpyNode1D( &cpy, g, &prev, 1, S->h_batch, S->d_batch,
+                                       batch_record_ints( S->max_species ) * sizeof( int ), cudaMemcpyDeviceToHost ) ==
+             cudaSuccess;
+    if( ok && r == SG_OK ) ok = cudaGraphInstantiate( out, g, 0 ) == cudaSuccess;
+    cudaGraphDestroy( g );
+    if( !ok || r != SG_OK ) {
+        if( *out ) cudaGraphExecDestroy( *out );
+        *out = nullptr;
+        cudaGetLastError(); // a refused batched graph leaves no error behind
+    }
+    return r;
 }
 
 // Optical-depth planes of a radiating species for both buffers (the old ones are
@@ -3452,6 +3566,8 @@ int sg_sim_create( const sg_sim_config *cfg, sg_sim **out )
     if( e == cudaSuccess ) e = cudaMemset( S->d_step, 0, sizeof( int64_t ) );
     if( e == cudaSuccess ) e = cudaMalloc( &S->d_flags, ( 1 + 2 * S->max_species ) * sizeof( int ) );
     if( e == cudaSuccess ) e = cudaMallocHost( &S->h_flags, ( 1 + 2 * S->max_species ) * sizeof( int ) );
+    if( e == cudaSuccess ) e = cudaMalloc( &S->d_batch, batch_record_ints( S->max_species ) * sizeof( int ) );
+    if( e == cudaSuccess ) e = cudaMallocHost( &S->h_batch, ( batch_record_ints( S->max_species ) + 1 ) * sizeof( int ) );
     if( e == cudaSuccess ) e = cudaMalloc( &S->scan_scratch, scan_scratch_elems( nt ) * sizeof( int64_t ) );
     if( e == cudaSuccess ) e = cudaMalloc( &S->tmp_start, nt * sizeof( int64_t ) );
     if( e == cudaSuccess ) e = cudaMalloc( &S->tmp_cap, nt * sizeof( int ) );
@@ -3503,6 +3619,8 @@ int sg_sim_destroy( sg_sim *S )
     for( int c = 0; c < 6; c++ ) release( S->tma_pad[c] );
     release( S->d_step );
     if( S->h_flags ) cudaFreeHost( S->h_flags );
+    release( S->d_batch );
+    if( S->h_batch ) cudaFreeHost( S->h_batch );
     release( S->scan_scratch );
     release( S->tmp_start );
     release( S->tmp_cap );
@@ -3744,26 +3862,20 @@ int sg_sim_get_field( sg_sim *S, int comp, double *host )
 
 // After the step enqueued on S->stream: waits for it, swaps the buffers, reads the
 // status and removal counts, re-lays out spilled species and shifts the window.
-static int finish_step( sg_sim *S, bool moving )
+// A finished step's flags (status, spills, removals; layout at d_flags): the error it
+// raised, or the particles it removed and the re-layout of a species that spilled.
+// removed: the removals to account (a batch passes its sums over its steps).
+static int apply_step_flags( sg_sim *S, const int *flags, const int *removed )
 {
-    SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
-    for( auto &s : S->sp ) s.cur = 1 - s.cur;
-    const int status = S->h_flags[0];
-    // stage times from the events recorded inside the step (external event nodes in a graph)
-    if( cudaEventElapsedTime( &S->last_ms[0], S->ev[0], S->ev[1] ) != cudaSuccess ||
-        cudaEventElapsedTime( &S->last_ms[1], S->ev[1], S->ev[2] ) != cudaSuccess ||
-        cudaEventElapsedTime( &S->last_ms[2], S->ev[3], S->ev[2] ) != cudaSuccess ) {
-        cudaGetLastError(); // timing is informative only; do not leave the error pending
-        S->last_ms[0] = S->last_ms[1] = S->last_ms[2] = -1.0f;
-    }
+    const int status = flags[0];
     if( status ) {
         return set_error( status, status == SG_ERR_BOUNDS ? "a particle moved more than one cell in a step or left its tile"
                                   : status == SG_ERR_ARG ? "a tile of the packed state exceeds its segment in the current layout"
                                                          : "the spill list overflowed (capacity too small)" );
     }
-    for( size_t k = 0; k < S->sp.size(); k++ ) S->sp[k].npart -= S->h_flags[1 + S->max_species + k];
+    for( size_t k = 0; k < S->sp.size(); k++ ) S->sp[k].npart -= removed[k];
     for( size_t k = 0; k < S->sp.size(); k++ ) {
-        const int nspill = S->h_flags[1 + k];
+        const int nspill = flags[1 + k];
         if( nspill > 0 ) {
             S->relayouts++;
             S->spilled += nspill;
@@ -3771,6 +3883,22 @@ static int finish_step( sg_sim *S, bool moving )
             if( r ) return r;
         }
     }
+    return SG_OK;
+}
+
+static int finish_step( sg_sim *S, bool moving )
+{
+    SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
+    for( auto &s : S->sp ) s.cur = 1 - s.cur;
+    // stage times from the events recorded inside the step (external event nodes in a graph)
+    if( cudaEventElapsedTime( &S->last_ms[0], S->ev[0], S->ev[1] ) != cudaSuccess ||
+        cudaEventElapsedTime( &S->last_ms[1], S->ev[1], S->ev[2] ) != cudaSuccess ||
+        cudaEventElapsedTime( &S->last_ms[2], S->ev[3], S->ev[2] ) != cudaSuccess ) {
+        cudaGetLastError(); // timing is informative only; do not leave the error pending
+        S->last_ms[0] = S->last_ms[1] = S->last_ms[2] = -1.0f;
+    }
+    int r = apply_step_flags( S, S->h_flags, S->h_flags + 1 + S->max_species );
+    if( r ) return r;
     if( moving ) {
         int r = window_shift( S );
         if( r ) return r;
@@ -3780,18 +3908,84 @@ static int finish_step( sg_sim *S, bool moving )
     return SG_OK;
 }
 
+// Whether the window moves at the end of step `step` (SimWindow::isMoving,
+// SimWindow.cpp:93-96), with the window where it is now.
+static bool window_moves_at( const sg_sim *S, int64_t step )
+{
+    const double time_dual = ( ( double )step + 1.5 ) * S->g.dt;
+    return S->win_on && ( time_dual - S->win_t_start ) * S->win_velocity > S->win_x_moved;
+}
+
+// Up to `limit` steps (2 <= limit <= BATCH_STEPS, none of them moving the window) as one
+// batched graph and one wait.  *done: the steps made (0 when batches are unavailable).
+static int run_batch( sg_sim *S, int limit, int *done )
+{
+    *done = 0;
+    const int parity = S->sp.empty() ? 0 : S->sp[0].cur;
+    if( S->batch_parity < 0 ) {
+        int r = build_batch( S, &S->batch[0] );
+        if( r ) return r;
+        if( S->batch[0] ) {
+            for( auto &s : S->sp ) s.cur = 1 - s.cur;
+            r = build_batch( S, &S->batch[1] );
+            for( auto &s : S->sp ) s.cur = 1 - s.cur;
+            if( r ) return r;
+        }
+        if( !S->batch[0] || !S->batch[1] ) {
+            S->batch_unsupported = true;
+            drop_graphs( S );
+            return SG_OK;
+        }
+        S->batch_parity = parity;
+    }
+    const int rec = batch_record_ints( S->max_species );
+    S->h_batch[rec] = limit;
+    SG_CUDA_TRY( cudaMemcpyAsync( S->d_batch + 2, S->h_batch + rec, sizeof( int ), cudaMemcpyHostToDevice, S->stream ) );
+    SG_CUDA_TRY( cudaGraphLaunch( S->batch[parity == S->batch_parity ? 0 : 1], S->stream ) );
+    SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
+    const int n = S->h_batch[1];
+    if( n < 1 || n > limit ) return set_error( SG_ERR_CUDA, "batched step record out of range (%d of %d)", n, limit );
+    for( auto &s : S->sp )
+        if( n & 1 ) s.cur = 1 - s.cur;
+    S->last_ms[0] = S->last_ms[1] = S->last_ms[2] = -1.0f; // no stage events inside a batch
+    // the flags are those of the batch's last step, the removals its sums over the steps
+    S->hstep += n - 1;
+    int r = apply_step_flags( S, S->h_batch + 3 + S->max_species, S->h_batch + 3 );
+    if( r ) return r;
+    S->hstep++;
+    S->batches++;
+    S->batched_steps += n;
+    *done = n;
+    return SG_OK;
+}
+
 int sg_sim_step( sg_sim *S, int nsteps )
 {
     SG_REQUIRE( S, "NULL simulation" );
     SG_REQUIRE( nsteps >= 0, "nsteps < 0" );
-    for( int it = 0; it < nsteps; it++ ) {
+    for( int it = 0; it < nsteps; ) {
         int rp = pad_fields( S, S->stream );
         if( rp ) return rp;
+        // steps before the window's next move go in batches, with one wait per batch
+        int limit = 0;
+        if( S->cfg.use_graph && !S->batch_unsupported && nsteps - it > 1 && !S->sp.empty() ) {
+            const int most = std::min( nsteps - it, BATCH_STEPS );
+            while( limit < most && !window_moves_at( S, S->hstep + limit ) ) limit++;
+        }
+        if( limit > 1 ) {
+            int done = 0;
+            int r = run_batch( S, limit, &done );
+            if( r ) return r;
+            if( done > 0 ) {
+                it += done;
+                continue;
+            }
+        }
+        it++;
         const int parity = S->sp.empty() ? 0 : S->sp[0].cur;
         // the window moves at the end of this step (SimWindow::isMoving, SimWindow.cpp:93-96);
         // the x boundaries of this step are then skipped (ElectroMagn.cpp:374)
-        const double time_dual = ( ( double )S->hstep + 1.5 ) * S->g.dt;
-        const bool moving = S->win_on && ( time_dual - S->win_t_start ) * S->win_velocity > S->win_x_moved;
+        const bool moving = window_moves_at( S, S->hstep );
         if( moving ) {
             S->obc.side_mask = 0xC;
             int r = enqueue_step( S, S->stream );
@@ -3976,6 +4170,15 @@ int sg_sim_layout_stats( sg_sim *S, int64_t *relayouts, int64_t *spilled )
     SG_REQUIRE( S, "NULL simulation" );
     if( relayouts ) *relayouts = S->relayouts;
     if( spilled ) *spilled = S->spilled;
+    return SG_OK;
+}
+
+int sg_sim_batch_stats( sg_sim *S, int64_t *batches, int64_t *steps, int *unsupported )
+{
+    SG_REQUIRE( S, "NULL simulation" );
+    if( batches ) *batches = S->batches;
+    if( steps ) *steps = S->batched_steps;
+    if( unsupported ) *unsupported = S->batch_unsupported ? 1 : 0;
     return SG_OK;
 }
 

@@ -270,6 +270,13 @@ class Simulation:
         check(_lib.lib().sg_sim_layout_stats(self._h, ctypes.byref(a), ctypes.byref(b)), "layout_stats")
         return a.value, b.value
 
+    def batch_stats(self):
+        """(batched graphs launched, steps they made, 1 if the runtime refused batching)."""
+        a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int()
+        check(_lib.lib().sg_sim_batch_stats(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)),
+              "batch_stats")
+        return a.value, b.value, c.value
+
     def last_timing(self):
         """Device ms of the last step: (particles, fields, total) and kernel launches per step."""
         a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
