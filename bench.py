@@ -38,6 +38,8 @@ sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s on 1 GB300 (mixed vs FP64 form), % of HBM roofline"
 UNIT = "particle-steps/s"
+# the step's result read back every e2e step: the 16 FP64 energy sums (sg_sim_energy)
+ENERGY_READBACK_BYTES = 16 * 8
 SIGMA_10KEV = float(np.sqrt(10.0 / 511.0))
 
 
@@ -345,7 +347,7 @@ def run_gpu(args, rank, world, local_rank):
         torch.cuda.synchronize()
         ems = max_over_ranks(e0.elapsed_time(e1), device)
         e2e = {"value": whole_job_rate(n, world, ke, ems), "unit": UNIT, "h2d_bytes_per_step": int(sum(nb)),
-               "d2h_bytes_per_step": int(sum(nb) + 16), "steps": ke}
+               "d2h_bytes_per_step": int(sum(nb) + ENERGY_READBACK_BYTES), "steps": ke}
         del hosts
     elif not args.no_e2e:
         nbytes = sim.packed_bytes(0)
@@ -375,7 +377,7 @@ def run_gpu(args, rank, world, local_rank):
         torch.cuda.synchronize()
         ems = max_over_ranks(e0.elapsed_time(e1), device)
         e2e = {"value": whole_job_rate(n, world, ke, ems), "unit": UNIT, "h2d_bytes_per_step": int(nbytes),
-               "d2h_bytes_per_step": int(nbytes + 16), "steps": ke}
+               "d2h_bytes_per_step": int(nbytes + ENERGY_READBACK_BYTES), "steps": ke}
         if args.e2e_chunks > 0:
             e2e["last_step_stages_ms"] = sim.stream_timing()
         del host

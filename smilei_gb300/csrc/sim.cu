@@ -2314,25 +2314,34 @@ __device__ __forceinline__ double block_sum( double v )
     return v;
 }
 
-// sum over live particles of w * (gamma - 1) (DiagnosticScalar.cpp:505-522), one block per tile.
+// sum over live particles of w * (gamma - 1) (DiagnosticScalar.cpp:505-522): a warp per
+// tile at a time, each lane summing its share of the tile (a contiguous segment) and
+// adding that to its FP64 total once per tile.
 template <bool MIXED>
 __global__ void k_kinetic( int nt, const int64_t *__restrict__ seg_start, const int *__restrict__ count,
                            PBuf<MIXED> b, double *__restrict__ out )
 {
+    const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
     double acc = 0.0;
-    for( int t = blockIdx.x; t < nt; t += gridDim.x ) {
+    for( int t = blockIdx.x * wpb + ( threadIdx.x >> 5 ); t < nt; t += gridDim.x * wpb ) {
         const int n = count[t];
         const int64_t s0 = seg_start[t];
-        for( int i = threadIdx.x; i < n; i += blockDim.x ) {
-            if constexpr( MIXED ) {
-                // FP32 momenta: gamma - 1 = p^2 / (1 + gamma) in FP32 (no cancellation at small
-                // p; about 1e-8 relative on the sum), summed in FP64 -- one FP64 add per particle
+        if constexpr( MIXED ) {
+            // FP32 momenta: gamma - 1 = p^2 / (1 + gamma) in FP32 (no cancellation at small p),
+            // a lane's terms of the tile (about n / 32) summed in FP32, then in FP64
+            float part = 0.0f;
+#pragma unroll 4
+            for( int i = lane; i < n; i += 32 ) {
                 const float px = b.p[0][s0 + i], py = b.p[1][s0 + i], pz = b.p[2][s0 + i];
                 const float p2 = fmaf( px, px, fmaf( py, py, pz * pz ) );
-                acc += ( double )b.w[s0 + i] * ( double )( p2 / ( 1.0f + sqrtf( 1.0f + p2 ) ) );
-            } else {
+                part = fmaf( b.w[s0 + i], p2 / ( 1.0f + sqrtf( 1.0f + p2 ) ), part );
+            }
+            acc += ( double )part;
+        } else {
+#pragma unroll 4
+            for( int i = lane; i < n; i += 32 ) {
                 const double px = b.p[0][s0 + i], py = b.p[1][s0 + i], pz = b.p[2][s0 + i];
-                acc += ( double )b.w[s0 + i] * ( sqrt( 1.0 + px * px + py * py + pz * pz ) - 1.0 );
+                acc += b.w[s0 + i] * ( sqrt( 1.0 + px * px + py * py + pz * pz ) - 1.0 );
             }
         }
     }
@@ -2364,23 +2373,43 @@ __global__ void k_species_sums( int nt, const int64_t *__restrict__ seg_start, c
     }
 }
 
-// sum of F^2 over the N physical points per dimension (array index OS .. OS+N-1).
+// Six field arrays for k_norm2: pointers and their extents along dimensions 1 and 2.
+struct Norm2Set {
+    const void *a[6];
+    int e1[6], e2[6];
+};
+
+// sum of F^2 over the N physical points per dimension (array index OS .. OS+N-1) of array
+// blockIdx.y of `f`, into out[blockIdx.y * per_array]: a warp per row of the last
+// dimension at a time, each lane summing its points of the row in the field's type and
+// adding that to its FP64 total once per row.
 template <class T>
-__global__ void k_norm2( GridInfo g, const T *__restrict__ a, int sx, int sy, int sz, double *__restrict__ out )
+__global__ void k_norm2( GridInfo g, Norm2Set f, int per_array, double *__restrict__ out )
 {
-    const int e1 = ext( g, 1, sy ), e2 = ext( g, 2, sz );
-    const int n0 = g.N[0], n1 = g.N[1], n2 = g.ndim == 3 ? g.N[2] : 1;
-    const int o2 = g.ndim == 3 ? OS : 0;
-    const int64_t n = ( int64_t )n0 * n1 * n2;
+    const T *__restrict__ a = static_cast<const T *>( f.a[blockIdx.y] );
+    const int e1 = f.e1[blockIdx.y], e2 = f.e2[blockIdx.y];
+    const bool d3 = g.ndim == 3;
+    const int nrow = d3 ? g.N[0] * g.N[1] : g.N[0], len = d3 ? g.N[2] : g.N[1];
+    const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
     double acc = 0.0;
-    for( int64_t t = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x; t < n; t += ( int64_t )gridDim.x * blockDim.x ) {
-        const int k = ( int )( t % n2 ), j = ( int )( ( t / n2 ) % n1 ), i = ( int )( t / ( ( int64_t )n2 * n1 ) );
-        const double v = a[( ( int64_t )( i + OS ) * e1 + ( j + OS ) ) * e2 + ( k + o2 )];
-        acc += v * v;
+    for( int r = blockIdx.x * wpb + ( threadIdx.x >> 5 ); r < nrow; r += gridDim.x * wpb ) {
+        int64_t base;
+        if( d3 ) {
+            const int i = r / g.N[1], j = r - i * g.N[1];
+            base = ( ( int64_t )( i + OS ) * e1 + ( j + OS ) ) * e2 + OS;
+        } else {
+            base = ( int64_t )( r + OS ) * e1 + OS;
+        }
+        T part = T( 0 );
+#pragma unroll 4
+        for( int k = lane; k < len; k += 32 ) {
+            const T v = a[base + k];
+            part = fma( v, v, part );
+        }
+        acc += ( double )part;
     }
-    ( void )sx;
     acc = block_sum( acc );
-    if( threadIdx.x == 0 ) atomicAdd( out, acc );
+    if( threadIdx.x == 0 ) atomicAdd( out + blockIdx.y * per_array, acc );
 }
 
 __global__ void k_bump_step( int64_t *step ) { *step += 1; }
@@ -2684,6 +2713,10 @@ struct sg_sim {
     int64_t *h_chunk_end = nullptr;     // pinned: first and end packed particle of each range
     int64_t *d_chunk_end = nullptr;     // its device address
     float stream_ms[4] = { -1, -1, -1, -1 }; // last streamed step: copy in, particles, copy out, fields done
+    // energy sums of the current state ([1] field, [2 + k] kinetic of species k), in pinned
+    // memory; a streamed step computes them while its last ranges are copied out
+    double *h_energy = nullptr;
+    bool energy_valid = false;
 };
 
 namespace sg {
@@ -3568,6 +3601,7 @@ int sg_sim_create( const sg_sim_config *cfg, sg_sim **out )
     if( e == cudaSuccess ) e = cudaMallocHost( &S->h_flags, ( 1 + 2 * S->max_species ) * sizeof( int ) );
     if( e == cudaSuccess ) e = cudaMalloc( &S->d_batch, batch_record_ints( S->max_species ) * sizeof( int ) );
     if( e == cudaSuccess ) e = cudaMallocHost( &S->h_batch, ( batch_record_ints( S->max_species ) + 1 ) * sizeof( int ) );
+    if( e == cudaSuccess ) e = cudaMallocHost( &S->h_energy, 16 * sizeof( double ) );
     if( e == cudaSuccess ) e = cudaMalloc( &S->scan_scratch, scan_scratch_elems( nt ) * sizeof( int64_t ) );
     if( e == cudaSuccess ) e = cudaMalloc( &S->tmp_start, nt * sizeof( int64_t ) );
     if( e == cudaSuccess ) e = cudaMalloc( &S->tmp_cap, nt * sizeof( int ) );
@@ -3621,6 +3655,7 @@ int sg_sim_destroy( sg_sim *S )
     if( S->h_flags ) cudaFreeHost( S->h_flags );
     release( S->d_batch );
     if( S->h_batch ) cudaFreeHost( S->h_batch );
+    if( S->h_energy ) cudaFreeHost( S->h_energy );
     release( S->scan_scratch );
     release( S->tmp_start );
     release( S->tmp_cap );
@@ -3711,6 +3746,7 @@ int sg_sim_set_stream( sg_sim *S, sg_stream_t stream )
 int sg_sim_add_species_device( sg_sim *S, double mass, double charge, int pusher, int64_t npart, const double *pos,
                                const double *mom, const double *weight, int *index )
 {
+    if( S ) S->energy_valid = false;
     SG_REQUIRE( S, "NULL simulation" );
     SG_REQUIRE( mass > 0.0, "mass must be positive" );
     SG_REQUIRE( pusher >= 0 && pusher <= 2, "pusher must be 0 (boris), 1 (vay) or 2 (higueracary)" );
@@ -3820,6 +3856,7 @@ int sg_sim_field_shape( sg_sim *S, int comp, int *shape3 )
 
 int sg_sim_set_field( sg_sim *S, int comp, const double *host )
 {
+    if( S ) S->energy_valid = false;
     SG_REQUIRE( S && host, "NULL argument" );
     SG_REQUIRE( comp >= 0 && comp < 12, "component out of range" );
     const int64_t n = S->fsize[comp];
@@ -3961,6 +3998,7 @@ static int run_batch( sg_sim *S, int limit, int *done )
 
 int sg_sim_step( sg_sim *S, int nsteps )
 {
+    if( S ) S->energy_valid = false;
     SG_REQUIRE( S, "NULL simulation" );
     SG_REQUIRE( nsteps >= 0, "nsteps < 0" );
     for( int it = 0; it < nsteps; ) {
@@ -4117,6 +4155,7 @@ int sg_sim_radiation_stats( sg_sim *S, int species, double *radiated, unsigned l
 
 int sg_sim_fill_species( sg_sim *S, int species, int x0_cell, int x1_cell )
 {
+    if( S ) S->energy_valid = false;
     SG_REQUIRE( S, "NULL simulation" );
     SG_REQUIRE( species >= 0 && species < ( int )S->sp.size(), "species %d out of range", species );
     SpeciesState &s = S->sp[species];
@@ -4250,6 +4289,7 @@ int sg_sim_state_bytes( sg_sim *S, int species, size_t *bytes )
 
 int sg_sim_copy_state( sg_sim *S, int species, void *host, int to_device )
 {
+    if( S ) S->energy_valid = false;
     SG_REQUIRE( S && host, "NULL argument" );
     SG_REQUIRE( species >= 0 && species < ( int )S->sp.size(), "no species %d", species );
     SpeciesState &s = S->sp[species];
@@ -4307,6 +4347,7 @@ int sg_sim_pack_state( sg_sim *S, int species, void *host )
 
 int sg_sim_unpack_state( sg_sim *S, int species, const void *host )
 {
+    if( S ) S->energy_valid = false;
     SG_REQUIRE( S && host, "NULL argument" );
     SG_REQUIRE( species >= 0 && species < ( int )S->sp.size(), "no species %d", species );
     SpeciesState &s = S->sp[species];
@@ -4406,6 +4447,8 @@ int sg_stream_ranges( int ndim, const int *ntiles, int periodic, const int *coun
     return SG_OK;
 }
 
+int enqueue_energy( sg_sim *S, cudaStream_t st, bool next );
+
 int sg_sim_step_host( sg_sim *S, int species, const void *host_in, void *host_out, int chunks )
 {
     SG_REQUIRE( S && host_in && host_out, "NULL argument" );
@@ -4413,6 +4456,7 @@ int sg_sim_step_host( sg_sim *S, int species, const void *host_in, void *host_ou
     SG_REQUIRE( chunks >= 1 && chunks <= 64, "chunks must be in [1, 64], got %d", chunks );
     SpeciesState &s = S->sp[species];
     SG_REQUIRE( !s.radiates, "a radiating species does not stream: its radiation pass reads every particle before the push" );
+    S->energy_valid = false;
     const double time_dual = ( ( double )S->hstep + 1.5 ) * S->g.dt;
     const bool moving = S->win_on && ( time_dual - S->win_t_start ) * S->win_velocity > S->win_x_moved;
     SG_REQUIRE( !moving, "the window moves in this step (the state size changes): unpack, step and pack instead" );
@@ -4493,6 +4537,8 @@ int sg_sim_step_host( sg_sim *S, int species, const void *host_in, void *host_ou
     }
     r = pad_fields( S, S->stream );
     if( r == SG_OK ) r = enqueue_step( S, S->stream, &in );
+    // the energy sums of the new state run while the last ranges are copied out
+    if( r == SG_OK && in.pack ) r = enqueue_energy( S, S->stream, true );
     if( r ) {
         cudaStreamSynchronize( cs );
         cudaStreamSynchronize( S->stream );
@@ -4548,6 +4594,11 @@ int sg_sim_step_host( sg_sim *S, int species, const void *host_in, void *host_ou
         // step are not the new state
         if( valid && copied == n && S->h_flags[1 + species] == 0 && S->h_flags[1 + S->max_species + species] == 0 ) {
             std::memcpy( hout, &n, 8 );
+            // the sums saw every particle unless some species spilled (its spilled
+            // particles were in the overflow list)
+            bool spill = false;
+            for( size_t k = 0; k < S->sp.size(); k++ ) spill = spill || S->h_flags[1 + k] != 0;
+            S->energy_valid = !spill;
             return SG_OK;
         }
     } else {
@@ -4567,28 +4618,52 @@ int sg_sim_stream_timing( sg_sim *S, float *ms )
     return SG_OK;
 }
 
-int sg_sim_energy( sg_sim *S, double *ukin, double *uelm )
+// E and the time-centred B_m (DiagnosticScalar.cpp:640-646), in that order.
+static Norm2Set energy_fields( const sg_sim *S )
 {
-    SG_REQUIRE( S, "NULL simulation" );
-    cudaStream_t st = S->stream;
+    Norm2Set f{};
+    const int comps[6] = { 0, 1, 2, 6, 7, 8 };
+    for( int k = 0; k < 6; k++ ) {
+        const int c = comps[k];
+        f.a[k] = S->fptr[c];
+        f.e1[k] = ext( S->g, 1, comp_stag( c, 1 ) );
+        f.e2[k] = ext( S->g, 2, comp_stag( c, 2 ) );
+    }
+    return f;
+}
+
+// Enqueues the energy sums on st into S->h_energy: each species' sum of w (gamma - 1)
+// over buffer `cur ^ next` (next: the buffers a step enqueued just before writes) and
+// the squared E and time-centred B_m.
+int enqueue_energy( sg_sim *S, cudaStream_t st, bool next )
+{
     SG_CUDA_TRY( cudaMemsetAsync( S->d_red, 0, 16 * sizeof( double ), st ) );
     const int nt = S->g.ntiles;
     for( size_t k = 0; k < S->sp.size(); k++ ) {
         SpeciesState &s = S->sp[k];
-        if( S->mixed ) k_kinetic<true><<<std::min( nt, 1216 ), 256, 0, st>>>( nt, s.seg_start, s.count[s.cur], s.bm[s.cur], S->d_red + 2 + k % 14 );
-        else k_kinetic<false><<<std::min( nt, 1216 ), 256, 0, st>>>( nt, s.seg_start, s.count[s.cur], s.bd[s.cur], S->d_red + 2 + k % 14 );
+        const int b = next ? 1 - s.cur : s.cur;
+        if( S->mixed ) k_kinetic<true><<<std::min( nt, 1216 ), 256, 0, st>>>( nt, s.seg_start, s.count[b], s.bm[b], S->d_red + 2 + k % 14 );
+        else k_kinetic<false><<<std::min( nt, 1216 ), 256, 0, st>>>( nt, s.seg_start, s.count[b], s.bd[b], S->d_red + 2 + k % 14 );
         SG_LAUNCH_CHECK( "k_kinetic" );
     }
-    const int comps[6] = { 0, 1, 2, 6, 7, 8 }; // E and the time-centred B_m (DiagnosticScalar.cpp:640-646)
-    for( int c : comps ) {
-        const int sx = comp_stag( c, 0 ), sy = comp_stag( c, 1 ), sz = comp_stag( c, 2 );
-        if( S->mixed ) k_norm2<float><<<1216, 256, 0, st>>>( S->g, static_cast<float *>( S->fptr[c] ), sx, sy, sz, S->d_red + 1 );
-        else k_norm2<double><<<1216, 256, 0, st>>>( S->g, static_cast<double *>( S->fptr[c] ), sx, sy, sz, S->d_red + 1 );
-        SG_LAUNCH_CHECK( "k_norm2" );
+    const Norm2Set f = energy_fields( S );
+    if( S->mixed ) k_norm2<float><<<dim3( 304, 6 ), 256, 0, st>>>( S->g, f, 0, S->d_red + 1 );
+    else k_norm2<double><<<dim3( 304, 6 ), 256, 0, st>>>( S->g, f, 0, S->d_red + 1 );
+    SG_LAUNCH_CHECK( "k_norm2" );
+    SG_CUDA_TRY( cudaMemcpyAsync( S->h_energy, S->d_red, 16 * sizeof( double ), cudaMemcpyDeviceToHost, st ) );
+    return SG_OK;
+}
+
+int sg_sim_energy( sg_sim *S, double *ukin, double *uelm )
+{
+    SG_REQUIRE( S, "NULL simulation" );
+    // a streamed step leaves the sums of the state it produced
+    if( !S->energy_valid ) {
+        int r = enqueue_energy( S, S->stream, false );
+        if( r ) return r;
     }
-    double h[16];
-    SG_CUDA_TRY( cudaMemcpyAsync( h, S->d_red, sizeof( h ), cudaMemcpyDeviceToHost, st ) );
-    SG_CUDA_TRY( cudaStreamSynchronize( st ) );
+    SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
+    const double *h = S->h_energy;
     double vol = 1.0;
     for( int d = 0; d < S->g.ndim; d++ ) vol *= S->g.dx[d];
     double uk = 0.0;
@@ -4624,14 +4699,10 @@ int sg_sim_field_energies( sg_sim *S, double *out )
     SG_REQUIRE( S && out, "NULL argument" );
     cudaStream_t st = S->stream;
     SG_CUDA_TRY( cudaMemsetAsync( S->d_red, 0, 6 * sizeof( double ), st ) );
-    const int comps[6] = { 0, 1, 2, 6, 7, 8 };
-    for( int k = 0; k < 6; k++ ) {
-        const int c = comps[k];
-        const int sx = comp_stag( c, 0 ), sy = comp_stag( c, 1 ), sz = comp_stag( c, 2 );
-        if( S->mixed ) k_norm2<float><<<1216, 256, 0, st>>>( S->g, static_cast<float *>( S->fptr[c] ), sx, sy, sz, S->d_red + k );
-        else k_norm2<double><<<1216, 256, 0, st>>>( S->g, static_cast<double *>( S->fptr[c] ), sx, sy, sz, S->d_red + k );
-        SG_LAUNCH_CHECK( "k_norm2" );
-    }
+    const Norm2Set f = energy_fields( S );
+    if( S->mixed ) k_norm2<float><<<dim3( 304, 6 ), 256, 0, st>>>( S->g, f, 1, S->d_red );
+    else k_norm2<double><<<dim3( 304, 6 ), 256, 0, st>>>( S->g, f, 1, S->d_red );
+    SG_LAUNCH_CHECK( "k_norm2" );
     double h[6];
     SG_CUDA_TRY( cudaMemcpyAsync( h, S->d_red, sizeof( h ), cudaMemcpyDeviceToHost, st ) );
     SG_CUDA_TRY( cudaStreamSynchronize( st ) );
@@ -4994,6 +5065,7 @@ int sg_sim_get_rho( sg_sim *S, double *host )
 
 int sg_sim_solve_poisson( sg_sim *S, double max_error, int max_iter, int *iterations, double *ctrl_out )
 {
+    if( S ) S->energy_valid = false;
     SG_REQUIRE( S, "NULL simulation" );
     SG_REQUIRE( !S->g.open[0] && !S->g.open[1] && !S->g.open[2], "charge density, Poisson and residual need a periodic grid" );
     SG_REQUIRE( max_iter >= 0, "max_iter < 0" );

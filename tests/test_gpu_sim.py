@@ -220,6 +220,9 @@ def test_step_host_matches_unpack_step_pack(sim_mod, form, n_cells):
             np.testing.assert_allclose(mb, ma, **tol)
     ua, ub = a.energy(), b.energy()
     np.testing.assert_allclose(ub, ua, rtol=1e-5 if form == "mixed" else 1e-10)
+    # the streamed step left the sums of its new state; a fresh pass gives the same
+    b.step(0)
+    np.testing.assert_allclose(b.energy(), ub, rtol=1e-12)
     with pytest.raises(RuntimeError):
         b.step_host(0, hb.ctypes.data, chunks=0)
     bad = hb.copy()
