@@ -65,22 +65,24 @@ for p in "${pids[@]}"; do wait "$p"; done
 g++ -shared -fopenmp -o "$OUT/libsmilei_ref_ops.so" "${objs[@]}" -Wl,--allow-shlib-undefined
 echo "build_ref: $OUT/libsmilei_ref_ops.so"
 
-# The reference's own CUDA current deposit (Projector3D2OrderGPUKernelCUDAHIP.cu, the
-# kernel its NVIDIA builds launch from Projector3D2OrderGPU) as device code only: a
-# cubin for sm_103a, loaded through the driver API by oracle/ref_gpu_deposit.py on a GPU
+# The reference's own CUDA current deposits (Projector{3D,2D}2OrderGPUKernelCUDAHIP.cu,
+# the kernels its NVIDIA builds launch from Projector{3D,2D}2OrderGPU) as device code
+# only: cubins for sm_103a, loaded through the driver API by oracle/ref_gpu_deposit.py on a GPU
 # host to time it beside this project's kernel.  The defines are those of the
 # reference's OpenACC + CUDA build; its host code is not used.
 NVCC="${NVCC:-/usr/local/cuda/bin/nvcc}"
 if [ -x "$NVCC" ]; then
-    if "$NVCC" -cubin -gencode arch=compute_103a,code=sm_103a -std=c++14 -O3 --expt-relaxed-constexpr \
-        -DSMILEI_ACCELERATOR_GPU -DSMILEI_ACCELERATOR_GPU_OACC -D__VERSION=\"ref\" -DOMPI_SKIP_MPICXX -w $INC \
-        -Xptxas -v "$SRC/Projector/Projector3D2OrderGPUKernelCUDAHIP.cu" -o "$OUT/ref_deposit3d.cubin" \
-        > "$OUT/ref_deposit3d.ptxas.txt" 2>&1; then
-        # the kernel's entry name, as ptxas reports it
-        grep -o "_ZN7cudahip6kernel31DepositCurrentDensity_3D_Order2[A-Za-z0-9_]*" "$OUT/ref_deposit3d.ptxas.txt" \
-            | head -1 > "$OUT/ref_deposit3d.entry"
-        echo "build_ref: $OUT/ref_deposit3d.cubin"
-    else
-        echo "build_ref: the reference's CUDA deposit did not compile (see $OUT/ref_deposit3d.ptxas.txt)" >&2
-    fi
+    for D in 3 2; do
+        if "$NVCC" -cubin -gencode arch=compute_103a,code=sm_103a -std=c++14 -O3 --expt-relaxed-constexpr \
+            -DSMILEI_ACCELERATOR_GPU -DSMILEI_ACCELERATOR_GPU_OACC -D__VERSION=\"ref\" -DOMPI_SKIP_MPICXX -w $INC \
+            -Xptxas -v "$SRC/Projector/Projector${D}D2OrderGPUKernelCUDAHIP.cu" -o "$OUT/ref_deposit${D}d.cubin" \
+            > "$OUT/ref_deposit${D}d.ptxas.txt" 2>&1; then
+            # the current deposit's entry name, as ptxas reports it
+            grep -o "_ZN[0-9]*cudahip[0-9a-z]*6kernel31DepositCurrentDensity_${D}D_Order2[A-Za-z0-9_]*" \
+                "$OUT/ref_deposit${D}d.ptxas.txt" | head -1 > "$OUT/ref_deposit${D}d.entry"
+            echo "build_ref: $OUT/ref_deposit${D}d.cubin"
+        else
+            echo "build_ref: the reference's ${D}D CUDA deposit did not compile (see $OUT/ref_deposit${D}d.ptxas.txt)" >&2
+        fi
+    done
 fi

@@ -1,6 +1,8 @@
-"""The reference's own CUDA current deposit (DepositCurrentDensity_3D_Order2,
-src/Projector/Projector3D2OrderGPUKernelCUDAHIP.cu:136-516), compiled from the reference
-tree by oracle/build_ref.sh and run here through oracle/ref_gpu_deposit.py.
+"""The reference's own CUDA current deposits (DepositCurrentDensity_3D_Order2,
+src/Projector/Projector3D2OrderGPUKernelCUDAHIP.cu:136-516, and
+DepositCurrentDensity_2D_Order2, Projector2D2OrderGPUKernelCUDAHIP.cu:545-870), compiled
+from the reference tree by oracle/build_ref.sh and run here through
+oracle/ref_gpu_deposit.py.
 
 - Driven as currentDepositionKernel3D drives it, its currents match the oracle's
   Esirkepov deposit (oracle/pic_oracle.c or_project) within 1e-12 on a 16x12x8 patch
@@ -13,7 +15,11 @@ tree by oracle/build_ref.sh and run here through oracle/ref_gpu_deposit.py.
   re-binning; mixed and FP64 forms) on the same plasma; the line printed holds the
   times.
 
-Skipped where the cubin was not built (no reference tree when build() ran).
+- The 2D kernel matches the oracle within 1e-12 for particles moving either way, and is
+  timed on the 2D thermal plasma (256 x 256, electrons and protons at 16 ppc each)
+  against this project's particle kernels of a step.
+
+Skipped where the cubins were not built (no reference tree when build() ran).
 """
 import json
 
@@ -197,3 +203,139 @@ def test_fused_step_against_reference_gpu_deposit_at_256(ref):
             "reference_default_over_fused_fp64": ref_ms["default"] / ours["fp64"]}
     print("REF_GPU_DEPOSIT " + json.dumps(line))
     assert ours["mixed"] < ref_ms["default"] and ours["fp64"] < ref_ms["default"]
+
+
+@pytest.fixture(scope="module")
+def ref2():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from oracle import ref_gpu_deposit
+    if not ref_gpu_deposit.available(2):
+        pytest.skip("the reference's 2D CUDA deposit was not compiled (oracle/build_ref.sh)")
+    torch.zeros(1, device="cuda")
+    return ref_gpu_deposit.RefGpuDeposit(ndim=2)
+
+
+def _launch2d(ref2, c, J, pos, momz, q, w, bin_index, invgf, iold, delta, stream=0, cell_sorting=False):
+    ref2.launch2d(c["nb"], J=[a.data_ptr() for a in J], J_sizes=[a.numel() for a in J], pos=pos, momz=momz, charge=q,
+                  weight=w, bin_index=bin_index, invgf=invgf, iold=iold, deltaold=delta,
+                  inv_cell_volume=1.0 / float(np.prod(c["cl"])), dx_inv=[1.0 / v for v in c["cl"]],
+                  dx_ov_dt=[v / c["dt"] for v in c["cl"]], domain_begin=[-2, -2], nprimy=c["n_prim"][1],
+                  cell_sorting=cell_sorting, stream=stream)
+
+
+def test_reference_gpu_deposit_2d_matches_oracle(ref2, cpu_oracle):
+    """The 2D kernel's loops run over the whole 5 x 5 stencil: its three currents match the
+    oracle's for particles moving either way."""
+    rng = np.random.default_rng(23)
+    cells = np.array([16, 12])
+    cl = np.array([0.1, 0.15])
+    nb = cells // 4
+    n = int(cells.prod()) * 6
+    cell = rng.integers(0, cells, size=(n, 2))
+    binid = (cell[:, 0] // 4) * nb[1] + cell[:, 1] // 4
+    order = np.argsort(binid, kind="stable")
+    cell, binid = cell[order], binid[order]
+    frac = rng.uniform(0, 1, (n, 2))
+    xold = ((cell + frac) * cl).T.copy()
+    xnew = ((cell + frac + rng.uniform(-0.45, 0.45, (n, 2))) * cl).T.copy()
+    mom = rng.normal(0, 0.3, (3, n))
+    invgf = 1.0 / np.sqrt(1.0 + (mom ** 2).sum(0))
+    w = rng.uniform(0.5, 1.5, n)
+    q = np.where(rng.uniform(size=n) < 0.5, -1, 1).astype(np.int16)
+    iold = np.zeros(2 * n, np.int32)
+    delta = np.zeros(2 * n)
+    for d in range(2):
+        xn = xold[d] / cl[d]
+        ip = np.floor(xn + 0.5)
+        iold[d * n:(d + 1) * n] = (ip + 2).astype(np.int32)
+        delta[d * n:(d + 1) * n] = xn - ip
+        ipo = iold[d * n:(d + 1) * n] - 2 - 4 * (cell[:, d] // 4)
+        assert ipo.min() >= 0 and ipo.max() <= 4
+    n_prim = (cells + 5).tolist()
+    c = dict(nb=nb, cl=cl, dt=0.05, n_prim=n_prim)
+    shapes = [(n_prim[0] + 1, n_prim[1]), (n_prim[0], n_prim[1] + 1), (n_prim[0], n_prim[1])]
+    J = cpu_oracle.project(0, 2, n_prim, [-2, -2], cl, c["dt"], xnew, mom, w, q, invgf, iold, delta,
+                           [np.zeros(s) for s in shapes] + [None])[:3]
+    Jd = [torch.zeros(s, dtype=torch.float64, device="cuda") for s in shapes]
+    t = [_cu(xnew[0]), _cu(xnew[1]), _cu(mom[2]), _cu(q), _cu(w), _cu(np.cumsum(np.bincount(binid, minlength=int(nb.prod()))), np.int32),
+         _cu(invgf), _cu(iold), _cu(delta)]
+    _launch2d(ref2, c, Jd, [t[0].data_ptr(), t[1].data_ptr()], *[a.data_ptr() for a in t[2:]])
+    torch.cuda.synchronize()
+    for k in range(3):
+        assert rel_err(Jd[k].cpu().numpy(), J[k]) <= 1e-12, k
+
+
+def test_fused_step_against_reference_gpu_deposit_2d_thermal(ref2):
+    """The 2D thermal plasma of the bench (256 x 256 cells, electrons and protons at 16 ppc
+    each, Boris): the reference's deposit of both species against this project's particle
+    kernels of a step (gather, push, deposit and re-binning of both species)."""
+    from smilei_gb300 import simulation, _lib
+    N, ppc, dx = 256, 16, 0.1
+    dt = 0.95 * dx / np.sqrt(2.0)
+    sig = np.sqrt(10.0 / 511.0)
+    species = [(1.0, -1, sig), (1836.0, 1, sig / np.sqrt(1836.0))]
+    nb = N // 4
+    n = N * N * ppc
+    c = dict(nb=[nb, nb], cl=[dx, dx], dt=dt, n_prim=[N + 5, N + 5])
+    stream = torch.cuda.current_stream()
+    shapes = [(N + 6, N + 5), (N + 5, N + 6), (N + 5, N + 5)]
+    Jd = [torch.zeros(s, dtype=torch.float64, device="cuda") for s in shapes]
+    g = torch.Generator(device="cuda")
+    g.manual_seed(9)
+    plasma, launches = [], []
+    for k, (mass, charge, sigma) in enumerate(species):
+        cb = torch.arange(n, device="cuda", dtype=torch.int64) // ppc
+        b, loc = cb // 16, cb % 16
+        cell = [(b // nb) * 4 + loc // 4, (b % nb) * 4 + loc % 4]
+        xold = torch.empty((2, n), dtype=torch.float64, device="cuda")
+        for d in range(2):
+            xold[d] = (cell[d].to(torch.float64) + torch.rand(n, generator=g, device="cuda", dtype=torch.float64)) * dx
+        mom = torch.randn((3, n), generator=g, device="cuda", dtype=torch.float64) * sigma
+        invgf = 1.0 / torch.sqrt(1.0 + (mom * mom).sum(0))
+        xnew = (xold + mom[:2] * invgf * dt).contiguous()
+        ip = torch.floor(xold / dx + 0.5)
+        iold = (ip + 2).to(torch.int32).reshape(-1).contiguous()
+        delta = (xold / dx - ip).reshape(-1).contiguous()
+        w = torch.full((n,), dx * dx / ppc, dtype=torch.float64, device="cuda")
+        q = torch.full((n,), charge, dtype=torch.int16, device="cuda")
+        bin_index = ((torch.arange(nb * nb, device="cuda", dtype=torch.int64) + 1) * 16 * ppc).to(torch.int32)
+        momz = mom[2].contiguous()
+        keep = [xnew, iold, delta, w, q, bin_index, momz, invgf]
+        launches.append((keep, [xnew[0].data_ptr(), xnew[1].data_ptr()], momz.data_ptr(), q.data_ptr(), w.data_ptr(),
+                         bin_index.data_ptr(), invgf.data_ptr(), iold.data_ptr(), delta.data_ptr()))
+        plasma.append((mass, float(charge), xold, mom, w))
+    ref_ms = {}
+    for sorting in (False, True):
+        for _, pos, *ptrs in launches:
+            _launch2d(ref2, c, Jd, pos, *ptrs, stream=stream.cuda_stream, cell_sorting=sorting)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(5):
+            for _, pos, *ptrs in launches:
+                _launch2d(ref2, c, Jd, pos, *ptrs, stream=stream.cuda_stream, cell_sorting=sorting)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ref_ms["cell_sorting" if sorting else "default"] = e0.elapsed_time(e1) / 5
+    assert float(Jd[2].abs().sum()) > 0.0
+    ours = {}
+    for form in ("mixed", "fp64"):
+        s = torch.cuda.Stream()
+        sim = simulation.Simulation([N, N], [dx, dx], dt, form=form)
+        _lib.check(_lib.lib().sg_sim_set_stream(sim._h, s.cuda_stream), "set_stream")
+        for mass, charge, xold, mom, w in plasma:
+            sim.add_species(mass, charge, "boris", xold, mom, w)
+        with torch.cuda.stream(s):
+            sim.step(3)
+            tp = []
+            for _ in range(5):
+                sim.step(1)
+                tp.append(sim.last_timing()[0])
+        sim.close()
+        ours[form] = float(np.mean(tp))
+    line = {"particles": 2 * n, "reference_deposit_ms_both_species": ref_ms, "fused_particle_kernels_ms": ours,
+            "reference_default_over_fused_mixed": ref_ms["default"] / ours["mixed"],
+            "reference_default_over_fused_fp64": ref_ms["default"] / ours["fp64"]}
+    print("REF_GPU_DEPOSIT_2D " + json.dumps(line))
+    assert ours["mixed"] < ref_ms["default"]
