@@ -2717,6 +2717,8 @@ struct sg_sim {
     // memory; a streamed step computes them while its last ranges are copied out
     double *h_energy = nullptr;
     bool energy_valid = false;
+    std::vector<int64_t> h_off; // streamed step: prefix of the packed tile counts (kept, not refaulted)
+    size_t max_pitch = 0;       // the device's largest pitch for strided copies
 };
 
 namespace sg {
@@ -4449,6 +4451,22 @@ int sg_stream_ranges( int ndim, const int *ntiles, int periodic, const int *coun
 
 int enqueue_energy( sg_sim *S, cudaStream_t st, bool next );
 
+// Particles [p0, p1) of every plane of a packed state (planes of n values of esz bytes
+// after an hdr-byte header) between host and device: one strided copy where the planes'
+// distance is within the device's pitch limit, else one copy per plane.
+static cudaError_t copy_planes( char *dst, const char *src, size_t hdr, int planes, int64_t n, int64_t p0, int64_t p1,
+                                size_t esz, size_t max_pitch, cudaMemcpyKind kind, cudaStream_t st )
+{
+    if( p1 <= p0 ) return cudaSuccess;
+    const size_t pitch = ( size_t )n * esz, o = hdr + ( size_t )p0 * esz, w = ( size_t )( p1 - p0 ) * esz;
+    if( pitch <= max_pitch ) return cudaMemcpy2DAsync( dst + o, pitch, src + o, pitch, w, ( size_t )planes, kind, st );
+    for( int k = 0; k < planes; k++ ) {
+        const cudaError_t e = cudaMemcpyAsync( dst + o + k * pitch, src + o + k * pitch, w, kind, st );
+        if( e != cudaSuccess ) return e;
+    }
+    return cudaSuccess;
+}
+
 int sg_sim_step_host( sg_sim *S, int species, const void *host_in, void *host_out, int chunks )
 {
     SG_REQUIRE( S && host_in && host_out, "NULL argument" );
@@ -4469,7 +4487,9 @@ int sg_sim_step_host( sg_sim *S, int species, const void *host_in, void *host_ou
                 ( long long )s.npart );
     const int nt = S->g.ntiles, nd = S->g.ndim;
     const int *hc = reinterpret_cast<const int *>( hin + 8 );
-    std::vector<int64_t> hoff( nt + 1, 0 );
+    std::vector<int64_t> &hoff = S->h_off;
+    hoff.resize( ( size_t )nt + 1 );
+    hoff[0] = 0;
     for( int t = 0; t < nt; t++ ) {
         SG_REQUIRE( hc[t] >= 0, "tile %d of the packed state has a negative count", t );
         hoff[t + 1] = hoff[t] + hc[t];
@@ -4497,6 +4517,12 @@ int sg_sim_step_host( sg_sim *S, int species, const void *host_in, void *host_ou
     r = packed_staging( S, bytes );
     if( r ) return r;
     if( !S->copy_stream ) SG_CUDA_TRY( cudaStreamCreateWithFlags( &S->copy_stream, cudaStreamNonBlocking ) );
+    if( !S->max_pitch ) {
+        int dev = 0, mp = 0;
+        SG_CUDA_TRY( cudaGetDevice( &dev ) );
+        SG_CUDA_TRY( cudaDeviceGetAttribute( &mp, cudaDevAttrMaxPitch, dev ) );
+        S->max_pitch = ( size_t )( mp > 0 ? mp : 1 );
+    }
     while( ( int )S->copy_ev.size() < 2 * nr + 3 ) {
         cudaEvent_t e = nullptr;
         SG_CUDA_TRY( cudaEventCreate( &e ) ); // timed: the stage times of the step
@@ -4529,10 +4555,7 @@ int sg_sim_step_host( sg_sim *S, int species, const void *host_in, void *host_ou
     SG_CUDA_TRY( cudaEventRecord( S->copy_ev[1], cs ) );
     for( int j = 0; j < nr; j++ ) {
         const int64_t p0 = hoff[in.ta[j]], p1 = hoff[in.tb[j]];
-        for( int k = 0; k < planes && p1 > p0; k++ ) {
-            const size_t o = hdr + ( ( size_t )k * ( size_t )n + ( size_t )p0 ) * esz;
-            SG_CUDA_TRY( cudaMemcpyAsync( stg + o, hin + o, ( size_t )( p1 - p0 ) * esz, cudaMemcpyHostToDevice, cs ) );
-        }
+        SG_CUDA_TRY( copy_planes( stg, hin, hdr, planes, n, p0, p1, esz, S->max_pitch, cudaMemcpyHostToDevice, cs ) );
         SG_CUDA_TRY( cudaEventRecord( S->copy_ev[2 + j], cs ) );
     }
     r = pad_fields( S, S->stream );
@@ -4569,10 +4592,8 @@ int sg_sim_step_host( sg_sim *S, int species, const void *host_in, void *host_ou
             for( int i = 0; i < nr; i++ )
                 if( hoff[in.ta[i]] < p1 && hoff[in.tb[i]] > p0 ) last_in = std::max( last_in, i );
             if( last_in >= 0 ) e = cudaStreamWaitEvent( S->out_stream, S->copy_ev[2 + last_in], 0 );
-            for( int k = 0; k < planes && p1 > p0 && e == cudaSuccess; k++ ) {
-                const size_t o = hdr + ( ( size_t )k * ( size_t )n + ( size_t )p0 ) * esz;
-                e = cudaMemcpyAsync( hout + o, ostg + o, ( size_t )( p1 - p0 ) * esz, cudaMemcpyDeviceToHost, S->out_stream );
-            }
+            if( e == cudaSuccess )
+                e = copy_planes( hout, ostg, hdr, planes, n, p0, p1, esz, S->max_pitch, cudaMemcpyDeviceToHost, S->out_stream );
             if( e != cudaSuccess ) break;
         }
         if( e == cudaSuccess ) e = cudaMemcpyAsync( hout + 8, ostg + 8, 4 * ( size_t )nt, cudaMemcpyDeviceToHost, S->out_stream );
