@@ -40,14 +40,19 @@ def _build(simulation, n_cells, cl, dt, form, fields, species, **kw):
     return sim
 
 
-@pytest.mark.parametrize("ndim,form,nsteps,tol", [(3, "fp64", 19, 1e-12), (2, "fp64", 19, 1e-12),
-                                                  (3, "mixed", 10, 1e-4), (2, "mixed", 10, 1e-4)])
-def test_batched_steps_match_single_steps(sim_mod, ndim, form, nsteps, tol):
+@pytest.mark.parametrize("ndim,form,nsteps,tol,queue", [(3, "fp64", 19, 1e-12, False), (2, "fp64", 19, 1e-12, False),
+                                                        (3, "mixed", 10, 1e-4, False), (2, "mixed", 10, 1e-4, False),
+                                                        (3, "mixed", 10, 1e-4, True)])
+def test_batched_steps_match_single_steps(sim_mod, ndim, form, nsteps, tol, queue):
+    """queue: the persistent tile-queue kernel, whose counter is reset inside each step."""
     simulation, synthetic, tg = sim_mod
     spec = [(1.0, -1, "boris", 4, 0.3), (1836.0, 1, "higueracary", 2, 0.01)]
     n_cells, cl, dt, fields, species = tg.make_case(synthetic, ndim, 7, spec)
     a = _build(simulation, n_cells, cl, dt, form, fields, species)
     b = _build(simulation, n_cells, cl, dt, form, fields, species)
+    if queue:
+        a.set_tile_queue(True)
+        b.set_tile_queue(True)
     a.step(nsteps)
     for _ in range(nsteps):
         b.step(1)
