@@ -365,6 +365,26 @@ int sg_sim_set_species_radiation( sg_sim *sim, int species, const sg_rad_tables 
  * radiating species since sg_sim_set_species_radiation. */
 int sg_sim_radiation_stats( sg_sim *sim, int species, double *radiated, unsigned long long *emissions );
 
+/* Macro-photons of a radiating species in the resident step, as a species whose
+ * radiation_photon_species is set (RadiationMonteCarlo.cpp:425-545): an emission whose
+ * photon gamma is at least gamma_threshold, while the particle has made fewer than
+ * max_emissions photon groups in the step, appends `sampling` photons (weight w /
+ * sampling, momentum photon_gamma p / |p| after the recoil, chi, tau = -1) at the
+ * particle's position to a device store of `capacity` photons, and its energy is not
+ * added to the radiated tally.  Each step then pushes every stored photon
+ * (PusherPhoton, src/Pusher/PusherPhoton.cpp:30-85: x += dt p / |p|, wrapped on periodic
+ * axes; on an open axis it keeps going, and a moving window does not shift it).  Photons
+ * past the capacity are counted, not stored.  capacity 0 removes the store.  Call after
+ * sg_sim_set_species_radiation. */
+int sg_sim_set_species_photons( sg_sim *sim, int species, int sampling, double gamma_threshold, int max_emissions,
+                                int64_t capacity );
+
+/* The photons wanted so far (*count; may pass the capacity) and host copies of the n =
+ * min(count, capacity) stored ones: pos[d * n + k] (x, y), mom[c * n + k], weight[k],
+ * chi[k], tau[k].  Any output may be NULL. */
+int sg_sim_get_photons( sg_sim *sim, int species, int64_t *count, double *pos, double *mom, double *weight,
+                        double *chi, double *tau );
+
 /* Device time of the last sg_sim_step call split by stage (ms): particles, fold,
  * maxwell, total; and the number of kernel launches per step. */
 int sg_sim_last_timing( sg_sim *sim, double *ms_particles, double *ms_fields, double *ms_total, int *launches_per_step );

@@ -79,6 +79,8 @@ _SIGNATURES = {
     "sg_sim_add_laser_gaussian2d": (_I, [_VP, _VP]),
     "sg_sim_layout_stats": (_I, [_VP, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
     "sg_sim_batch_stats": (_I, [_VP, ctypes.POINTER(_I64), ctypes.POINTER(_I64), ctypes.POINTER(_I)]),
+    "sg_sim_set_species_photons": (_I, [_VP, _I, _I, _D, _I, _I64]),
+    "sg_sim_get_photons": (_I, [_VP, _I, ctypes.POINTER(_I64), _VP, _VP, _VP, _VP, _VP]),
     "sg_sim_set_moving_window": (_I, [_VP, _D, _D, _I]),
     "sg_sim_window_state": (_I, [_VP, ctypes.POINTER(_I64), ctypes.POINTER(_D), ctypes.POINTER(_I64)]),
     "sg_sim_set_species_profile": (_I, [_VP, _I, _VP, _I, _D, ctypes.c_uint64]),

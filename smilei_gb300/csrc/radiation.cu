@@ -635,7 +635,8 @@ __device__ __forceinline__ float mlp_coop( const MlpView &m, const MlpShared<H> 
 // FP64), RadiationMonteCarlo::operator() (RadiationMonteCarlo.cpp:62-611).  Called by
 // every lane of a warp (inactive lanes too): the loop is warp-synchronous, so that the
 // lanes that emit through the network evaluate it together, one emission after another.
-// ph.count == null: no macro-photons (then q and n are unused).
+// ph.count == null: no macro-photons (then xp is unused); xp: the particle's position
+// (ph.ndim values), where its photons start.
 // P: the arithmetic of the momenta and of the recoil (double for FP64 momenta, float
 // for the mixed form's FP32 momenta).
 template <int H, class P>
@@ -643,7 +644,7 @@ __device__ __forceinline__ void mc_pass_f32( const RadTab &t, const MlpView &m, 
                                              const MlpShared<H == 0 ? 4 : H> &sw, bool active, double dt, double qm2,
                                              const float *E3, const float *B3, P &px, P &py, P &pz,
                                              float &tp, uint32_t &rs, double wgt, double &rad, unsigned long long &nem,
-                                             const PhotonOut &ph, int64_t q, int64_t n )
+                                             const PhotonOut &ph, const double *xp )
 {
     const int lane = threadIdx.x & 31;
     const float Ex = E3[0], Ey = E3[1], Ez = E3[2], Bx = B3[0], By = B3[1], Bz = B3[2];
@@ -775,7 +776,7 @@ __device__ __forceinline__ void mc_pass_f32( const RadTab &t, const MlpView &m, 
                 for( int k = 0; k < ph.sampling; k++ ) {
                     const unsigned long long o = o0 + ( unsigned long long )k;
                     if( o >= ( unsigned long long )ph.cap ) break;
-                    for( int dd = 0; dd < ph.ndim; dd++ ) ph.ph_pos[dd * ph.cap + o] = ph.pos[dd * n + q];
+                    for( int dd = 0; dd < ph.ndim; dd++ ) ph.ph_pos[dd * ph.cap + o] = xp[dd];
                     ph.ph_mom[o] = ( double )pg * px * inv;
                     ph.ph_mom[ph.cap + o] = ( double )pg * py * inv;
                     ph.ph_mom[2 * ph.cap + o] = ( double )pg * pz * inv;
@@ -911,7 +912,9 @@ __global__ void k_monte_carlo( RadTab t, MlpView m, int use_mlp, int64_t n, doub
             tp = ( float )tau[q];
         }
         uint32_t rs = rng_init( seed, first_id + ( uint32_t )q, step );
-        mc_pass_f32<H, double>( t, m, use_mlp, sw, active, dt, qm2, E3, B3, px, py, pz, tp, rs, w[q], rad, nem, ph, q, n );
+        double xp[3] = { 0.0, 0.0, 0.0 };
+        for( int d = 0; ph.count && active && d < ph.ndim; d++ ) xp[d] = ph.pos[d * n + q];
+        mc_pass_f32<H, double>( t, m, use_mlp, sw, active, dt, qm2, E3, B3, px, py, pz, tp, rs, w[q], rad, nem, ph, xp );
         if( active ) {
             mom[p] = px;
             mom[n + p] = py;
@@ -990,6 +993,21 @@ __global__ void __launch_bounds__( 128 ) k_radiate_resident( RadTab t, MlpView m
     }
     const uint32_t step = ( uint32_t )*r.step;
     const int nyp = r.np[1], nyd = nyp + 1;
+    // macro-photons of the species, when it has a photon store
+    PhotonOut ph{};
+    if( r.ph_count ) {
+        ph.ndim = 2;
+        ph.sampling = r.ph_sampling;
+        ph.max_emissions = r.ph_max_emissions;
+        ph.threshold = r.ph_threshold;
+        ph.cap = r.ph_cap;
+        ph.count = r.ph_count;
+        ph.ph_pos = r.ph_pos;
+        ph.ph_mom = r.ph_mom;
+        ph.ph_w = r.ph_w;
+        ph.ph_chi = r.ph_chi;
+        ph.ph_tau = r.ph_tau;
+    }
     double rad = 0.0;
     unsigned long long nem = 0;
     // one thread per buffer slot (all tiles' segments, holes included), so that a few
@@ -1009,10 +1027,13 @@ __global__ void __launch_bounds__( 128 ) k_radiate_resident( RadTab t, MlpView m
         }
         float px = 0.0f, py = 0.0f, pz = 0.0f;
         float E3[3] = { 0.0f, 0.0f, 0.0f }, B3[3] = { 0.0f, 0.0f, 0.0f }, tp = 0.0f, wq = 0.0f;
+        double xp[3] = { 0.0, 0.0, 0.0 }; // the particle's position, where its photons start
         if( active ) {
             const unsigned k = r.key[o];
             const int gx = ( int )( k >> 16 ), gy = ( int )( k & 65535u );
             const float dxl = r.d[0][o], dyl = r.d[1][o];
+            xp[0] = ( ( double )gx + ( double )dxl ) * r.dx[0];
+            xp[1] = ( ( double )gy + ( double )dyl ) * r.dx[1];
             float cpx[3], cpy[3], cdx[3], cdy[3];
             bspl2( dxl, cpx[0], cpx[1], cpx[2] );
             bspl2( dyl, cpy[0], cpy[1], cpy[2] );
@@ -1036,7 +1057,7 @@ __global__ void __launch_bounds__( 128 ) k_radiate_resident( RadTab t, MlpView m
         }
         uint32_t rs = rng_init( r.seed, ( uint32_t )o, step );
         mc_pass_f32<H, float>( t, m, use_mlp, sw, active, r.dt, r.qm2, E3, B3, px, py, pz, tp, rs, ( double )wq, rad, nem,
-                               PhotonOut{}, 0, 0 );
+                               ph, xp );
         if( active ) {
             r.p[0][o] = px;
             r.p[1][o] = py;

@@ -11,7 +11,7 @@ namespace sg {
 
 // One radiating species of a 2D mixed-form simulation, as the pass sees it: tile
 // segments of packed node keys and FP32 offsets, momenta, weights and optical depths,
-// and the E, B_m field arrays (x-major, ghost width 2).
+// the E, B_m field arrays (x-major, ghost width 2), and where its photons go.
 struct ResidentRad {
     int N[2], np[2], T[2], nt[2], ntiles;
     double dx[2], dxi[2];
@@ -29,6 +29,13 @@ struct ResidentRad {
     const int64_t *step; // device step counter: the random streams of a step
     double *radiated;    // device tallies
     unsigned long long *emissions;
+    // macro-photon store (ph_count null: none; an emission's energy then goes to
+    // `radiated`): ph_pos[d * ph_cap + k], ph_mom[c * ph_cap + k], ph_w/chi/tau[k]
+    int ph_sampling, ph_max_emissions;
+    double ph_threshold;
+    int64_t ph_cap;
+    unsigned long long *ph_count;
+    double *ph_pos, *ph_mom, *ph_w, *ph_chi, *ph_tau;
 };
 
 // Enqueues the pass on `stream` (FP32 arithmetic; the table, or the network where

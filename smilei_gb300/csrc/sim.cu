@@ -2414,6 +2414,26 @@ __global__ void k_norm2( GridInfo g, Norm2Set f, int per_array, double *__restri
 
 __global__ void k_bump_step( int64_t *step ) { *step += 1; }
 
+// PusherPhoton::operator() (src/Pusher/PusherPhoton.cpp:30-85) on a species' stored
+// macro-photons (2D, FP64 planes of cap values): x += dt p / |p|, then the periodic wrap
+// on periodic axes (length L[d]; BoundaryConditionType.cpp periodic).  The count of
+// stored photons is read on the device: min(*count, cap).
+__global__ void k_push_resident_photons( int64_t cap, const unsigned long long *__restrict__ count, double dt,
+                                         double *__restrict__ pos, const double *__restrict__ mom, double L0,
+                                         double L1, int periodic0, int periodic1 )
+{
+    const int64_t n = min( ( int64_t )*count, cap );
+    for( int64_t k = ( int64_t )blockIdx.x * blockDim.x + threadIdx.x; k < n; k += ( int64_t )gridDim.x * blockDim.x ) {
+        const double px = mom[k], py = mom[cap + k], pz = mom[2 * cap + k];
+        const double inv = 1.0 / sqrt( px * px + py * py + pz * pz );
+        double x = pos[k] + dt * px * inv, y = pos[cap + k] + dt * py * inv;
+        if( periodic0 ) x = x < 0.0 ? x + L0 : ( x >= L0 ? x - L0 : x );
+        if( periodic1 ) y = y < 0.0 ? y + L1 : ( y >= L1 ? y - L1 : y );
+        pos[k] = x;
+        pos[cap + k] = y;
+    }
+}
+
 // Steps in one batched graph.
 constexpr int BATCH_STEPS = 8;
 
@@ -2596,6 +2616,14 @@ struct SpeciesState {
     const sg_mlp *rad_mlp = nullptr;
     uint32_t rad_seed = 0;
     double *d_rad = nullptr;   // device tallies: radiated energy, emissions (as unsigned long long)
+    // its macro-photons (RadiationMonteCarlo.cpp:425-545 with a photon species): a device
+    // store of ph_cap photons (FP64: x, y; px, py, pz; weight; chi; tau planes of ph_cap)
+    // and the count of photons wanted so far (may pass ph_cap: those are not stored)
+    double *ph_mem = nullptr;
+    int64_t ph_cap = 0;
+    unsigned long long *ph_count = nullptr;
+    int ph_sampling = 1, ph_max_emissions = 1;
+    double ph_threshold = 2.0;
     double slack = 0.0;        // capacity slack of this species' layout (0: the configuration's)
     int64_t last_relayout = -1; // step of its last re-layout after a spill
     bool inject = false;       // fresh window cells are filled from this profile
@@ -2956,6 +2984,18 @@ int launch_radiation( sg_sim *S, SpeciesState &s, cudaStream_t st )
     r.step = S->d_rad_step;
     r.radiated = s.d_rad;
     r.emissions = reinterpret_cast<unsigned long long *>( s.d_rad + 1 );
+    if( s.ph_mem ) {
+        r.ph_sampling = s.ph_sampling;
+        r.ph_max_emissions = s.ph_max_emissions;
+        r.ph_threshold = s.ph_threshold;
+        r.ph_cap = s.ph_cap;
+        r.ph_count = s.ph_count;
+        r.ph_pos = s.ph_mem;
+        r.ph_mom = s.ph_mem + 2 * s.ph_cap;
+        r.ph_w = s.ph_mem + 5 * s.ph_cap;
+        r.ph_chi = s.ph_mem + 6 * s.ph_cap;
+        r.ph_tau = s.ph_mem + 7 * s.ph_cap;
+    }
     return launch_radiate_resident( s.rad_tables, s.rad_mlp, r, st );
 }
 
@@ -3046,6 +3086,16 @@ int enqueue_step( sg_sim *S, cudaStream_t st, const StreamIn *in = nullptr, bool
     if( radiated ) {
         k_bump_step<<<1, 1, 0, st>>>( S->d_rad_step );
         SG_LAUNCH_CHECK( "k_bump_step" );
+        launches++;
+    }
+    // the photon species' own push, over every stored photon, those just created too
+    for( auto &s : S->sp ) {
+        if( !s.ph_mem ) continue;
+        const GridInfo &g = S->g;
+        k_push_resident_photons<<<152 * 4, 256, 0, st>>>( s.ph_cap, s.ph_count, g.dt, s.ph_mem, s.ph_mem + 2 * s.ph_cap,
+                                                          g.N[0] * g.dx[0], g.N[1] * g.dx[1], g.open[0] ? 0 : 1,
+                                                          g.open[1] ? 0 : 1 );
+        SG_LAUNCH_CHECK( "k_push_resident_photons" );
         launches++;
     }
     for( auto &s : S->sp ) {
@@ -3647,6 +3697,8 @@ int sg_sim_destroy( sg_sim *S )
         release( s.tau_mem[1] );
         release( s.ovf_tau );
         release( s.d_rad );
+        release( s.ph_mem );
+        release( s.ph_count );
     }
     release( S->d_rad_step );
     release( S->fmem );
@@ -4152,6 +4204,61 @@ int sg_sim_radiation_stats( sg_sim *S, int species, double *radiated, unsigned l
     SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
     if( radiated ) *radiated = h[0];
     if( emissions ) std::memcpy( emissions, &h[1], sizeof( unsigned long long ) );
+    return SG_OK;
+}
+
+int sg_sim_set_species_photons( sg_sim *S, int species, int sampling, double gamma_threshold, int max_emissions,
+                                int64_t capacity )
+{
+    SG_REQUIRE( S, "NULL simulation" );
+    SG_REQUIRE( species >= 0 && species < ( int )S->sp.size(), "species %d out of range", species );
+    SpeciesState &s = S->sp[species];
+    SG_REQUIRE( s.radiates, "species %d does not radiate (sg_sim_set_species_radiation first)", species );
+    SG_REQUIRE( capacity >= 0, "capacity < 0" );
+    SG_REQUIRE( capacity == 0 || ( sampling >= 1 && max_emissions >= 1 ), "sampling and max_emissions must be >= 1" );
+    SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
+    drop_graphs( S ); // the pass and the step hold the store's pointers
+    release( s.ph_mem );
+    release( s.ph_count );
+    s.ph_mem = nullptr;
+    s.ph_count = nullptr;
+    s.ph_cap = 0;
+    if( capacity == 0 ) return SG_OK;
+    if( cudaMalloc( &s.ph_mem, ( size_t )capacity * 8 * sizeof( double ) ) != cudaSuccess ||
+        cudaMalloc( &s.ph_count, sizeof( unsigned long long ) ) != cudaSuccess ) {
+        release( s.ph_mem );
+        s.ph_mem = nullptr;
+        return set_error( SG_ERR_NOMEM, "cannot allocate a store of %lld photons", ( long long )capacity );
+    }
+    SG_CUDA_TRY( cudaMemsetAsync( s.ph_count, 0, sizeof( unsigned long long ), S->stream ) );
+    s.ph_cap = capacity;
+    s.ph_sampling = sampling;
+    s.ph_threshold = gamma_threshold;
+    s.ph_max_emissions = max_emissions;
+    SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
+    return SG_OK;
+}
+
+int sg_sim_get_photons( sg_sim *S, int species, int64_t *count, double *pos, double *mom, double *weight, double *chi,
+                        double *tau )
+{
+    SG_REQUIRE( S, "NULL simulation" );
+    SG_REQUIRE( species >= 0 && species < ( int )S->sp.size(), "species %d out of range", species );
+    const SpeciesState &s = S->sp[species];
+    SG_REQUIRE( s.ph_mem, "species %d has no photon store (sg_sim_set_species_photons)", species );
+    unsigned long long c = 0;
+    SG_CUDA_TRY( cudaMemcpyAsync( &c, s.ph_count, sizeof( c ), cudaMemcpyDeviceToHost, S->stream ) );
+    SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
+    if( count ) *count = ( int64_t )c;
+    const int64_t n = std::min<int64_t>( ( int64_t )c, s.ph_cap );
+    const size_t b = ( size_t )n * sizeof( double );
+    const int64_t cap = s.ph_cap;
+    for( int d = 0; pos && d < 2; d++ ) SG_CUDA_TRY( cudaMemcpy( pos + d * n, s.ph_mem + d * cap, b, cudaMemcpyDeviceToHost ) );
+    for( int d = 0; mom && d < 3; d++ )
+        SG_CUDA_TRY( cudaMemcpy( mom + d * n, s.ph_mem + ( 2 + d ) * cap, b, cudaMemcpyDeviceToHost ) );
+    if( weight ) SG_CUDA_TRY( cudaMemcpy( weight, s.ph_mem + 5 * cap, b, cudaMemcpyDeviceToHost ) );
+    if( chi ) SG_CUDA_TRY( cudaMemcpy( chi, s.ph_mem + 6 * cap, b, cudaMemcpyDeviceToHost ) );
+    if( tau ) SG_CUDA_TRY( cudaMemcpy( tau, s.ph_mem + 7 * cap, b, cudaMemcpyDeviceToHost ) );
     return SG_OK;
 }
 

@@ -259,6 +259,29 @@ class Simulation:
               "radiation_stats")
         return r.value, e.value
 
+    def set_species_photons(self, species, sampling=1, gamma_threshold=2.0, max_emissions=10, capacity=1 << 20):
+        """Macro-photons of a radiating species (sg_sim_set_species_photons): emissions
+        above gamma_threshold create `sampling` photons each in a device store of
+        `capacity`, pushed every step; capacity 0 removes the store."""
+        check(_lib.lib().sg_sim_set_species_photons(self._h, int(species), int(sampling), float(gamma_threshold),
+                                                    int(max_emissions), int(capacity)), "set_species_photons")
+        if not hasattr(self, "_ph_cap"):
+            self._ph_cap = {}
+        self._ph_cap[int(species)] = int(capacity)
+
+    def get_photons(self, species):
+        """(photons wanted so far, dict(pos[2, n], mom[3, n], weight, chi, tau)) of the n
+        stored ones (n = min(count, capacity))."""
+        c = ctypes.c_int64()
+        check(_lib.lib().sg_sim_get_photons(self._h, int(species), ctypes.byref(c), None, None, None, None, None),
+              "get_photons")
+        n = min(c.value, getattr(self, "_ph_cap", {}).get(int(species), 0))
+        pos, mom = np.zeros((2, n)), np.zeros((3, n))
+        w, chi, tau = np.zeros(n), np.zeros(n), np.zeros(n)
+        check(_lib.lib().sg_sim_get_photons(self._h, int(species), ctypes.byref(c), pos.ctypes.data, mom.ctypes.data,
+                                            w.ctypes.data, chi.ctypes.data, tau.ctypes.data), "get_photons")
+        return c.value, dict(pos=pos, mom=mom, weight=w, chi=chi, tau=tau)
+
     def fill_species(self, species, x0=0, x1=None):
         """Creates the species' particles in window cells [x0, x1) (default: the whole grid)."""
         x1 = self.n_cells[0] if x1 is None else x1

@@ -392,3 +392,58 @@ def test_resident_radiation_matches_the_operator_loop(rad):
     assert r0 == 0.0 and e0 == 0
     assert np.allclose(np.sort(m0[0]), np.sort(mom[0]), rtol=1e-6)
     T32.close()
+
+
+def test_resident_photons_carry_the_emitted_energy(rad):
+    """Macro-photons of the resident step (sg_sim_set_species_photons) in a uniform
+    magnetic field (B_z = 50, no E: the push changes no particle energy, so only the
+    radiation does): over one step the electrons' kinetic energy falls by the radiated
+    tally plus the photons' energy (sum w_ph |p_ph|); every photon carries w / sampling,
+    tau = -1, a positive chi and at least the threshold energy, and sits in the box.  A
+    second step moves each photon of the first by dt p / |p| (wrapped) and appends the
+    new ones after them."""
+    radiation, _, _ = rad
+    from smilei_gb300 import simulation, synthetic
+    g = np.load(__import__("os").path.join(__import__("os").path.dirname(__file__), "golden", "radiation.npz"))
+    f_dn, f_cl, inv_es = radiation.normalised_factors(2.0 * np.pi * 299792458.0 / 1e-6)
+    T32 = radiation.RadiationTables(g["integfochi"], g["integfochi_min"], g["integfochi_max"], g["xi_table"],
+                                    g["xi_min"], g["xi_max"], g["xi_axis1_min"], f_dn, f_cl, inv_es)
+    T32.set_fp32_math(True)
+    n_cells, cl, dt = [32, 32], [0.5, 0.5], 0.3
+    L = np.array([n_cells[0] * cl[0], n_cells[1] * cl[1]])
+    rng = np.random.default_rng(31)
+    n = 200000
+    pos = np.stack([rng.uniform(0, L[0], n), rng.uniform(0, L[1], n)])
+    mom = np.stack([np.full(n, -1000.0), rng.normal(0, 1, n), np.zeros(n)])
+    w = np.full(n, 1e-9)
+    sim = simulation.Simulation(n_cells, cl, dt, form="mixed")
+    st = synthetic.STAGGER
+    for k in ("Bz", "Bz_m"):
+        sim.set_field(k, np.full(tuple(n_cells[d] + 5 + st["Bz"][d] for d in range(2)), 50.0))
+    sim.add_species(1.0, -1.0, "boris", pos, mom, w)  # Boris keeps |p| in a pure magnetic field
+    sim.set_species_radiation(0, T32, None, seed=11)
+    sampling, threshold = 2, 20.0
+    sim.set_species_photons(0, sampling=sampling, gamma_threshold=threshold, max_emissions=3, capacity=2_000_000)
+    uk0 = sim.energy()[0]
+    sim.step(1)
+    uk1 = sim.energy()[0]
+    rad_e, nem = sim.radiation_stats(0)
+    count1, ph1 = sim.get_photons(0)
+    assert nem > 10000 and 0 < count1 <= 2_000_000 and count1 % sampling == 0
+    e_ph = float(np.sum(ph1["weight"] * np.sqrt((ph1["mom"] ** 2).sum(0))))
+    assert e_ph > 0.5 * rad_e  # most of the emitted energy goes into photons above the threshold
+    assert abs((uk0 - uk1) - (rad_e + e_ph)) <= 1e-4 * (uk0 - uk1), (uk0 - uk1, rad_e, e_ph)
+    assert np.allclose(ph1["weight"], 1e-9 / sampling, rtol=1e-6)
+    assert np.all(ph1["tau"] == -1.0) and np.all(ph1["chi"] > 0.0)
+    assert np.all(np.sqrt((ph1["mom"] ** 2).sum(0)) >= threshold * (1 - 1e-6))
+    assert np.all((ph1["pos"] >= 0.0) & (ph1["pos"] < L[:, None]))
+    sim.step(1)
+    count2, ph2 = sim.get_photons(0)
+    assert count2 > count1
+    p = ph1["mom"]
+    moved = ph1["pos"] + dt * p[:2] / np.sqrt((p ** 2).sum(0))
+    moved = np.where(moved >= L[:, None], moved - L[:, None], np.where(moved < 0.0, moved + L[:, None], moved))
+    assert np.allclose(ph2["pos"][:, :count1], moved, rtol=0, atol=1e-12)
+    assert np.array_equal(ph2["mom"][:, :count1], ph1["mom"])
+    sim.close()
+    T32.close()
