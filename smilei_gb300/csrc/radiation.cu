@@ -520,6 +520,7 @@ struct PhotonOut {
     int64_t cap;
     unsigned long long *count;
     double *ph_pos, *ph_mom, *ph_w, *ph_chi, *ph_tau; // ph_pos[d * cap + k], ph_mom[c * cap + k]
+    double dx[2]; // resident photons: cell lengths, a photon starting at (node + offset) dx
 };
 
 // RadiationMonteCarlo::operator() per particle (see the file header).
@@ -635,16 +636,18 @@ __device__ __forceinline__ float mlp_coop( const MlpView &m, const MlpShared<H> 
 // FP64), RadiationMonteCarlo::operator() (RadiationMonteCarlo.cpp:62-611).  Called by
 // every lane of a warp (inactive lanes too): the loop is warp-synchronous, so that the
 // lanes that emit through the network evaluate it together, one emission after another.
-// ph.count == null: no macro-photons (then xp is unused); xp: the particle's position
-// (ph.ndim values), where its photons start.
+// ph.count == null: no macro-photons (then xp, xn, xo are unused).  Its photons start at
+// the particle's position: xp (ph.ndim values) or, with xp null, (xn + xo) ph.dx (node
+// and offset; the FP64 position is formed only when a photon is made).
 // P: the arithmetic of the momenta and of the recoil (double for FP64 momenta, float
-// for the mixed form's FP32 momenta).
-template <int H, class P>
+// for the mixed form's FP32 momenta).  PH false: no photon output is compiled in.
+template <int H, class P, bool PH = true>
 __device__ __forceinline__ void mc_pass_f32( const RadTab &t, const MlpView &m, int use_mlp,
                                              const MlpShared<H == 0 ? 4 : H> &sw, bool active, double dt, double qm2,
                                              const float *E3, const float *B3, P &px, P &py, P &pz,
                                              float &tp, uint32_t &rs, double wgt, double &rad, unsigned long long &nem,
-                                             const PhotonOut &ph, const double *xp )
+                                             const PhotonOut &ph, const double *xp, const int *xn = nullptr,
+                                             const float *xo = nullptr )
 {
     const int lane = threadIdx.x & 31;
     const float Ex = E3[0], Ey = E3[1], Ez = E3[2], Bx = B3[0], By = B3[1], Bz = B3[2];
@@ -770,13 +773,14 @@ __device__ __forceinline__ void mc_pass_f32( const RadTab &t, const MlpView &m, 
             px -= px * f;
             py -= py * f;
             pz -= pz * f;
-            if( ph.count && ( double )pg >= ph.threshold && i_photon < ph.max_emissions ) {
+            if( PH && ph.count && ( double )pg >= ph.threshold && i_photon < ph.max_emissions ) {
                 const double inv = 1.0 / sqrt( ( double )( px * px + py * py + pz * pz ) );
                 const unsigned long long o0 = atomicAdd( ph.count, ( unsigned long long )ph.sampling );
                 for( int k = 0; k < ph.sampling; k++ ) {
                     const unsigned long long o = o0 + ( unsigned long long )k;
                     if( o >= ( unsigned long long )ph.cap ) break;
-                    for( int dd = 0; dd < ph.ndim; dd++ ) ph.ph_pos[dd * ph.cap + o] = xp[dd];
+                    for( int dd = 0; dd < ph.ndim; dd++ )
+                        ph.ph_pos[dd * ph.cap + o] = xp ? xp[dd] : ( ( double )xn[dd] + ( double )xo[dd] ) * ph.dx[dd];
                     ph.ph_mom[o] = ( double )pg * px * inv;
                     ph.ph_mom[ph.cap + o] = ( double )pg * py * inv;
                     ph.ph_mom[2 * ph.cap + o] = ( double )pg * pz * inv;
@@ -982,7 +986,7 @@ __device__ __forceinline__ float gather2( const float *__restrict__ F, int ny, i
     return r;
 }
 
-template <int H>
+template <int H, bool PH>
 __global__ void __launch_bounds__( 128 ) k_radiate_resident( RadTab t, MlpView m, int use_mlp, ResidentRad r,
                                                              int64_t nslots )
 {
@@ -995,8 +999,10 @@ __global__ void __launch_bounds__( 128 ) k_radiate_resident( RadTab t, MlpView m
     const int nyp = r.np[1], nyd = nyp + 1;
     // macro-photons of the species, when it has a photon store
     PhotonOut ph{};
-    if( r.ph_count ) {
+    if( PH && r.ph_count ) {
         ph.ndim = 2;
+        ph.dx[0] = r.dx[0];
+        ph.dx[1] = r.dx[1];
         ph.sampling = r.ph_sampling;
         ph.max_emissions = r.ph_max_emissions;
         ph.threshold = r.ph_threshold;
@@ -1027,13 +1033,16 @@ __global__ void __launch_bounds__( 128 ) k_radiate_resident( RadTab t, MlpView m
         }
         float px = 0.0f, py = 0.0f, pz = 0.0f;
         float E3[3] = { 0.0f, 0.0f, 0.0f }, B3[3] = { 0.0f, 0.0f, 0.0f }, tp = 0.0f, wq = 0.0f;
-        double xp[3] = { 0.0, 0.0, 0.0 }; // the particle's position, where its photons start
+        int xn[2] = { 0, 0 };            // the particle's node and offset: where its photons start
+        float xo[2] = { 0.0f, 0.0f };
         if( active ) {
             const unsigned k = r.key[o];
             const int gx = ( int )( k >> 16 ), gy = ( int )( k & 65535u );
             const float dxl = r.d[0][o], dyl = r.d[1][o];
-            xp[0] = ( ( double )gx + ( double )dxl ) * r.dx[0];
-            xp[1] = ( ( double )gy + ( double )dyl ) * r.dx[1];
+            xn[0] = gx;
+            xn[1] = gy;
+            xo[0] = dxl;
+            xo[1] = dyl;
             float cpx[3], cpy[3], cdx[3], cdy[3];
             bspl2( dxl, cpx[0], cpx[1], cpx[2] );
             bspl2( dyl, cpy[0], cpy[1], cpy[2] );
@@ -1056,8 +1065,8 @@ __global__ void __launch_bounds__( 128 ) k_radiate_resident( RadTab t, MlpView m
             wq = r.w[o];
         }
         uint32_t rs = rng_init( r.seed, ( uint32_t )o, step );
-        mc_pass_f32<H, float>( t, m, use_mlp, sw, active, r.dt, r.qm2, E3, B3, px, py, pz, tp, rs, ( double )wq, rad, nem,
-                               ph, xp );
+        mc_pass_f32<H, float, PH>( t, m, use_mlp, sw, active, r.dt, r.qm2, E3, B3, px, py, pz, tp, rs, ( double )wq, rad,
+                                   nem, ph, nullptr, xn, xo );
         if( active ) {
             r.p[0][o] = px;
             r.p[1][o] = py;
@@ -1298,10 +1307,19 @@ int launch_radiate_resident( const sg_rad_tables *T, const sg_mlp *mlp, const Re
     const int H = mlp ? v.H : 0;
     const unsigned blocks = ( unsigned )std::min<int64_t>( ( r.nslots + 127 ) / 128, 152 * 64 );
     if( r.nslots <= 0 ) return SG_OK;
-    if( H == 64 ) k_radiate_resident<64><<<blocks, 128, 0, st>>>( T->t, v, 1, r, r.nslots );
-    else if( H == 32 ) k_radiate_resident<32><<<blocks, 128, 0, st>>>( T->t, v, 1, r, r.nslots );
-    else if( H == 16 ) k_radiate_resident<16><<<blocks, 128, 0, st>>>( T->t, v, 1, r, r.nslots );
-    else k_radiate_resident<0><<<blocks, 128, 0, st>>>( T->t, v, mlp ? 1 : 0, r, r.nslots );
+    // the photon output is a separate instance, so that a species without one keeps the
+    // registers of the plain pass
+    if( r.ph_count ) {
+        if( H == 64 ) k_radiate_resident<64, true><<<blocks, 128, 0, st>>>( T->t, v, 1, r, r.nslots );
+        else if( H == 32 ) k_radiate_resident<32, true><<<blocks, 128, 0, st>>>( T->t, v, 1, r, r.nslots );
+        else if( H == 16 ) k_radiate_resident<16, true><<<blocks, 128, 0, st>>>( T->t, v, 1, r, r.nslots );
+        else k_radiate_resident<0, true><<<blocks, 128, 0, st>>>( T->t, v, mlp ? 1 : 0, r, r.nslots );
+    } else {
+        if( H == 64 ) k_radiate_resident<64, false><<<blocks, 128, 0, st>>>( T->t, v, 1, r, r.nslots );
+        else if( H == 32 ) k_radiate_resident<32, false><<<blocks, 128, 0, st>>>( T->t, v, 1, r, r.nslots );
+        else if( H == 16 ) k_radiate_resident<16, false><<<blocks, 128, 0, st>>>( T->t, v, 1, r, r.nslots );
+        else k_radiate_resident<0, false><<<blocks, 128, 0, st>>>( T->t, v, mlp ? 1 : 0, r, r.nslots );
+    }
     SG_LAUNCH_CHECK( "k_radiate_resident" );
     return SG_OK;
 }
