@@ -548,6 +548,58 @@ __device__ __forceinline__ void footprint_weights( T dold, T dnew, int s, T *A, 
     P[1] = P[0] + D[1];
 }
 
+// footprint_weights for dimensions 0 and 1 at once in paired FP32 arithmetic (FADD2,
+// FMUL2: two IEEE operations per instruction), then dimension 2: the same formulas,
+// the splines rounded to the 2^-24 grid as dep_spline rounds them.
+__device__ __forceinline__ float2 neg2( float2 a ) { return make_float2( -a.x, -a.y ); }
+
+__device__ __forceinline__ void dep_spline2( float2 d, float2 &c0, float2 &c1, float2 &c2 )
+{
+    const float2 half = make_float2( 0.5f, 0.5f ), quarter = make_float2( 0.25f, 0.25f );
+    const float2 d2 = __fmul2_rn( d, d );
+    c0 = __fmul2_rn( half, __fadd2_rn( __fadd2_rn( d2, neg2( d ) ), quarter ) );
+    c2 = __fmul2_rn( half, __fadd2_rn( __fadd2_rn( d2, d ), quarter ) );
+    c0 = __fadd2_rn( __fadd2_rn( c0, half ), neg2( half ) );
+    c2 = __fadd2_rn( __fadd2_rn( c2, half ), neg2( half ) );
+    c1 = __fadd2_rn( __fadd2_rn( make_float2( 1.0f, 1.0f ), neg2( c0 ) ), neg2( c2 ) );
+}
+
+template <class T>
+__device__ __forceinline__ void footprint_weights3( const T *dold, const T *dnew, const int *s, T ( *A )[3], T ( *D )[3],
+                                                    T ( *P )[2], T *nov )
+{
+    if constexpr( sizeof( T ) == 4 ) {
+        float2 o0, o1, o2, n0, n1, n2;
+        dep_spline2( make_float2( dold[0], dold[1] ), o0, o1, o2 );
+        dep_spline2( make_float2( dnew[0], dnew[1] ), n0, n1, n2 );
+        const float2 z = make_float2( 0.f, 0.f );
+        // the shift selects, lane by lane
+        const float2 f0 = make_float2( s[0] > 0 ? 0.f : ( s[0] < 0 ? n1.x : n0.x ), s[1] > 0 ? 0.f : ( s[1] < 0 ? n1.y : n0.y ) );
+        const float2 f1 = make_float2( s[0] > 0 ? n0.x : ( s[0] < 0 ? n2.x : n1.x ), s[1] > 0 ? n0.y : ( s[1] < 0 ? n2.y : n1.y ) );
+        const float2 f2 = make_float2( s[0] > 0 ? n1.x : ( s[0] < 0 ? 0.f : n2.x ), s[1] > 0 ? n1.y : ( s[1] < 0 ? 0.f : n2.y ) );
+        const float2 nv = make_float2( s[0] > 0 ? n2.x : n0.x, s[1] > 0 ? n2.y : n0.y );
+        const float2 half = make_float2( 0.5f, 0.5f );
+        const float2 a0 = __fmul2_rn( half, __fadd2_rn( o0, f0 ) ), a1 = __fmul2_rn( half, __fadd2_rn( o1, f1 ) ),
+                     a2 = __fmul2_rn( half, __fadd2_rn( o2, f2 ) );
+        const float2 e0 = __fadd2_rn( f0, neg2( o0 ) ), e1 = __fadd2_rn( f1, neg2( o1 ) ), e2 = __fadd2_rn( f2, neg2( o2 ) );
+        const float2 p0 = __fadd2_rn( e0, make_float2( s[0] < 0 ? nv.x : 0.f, s[1] < 0 ? nv.y : 0.f ) );
+        const float2 p1 = __fadd2_rn( p0, e1 );
+        ( void )z;
+        A[0][0] = a0.x; A[0][1] = a1.x; A[0][2] = a2.x;
+        A[1][0] = a0.y; A[1][1] = a1.y; A[1][2] = a2.y;
+        D[0][0] = e0.x; D[0][1] = e1.x; D[0][2] = e2.x;
+        D[1][0] = e0.y; D[1][1] = e1.y; D[1][2] = e2.y;
+        P[0][0] = p0.x; P[0][1] = p1.x;
+        P[1][0] = p0.y; P[1][1] = p1.y;
+        nov[0] = nv.x;
+        nov[1] = nv.y;
+        footprint_weights<T>( dold[2], dnew[2], s[2], A[2], D[2], P[2], nov[2] );
+    } else {
+#pragma unroll
+        for( int d = 0; d < 3; d++ ) footprint_weights<T>( dold[d], dnew[d], s[d], A[d], D[d], P[d], nov[d] );
+    }
+}
+
 template <class T>
 __device__ __forceinline__ T pick4( int i, T a0, T a1, T a2, T a3 )
 {
@@ -1373,10 +1425,15 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
                 const T cr[3] = { cr3[0] * wq, cr3[1] * wq, cr3[2] * wq };
                 {
                     T A[3][3], D[3][3], P[3][2];
+                    if constexpr( DIM == 3 ) {
+                        T nov[3]; // (the node-changing pass deposits the plane beyond the footprint)
+                        footprint_weights3<T>( dold, dn, sh, A, D, P, nov );
+                    } else {
 #pragma unroll
-                    for( int d = 0; d < DIM; d++ ) {
-                        T nov; // (the node-changing pass deposits the plane beyond the footprint)
-                        footprint_weights<T>( dold[d], dn[d], sh[d], A[d], D[d], P[d], nov );
+                        for( int d = 0; d < DIM; d++ ) {
+                            T nov;
+                            footprint_weights<T>( dold[d], dn[d], sh[d], A[d], D[d], P[d], nov );
+                        }
                     }
                     if( DIM == 3 ) {
                         // along-axis a = hf, transverse b = 1 - hf and 2
@@ -1471,9 +1528,9 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
             if constexpr( DIM == 3 ) {
                 // the per-cell pass took the footprint part, this the planes beyond
                 T A[3][3], D[3][3], P[3][2], nov[3];
-#pragma unroll
-                for( int d = 0; d < 3; d++ )
-                    footprint_weights<T>( ( T )sRec[d * nmax + q], ( T )sRec[( 3 + d ) * nmax + q], sh[d], A[d], D[d], P[d], nov[d] );
+                const T dq_old[3] = { ( T )sRec[q], ( T )sRec[nmax + q], ( T )sRec[2 * nmax + q] };
+                const T dq_new[3] = { ( T )sRec[3 * nmax + q], ( T )sRec[4 * nmax + q], ( T )sRec[5 * nmax + q] };
+                footprint_weights3<T>( dq_old, dq_new, sh, A, D, P, nov );
                 deposit_beyond<T>( sJ2, jsz, td.JXS, td.JZ, cl, A, D, P, cr, nov, sh );
                 continue;
             }
