@@ -564,11 +564,11 @@ __device__ __forceinline__ void dep_spline2( float2 d, float2 &c0, float2 &c1, f
     c1 = __fadd2_rn( __fadd2_rn( make_float2( 1.0f, 1.0f ), neg2( c0 ) ), neg2( c2 ) );
 }
 
-template <class T>
-__device__ __forceinline__ void footprint_weights3( const T *dold, const T *dnew, const int *s, T ( *A )[3], T ( *D )[3],
-                                                    T ( *P )[2], T *nov )
+// Dimensions 0 and 1 of footprint_weights in paired FP32 arithmetic.
+__device__ __forceinline__ void footprint_weights_xy( const float *dold, const float *dnew, const int *s,
+                                                      float ( *A )[3], float ( *D )[3], float ( *P )[2], float *nov )
 {
-    if constexpr( sizeof( T ) == 4 ) {
+    {
         float2 o0, o1, o2, n0, n1, n2;
         dep_spline2( make_float2( dold[0], dold[1] ), o0, o1, o2 );
         dep_spline2( make_float2( dnew[0], dnew[1] ), n0, n1, n2 );
@@ -593,6 +593,15 @@ __device__ __forceinline__ void footprint_weights3( const T *dold, const T *dnew
         P[1][0] = p0.y; P[1][1] = p1.y;
         nov[0] = nv.x;
         nov[1] = nv.y;
+    }
+}
+
+template <class T>
+__device__ __forceinline__ void footprint_weights3( const T *dold, const T *dnew, const int *s, T ( *A )[3], T ( *D )[3],
+                                                    T ( *P )[2], T *nov )
+{
+    if constexpr( sizeof( T ) == 4 ) {
+        footprint_weights_xy( dold, dnew, s, A, D, P, nov );
         footprint_weights<T>( dold[2], dnew[2], s[2], A[2], D[2], P[2], nov[2] );
     } else {
 #pragma unroll
@@ -1428,6 +1437,9 @@ __global__ void __launch_bounds__( 128, CELLS ? 5 : ( MIXED ? 8 : 4 ) ) k_step_p
                     if constexpr( DIM == 3 ) {
                         T nov[3]; // (the node-changing pass deposits the plane beyond the footprint)
                         footprint_weights3<T>( dold, dn, sh, A, D, P, nov );
+                    } else if constexpr( MIXED ) {
+                        T nov[3];
+                        footprint_weights_xy( dold, dn, sh, A, D, P, nov );
                     } else {
 #pragma unroll
                         for( int d = 0; d < DIM; d++ ) {
