@@ -602,7 +602,19 @@ __device__ __forceinline__ void footprint_weights3( const T *dold, const T *dnew
 {
     if constexpr( sizeof( T ) == 4 ) {
         footprint_weights_xy( dold, dnew, s, A, D, P, nov );
-        footprint_weights<T>( dold[2], dnew[2], s[2], A[2], D[2], P[2], nov[2] );
+        // z: its old and new splines as one pair, then footprint_weights' formulas
+        float2 c0, c1, c2;
+        dep_spline2( make_float2( dold[2], dnew[2] ), c0, c1, c2 );
+        const int sz = s[2];
+        const float o0 = c0.x, o1 = c1.x, o2 = c2.x, n0 = c0.y, n1 = c1.y, n2 = c2.y;
+        const float f0 = sz > 0 ? 0.f : ( sz < 0 ? n1 : n0 );
+        const float f1 = sz > 0 ? n0 : ( sz < 0 ? n2 : n1 );
+        const float f2 = sz > 0 ? n1 : ( sz < 0 ? 0.f : n2 );
+        nov[2] = sz > 0 ? n2 : n0;
+        A[2][0] = 0.5f * ( o0 + f0 ); A[2][1] = 0.5f * ( o1 + f1 ); A[2][2] = 0.5f * ( o2 + f2 );
+        D[2][0] = f0 - o0; D[2][1] = f1 - o1; D[2][2] = f2 - o2;
+        P[2][0] = D[2][0] + ( sz < 0 ? nov[2] : 0.f );
+        P[2][1] = P[2][0] + D[2][1];
     } else {
 #pragma unroll
         for( int d = 0; d < 3; d++ ) footprint_weights<T>( dold[d], dnew[d], s[d], A[d], D[d], P[d], nov[d] );
