@@ -4094,26 +4094,24 @@ static int run_batch( sg_sim *S, int limit, int *done )
 {
     *done = 0;
     const int parity = S->sp.empty() ? 0 : S->sp[0].cur;
-    if( S->batch_parity < 0 ) {
-        int r = build_batch( S, &S->batch[0] );
+    // the graph for the present parity, built when first needed (a batch of an even
+    // number of steps ends on the parity it started from, so the other one is built
+    // only after a batch a spill cut short)
+    if( S->batch_parity < 0 ) S->batch_parity = parity;
+    const int idx = parity == S->batch_parity ? 0 : 1;
+    if( !S->batch[idx] ) {
+        int r = build_batch( S, &S->batch[idx] );
         if( r ) return r;
-        if( S->batch[0] ) {
-            for( auto &s : S->sp ) s.cur = 1 - s.cur;
-            r = build_batch( S, &S->batch[1] );
-            for( auto &s : S->sp ) s.cur = 1 - s.cur;
-            if( r ) return r;
-        }
-        if( !S->batch[0] || !S->batch[1] ) {
+        if( !S->batch[idx] ) {
             S->batch_unsupported = true;
             drop_graphs( S );
             return SG_OK;
         }
-        S->batch_parity = parity;
     }
     const int rec = batch_record_ints( S->max_species );
     S->h_batch[rec] = limit;
     SG_CUDA_TRY( cudaMemcpyAsync( S->d_batch + 2, S->h_batch + rec, sizeof( int ), cudaMemcpyHostToDevice, S->stream ) );
-    SG_CUDA_TRY( cudaGraphLaunch( S->batch[parity == S->batch_parity ? 0 : 1], S->stream ) );
+    SG_CUDA_TRY( cudaGraphLaunch( S->batch[idx], S->stream ) );
     SG_CUDA_TRY( cudaStreamSynchronize( S->stream ) );
     const int n = S->h_batch[1];
     if( n < 1 || n > limit ) return set_error( SG_ERR_CUDA, "batched step record out of range (%d of %d)", n, limit );
