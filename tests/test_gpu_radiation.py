@@ -421,6 +421,11 @@ def test_resident_photons_carry_the_emitted_energy(rad):
     for k in ("Bz", "Bz_m"):
         sim.set_field(k, np.full(tuple(n_cells[d] + 5 + st["Bz"][d] for d in range(2)), 50.0))
     sim.add_species(1.0, -1.0, "boris", pos, mom, w)  # Boris keeps |p| in a pure magnetic field
+    # a photon store needs a radiating species; reading one needs a store
+    with pytest.raises(RuntimeError):
+        sim.set_species_photons(0, sampling=2, gamma_threshold=20.0, capacity=1000)
+    with pytest.raises(RuntimeError):
+        sim.get_photons(0)
     sim.set_species_radiation(0, T32, None, seed=11)
     sampling, threshold = 2, 20.0
     sim.set_species_photons(0, sampling=sampling, gamma_threshold=threshold, max_emissions=3, capacity=2_000_000)
